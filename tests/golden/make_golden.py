@@ -1,0 +1,195 @@
+"""Generate the golden fixtures in this folder from the reference PySPH.
+
+Runs the compat-patched reference build (``oracle/_ref/src``, made by
+``python oracle/build_ref.py``) on seeded synthetic inputs and stores, per
+fixture, the inputs, the per-evaluation outputs of every calc, the neighbour
+sets and the state after the step.  The fixtures are what the parity tests
+compare the GPU path (and the C restatement in ``oracle/``) against.
+
+Usage: ``python tests/golden/make_golden.py`` (needs the reference build; it
+is not run by the tests).
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref", "src"))
+
+import pysph.base.api as rbase  # noqa: E402  (reference)
+import pysph.sph.api as rsph  # noqa: E402
+import pysph.solver.api as rsolver  # noqa: E402
+
+from pysph_gb300 import workloads as W  # noqa: E402
+
+REF = types.SimpleNamespace(base=rbase, sph=rsph, solver=rsolver)
+
+STATE = ("x", "y", "z", "u", "v", "w")
+EVAL_PROPS = ("x", "y", "z", "u", "v", "w", "rho", "p", "cs")
+
+
+def neighbours_csr(particles, src, dst, radius_scale=2.0):
+    """Neighbour lists (reference order, self last) as CSR arrays."""
+    loc = particles.nnps_manager.get_neighbor_particle_locator(src, dst, radius_scale)
+    offs = [0]
+    idx = []
+    for i in range(dst.get_number_of_particles()):
+        nb = loc.py_get_nearest_particles(i).get_npy_array().copy()
+        idx.append(nb)
+        offs.append(offs[-1] + nb.size)
+    return np.asarray(offs, np.int64), np.concatenate(idx).astype(np.int32)
+
+
+def run_step(s, particles, dt, out, nbr_pairs=()):
+    """One integrator step, snapshotting every evaluation."""
+    integ = s.integrator
+    arrays = particles.arrays
+    for pa in arrays:
+        for p in pa.properties:
+            if p in ("tag", "group", "local", "idx") or p.startswith("_"):
+                continue
+            out["in_%s_%s" % (pa.name, p)] = pa.get(p).copy()
+    for (si, di) in nbr_pairs:
+        o, ix = neighbours_csr(particles, arrays[si], arrays[di])
+        out["nbr_%s_%s_offsets" % (arrays[di].name, arrays[si].name)] = o
+        out["nbr_%s_%s_index" % (arrays[di].name, arrays[si].name)] = ix
+
+    counter = [0]
+    orig_eval = integ.eval
+
+    def eval_and_record(calcs):
+        e = counter[0] + 1
+        for pa in arrays:
+            for p in STATE:
+                out["eval%d_pre_%s_%s" % (e, pa.name, p)] = pa.get(p).copy()
+        orig_eval(calcs)
+        for pa in arrays:
+            for p in ("rho", "p", "cs"):
+                out["eval%d_%s_%s" % (e, pa.name, p)] = pa.get(p).copy()
+        for calc in calcs:
+            if calc.integrates:
+                pa = arrays[calc.dnum]
+                names = calc.dst_writes["k%d" % e]
+                for j, upd in enumerate(calc.updates):
+                    out["eval%d_k_%s_%s" % (e, calc.id, upd)] = pa.get(names[j]).copy()
+        counter[0] += 1
+
+    integ.eval = eval_and_record
+    integ.integrate(dt)
+    integ.eval = orig_eval
+    for pa in arrays:
+        for p in STATE + ("rho", "p", "cs"):
+            out["out_%s_%s" % (pa.name, p)] = pa.get(p).copy()
+    out["n_evals"] = np.int64(counter[0])
+    out["dt"] = np.float64(dt)
+
+
+def fixture_kernel():
+    """Cubic-spline W and grad W on a grid of distances, h and dimensions."""
+    out = {}
+    rs = np.concatenate([np.linspace(0.0, 2.2, 45), [1e-15, 0.5, 1.0, 2.0, 1.0 - 1e-12, 2.0 - 1e-12]])
+    for dim in (1, 2, 3):
+        k = rbase.CubicSplineKernel(dim=dim)
+        for h in (0.1, 0.37, 1.0):
+            w = np.zeros(rs.size)
+            g = np.zeros((rs.size, 3))
+            pa = rbase.Point(0.0, 0.0, 0.0)
+            for n, r in enumerate(rs):
+                # points along a skew direction so every component is exercised
+                d = np.array([0.6, -0.48, 0.64])[:dim]
+                d = d / np.linalg.norm(d)
+                q = np.zeros(3)
+                q[:dim] = d * r * h
+                pb = rbase.Point(*q)
+                w[n] = k.py_function(pa, pb, h)
+                gp = rbase.Point()
+                k.py_gradient(pa, pb, h, gp)
+                g[n] = (gp.x, gp.y, gp.z)
+            out["w_d%d_h%g" % (dim, h)] = w
+            out["g_d%d_h%g" % (dim, h)] = g
+    out["r_over_h"] = rs
+    return out
+
+
+def fixture_square4():
+    """Four particles on a unit square (the reference's SPH function tests)."""
+    out = {}
+    x = np.array([0, 0, 1, 1], np.float64)
+    y = np.array([0, 1, 1, 0], np.float64)
+    u = np.array([1, 0, 0, -1], np.float64)
+    p = np.array([0, 0, 1, 1], np.float64)
+    pa = rbase.get_particle_array(name="test", x=x, y=y, z=np.zeros(4), m=np.ones(4),
+                                  u=u, p=p, cs=np.ones(4),
+                                  tmpx=np.zeros(4), tmpy=np.zeros(4), tmpz=np.zeros(4))
+    particles = rbase.Particles(arrays=[pa])
+    kern = rbase.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("rho", rsph.SPHRho.withargs(), ["tmpx"]),
+            ("pgrad", rsph.SPHPressureGradient.withargs(dim=2), ["tmpx", "tmpy"]),
+            ("avisc", rsph.MonaghanArtificialVsicosity.withargs(alpha=1.0, beta=1.0),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("xsph", rsph.XSPHCorrection.withargs(eps=0.5, dim=2), ["tmpx", "tmpy"])):
+        func = fn.get_func(pa, pa)
+        calc = rsph.SPHCalc(particles, [pa], pa, kern, [func], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            out["%s_%d" % (name, k)] = pa.get(upn).copy()
+    for p_ in ("x", "y", "u", "p", "m", "h", "rho", "cs"):
+        out["in_" + p_] = pa.get(p_).copy()
+    return out
+
+
+def fixture_drop(steps=1, dx=0.025):
+    props = W.elliptical_drop(dx=dx)
+    s, particles = W.setup_drop(REF, props)
+    out = {}
+    run_step(s, particles, 1e-5, out, nbr_pairs=[(0, 0)])
+    for _ in range(steps - 1):
+        s.integrator.integrate(1e-5)
+    if steps > 1:
+        pa = particles.arrays[0]
+        for p in ("x", "y", "u", "v", "rho", "p", "cs"):
+            out["final_%s" % p] = pa.get(p).copy()
+        out["steps"] = np.int64(steps)
+    return out
+
+
+def fixture_dam(dx=0.04):
+    fl, wl = W.dam_break(dx=dx)
+    c0 = W.dam_break_c0()
+    s, particles = W.setup_dam_break(REF, fl, wl, dx=dx, c0=c0)
+    out = {"dx": np.float64(dx), "c0": np.float64(c0)}
+    run_step(s, particles, 1e-4, out, nbr_pairs=[(0, 0), (1, 0)])
+    return out
+
+
+def fixture_cube(n=4096):
+    props = W.cube_lattice(n)
+    s, particles = W.setup_cube(REF, props)
+    out = {}
+    run_step(s, particles, 1e-4, out, nbr_pairs=[(0, 0)])
+    return out
+
+
+def main():
+    fixtures = {
+        "kernel": fixture_kernel,
+        "square4": fixture_square4,
+        "drop_step": lambda: fixture_drop(1),
+        "drop_traj10": lambda: fixture_drop(10),
+        "dam_step": fixture_dam,
+        "cube_step": fixture_cube,
+    }
+    for name, fn in fixtures.items():
+        data = fn()
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **data)
+        print("wrote", path, os.path.getsize(path) // 1024, "KiB")
+
+
+if __name__ == "__main__":
+    main()
