@@ -1,0 +1,339 @@
+"""CPU oracle for the SPH particle-step hot path -- TEST INFRASTRUCTURE.
+
+The oracle is the checker the GPU path is compared with.  It restates the
+reference PySPH algorithm in FP64 (``oracle/sph_oracle.c`` for the
+neighbour search and pair sums; the integrator bookkeeping below) and is
+pinned against the golden fixtures that the reference itself produced
+(``tests/golden``).  Only tests, ``__graft_entry__.smoke()`` and the CPU
+baseline of ``bench.py`` may import it; the product never does.
+
+Reference routines restated here (paths relative to ``source/pysph``):
+
+* ``solver/integrator.py:229-645`` -- calc bookkeeping, Euler and RK2 steps
+  (``Problem.integrate_euler`` / ``Problem.integrate_rk2``);
+* ``sph/sph_calc.pyx:223-276`` -- zero the outputs, then sum over sources
+  (``Problem._run_op``);
+* the per-function pair sums and the neighbour search -- see the C file.
+"""
+import ctypes
+import os
+import platform
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(HERE, "sph_oracle.c")
+_BUILD = os.path.join(HERE, "_build")
+_LIB = os.path.join(_BUILD, "libsph_oracle_%s.so" % platform.machine())
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the C restatement (gcc, OpenMP, no FMA contraction)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    if (not force and os.path.exists(_LIB)
+            and os.path.getmtime(_LIB) >= os.path.getmtime(_SRC)):
+        return _LIB
+    tmp = _LIB + ".%d.tmp" % os.getpid()
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", _SRC, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB)
+    return _LIB
+
+
+class OrcArray(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64)] + [
+        (name, ctypes.c_void_p) for name in
+        ("x", "y", "z", "u", "v", "w", "m", "h", "rho", "p", "cs",
+         "nx", "ny", "nz", "tx", "ty", "tz", "tag")]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = ctypes.CDLL(build())
+            P = ctypes.POINTER(OrcArray)
+            d = ctypes.c_double
+            vp = ctypes.c_void_p
+            i = ctypes.c_int
+            L.orc_neighbors.restype = ctypes.c_int64
+            L.orc_neighbors.argtypes = [P, P, d, d, i, vp, vp]
+            L.orc_sph_rho.argtypes = [P, P, vp, vp, i, vp]
+            L.orc_tait.argtypes = [P, d, d, d, vp, vp]
+            L.orc_pgrad.argtypes = [P, P, vp, vp, i, i, vp, vp, vp]
+            L.orc_avisc.argtypes = [P, P, vp, vp, i, d, d, d, vp, vp, vp]
+            L.orc_xsph.argtypes = [P, P, vp, vp, i, d, i, vp, vp, vp]
+            L.orc_bforce.argtypes = [P, P, vp, vp, d, vp, vp, vp]
+            L.orc_const3.argtypes = [P, d, d, d, i, vp, vp, vp]
+            L.orc_position_stepping.argtypes = [P, i, vp, vp, vp]
+            L.orc_cubic_w.restype = d
+            L.orc_cubic_w.argtypes = [i] + [d] * 7
+            L.orc_cubic_grad.argtypes = [i] + [d] * 7 + [vp]
+            L.orc_num_threads.restype = i
+            _lib = L
+    return _lib
+
+
+def num_threads():
+    return lib().orc_num_threads()
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class _Arr:
+    """Keeps the numpy buffers alive while an OrcArray points at them."""
+
+    def __init__(self, props):
+        n = len(props["x"])
+        self.keep = {}
+        st = OrcArray()
+        st.n = n
+        for name, _ in OrcArray._fields_[1:]:
+            a = props.get(name)
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.int64 if name == "tag" else np.float64)
+                self.keep[name] = a
+            setattr(st, name, _ptr(a))
+        self.st = st
+        self.ref = ctypes.byref(st)
+
+
+def cubic_w(dim, a, b, h):
+    return lib().orc_cubic_w(dim, *a, *b, h)
+
+
+def cubic_grad(dim, a, b, h):
+    g = np.zeros(3)
+    lib().orc_cubic_grad(dim, *a, *b, h, g.ctypes.data)
+    return g
+
+
+def neighbors(dst, src, cell_size, radius_scale=2.0, same=False):
+    """CSR neighbour lists (ascending source index, self last if ``same``)."""
+    D, S = _Arr(dst), _Arr(src)
+    n = D.st.n
+    offsets = np.zeros(n + 1, np.int64)
+    lib().orc_neighbors(D.ref, S.ref, cell_size, radius_scale, int(same),
+                        offsets.ctypes.data, None)
+    np.cumsum(offsets, out=offsets)
+    index = np.zeros(max(int(offsets[-1]), 1), np.int64)
+    lib().orc_neighbors(D.ref, S.ref, cell_size, radius_scale, int(same),
+                        offsets.ctypes.data, index.ctypes.data)
+    return offsets, index[: offsets[-1]]
+
+
+def pair_sum(kind, dst, src, offsets, index, dim, params=None, nout=3):
+    """Evaluate one SPH function from explicit neighbour lists.
+
+    Returns a list of ``nout`` FP64 arrays (zero-initialised, then summed,
+    like ``SPHCalc.sph``)."""
+    params = params or {}
+    D, S = _Arr(dst), _Arr(src)
+    n = D.st.n
+    outs = [np.zeros(n) for _ in range(3)]
+    o = [x.ctypes.data for x in outs]
+    off = np.ascontiguousarray(offsets, np.int64)
+    idx = np.ascontiguousarray(index, np.int64)
+    L = lib()
+    if kind == "rho":
+        L.orc_sph_rho(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, o[0])
+        return outs[:1]
+    if kind == "pgrad":
+        L.orc_pgrad(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, nout, *o)
+    elif kind == "avisc":
+        L.orc_avisc(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
+                    params.get("alpha", 1.0), params.get("beta", 1.0), 0.0, *o)
+    elif kind == "xsph":
+        L.orc_xsph(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
+                   params.get("eps", 0.5), nout, *o)
+    elif kind == "bforce":
+        L.orc_bforce(D.ref, S.ref, off.ctypes.data, idx.ctypes.data,
+                     params.get("delp", 1.0), *o)
+    else:
+        raise ValueError(kind)
+    return outs[:nout]
+
+
+def tait(dst, co, ro, gamma=7.0):
+    D = _Arr(dst)
+    p = np.zeros(D.st.n)
+    cs = np.zeros(D.st.n)
+    lib().orc_tait(D.ref, co, ro, gamma, p.ctypes.data, cs.ctypes.data)
+    return p, cs
+
+
+# ---------------------------------------------------------------------------
+# Problem: a set of particle arrays plus an ordered list of operations,
+# stepped exactly like solver/integrator.py steps its calcs.
+# ---------------------------------------------------------------------------
+
+class Op:
+    """One calc: ``kind`` in rho | tait | pgrad | avisc | xsph | bforce |
+    gravity | step, on destination ``dest`` from ``sources``."""
+
+    def __init__(self, kind, dest, updates, sources=(), integrates=False, **params):
+        self.kind = kind
+        self.dest = dest
+        self.sources = list(sources)
+        self.updates = list(updates)
+        self.integrates = integrates
+        self.params = params
+
+
+class Problem:
+    def __init__(self, arrays, ops, dim, radius_scale=2.0):
+        # arrays: dict name -> dict of float64 property arrays (copied)
+        self.arrays = {}
+        for name, props in arrays.items():
+            n = len(props["x"])
+            a = {k: np.array(v, dtype=np.int64 if k == "tag" else np.float64)
+                 for k, v in props.items()}
+            for k, default in (("y", 0.0), ("z", 0.0), ("u", 0.0), ("v", 0.0),
+                               ("w", 0.0), ("m", 1.0), ("h", 1.0), ("p", 0.0),
+                               ("rho", 1.0), ("cs", 0.0), ("e", 0.0)):
+                if k not in a:
+                    a[k] = np.full(n, default)
+            self.arrays[name] = a
+        self.ops = ops
+        self.dim = dim
+        self.radius_scale = radius_scale
+        max_h = max(float(a["h"].max()) for a in self.arrays.values() if a["h"].size)
+        # CellManager.compute_cell_size: base/cell.pyx:893-925
+        self.cell_size = radius_scale * max_h
+        self.k = {}
+        self.nbr_cache = {}
+
+    def neighbours(self, dest, src):
+        key = (dest, src)
+        if key not in self.nbr_cache:
+            self.nbr_cache[key] = neighbors(self.arrays[dest], self.arrays[src],
+                                            self.cell_size, self.radius_scale,
+                                            same=(dest == src))
+        return self.nbr_cache[key]
+
+    def _moved(self):
+        self.nbr_cache = {}
+
+    def _run_op(self, op):
+        """Evaluate one calc; returns its outputs (list, one per update)."""
+        d = self.arrays[op.dest]
+        nout = len(op.updates)
+        n = len(d["x"])
+        outs = [np.zeros(n) for _ in range(nout)]
+        if op.kind == "tait":
+            p, cs = tait(d, op.params["co"], op.params["ro"], op.params.get("gamma", 7.0))
+            return [p, cs]
+        if op.kind == "gravity":
+            D = _Arr(d)
+            tmp = [np.zeros(n) for _ in range(3)]
+            lib().orc_const3(D.ref, op.params.get("gx", 0.0), op.params.get("gy", 0.0),
+                             op.params.get("gz", 0.0), nout, *[t.ctypes.data for t in tmp])
+            return tmp[:nout]
+        if op.kind == "step":
+            D = _Arr(d)
+            tmp = [np.zeros(n) for _ in range(3)]
+            lib().orc_position_stepping(D.ref, nout, *[t.ctypes.data for t in tmp])
+            return tmp[:nout]
+        for s in op.sources:
+            off, idx = self.neighbours(op.dest, s)
+            res = pair_sum(op.kind, d, self.arrays[s], off, idx, self.dim, op.params, nout)
+            for o, r in zip(outs, res):
+                o += r
+        return outs
+
+    # integrator.py:432-470
+    def eval(self, kname):
+        for ci, op in enumerate(self.ops):
+            res = self._run_op(op)
+            if op.integrates:
+                self.k[(kname, ci)] = res
+            else:
+                for upd, r in zip(op.updates, res):
+                    self.arrays[op.dest][upd] = r
+
+    def _integrating(self):
+        return [(ci, op) for ci, op in enumerate(self.ops) if op.integrates]
+
+    # integrator.py:339-367
+    def _set_initial(self):
+        init = {}
+        for ci, op in self._integrating():
+            for upd in op.updates:
+                init[(op.dest, upd)] = self.arrays[op.dest][upd].copy()
+        return init
+
+    # integrator.py:525-573
+    def integrate_euler(self, dt):
+        init = self._set_initial()
+        self.eval("k1")
+        for ci, op in self._integrating():
+            for j, upd in enumerate(op.updates):
+                updated = init[(op.dest, upd)] + self.k[("k1", ci)][j] * dt
+                self.arrays[op.dest][upd] = updated
+                init[(op.dest, upd)] = updated
+        self._moved()
+
+    # integrator.py:581-645
+    def integrate_rk2(self, dt):
+        init = self._set_initial()
+        self.eval("k1")
+        for (dest, upd), a in init.items():
+            self.arrays[dest][upd] = a.copy()
+        for ci, op in self._integrating():
+            for j, upd in enumerate(op.updates):
+                cur = self.arrays[op.dest][upd]
+                self.arrays[op.dest][upd] = cur + self.k[("k1", ci)][j] * dt
+        self._moved()
+        self.eval("k2")
+        for ci, op in self._integrating():
+            for j, upd in enumerate(op.updates):
+                updated = init[(op.dest, upd)] + 0.5 * dt * (
+                    self.k[("k1", ci)][j] + self.k[("k2", ci)][j])
+                self.arrays[op.dest][upd] = updated
+                init[(op.dest, upd)] = updated
+        self._moved()
+
+
+# ---------------------------------------------------------------------------
+# operation lists matching pysph_gb300.workloads.setup_* (same order, same
+# parameters), expressed independently of the product's solver classes.
+# ---------------------------------------------------------------------------
+
+def drop_ops(c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5):
+    return [
+        Op("rho", "fluid", ["rho"], ["fluid"]),
+        Op("tait", "fluid", ["p", "cs"], co=c0, ro=rho0),
+        Op("pgrad", "fluid", ["u", "v"], ["fluid"], integrates=True),
+        Op("avisc", "fluid", ["u", "v", "w"], ["fluid"], integrates=True, alpha=alpha, beta=beta),
+        Op("step", "fluid", ["x", "y"], integrates=True),
+        Op("xsph", "fluid", ["x", "y"], ["fluid"], integrates=True, eps=eps),
+    ]
+
+
+def dam_ops(dx, c0, rho0=1000.0, alpha=0.1, beta=0.0, g=-9.81):
+    return [
+        Op("tait", "fluid", ["p", "cs"], co=c0, ro=rho0),
+        Op("rho", "fluid", ["rho"], ["fluid"]),
+        Op("pgrad", "fluid", ["u", "v"], ["fluid"], integrates=True),
+        Op("avisc", "fluid", ["u", "v", "w"], ["fluid"], integrates=True, alpha=alpha, beta=beta),
+        Op("bforce", "fluid", ["u", "v", "w"], ["boundary"], integrates=True, delp=dx),
+        Op("gravity", "fluid", ["u", "v", "w"], integrates=True, gy=g),
+        Op("step", "fluid", ["x", "y"], integrates=True),
+    ]
+
+
+def cube_ops(c0=1.0, rho0=1.0, alpha=0.1, beta=0.0):
+    return [
+        Op("rho", "fluid", ["rho"], ["fluid"]),
+        Op("tait", "fluid", ["p", "cs"], co=c0, ro=rho0),
+        Op("pgrad", "fluid", ["u", "v", "w"], ["fluid"], integrates=True),
+        Op("avisc", "fluid", ["u", "v", "w"], ["fluid"], integrates=True, alpha=alpha, beta=beta),
+        Op("step", "fluid", ["x", "y", "z"], integrates=True),
+    ]

@@ -1,0 +1,140 @@
+"""Pin the CPU oracle against the reference PySPH's own outputs.
+
+The golden fixtures were produced by the reference (``tests/golden/
+make_golden.py``).  Given the reference's neighbour lists in the reference's
+order, the oracle's pair sums must match bit for bit (FP64, no FMA); its own
+neighbour search must give identical index sets; a full oracle step must
+match the reference step to FP64 round-off.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import csr_sets, inputs, load, normwise
+
+
+def test_kernel_values_bit_exact():
+    g = load("kernel")
+    rs = g["r_over_h"]
+    for dim in (1, 2, 3):
+        for h in (0.1, 0.37, 1.0):
+            d = np.array([0.6, -0.48, 0.64])[:dim]
+            d = d / np.linalg.norm(d)
+            for n, r in enumerate(rs):
+                q = np.zeros(3)
+                q[:dim] = d * r * h
+                w = oracle.cubic_w(dim, (0, 0, 0), tuple(q), h)
+                gr = oracle.cubic_grad(dim, (0, 0, 0), tuple(q), h)
+                assert w == g["w_d%d_h%g" % (dim, h)][n]
+                np.testing.assert_array_equal(gr, g["g_d%d_h%g" % (dim, h)][n])
+
+
+def test_square4_functions():
+    g = load("square4")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    off, idx = oracle.neighbors(props, props, cell_size=2.0, same=True)
+    for kind, nout, params in (("rho", 1, {}), ("pgrad", 2, {}),
+                               ("avisc", 3, {"alpha": 1.0, "beta": 1.0}),
+                               ("xsph", 2, {"eps": 0.5})):
+        res = oracle.pair_sum(kind, props, props, off, idx, 2, params, nout)
+        for k in range(nout):
+            np.testing.assert_allclose(res[k], g["%s_%d" % (kind, k)], rtol=1e-14, atol=1e-14)
+
+
+def _check_neighbours(g, dest, src, props_d, props_s, cell_size):
+    off, idx = oracle.neighbors(props_d, props_s, cell_size, same=(dest == src))
+    ro = g["nbr_%s_%s_offsets" % (dest, src)]
+    ri = g["nbr_%s_%s_index" % (dest, src)]
+    assert csr_sets(off, idx) == csr_sets(ro, ri)
+    if dest == src:
+        last = idx[off[1:] - 1]
+        np.testing.assert_array_equal(last, np.arange(len(off) - 1))
+        np.testing.assert_array_equal(ri[ro[1:] - 1], np.arange(len(ro) - 1))
+
+
+@pytest.mark.parametrize("name,dim", [("drop_step", 2), ("cube_step", 3)])
+def test_neighbour_sets_match_reference(name, dim):
+    g = load(name)
+    p = inputs(g, "fluid")
+    _check_neighbours(g, "fluid", "fluid", p, p, 2.0 * p["h"].max())
+
+
+def test_dam_neighbour_sets_match_reference():
+    g = load("dam_step")
+    f, w = inputs(g, "fluid"), inputs(g, "boundary")
+    cs = 2.0 * max(f["h"].max(), w["h"].max())
+    _check_neighbours(g, "fluid", "fluid", f, f, cs)
+    _check_neighbours(g, "fluid", "boundary", f, w, cs)
+
+
+def test_drop_pair_sums_bit_exact_with_reference_lists():
+    """Same neighbour order as the reference -> identical FP64 sums."""
+    g = load("drop_step")
+    p = inputs(g, "fluid")
+    off = g["nbr_fluid_fluid_offsets"]
+    idx = g["nbr_fluid_fluid_index"]
+    rho = oracle.pair_sum("rho", p, p, off, idx, 2)[0]
+    np.testing.assert_array_equal(rho, g["eval1_fluid_rho"])
+    p2 = dict(p, rho=g["eval1_fluid_rho"], p=g["eval1_fluid_p"], cs=g["eval1_fluid_cs"])
+    pt, ct = oracle.tait(dict(p, rho=g["eval1_fluid_rho"]), 1400.0, 1.0)
+    np.testing.assert_array_equal(pt, g["eval1_fluid_p"])
+    np.testing.assert_array_equal(ct, g["eval1_fluid_cs"])
+    pg = oracle.pair_sum("pgrad", p2, p2, off, idx, 2, nout=2)
+    np.testing.assert_array_equal(pg[0], g["eval1_k_pgrad_fluid_u"])
+    np.testing.assert_array_equal(pg[1], g["eval1_k_pgrad_fluid_v"])
+    av = oracle.pair_sum("avisc", p2, p2, off, idx, 2, {"alpha": 0.01, "beta": 0.0}, 3)
+    for k, c in enumerate("uvw"):
+        np.testing.assert_array_equal(av[k], g["eval1_k_avisc_fluid_" + c])
+    xs = oracle.pair_sum("xsph", p2, p2, off, idx, 2, {"eps": 0.5}, 2)
+    np.testing.assert_array_equal(xs[0], g["eval1_k_xsph_fluid_x"])
+    np.testing.assert_array_equal(xs[1], g["eval1_k_xsph_fluid_y"])
+
+
+def _step_problem(g, arrays, ops, dim, scheme):
+    prob = oracle.Problem(arrays, ops, dim)
+    getattr(prob, "integrate_" + scheme)(float(g["dt"]))
+    return prob
+
+
+def _cmp_step(g, prob, names, tol):
+    for arr in names:
+        for p_ in ("x", "y", "z", "u", "v", "w", "rho", "p", "cs"):
+            key = "out_%s_%s" % (arr, p_)
+            if key in g:
+                err = normwise(prob.arrays[arr][p_], g[key])
+                assert err <= tol, (key, err)
+
+
+def test_drop_euler_step_matches_reference():
+    g = load("drop_step")
+    prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2, "euler")
+    _cmp_step(g, prob, ["fluid"], 1e-13)
+    for c in "uvw":
+        assert normwise(prob.k[("k1", 3)][" uvw".index(c) - 1], g["eval1_k_avisc_fluid_" + c]) < 1e-13
+
+
+def test_drop_ten_euler_steps_match_reference():
+    g = load("drop_traj10")
+    prob = oracle.Problem({"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2)
+    for _ in range(int(g["steps"])):
+        prob.integrate_euler(float(g["dt"]))
+    for p_ in ("x", "y", "u", "v", "rho", "p", "cs"):
+        assert normwise(prob.arrays["fluid"][p_], g["final_" + p_]) < 1e-11, p_
+
+
+def test_dam_rk2_step_matches_reference():
+    g = load("dam_step")
+    arrays = {"fluid": inputs(g, "fluid"), "boundary": inputs(g, "boundary")}
+    prob = _step_problem(g, arrays, oracle.dam_ops(float(g["dx"]), float(g["c0"])), 2, "rk2")
+    _cmp_step(g, prob, ["fluid", "boundary"], 1e-13)
+    kb = prob.k[("k2", 4)]
+    assert normwise(kb[0], g["eval2_k_bforce_fluid_u"]) < 1e-13
+    assert normwise(kb[1], g["eval2_k_bforce_fluid_v"]) < 1e-13
+
+
+def test_cube_rk2_step_matches_reference():
+    g = load("cube_step")
+    prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.cube_ops(), 3, "rk2")
+    _cmp_step(g, prob, ["fluid"], 1e-13)
+    for c, k in zip("uvw", range(3)):
+        assert normwise(prob.k[("k2", 2)][k], g["eval2_k_pgrad_fluid_" + c]) < 1e-13
