@@ -1,0 +1,182 @@
+/*
+ * pysph_gb300 -- C ABI of the GB300 (sm_103a) SPH particle-step hot path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (SPH_OK = 0, negative on error; sph_last_error() gives the message) and is
+ * asynchronous on the context's CUDA stream unless documented otherwise.
+ * Particle data are DEVICE pointers owned by the caller (the Python facade
+ * keeps them in torch tensors); the context owns only its scratch (cell
+ * tables, sorted snapshots).  A context is not re-entrant.
+ *
+ * Reference interfaces replaced (paths relative to the reference's
+ * source/pysph/):
+ *   sph_nnps_build        base/cell.pyx:927-1015 CellManager.update/cells_update
+ *                         (+ check_jump_tolerance :1422-1437) and
+ *                         base/nnps.pyx:566-620 FixedDestNbrParticleLocator.update
+ *   sph_nnps_count/fill   base/nnps.pyx:458-523,633-648 get_nearest_particles
+ *   sph_density           sph/sph_calc.pyx:223-270 SPHCalc.sph over
+ *                         sph/funcs/density_funcs.pyx:38-74 SPHRho (optionally
+ *                         fused with sph/funcs/eos_funcs.pyx:105-116 TaitEquation)
+ *   sph_rates             SPHCalc.sph over pressure_funcs.pyx:40-91,
+ *                         viscosity_funcs.pyx:41-124, xsph_funcs.pyx:31-88,
+ *                         boundary_funcs.pyx:54-110 (+ external_force.pyx:39-45,
+ *                         position_funcs.pyx:32-60 folded in)
+ *   sph_tait              sph/funcs/eos_funcs.pyx:105-116 TaitEquation.eval_single
+ *   sph_const_rates       external_force.pyx:39-45 GravityForce,
+ *                         position_funcs.pyx:32-60 PositionStepping
+ *   sph_integrate         solver/integrator.py:339-645 set_initial_arrays /
+ *                         step / final_step of Euler and RK2
+ *   sph_invariants        (no counterpart: FP64 mass/momentum/energy sums)
+ */
+#ifndef PYSPH_GB300_H
+#define PYSPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_OK 0
+#define SPH_ERR_ARG (-1)      /* invalid argument (ValueError)                 */
+#define SPH_ERR_CUDA (-2)     /* CUDA runtime error                            */
+#define SPH_ERR_GRID (-3)     /* dense cell grid would exceed its capacity     */
+#define SPH_ERR_JUMP (-4)     /* a particle moved by more than one cell width  */
+#define SPH_ERR_STATE (-5)    /* call out of order (e.g. no neighbour build)   */
+#define SPH_ERR_NOTSUP (-6)   /* unsupported configuration (NotImplementedError)*/
+
+/* device error-word bits (sph_error_word) */
+#define SPH_EFLAG_JUMP 1u
+#define SPH_EFLAG_NONFINITE 2u
+
+#define SPH_MAX_SOURCES 8
+
+/* Particle tags (base/particle_array.pxd:20-26): only LocalReal (0)
+ * destinations are evaluated; others get 0. */
+#define SPH_TAG_LOCAL_REAL 0
+
+typedef struct sph_ctx sph_ctx;
+
+/* One particle array: FP64 device arrays of length n.  NULL = absent (read
+ * as 0).  nx..tz are the wall normals/tangents MonaghanBoundaryForce reads. */
+typedef struct {
+    int64_t n;
+    const double *x, *y, *z, *u, *v, *w, *m, *h, *rho, *p, *cs;
+    const double *nx, *ny, *nz, *tx, *ty, *tz;
+    const int64_t *tag; /* NULL: every particle LocalReal */
+} sph_array_view;
+
+/* term flags of one source in sph_rates */
+#define SPH_TERM_PGRAD 1u   /* SPHPressureGradient            */
+#define SPH_TERM_AVISC 2u   /* MonaghanArtificialVsicosity    */
+#define SPH_TERM_XSPH 4u    /* XSPHCorrection                 */
+#define SPH_TERM_BFORCE 8u  /* MonaghanBoundaryForce          */
+
+typedef struct {
+    int src;           /* array slot of the source (index into the last build) */
+    uint32_t flags;    /* SPH_TERM_* */
+    double alpha, beta, eta; /* avisc (eta = 0 reproduces the reference)        */
+    double eps;        /* xsph */
+    double delp;       /* boundary force */
+} sph_source_term;
+
+typedef struct {
+    int dim;              /* kernel dimension 1..3                              */
+    int tait;             /* 1: also compute p, cs by the Tait equation           */
+    double co, ro, gamma; /* Tait parameters                                    */
+} sph_density_params;
+
+typedef struct {
+    int dim;
+    int add_velocity;     /* PositionStepping: pos_out += (u, v, w) of the dest */
+    double gx, gy, gz;    /* GravityForce: acc_out += g (when add_gravity)      */
+    int add_gravity;
+} sph_rates_params;
+
+/* One line of an integrator update, applied elementwise over n particles:
+ *   tmp = base[i] + c1 * (k1[i] (+ k2[i]))     (k2 may be NULL)
+ *   out[i] = tmp;  if (save) save[i] = tmp;
+ * With mode 1, tmp = base[i] + k1[i] * c1 (Euler / RK2 predictor form).
+ * The FP64 operations are rounded exactly as the NumPy expressions of
+ * solver/integrator.py:472-645. */
+typedef struct {
+    double *out;
+    double *save;
+    const double *base;
+    const double *k1;
+    const double *k2;
+    double c1;
+    int mode; /* 0: base + c1*(k1+k2); 1: base + k1*c1; 2: copy base */
+} sph_axpy_line;
+
+#define SPH_MAX_AXPY_LINES 12
+
+/* context */
+int sph_ctx_create(int dim, sph_ctx **out);
+int sph_ctx_destroy(sph_ctx *ctx);
+int sph_ctx_set_stream(sph_ctx *ctx, void *cuda_stream);
+int sph_last_error(char *buf, size_t len);
+int sph_version(void);
+
+/* Neighbour structure for all arrays of one Particles collection.  Bins
+ * every array on a dense grid of cells of size cell_size/subdiv (subdiv in
+ * 1..3), sorts each array by cell (deterministic order within a cell) and
+ * gathers the sorted FP32 snapshots.  Synchronises the stream once (to size
+ * the grid).  check_jump: fail with SPH_ERR_JUMP if any particle's cell
+ * (of size cell_size) moved by more than one since the previous build. */
+int sph_nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+                   double radius_scale, int subdiv, int check_jump);
+
+/* Neighbour lists of destination dst among source src (radius
+ * radius_scale*h_dst, radius_scale no larger than the build's), as original particle
+ * indices: counts[i] (device, int64, n_dst) then, given the exclusive prefix
+ * offsets (device, n_dst+1), the index lists, each sorted ascending with the
+ * destination itself moved last when dst == src. */
+int sph_nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *counts);
+int sph_nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
+                  int64_t *index);
+
+/* Re-gather the sorted FP32 snapshot of one array from (possibly new) device
+ * pointers, keeping the cell order of the last build.  For data changed
+ * since the build without moving particles across cells (velocities,
+ * densities, pressures written outside sph_density). */
+int sph_refresh_state(sph_ctx *ctx, int array, const sph_array_view *view);
+
+int sph_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
+                double *rho_out, double *p_out, double *cs_out);
+
+/* acc_out[3] / pos_out[3]: FP64 outputs (entries may be NULL).  accumulate:
+ * 0 stores the sum, 1 adds it to the outputs. */
+int sph_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+              const sph_rates_params *prm, double *const *acc_out, double *const *pos_out,
+              int accumulate);
+
+int sph_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, double co,
+             double ro, double gamma, double *p_out, double *cs_out);
+
+/* kind 0: out_k = g_k (GravityForce); kind 1: out_k = (u, v, w)_k of src
+ * (PositionStepping).  nout outputs, non-LocalReal get 0. */
+int sph_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, const double *g3,
+                    const double *u, const double *v, const double *w, int nout,
+                    double *const *out);
+
+int sph_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
+
+/* FP64 sums over LocalReal particles: out[0]=mass, out[1..3]=momentum,
+ * out[4]=kinetic energy, out[5]=number of LocalReal particles.  out must
+ * hold 6 doubles.  Synchronises. */
+int sph_invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
+
+/* Read and clear the device error word (synchronises). */
+int sph_error_word(sph_ctx *ctx, uint32_t *out);
+
+/* Mean neighbour count (incl. self) of dst among src from the last build,
+ * computed on the device (synchronises).  Used for pair-interaction counts. */
+int sph_mean_neighbours(sph_ctx *ctx, int dst, int src, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYSPH_GB300_H */

@@ -268,14 +268,35 @@ def compile_all(jobs):
         raise SystemExit("reference build failed: %s" % failed)
 
 
+STAMP = os.path.join(REF_OUT, "built.stamp")
+
+
+def _up_to_date():
+    if not os.path.exists(STAMP):
+        return False
+    with open(STAMP) as fh:
+        recorded = fh.read().strip()
+    ext = sysconfig.get_config_var("EXT_SUFFIX")
+    sos = [os.path.join(SRC_OUT, *m.split(".")) + ext for m in MODULES]
+    return recorded == _recipe_id() and all(os.path.exists(x) for x in sos)
+
+
+def _recipe_id():
+    return "%s:%s" % (os.path.getmtime(os.path.abspath(__file__)), sysconfig.get_config_var("EXT_SUFFIX"))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--cythonize-only", action="store_true")
     ap.add_argument("--compile", action="store_true",
                     help="compile already generated C++ sources only")
     args = ap.parse_args()
+    if not args.force and _up_to_date():
+        print("reference oracle up to date in", SRC_OUT)
+        return
     if not args.compile:
         if not os.path.isdir(args.reference):
             raise SystemExit("reference tree not found: %s" % args.reference)
@@ -285,6 +306,8 @@ def main():
         if args.cythonize_only:
             return
     compile_all(args.jobs)
+    with open(STAMP, "w") as fh:
+        fh.write(_recipe_id())
     print("reference oracle built in", SRC_OUT)
 
 

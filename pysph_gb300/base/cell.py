@@ -1,0 +1,196 @@
+"""CellManager: the GPU neighbour structure of one collection of arrays.
+
+Reference: base/cell.pyx:757-1437.  The reference bins particles into a
+dict of ``Cell`` objects with one index list per array and rebins the
+escaped particles on every update.  Here an update is one native build
+(``sph_nnps_build``): every array is binned on a dense grid, sorted by cell
+and gathered into FP32 cell-local snapshots that the pair kernels read.
+
+Kept from the reference: ``cell_size = max_radius_scale * max(h)`` computed
+once at initialisation (:893-925), the jump-tolerance check that raises
+``RuntimeError('Particle moved by more than one cell width')`` (:1422-1437),
+``array_indices`` and ``arrays_to_bin``.  Periodic domains (:1277-1376,
+:1568) are not part of this build.
+"""
+import ctypes
+
+import torch
+
+from .. import native
+
+SNAPSHOT_PROPS = frozenset(("x", "y", "z", "u", "v", "w", "m", "h", "rho", "p", "cs",
+                            "nx", "ny", "nz", "tx", "ty", "tz", "tag"))
+
+
+def array_view(pa):
+    """``sph_array_view`` of a ParticleArray's device tensors."""
+    v = native.ArrayView()
+    v.n = pa.get_number_of_particles()
+    props = pa.properties
+    for f in native.VIEW_FIELDS:
+        t = props.get(f)
+        if t is not None and t.dtype != torch.float64:
+            t = None
+        setattr(v, f, t.data_ptr() if t is not None and t.numel() > 0 else None)
+    t = props.get("tag")
+    v.tag = t.data_ptr() if t is not None and t.numel() > 0 else None
+    return v
+
+
+class CellManager:
+    """Dense-grid cell structure over ``arrays_to_bin``."""
+
+    def __init__(self, arrays_to_bin=None, min_cell_size=-1.0, max_cell_size=0,
+                 periodic_domain=None, initialize=True, max_radius_scale=2.0):
+        if periodic_domain is not None:
+            raise NotImplementedError("periodic domains are not part of the GPU hot path")
+        self.max_radius_scale = max_radius_scale
+        self.min_cell_size = min_cell_size
+        self.max_cell_size = max_cell_size
+        self.arrays_to_bin = list(arrays_to_bin or [])
+        self.num_arrays = len(self.arrays_to_bin)
+        self.array_indices = {}
+        self.coord_x, self.coord_y, self.coord_z = "x", "y", "z"
+        self.jump_tolerance = 1
+        self.cell_size = 0.0
+        self.periodic_domain = None
+        self.is_dirty = True
+        self.initialized = False
+        # internal grid cells per reference cell (1..3); see the autotuner
+        self.cell_subdivision = None
+        self._ctx = None
+        self._snap_versions = []
+        self._build_count = 0
+        if initialize:
+            self.initialize()
+
+    # -- setup ----------------------------------------------------------------
+    def _rebuild_array_indices(self):
+        self.array_indices = {pa.name: i for i, pa in enumerate(self.arrays_to_bin)}
+
+    def initialize(self):
+        if self.initialized:
+            return
+        self._rebuild_array_indices()
+        self.compute_cell_size(self.min_cell_size, self.max_cell_size)
+        self.initialized = True
+        self.update()
+
+    def _compute_minmax_h(self):
+        lo, hi = float("inf"), 0.0
+        for pa in self.arrays_to_bin:
+            if pa.get_number_of_particles() == 0:
+                continue
+            h = pa.get_device("h")
+            lo = min(lo, float(h.min()))
+            hi = max(hi, float(h.max()))
+        return lo, hi
+
+    def compute_cell_size(self, min_size=0, max_size=0):
+        """cell.pyx:893-925."""
+        if min_size <= 0:
+            min_h, max_h = self._compute_minmax_h()
+            self.min_h, self.max_h = min_h, max_h
+            self.cell_size = self.max_radius_scale * max_h
+        else:
+            self.cell_size = min_size
+        if self.cell_size > max_size > 0:
+            self.cell_size = max_size
+        if self.cell_size == 0.0:
+            self.cell_size = 1.0
+        return self.cell_size
+
+    def add_array_to_bin(self, parr):
+        self.arrays_to_bin.append(parr)
+        self.num_arrays = len(self.arrays_to_bin)
+        self._rebuild_array_indices()
+        self.is_dirty = True
+
+    def set_jump_tolerance(self, jump_tolerance):
+        if jump_tolerance != 1:
+            raise NotImplementedError("only the reference's default jump tolerance of 1 is supported")
+        self.jump_tolerance = jump_tolerance
+
+    def get_number_of_particles(self):
+        return sum(pa.get_number_of_particles() for pa in self.arrays_to_bin)
+
+    # -- device structure -------------------------------------------------------
+    def context(self):
+        """The native context (created on first use; needs a GPU)."""
+        L = native.lib()
+        if self._ctx is None:
+            dim = 3
+            h = ctypes.c_void_p()
+            native.check(L.sph_ctx_create(dim, ctypes.byref(h)), "sph_ctx_create")
+            self._ctx = h
+        native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
+            torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
+        return self._ctx
+
+    def _subdivision(self):
+        if self.cell_subdivision is None:
+            from ..tuning import choose_subdivision
+            self.cell_subdivision = choose_subdivision(self)
+        return self.cell_subdivision
+
+    def update_status(self):
+        for pa in self.arrays_to_bin:
+            if pa.is_dirty:
+                self.is_dirty = True
+        return 0
+
+    def update(self):
+        """Rebuild the device structure if any array moved (cell.pyx:927-962)."""
+        self.update_status()
+        if not self.is_dirty:
+            return 0
+        if not torch.cuda.is_available():
+            # no device: the structure is built on first use, where the
+            # computation itself raises (there is no CPU path)
+            return 0
+        ctx = self.context()
+        views = (native.ArrayView * len(self.arrays_to_bin))(
+            *[array_view(pa) for pa in self.arrays_to_bin])
+        rc = native.lib().sph_nnps_build(ctx, views, len(self.arrays_to_bin), self.cell_size,
+                                         self.max_radius_scale, self._subdivision(), 1)
+        native.check(rc, "CellManager.update")
+        self._views = views
+        self._snap_versions = [pa.version for pa in self.arrays_to_bin]
+        for pa in self.arrays_to_bin:
+            pa.set_dirty(False)
+        self.is_dirty = False
+        self._build_count += 1
+        return 0
+
+    def ensure_current(self):
+        """Make every snapshot reflect the arrays' current device data."""
+        self.update_status()
+        if self.is_dirty:
+            self.update()
+            return
+        ctx = None
+        for i, pa in enumerate(self.arrays_to_bin):
+            if pa.version != self._snap_versions[i]:
+                ctx = ctx or self.context()
+                v = array_view(pa)
+                native.check(native.lib().sph_refresh_state(ctx, i, ctypes.byref(v)),
+                             "refresh snapshot")
+                self._snap_versions[i] = pa.version
+
+    def mark_fresh(self, pa):
+        """The snapshot of ``pa`` already matches its data (written together)."""
+        self._snap_versions[self.array_indices[pa.name]] = pa.version
+
+    def slot(self, pa):
+        try:
+            return self.array_indices[pa.name]
+        except KeyError:
+            raise ValueError("Source %s does not exist" % pa.name) from None
+
+    def __del__(self):
+        ctx = getattr(self, "_ctx", None)
+        if ctx is not None:
+            try:
+                native.load_library(False).sph_ctx_destroy(ctx)
+            except Exception:
+                pass

@@ -1,0 +1,208 @@
+// C ABI of the pysph_gb300 library: context management, argument checks and
+// error reporting around the kernels of nnps.cu, pairs.cu and elementwise.cu.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_check(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return SPH_ERR_CUDA;
+}
+
+int red_part_doubles();
+
+namespace {
+
+__global__ void k_sum_i64(const int64_t *v, int64_t n, unsigned long long *out) {
+    unsigned long long s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s += (unsigned long long)v[i];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+}  // namespace
+
+}  // namespace sphgb
+
+using namespace sphgb;
+
+#define CHECK_CTX(c)                                                     \
+    do {                                                                 \
+        if (!(c)) return set_error(SPH_ERR_ARG, "null sph_ctx");         \
+    } while (0)
+
+extern "C" {
+
+int sph_version(void) { return 1; }
+
+int sph_last_error(char *buf, size_t len) {
+    if (!buf || len == 0) return SPH_ERR_ARG;
+    size_t n = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;
+    memcpy(buf, g_last_error.data(), n);
+    buf[n] = 0;
+    return SPH_OK;
+}
+
+int sph_ctx_create(int dim, sph_ctx **out) {
+    if (!out) return set_error(SPH_ERR_ARG, "sph_ctx_create: null out");
+    if (dim < 1 || dim > 3) return set_error(SPH_ERR_ARG, "sph_ctx_create: dim must be 1..3");
+    sph_ctx *c = new (std::nothrow) sph_ctx();
+    if (!c) return set_error(SPH_ERR_ARG, "sph_ctx_create: out of host memory");
+    c->dim = dim;
+    cudaError_t e;
+    if ((e = cudaMalloc(&c->d_box, 8 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_hmax, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_err, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
+        (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess) {
+        sph_ctx_destroy(c);
+        return cuda_check(e, "sph_ctx_create");
+    }
+    cudaMemset(c->d_err, 0, sizeof(unsigned));
+    *out = c;
+    return SPH_OK;
+}
+
+int sph_ctx_destroy(sph_ctx *c) {
+    if (!c) return SPH_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &A : c->arrays) {
+        cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
+        cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st);
+        cudaFree(A.nrm); cudaFree(A.tan);
+        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell);
+    }
+    cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_err);
+    cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);
+    if (c->h_box) cudaFreeHost(c->h_box);
+    if (c->h_red) cudaFreeHost(c->h_red);
+    delete c;
+    return SPH_OK;
+}
+
+int sph_ctx_set_stream(sph_ctx *c, void *stream) {
+    CHECK_CTX(c);
+    c->stream = (cudaStream_t)stream;
+    return SPH_OK;
+}
+
+int sph_nnps_build(sph_ctx *c, const sph_array_view *arrays, int narrays, double cell_size,
+                   double radius_scale, int subdiv, int check_jump) {
+    CHECK_CTX(c);
+    return nnps_build(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
+}
+
+int sph_nnps_count(sph_ctx *c, int dst, int src, double radius_scale, int64_t *counts) {
+    CHECK_CTX(c);
+    if (!counts) return set_error(SPH_ERR_ARG, "sph_nnps_count: null counts");
+    return nnps_count(c, dst, src, radius_scale, counts);
+}
+
+int sph_nnps_fill(sph_ctx *c, int dst, int src, double radius_scale, const int64_t *offsets,
+                  int64_t *index) {
+    CHECK_CTX(c);
+    if (!offsets || !index) return set_error(SPH_ERR_ARG, "sph_nnps_fill: null output");
+    return nnps_fill(c, dst, src, radius_scale, offsets, index);
+}
+
+int sph_refresh_state(sph_ctx *c, int array, const sph_array_view *view) {
+    CHECK_CTX(c);
+    if (!view) return set_error(SPH_ERR_ARG, "sph_refresh_state: null view");
+    return refresh_state(c, array, view);
+}
+
+int sph_density(sph_ctx *c, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
+                double *rho_out, double *p_out, double *cs_out) {
+    CHECK_CTX(c);
+    if (nsrc > 0 && !srcs) return set_error(SPH_ERR_ARG, "sph_density: null sources");
+    if (prm && prm->tait && (!p_out || !cs_out))
+        return set_error(SPH_ERR_ARG, "sph_density: Tait needs p and cs outputs");
+    return launch_density(c, dst, srcs, nsrc, prm, rho_out, p_out, cs_out);
+}
+
+int sph_rates(sph_ctx *c, int dst, const sph_source_term *terms, int nterms,
+              const sph_rates_params *prm, double *const *acc_out, double *const *pos_out,
+              int accumulate) {
+    CHECK_CTX(c);
+    if (nterms > 0 && !terms) return set_error(SPH_ERR_ARG, "sph_rates: null terms");
+    return launch_rates(c, dst, terms, nterms, prm, acc_out, pos_out, accumulate);
+}
+
+int sph_tait(sph_ctx *c, int64_t n, const double *rho, const int64_t *tag, double co, double ro,
+             double gamma, double *p_out, double *cs_out) {
+    CHECK_CTX(c);
+    return launch_tait(c, n, rho, tag, co, ro, gamma, p_out, cs_out);
+}
+
+int sph_const_rates(sph_ctx *c, int kind, int64_t n, const int64_t *tag, const double *g3,
+                    const double *u, const double *v, const double *w, int nout,
+                    double *const *out) {
+    CHECK_CTX(c);
+    return launch_const_rates(c, kind, n, tag, g3, u, v, w, nout, out);
+}
+
+int sph_integrate(sph_ctx *c, int64_t n, const sph_axpy_line *lines, int nlines) {
+    CHECK_CTX(c);
+    return launch_integrate(c, n, lines, nlines);
+}
+
+int sph_invariants(sph_ctx *c, const sph_array_view *a, double *out) {
+    CHECK_CTX(c);
+    return invariants(c, a, out);
+}
+
+int sph_error_word(sph_ctx *c, unsigned *out) {
+    CHECK_CTX(c);
+    if (!out) return set_error(SPH_ERR_ARG, "sph_error_word: null out");
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream);
+    if (e != cudaSuccess) return cuda_check(e, "sph_error_word");
+    *out = h;
+    return SPH_OK;
+}
+
+int sph_mean_neighbours(sph_ctx *c, int dst, int src, double *out) {
+    CHECK_CTX(c);
+    if (!out) return set_error(SPH_ERR_ARG, "sph_mean_neighbours: null out");
+    if (!c->built || dst < 0 || dst >= (int)c->arrays.size())
+        return set_error(SPH_ERR_STATE, "sph_mean_neighbours: no neighbour build");
+    int64_t n = c->arrays[dst].n;
+    if (n == 0) { *out = 0.0; return SPH_OK; }
+    if (n + 1 > c->cnt_cap) {
+        cudaFree(c->d_cnt);
+        c->d_cnt = nullptr;
+        SPH_CUDA(cudaMalloc(&c->d_cnt, sizeof(int64_t) * (n + 1)));
+        c->cnt_cap = n + 1;
+    }
+    int rc = nnps_count(c, dst, src, c->grid.radius_scale, c->d_cnt);
+    if (rc) return rc;
+    unsigned long long *acc = (unsigned long long *)(c->d_part);
+    SPH_CUDA(cudaMemsetAsync(acc, 0, sizeof(unsigned long long), c->stream));
+    k_sum_i64<<<grid_blocks(n, 256, 2), 256, 0, c->stream>>>(c->d_cnt, n, acc);
+    SPH_LAUNCH_CHECK("k_sum_i64");
+    unsigned long long h = 0;
+    SPH_CUDA(cudaMemcpyAsync(&h, acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    SPH_CUDA(cudaStreamSynchronize(c->stream));
+    *out = (double)h / (double)n;
+    return SPH_OK;
+}
+
+}  // extern "C"

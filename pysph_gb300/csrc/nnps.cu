@@ -1,0 +1,542 @@
+// Cell-list neighbour structure on a dense grid (sm_103a).
+//
+// Replaces the reference's CellManager (base/cell.pyx:757-1437: dict of
+// IntPoint -> Cell with per-array index lists, rebinned particle by particle)
+// and the FixedDestNbrParticleLocator cache (base/nnps.pyx:385-620: one
+// LongArray of neighbour indices per destination).  Here a build is:
+//
+//   k_box       bounding box of all arrays in internal cells, max h, and the
+//               reference's jump-tolerance check (cell.pyx:1422-1437)
+//   k_keys      dense cell index per particle + per-cell counts (atomics)
+//   scan        exclusive prefix of the counts -> cstart
+//   k_scatter   counting-sort scatter (order within a cell arbitrary)
+//   k_cellsort  per-cell insertion sort by original index (deterministic)
+//   k_reorder   gather of the sorted FP32 snapshot (cell-local offsets)
+//
+// No per-destination neighbour list is stored: the pair kernels walk the
+// stencil rows of the sorted arrays directly.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int floor_cell(double x, double inv_cs) {
+    return (int)floor(x * inv_cs);
+}
+
+// -------------------------------------------------------------------------
+// bounding box / max h / jump check
+// -------------------------------------------------------------------------
+__global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *refcell,
+                      int check_jump, int *box, unsigned long long *hmax, unsigned *err) {
+    int mn[3] = {INT_MAX, INT_MAX, INT_MAX};
+    int mx[3] = {INT_MIN, INT_MIN, INT_MIN};
+    double hm = 0.0;
+    bool jump = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double p[3] = {ld0(a.x, i), ld0(a.y, i), ld0(a.z, i)};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int c = floor_cell(p[d], inv_cs);
+            mn[d] = min(mn[d], c);
+            mx[d] = max(mx[d], c);
+        }
+        hm = fmax(hm, a.h[i]);
+        if (refcell) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                int c = floor_cell(p[d], inv_cs_ref);
+                if (check_jump && abs(c - refcell[3 * i + d]) > 1) jump = true;
+                refcell[3 * i + d] = c;
+            }
+        }
+    }
+    // warp, then block, then one set of atomics per block
+    __shared__ int s_mn[3][32], s_mx[3][32];
+    __shared__ double s_h[32];
+    __shared__ int s_j[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = __reduce_min_sync(0xffffffffu, mn[d]);
+        mx[d] = __reduce_max_sync(0xffffffffu, mx[d]);
+    }
+    for (int off = 16; off > 0; off >>= 1) hm = fmax(hm, __shfl_xor_sync(0xffffffffu, hm, off));
+    int anyjump = __any_sync(0xffffffffu, jump) ? 1 : 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { s_mn[d][wid] = mn[d]; s_mx[d][wid] = mx[d]; }
+        s_h[wid] = hm;
+        s_j[wid] = anyjump;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        int a[3], b[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            a[d] = lane < nw ? s_mn[d][lane] : INT_MAX;
+            b[d] = lane < nw ? s_mx[d][lane] : INT_MIN;
+            a[d] = __reduce_min_sync(0xffffffffu, a[d]);
+            b[d] = __reduce_max_sync(0xffffffffu, b[d]);
+        }
+        double hh = lane < nw ? s_h[lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) hh = fmax(hh, __shfl_xor_sync(0xffffffffu, hh, off));
+        int jj = __any_sync(0xffffffffu, lane < nw && s_j[lane]);
+        if (lane == 0) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                atomicMin(&box[d], a[d]);
+                atomicMax(&box[3 + d], b[d]);
+            }
+            atomicMax(hmax, (unsigned long long)__double_as_longlong(hh));
+            if (jj) atomicOr(err, SPH_EFLAG_JUMP);
+        }
+    }
+}
+
+__global__ void k_box_init(int *box, unsigned long long *hmax) {
+    if (threadIdx.x < 3) {
+        box[threadIdx.x] = INT_MAX;
+        box[3 + threadIdx.x] = INT_MIN;
+    }
+    if (threadIdx.x == 0) *hmax = 0ull;
+}
+
+// -------------------------------------------------------------------------
+// keys, counting sort
+// -------------------------------------------------------------------------
+__global__ void k_keys(sph_array_view a, Grid g, int *key, int *count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int cx = floor_cell(ld0(a.x, i), g.inv_cs) - g.bx0;
+        int cy = floor_cell(ld0(a.y, i), g.inv_cs) - g.by0;
+        int cz = floor_cell(ld0(a.z, i), g.inv_cs) - g.bz0;
+        int k = cx + g.nx * (cy + g.ny * cz);
+        key[i] = k;
+        atomicAdd(&count[k], 1);
+    }
+}
+
+// exclusive scan, 3 phases: per-tile scan + tile totals, scan of totals, add
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem, int &total) {
+    // warp inclusive scan
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) smem[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = blockDim.x >> 5;
+        int s = lane < nw ? smem[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, off);
+            if (lane >= off) s += y;
+        }
+        if (lane < nw) smem[lane] = s;
+    }
+    __syncthreads();
+    int warp_prefix = wid > 0 ? smem[wid - 1] : 0;
+    total = smem[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void k_scan_tiles(int *data, int64_t n, int *tile_tot) {
+    __shared__ int smem[32];
+    int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? data[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int pre = block_exclusive_scan(s, smem, total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) data[base + k] = pre;
+        pre += v[k];
+    }
+    if (threadIdx.x == 0) tile_tot[blockIdx.x] = total;
+}
+
+__global__ void k_scan_totals(int *tot, int64_t ntiles) {
+    __shared__ int smem[32];
+    int carry = 0;
+    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
+        int64_t i = b + threadIdx.x;
+        int v = i < ntiles ? tot[i] : 0;
+        int total;
+        int pre = block_exclusive_scan(v, smem, total);
+        if (i < ntiles) tot[i] = pre + carry;
+        carry += total;
+    }
+}
+
+__global__ void k_scan_add(int *data, int64_t n, const int *tile_off) {
+    int add = tile_off[blockIdx.x];
+    int64_t base = blockIdx.x * (int64_t)kScanTile;
+    for (int k = threadIdx.x; k < kScanTile; k += blockDim.x)
+        if (base + k < n) data[base + k] += add;
+}
+
+__global__ void k_scatter(int64_t n, const int *key, int *cursor, int *perm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int slot = atomicAdd(&cursor[key[i]], 1);
+        perm[slot] = (int)i;
+    }
+}
+
+__global__ void k_cellsort(int64_t ncells, const int *cstart, int *perm) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int s = cstart[c], e = cstart[c + 1];
+        for (int a = s + 1; a < e; ++a) {
+            int v = perm[a];
+            int b = a - 1;
+            while (b >= s && perm[b] > v) {
+                perm[b + 1] = perm[b];
+                --b;
+            }
+            perm[b + 1] = v;
+        }
+    }
+}
+
+// -------------------------------------------------------------------------
+// sorted snapshot
+// -------------------------------------------------------------------------
+__global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *key, int *skey,
+                          float4 *posm, float4 *velh, float4 *st, float4 *nrm, float4 *tan) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        int i = perm[s];
+        int k = key[i];
+        skey[s] = k;
+        int cx, cy, cz;
+        decode_cell(g, k, cx, cy, cz);
+        double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
+        float xi = (float)fma(-ox, g.cs, ld0(a.x, i));
+        float yi = (float)fma(-oy, g.cs, ld0(a.y, i));
+        float zi = (float)fma(-oz, g.cs, ld0(a.z, i));
+        posm[s] = make_float4(xi, yi, zi, (float)a.m[i]);
+        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
+                              (float)a.h[i]);
+        float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), p);
+        if (nrm) {
+            nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
+            tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
+        }
+    }
+}
+
+// -------------------------------------------------------------------------
+// neighbour export (exact FP64 test; API / parity path, not the hot loop)
+// -------------------------------------------------------------------------
+template <bool FILL>
+__global__ void k_nbr(sph_array_view d, sph_array_view s, Grid g, const int *dkey,
+                      const int *scstart, const int *sperm, double radius_scale, int same,
+                      int64_t *counts, const int64_t *offsets, int64_t *index) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int cx, cy, cz;
+        decode_cell(g, dkey[i], cx, cy, cz);
+        double px = ld0(d.x, i), py = ld0(d.y, i), pz = ld0(d.z, i);
+        double radius = __dmul_rn(d.h[i], radius_scale);
+        double r2 = __dmul_rn(radius, radius);
+        int64_t cnt = 0;
+        int64_t base = FILL ? offsets[i] : 0;
+        for (int dz = -g.kz; dz <= g.kz; ++dz)
+            for (int dy = -g.ky; dy <= g.ky; ++dy) {
+                int64_t rowbase = (int64_t)g.nx * ((cy + dy) + (int64_t)g.ny * (cz + dz));
+                int rs = scstart[rowbase + cx - g.kx], re = scstart[rowbase + cx + g.kx + 1];
+                for (int t = rs; t < re; ++t) {
+                    int j = sperm[t];
+                    if (exact_within(ld0(s.x, j), ld0(s.y, j), ld0(s.z, j), px, py, pz, r2)) {
+                        if (FILL) index[base + cnt] = j;
+                        ++cnt;
+                    }
+                }
+            }
+        if (FILL) {
+            // ascending, self last (base/nnps.pyx:611-618 keeps self last)
+            for (int64_t a2 = base + 1; a2 < base + cnt; ++a2) {
+                int64_t v = index[a2];
+                int64_t b = a2 - 1;
+                while (b >= base && index[b] > v) {
+                    index[b + 1] = index[b];
+                    --b;
+                }
+                index[b + 1] = v;
+            }
+            if (same) {
+                for (int64_t t = base; t + 1 < base + cnt; ++t)
+                    if (index[t] == i) {
+                        for (int64_t u = t; u + 1 < base + cnt; ++u) index[u] = index[u + 1];
+                        index[base + cnt - 1] = i;
+                        break;
+                    }
+            }
+        } else {
+            counts[i] = cnt;
+        }
+    }
+}
+
+template <class T>
+int ensure(T **p, int64_t &cap, int64_t need) {
+    if (need <= cap && *p) return SPH_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    int64_t c = std::max<int64_t>(need + need / 8, 256);
+    SPH_CUDA(cudaMalloc((void **)p, sizeof(T) * c));
+    cap = c;
+    return SPH_OK;
+}
+
+int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
+    int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    int rc = ensure(&ctx->scan_tmp, ctx->scan_tmp_cap, ntiles);
+    if (rc) return rc;
+    k_scan_tiles<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    k_scan_totals<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, ntiles);
+    k_scan_add<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    SPH_LAUNCH_CHECK("scan");
+    return SPH_OK;
+}
+
+int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
+    if (n <= A.cap && A.perm && (!nrm || A.nrm)) return SPH_OK;
+    cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
+    cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st); cudaFree(A.nrm); cudaFree(A.tan);
+    A.key = A.perm = A.skey = nullptr;
+    A.posm = A.velh = A.st = A.nrm = A.tan = nullptr;
+    int64_t c = std::max<int64_t>(n, 1);
+    SPH_CUDA(cudaMalloc(&A.key, sizeof(int) * c));
+    SPH_CUDA(cudaMalloc(&A.perm, sizeof(int) * c));
+    SPH_CUDA(cudaMalloc(&A.skey, sizeof(int) * c));
+    SPH_CUDA(cudaMalloc(&A.posm, sizeof(float4) * c));
+    SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * c));
+    SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * c));
+    if (nrm) {
+        SPH_CUDA(cudaMalloc(&A.nrm, sizeof(float4) * c));
+        SPH_CUDA(cudaMalloc(&A.tan, sizeof(float4) * c));
+    }
+    A.cap = c;
+    return SPH_OK;
+}
+
+}  // namespace
+
+int grid_blocks(int64_t n, int threads, int per_sm) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    int64_t need = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sms * per_sm;
+    return (int)std::max<int64_t>(1, std::min(need, cap));
+}
+
+int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+               double radius_scale, int subdiv, int check_jump) {
+    if (narrays <= 0 || !arrays) return set_error(SPH_ERR_ARG, "nnps_build: no arrays");
+    if (!(cell_size > 0)) return set_error(SPH_ERR_ARG, "nnps_build: cell_size must be > 0");
+    if (subdiv < 1 || subdiv > 3) return set_error(SPH_ERR_ARG, "nnps_build: subdiv must be 1..3");
+    cudaStream_t st = ctx->stream;
+    bool same_layout = (int)ctx->arrays.size() == narrays;
+    if (same_layout)
+        for (int a = 0; a < narrays; ++a)
+            if (ctx->arrays[a].ref_n != arrays[a].n) same_layout = false;
+    if ((int)ctx->arrays.size() < narrays) ctx->arrays.resize(narrays);
+    if (ctx->cell_size_ref != cell_size) same_layout = false;
+    ctx->cell_size_ref = cell_size;
+
+    const double cs = cell_size / subdiv;
+    const double inv_cs = 1.0 / cs;
+    const double inv_cs_ref = 1.0 / cell_size;
+
+    k_box_init<<<1, 32, 0, st>>>(ctx->d_box, ctx->d_hmax);
+    SPH_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), st));
+    for (int a = 0; a < narrays; ++a) {
+        ArraySnap &A = ctx->arrays[a];
+        const sph_array_view &v = arrays[a];
+        if (v.n < 0 || (v.n > 0 && (!v.x || !v.h || !v.m)))
+            return set_error(SPH_ERR_ARG, "nnps_build: array needs x, h and m");
+        if (v.n >= (int64_t)INT32_MAX) return set_error(SPH_ERR_ARG, "nnps_build: array too large");
+        int64_t rn = A.ref_n;
+        if (rn != v.n) {
+            cudaFree(A.refcell);
+            A.refcell = nullptr;
+            SPH_CUDA(cudaMalloc(&A.refcell, sizeof(int) * 3 * std::max<int64_t>(v.n, 1)));
+            A.ref_n = v.n;
+        }
+        if (v.n == 0) continue;
+        int jb = (check_jump && same_layout) ? 1 : 0;
+        k_box<<<grid_blocks(v.n, kThreads, 2), kThreads, 0, st>>>(v, inv_cs, inv_cs_ref, A.refcell, jb,
+                                                               ctx->d_box, ctx->d_hmax, ctx->d_err);
+        SPH_LAUNCH_CHECK("k_box");
+    }
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box, ctx->d_box, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 6, ctx->d_hmax, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaStreamSynchronize(st));
+    unsigned err = (unsigned)ctx->h_box[8];
+    if (err & SPH_EFLAG_JUMP) {
+        ctx->built = false;
+        return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
+    }
+    int64_t total_n = 0;
+    for (int a = 0; a < narrays; ++a) total_n += arrays[a].n;
+    if (total_n == 0) return set_error(SPH_ERR_ARG, "nnps_build: no particles");
+
+    double hmax;
+    memcpy(&hmax, ctx->h_box + 6, sizeof(hmax));
+    Grid g;
+    g.cs = cs;
+    g.inv_cs = inv_cs;
+    g.cs_f = (float)cs;
+    g.radius_scale = radius_scale;
+    int k = (int)std::ceil(radius_scale * hmax * inv_cs - 1e-9);
+    if (k < 1) k = 1;
+    if (k > 3)
+        return set_error(SPH_ERR_NOTSUP,
+                         "nnps_build: search radius spans more than 3 cells (cell size too small)");
+    int mn[3], mx[3];
+    for (int d = 0; d < 3; ++d) { mn[d] = ctx->h_box[d]; mx[d] = ctx->h_box[3 + d]; }
+    g.kx = k;
+    g.ky = (mx[1] > mn[1]) ? k : 0;
+    g.kz = (mx[2] > mn[2]) ? k : 0;
+    g.bx0 = mn[0] - g.kx;
+    g.by0 = mn[1] - g.ky;
+    g.bz0 = mn[2] - g.kz;
+    int64_t nx = (int64_t)mx[0] - mn[0] + 1 + 2 * g.kx;
+    int64_t ny = (int64_t)mx[1] - mn[1] + 1 + 2 * g.ky;
+    int64_t nz = (int64_t)mx[2] - mn[2] + 1 + 2 * g.kz;
+    const int64_t kMaxCells = (int64_t)1 << 27;
+    if (nx * ny > kMaxCells || nx * ny * nz > kMaxCells)
+        return set_error(SPH_ERR_GRID,
+                         "nnps_build: particle extent needs more than 2^27 grid cells");
+    g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
+    g.ncells = nx * ny * nz;
+    ctx->grid = g;
+
+    for (int a = 0; a < narrays; ++a) {
+        ArraySnap &A = ctx->arrays[a];
+        const sph_array_view &v = arrays[a];
+        A.view = v;
+        A.n = v.n;
+        A.has_nrm = v.nx || v.ny || v.nz;
+        int rc = alloc_array(A, v.n, A.has_nrm);
+        if (rc) return rc;
+        if (g.ncells + 1 > A.cell_cap || !A.cstart) {
+            cudaFree(A.cstart);
+            cudaFree(A.cursor);
+            A.cstart = A.cursor = nullptr;
+            int64_t c = g.ncells + 1 + (g.ncells + 1) / 4;
+            SPH_CUDA(cudaMalloc(&A.cstart, sizeof(int) * c));
+            SPH_CUDA(cudaMalloc(&A.cursor, sizeof(int) * c));
+            A.cell_cap = c;
+        }
+        SPH_CUDA(cudaMemsetAsync(A.cstart, 0, sizeof(int) * (g.ncells + 1), st));
+        if (v.n > 0) {
+            int nb = grid_blocks(v.n, kThreads);
+            k_keys<<<nb, kThreads, 0, st>>>(v, g, A.key, A.cstart);
+            SPH_LAUNCH_CHECK("k_keys");
+        }
+        rc = scan_exclusive(ctx, A.cstart, g.ncells + 1);
+        if (rc) return rc;
+        if (v.n > 0) {
+            SPH_CUDA(cudaMemcpyAsync(A.cursor, A.cstart, sizeof(int) * g.ncells,
+                                     cudaMemcpyDeviceToDevice, st));
+            int nb = grid_blocks(v.n, kThreads);
+            k_scatter<<<nb, kThreads, 0, st>>>(v.n, A.key, A.cursor, A.perm);
+            k_cellsort<<<grid_blocks(g.ncells, kThreads), kThreads, 0, st>>>(g.ncells, A.cstart, A.perm);
+            k_reorder<<<nb, kThreads, 0, st>>>(v, g, A.perm, A.key, A.skey, A.posm, A.velh, A.st,
+                                               A.has_nrm ? A.nrm : nullptr,
+                                               A.has_nrm ? A.tan : nullptr);
+            SPH_LAUNCH_CHECK("nnps sort/reorder");
+        }
+    }
+    ctx->built = true;
+    return SPH_OK;
+}
+
+int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
+    if (!ctx->built || a < 0 || a >= (int)ctx->arrays.size())
+        return set_error(SPH_ERR_STATE, "refresh_state: no neighbour build for this array");
+    ArraySnap &A = ctx->arrays[a];
+    if (view->n != A.n)
+        return set_error(SPH_ERR_STATE, "refresh_state: particle count changed; rebuild needed");
+    bool nrm = view->nx || view->ny || view->nz;
+    if (nrm && !A.nrm)
+        return set_error(SPH_ERR_STATE, "refresh_state: normals added; rebuild needed");
+    A.view = *view;
+    A.has_nrm = nrm;
+    if (A.n == 0) return SPH_OK;
+    k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
+        A.view, ctx->grid, A.perm, A.key, A.skey, A.posm, A.velh, A.st, nrm ? A.nrm : nullptr,
+        nrm ? A.tan : nullptr);
+    SPH_LAUNCH_CHECK("k_reorder (refresh)");
+    return SPH_OK;
+}
+
+int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *counts) {
+    if (!ctx->built || dst < 0 || src < 0 || dst >= (int)ctx->arrays.size() ||
+        src >= (int)ctx->arrays.size())
+        return set_error(SPH_ERR_STATE, "nnps_count: no neighbour build for these arrays");
+    if (radius_scale > ctx->grid.radius_scale)
+        return set_error(SPH_ERR_ARG, "nnps_count: radius_scale larger than the build's");
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[src];
+    if (D.n == 0) return SPH_OK;
+    k_nbr<false><<<grid_blocks(D.n, 128), 128, 0, ctx->stream>>>(
+        D.view, S.view, ctx->grid, D.key, S.cstart, S.perm, radius_scale, dst == src,
+        counts, nullptr, nullptr);
+    SPH_LAUNCH_CHECK("k_nbr count");
+    return SPH_OK;
+}
+
+int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
+              int64_t *index) {
+    if (!ctx->built || dst < 0 || src < 0 || dst >= (int)ctx->arrays.size() ||
+        src >= (int)ctx->arrays.size())
+        return set_error(SPH_ERR_STATE, "nnps_fill: no neighbour build for these arrays");
+    if (radius_scale > ctx->grid.radius_scale)
+        return set_error(SPH_ERR_ARG, "nnps_fill: radius_scale larger than the build's");
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[src];
+    if (D.n == 0) return SPH_OK;
+    k_nbr<true><<<grid_blocks(D.n, 128), 128, 0, ctx->stream>>>(
+        D.view, S.view, ctx->grid, D.key, S.cstart, S.perm, radius_scale, dst == src,
+        nullptr, offsets, index);
+    SPH_LAUNCH_CHECK("k_nbr fill");
+    return SPH_OK;
+}
+
+}  // namespace sphgb

@@ -1,0 +1,322 @@
+// Internal declarations of the pysph_gb300 CUDA library (sm_103a).
+//
+// Data layout (per particle array, per neighbour build):
+//   original order (caller-owned FP64 SoA):  x y z u v w m h rho p cs [nx..tz] tag
+//   sorted order (context-owned, cell-major, deterministic within a cell):
+//     perm[s]  -> original index of sorted slot s          int32
+//     skey[s]  -> dense-grid cell of slot s                int32
+//     posm[s]  =  (xi_x, xi_y, xi_z, m)  cell-local FP32 offsets + mass
+//     velh[s]  =  (u, v, w, h)                              FP32
+//     st[s]    =  (rho, p/rho^2, cs, 0)                     FP32
+//     nrm[s], tan[s] (walls only)
+//   per array dense cell table cstart[ncells+1] (exclusive prefix of counts).
+// A row of 2K+1 cells along x is contiguous in the sorted arrays, so one
+// (dy, dz) stencil row is a single index range [cstart[c-K], cstart[c+K+1]).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "pysph_gb300.h"
+
+namespace sphgb {
+
+constexpr int kQueue = 64;      // per-warp pair queue entries (2 x 32 lanes)
+constexpr int kPairBlock = 256; // threads per block of the pair kernels
+
+struct Grid {
+    int bx0 = 0, by0 = 0, bz0 = 0; // origin of the dense grid (internal cell coords)
+    int nx = 1, ny = 1, nz = 1;    // dense grid dims
+    int kx = 1, ky = 0, kz = 0;    // stencil half widths (cells)
+    int64_t ncells = 1;
+    double cs = 1.0;               // internal cell size
+    double inv_cs = 1.0;
+    float cs_f = 1.f;
+    double radius_scale = 2.0;
+};
+
+struct ArraySnap {
+    int64_t n = 0;
+    int64_t cap = 0;
+    sph_array_view view{};
+    bool has_nrm = false;
+    int *key = nullptr;   // original order, dense cell index
+    int *perm = nullptr;  // sorted -> original
+    int *skey = nullptr;  // sorted: cell
+    float4 *posm = nullptr, *velh = nullptr, *st = nullptr, *nrm = nullptr, *tan = nullptr;
+    int *cstart = nullptr; // ncells + 1
+    int *cursor = nullptr; // ncells
+    int64_t cell_cap = 0;
+    int *refcell = nullptr; // original order, 3 ints per particle (jump check)
+    int64_t ref_n = -1;     // particle count the refcell entries belong to
+};
+
+}  // namespace sphgb
+
+struct sph_ctx {
+    int dim = 3;
+    cudaStream_t stream = 0;
+    std::vector<sphgb::ArraySnap> arrays;
+    sphgb::Grid grid;
+    bool built = false;
+    // small device / pinned scratch
+    int *d_box = nullptr;               // [6] internal-cell min xyz, max xyz
+    unsigned long long *d_hmax = nullptr;
+    unsigned *d_err = nullptr;
+    int *h_box = nullptr;               // pinned mirror: box[6], hmax bits (2 ints), err
+    int *scan_tmp = nullptr;
+    int64_t scan_tmp_cap = 0;
+    double *d_part = nullptr;           // reduction partials
+    double *h_red = nullptr;            // pinned
+    int64_t *d_cnt = nullptr;           // int64 scratch (mean neighbours)
+    int64_t cnt_cap = 0;
+    double cell_size_ref = 0;           // reference cell size of the jump check
+};
+
+namespace sphgb {
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+int set_error(int code, const std::string &msg);
+int cuda_check(cudaError_t e, const char *what);
+#define SPH_CUDA(call)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return sphgb::cuda_check(e_, #call); \
+    } while (0)
+#define SPH_LAUNCH_CHECK(what)                                  \
+    do {                                                        \
+        cudaError_t e_ = cudaGetLastError();                    \
+        if (e_ != cudaSuccess) return sphgb::cuda_check(e_, what); \
+    } while (0)
+
+int grid_blocks(int64_t n, int threads, int per_sm = 8);
+
+// launchers implemented in the .cu files
+int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+               double radius_scale, int subdiv, int check_jump);
+int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *counts);
+int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
+              int64_t *index);
+int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view);
+int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc,
+                   const sph_density_params *prm, double *rho, double *p, double *cs);
+int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+                 const sph_rates_params *prm, double *const *acc, double *const *pos,
+                 int accumulate);
+int launch_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, double co,
+                double ro, double gamma, double *p, double *cs);
+int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, const double *g3,
+                       const double *u, const double *v, const double *w, int nout,
+                       double *const *out);
+int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
+int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+
+// Neumaier-compensated FP32 accumulator (sum = hi + lo).
+struct CSum {
+    float hi, lo;
+    __device__ __forceinline__ CSum() : hi(0.f), lo(0.f) {}
+    __device__ __forceinline__ void add(float x) {
+        float t = hi + x;
+        float e = (fabsf(hi) >= fabsf(x)) ? ((hi - t) + x) : ((x - t) + hi);
+        hi = t;
+        lo += e;
+    }
+    // merge another compensated sum (error-free TwoSum of the leading parts)
+    __device__ __forceinline__ void merge(float ohi, float olo) {
+        float s = hi + ohi;
+        float bp = s - hi;
+        float err = (hi - (s - bp)) + (ohi - bp);
+        hi = s;
+        lo = lo + olo + err;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// butterfly reduction of a compensated sum over the LPD lanes of a group
+template <int LPD>
+__device__ __forceinline__ void group_reduce(CSum &c) {
+#pragma unroll
+    for (int off = LPD / 2; off > 0; off >>= 1) {
+        float ohi = __shfl_xor_sync(0xffffffffu, c.hi, off);
+        float olo = __shfl_xor_sync(0xffffffffu, c.lo, off);
+        c.merge(ohi, olo);
+    }
+}
+
+// cubic spline normalisation for h = 1 (base/kernels.pyx:437-443)
+__device__ __forceinline__ float cubic_fac(int dim, float ih) {
+    // 1D: 2/3, 2D: 10/(7 pi), 3D: 1/pi, times h^-dim
+    if (dim == 3) return 0.318309886183790672f * ih * ih * ih;
+    if (dim == 2) return 0.454728408833986667f * ih * ih;
+    return 0.666666666666666667f * ih;
+}
+
+// W(q) / fac  (base/kernels.pyx:351-374)
+__device__ __forceinline__ float cubic_w(float q) {
+    float t = 2.f - q;
+    float outer = 0.25f * t * t * t;
+    float inner = 1.f - 1.5f * (q * q) * (1.f - 0.5f * q);
+    return q > 2.f ? 0.f : (q > 1.f ? outer : inner);
+}
+
+// dW/dr / (r fac)  (base/kernels.pyx:376-413); ih = 1/h, rinv = 1/r
+__device__ __forceinline__ float cubic_gfac(float q, float ih, float rinv) {
+    float t = 2.f - q;
+    float outer = -0.75f * t * t * ih * rinv;
+    float inner = 3.f * (0.75f * q - 1.f) * ih * ih;
+    return q > 2.f ? 0.f : (q >= 1.f ? outer : (q > 1e-14f ? inner : 0.f));
+}
+
+// FP64 neighbour test exactly as base/nnps.pyx:337-353 (no FMA contraction):
+// d2 = (sx-px)^2 + (sy-py)^2 + (sz-pz)^2 < (radius_scale*h)^2
+__device__ __forceinline__ bool exact_within(double sx, double sy, double sz, double px,
+                                             double py, double pz, double radius2) {
+    double dx = __dsub_rn(sx, px), dy = __dsub_rn(sy, py), dz = __dsub_rn(sz, pz);
+    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return d2 < radius2;
+}
+
+__device__ __forceinline__ double ld0(const double *p, int64_t i) { return p ? p[i] : 0.0; }
+
+// Per-source view used by the pair kernels.
+struct SrcDev {
+    const float4 *posm, *velh, *st, *nrm, *tan;
+    const int *cstart, *perm;
+    const double *x, *y, *z;
+    uint32_t flags;
+    float alpha, beta, eta2, eps, delp;
+};
+
+// Per-destination data shared by the LPD lanes of a group.
+struct DestCtx {
+    float xi_x, xi_y, xi_z; // cell-local offsets
+    int cx, cy, cz;         // dense grid coords of the dest cell
+    float r2lo, r2hi;       // FP32 accept / reject bands
+    double px, py, pz;      // FP64 position (band recheck)
+    double radius2;         // (radius_scale*h)^2 in FP64
+    bool active;            // has a candidate range at all
+};
+
+// Queue entry: relative vector dest-src (FP32) and the mass of the source.
+struct QEntry {
+    float4 r; // rx, ry, rz, m_j
+};
+
+// Warp-cooperative traversal of the stencil of each group's destination.
+// Every lane of the warp must call this with identical (uniform) grid data;
+// groups of LPD lanes own one destination each.  Candidates are tested by
+// all lanes in parallel; hits are compacted into a per-group queue in shared
+// memory and handed to `proc(j, entry)` LPD at a time, so the pair body runs
+// with all lanes busy.
+template <int KX, int LPD, class Proc>
+__device__ __forceinline__ void traverse(const Grid &g, const SrcDev &S, const DestCtx &d,
+                                         int *qj, QEntry *qe, Proc &proc) {
+    const int lane = threadIdx.x & 31;
+    const int grp = lane / LPD;
+    const int gl = lane % LPD;
+    const unsigned gshift = grp * LPD;
+    const unsigned gbits = (LPD == 32) ? 0xffffffffu : (((1u << (LPD % 32)) - 1u) << gshift);
+    int *myqj = qj + grp * 2 * LPD;
+    QEntry *myqe = qe + grp * 2 * LPD;
+    int qn = 0;
+
+    auto flush = [&](bool all) {
+        // process min(qn, LPD) entries of every group, then shift the rest down
+        while (__any_sync(0xffffffffu, all ? (qn > 0) : (qn >= LPD))) {
+            int take = min(qn, LPD);
+            if (gl < take) proc(myqj[gl], myqe[gl]);
+            int rest = qn - take;
+            int mj = 0;
+            QEntry me;
+            bool mv = gl < rest;
+            if (mv) {
+                mj = myqj[LPD + gl];
+                me = myqe[LPD + gl];
+            }
+            __syncwarp();
+            if (mv) {
+                myqj[gl] = mj;
+                myqe[gl] = me;
+            }
+            __syncwarp();
+            qn = rest;
+            if (!all) break;
+        }
+    };
+
+    const float csf = g.cs_f;
+    for (int dz = -g.kz; dz <= g.kz; ++dz) {
+        for (int dy = -g.ky; dy <= g.ky; ++dy) {
+            int rs = 0, re = 0;
+            int bnd[2 * KX];
+            if (d.active) {
+                int64_t rowbase = (int64_t)g.nx * ((d.cy + dy) + (int64_t)g.ny * (d.cz + dz));
+                int64_t c0 = rowbase + d.cx - KX;
+                rs = S.cstart[c0];
+#pragma unroll
+                for (int t = 0; t < 2 * KX; ++t) bnd[t] = S.cstart[c0 + t + 1];
+                re = S.cstart[c0 + 2 * KX + 1];
+            } else {
+#pragma unroll
+                for (int t = 0; t < 2 * KX; ++t) bnd[t] = 0;
+            }
+            const float sy = -(float)dy * csf;
+            const float sz = -(float)dz * csf;
+            int rounds = (re - rs + LPD - 1) / LPD;
+            int maxr = __reduce_max_sync(0xffffffffu, rounds);
+            for (int r = 0; r < maxr; ++r) {
+                int j = rs + r * LPD + gl;
+                bool hit = false;
+                float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < re) {
+                    float4 pj = S.posm[j];
+                    int t = 0;
+#pragma unroll
+                    for (int b = 0; b < 2 * KX; ++b) t += (j >= bnd[b]) ? 1 : 0;
+                    float sx = -(float)(t - KX) * csf;
+                    float rx = (d.xi_x - pj.x) + sx;
+                    float ry = (d.xi_y - pj.y) + sy;
+                    float rz = (d.xi_z - pj.z) + sz;
+                    float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    hit = r2 < d.r2lo;
+                    if (!hit && r2 <= d.r2hi) {
+                        int oj = S.perm[j];
+                        hit = exact_within(S.x ? S.x[oj] : 0.0, S.y ? S.y[oj] : 0.0,
+                                           S.z ? S.z[oj] : 0.0, d.px, d.py, d.pz, d.radius2);
+                    }
+                    e = make_float4(rx, ry, rz, pj.w);
+                }
+                unsigned m = __ballot_sync(0xffffffffu, hit);
+                unsigned gm = (m & gbits) >> gshift;
+                if (hit) {
+                    int pos = qn + __popc(gm & ((1u << gl) - 1u));
+                    myqj[pos] = j;
+                    myqe[pos].r = e;
+                }
+                qn += __popc(gm);
+                __syncwarp();
+                flush(false);
+            }
+        }
+    }
+    flush(true);
+}
+
+// Set up the DestCtx of sorted dest slot ds (all lanes of the group call it).
+__device__ __forceinline__ void decode_cell(const Grid &g, int key, int &cx, int &cy, int &cz) {
+    cx = key % g.nx;
+    int rest = key / g.nx;
+    cy = rest % g.ny;
+    cz = rest / g.ny;
+}
+
+}  // namespace sphgb

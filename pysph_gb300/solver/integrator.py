@@ -1,0 +1,366 @@
+"""Euler and RK2 integrators driving the GPU stages.
+
+Reference: solver/integrator.py.  The reference evaluates its calcs one by
+one (``eval`` :432-470), storing every integrating calc's result in its own
+``_k<n>_<prop><i><j>`` array, then steps the properties with NumPy
+(``step`` :472-514, Euler ``final_step`` :535-553, RK2 ``final_step``
+:597-619).  Here ``setup_integrator`` compiles the calc list into stages:
+
+* ``DensityStage``  -- SPHRho over all its sources, fused with an
+  immediately following TaitEquation on the same destination;
+* ``TaitStage``     -- a TaitEquation on its own (e.g. before SPHRho);
+* ``RatesStage``    -- a maximal run of consecutive integrating calcs on one
+  destination (pressure gradient, artificial viscosity, boundary force,
+  XSPH, gravity, position stepping) as ONE rates-kernel launch writing the
+  summed rate of each integrated property.
+
+Integrating calcs only write rates, never state, so merging a consecutive
+run of them changes nothing but the order of the FP64 additions (the
+reference adds each calc's ``k*dt`` in turn).  The state update is one FP64
+kernel per array with the rounding of the reference's NumPy expressions.
+"""
+import logging
+
+import torch
+
+from ..sph import gpu
+from ..sph.sph_calc import RATE_KINDS, _kind_of, _term
+
+logger = logging.getLogger()
+
+VEL = ("u", "v", "w")
+POS = ("x", "y", "z")
+VEL_KINDS = ("pgrad", "avisc", "bforce", "gravity")
+POS_KINDS = ("xsph", "step")
+
+
+class DensityStage:
+    def __init__(self, calc, tait=None):
+        self.calc = calc
+        self.tait = tait
+        self.dest = calc.dest
+
+    def run(self, integ, kname):
+        c = self.calc
+        cm = integ.particles.cell_manager
+        rho = self.dest.get_device(c.updates[0])
+        if self.tait is not None:
+            t = self.tait.funcs[0]
+            p = self.dest.get_device(self.tait.updates[0])
+            cs = self.dest.get_device(self.tait.updates[1])
+            gpu.density(cm, self.dest, c.sources, c.kernel.dim, rho, (t.co, t.ro, t.gamma), p, cs)
+            names = [c.updates[0]] + list(self.tait.updates)
+            own = names == ["rho", "p", "cs"]
+        else:
+            gpu.density(cm, self.dest, c.sources, c.kernel.dim, rho)
+            names = [c.updates[0]]
+            own = names == ["rho"]
+        gpu.note_written(cm, self.dest, names, consistent=own)
+
+
+class TaitStage:
+    def __init__(self, calc):
+        self.calc = calc
+        self.dest = calc.dest
+
+    def run(self, integ, kname):
+        c = self.calc
+        f = c.funcs[0]
+        cm = integ.particles.cell_manager
+        gpu.tait(cm, self.dest, f.co, f.ro, f.gamma, self.dest.get_device(c.updates[0]),
+                 self.dest.get_device(c.updates[1]))
+        gpu.note_written(cm, self.dest, c.updates)
+
+
+class CalcStage:
+    """A non-integrating calc evaluated on its own (``calc.sph(*updates)``)."""
+
+    def __init__(self, calc):
+        self.calc = calc
+        self.dest = calc.dest
+
+    def run(self, integ, kname):
+        self.calc.sph(*self.calc.updates)
+
+
+class RatesStage:
+    def __init__(self, calcs):
+        self.calcs = calcs
+        self.dest = calcs[0].dest
+        self.terms = []
+        self.gravity = None
+        self.add_velocity = False
+        self.props = []
+        dim = None
+        for c in calcs:
+            kind = _kind_of(c.funcs[0])
+            if kind not in RATE_KINDS + ("gravity", "step"):
+                raise NotImplementedError("%s cannot be integrated on the GPU" % kind)
+            allowed = VEL if kind in VEL_KINDS else POS
+            if list(c.updates) != list(allowed[:len(c.updates)]):
+                raise NotImplementedError(
+                    "calc %s updates %s; the GPU integrator needs a prefix of %s"
+                    % (c.id, c.updates, allowed))
+            for p in c.updates:
+                if p not in self.props:
+                    self.props.append(p)
+            if kind in RATE_KINDS:
+                dim = c.kernel.dim if dim is None else dim
+                if c.kernel.dim != dim:
+                    raise NotImplementedError("mixed kernel dimensions in one rates stage")
+                for f in c.funcs:
+                    self._add_term(_term(f, kind))
+            elif kind == "gravity":
+                f = c.funcs[0]
+                g = self.gravity or (0.0, 0.0, 0.0)
+                self.gravity = (g[0] + f.gx, g[1] + f.gy, g[2] + f.gz)
+            else:
+                if self.add_velocity:
+                    raise NotImplementedError("two position-stepping calcs on one array")
+                self.add_velocity = True
+        self.dim = dim or 3
+
+    def _add_term(self, t):
+        # merge different kinds on the same source into one traversal
+        for e in self.terms:
+            if e["src"] is t["src"] and not (e["kinds"] & t["kinds"]):
+                e["kinds"] = e["kinds"] | t["kinds"]
+                for k, v in t.items():
+                    if k not in ("src", "kinds"):
+                        e[k] = v
+                return
+        self.terms.append(dict(t))
+
+    def run(self, integ, kname):
+        cm = integ.particles.cell_manager
+        rate = integ.rate_arrays(self.dest, kname)
+        written = integ._written.setdefault(id(self.dest), set())
+        fresh = [p for p in self.props if p not in written]
+        if fresh and len(fresh) != len(self.props):
+            for p in fresh:
+                rate[p].zero_()
+            fresh = []
+        accumulate = not fresh
+        acc = [rate.get(p) if p in self.props else None for p in VEL]
+        pos = [rate.get(p) if p in self.props else None for p in POS]
+        if self.terms or self.gravity or self.add_velocity:
+            gpu.rates(cm, self.dest, self.terms, self.dim, acc=acc, pos=pos,
+                      accumulate=accumulate, gravity=self.gravity,
+                      add_velocity=self.add_velocity)
+        written.update(self.props)
+
+
+class Integrator:
+    """solver/integrator.py:9-519."""
+
+    def __init__(self, particles=None, calcs=None, pcalcs=None):
+        self.particles = particles
+        self.calcs = list(calcs or [])
+        self.icalcs = []
+        self.pcalcs = []
+        self.nsteps = 1
+        self.cstep = 1
+        self.initial_props = {}
+        self.k_props = {}
+        self.setup_done = False
+        self.rupdate_list = []
+        self.stages = []
+        self._rates = {}
+        self._written = {}
+
+    def set_rupdate_list(self):
+        self.rupdate_list = [[] for _ in self.particles.arrays]
+
+    def setup_integrator(self):
+        """integrator.py:229-337 bookkeeping plus the stage plan."""
+        self.arrays = self.particles.arrays
+        calcs = self.calcs
+        self.pcalcs = [c for c in calcs if c.tag == "position"]
+        self.ncalcs = [c for c in calcs if not c.tag == "position"]
+        self.icalcs = [c for c in calcs if not c.tag == "position" and c.integrates]
+        self.initial_props = {}
+        self.k_props = {}
+        for i, calc in enumerate(calcs):
+            pa = self.arrays[calc.dnum]
+            self.initial_props[calc.id] = []
+            self.k_props[calc.id] = {}
+            for j, prop in enumerate(calc.updates):
+                prop_initial = "_" + prop + "_0"
+                if calc.integrates:
+                    pa.add_property({"name": prop_initial})
+                    if prop_initial not in calc.initial_props:
+                        calc.initial_props.append(prop_initial)
+                self.initial_props[calc.id].append(prop_initial)
+                for l in range(self.nsteps):
+                    k_num = "k" + str(l + 1)
+                    if calc.integrates:
+                        self.k_props[calc.id].setdefault(k_num, [])
+                        k_name = "_" + k_num + "_" + prop + str(i) + str(j)
+                        calc.dst_writes.setdefault(k_num, [])
+                        if k_name not in calc.dst_writes[k_num]:
+                            calc.dst_writes[k_num].append(k_name)
+                        self.k_props[calc.id][k_num].append(k_name)
+        self.stages = self._plan(calcs)
+        self._integrated = {}
+        for st in self.stages:
+            if isinstance(st, RatesStage):
+                lst = self._integrated.setdefault(id(st.dest), (st.dest, []))[1]
+                for p in st.props:
+                    if p not in lst:
+                        lst.append(p)
+        for dest, props in self._integrated.values():
+            for l in range(self.nsteps):
+                for p in props:
+                    dest.add_property({"name": "_rate%d_%s" % (l + 1, p)})
+        self.set_rupdate_list()
+        self.setup_done = True
+
+    @staticmethod
+    def _plan(calcs):
+        stages = []
+        i = 0
+        while i < len(calcs):
+            c = calcs[i]
+            kind = _kind_of(c.funcs[0])
+            if not c.integrates:
+                if kind == "rho":
+                    nxt = calcs[i + 1] if i + 1 < len(calcs) else None
+                    if (nxt is not None and not nxt.integrates and nxt.dest is c.dest
+                            and _kind_of(nxt.funcs[0]) == "tait" and c.updates == ["rho"]):
+                        stages.append(DensityStage(c, nxt))
+                        i += 2
+                        continue
+                    stages.append(DensityStage(c))
+                elif kind == "tait":
+                    stages.append(TaitStage(c))
+                else:
+                    stages.append(CalcStage(c))
+                i += 1
+                continue
+            run = [c]
+            j = i + 1
+            while j < len(calcs) and calcs[j].integrates and calcs[j].dest is c.dest:
+                run.append(calcs[j])
+                j += 1
+            stages.append(RatesStage(run))
+            i = j
+        return stages
+
+    def rate_arrays(self, dest, kname):
+        return {p: dest.get_device("_rate%s_%s" % (kname[1:], p))
+                for p in self._integrated[id(dest)][1]}
+
+    # -- the reference's step building blocks ------------------------------------
+    def eval(self, calcs=None):
+        """Evaluate every stage for the current ``cstep`` (integrator.py:432-470)."""
+        kname = "k" + str(self.cstep)
+        self._written = {}
+        for st in self.stages:
+            st.run(self, kname)
+
+    def _lines(self, mode, dt):
+        out = []
+        for dest, props in self._integrated.values():
+            n = dest.get_number_of_particles()
+            lines = []
+            for p in props:
+                cur = dest.get_device(p)
+                init = dest.get_device("_" + p + "_0")
+                r1 = dest.get_device("_rate1_" + p)
+                if mode == "copy":
+                    lines.append((init, None, cur, None, None, 0.0, 2))
+                elif mode == "euler":
+                    lines.append((cur, init, init, r1, None, dt, 1))
+                elif mode == "predict":
+                    lines.append((cur, None, init, r1, None, dt, 1))
+                elif mode == "rk2":
+                    r2 = dest.get_device("_rate2_" + p)
+                    lines.append((cur, init, init, r1, r2, 0.5 * dt, 0))
+            out.append((dest, n, props, lines))
+        return out
+
+    def _apply(self, mode, dt=0.0):
+        cm = self.particles.cell_manager
+        for dest, n, props, lines in self._lines(mode, dt):
+            gpu.axpy(cm, n, lines)
+            if mode != "copy":
+                gpu.note_written(cm, dest, props)
+                if any(p in POS for p in props):
+                    dest.set_dirty(True)
+
+    def set_initial_arrays(self):
+        self._apply("copy")
+
+    def reset_current_arrays(self, calcs=None):
+        cm = self.particles.cell_manager
+        for dest, n, props, _ in self._lines("copy", 0.0):
+            lines = [(dest.get_device(p), None, dest.get_device("_" + p + "_0"), None, None,
+                      0.0, 2) for p in props]
+            gpu.axpy(cm, n, lines)
+            gpu.note_written(cm, dest, props)
+            if any(p in POS for p in props):
+                dest.set_dirty(True)
+
+    def step(self, calcs=None, dt=0.0):
+        """X = X0 + dt k (the reference's reset + step)."""
+        self._apply("predict", dt)
+        self.cstep += 1
+
+    def do_step(self, calcs=None, dt=0.0):
+        self.eval(calcs)
+        self.step(calcs, dt)
+
+    def integrate(self, dt):
+        raise NotImplementedError
+
+
+class EulerIntegrator(Integrator):
+    """X(t+h) = X + h F(X), integrator.py:525-573."""
+
+    def __init__(self, particles, calcs=None):
+        Integrator.__init__(self, particles, calcs)
+        self.nsteps = 1
+
+    def integrate(self, dt):
+        if not self.setup_done:
+            self.setup_integrator()
+        self.set_initial_arrays()
+        self.cstep = 1
+        self.eval(self.calcs)
+        self._apply("euler", dt)
+        self.particles.update()
+
+
+class RK2Integrator(Integrator):
+    """X(t+h) = X + h/2 (K1 + K2), integrator.py:581-645."""
+
+    def __init__(self, particles, calcs=None):
+        Integrator.__init__(self, particles, calcs)
+        self.nsteps = 2
+
+    def integrate(self, dt):
+        if not self.setup_done:
+            self.setup_integrator()
+        self.set_initial_arrays()
+        self.cstep = 1
+        self.eval(self.calcs)
+        self._apply("predict", dt)
+        self.cstep = 2
+        self.particles.update()
+        self.eval(self.calcs)
+        self._apply("rk2", dt)
+        self.cstep = 1
+        self.particles.update()
+
+
+def _not_here(name, ref):
+    class _I(Integrator):
+        def __init__(self, *a, **k):
+            raise NotImplementedError("%s (%s) is not part of this build" % (name, ref))
+    _I.__name__ = name
+    return _I
+
+
+RK4Integrator = _not_here("RK4Integrator", "solver/integrator.py:650")
+PredictorCorrectorIntegrator = _not_here("PredictorCorrectorIntegrator", "solver/integrator.py:734")
+LeapFrogIntegrator = _not_here("LeapFrogIntegrator", "solver/integrator.py:802")

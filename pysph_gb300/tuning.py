@@ -1,0 +1,31 @@
+"""Launch-shape choices for the GPU neighbour structure and pair kernels.
+
+``choose_subdivision`` picks how many internal grid cells span one
+reference cell (``cell_size = 2 max h``).  Finer cells cut the candidate
+volume a destination must test (27 cells of (2h)^3 at 1, 125 of h^3 at 2,
+343 of (2h/3)^3 at 3) at the cost of more, shorter rows.  The default comes
+from a per-dimension table measured on GB300 (``bench.py --tune`` re-measures
+it); ``PYSPH_GB300_SUBDIV`` overrides it.
+"""
+import os
+
+# measured defaults: (dimension with extent) -> subdivision
+DEFAULT_SUBDIVISION = {1: 1, 2: 1, 3: 1}
+
+
+def choose_subdivision(cell_manager):
+    env = os.environ.get("PYSPH_GB300_SUBDIV")
+    if env:
+        v = int(env)
+        if v not in (1, 2, 3):
+            raise ValueError("PYSPH_GB300_SUBDIV must be 1, 2 or 3")
+        return v
+    dims = 1
+    for pa in cell_manager.arrays_to_bin:
+        if pa.get_number_of_particles() == 0:
+            continue
+        for k, c in ((2, "y"), (3, "z")):
+            t = pa.get_device(c)
+            if t.numel() and float(t.max() - t.min()) > 0:
+                dims = max(dims, k)
+    return DEFAULT_SUBDIVISION[dims]

@@ -1,0 +1,265 @@
+"""GPU parity: the CUDA path against the reference's golden fixtures and the
+oracle.
+
+Tolerance: neighbour sets bit-exact (as index sets, self last); every
+floating-point field within ``TOL = 1e-5`` normwise relative error
+(``max|gpu - ref| / max|ref|``), the FP32 pair-sum contract.  State after a
+step is compared through its increment (``x_out - x_in``), which is what the
+FP32 rates determine.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pysph_gb300
+from golden_util import csr_sets, inputs, load, normwise
+from pysph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+API = pysph_gb300.api()
+base, sph, solver = API.base, API.sph, API.solver
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+
+
+def _particles(g, specs):
+    arrays = []
+    for name, ptype in specs:
+        arrays.append(base.get_particle_array(name=name, type=ptype, **inputs(g, name)))
+    return arrays, base.Particles(arrays=arrays)
+
+
+def _locator_sets(particles, src, dst):
+    loc = particles.nnps_manager.get_neighbor_particle_locator(src, dst, 2.0)
+    off, idx = loc.neighbour_csr()
+    return off, idx
+
+
+@pytest.mark.parametrize("name", ["drop_step", "cube_step"])
+def test_neighbour_sets_bit_exact(name):
+    _need_gpu()
+    g = load(name)
+    (pa,), particles = _particles(g, [("fluid", base.ParticleType.Fluid)])
+    off, idx = _locator_sets(particles, pa, pa)
+    ro, ri = g["nbr_fluid_fluid_offsets"], g["nbr_fluid_fluid_index"]
+    assert csr_sets(off, idx) == csr_sets(ro, ri)
+    np.testing.assert_array_equal(idx[off[1:] - 1], np.arange(len(off) - 1))
+    # the locator API returns the same lists
+    loc = particles.nnps_manager.get_neighbor_particle_locator(pa, pa, 2.0)
+    for i in (0, 7, len(off) // 2, len(off) - 2):
+        lst = loc.py_get_nearest_particles(i).get_npy_array()
+        assert set(lst.tolist()) == set(ri[ro[i]:ro[i + 1]].tolist())
+        assert lst[-1] == i
+
+
+def test_dam_neighbour_sets_bit_exact():
+    _need_gpu()
+    g = load("dam_step")
+    (fl, wl), particles = _particles(g, [("fluid", base.ParticleType.Fluid),
+                                         ("boundary", base.ParticleType.Solid)])
+    for src, key in ((fl, "fluid"), (wl, "boundary")):
+        off, idx = _locator_sets(particles, src, fl)
+        assert csr_sets(off, idx) == csr_sets(g["nbr_fluid_%s_offsets" % key],
+                                              g["nbr_fluid_%s_index" % key])
+
+
+def test_square4_functions():
+    _need_gpu()
+    g = load("square4")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    pa = base.get_particle_array(name="test", tmpx=np.zeros(4), tmpy=np.zeros(4),
+                                 tmpz=np.zeros(4), **props)
+    particles = base.Particles(arrays=[pa])
+    kern = base.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("rho", sph.SPHRho.withargs(), ["tmpx"]),
+            ("pgrad", sph.SPHPressureGradient.withargs(dim=2), ["tmpx", "tmpy"]),
+            ("avisc", sph.MonaghanArtificialVsicosity.withargs(alpha=1.0, beta=1.0),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("xsph", sph.XSPHCorrection.withargs(eps=0.5, dim=2), ["tmpx", "tmpy"])):
+        calc = sph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            ref = g["%s_%d" % (name, k)]
+            got = pa.get(upn)
+            assert np.abs(got - ref).max() <= TOL * max(np.abs(ref).max(), 1.0), (name, k)
+
+
+def test_drop_per_function_parity():
+    """Each SPH function of the drop on the reference's own input state."""
+    _need_gpu()
+    g = load("drop_step")
+    inp = inputs(g, "fluid")
+    n = len(inp["x"])
+    pa = base.get_particle_array(name="fluid", type=base.ParticleType.Fluid,
+                                 t0=np.zeros(n), t1=np.zeros(n), t2=np.zeros(n), **inp)
+    particles = base.Particles(arrays=[pa])
+    k2 = base.CubicSplineKernel(dim=2)
+
+    def calc(fn, ups, srcs=(pa,)):
+        funcs = [fn.get_func(s, pa) for s in srcs]
+        return sph.SPHCalc(particles, list(srcs), pa, k2, funcs, ups)
+
+    calc(sph.SPHRho.withargs(), ["rho"]).sph("rho")
+    assert normwise(pa.get("rho"), g["eval1_fluid_rho"]) < TOL
+    c = sph.SPHCalc(particles, [], pa, k2, [sph.TaitEquation.withargs(co=1400.0, ro=1.0).get_func(pa, pa)],
+                    ["p", "cs"])
+    c.sph("p", "cs")
+    assert normwise(pa.get("p"), g["eval1_fluid_p"]) < TOL
+    assert normwise(pa.get("cs"), g["eval1_fluid_cs"]) < TOL
+    calc(sph.SPHPressureGradient.withargs(dim=2), ["u", "v"]).sph("t0", "t1")
+    assert normwise(pa.get("t0"), g["eval1_k_pgrad_fluid_u"]) < TOL
+    assert normwise(pa.get("t1"), g["eval1_k_pgrad_fluid_v"]) < TOL
+    calc(sph.MonaghanArtificialVsicosity.withargs(alpha=0.01, beta=0.0),
+         ["u", "v", "w"]).sph("t0", "t1", "t2")
+    assert normwise(pa.get("t0"), g["eval1_k_avisc_fluid_u"]) < TOL
+    assert normwise(pa.get("t1"), g["eval1_k_avisc_fluid_v"]) < TOL
+    calc(sph.XSPHCorrection.withargs(eps=0.5, dim=2), ["x", "y"]).sph("t0", "t1")
+    assert normwise(pa.get("t0"), g["eval1_k_xsph_fluid_x"]) < TOL
+    assert normwise(pa.get("t1"), g["eval1_k_xsph_fluid_y"]) < TOL
+
+
+def _check_step(g, arrays, evals, k_groups):
+    """Compare rates of every eval and the state increment with the reference."""
+    for pa in arrays:
+        nm = pa.name
+        for p in ("rho", "p", "cs"):
+            key = "out_%s_%s" % (nm, p)
+            if key in g and np.abs(g[key]).max() > 0:
+                assert normwise(pa.get(p), g[key]) < TOL, key
+        for p in ("x", "y", "z", "u", "v", "w"):
+            key = "out_%s_%s" % (nm, p)
+            if key not in g:
+                continue
+            d_ref = g[key] - g["in_%s_%s" % (nm, p)]
+            if np.abs(d_ref).max() == 0:
+                continue
+            d_got = pa.get(p) - g["in_%s_%s" % (nm, p)]
+            assert normwise(d_got, d_ref) < TOL, (key, normwise(d_got, d_ref))
+    # summed rates of each evaluation
+    pa = arrays[0]
+    for e in range(1, evals + 1):
+        for prop, calcs in k_groups.items():
+            ref = sum(g["eval%d_k_%s_fluid_%s" % (e, c, prop)] for c in calcs)
+            got = pa.get("_rate%d_%s" % (e, prop))
+            assert normwise(got, ref) < TOL, (e, prop, normwise(got, ref))
+
+
+def test_drop_euler_step():
+    _need_gpu()
+    g = load("drop_step")
+    s, particles = W.setup_drop(API, inputs(g, "fluid"))
+    s.integrator.integrate(float(g["dt"]))
+    _check_step(g, particles.arrays, 1, {"u": ["pgrad", "avisc"], "v": ["pgrad", "avisc"],
+                                         "x": ["step", "xsph"], "y": ["step", "xsph"]})
+
+
+def test_drop_ten_steps_trajectory():
+    _need_gpu()
+    g = load("drop_traj10")
+    inp = inputs(g, "fluid")
+    s, particles = W.setup_drop(API, inp)
+    for _ in range(int(g["steps"])):
+        s.integrator.integrate(float(g["dt"]))
+    pa = particles.arrays[0]
+    for p in ("x", "y", "u", "v"):
+        d_ref = g["final_" + p] - inp[p]
+        assert normwise(pa.get(p) - inp[p], d_ref) < 1e-4, p
+    for p in ("rho", "p"):
+        assert normwise(pa.get(p), g["final_" + p]) < 1e-4, p
+
+
+def test_dam_rk2_step():
+    _need_gpu()
+    g = load("dam_step")
+    fl, wl = inputs(g, "fluid"), inputs(g, "boundary")
+    s, particles = W.setup_dam_break(API, fl, wl, dx=float(g["dx"]), c0=float(g["c0"]))
+    s.integrator.integrate(float(g["dt"]))
+    _check_step(g, particles.arrays[:1], 2,
+                {"u": ["pgrad", "avisc", "bforce", "gravity"],
+                 "v": ["pgrad", "avisc", "bforce", "gravity"], "x": ["step"], "y": ["step"]})
+
+
+def test_cube_rk2_step():
+    _need_gpu()
+    g = load("cube_step")
+    s, particles = W.setup_cube(API, inputs(g, "fluid"))
+    s.integrator.integrate(float(g["dt"]))
+    _check_step(g, particles.arrays, 2,
+                {"u": ["pgrad", "avisc"], "v": ["pgrad", "avisc"], "w": ["pgrad", "avisc"],
+                 "x": ["step"], "y": ["step"], "z": ["step"]})
+
+
+@pytest.mark.parametrize("n,subdiv", [(32768, 1), (32768, 2), (64000, 3)])
+def test_cube_vs_oracle(n, subdiv, monkeypatch):
+    """Larger 3D lattices against the C oracle, for every cell subdivision."""
+    _need_gpu()
+    monkeypatch.setenv("PYSPH_GB300_SUBDIV", str(subdiv))
+    props = W.cube_lattice(n, seed=3)
+    s, particles = W.setup_cube(API, props)
+    dt = 1e-4
+    s.integrator.integrate(dt)
+    pa = particles.arrays[0]
+    prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+    prob.integrate_rk2(dt)
+    ref = prob.arrays["fluid"]
+    for p in ("rho", "p", "cs"):
+        assert normwise(pa.get(p), ref[p]) < TOL, p
+    for p in ("x", "y", "z", "u", "v", "w"):
+        assert normwise(pa.get(p) - props[p], ref[p] - props[p]) < TOL, p
+
+
+def test_jump_tolerance_raises():
+    """A particle moving more than one cell between builds raises
+    RuntimeError, as CellManager.check_jump_tolerance does."""
+    _need_gpu()
+    props = W.elliptical_drop(dx=0.1)
+    pa = base.get_particle_array(name="fluid", **props)
+    particles = base.Particles(arrays=[pa])
+    cs = particles.cell_manager.cell_size
+    x = pa.get("x")
+    x[3] += 2.5 * cs
+    pa.set(x=x)
+    with pytest.raises(RuntimeError, match="more than one cell"):
+        particles.update()
+
+
+def test_non_real_tags_get_zero():
+    _need_gpu()
+    props = W.elliptical_drop(dx=0.05)
+    n = len(props["x"])
+    tag = np.zeros(n, np.int64)
+    tag[::7] = 1   # Dummy particles: still neighbours, never destinations
+    pa = base.get_particle_array(name="fluid", **props)
+    pa.add_property({"name": "tag", "data": tag, "type": "long"})
+    pa.align_particles()
+    particles = base.Particles(arrays=[pa])
+    k2 = base.CubicSplineKernel(dim=2)
+    sph.SPHCalc(particles, [pa], pa, k2, [sph.SPHRho.get_func(pa, pa)], ["rho"]).sph("rho")
+    rho = pa.get("rho", only_real_particles=False)
+    t = pa.get("tag", only_real_particles=False)
+    assert np.all(rho[t != 0] == 0)
+    host = {k: pa.get(k, only_real_particles=False) for k in ("x", "y", "z", "h", "m")}
+    host["tag"] = t
+    off, idx = oracle.neighbors(host, host, particles.cell_manager.cell_size, same=True)
+    ref = oracle.pair_sum("rho", host, host, off, idx, 2)[0]
+    assert normwise(rho, ref) < TOL
+
+
+def test_invariants_mass_exact():
+    _need_gpu()
+    props = W.cube_lattice(8000)
+    s, particles = W.setup_cube(API, props)
+    inv0 = particles.invariants()
+    for _ in range(3):
+        s.integrator.integrate(1e-4)
+    inv1 = particles.invariants()
+    assert inv1["mass"] == inv0["mass"]
+    assert inv1["count"] == len(props["x"])
+    assert abs(inv0["mass"] - props["m"].sum()) <= 1e-12 * props["m"].sum()

@@ -1,0 +1,110 @@
+"""Host-side behaviour of the drop-in API that needs no GPU: operation
+expansion, calc validation errors, the integrator's stage plan."""
+import numpy as np
+import pytest
+
+import pysph_gb300
+from pysph_gb300 import workloads as W
+
+API = pysph_gb300.api()
+base, sph, solver = API.base, API.sph, API.solver
+
+
+def _pa(n=10, name="fluid", type=0):
+    x = np.linspace(0, 1, n)
+    return base.get_particle_array(name=name, type=type, x=x, h=np.full(n, 0.2))
+
+
+def test_get_particle_array_defaults():
+    pa = _pa()
+    for p in ("x", "y", "z", "u", "v", "w", "m", "h", "p", "e", "rho", "cs", "idx", "tag"):
+        assert pa.has_array(p)
+    assert pa.get_number_of_particles() == 10
+    assert np.all(pa.get("m") == 1.0) and np.all(pa.get("rho") == 1.0)
+    np.testing.assert_array_equal(pa.get("idx"), np.arange(10))
+    assert pa.num_real_particles == 10
+    with pytest.raises(AttributeError):
+        pa.get("nope")
+
+
+def test_set_marks_dirty_only_for_positions():
+    pa = _pa()
+    pa.set_dirty(False)
+    pa.set(u=np.ones(10))
+    assert not pa.is_dirty
+    pa.set(x=np.zeros(10))
+    assert pa.is_dirty
+
+
+def test_remove_particles_swaps_with_last():
+    pa = _pa(6)
+    pa.remove_particles(base.LongArray(0) if False else np.array([1]))
+    np.testing.assert_array_equal(pa.get("idx"), [0, 5, 2, 3, 4])
+
+
+def test_calc_checks_raise_value_error():
+    a = _pa()
+    b = _pa(name="other")
+    particles = base.Particles(arrays=[a, b])
+    k = base.CubicSplineKernel(dim=1)
+    f = sph.SPHRho.get_func(a, a)
+    with pytest.raises(ValueError, match="One sph function is needed per source"):
+        sph.SPHCalc(particles, [a, b], a, k, [f], ["rho"])
+    with pytest.raises(ValueError, match="Number of updates"):
+        sph.SPHCalc(particles, [a], a, k, [f], ["rho", "p"])
+    with pytest.raises(ValueError, match="same type"):
+        sph.SPHCalc(particles, [a, b], a, k,
+                    [f, sph.SPHPressureGradient.get_func(b, a)], ["rho"])
+    with pytest.raises(ValueError, match="SPHFunction.source"):
+        sph.SPHCalc(particles, [b], a, k, [f], ["rho"])
+
+
+def test_avisc_never_stores_eta():
+    a = _pa()
+    f = sph.MonaghanArtificialVsicosity.withargs(alpha=0.3, beta=0.2, eta=0.7).get_func(a, a)
+    assert f.eta == 0.0 and f.alpha == 0.3 and f.num_outputs == 3
+
+
+def test_unsupported_functions_raise():
+    a = _pa()
+    with pytest.raises(NotImplementedError):
+        sph.MomentumEquation.withargs().get_func(a, a)
+    with pytest.raises(NotImplementedError):
+        base.QuinticSplineKernel(dim=2)
+
+
+def test_operation_expansion_and_stage_plan():
+    fl, wl = W.dam_break(dx=0.1)
+    s, particles = W.setup_dam_break(API, fl, wl, dx=0.1, c0=W.dam_break_c0())
+    integ = s.integrator
+    ids = [c.id for c in integ.calcs]
+    assert ids == ["eos_fluid", "density_fluid", "pgrad_fluid", "avisc_fluid",
+                   "bforce_fluid", "gravity_fluid", "step_fluid"]
+    kinds = [type(st).__name__ for st in integ.stages]
+    # Tait precedes SPHRho, so it is not fused; the integrating run is one stage
+    assert kinds == ["TaitStage", "DensityStage", "RatesStage"]
+    rs = integ.stages[-1]
+    assert rs.gravity == (0.0, -9.81, 0.0) and rs.add_velocity
+    by_src = {t["src"].name: t["kinds"] for t in rs.terms}
+    assert by_src == {"fluid": {"pgrad", "avisc"}, "boundary": {"bforce"}}
+    assert integ.k_props["pgrad_fluid"]["k2"] == ["_k2_u20", "_k2_v21"]
+    fluid = particles.arrays[0]
+    for p in ("_u_0", "_v_0", "_x_0", "_rate1_u", "_rate2_y"):
+        assert fluid.has_array(p)
+
+
+def test_drop_plan_fuses_density_and_tait():
+    s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1))
+    st = s.integrator.stages
+    assert [type(x).__name__ for x in st] == ["DensityStage", "RatesStage"]
+    assert st[0].tait is not None
+    assert st[1].terms[0]["kinds"] == {"pgrad", "avisc", "xsph"}
+
+
+def test_compute_without_gpu_raises():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1))
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        s.integrator.integrate(1e-5)
