@@ -118,6 +118,8 @@ int sph_ctx_destroy(sph_ctx *ctx);
 int sph_ctx_set_stream(sph_ctx *ctx, void *cuda_stream);
 int sph_last_error(char *buf, size_t len);
 int sph_version(void);
+/* Number of kernels this library has launched in the process (diagnostic). */
+int sph_launch_count(int64_t *out);
 
 /* Neighbour structure for all arrays of one Particles collection.  Bins
  * every array on a dense grid of cells of size cell_size/subdiv (subdiv in

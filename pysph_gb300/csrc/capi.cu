@@ -2,6 +2,7 @@
 // error reporting around the kernels of nnps.cu, pairs.cu and elementwise.cu.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <new>
 #include <string>
@@ -11,6 +12,9 @@
 namespace sphgb {
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int set_error(int code, const std::string &msg) {
     g_last_error = msg;
@@ -49,6 +53,12 @@ using namespace sphgb;
 extern "C" {
 
 int sph_version(void) { return 1; }
+
+int sph_launch_count(int64_t *out) {
+    if (!out) return set_error(SPH_ERR_ARG, "sph_launch_count: null out");
+    *out = (int64_t)g_launches.load(std::memory_order_relaxed);
+    return SPH_OK;
+}
 
 int sph_last_error(char *buf, size_t len) {
     if (!buf || len == 0) return SPH_ERR_ARG;
@@ -197,6 +207,7 @@ int sph_mean_neighbours(sph_ctx *c, int dst, int src, double *out) {
     unsigned long long *acc = (unsigned long long *)(c->d_part);
     SPH_CUDA(cudaMemsetAsync(acc, 0, sizeof(unsigned long long), c->stream));
     k_sum_i64<<<grid_blocks(n, 256, 2), 256, 0, c->stream>>>(c->d_cnt, n, acc);
+    count_launch();
     SPH_LAUNCH_CHECK("k_sum_i64");
     unsigned long long h = 0;
     SPH_CUDA(cudaMemcpyAsync(&h, acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream));

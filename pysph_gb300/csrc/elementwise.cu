@@ -130,6 +130,7 @@ int launch_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, 
     if (n == 0) return SPH_OK;
     k_tait<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, rho, tag, (float)co, (float)ro,
                                                                   (float)gamma, p, cs);
+    count_launch();
     SPH_LAUNCH_CHECK("k_tait");
     return SPH_OK;
 }
@@ -150,6 +151,7 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
     a.vel[0] = u; a.vel[1] = v; a.vel[2] = w;
     if (n == 0) return SPH_OK;
     k_const<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, tag, a);
+    count_launch();
     SPH_LAUNCH_CHECK("k_const");
     return SPH_OK;
 }
@@ -166,6 +168,7 @@ int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nl
     }
     if (n == 0 || nlines == 0) return SPH_OK;
     k_axpy<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, a);
+    count_launch();
     SPH_LAUNCH_CHECK("k_axpy");
     return SPH_OK;
 }
@@ -175,9 +178,11 @@ int invariants(sph_ctx *ctx, const sph_array_view *a, double *out) {
     SPH_CUDA(cudaMemsetAsync(ctx->d_part, 0, sizeof(double) * (kRedBlocks * 6 + 8), ctx->stream));
     if (a->n > 0) {
         k_invariants<<<kRedBlocks, kThreads, 0, ctx->stream>>>(*a, ctx->d_part);
-        SPH_LAUNCH_CHECK("k_invariants");
+        count_launch();
+    SPH_LAUNCH_CHECK("k_invariants");
     }
     k_invariants_final<<<1, 32, 0, ctx->stream>>>(ctx->d_part, kRedBlocks, ctx->d_part + kRedBlocks * 6);
+    count_launch();
     SPH_LAUNCH_CHECK("k_invariants_final");
     SPH_CUDA(cudaMemcpyAsync(ctx->h_red, ctx->d_part + kRedBlocks * 6, 6 * sizeof(double),
                              cudaMemcpyDeviceToHost, ctx->stream));

@@ -322,6 +322,7 @@ int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
     k_scan_tiles<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
     k_scan_totals<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, ntiles);
     k_scan_add<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    count_launch(3);
     SPH_LAUNCH_CHECK("scan");
     return SPH_OK;
 }
@@ -381,6 +382,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     const double inv_cs_ref = 1.0 / cell_size;
 
     k_box_init<<<1, 32, 0, st>>>(ctx->d_box, ctx->d_hmax);
+    count_launch();
     SPH_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), st));
     for (int a = 0; a < narrays; ++a) {
         ArraySnap &A = ctx->arrays[a];
@@ -399,6 +401,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         int jb = (check_jump && same_layout) ? 1 : 0;
         k_box<<<grid_blocks(v.n, kThreads, 2), kThreads, 0, st>>>(v, inv_cs, inv_cs_ref, A.refcell, jb,
                                                                ctx->d_box, ctx->d_hmax, ctx->d_err);
+        count_launch();
         SPH_LAUNCH_CHECK("k_box");
     }
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box, ctx->d_box, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -467,6 +470,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         if (v.n > 0) {
             int nb = grid_blocks(v.n, kThreads);
             k_keys<<<nb, kThreads, 0, st>>>(v, g, A.key, A.cstart);
+            count_launch();
             SPH_LAUNCH_CHECK("k_keys");
         }
         rc = scan_exclusive(ctx, A.cstart, g.ncells + 1);
@@ -480,6 +484,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
             k_reorder<<<nb, kThreads, 0, st>>>(v, g, A.perm, A.key, A.skey, A.posm, A.velh, A.st,
                                                A.has_nrm ? A.nrm : nullptr,
                                                A.has_nrm ? A.tan : nullptr);
+            count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
         }
     }
@@ -502,6 +507,7 @@ int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
     k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
         A.view, ctx->grid, A.perm, A.key, A.skey, A.posm, A.velh, A.st, nrm ? A.nrm : nullptr,
         nrm ? A.tan : nullptr);
+    count_launch();
     SPH_LAUNCH_CHECK("k_reorder (refresh)");
     return SPH_OK;
 }
@@ -518,6 +524,7 @@ int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *cou
     k_nbr<false><<<grid_blocks(D.n, 128), 128, 0, ctx->stream>>>(
         D.view, S.view, ctx->grid, D.key, S.cstart, S.perm, radius_scale, dst == src,
         counts, nullptr, nullptr);
+    count_launch();
     SPH_LAUNCH_CHECK("k_nbr count");
     return SPH_OK;
 }
@@ -535,6 +542,7 @@ int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t
     k_nbr<true><<<grid_blocks(D.n, 128), 128, 0, ctx->stream>>>(
         D.view, S.view, ctx->grid, D.key, S.cstart, S.perm, radius_scale, dst == src,
         nullptr, offsets, index);
+    count_launch();
     SPH_LAUNCH_CHECK("k_nbr fill");
     return SPH_OK;
 }

@@ -346,6 +346,7 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     else if (kx == 2) { if (lpd == 32) DISPATCH(2, 32); else if (lpd == 16) DISPATCH(2, 16); else DISPATCH(2, 8); }
     else { if (lpd == 32) DISPATCH(3, 32); else if (lpd == 16) DISPATCH(3, 16); else DISPATCH(3, 8); }
 #undef DISPATCH
+    count_launch();
     SPH_LAUNCH_CHECK("k_density");
     return SPH_OK;
 }
@@ -393,6 +394,7 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
     else if (kx == 2) { if (lpd == 32) DISPATCH(2, 32); else if (lpd == 16) DISPATCH(2, 16); else DISPATCH(2, 8); }
     else { if (lpd == 32) DISPATCH(3, 32); else if (lpd == 16) DISPATCH(3, 16); else DISPATCH(3, 8); }
 #undef DISPATCH
+    count_launch();
     SPH_LAUNCH_CHECK("k_rates");
     return SPH_OK;
 }

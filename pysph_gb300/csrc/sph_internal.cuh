@@ -96,6 +96,9 @@ int cuda_check(cudaError_t e, const char *what);
 
 int grid_blocks(int64_t n, int threads, int per_sm = 8);
 
+// kernels launched by this library (diagnostic counter, sph_launch_count)
+void count_launch(int n = 1);
+
 // launchers implemented in the .cu files
 int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
                double radius_scale, int subdiv, int check_jump);

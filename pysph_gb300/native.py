@@ -35,6 +35,7 @@ EXPORTS = (
     "sph_version", "sph_nnps_build", "sph_nnps_count", "sph_nnps_fill",
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
+    "sph_launch_count",
 )
 
 
@@ -113,6 +114,7 @@ def load_library(build_if_missing=True):
         L.sph_invariants.argtypes = [vp, P(ArrayView), P(d)]
         L.sph_error_word.argtypes = [vp, P(ctypes.c_uint32)]
         L.sph_mean_neighbours.argtypes = [vp, i32, i32, P(d)]
+        L.sph_launch_count.argtypes = [P(i64)]
         for name in EXPORTS:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
@@ -151,6 +153,13 @@ def check(rc, what=""):
     if exc is not None:
         raise exc(msg)
     raise NativeError(rc, msg)
+
+
+def launch_count():
+    """Kernels launched by the library so far in this process."""
+    out = ctypes.c_int64()
+    check(load_library(False).sph_launch_count(ctypes.byref(out)), "launch count")
+    return out.value
 
 
 def ptr(t):
