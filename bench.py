@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Throughput of the SPH particle step on GB300.
+
+Workload: the 3D throughput configuration at 1,000,000 particles -- a
+jittered 100^3 lattice filling the unit cube (+-0.1 dx uniform jitter,
+seeded), h = 1.2 dx, velocities N(0, 0.01^2), rho0 = 1, Tait c0 = 1,
+Monaghan alpha = 0.1; one step = NNPS + SPHRho + Tait + pressure gradient
++ artificial viscosity + RK2 (two evaluations).  Inputs are synthetic.
+
+Metric: pair interactions per second = 4 * K * N / step time (K = mean
+neighbour count including self; 2 pair passes x 2 evaluations per RK2 step),
+summed over all GPUs (independent replicas, weak scaling).
+
+``value`` is timed on the device with CUDA events around each step (inputs
+resident in HBM; L2 flushed between steps outside the timed events).
+``e2e`` is the same metric through the public API with host buffers: every
+step uploads the particle state from pinned host memory (``ParticleArray.set``),
+integrates, and reads the new state back (``ParticleArray.get``).
+
+``--impl reference`` times the reference PySPH's own Cython path (built by
+``oracle/build_ref.py`` into ``oracle/_ref``) on the host cores instead: one
+single-threaded process per core, each stepping a bounded sample of the same
+workload (a 32^3 lattice with the same spacing ratio).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "pair interactions/s (3D SPH RK2 step, NNPS+SPHRho+Tait+PGrad+AV)"
+UNIT = "pair-interactions/s"
+DT = 1e-4
+
+# Algorithmic bytes per particle per launch (FP32 snapshot reads + FP64
+# outputs the interface requires; neighbour re-reads excluded):
+#   rates:   posm+velh+st 48 B read, FP64 velocity 24 B read (position
+#            stepping), FP64 rates 48 B written                    = 120 B
+#   density: posm+velh 32 B read, FP64 rho,p,cs 24 B + st 16 B written = 72 B
+ALG_BYTES = {"RatesStage": 120.0, "DensityStage": 72.0}
+# Survey algorithmic bytes of a whole RK2 step per particle (3D)
+STEP_ALG_BYTES = 694.0
+# FLOPs per neighbour pair: density 24, momentum 72 (FMA = 2)
+PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0}
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's own Cython path (or the oracle port)
+# ---------------------------------------------------------------------------
+SAMPLE_N = 32768
+
+
+def _reference_api():
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref", "src"))
+    import types
+    import pysph.base.api as rbase  # noqa: F401
+    import pysph.sph.api as rsph
+    import pysph.solver.api as rsolver
+    return types.SimpleNamespace(base=rbase, sph=rsph, solver=rsolver)
+
+
+def reference_available():
+    try:
+        import sysconfig
+        ext = sysconfig.get_config_var("EXT_SUFFIX")
+        return os.path.exists(os.path.join(ROOT, "oracle", "_ref", "src", "pysph", "sph",
+                                           "sph_calc" + ext))
+    except Exception:
+        return False
+
+
+def _cpu_worker(args):
+    """Time ``steps`` RK2 steps of the sample after ``warmup`` (one process)."""
+    kind, n, warmup, steps, seed = args
+    import numpy as np
+
+    from pysph_gb300 import workloads as W
+    props = W.cube_lattice(n, seed=seed)
+    import oracle
+    off, _ = oracle.neighbors(props, props, 2.0 * props["h"].max(), same=True)
+    kbar = float(np.diff(off).mean())
+    if kind == "reference":
+        import io
+        import contextlib
+        api = _reference_api()
+        with contextlib.redirect_stdout(io.StringIO()):
+            s, particles = W.setup_cube(api, props)
+        step = lambda: s.integrator.integrate(DT)  # noqa: E731
+    else:
+        prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+        step = lambda: prob.integrate_rk2(DT)  # noqa: E731
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    return {"pairs": 4.0 * kbar * n * steps, "seconds": dt, "kbar": kbar}
+
+
+def cpu_baseline(procs, warmup, steps, n=SAMPLE_N):
+    kind = "reference" if reference_available() else "port"
+    import multiprocessing as mp
+    jobs = [(kind, n, warmup, steps, 100 + i) for i in range(procs)]
+    if procs == 1:
+        res = [_cpu_worker(jobs[0])]
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(procs) as pool:
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, jobs)
+            wall = time.perf_counter() - t0
+    total_pairs = sum(r["pairs"] for r in res)
+    if procs == 1:
+        value = total_pairs / res[0]["seconds"]
+    else:
+        # aggregate over concurrently running processes: slowest one bounds it
+        value = total_pairs / max(r["seconds"] for r in res)
+    cores = procs
+    if kind == "port":
+        import oracle
+        cores = procs * oracle.num_threads()
+    return {
+        "value": value, "unit": UNIT, "cores": cores, "kind": kind,
+        "sample": "%d independent %s processes, each %d RK2 steps of a %d-particle "
+                  "jittered lattice (h=1.2dx, same physics), after %d warm-up steps; "
+                  "mean neighbours %.1f" % (procs, "reference PySPH Cython" if kind == "reference"
+                                            else "oracle C port", steps, n, warmup,
+                                            statistics.mean(r["kbar"] for r in res)),
+    }
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_gpu(args):
+    import torch
+
+    import pysph_gb300
+    from pysph_gb300 import native
+    from pysph_gb300 import workloads as W
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+        pg = dist
+
+    api = pysph_gb300.api()
+    props = W.cube_lattice(args.n, seed=rank)
+    n = len(props["x"])
+    s, particles = W.setup_cube(api, props)
+    integ = s.integrator
+    for _ in range(args.warmup):
+        integ.integrate(DT)
+    torch.cuda.synchronize()
+
+    cm = particles.cell_manager
+    import ctypes
+    kb = ctypes.c_double()
+    native.check(native.lib().sph_mean_neighbours(cm.context(), 0, 0, ctypes.byref(kb)))
+    kbar = kb.value
+    pairs_per_step = 4.0 * kbar * n
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(local)
+    clocks.start()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    launches0 = native.launch_count()
+    integ.stage_events = []
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        integ.integrate(DT)
+        b.record()
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    launches = native.launch_count() - launches0
+    clk = clocks.stop()
+    events = integ.stage_events
+    integ.stage_events = None
+    t_total = sum(step_ms) / 1e3
+    if pg:
+        t = torch.tensor([t_total], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_total = float(t.item())
+    stage_ms = {}
+    for name, a, b in events:
+        stage_ms.setdefault(name, []).append(a.elapsed_time(b))
+
+    # e2e through the public API with host buffers
+    fields_in = ("x", "y", "z", "u", "v", "w")
+    fields_out = ("x", "y", "z", "u", "v", "w", "rho", "p")
+    pa = particles.arrays[0]
+    host = {f: torch.from_numpy(pa.get(f)).pin_memory() for f in fields_in}
+    torch.cuda.synchronize()
+    e2e_steps = max(1, args.steps)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pa.set(**host)
+        integ.integrate(DT)
+        out = pa.get(*fields_out)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    if pg:
+        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    del out
+
+    steps = args.steps
+    value = world * pairs_per_step * steps / t_total
+    e2e_value = world * pairs_per_step * e2e_steps / e2e_t
+    peak, peak_kind = measured_peaks()
+    # dominant kernel by device time
+    dom = max(ALG_BYTES, key=lambda k: sum(stage_ms.get(k, [0.0])))
+    launches_dom = len(stage_ms.get(dom, []))
+    avg_ms = statistics.mean(stage_ms[dom]) if launches_dom else float("nan")
+    achieved = ALG_BYTES[dom] * n / (avg_ms / 1e3) / 1e9
+    flops = PAIR_FLOPS[dom] * kbar * n / (avg_ms / 1e3) / 1e12
+    step_s = t_total / steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair sums, f64 integration",
+        "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": "3D jittered lattice, %d particles (%d^3), h=1.2dx, RK2, "
+                               "NNPS+SPHRho+Tait+PGrad+MonaghanAV" % (n, round(n ** (1 / 3))),
+                   "particles_per_gpu": n, "mean_neighbours": kbar,
+                   "pair_passes_per_step": 4, "dt": DT,
+                   "cache": "L2 flushed between timed steps (256 MiB write outside the events)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "steps_per_s": 1.0 / step_s,
+        "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * n * len(fields_in),
+                "d2h_bytes_per_step": 8 * n * len(fields_out),
+                "ms_per_step": e2e_t / e2e_steps * 1e3},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "alg_bytes_per_particle": ALG_BYTES[dom],
+                     "note": "pair kernels issue-bound; fp32 context in fp32_context"},
+        "fp32_context": {"kernel": dom, "achieved_tflops": flops,
+                         "nominal_peak_tflops": FP32_NOMINAL_TFLOPS,
+                         "frac_of_nominal": flops / FP32_NOMINAL_TFLOPS},
+        "step_roofline": {"alg_bytes_per_particle_step": STEP_ALG_BYTES,
+                          "achieved_gbs": STEP_ALG_BYTES * n / step_s / 1e9,
+                          "frac": STEP_ALG_BYTES * n / step_s / 1e9 / peak},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(1, 1, args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    procs = args.procs or os.cpu_count() or 1
+    cb = cpu_baseline(procs, args.warmup, args.steps)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": "3D jittered lattice, h=1.2dx, RK2, NNPS+SPHRho+Tait+PGrad+"
+                               "MonaghanAV; bounded sample of %d particles per process"
+                               % SAMPLE_N},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--procs", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

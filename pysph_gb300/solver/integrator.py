@@ -167,6 +167,9 @@ class Integrator:
         self.stages = []
         self._rates = {}
         self._written = {}
+        # when a list, CUDA events (name, start, end) are recorded around
+        # every stage and neighbour build on the current stream
+        self.stage_events = None
 
     def set_rupdate_list(self):
         self.rupdate_list = [[] for _ in self.particles.arrays]
@@ -256,7 +259,24 @@ class Integrator:
         kname = "k" + str(self.cstep)
         self._written = {}
         for st in self.stages:
-            st.run(self, kname)
+            if self.stage_events is None:
+                st.run(self, kname)
+            else:
+                self._timed(type(st).__name__, st.run, self, kname)
+
+    def _timed(self, name, fn, *args):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn(*args)
+        b.record()
+        self.stage_events.append((name, a, b))
+
+    def _update_particles(self):
+        if self.stage_events is None:
+            self.particles.update()
+        else:
+            self._timed("NNPSBuild", self.particles.update)
 
     def _lines(self, mode, dt):
         out = []
@@ -328,7 +348,7 @@ class EulerIntegrator(Integrator):
         self.cstep = 1
         self.eval(self.calcs)
         self._apply("euler", dt)
-        self.particles.update()
+        self._update_particles()
 
 
 class RK2Integrator(Integrator):
@@ -346,11 +366,11 @@ class RK2Integrator(Integrator):
         self.eval(self.calcs)
         self._apply("predict", dt)
         self.cstep = 2
-        self.particles.update()
+        self._update_particles()
         self.eval(self.calcs)
         self._apply("rk2", dt)
         self.cstep = 1
-        self.particles.update()
+        self._update_particles()
 
 
 def _not_here(name, ref):

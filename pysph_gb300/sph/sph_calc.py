@@ -117,7 +117,7 @@ class SPHCalc:
         """sph_calc.pyx:132-183."""
         if (len(self.sources) == 0 or self.nnps_manager is None or self.dest is None or
                 self.kernel is None or len(self.funcs) == 0):
-            logger.warning("invalid input to setup_internals")
+            logger.debug("invalid input to setup_internals")
             return
         if len(self.funcs) != len(self.sources):
             raise ValueError("One sph function is needed per source")
