@@ -80,7 +80,8 @@ int sph_ctx_create(int dim, sph_ctx **out) {
         (e = cudaMalloc(&c->d_err, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
-        (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess) {
+        (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMallocHost(&c->h_maxcnt, kMaxListSlots * sizeof(int))) != cudaSuccess) {
         sph_ctx_destroy(c);
         return cuda_check(e, "sph_ctx_create");
     }
@@ -92,6 +93,7 @@ int sph_ctx_create(int dim, sph_ctx **out) {
 int sph_ctx_destroy(sph_ctx *c) {
     if (!c) return SPH_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    free_lists(c);
     for (auto &A : c->arrays) {
         cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
         cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st);
@@ -102,6 +104,7 @@ int sph_ctx_destroy(sph_ctx *c) {
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);
     if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_red) cudaFreeHost(c->h_red);
+    if (c->h_maxcnt) cudaFreeHost(c->h_maxcnt);
     delete c;
     return SPH_OK;
 }

@@ -373,7 +373,10 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     if (same_layout)
         for (int a = 0; a < narrays; ++a)
             if (ctx->arrays[a].ref_n != arrays[a].n) same_layout = false;
-    if ((int)ctx->arrays.size() < narrays) ctx->arrays.resize(narrays);
+    if ((int)ctx->arrays.size() != narrays) {
+        free_lists(ctx);
+        if ((int)ctx->arrays.size() < narrays) ctx->arrays.resize(narrays);
+    }
     if (ctx->cell_size_ref != cell_size) same_layout = false;
     ctx->cell_size_ref = cell_size;
 
@@ -408,7 +411,12 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 6, ctx->d_hmax, sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, st));
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    {
+        const int rcm = list_maxima_async(ctx);
+        if (rcm) return rcm;
+    }
     SPH_CUDA(cudaStreamSynchronize(st));
+    list_maxima_collect(ctx);
     unsigned err = (unsigned)ctx->h_box[8];
     if (err & SPH_EFLAG_JUMP) {
         ctx->built = false;
@@ -489,6 +497,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         }
     }
     ctx->built = true;
+    ctx->build_id += 1;
     return SPH_OK;
 }
 

@@ -1,16 +1,26 @@
-// Pair-loop kernels (sm_103a): summation density (+ Tait) and the rates
-// kernel (pressure gradient, Monaghan artificial viscosity, XSPH, Monaghan
-// boundary force, with gravity / position stepping folded into the store).
+// Pair-loop kernels (sm_103a): neighbour lists, summation density (+ Tait)
+// and the rates kernel (pressure gradient, Monaghan artificial viscosity,
+// XSPH, Monaghan boundary force, with gravity / position stepping folded
+// into the store).
 //
 // Replaces SPHCalc.sph -> SPHFunction.eval -> eval_single -> eval_nbr of the
 // reference (sph/sph_calc.pyx:223-270, sph/sph_func.pyx:199-234,381-394,
-// 466-484) for the functions listed in the header.  One group of LPD lanes
-// owns one destination (in cell-sorted order); the stencil candidates are
-// tested by all lanes, hits are queued and evaluated LPD at a time, and the
-// per-lane compensated FP32 sums are combined by an error-free butterfly.
+// 466-484).  One thread owns one destination in cell-sorted order, so the
+// threads of a warp walk the same stencil rows and their candidate loads
+// are broadcasts.  Per evaluation:
+//
+//   k_nbrlist  tests the stencil candidates once (FP32 with an FP64 band
+//              recheck, exact neighbour sets) and writes a k-major list of
+//              (source slot | stencil offset code);
+//   k_density  streams the list: sum m W, then Tait, per destination;
+//   k_rates    streams the list: every rate term of the fused calcs.
+//
+// Sums are sequential per destination with Neumaier compensation, in the
+// neighbour order of the list (stencil rows, ascending slot).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "sph_internal.cuh"
 
@@ -22,14 +32,27 @@ struct DestDev {
     const float4 *posm, *velh, *st;
     const int *skey, *perm;
     const int64_t *tag;
-    const double *x, *y, *z, *u, *v, *w, *h, *m, *cs, *rho, *p;
+    const double *x, *y, *z, *u, *v, *w, *h;
     int64_t n;
+};
+
+struct ListArgs {
+    Grid g;
+    DestDev d;
+    SrcDev s;
+    uint32_t *nbr;
+    int *cnt;
+    int *maxcnt;
+    int64_t stride;
+    int cap;
 };
 
 struct DensityArgs {
     Grid g;
     DestDev d;
     SrcDev s[SPH_MAX_SOURCES];
+    int cap[SPH_MAX_SOURCES];
+    int64_t stride[SPH_MAX_SOURCES];
     int nsrc;
     int dim;
     int tait;
@@ -42,6 +65,8 @@ struct RatesArgs {
     Grid g;
     DestDev d;
     SrcDev s[SPH_MAX_SOURCES];
+    int cap[SPH_MAX_SOURCES];
+    int64_t stride[SPH_MAX_SOURCES];
     int nsrc;
     int dim;
     int add_velocity, add_gravity, accumulate;
@@ -50,96 +75,139 @@ struct RatesArgs {
     double *pos[3];
 };
 
-// Fill the group's destination context (identical in every lane of it).
-__device__ __forceinline__ void load_dest(const Grid &g, const DestDev &D, int ds, bool valid,
-                                          DestCtx &dc, int &orig, bool &real) {
-    dc.active = false;
-    orig = 0;
-    real = false;
-    dc.xi_x = dc.xi_y = dc.xi_z = 0.f;
-    dc.cx = dc.cy = dc.cz = 0;
-    dc.r2lo = dc.r2hi = -1.f;
-    dc.px = dc.py = dc.pz = 0.0;
-    dc.radius2 = -1.0;
-    if (!valid) return;
-    orig = D.perm[ds];
-    real = (D.tag == nullptr) || (D.tag[orig] == SPH_TAG_LOCAL_REAL);
-    if (!real) return;
-    float4 p = D.posm[ds];
-    dc.xi_x = p.x; dc.xi_y = p.y; dc.xi_z = p.z;
-    decode_cell(g, D.skey[ds], dc.cx, dc.cy, dc.cz);
-    double radius = __dmul_rn(D.h[orig], g.radius_scale);
-    dc.radius2 = __dmul_rn(radius, radius);
-    float r2 = (float)dc.radius2;
-    dc.r2lo = r2 * (1.f - 1e-5f);
-    dc.r2hi = r2 * (1.f + 1e-5f);
-    dc.px = ld0(D.x, orig); dc.py = ld0(D.y, orig); dc.pz = ld0(D.z, orig);
-    dc.active = true;
+// Destination of thread slot s; false for a non-LocalReal particle.
+__device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s, DestPos &d) {
+    const int orig = D.perm[s];
+    d.orig = orig;
+    if (D.tag != nullptr && D.tag[orig] != SPH_TAG_LOCAL_REAL) return false;
+    const float4 p = D.posm[s];
+    d.xi_x = p.x; d.xi_y = p.y; d.xi_z = p.z;
+    decode_cell(g, D.skey[s], d.cx, d.cy, d.cz);
+    const double radius = __dmul_rn(D.h[orig], g.radius_scale);
+    d.radius2 = __dmul_rn(radius, radius);
+    const float r2 = (float)d.radius2;
+    d.r2lo = r2 * (1.f - 1e-5f);
+    d.r2hi = r2 * (1.f + 1e-5f);
+    return true;
+}
+
+// shift table: code -> -(dx, dy, dz) * cs
+template <int KX>
+__device__ __forceinline__ void fill_shift_table(float4 *tab, const Grid &g) {
+    constexpr int W = 2 * KX + 1;
+    for (int c = threadIdx.x; c < W * W * W; c += blockDim.x) {
+        const int dx = c % W - KX, dy = (c / W) % W - KX, dz = c / (W * W) - KX;
+        tab[c] = make_float4(-(float)dx * g.cs_f, -(float)dy * g.cs_f, -(float)dz * g.cs_f, 0.f);
+    }
+    __syncthreads();
+}
+
+// Stream the neighbours of dest slot s from the list, then (if the list
+// overflowed) the remaining ones by re-traversal, calling fn(j, rx, ry, rz, mj).
+template <int KX, class Fn>
+__device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int cap, int64_t stride,
+                                           int s, const DestPos &d, const float4 *tab,
+                                           const DestDev &D, Fn &&fn) {
+    using C = Code<KX>;
+    const int c = S.ncnt[s];
+    const int m = min(c, cap);
+    for (int k = 0; k < m; ++k) {
+        const uint32_t e = S.nbr[(int64_t)k * stride + s];
+        const int j = (int)(e & C::JMASK);
+        const float4 sh = tab[e >> C::SHIFT];
+        const float4 pj = S.posm[j];
+        fn(j, (d.xi_x - pj.x) + sh.x, (d.xi_y - pj.y) + sh.y, (d.xi_z - pj.z) + sh.z, pj.w);
+    }
+    if (c > cap) {
+        int skip = cap;
+        for_neighbours<KX>(g, S, d, D.x, D.y, D.z,
+                           [&](int j, float rx, float ry, float rz, int, float mj) {
+                               if (skip > 0) {
+                                   --skip;
+                                   return;
+                               }
+                               fn(j, rx, ry, rz, mj);
+                           });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// neighbour list (base/nnps.pyx:525-620 FixedDestNbrParticleLocator cache)
+// ---------------------------------------------------------------------------
+template <int KX>
+__global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ ListArgs A) {
+    using C = Code<KX>;
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int c = 0;
+    if (s < A.d.n) {
+        DestPos d;
+        if (load_dest(A.g, A.d, (int)s, d)) {
+            uint32_t *out = A.nbr + s;
+            const int cap = A.cap;
+            const int64_t stride = A.stride;
+            for_neighbours<KX>(A.g, A.s, d, A.d.x, A.d.y, A.d.z,
+                               [&](int j, float, float, float, int code, float) {
+                                   if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
+                                   ++c;
+                               });
+        }
+        A.cnt[s] = c;
+    }
+    const int wmax = __reduce_max_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) atomicMax(A.maxcnt, wmax);
 }
 
 // ---------------------------------------------------------------------------
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
-template <int KX, int LPD>
+template <int KX>
 __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ DensityArgs A) {
-    __shared__ int s_qj[kPairBlock / 32][kQueue];
-    __shared__ QEntry s_qe[kPairBlock / 32][kQueue];
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    constexpr int G = 32 / LPD;
-    const int grp = lane / LPD, gl = lane % LPD;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w0 = blockIdx.x * (int64_t)(blockDim.x >> 5) + warp; w0 * G < A.d.n; w0 += nwarps) {
-        int64_t ds = w0 * G + grp;
-        bool valid = ds < A.d.n;
-        DestCtx dc;
-        int orig;
-        bool real;
-        load_dest(A.g, A.d, (int)ds, valid, dc, orig, real);
-        float hi = valid ? A.d.velh[ds].w : 1.f;
-        CSum rho;
+    __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
+    fill_shift_table<KX>(tab, A.g);
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= A.d.n) return;
+    DestPos d;
+    const bool real = load_dest(A.g, A.d, (int)s, d);
+    CSum rho;
+    if (real) {
+        const float hi = A.d.velh[s].w;
         const int dim = A.dim;
         for (int si = 0; si < A.nsrc; ++si) {
             const SrcDev &S = A.s[si];
-            auto proc = [&](int j, const QEntry &e) {
-                float hj = S.velh[j].w;
-                float hab = 0.5f * (hi + hj);
-                float ih = __fdividef(1.f, hab);
-                float r2 = fmaf(e.r.x, e.r.x, fmaf(e.r.y, e.r.y, e.r.z * e.r.z));
-                float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                float w = cubic_w(r * ih) * cubic_fac(dim, ih);
-                rho.add(w * e.r.w);
-            };
-            traverse<KX, LPD>(A.g, S, dc, s_qj[warp], s_qe[warp], proc);
+            for_listed<KX>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+                           [&](int j, float rx, float ry, float rz, float mj) {
+                               const float hab = 0.5f * (hi + S.velh[j].w);
+                               const float ih = __fdividef(1.f, hab);
+                               const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                               const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                               rho.add(cubic_w(r * ih) * cubic_fac(dim, ih) * mj);
+                           });
         }
-        group_reduce<LPD>(rho);
-        if (valid && gl == 0) {
-            double r64 = real ? rho.value() : 0.0;
-            if (A.rho_out) A.rho_out[orig] = r64;
-            float rf = (float)r64;
-            float pf = 0.f, cf = 0.f;
-            if (A.tait && real) {
-                // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), evaluated
-                // through log1p/expm1 of the density excess so that p keeps its
-                // relative accuracy as rho -> ro.
-                float B = A.co * A.co * A.ro / A.gamma;
-                float lr = log1pf((rf - A.ro) / A.ro);
-                pf = B * expm1f(A.gamma * lr);
-                cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
-                if (A.p_out) A.p_out[orig] = (double)pf;
-                if (A.cs_out) A.cs_out[orig] = (double)cf;
-            } else if (A.tait) {
-                if (A.p_out) A.p_out[orig] = 0.0;
-                if (A.cs_out) A.cs_out[orig] = 0.0;
-            }
-            if (A.st_out) {
-                float4 old = A.st_out[ds];
-                if (A.tait) {
-                    A.st_out[ds] = make_float4(rf, pf / (rf * rf), cf, pf);
-                } else {
-                    A.st_out[ds] = make_float4(rf, old.w / (rf * rf), old.z, old.w);
-                }
-            }
+    }
+    const int orig = d.orig;
+    const double r64 = real ? rho.value() : 0.0;
+    if (A.rho_out) A.rho_out[orig] = r64;
+    const float rf = (float)r64;
+    float pf = 0.f, cf = 0.f;
+    if (A.tait) {
+        if (real) {
+            // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), through
+            // log1p/expm1 of the density excess so p keeps its relative accuracy
+            // as rho -> ro.
+            const float B = A.co * A.co * A.ro / A.gamma;
+            const float lr = log1pf((rf - A.ro) / A.ro);
+            pf = B * expm1f(A.gamma * lr);
+            cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
+        }
+        A.p_out[orig] = (double)pf;
+        A.cs_out[orig] = (double)cf;
+    }
+    if (A.st_out) {
+        if (A.tait) {
+            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, pf);
+        } else {
+            const float4 old = A.st_out[s];
+            A.st_out[s] = make_float4(rf, old.w / (rf * rf), old.z, old.w);
         }
     }
 }
@@ -149,77 +217,71 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
 // 41-124), XSPH (xsph_funcs.pyx:31-88), Monaghan BF (boundary_funcs.pyx:
 // 54-110), gravity (external_force.pyx:39-45), stepping (position_funcs.pyx)
 // ---------------------------------------------------------------------------
-template <int KX, int LPD>
+template <int KX>
 __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ RatesArgs A) {
-    __shared__ int s_qj[kPairBlock / 32][kQueue];
-    __shared__ QEntry s_qe[kPairBlock / 32][kQueue];
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    constexpr int G = 32 / LPD;
-    const int grp = lane / LPD, gl = lane % LPD;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w0 = blockIdx.x * (int64_t)(blockDim.x >> 5) + warp; w0 * G < A.d.n; w0 += nwarps) {
-        int64_t ds = w0 * G + grp;
-        bool valid = ds < A.d.n;
-        DestCtx dc;
-        int orig;
-        bool real;
-        load_dest(A.g, A.d, (int)ds, valid, dc, orig, real);
-        float4 vi = valid ? A.d.velh[ds] : make_float4(0.f, 0.f, 0.f, 1.f);
-        float4 sti = valid ? A.d.st[ds] : make_float4(1.f, 0.f, 0.f, 0.f);
-        float mi = valid ? A.d.posm[ds].w : 0.f;
+    __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
+    fill_shift_table<KX>(tab, A.g);
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= A.d.n) return;
+    DestPos d;
+    const bool real = load_dest(A.g, A.d, (int)s, d);
+    CSum ax, ay, az, xx, xy, xz;
+    if (real) {
+        const float4 vi = A.d.velh[s];
+        const float4 sti = A.d.st[s];
+        const float mi = A.d.posm[s].w;
         const float hi = vi.w, rhoi = sti.x, pri = sti.y, ci = sti.z;
-        CSum ax, ay, az, xx, xy, xz;
         const int dim = A.dim;
         for (int si = 0; si < A.nsrc; ++si) {
             const SrcDev &S = A.s[si];
             const uint32_t fl = S.flags;
-            auto proc = [&](int j, const QEntry &e) {
-                const float rx = e.r.x, ry = e.r.y, rz = e.r.z, mj = e.r.w;
-                float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                float4 vj = S.velh[j];
-                float hab = 0.5f * (hi + vj.w);
-                float ih = __fdividef(1.f, hab);
-                float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
-                float q = r2 * rinv * ih;
-                float fac = cubic_fac(dim, ih);
-                if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC)) {
-                    float4 stj = S.st[j];
-                    float t = 0.f;
-                    if (fl & SPH_TERM_PGRAD) t -= mj * (pri + stj.y);
-                    if (fl & SPH_TERM_AVISC) {
-                        float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
-                        if (dot < 0.f) {
-                            float cab = 0.5f * (ci + stj.z);
-                            float rhoab = 0.5f * (rhoi + stj.x);
-                            float mu = hab * dot / (r2 + S.eta2 * hab * hab);
-                            float piab = (-S.alpha * cab * mu + S.beta * mu * mu) / rhoab;
-                            t -= mj * piab;
+            for_listed<KX>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+                           [&](int j, float rx, float ry, float rz, float mj) {
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float4 vj = S.velh[j];
+                const float hab = 0.5f * (hi + vj.w);
+                const float ih = __fdividef(1.f, hab);
+                const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+                const float q = r2 * rinv * ih;
+                const float fac = cubic_fac(dim, ih);
+                if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) {
+                    const float4 stj = S.st[j];
+                    if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC)) {
+                        float t = 0.f;
+                        if (fl & SPH_TERM_PGRAD) t -= mj * (pri + stj.y);
+                        if (fl & SPH_TERM_AVISC) {
+                            const float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+                            if (dot < 0.f) {
+                                const float cab = 0.5f * (ci + stj.z);
+                                const float rhoab = 0.5f * (rhoi + stj.x);
+                                const float mu = hab * dot / (r2 + S.eta2 * hab * hab);
+                                const float piab = (-S.alpha * cab * mu + S.beta * mu * mu) / rhoab;
+                                t -= mj * piab;
+                            }
                         }
+                        const float gf = cubic_gfac(q, ih, rinv) * fac * t;
+                        ax.add(gf * rx);
+                        ay.add(gf * ry);
+                        az.add(gf * rz);
                     }
-                    float gf = cubic_gfac(q, ih, rinv) * fac * t;
-                    ax.add(gf * rx);
-                    ay.add(gf * ry);
-                    az.add(gf * rz);
-                }
-                if (fl & SPH_TERM_XSPH) {
-                    float rhoj = S.st[j].x;
-                    float rhoab = 0.5f * (rhoj + rhoi);
-                    float temp = mj * (cubic_w(q) * fac) / rhoab * S.eps;
-                    xx.add(temp * (vj.x - vi.x));
-                    xy.add(temp * (vj.y - vi.y));
-                    xz.add(temp * (vj.z - vi.z));
+                    if (fl & SPH_TERM_XSPH) {
+                        const float rhoab = 0.5f * (stj.x + rhoi);
+                        const float temp = mj * (cubic_w(q) * fac) / rhoab * S.eps;
+                        xx.add(temp * (vj.x - vi.x));
+                        xy.add(temp * (vj.y - vi.y));
+                        xz.add(temp * (vj.z - vi.z));
+                    }
                 }
                 if (fl & SPH_TERM_BFORCE) {
-                    float4 nj = S.nrm[j], tj = S.tan[j];
-                    float xt = rx * tj.x + ry * tj.y + rz * tj.z;
-                    float yn = rx * nj.x + ry * nj.y + rz * nj.z;
-                    float qb = yn / hi;
+                    const float4 nj = S.nrm[j], tj = S.tan[j];
+                    const float xt = rx * tj.x + ry * tj.y + rz * tj.z;
+                    const float yn = rx * nj.x + ry * nj.y + rz * nj.z;
+                    const float qb = yn / hi;
                     float force = 0.f;
-                    float axt = fabsf(xt);
+                    const float axt = fabsf(xt);
                     if (axt <= S.delp) {
-                        float beta = 0.02f * ci * ci / yn;
-                        float tforce = 1.f - axt / S.delp;
+                        const float beta = 0.02f * ci * ci / yn;
+                        const float tforce = 1.f - axt / S.delp;
                         float nforce;
                         if (0.f < qb && qb <= 2.f / 3.f)
                             nforce = 2.f / 3.f;
@@ -235,53 +297,27 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                     ay.add(force * nj.y);
                     az.add(force * nj.z);
                 }
-            };
-            traverse<KX, LPD>(A.g, S, dc, s_qj[warp], s_qe[warp], proc);
-        }
-        group_reduce<LPD>(ax);
-        group_reduce<LPD>(ay);
-        group_reduce<LPD>(az);
-        group_reduce<LPD>(xx);
-        group_reduce<LPD>(xy);
-        group_reduce<LPD>(xz);
-        if (valid && gl == 0) {
-            double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
-            if (real) {
-                a3[0] = ax.value(); a3[1] = ay.value(); a3[2] = az.value();
-                p3[0] = xx.value(); p3[1] = xy.value(); p3[2] = xz.value();
-                if (A.add_gravity) { a3[0] += A.gx; a3[1] += A.gy; a3[2] += A.gz; }
-                if (A.add_velocity) {
-                    // exact FP64 velocity of the destination (position_funcs.pyx:47-50)
-                    p3[0] += ld0(A.d.u, orig);
-                    p3[1] += ld0(A.d.v, orig);
-                    p3[2] += ld0(A.d.w, orig);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (A.acc[c]) A.acc[c][orig] = (A.accumulate ? A.acc[c][orig] : 0.0) + a3[c];
-                if (A.pos[c]) A.pos[c][orig] = (A.accumulate ? A.pos[c][orig] : 0.0) + p3[c];
-            }
+            });
         }
     }
-}
-
-template <int KX, int LPD>
-void launch_density_t(const DensityArgs &a, int blocks, cudaStream_t st) {
-    k_density<KX, LPD><<<blocks, kPairBlock, 0, st>>>(a);
-}
-
-template <int KX, int LPD>
-void launch_rates_t(const RatesArgs &a, int blocks, cudaStream_t st) {
-    k_rates<KX, LPD><<<blocks, kPairBlock, 0, st>>>(a);
-}
-
-// lanes per destination: enough lanes for the expected candidate count
-int choose_lpd(const Grid &g) {
-    int rows = (2 * g.ky + 1) * (2 * g.kz + 1);
-    if (rows >= 9) return 32;
-    if (rows >= 3) return 16;
-    return 8;
+    const int orig = d.orig;
+    double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
+    if (real) {
+        a3[0] = ax.value(); a3[1] = ay.value(); a3[2] = az.value();
+        p3[0] = xx.value(); p3[1] = xy.value(); p3[2] = xz.value();
+        if (A.add_gravity) { a3[0] += A.gx; a3[1] += A.gy; a3[2] += A.gz; }
+        if (A.add_velocity) {
+            // exact FP64 velocity of the destination (position_funcs.pyx:47-50)
+            p3[0] += ld0(A.d.u, orig);
+            p3[1] += ld0(A.d.v, orig);
+            p3[2] += ld0(A.d.w, orig);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (A.acc[c]) A.acc[c][orig] = (A.accumulate ? A.acc[c][orig] : 0.0) + a3[c];
+        if (A.pos[c]) A.pos[c][orig] = (A.accumulate ? A.pos[c][orig] : 0.0) + p3[c];
+    }
 }
 
 DestDev make_dest(const ArraySnap &D) {
@@ -291,8 +327,7 @@ DestDev make_dest(const ArraySnap &D) {
     d.tag = D.view.tag;
     d.x = D.view.x; d.y = D.view.y; d.z = D.view.z;
     d.u = D.view.u; d.v = D.view.v; d.w = D.view.w;
-    d.h = D.view.h; d.m = D.view.m; d.cs = D.view.cs;
-    d.rho = D.view.rho; d.p = D.view.p;
+    d.h = D.view.h;
     d.n = D.n;
     return d;
 }
@@ -305,18 +340,126 @@ SrcDev make_src(const ArraySnap &S) {
     return s;
 }
 
-int blocks_for(int64_t n, int lpd) {
-    int64_t warps = (n * lpd + 31) / 32;
-    int64_t blocks = (warps + (kPairBlock / 32) - 1) / (kPairBlock / 32);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(blocks, 1 << 30));
+int blocks_for(int64_t n) {
+    return (int)std::max<int64_t>(1, (n + kPairBlock - 1) / kPairBlock);
+}
+
+// List capacity override (environment SPH_LIST_CAP, >= 1): forces the
+// re-traversal path of destinations with more neighbours than the capacity.
+int cap_override() {
+    static int v = -2;
+    if (v == -2) {
+        const char *e = getenv("SPH_LIST_CAP");
+        v = e ? atoi(e) : -1;
+        if (v < 1) v = -1;
+    }
+    return v;
+}
+
+// default list capacity before the first count is known
+int default_cap(const Grid &g) {
+    if (g.kz > 0) return 96;
+    if (g.ky > 0) return 40;
+    return 16;
+}
+
+int64_t code_limit(int kx) {
+    return kx == 1 ? (1ll << Code<1>::SHIFT) : (kx == 2 ? (1ll << Code<2>::SHIFT) : (1ll << Code<3>::SHIFT));
+}
+
+// Build (if stale) the neighbour list of (dst, src) for the current build.
+int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
+    const int na = (int)ctx->arrays.size();
+    if ((int)ctx->lists.size() < na * na) ctx->lists.resize((size_t)na * na);
+    NbrList &L = ctx->lists[(size_t)dst * na + src];
+    *out = &L;
+    if (L.build == ctx->build_id) return SPH_OK;
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[src];
+    const Grid &g = ctx->grid;
+    if (S.n >= code_limit(g.kx))
+        return set_error(SPH_ERR_NOTSUP, "neighbour list: too many source particles for this "
+                                         "cell subdivision (use a smaller subdivision)");
+    if (!L.maxcnt) {
+        SPH_CUDA(cudaMalloc(&L.maxcnt, sizeof(int)));
+        SPH_CUDA(cudaMemsetAsync(L.maxcnt, 0, sizeof(int), ctx->stream));
+    }
+    // capacity: largest count seen so far plus headroom (dests beyond it are
+    // completed by re-traversal, so a short list is slow, never wrong)
+    int cap = L.cap > 0 ? L.cap : default_cap(g);
+    if (L.seen_max > 0) {
+        const int want = (L.seen_max + L.seen_max / 4 + 15) / 8 * 8;
+        if (want > cap || want < cap / 2) cap = want;
+    }
+    if (cap_override() > 0) cap = cap_override();
+    const int64_t stride = std::max<int64_t>(D.n, 1);
+    const int64_t need = stride * cap;
+    if (need > L.entries || !L.nbr || !L.cnt || stride > L.stride_cap) {
+        cudaFree(L.nbr);
+        cudaFree(L.cnt);
+        L.nbr = nullptr;
+        L.cnt = nullptr;
+        SPH_CUDA(cudaMalloc(&L.nbr, sizeof(uint32_t) * need));
+        SPH_CUDA(cudaMalloc(&L.cnt, sizeof(int) * stride));
+        L.entries = need;
+        L.stride_cap = stride;
+    }
+    if (cap_override() > 0) cap = cap_override();
+    L.cap = cap;
+    L.stride = stride;
+    if (D.n > 0) {
+        ListArgs a{};
+        a.g = g;
+        a.d = make_dest(D);
+        a.s = make_src(S);
+        a.nbr = L.nbr;
+        a.cnt = L.cnt;
+        a.maxcnt = L.maxcnt;
+        a.stride = stride;
+        a.cap = cap;
+        const int b = blocks_for(D.n);
+        if (g.kx == 1) k_nbrlist<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        else if (g.kx == 2) k_nbrlist<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        else k_nbrlist<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        count_launch();
+        SPH_LAUNCH_CHECK("k_nbrlist");
+    }
+    L.build = ctx->build_id;
+    return SPH_OK;
 }
 
 }  // namespace
 
+// Queue copies of the lists' largest counts (read at the next build's sync).
+int list_maxima_async(sph_ctx *ctx) {
+    const int nl = (int)ctx->lists.size();
+    for (int i = 0; i < nl && i < kMaxListSlots; ++i)
+        if (ctx->lists[i].maxcnt)
+            SPH_CUDA(cudaMemcpyAsync(ctx->h_maxcnt + i, ctx->lists[i].maxcnt, sizeof(int),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    return SPH_OK;
+}
+
+void list_maxima_collect(sph_ctx *ctx) {
+    const int nl = (int)ctx->lists.size();
+    for (int i = 0; i < nl && i < kMaxListSlots; ++i)
+        if (ctx->lists[i].maxcnt)
+            ctx->lists[i].seen_max = std::max(ctx->lists[i].seen_max, ctx->h_maxcnt[i]);
+}
+
+void free_lists(sph_ctx *ctx) {
+    for (auto &L : ctx->lists) {
+        cudaFree(L.nbr);
+        cudaFree(L.cnt);
+        cudaFree(L.maxcnt);
+    }
+    ctx->lists.clear();
+}
+
 int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
                    double *rho, double *p, double *cs) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "density: no neighbour build");
-    int na = (int)ctx->arrays.size();
+    const int na = (int)ctx->arrays.size();
     if (dst < 0 || dst >= na || nsrc < 0 || nsrc > SPH_MAX_SOURCES || !prm)
         return set_error(SPH_ERR_ARG, "density: bad destination / sources");
     ArraySnap &D = ctx->arrays[dst];
@@ -326,7 +469,14 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     a.nsrc = nsrc;
     for (int i = 0; i < nsrc; ++i) {
         if (srcs[i] < 0 || srcs[i] >= na) return set_error(SPH_ERR_ARG, "density: bad source");
+        NbrList *L;
+        const int rc = ensure_list(ctx, dst, srcs[i], &L);
+        if (rc) return rc;
         a.s[i] = make_src(ctx->arrays[srcs[i]]);
+        a.s[i].nbr = L->nbr;
+        a.s[i].ncnt = L->cnt;
+        a.cap[i] = L->cap;
+        a.stride[i] = L->stride;
     }
     a.dim = prm->dim;
     a.tait = prm->tait;
@@ -334,18 +484,14 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     a.rho_out = rho; a.p_out = p; a.cs_out = cs;
     // the sorted state of the destination follows its own rho (and p, cs with
     // Tait); a density written to some other property leaves it untouched
-    bool own = rho != nullptr && rho == D.view.rho &&
-               (!prm->tait || (p == D.view.p && cs == D.view.cs));
+    const bool own = rho != nullptr && rho == D.view.rho &&
+                     (!prm->tait || (p == D.view.p && cs == D.view.cs));
     a.st_out = own ? D.st : nullptr;
     if (D.n == 0) return SPH_OK;
-    int lpd = choose_lpd(ctx->grid);
-    int blocks = blocks_for(D.n, lpd);
-    int kx = ctx->grid.kx;
-#define DISPATCH(KX_, L_) launch_density_t<KX_, L_>(a, blocks, ctx->stream)
-    if (kx == 1) { if (lpd == 32) DISPATCH(1, 32); else if (lpd == 16) DISPATCH(1, 16); else DISPATCH(1, 8); }
-    else if (kx == 2) { if (lpd == 32) DISPATCH(2, 32); else if (lpd == 16) DISPATCH(2, 16); else DISPATCH(2, 8); }
-    else { if (lpd == 32) DISPATCH(3, 32); else if (lpd == 16) DISPATCH(3, 16); else DISPATCH(3, 8); }
-#undef DISPATCH
+    const int b = blocks_for(D.n);
+    if (a.g.kx == 1) k_density<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else if (a.g.kx == 2) k_density<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else k_density<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
     return SPH_OK;
@@ -355,7 +501,7 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
                  const sph_rates_params *prm, double *const *acc, double *const *pos,
                  int accumulate) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "rates: no neighbour build");
-    int na = (int)ctx->arrays.size();
+    const int na = (int)ctx->arrays.size();
     if (dst < 0 || dst >= na || nterms < 0 || nterms > SPH_MAX_SOURCES || !prm)
         return set_error(SPH_ERR_ARG, "rates: bad destination / sources");
     ArraySnap &D = ctx->arrays[dst];
@@ -364,11 +510,18 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
     a.d = make_dest(D);
     a.nsrc = nterms;
     for (int i = 0; i < nterms; ++i) {
-        int s = terms[i].src;
+        const int s = terms[i].src;
         if (s < 0 || s >= na) return set_error(SPH_ERR_ARG, "rates: bad source");
         if ((terms[i].flags & SPH_TERM_BFORCE) && !ctx->arrays[s].has_nrm)
             return set_error(SPH_ERR_ARG, "rates: boundary force source has no normals");
+        NbrList *L;
+        const int rc = ensure_list(ctx, dst, s, &L);
+        if (rc) return rc;
         a.s[i] = make_src(ctx->arrays[s]);
+        a.s[i].nbr = L->nbr;
+        a.s[i].ncnt = L->cnt;
+        a.cap[i] = L->cap;
+        a.stride[i] = L->stride;
         a.s[i].flags = terms[i].flags;
         a.s[i].alpha = (float)terms[i].alpha;
         a.s[i].beta = (float)terms[i].beta;
@@ -386,14 +539,10 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
         a.pos[c] = pos ? pos[c] : nullptr;
     }
     if (D.n == 0) return SPH_OK;
-    int lpd = choose_lpd(ctx->grid);
-    int blocks = blocks_for(D.n, lpd);
-    int kx = ctx->grid.kx;
-#define DISPATCH(KX_, L_) launch_rates_t<KX_, L_>(a, blocks, ctx->stream)
-    if (kx == 1) { if (lpd == 32) DISPATCH(1, 32); else if (lpd == 16) DISPATCH(1, 16); else DISPATCH(1, 8); }
-    else if (kx == 2) { if (lpd == 32) DISPATCH(2, 32); else if (lpd == 16) DISPATCH(2, 16); else DISPATCH(2, 8); }
-    else { if (lpd == 32) DISPATCH(3, 32); else if (lpd == 16) DISPATCH(3, 16); else DISPATCH(3, 8); }
-#undef DISPATCH
+    const int b = blocks_for(D.n);
+    if (a.g.kx == 1) k_rates<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else if (a.g.kx == 2) k_rates<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else k_rates<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
     count_launch();
     SPH_LAUNCH_CHECK("k_rates");
     return SPH_OK;

@@ -24,8 +24,8 @@
 
 namespace sphgb {
 
-constexpr int kQueue = 64;      // per-warp pair queue entries (2 x 32 lanes)
-constexpr int kPairBlock = 256; // threads per block of the pair kernels
+constexpr int kPairBlock = 128; // threads per block of the pair kernels
+constexpr int kMaxListSlots = 64; // (dst, src) lists whose maxima are tracked
 
 struct Grid {
     int bx0 = 0, by0 = 0, bz0 = 0; // origin of the dense grid (internal cell coords)
@@ -54,6 +54,22 @@ struct ArraySnap {
     int64_t ref_n = -1;     // particle count the refcell entries belong to
 };
 
+// Neighbour list of one (destination, source) pair of arrays: entry k of
+// destination slot s at nbr[k * stride + s] (k-major, coalesced for
+// consecutive destinations), count in cnt[s].  Destinations with more than
+// cap neighbours keep the first cap and are completed by a re-traversal.
+struct NbrList {
+    uint32_t *nbr = nullptr;
+    int *cnt = nullptr;
+    int *maxcnt = nullptr;   // device: largest count of the last list build
+    int64_t entries = 0;     // allocated entries
+    int64_t stride = 0;
+    int64_t stride_cap = 0;  // allocated count slots
+    int cap = 0;
+    long long build = -1;    // build id the list belongs to
+    int seen_max = 0;        // largest count observed (host copy)
+};
+
 }  // namespace sphgb
 
 struct sph_ctx {
@@ -74,6 +90,9 @@ struct sph_ctx {
     int64_t *d_cnt = nullptr;           // int64 scratch (mean neighbours)
     int64_t cnt_cap = 0;
     double cell_size_ref = 0;           // reference cell size of the jump check
+    long long build_id = 0;             // incremented by every neighbour build
+    std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
+    int *h_maxcnt = nullptr;            // pinned scratch for list maxima
 };
 
 namespace sphgb {
@@ -118,6 +137,9 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
                        double *const *out);
 int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
 int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
+int list_maxima_async(sph_ctx *ctx);
+void list_maxima_collect(sph_ctx *ctx);
+void free_lists(sph_ctx *ctx);
 
 // ---------------------------------------------------------------------------
 // device helpers
@@ -143,17 +165,6 @@ struct CSum {
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
-
-// butterfly reduction of a compensated sum over the LPD lanes of a group
-template <int LPD>
-__device__ __forceinline__ void group_reduce(CSum &c) {
-#pragma unroll
-    for (int off = LPD / 2; off > 0; off >>= 1) {
-        float ohi = __shfl_xor_sync(0xffffffffu, c.hi, off);
-        float olo = __shfl_xor_sync(0xffffffffu, c.lo, off);
-        c.merge(ohi, olo);
-    }
-}
 
 // cubic spline normalisation for h = 1 (base/kernels.pyx:437-443)
 __device__ __forceinline__ float cubic_fac(int dim, float ih) {
@@ -195,126 +206,82 @@ struct SrcDev {
     const float4 *posm, *velh, *st, *nrm, *tan;
     const int *cstart, *perm;
     const double *x, *y, *z;
+    const uint32_t *nbr;   // k-major neighbour list of (dest, this source)
+    const int *ncnt;       // neighbour count per dest slot
     uint32_t flags;
     float alpha, beta, eta2, eps, delp;
 };
 
-// Per-destination data shared by the LPD lanes of a group.
-struct DestCtx {
-    float xi_x, xi_y, xi_z; // cell-local offsets
-    int cx, cy, cz;         // dense grid coords of the dest cell
-    float r2lo, r2hi;       // FP32 accept / reject bands
-    double px, py, pz;      // FP64 position (band recheck)
-    double radius2;         // (radius_scale*h)^2 in FP64
-    bool active;            // has a candidate range at all
+// Neighbour-list entry: source slot j in the low bits, stencil offset code
+// (dx+K) + (2K+1)((dy+K) + (2K+1)(dz+K)) in the high CODE_BITS bits.
+template <int K>
+struct Code {
+    static constexpr int W = 2 * K + 1;
+    static constexpr int N = W * W * W;
+    static constexpr int BITS = (N <= 32) ? 5 : (N <= 128 ? 7 : 9);
+    static constexpr int SHIFT = 32 - BITS;
+    static constexpr uint32_t JMASK = (1u << SHIFT) - 1u;
 };
 
-// Queue entry: relative vector dest-src (FP32) and the mass of the source.
-struct QEntry {
-    float4 r; // rx, ry, rz, m_j
+// Destination state of one thread (cell-local FP32 offsets, dense cell).
+struct DestPos {
+    float xi_x, xi_y, xi_z;
+    int cx, cy, cz;
+    float r2lo, r2hi;   // FP32 accept / reject bands around (radius_scale h)^2
+    double radius2;     // exact FP64 threshold
+    int orig;           // original index (FP64 recheck)
 };
 
-// Warp-cooperative traversal of the stencil of each group's destination.
-// Every lane of the warp must call this with identical (uniform) grid data;
-// groups of LPD lanes own one destination each.  Candidates are tested by
-// all lanes in parallel; hits are compacted into a per-group queue in shared
-// memory and handed to `proc(j, entry)` LPD at a time, so the pair body runs
-// with all lanes busy.
-template <int KX, int LPD, class Proc>
-__device__ __forceinline__ void traverse(const Grid &g, const SrcDev &S, const DestCtx &d,
-                                         int *qj, QEntry *qe, Proc &proc) {
-    const int lane = threadIdx.x & 31;
-    const int grp = lane / LPD;
-    const int gl = lane % LPD;
-    const unsigned gshift = grp * LPD;
-    const unsigned gbits = (LPD == 32) ? 0xffffffffu : (((1u << (LPD % 32)) - 1u) << gshift);
-    int *myqj = qj + grp * 2 * LPD;
-    QEntry *myqe = qe + grp * 2 * LPD;
-    int qn = 0;
-
-    auto flush = [&](bool all) {
-        // process min(qn, LPD) entries of every group, then shift the rest down
-        while (__any_sync(0xffffffffu, all ? (qn > 0) : (qn >= LPD))) {
-            int take = min(qn, LPD);
-            if (gl < take) proc(myqj[gl], myqe[gl]);
-            int rest = qn - take;
-            int mj = 0;
-            QEntry me;
-            bool mv = gl < rest;
-            if (mv) {
-                mj = myqj[LPD + gl];
-                me = myqe[LPD + gl];
-            }
-            __syncwarp();
-            if (mv) {
-                myqj[gl] = mj;
-                myqe[gl] = me;
-            }
-            __syncwarp();
-            qn = rest;
-            if (!all) break;
-        }
-    };
-
+// Visit every source particle within radius of the destination, in a fixed
+// order (stencil rows in (dz, dy) order, ascending sorted slot within a
+// row).  fn(j, rx, ry, rz, code) gets r = x_dest - x_src in FP32.  The FP32
+// distance is trusted outside a +-1e-5 relative band around the threshold;
+// inside it the FP64 test of base/nnps.pyx:337-353 decides, so the set is
+// exactly the reference's.
+template <int KX, class Fn>
+__device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
+                                               const double *dx64, const double *dy64,
+                                               const double *dz64, Fn &&fn) {
     const float csf = g.cs_f;
+    double px = 0.0, py = 0.0, pz = 0.0;
+    bool have64 = false;
     for (int dz = -g.kz; dz <= g.kz; ++dz) {
         for (int dy = -g.ky; dy <= g.ky; ++dy) {
-            int rs = 0, re = 0;
+            const int64_t rowbase = (int64_t)g.nx * ((d.cy + dy) + (int64_t)g.ny * (d.cz + dz));
+            const int64_t c0 = rowbase + d.cx - KX;
+            const int rs = S.cstart[c0];
+            const int re = S.cstart[c0 + 2 * KX + 1];
             int bnd[2 * KX];
-            if (d.active) {
-                int64_t rowbase = (int64_t)g.nx * ((d.cy + dy) + (int64_t)g.ny * (d.cz + dz));
-                int64_t c0 = rowbase + d.cx - KX;
-                rs = S.cstart[c0];
 #pragma unroll
-                for (int t = 0; t < 2 * KX; ++t) bnd[t] = S.cstart[c0 + t + 1];
-                re = S.cstart[c0 + 2 * KX + 1];
-            } else {
+            for (int t = 0; t < 2 * KX; ++t) bnd[t] = S.cstart[c0 + t + 1];
+            const float sy = -(float)dy * csf, sz = -(float)dz * csf;
+            const int code_yz = (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
+            for (int j = rs; j < re; ++j) {
+                const float4 pj = S.posm[j];
+                int t = 0;
 #pragma unroll
-                for (int t = 0; t < 2 * KX; ++t) bnd[t] = 0;
-            }
-            const float sy = -(float)dy * csf;
-            const float sz = -(float)dz * csf;
-            int rounds = (re - rs + LPD - 1) / LPD;
-            int maxr = __reduce_max_sync(0xffffffffu, rounds);
-            for (int r = 0; r < maxr; ++r) {
-                int j = rs + r * LPD + gl;
-                bool hit = false;
-                float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (j < re) {
-                    float4 pj = S.posm[j];
-                    int t = 0;
-#pragma unroll
-                    for (int b = 0; b < 2 * KX; ++b) t += (j >= bnd[b]) ? 1 : 0;
-                    float sx = -(float)(t - KX) * csf;
-                    float rx = (d.xi_x - pj.x) + sx;
-                    float ry = (d.xi_y - pj.y) + sy;
-                    float rz = (d.xi_z - pj.z) + sz;
-                    float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                    hit = r2 < d.r2lo;
-                    if (!hit && r2 <= d.r2hi) {
-                        int oj = S.perm[j];
-                        hit = exact_within(S.x ? S.x[oj] : 0.0, S.y ? S.y[oj] : 0.0,
-                                           S.z ? S.z[oj] : 0.0, d.px, d.py, d.pz, d.radius2);
+                for (int b = 0; b < 2 * KX; ++b) t += (j >= bnd[b]) ? 1 : 0;
+                const float rx = (d.xi_x - pj.x) - (float)(t - KX) * csf;
+                const float ry = (d.xi_y - pj.y) + sy;
+                const float rz = (d.xi_z - pj.z) + sz;
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                bool hit = r2 < d.r2lo;
+                if (!hit && r2 <= d.r2hi) {
+                    if (!have64) {
+                        px = ld0(dx64, d.orig); py = ld0(dy64, d.orig); pz = ld0(dz64, d.orig);
+                        have64 = true;
                     }
-                    e = make_float4(rx, ry, rz, pj.w);
+                    const int oj = S.perm[j];
+                    hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), px, py, pz,
+                                       d.radius2);
                 }
-                unsigned m = __ballot_sync(0xffffffffu, hit);
-                unsigned gm = (m & gbits) >> gshift;
-                if (hit) {
-                    int pos = qn + __popc(gm & ((1u << gl) - 1u));
-                    myqj[pos] = j;
-                    myqe[pos].r = e;
-                }
-                qn += __popc(gm);
-                __syncwarp();
-                flush(false);
+                if (hit) fn(j, rx, ry, rz, t + code_yz, pj.w);
             }
         }
     }
-    flush(true);
 }
 
-// Set up the DestCtx of sorted dest slot ds (all lanes of the group call it).
+// Dense-grid coordinates of a cell key.
 __device__ __forceinline__ void decode_cell(const Grid &g, int key, int &cx, int &cy, int &cz) {
     cx = key % g.nx;
     int rest = key / g.nx;

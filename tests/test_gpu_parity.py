@@ -263,3 +263,35 @@ def test_invariants_mass_exact():
     assert inv1["mass"] == inv0["mass"]
     assert inv1["count"] == len(props["x"])
     assert abs(inv0["mass"] - props["m"].sum()) <= 1e-12 * props["m"].sum()
+
+
+def test_list_overflow_retraversal_matches():
+    """Destinations with more neighbours than the list capacity are
+    completed by re-traversal; results must not change."""
+    _need_gpu()
+    import subprocess
+    import sys
+    code = r'''
+import sys, numpy as np
+sys.path.insert(0, ".")
+import oracle, pysph_gb300
+from pysph_gb300 import workloads as W
+from tests.golden_util import normwise
+props = W.cube_lattice(8000, seed=5)
+s, particles = W.setup_cube(pysph_gb300.api(), props)
+s.integrator.integrate(1e-4)
+pa = particles.arrays[0]
+prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+prob.integrate_rk2(1e-4)
+for p in ("rho", "p"):
+    assert normwise(pa.get(p), prob.arrays["fluid"][p]) < 1e-5, p
+for p in ("x", "u", "w"):
+    assert normwise(pa.get(p) - props[p], prob.arrays["fluid"][p] - props[p]) < 1e-5, p
+print("ok")
+'''
+    import os
+    env = dict(os.environ, SPH_LIST_CAP="7")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]
