@@ -35,7 +35,7 @@ EXPORTS = (
     "sph_version", "sph_nnps_build", "sph_nnps_count", "sph_nnps_fill",
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
-    "sph_launch_count",
+    "sph_launch_count", "sph_invariants_noalloc",
 )
 
 
@@ -115,6 +115,7 @@ def load_library(build_if_missing=True):
         L.sph_error_word.argtypes = [vp, P(ctypes.c_uint32)]
         L.sph_mean_neighbours.argtypes = [vp, i32, i32, P(d)]
         L.sph_launch_count.argtypes = [P(i64)]
+        L.sph_invariants_noalloc.argtypes = [P(ArrayView), P(d), vp]
         for name in EXPORTS:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
