@@ -45,11 +45,11 @@ DT = 1e-4
 #   rates:   posm+velh+st 48 B read, FP64 velocity 24 B read (position
 #            stepping), FP64 rates 48 B written                    = 120 B
 #   density: posm+velh 32 B read, FP64 rho,p,cs 24 B + st 16 B written = 72 B
-ALG_BYTES = {"RatesStage": 120.0, "DensityStage": 72.0}
+ALG_BYTES = {"RatesStage": 120.0, "DensityStage": 72.0, "ListStage": 8.0}
 # Survey algorithmic bytes of a whole RK2 step per particle (3D)
 STEP_ALG_BYTES = 694.0
 # FLOPs per neighbour pair: density 24, momentum 72 (FMA = 2)
-PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0}
+PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 

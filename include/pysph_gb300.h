@@ -139,6 +139,13 @@ int sph_nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t 
 int sph_nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
                   int64_t *index);
 
+/* Build (if stale) the neighbour lists of destination dst among each of the
+ * nsrc sources for the current neighbour build -- the counterpart of the
+ * reference locator's cache update, base/nnps.pyx:566-620.  sph_density and
+ * sph_rates build missing lists themselves; this entry point lets a caller
+ * do it ahead of time. */
+int sph_nbr_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc);
+
 /* Re-gather the sorted FP32 snapshot of one array from (possibly new) device
  * pointers, keeping the cell order of the last build.  For data changed
  * since the build without moving particles across cells (velocities,

@@ -76,7 +76,7 @@ int sph_ctx_create(int dim, sph_ctx **out) {
     c->dim = dim;
     cudaError_t e;
     if ((e = cudaMalloc(&c->d_box, 8 * sizeof(int))) != cudaSuccess ||
-        (e = cudaMalloc(&c->d_hmax, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_hmax, 2 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_err, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
@@ -132,6 +132,11 @@ int sph_nnps_fill(sph_ctx *c, int dst, int src, double radius_scale, const int64
     CHECK_CTX(c);
     if (!offsets || !index) return set_error(SPH_ERR_ARG, "sph_nnps_fill: null output");
     return nnps_fill(c, dst, src, radius_scale, offsets, index);
+}
+
+int sph_nbr_lists(sph_ctx *c, int dst, const int *srcs, int nsrc) {
+    CHECK_CTX(c);
+    return build_lists(c, dst, srcs, nsrc);
 }
 
 int sph_refresh_state(sph_ctx *c, int array, const sph_array_view *view) {

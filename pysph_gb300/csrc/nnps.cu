@@ -40,7 +40,7 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
                       int check_jump, int *box, unsigned long long *hmax, unsigned *err) {
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX};
     int mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-    double hm = 0.0;
+    double hm = 0.0, hn = 1.0e308;
     bool jump = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -52,6 +52,7 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
             mx[d] = max(mx[d], c);
         }
         hm = fmax(hm, a.h[i]);
+        hn = fmin(hn, a.h[i]);
         if (refcell) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -63,7 +64,7 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
     }
     // warp, then block, then one set of atomics per block
     __shared__ int s_mn[3][32], s_mx[3][32];
-    __shared__ double s_h[32];
+    __shared__ double s_h[32], s_hn[32];
     __shared__ int s_j[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -71,12 +72,16 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
         mn[d] = __reduce_min_sync(0xffffffffu, mn[d]);
         mx[d] = __reduce_max_sync(0xffffffffu, mx[d]);
     }
-    for (int off = 16; off > 0; off >>= 1) hm = fmax(hm, __shfl_xor_sync(0xffffffffu, hm, off));
+    for (int off = 16; off > 0; off >>= 1) {
+        hm = fmax(hm, __shfl_xor_sync(0xffffffffu, hm, off));
+        hn = fmin(hn, __shfl_xor_sync(0xffffffffu, hn, off));
+    }
     int anyjump = __any_sync(0xffffffffu, jump) ? 1 : 0;
     if (lane == 0) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) { s_mn[d][wid] = mn[d]; s_mx[d][wid] = mx[d]; }
         s_h[wid] = hm;
+        s_hn[wid] = hn;
         s_j[wid] = anyjump;
     }
     __syncthreads();
@@ -90,7 +95,11 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
             b[d] = __reduce_max_sync(0xffffffffu, b[d]);
         }
         double hh = lane < nw ? s_h[lane] : 0.0;
-        for (int off = 16; off > 0; off >>= 1) hh = fmax(hh, __shfl_xor_sync(0xffffffffu, hh, off));
+        double hl = lane < nw ? s_hn[lane] : 1.0e308;
+        for (int off = 16; off > 0; off >>= 1) {
+            hh = fmax(hh, __shfl_xor_sync(0xffffffffu, hh, off));
+            hl = fmin(hl, __shfl_xor_sync(0xffffffffu, hl, off));
+        }
         int jj = __any_sync(0xffffffffu, lane < nw && s_j[lane]);
         if (lane == 0) {
 #pragma unroll
@@ -99,6 +108,7 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
                 atomicMax(&box[3 + d], b[d]);
             }
             atomicMax(hmax, (unsigned long long)__double_as_longlong(hh));
+            atomicMin(hmax + 1, (unsigned long long)__double_as_longlong(hl));
             if (jj) atomicOr(err, SPH_EFLAG_JUMP);
         }
     }
@@ -109,7 +119,10 @@ __global__ void k_box_init(int *box, unsigned long long *hmax) {
         box[threadIdx.x] = INT_MAX;
         box[3 + threadIdx.x] = INT_MIN;
     }
-    if (threadIdx.x == 0) *hmax = 0ull;
+    if (threadIdx.x == 0) {
+        hmax[0] = 0ull;
+        hmax[1] = (unsigned long long)__double_as_longlong(1.0e308);
+    }
 }
 
 // -------------------------------------------------------------------------
@@ -239,11 +252,11 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
         float xi = (float)fma(-ox, g.cs, ld0(a.x, i));
         float yi = (float)fma(-oy, g.cs, ld0(a.y, i));
         float zi = (float)fma(-oz, g.cs, ld0(a.z, i));
-        posm[s] = make_float4(xi, yi, zi, (float)a.m[i]);
+        posm[s] = make_float4(xi, yi, zi, (float)cx);
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
                               (float)a.h[i]);
         float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
-        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), p);
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
         if (nrm) {
             nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
             tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
@@ -402,13 +415,15 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         }
         if (v.n == 0) continue;
         int jb = (check_jump && same_layout) ? 1 : 0;
-        k_box<<<grid_blocks(v.n, kThreads, 2), kThreads, 0, st>>>(v, inv_cs, inv_cs_ref, A.refcell, jb,
+        k_box<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(v, inv_cs, inv_cs_ref, A.refcell, jb,
                                                                ctx->d_box, ctx->d_hmax, ctx->d_err);
         count_launch();
         SPH_LAUNCH_CHECK("k_box");
     }
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box, ctx->d_box, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 6, ctx->d_hmax, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 10, ctx->d_hmax + 1, sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, st));
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     {
@@ -426,13 +441,16 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     for (int a = 0; a < narrays; ++a) total_n += arrays[a].n;
     if (total_n == 0) return set_error(SPH_ERR_ARG, "nnps_build: no particles");
 
-    double hmax;
+    double hmax, hmin;
     memcpy(&hmax, ctx->h_box + 6, sizeof(hmax));
+    memcpy(&hmin, ctx->h_box + 10, sizeof(hmin));
     Grid g;
     g.cs = cs;
     g.inv_cs = inv_cs;
     g.cs_f = (float)cs;
     g.radius_scale = radius_scale;
+    g.uniform_h = (hmin == hmax) ? 1 : 0;
+    g.h_uniform = (float)hmax;
     int k = (int)std::ceil(radius_scale * hmax * inv_cs - 1e-9);
     if (k < 1) k = 1;
     if (k > 3)
@@ -453,6 +471,8 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     if (nx * ny > kMaxCells || nx * ny * nz > kMaxCells)
         return set_error(SPH_ERR_GRID,
                          "nnps_build: particle extent needs more than 2^27 grid cells");
+    if (nx > (1 << 24))
+        return set_error(SPH_ERR_GRID, "nnps_build: more than 2^24 cells along x");
     g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
     g.ncells = nx * ny * nz;
     ctx->grid = g;

@@ -32,7 +32,7 @@ struct DestDev {
     const float4 *posm, *velh, *st;
     const int *skey, *perm;
     const int64_t *tag;
-    const double *x, *y, *z, *u, *v, *w, *h;
+    const double *x, *y, *z, *u, *v, *w, *h, *p;
     int64_t n;
 };
 
@@ -102,31 +102,48 @@ __device__ __forceinline__ void fill_shift_table(float4 *tab, const Grid &g) {
     __syncthreads();
 }
 
-// Stream the neighbours of dest slot s from the list, then (if the list
-// overflowed) the remaining ones by re-traversal, calling fn(j, rx, ry, rz, mj).
-template <int KX, class Fn>
+// Stream the neighbours of dest slot s from the list in batches of B (the
+// B list entries and then the B neighbour positions are loaded before any is
+// used, so the dependent loads overlap), then -- if the list overflowed --
+// the remaining ones by re-traversal.  fn(ok, j, rx, ry, rz) is called for
+// every slot of a batch; ok is false for the padding of the last batch (its
+// data are those of a valid neighbour, its contribution must be dropped).
+// done() is called after every batch.
+template <int KX, int B, class Fn, class Done>
 __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int cap, int64_t stride,
                                            int s, const DestPos &d, const float4 *tab,
-                                           const DestDev &D, Fn &&fn) {
+                                           const DestDev &D, Fn &&fn, Done &&done) {
     using C = Code<KX>;
     const int c = S.ncnt[s];
     const int m = min(c, cap);
-    for (int k = 0; k < m; ++k) {
-        const uint32_t e = S.nbr[(int64_t)k * stride + s];
-        const int j = (int)(e & C::JMASK);
-        const float4 sh = tab[e >> C::SHIFT];
-        const float4 pj = S.posm[j];
-        fn(j, (d.xi_x - pj.x) + sh.x, (d.xi_y - pj.y) + sh.y, (d.xi_z - pj.z) + sh.z, pj.w);
+    const uint32_t *lst = S.nbr + s;
+    for (int k = 0; k < m; k += B) {
+        uint32_t e[B];
+        e[0] = lst[(int64_t)k * stride];
+#pragma unroll
+        for (int b = 1; b < B; ++b) e[b] = (k + b < m) ? lst[(int64_t)(k + b) * stride] : e[0];
+        float4 p[B], sh[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            p[b] = S.posm[e[b] & C::JMASK];
+            sh[b] = tab[e[b] >> C::SHIFT];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+            fn(k + b < m, (int)(e[b] & C::JMASK), (d.xi_x - p[b].x) + sh[b].x,
+               (d.xi_y - p[b].y) + sh[b].y, (d.xi_z - p[b].z) + sh[b].z);
+        done();
     }
     if (c > cap) {
         int skip = cap;
         for_neighbours<KX>(g, S, d, D.x, D.y, D.z,
-                           [&](int j, float rx, float ry, float rz, int, float mj) {
+                           [&](int j, float rx, float ry, float rz, int) {
                                if (skip > 0) {
                                    --skip;
                                    return;
                                }
-                               fn(j, rx, ry, rz, mj);
+                               fn(true, j, rx, ry, rz);
+                               done();
                            });
     }
 }
@@ -146,7 +163,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
             const int cap = A.cap;
             const int64_t stride = A.stride;
             for_neighbours<KX>(A.g, A.s, d, A.d.x, A.d.y, A.d.z,
-                               [&](int j, float, float, float, int code, float) {
+                               [&](int j, float, float, float, int code) {
                                    if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                                    ++c;
                                });
@@ -172,16 +189,29 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
     if (real) {
         const float hi = A.d.velh[s].w;
         const int dim = A.dim;
+        const bool uh = A.g.uniform_h != 0;
+        const float ihi = __fdividef(1.f, hi);
+        const float faci = cubic_fac(dim, ihi);
+        float part = 0.f;
         for (int si = 0; si < A.nsrc; ++si) {
             const SrcDev &S = A.s[si];
-            for_listed<KX>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
-                           [&](int j, float rx, float ry, float rz, float mj) {
-                               const float hab = 0.5f * (hi + S.velh[j].w);
-                               const float ih = __fdividef(1.f, hab);
-                               const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                               const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                               rho.add(cubic_w(r * ih) * cubic_fac(dim, ih) * mj);
-                           });
+            for_listed<KX, 4>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+                [&](bool ok, int j, float rx, float ry, float rz) {
+                    const float mj = S.st[j].w;
+                    float ih = ihi, fac = faci;
+                    if (!uh) {
+                        ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
+                        fac = cubic_fac(dim, ih);
+                    }
+                    const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                    const float w = cubic_w(r * ih) * fac * mj;
+                    part += ok ? w : 0.f;
+                },
+                [&]() {
+                    rho.add(part);
+                    part = 0.f;
+                });
         }
     }
     const int orig = d.orig;
@@ -203,11 +233,12 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
         A.cs_out[orig] = (double)cf;
     }
     if (A.st_out) {
+        const float4 old = A.st_out[s];
         if (A.tait) {
-            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, pf);
+            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, old.w);
         } else {
-            const float4 old = A.st_out[s];
-            A.st_out[s] = make_float4(rf, old.w / (rf * rf), old.z, old.w);
+            const float pold = (float)ld0(A.d.p, orig);
+            A.st_out[s] = make_float4(rf, pold / (rf * rf), old.z, old.w);
         }
     }
 }
@@ -229,48 +260,55 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     if (real) {
         const float4 vi = A.d.velh[s];
         const float4 sti = A.d.st[s];
-        const float mi = A.d.posm[s].w;
-        const float hi = vi.w, rhoi = sti.x, pri = sti.y, ci = sti.z;
+        const float hi = vi.w, rhoi = sti.x, pri = sti.y, ci = sti.z, mi = sti.w;
         const int dim = A.dim;
+        const bool uh = A.g.uniform_h != 0;
+        const float ihi = __fdividef(1.f, hi);
+        const float faci = cubic_fac(dim, ihi);
+        float pax = 0.f, pay = 0.f, paz = 0.f, pxx = 0.f, pxy = 0.f, pxz = 0.f;
         for (int si = 0; si < A.nsrc; ++si) {
             const SrcDev &S = A.s[si];
             const uint32_t fl = S.flags;
-            for_listed<KX>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
-                           [&](int j, float rx, float ry, float rz, float mj) {
+            for_listed<KX, 2>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+                [&](bool ok, int j, float rx, float ry, float rz) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 const float4 vj = S.velh[j];
-                const float hab = 0.5f * (hi + vj.w);
-                const float ih = __fdividef(1.f, hab);
+                const float4 stj = S.st[j];
+                const float mj = stj.w;
+                float hab = hi, ih = ihi, fac = faci;
+                if (!uh) {
+                    hab = 0.5f * (hi + vj.w);
+                    ih = __fdividef(1.f, hab);
+                    fac = cubic_fac(dim, ih);
+                }
                 const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
                 const float q = r2 * rinv * ih;
-                const float fac = cubic_fac(dim, ih);
-                if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) {
-                    const float4 stj = S.st[j];
-                    if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC)) {
-                        float t = 0.f;
-                        if (fl & SPH_TERM_PGRAD) t -= mj * (pri + stj.y);
-                        if (fl & SPH_TERM_AVISC) {
-                            const float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
-                            if (dot < 0.f) {
-                                const float cab = 0.5f * (ci + stj.z);
-                                const float rhoab = 0.5f * (rhoi + stj.x);
-                                const float mu = hab * dot / (r2 + S.eta2 * hab * hab);
-                                const float piab = (-S.alpha * cab * mu + S.beta * mu * mu) / rhoab;
-                                t -= mj * piab;
-                            }
-                        }
-                        const float gf = cubic_gfac(q, ih, rinv) * fac * t;
-                        ax.add(gf * rx);
-                        ay.add(gf * ry);
-                        az.add(gf * rz);
+                const float okf = ok ? 1.f : 0.f;
+                if (fl & (SPH_TERM_PGRAD | SPH_TERM_AVISC)) {
+                    float t = 0.f;
+                    if (fl & SPH_TERM_PGRAD) t = -mj * (pri + stj.y);
+                    if (fl & SPH_TERM_AVISC) {
+                        // Pi_ab only for approaching pairs (v_ab . r_ab < 0), as a select
+                        const float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+                        const bool neg = dot < 0.f;
+                        const float den = neg ? fmaf(S.eta2 * hab, hab, r2) : 1.f;
+                        const float mu = neg ? __fdividef(hab * dot, den) : 0.f;
+                        const float cab = 0.5f * (ci + stj.z);
+                        const float rhoab = 0.5f * (rhoi + stj.x);
+                        const float piab = __fdividef(fmaf(S.beta * mu, mu, -S.alpha * cab * mu), rhoab);
+                        t -= mj * (neg ? piab : 0.f);
                     }
-                    if (fl & SPH_TERM_XSPH) {
-                        const float rhoab = 0.5f * (stj.x + rhoi);
-                        const float temp = mj * (cubic_w(q) * fac) / rhoab * S.eps;
-                        xx.add(temp * (vj.x - vi.x));
-                        xy.add(temp * (vj.y - vi.y));
-                        xz.add(temp * (vj.z - vi.z));
-                    }
+                    const float gf = cubic_gfac(q, ih, rinv) * fac * t * okf;
+                    pax = fmaf(gf, rx, pax);
+                    pay = fmaf(gf, ry, pay);
+                    paz = fmaf(gf, rz, paz);
+                }
+                if (fl & SPH_TERM_XSPH) {
+                    const float rhoab = 0.5f * (stj.x + rhoi);
+                    const float temp = __fdividef(mj * (cubic_w(q) * fac), rhoab) * S.eps * okf;
+                    pxx = fmaf(temp, vj.x - vi.x, pxx);
+                    pxy = fmaf(temp, vj.y - vi.y, pxy);
+                    pxz = fmaf(temp, vj.z - vi.z, pxz);
                 }
                 if (fl & SPH_TERM_BFORCE) {
                     const float4 nj = S.nrm[j], tj = S.tan[j];
@@ -293,10 +331,17 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                             nforce = 0.f;
                         force = (mj / (mi + mj)) * nforce * tforce * beta;
                     }
-                    ax.add(force * nj.x);
-                    ay.add(force * nj.y);
-                    az.add(force * nj.z);
+                    if (ok) {
+                        pax += force * nj.x;
+                        pay += force * nj.y;
+                        paz += force * nj.z;
+                    }
                 }
+            },
+            [&]() {
+                ax.add(pax); ay.add(pay); az.add(paz);
+                xx.add(pxx); xy.add(pxy); xz.add(pxz);
+                pax = pay = paz = pxx = pxy = pxz = 0.f;
             });
         }
     }
@@ -328,6 +373,7 @@ DestDev make_dest(const ArraySnap &D) {
     d.x = D.view.x; d.y = D.view.y; d.z = D.view.z;
     d.u = D.view.u; d.v = D.view.v; d.w = D.view.w;
     d.h = D.view.h;
+    d.p = D.view.p;
     d.n = D.n;
     return d;
 }
@@ -454,6 +500,20 @@ void free_lists(sph_ctx *ctx) {
         cudaFree(L.maxcnt);
     }
     ctx->lists.clear();
+}
+
+int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc) {
+    if (!ctx->built) return set_error(SPH_ERR_STATE, "lists: no neighbour build");
+    const int na = (int)ctx->arrays.size();
+    if (dst < 0 || dst >= na || nsrc < 0 || (nsrc > 0 && !srcs))
+        return set_error(SPH_ERR_ARG, "lists: bad destination / sources");
+    for (int i = 0; i < nsrc; ++i) {
+        if (srcs[i] < 0 || srcs[i] >= na) return set_error(SPH_ERR_ARG, "lists: bad source");
+        NbrList *L;
+        const int rc = ensure_list(ctx, dst, srcs[i], &L);
+        if (rc) return rc;
+    }
+    return SPH_OK;
 }
 
 int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,

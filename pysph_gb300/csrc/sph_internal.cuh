@@ -5,9 +5,9 @@
 //   sorted order (context-owned, cell-major, deterministic within a cell):
 //     perm[s]  -> original index of sorted slot s          int32
 //     skey[s]  -> dense-grid cell of slot s                int32
-//     posm[s]  =  (xi_x, xi_y, xi_z, m)  cell-local FP32 offsets + mass
+//     posm[s]  =  (xi_x, xi_y, xi_z, cx)  cell-local FP32 offsets, dense x cell
 //     velh[s]  =  (u, v, w, h)                              FP32
-//     st[s]    =  (rho, p/rho^2, cs, 0)                     FP32
+//     st[s]    =  (rho, p/rho^2, cs, m)                     FP32
 //     nrm[s], tan[s] (walls only)
 //   per array dense cell table cstart[ncells+1] (exclusive prefix of counts).
 // A row of 2K+1 cells along x is contiguous in the sorted arrays, so one
@@ -36,6 +36,8 @@ struct Grid {
     double inv_cs = 1.0;
     float cs_f = 1.f;
     double radius_scale = 2.0;
+    int uniform_h = 0;             // every particle of every array has the same h
+    float h_uniform = 1.f;
 };
 
 struct ArraySnap {
@@ -137,6 +139,7 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
                        double *const *out);
 int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
 int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
+int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc);
 int list_maxima_async(sph_ctx *ctx);
 void list_maxima_collect(sph_ctx *ctx);
 void free_lists(sph_ctx *ctx);
@@ -234,48 +237,55 @@ struct DestPos {
 
 // Visit every source particle within radius of the destination, in a fixed
 // order (stencil rows in (dz, dy) order, ascending sorted slot within a
-// row).  fn(j, rx, ry, rz, code) gets r = x_dest - x_src in FP32.  The FP32
-// distance is trusted outside a +-1e-5 relative band around the threshold;
-// inside it the FP64 test of base/nnps.pyx:337-353 decides, so the set is
-// exactly the reference's.
+// row).  Each row is first clipped to the chord of the search sphere: rows
+// farther than the radius in (y, z) are skipped and the x extent of the
+// others is cut to the cells the sphere reaches, so the loop over one row is
+// a single contiguous index range.  fn(j, rx, ry, rz, code) gets
+// r = x_dest - x_src in FP32 and the stencil offset code.  The FP32 distance
+// is trusted outside a +-1e-5 relative band around the threshold; inside it
+// the FP64 test of base/nnps.pyx:337-353 decides, so the set is exactly the
+// reference's.  posm[j].w holds the source's dense-grid x cell.
 template <int KX, class Fn>
 __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
                                                const double *dx64, const double *dy64,
                                                const double *dz64, Fn &&fn) {
     const float csf = g.cs_f;
-    double px = 0.0, py = 0.0, pz = 0.0;
-    bool have64 = false;
+    const float inv_cs = 1.f / csf;
+    // pruning radius: the accept/recheck threshold plus a relative margin
+    // that covers FP32 rounding of the slab distances and cell assignment
+    const float R2 = d.r2hi * 1.0002f;
+    const float cxf = (float)d.cx;
     for (int dz = -g.kz; dz <= g.kz; ++dz) {
+        const float ez = fmaxf(0.f, dz > 0 ? (float)dz * csf - d.xi_z
+                                           : (dz < 0 ? d.xi_z - (float)(dz + 1) * csf : 0.f));
+        const float ez2 = ez * ez;
+        if (ez2 > R2) continue;
         for (int dy = -g.ky; dy <= g.ky; ++dy) {
+            const float ey = fmaxf(0.f, dy > 0 ? (float)dy * csf - d.xi_y
+                                               : (dy < 0 ? d.xi_y - (float)(dy + 1) * csf : 0.f));
+            const float d2 = fmaf(ey, ey, ez2);
+            if (d2 > R2) continue;
+            const float half = sqrtf(R2 - d2) * 1.0001f + 1e-5f * csf;
+            const int tlo = max(-KX, (int)floorf((d.xi_x - half) * inv_cs));
+            const int thi = min(KX, (int)floorf((d.xi_x + half) * inv_cs));
             const int64_t rowbase = (int64_t)g.nx * ((d.cy + dy) + (int64_t)g.ny * (d.cz + dz));
-            const int64_t c0 = rowbase + d.cx - KX;
-            const int rs = S.cstart[c0];
-            const int re = S.cstart[c0 + 2 * KX + 1];
-            int bnd[2 * KX];
-#pragma unroll
-            for (int t = 0; t < 2 * KX; ++t) bnd[t] = S.cstart[c0 + t + 1];
-            const float sy = -(float)dy * csf, sz = -(float)dz * csf;
-            const int code_yz = (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
-            for (int j = rs; j < re; ++j) {
+            const int lo = S.cstart[rowbase + d.cx + tlo];
+            const int hi = S.cstart[rowbase + d.cx + thi + 1];
+            const float by = d.xi_y - (float)dy * csf, bz = d.xi_z - (float)dz * csf;
+            const int code_yz = KX + (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
+            for (int j = lo; j < hi; ++j) {
                 const float4 pj = S.posm[j];
-                int t = 0;
-#pragma unroll
-                for (int b = 0; b < 2 * KX; ++b) t += (j >= bnd[b]) ? 1 : 0;
-                const float rx = (d.xi_x - pj.x) - (float)(t - KX) * csf;
-                const float ry = (d.xi_y - pj.y) + sy;
-                const float rz = (d.xi_z - pj.z) + sz;
+                const float dxc = pj.w - cxf;  // exact: small integers in FP32
+                const float rx = fmaf(-dxc, csf, d.xi_x - pj.x);
+                const float ry = by - pj.y, rz = bz - pj.z;
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 bool hit = r2 < d.r2lo;
                 if (!hit && r2 <= d.r2hi) {
-                    if (!have64) {
-                        px = ld0(dx64, d.orig); py = ld0(dy64, d.orig); pz = ld0(dz64, d.orig);
-                        have64 = true;
-                    }
                     const int oj = S.perm[j];
-                    hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), px, py, pz,
-                                       d.radius2);
+                    hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(dx64, d.orig),
+                                       ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
                 }
-                if (hit) fn(j, rx, ry, rz, t + code_yz, pj.w);
+                if (hit) fn(j, rx, ry, rz, code_yz + (int)dxc);
             }
         }
     }

@@ -35,7 +35,7 @@ EXPORTS = (
     "sph_version", "sph_nnps_build", "sph_nnps_count", "sph_nnps_fill",
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
-    "sph_launch_count", "sph_invariants_noalloc",
+    "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
 )
 
 
@@ -106,6 +106,7 @@ def load_library(build_if_missing=True):
         L.sph_nnps_count.argtypes = [vp, i32, i32, d, vp]
         L.sph_nnps_fill.argtypes = [vp, i32, i32, d, vp, vp]
         L.sph_refresh_state.argtypes = [vp, i32, P(ArrayView)]
+        L.sph_nbr_lists.argtypes = [vp, i32, P(i32), i32]
         L.sph_density.argtypes = [vp, i32, P(i32), i32, P(DensityParams), vp, vp, vp]
         L.sph_rates.argtypes = [vp, i32, P(SourceTerm), i32, P(RatesParams), P(vp), P(vp), i32]
         L.sph_tait.argtypes = [vp, i64, vp, vp, d, d, d, vp, vp]

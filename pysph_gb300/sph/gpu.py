@@ -36,6 +36,14 @@ def note_written(cm, pa, names, consistent=False):
             cm.mark_fresh(pa)
 
 
+def nbr_lists(cm, dest, sources):
+    """Build the neighbour lists of ``dest`` among ``sources`` (if stale)."""
+    cm.ensure_current()
+    L = native.lib()
+    srcs = (ctypes.c_int * max(1, len(sources)))(*[cm.slot(s) for s in sources])
+    native.check(L.sph_nbr_lists(cm.context(), cm.slot(dest), srcs, len(sources)), "lists")
+
+
 def density(cm, dest, sources, dim, rho_out, tait=None, p_out=None, cs_out=None):
     """Summation density of ``dest`` from ``sources`` into ``rho_out``;
     with ``tait=(co, ro, gamma)`` also p and cs."""
