@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
-template <int KX>
+template <int KX, bool UH>
 __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ DensityArgs A) {
     __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
     fill_shift_table<KX>(tab, A.g);
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
     if (real) {
         const float hi = A.d.velh[s].w;
         const int dim = A.dim;
-        const bool uh = A.g.uniform_h != 0;
+        const bool uh = UH;
         const float ihi = __fdividef(1.f, hi);
         const float faci = cubic_fac(dim, ihi);
         float part = 0.f;
@@ -248,8 +248,14 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
 // 41-124), XSPH (xsph_funcs.pyx:31-88), Monaghan BF (boundary_funcs.pyx:
 // 54-110), gravity (external_force.pyx:39-45), stepping (position_funcs.pyx)
 // ---------------------------------------------------------------------------
-template <int KX>
+// SPEC 0: any terms, runtime flags; 1: PGrad + AV, uniform h, one source;
+// 2: PGrad + AV + XSPH, uniform h, one source.
+template <int KX, int SPEC>
 __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ RatesArgs A) {
+    constexpr uint32_t SF = SPEC == 1 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC)
+                          : (SPEC == 2 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH) : 0u);
+    constexpr bool MAY_XSPH = SPEC != 1;
+    constexpr bool MAY_BF = SPEC == 0;
     __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
     fill_shift_table<KX>(tab, A.g);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -262,14 +268,15 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         const float4 sti = A.d.st[s];
         const float hi = vi.w, rhoi = sti.x, pri = sti.y, ci = sti.z, mi = sti.w;
         const int dim = A.dim;
-        const bool uh = A.g.uniform_h != 0;
+        const bool uh = SPEC != 0 || A.g.uniform_h != 0;
         const float ihi = __fdividef(1.f, hi);
         const float faci = cubic_fac(dim, ihi);
         float pax = 0.f, pay = 0.f, paz = 0.f, pxx = 0.f, pxy = 0.f, pxz = 0.f;
-        for (int si = 0; si < A.nsrc; ++si) {
+        const int nsrc = SPEC != 0 ? 1 : A.nsrc;
+        for (int si = 0; si < nsrc; ++si) {
             const SrcDev &S = A.s[si];
-            const uint32_t fl = S.flags;
-            for_listed<KX, 2>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+            const uint32_t fl = SPEC != 0 ? SF : S.flags;
+            for_listed<KX, (SPEC != 0 ? 4 : 2)>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 const float4 vj = S.velh[j];
@@ -303,14 +310,14 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                     pay = fmaf(gf, ry, pay);
                     paz = fmaf(gf, rz, paz);
                 }
-                if (fl & SPH_TERM_XSPH) {
+                if (MAY_XSPH && (fl & SPH_TERM_XSPH)) {
                     const float rhoab = 0.5f * (stj.x + rhoi);
                     const float temp = __fdividef(mj * (cubic_w(q) * fac), rhoab) * S.eps * okf;
                     pxx = fmaf(temp, vj.x - vi.x, pxx);
                     pxy = fmaf(temp, vj.y - vi.y, pxy);
                     pxz = fmaf(temp, vj.z - vi.z, pxz);
                 }
-                if (fl & SPH_TERM_BFORCE) {
+                if (MAY_BF && (fl & SPH_TERM_BFORCE)) {
                     const float4 nj = S.nrm[j], tj = S.tan[j];
                     const float xt = rx * tj.x + ry * tj.y + rz * tj.z;
                     const float yn = rx * nj.x + ry * nj.y + rz * nj.z;
@@ -340,8 +347,11 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
             },
             [&]() {
                 ax.add(pax); ay.add(pay); az.add(paz);
-                xx.add(pxx); xy.add(pxy); xz.add(pxz);
-                pax = pay = paz = pxx = pxy = pxz = 0.f;
+                pax = pay = paz = 0.f;
+                if (MAY_XSPH) {
+                    xx.add(pxx); xy.add(pxy); xz.add(pxz);
+                    pxx = pxy = pxz = 0.f;
+                }
             });
         }
     }
@@ -549,9 +559,13 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     a.st_out = own ? D.st : nullptr;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
-    if (a.g.kx == 1) k_density<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else if (a.g.kx == 2) k_density<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else k_density<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    const bool uh = a.g.uniform_h != 0;
+#define DLAUNCH(K) (uh ? k_density<K, true><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                       : k_density<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+    if (a.g.kx == 1) DLAUNCH(1);
+    else if (a.g.kx == 2) DLAUNCH(2);
+    else DLAUNCH(3);
+#undef DLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
     return SPH_OK;
@@ -600,9 +614,18 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
     }
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
-    if (a.g.kx == 1) k_rates<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else if (a.g.kx == 2) k_rates<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else k_rates<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    int spec = 0;
+    if (nterms == 1 && a.g.uniform_h) {
+        if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC)) spec = 1;
+        else if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
+    }
+#define RLAUNCH(K) (spec == 1 ? k_rates<K, 1><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                    : spec == 2 ? k_rates<K, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                                : k_rates<K, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
+    if (a.g.kx == 1) RLAUNCH(1);
+    else if (a.g.kx == 2) RLAUNCH(2);
+    else RLAUNCH(3);
+#undef RLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_rates");
     return SPH_OK;
