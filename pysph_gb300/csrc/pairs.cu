@@ -53,6 +53,10 @@ struct DensityArgs {
     SrcDev s[SPH_MAX_SOURCES];
     int cap[SPH_MAX_SOURCES];
     int64_t stride[SPH_MAX_SOURCES];
+    // per source: build the neighbour list while summing (list is stale)
+    uint32_t *lnbr[SPH_MAX_SOURCES];
+    int *lcnt[SPH_MAX_SOURCES];
+    int *lmax[SPH_MAX_SOURCES];
     int nsrc;
     int dim;
     int tait;
@@ -186,6 +190,10 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
     DestPos d;
     const bool real = load_dest(A.g, A.d, (int)s, d);
     CSum rho;
+    if (!real) {
+        for (int si = 0; si < A.nsrc; ++si)
+            if (A.lnbr[si] != nullptr) A.lcnt[si][s] = 0;
+    }
     if (real) {
         const float hi = A.d.velh[s].w;
         const int dim = A.dim;
@@ -195,6 +203,34 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
         float part = 0.f;
         for (int si = 0; si < A.nsrc; ++si) {
             const SrcDev &S = A.s[si];
+            if (A.lnbr[si] != nullptr) {
+                // first pair pass of this build: test the stencil, write the
+                // list for the passes that follow and sum in the same order
+                using C = Code<KX>;
+                uint32_t *out = A.lnbr[si] + s;
+                const int cap = A.cap[si];
+                const int64_t stride = A.stride[si];
+                int c = 0;
+                for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                    [&](int j, float rx, float ry, float rz, int code) {
+                        if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
+                        ++c;
+                        const float mj = S.st[j].w;
+                        float ih = ihi, fac = faci;
+                        if (!uh) {
+                            ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
+                            fac = cubic_fac(dim, ih);
+                        }
+                        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                        const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                        rho.add(cubic_w(r * ih) * fac * mj);
+                    });
+                A.lcnt[si][s] = c;
+                const unsigned act = __activemask();
+                const int wmax = __reduce_max_sync(act, c);
+                if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.lmax[si], wmax);
+                continue;
+            }
             for_listed<KX, 4>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                     const float mj = S.st[j].w;
@@ -423,13 +459,15 @@ int64_t code_limit(int kx) {
     return kx == 1 ? (1ll << Code<1>::SHIFT) : (kx == 2 ? (1ll << Code<2>::SHIFT) : (1ll << Code<3>::SHIFT));
 }
 
-// Build (if stale) the neighbour list of (dst, src) for the current build.
-int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
+// Allocate / size the neighbour list of (dst, src) for the current build
+// (no launch).  *stale tells whether its contents must be (re)built.
+int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
     const int na = (int)ctx->arrays.size();
     if ((int)ctx->lists.size() < na * na) ctx->lists.resize((size_t)na * na);
     NbrList &L = ctx->lists[(size_t)dst * na + src];
     *out = &L;
-    if (L.build == ctx->build_id) return SPH_OK;
+    *stale = L.build != ctx->build_id;
+    if (!*stale) return SPH_OK;
     ArraySnap &D = ctx->arrays[dst];
     ArraySnap &S = ctx->arrays[src];
     const Grid &g = ctx->grid;
@@ -463,6 +501,18 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
     if (cap_override() > 0) cap = cap_override();
     L.cap = cap;
     L.stride = stride;
+    return SPH_OK;
+}
+
+// Build (if stale) the neighbour list of (dst, src) for the current build.
+int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
+    bool stale = false;
+    int rc = prepare_list(ctx, dst, src, out, &stale);
+    if (rc || !stale) return rc;
+    NbrList &L = **out;
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[src];
+    const Grid &g = ctx->grid;
     if (D.n > 0) {
         ListArgs a{};
         a.g = g;
@@ -471,8 +521,8 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
         a.nbr = L.nbr;
         a.cnt = L.cnt;
         a.maxcnt = L.maxcnt;
-        a.stride = stride;
-        a.cap = cap;
+        a.stride = L.stride;
+        a.cap = L.cap;
         const int b = blocks_for(D.n);
         if (g.kx == 1) k_nbrlist<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
         else if (g.kx == 2) k_nbrlist<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
@@ -537,16 +587,26 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     a.g = ctx->grid;
     a.d = make_dest(D);
     a.nsrc = nsrc;
+    NbrList *built[SPH_MAX_SOURCES] = {nullptr};
     for (int i = 0; i < nsrc; ++i) {
         if (srcs[i] < 0 || srcs[i] >= na) return set_error(SPH_ERR_ARG, "density: bad source");
+        for (int k = 0; k < i; ++k)
+            if (srcs[k] == srcs[i]) return set_error(SPH_ERR_ARG, "density: repeated source");
         NbrList *L;
-        const int rc = ensure_list(ctx, dst, srcs[i], &L);
+        bool stale = false;
+        const int rc = prepare_list(ctx, dst, srcs[i], &L, &stale);
         if (rc) return rc;
         a.s[i] = make_src(ctx->arrays[srcs[i]]);
         a.s[i].nbr = L->nbr;
         a.s[i].ncnt = L->cnt;
         a.cap[i] = L->cap;
         a.stride[i] = L->stride;
+        if (stale) {
+            a.lnbr[i] = L->nbr;
+            a.lcnt[i] = L->cnt;
+            a.lmax[i] = L->maxcnt;
+            built[i] = L;
+        }
     }
     a.dim = prm->dim;
     a.tait = prm->tait;
@@ -568,6 +628,8 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
 #undef DLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
+    for (int i = 0; i < nsrc; ++i)
+        if (built[i]) built[i]->build = ctx->build_id;
     return SPH_OK;
 }
 

@@ -7,7 +7,8 @@ one (``eval`` :432-470), storing every integrating calc's result in its own
 :597-619).  Here ``setup_integrator`` compiles the calc list into stages:
 
 * ``DensityStage``  -- SPHRho over all its sources, fused with an
-  immediately following TaitEquation on the same destination;
+  immediately following TaitEquation on the same destination (the first
+  pair pass after a neighbour build also writes the neighbour lists);
 * ``TaitStage``     -- a TaitEquation on its own (e.g. before SPHRho);
 * ``RatesStage``    -- a maximal run of consecutive integrating calcs on one
   destination (pressure gradient, artificial viscosity, boundary force,
@@ -32,18 +33,6 @@ VEL = ("u", "v", "w")
 POS = ("x", "y", "z")
 VEL_KINDS = ("pgrad", "avisc", "bforce", "gravity")
 POS_KINDS = ("xsph", "step")
-
-
-class ListStage:
-    """Neighbour lists of one destination (the reference locator's cache
-    update); density and rates stages would build them on demand."""
-
-    def __init__(self, dest, sources):
-        self.dest = dest
-        self.sources = list(sources)
-
-    def run(self, integ, kname):
-        gpu.nbr_lists(integ.particles.cell_manager, self.dest, self.sources)
 
 
 class DensityStage:
@@ -215,7 +204,7 @@ class Integrator:
                         if k_name not in calc.dst_writes[k_num]:
                             calc.dst_writes[k_num].append(k_name)
                         self.k_props[calc.id][k_num].append(k_name)
-        self.stages = self._with_lists(self._plan(calcs))
+        self.stages = self._plan(calcs)
         self._integrated = {}
         for st in self.stages:
             if isinstance(st, RatesStage):
@@ -260,24 +249,6 @@ class Integrator:
             stages.append(RatesStage(run))
             i = j
         return stages
-
-    @staticmethod
-    def _with_lists(stages):
-        """Put one list stage per destination before its first pair stage."""
-        out = []
-        seen = set()
-        for st in stages:
-            srcs = []
-            if isinstance(st, DensityStage):
-                srcs = st.calc.sources
-            elif isinstance(st, RatesStage):
-                srcs = [t["src"] for t in st.terms]
-            new = [s for s in srcs if (id(st.dest), id(s)) not in seen]
-            if new:
-                out.append(ListStage(st.dest, new))
-                seen.update((id(st.dest), id(s)) for s in new)
-            out.append(st)
-        return out
 
     def rate_arrays(self, dest, kname):
         return {p: dest.get_device("_rate%s_%s" % (kname[1:], p))

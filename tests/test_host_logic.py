@@ -82,9 +82,8 @@ def test_operation_expansion_and_stage_plan():
                    "bforce_fluid", "gravity_fluid", "step_fluid"]
     kinds = [type(st).__name__ for st in integ.stages]
     # Tait precedes SPHRho, so it is not fused; the integrating run is one stage
-    assert kinds == ["TaitStage", "ListStage", "DensityStage", "ListStage", "RatesStage"]
+    assert kinds == ["TaitStage", "DensityStage", "RatesStage"]
     rs = integ.stages[-1]
-    assert [s.name for s in integ.stages[3].sources] == ["boundary"]
     assert rs.gravity == (0.0, -9.81, 0.0) and rs.add_velocity
     by_src = {t["src"].name: t["kinds"] for t in rs.terms}
     assert by_src == {"fluid": {"pgrad", "avisc"}, "boundary": {"bforce"}}
@@ -97,9 +96,9 @@ def test_operation_expansion_and_stage_plan():
 def test_drop_plan_fuses_density_and_tait():
     s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1))
     st = s.integrator.stages
-    assert [type(x).__name__ for x in st] == ["ListStage", "DensityStage", "RatesStage"]
-    assert st[1].tait is not None
-    assert st[2].terms[0]["kinds"] == {"pgrad", "avisc", "xsph"}
+    assert [type(x).__name__ for x in st] == ["DensityStage", "RatesStage"]
+    assert st[0].tait is not None
+    assert st[1].terms[0]["kinds"] == {"pgrad", "avisc", "xsph"}
 
 
 def test_compute_without_gpu_raises():
