@@ -255,26 +255,30 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
     // that covers FP32 rounding of the slab distances and cell assignment
     const float R2 = d.r2hi * 1.0002f;
     const float cxf = (float)d.cx;
+    const int rowstride_z = g.nx * g.ny;  // < 2^27 cells: 32-bit indices
     for (int dz = -g.kz; dz <= g.kz; ++dz) {
         const float ez = fmaxf(0.f, dz > 0 ? (float)dz * csf - d.xi_z
                                            : (dz < 0 ? d.xi_z - (float)(dz + 1) * csf : 0.f));
         const float ez2 = ez * ez;
         if (ez2 > R2) continue;
+        const int zbase = (d.cz + dz) * rowstride_z + d.cx;
+        const float bz = d.xi_z - (float)dz * csf;
         for (int dy = -g.ky; dy <= g.ky; ++dy) {
             const float ey = fmaxf(0.f, dy > 0 ? (float)dy * csf - d.xi_y
                                                : (dy < 0 ? d.xi_y - (float)(dy + 1) * csf : 0.f));
-            const float d2 = fmaf(ey, ey, ez2);
-            if (d2 > R2) continue;
-            const float half = sqrtf(R2 - d2) * 1.0001f + 1e-5f * csf;
-            const int tlo = max(-KX, (int)floorf((d.xi_x - half) * inv_cs));
-            const int thi = min(KX, (int)floorf((d.xi_x + half) * inv_cs));
-            const int64_t rowbase = (int64_t)g.nx * ((d.cy + dy) + (int64_t)g.ny * (d.cz + dz));
-            const int lo = S.cstart[rowbase + d.cx + tlo];
-            const int hi = S.cstart[rowbase + d.cx + thi + 1];
-            const float by = d.xi_y - (float)dy * csf, bz = d.xi_z - (float)dz * csf;
+            const float rem = R2 - fmaf(ey, ey, ez2);
+            if (rem < 0.f) continue;
+            // chord half-width with a relative margin (covers the rsqrt error)
+            const float half = fmaf(rem * rsqrtf(fmaxf(rem, 1e-30f)), 1.0001f, 1e-5f * csf);
+            const int tlo = max(-KX, __float2int_rd((d.xi_x - half) * inv_cs));
+            const int thi = min(KX, __float2int_rd((d.xi_x + half) * inv_cs));
+            const int c0 = zbase + (d.cy + dy) * g.nx;
+            const int lo = __ldg(S.cstart + c0 + tlo);
+            const int hi = __ldg(S.cstart + c0 + thi + 1);
+            const float by = d.xi_y - (float)dy * csf;
             const int code_yz = KX + (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
             for (int j = lo; j < hi; ++j) {
-                const float4 pj = S.posm[j];
+                const float4 pj = __ldg(S.posm + j);
                 const float dxc = pj.w - cxf;  // exact: small integers in FP32
                 const float rx = fmaf(-dxc, csf, d.xi_x - pj.x);
                 const float ry = by - pj.y, rz = bz - pj.z;

@@ -28,4 +28,8 @@ def choose_subdivision(cell_manager):
             t = pa.get_device(c)
             if t.numel() and float(t.max() - t.min()) > 0:
                 dims = max(dims, k)
-    return DEFAULT_SUBDIVISION[dims]
+    sub = DEFAULT_SUBDIVISION[dims]
+    nmax = max((pa.get_number_of_particles() for pa in cell_manager.arrays_to_bin), default=0)
+    while sub > 1 and nmax >= MAX_PARTICLES[sub]:
+        sub -= 1
+    return sub
