@@ -4,13 +4,17 @@
 reference cell (``cell_size = 2 max h``).  Finer cells cut the candidate
 volume a destination must test (27 cells of (2h)^3 at 1, 125 of h^3 at 2,
 343 of (2h/3)^3 at 3) at the cost of more, shorter rows.  The default comes
-from a per-dimension table measured on GB300 (``bench.py --tune`` re-measures
-it); ``PYSPH_GB300_SUBDIV`` overrides it.
+from a per-dimension table measured on GB300 (1 M-particle 3D lattice: 3.18,
+2.40 and 2.33 ms per RK2 step at subdivisions 1, 2, 3);
+``PYSPH_GB300_SUBDIV`` overrides it.
 """
 import os
 
-# measured defaults: (dimension with extent) -> subdivision
-DEFAULT_SUBDIVISION = {1: 1, 2: 1, 3: 1}
+# measured defaults: (dimensions with extent) -> subdivision
+DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
+# neighbour-list entries hold the source slot in 32 - code bits: at
+# subdivision 3 (343 stencil codes, 9 bits) at most 2^23 source particles
+MAX_PARTICLES = {1: 1 << 27, 2: 1 << 25, 3: 1 << 23}
 
 
 def choose_subdivision(cell_manager):
