@@ -49,6 +49,7 @@ extern "C" {
 /* device error-word bits (sph_error_word) */
 #define SPH_EFLAG_JUMP 1u
 #define SPH_EFLAG_NONFINITE 2u
+#define SPH_EFLAG_BOX 4u      /* batch: a particle left its instance's grid */
 
 #define SPH_MAX_SOURCES 8
 
@@ -189,6 +190,52 @@ int sph_invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
  * SPH_ERR_ARG.  stream: a cudaStream_t (NULL = default stream).  out: 6
  * host doubles as for sph_invariants.  Synchronises the stream. */
 int sph_invariants_noalloc(const sph_array_view *a, double *out, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Batches of independent simulations (no counterpart in the reference,
+ * which runs one simulation per Solver).  All instances share one
+ * operation recipe -- SPHRho (+Tait) of each instance on itself, one set of
+ * rate terms among its own particles, gravity / position stepping, Euler or
+ * RK2 -- and their particles are concatenated in one set of arrays.  Every
+ * instance gets its own dense grid, fixed at set-up over [lo, hi] with a
+ * margin, so a time step needs no host synchronisation and no allocation:
+ * the step is captured once into a CUDA graph and replayed.
+ * --------------------------------------------------------------------- */
+typedef struct sph_batch sph_batch;
+
+typedef struct {
+    int64_t offset, n;    /* particle range of the instance (instances tile [0, n) in order) */
+    double cell_size;     /* reference cell size: radius_scale * max h of the instance */
+    double lo[3], hi[3];  /* region the instance's particles may occupy */
+    int uniform_h;        /* 1 if every particle of the instance has the same h */
+} sph_batch_instance;
+
+typedef struct {
+    int dim;              /* kernel dimension 1..3 (also: integrated components) */
+    int subdiv;           /* grid cells per reference cell, 1..3 */
+    int scheme;           /* 0: Euler (integrator.py:525-573), 1: RK2 (:581-645) */
+    int list_cap;         /* neighbour list capacity per particle (0: default) */
+    double radius_scale;  /* 2 for the cubic spline */
+    double dt;
+    sph_density_params density;  /* SPHRho (+ Tait when density.tait) */
+    sph_source_term term;        /* rate terms among an instance's particles (src unused) */
+    sph_rates_params rates;      /* gravity and position stepping */
+} sph_batch_recipe;
+
+int sph_batch_create(sph_batch **out);
+int sph_batch_destroy(sph_batch *b);
+/* Allocates everything the steps need and uploads the per-instance grids
+ * (synchronises).  all: the concatenated particle arrays (device). */
+int sph_batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instance *inst,
+                    int ninst, const sph_batch_recipe *recipe);
+/* Advance every instance by nsteps time steps on the batch's own stream
+ * (asynchronous).  use_graph: capture the step into a CUDA graph on the
+ * first call and replay it. */
+int sph_batch_step(sph_batch *b, int nsteps, int use_graph);
+/* Wait for the batch's stream. */
+int sph_batch_sync(sph_batch *b);
+/* Read and clear the batch's device error word (SPH_EFLAG_*; synchronises). */
+int sph_batch_error_word(sph_batch *b, uint32_t *out);
 
 /* Read and clear the device error word (synchronises). */
 int sph_error_word(sph_ctx *ctx, uint32_t *out);

@@ -1,0 +1,340 @@
+// Many independent simulations advanced together (sm_103a).
+//
+// The reference runs one simulation per Solver; for many small ones every
+// stage would be a handful of tiny launches.  A batch concatenates the
+// instances' particles into one particle set and gives every instance its
+// own dense grid (cell size from its own smoothing length), fixed at set-up
+// with a margin, so that a whole time step -- neighbour build, density +
+// Tait + neighbour lists, rates, FP64 update -- is a fixed sequence of
+// launches over all instances with no host synchronisation and no
+// allocation.  That sequence is captured once into a CUDA graph and
+// replayed.  Particles that leave their instance's grid or jump more than
+// one reference cell set bits of a device error word instead of stopping
+// the step; sph_batch_error_word reports them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__global__ void k_inst_fill(int *inst_of, int64_t offset, int64_t n, int k) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        inst_of[offset + i] = k;
+}
+
+// keys on the per-instance grids (+ jump check against the instance's
+// reference cell, base/cell.pyx:1422-1437)
+__global__ void k_bkeys(sph_array_view a, const Grid *grids, const double *inv_cs_ref,
+                        const int *inst_of, int *key, int *count, int *refcell, int check_jump,
+                        unsigned *err) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = inst_of[i];
+        const Grid &g = grids[k];
+        const double p[3] = {ld0(a.x, i), ld0(a.y, i), ld0(a.z, i)};
+        int c[3];
+        const int b0[3] = {g.bx0, g.by0, g.bz0};
+        const int nn[3] = {g.nx, g.ny, g.nz};
+        const int kk[3] = {g.kx, g.ky, g.kz};
+        bool out = false;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int v = (int)floor(p[d] * g.inv_cs) - b0[d];
+            // the stencil of a cell reaches k cells beyond it: keep k of margin
+            if (v < kk[d] || v >= nn[d] - kk[d]) {
+                out = true;
+                v = min(max(v, kk[d]), nn[d] - 1 - kk[d]);
+            }
+            c[d] = v;
+        }
+        if (out) atomicOr(err, SPH_EFLAG_BOX);
+        const int kc = (int)g.cell_base + c[0] + g.nx * (c[1] + g.ny * c[2]);
+        key[i] = kc;
+        atomicAdd(&count[kc], 1);
+        const double ir = inv_cs_ref[k];
+        bool jump = false;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int rc = (int)floor(p[d] * ir);
+            if (check_jump && abs(rc - refcell[3 * i + d]) > 1) jump = true;
+            refcell[3 * i + d] = rc;
+        }
+        if (jump) atomicOr(err, SPH_EFLAG_JUMP);
+    }
+}
+
+__global__ void k_breorder(sph_array_view a, const Grid *grids, const int *inst_of,
+                           const int *perm, const int *key, int *skey, int *sinst, float4 *posm,
+                           float4 *velh, float4 *st) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int i = perm[s];
+        const int k = inst_of[i];
+        const Grid &g = grids[k];
+        const int kl = key[i] - (int)g.cell_base;
+        skey[s] = kl;
+        sinst[s] = k;
+        int cx, cy, cz;
+        decode_cell(g, kl, cx, cy, cz);
+        const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
+        posm[s] = make_float4((float)fma(-ox, g.cs, ld0(a.x, i)), (float)fma(-oy, g.cs, ld0(a.y, i)),
+                              (float)fma(-oz, g.cs, ld0(a.z, i)), (float)cx);
+        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
+                              (float)a.h[i]);
+        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
+    }
+}
+
+}  // namespace
+
+int batch_build(sph_batch *b, int check_jump) {
+    cudaStream_t st = b->stream;
+    const int64_t n = b->view.n;
+    ArraySnap &A = b->snap;
+    SPH_CUDA(cudaMemsetAsync(A.cstart, 0, sizeof(int) * (b->total_cells + 1), st));
+    const int nb = grid_blocks(n, kThreads);
+    k_bkeys<<<nb, kThreads, 0, st>>>(b->view, b->d_grids, b->d_inv_ref, b->inst_of, A.key,
+                                     A.cstart, A.refcell, check_jump && b->steps_built > 0,
+                                     b->d_err);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_bkeys");
+    int rc = scan_exclusive(b->ctx, A.cstart, b->total_cells + 1);
+    if (rc) return rc;
+    SPH_CUDA(cudaMemcpyAsync(A.cursor, A.cstart, sizeof(int) * b->total_cells,
+                             cudaMemcpyDeviceToDevice, st));
+    launch_counting_sort(st, n, b->total_cells, A.key, A.cursor, A.cstart, A.perm);
+    k_breorder<<<nb, kThreads, 0, st>>>(b->view, b->d_grids, b->inst_of, A.perm, A.key, A.skey,
+                                        b->sinst, A.posm, A.velh, A.st);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_breorder");
+    b->steps_built += 1;
+    return SPH_OK;
+}
+
+int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instance *inst,
+                int ninst, const sph_batch_recipe *rec) {
+    if (!all || !inst || ninst <= 0 || !rec) return set_error(SPH_ERR_ARG, "batch: null argument");
+    if (all->n <= 0 || !all->x || !all->h || !all->m || !all->rho || !all->p || !all->cs)
+        return set_error(SPH_ERR_ARG, "batch: particle arrays need x, h, m, rho, p, cs");
+    if (rec->subdiv < 1 || rec->subdiv > 3) return set_error(SPH_ERR_ARG, "batch: subdiv must be 1..3");
+    if (rec->scheme != 0 && rec->scheme != 1) return set_error(SPH_ERR_ARG, "batch: scheme 0 (Euler) or 1 (RK2)");
+    if (rec->dim < 1 || rec->dim > 3) return set_error(SPH_ERR_ARG, "batch: dim must be 1..3");
+    int64_t covered = 0;
+    for (int k = 0; k < ninst; ++k) {
+        if (inst[k].offset != covered || inst[k].n <= 0)
+            return set_error(SPH_ERR_ARG, "batch: instances must tile [0, n) in order");
+        if (!(inst[k].cell_size > 0)) return set_error(SPH_ERR_ARG, "batch: cell_size must be > 0");
+        covered += inst[k].n;
+    }
+    if (covered != all->n) return set_error(SPH_ERR_ARG, "batch: instances must cover every particle");
+    if (all->n >= (int64_t)1 << 23) return set_error(SPH_ERR_NOTSUP, "batch: at most 2^23 particles");
+    b->view = *all;
+    b->rec = *rec;
+    b->ninst = ninst;
+    const int K = rec->subdiv;
+    b->h_grids.assign(ninst, Grid());
+    std::vector<double> inv_ref(ninst);
+    int64_t cells = 0;
+    for (int k = 0; k < ninst; ++k) {
+        Grid &g = b->h_grids[k];
+        g.cs = inst[k].cell_size / K;
+        g.inv_cs = 1.0 / g.cs;
+        g.cs_f = (float)g.cs;
+        g.radius_scale = rec->radius_scale;
+        g.kx = K;
+        g.ky = (inst[k].hi[1] > inst[k].lo[1]) ? K : 0;
+        g.kz = (inst[k].hi[2] > inst[k].lo[2]) ? K : 0;
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = (int)std::floor(inst[k].lo[d] * g.inv_cs);
+            hi[d] = (int)std::floor(inst[k].hi[d] * g.inv_cs);
+        }
+        g.bx0 = lo[0] - g.kx;
+        g.by0 = lo[1] - g.ky;
+        g.bz0 = lo[2] - g.kz;
+        const int64_t nx = (int64_t)hi[0] - lo[0] + 1 + 2 * g.kx;
+        const int64_t ny = (int64_t)hi[1] - lo[1] + 1 + 2 * g.ky;
+        const int64_t nz = (int64_t)hi[2] - lo[2] + 1 + 2 * g.kz;
+        if (nx * ny * nz > ((int64_t)1 << 26) || nx > (1 << 24))
+            return set_error(SPH_ERR_GRID, "batch: an instance's region needs too many cells");
+        g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
+        g.ncells = nx * ny * nz;
+        g.cell_base = cells;
+        g.uniform_h = inst[k].uniform_h ? 1 : 0;
+        cells += g.ncells;
+        inv_ref[k] = 1.0 / inst[k].cell_size;
+    }
+    if (cells >= ((int64_t)1 << 30)) return set_error(SPH_ERR_GRID, "batch: too many cells in total");
+    b->total_cells = cells;
+    b->uniform_h = 1;
+    for (auto &g : b->h_grids) b->uniform_h &= g.uniform_h;
+    cudaStream_t st = b->stream;
+    const int64_t n = all->n;
+    SPH_CUDA(cudaMalloc(&b->d_grids, sizeof(Grid) * ninst));
+    SPH_CUDA(cudaMemcpyAsync(b->d_grids, b->h_grids.data(), sizeof(Grid) * ninst,
+                             cudaMemcpyHostToDevice, st));
+    SPH_CUDA(cudaMalloc(&b->d_inv_ref, sizeof(double) * ninst));
+    SPH_CUDA(cudaMemcpyAsync(b->d_inv_ref, inv_ref.data(), sizeof(double) * ninst,
+                             cudaMemcpyHostToDevice, st));
+    SPH_CUDA(cudaMalloc(&b->inst_of, sizeof(int) * n));
+    SPH_CUDA(cudaMalloc(&b->sinst, sizeof(int) * n));
+    for (int k = 0; k < ninst; ++k) {
+        k_inst_fill<<<grid_blocks(inst[k].n, kThreads), kThreads, 0, st>>>(b->inst_of, inst[k].offset,
+                                                                          inst[k].n, k);
+        count_launch();
+    }
+    ArraySnap &A = b->snap;
+    A.n = n;
+    SPH_CUDA(cudaMalloc(&A.key, sizeof(int) * n));
+    SPH_CUDA(cudaMalloc(&A.perm, sizeof(int) * n));
+    SPH_CUDA(cudaMalloc(&A.skey, sizeof(int) * n));
+    SPH_CUDA(cudaMalloc(&A.posm, sizeof(float4) * n));
+    SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * n));
+    SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * n));
+    SPH_CUDA(cudaMalloc(&A.cstart, sizeof(int) * (cells + 1)));
+    SPH_CUDA(cudaMalloc(&A.cursor, sizeof(int) * (cells + 1)));
+    SPH_CUDA(cudaMalloc(&A.refcell, sizeof(int) * 3 * n));
+    A.view = *all;
+    // scan scratch (sized now: nothing is allocated while a step is captured)
+    {
+        const int64_t ntiles = (cells + 1 + 2047) / 2048 + 1;
+        SPH_CUDA(cudaMalloc(&b->ctx->scan_tmp, sizeof(int) * ntiles));
+        b->ctx->scan_tmp_cap = ntiles;
+    }
+    // neighbour list (built by every first density pass)
+    NbrList &L = b->list;
+    L.cap = rec->list_cap > 0 ? rec->list_cap : (rec->dim == 3 ? 96 : (rec->dim == 2 ? 40 : 16));
+    L.stride = n;
+    SPH_CUDA(cudaMalloc(&L.nbr, sizeof(uint32_t) * n * L.cap));
+    SPH_CUDA(cudaMalloc(&L.cnt, sizeof(int) * n));
+    SPH_CUDA(cudaMalloc(&L.maxcnt, sizeof(int)));
+    SPH_CUDA(cudaMemsetAsync(L.maxcnt, 0, sizeof(int), st));
+    L.entries = n * L.cap;
+    // integrator work arrays: per integrated component, x0 (RK2), rate1, rate2
+    const int ncomp = rec->dim;
+    for (int c = 0; c < 2 * ncomp; ++c) {
+        SPH_CUDA(cudaMalloc(&b->rate1[c], sizeof(double) * n));
+        SPH_CUDA(cudaMalloc(&b->rate2[c], sizeof(double) * n));
+        SPH_CUDA(cudaMalloc(&b->x0[c], sizeof(double) * n));
+    }
+    SPH_CUDA(cudaMalloc(&b->d_err, sizeof(unsigned)));
+    SPH_CUDA(cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), st));
+    SPH_CUDA(cudaStreamSynchronize(st));
+    b->ready = true;
+    return SPH_OK;
+}
+
+// one evaluation: neighbour build, density (+Tait, +lists), rates
+static int batch_eval(sph_batch *b, double *const *rate) {
+    int rc = batch_build(b, 1);
+    if (rc) return rc;
+    rc = batch_density(b);
+    if (rc) return rc;
+    double *acc[3] = {nullptr, nullptr, nullptr}, *pos[3] = {nullptr, nullptr, nullptr};
+    for (int c = 0; c < b->rec.dim; ++c) {
+        pos[c] = rate[c];
+        acc[c] = rate[b->rec.dim + c];
+    }
+    return batch_rates(b, acc, pos);
+}
+
+// state pointers of integrated component c: x, y, z then u, v, w
+static double *state_ptr(sph_batch *b, int c) {
+    const int d = b->rec.dim;
+    const double *p[6] = {b->view.x, b->view.y, b->view.z, b->view.u, b->view.v, b->view.w};
+    return const_cast<double *>(p[c < d ? c : 3 + (c - d)]);
+}
+
+// one time step as a fixed launch sequence (captured into the graph)
+static int batch_step_launches(sph_batch *b) {
+    const int nc = 2 * b->rec.dim;
+    const double dt = b->rec.dt;
+    sph_axpy_line lines[SPH_MAX_AXPY_LINES];
+    int rc;
+    if (b->rec.scheme == 0) {
+        rc = batch_eval(b, b->rate1);
+        if (rc) return rc;
+        for (int c = 0; c < nc; ++c)
+            lines[c] = sph_axpy_line{state_ptr(b, c), nullptr, state_ptr(b, c), b->rate1[c], nullptr, dt, 1};
+        return launch_integrate(b->ctx, b->view.n, lines, nc);
+    }
+    for (int c = 0; c < nc; ++c)
+        lines[c] = sph_axpy_line{b->x0[c], nullptr, state_ptr(b, c), nullptr, nullptr, 0.0, 2};
+    rc = launch_integrate(b->ctx, b->view.n, lines, nc);
+    if (rc) return rc;
+    rc = batch_eval(b, b->rate1);
+    if (rc) return rc;
+    for (int c = 0; c < nc; ++c)
+        lines[c] = sph_axpy_line{state_ptr(b, c), nullptr, b->x0[c], b->rate1[c], nullptr, dt, 1};
+    rc = launch_integrate(b->ctx, b->view.n, lines, nc);
+    if (rc) return rc;
+    rc = batch_eval(b, b->rate2);
+    if (rc) return rc;
+    for (int c = 0; c < nc; ++c)
+        lines[c] = sph_axpy_line{state_ptr(b, c), nullptr, b->x0[c], b->rate1[c], b->rate2[c],
+                                 0.5 * dt, 0};
+    return launch_integrate(b->ctx, b->view.n, lines, nc);
+}
+
+int batch_step(sph_batch *b, int nsteps, int use_graph) {
+    if (!b->ready) return set_error(SPH_ERR_STATE, "batch: not set up");
+    if (nsteps < 0) return set_error(SPH_ERR_ARG, "batch: negative step count");
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; ++s) {
+            const int rc = batch_step_launches(b);
+            if (rc) return rc;
+        }
+        return SPH_OK;
+    }
+    if (!b->graph_exec) {
+        // the first build of a batch fills the jump reference; run one step
+        // outside the graph so every captured build can check jumps
+        if (b->steps_built == 0) {
+            const int rc = batch_step_launches(b);
+            if (rc) return rc;
+            --nsteps;
+        }
+        cudaGraph_t graph = nullptr;
+        SPH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = batch_step_launches(b);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_check(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGraphInstantiate");
+    }
+    for (int s = 0; s < nsteps; ++s) SPH_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));
+    return SPH_OK;
+}
+
+void batch_free(sph_batch *b) {
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    ArraySnap &A = b->snap;
+    cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey); cudaFree(A.posm); cudaFree(A.velh);
+    cudaFree(A.st); cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell);
+    cudaFree(b->d_grids); cudaFree(b->d_inv_ref); cudaFree(b->inst_of); cudaFree(b->sinst);
+    cudaFree(b->list.nbr); cudaFree(b->list.cnt); cudaFree(b->list.maxcnt);
+    for (int c = 0; c < 6; ++c) {
+        cudaFree(b->rate1[c]);
+        cudaFree(b->rate2[c]);
+        cudaFree(b->x0[c]);
+    }
+    cudaFree(b->d_err);
+}
+
+}  // namespace sphgb

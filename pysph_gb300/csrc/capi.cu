@@ -185,6 +185,66 @@ int sph_invariants(sph_ctx *c, const sph_array_view *a, double *out) {
     return invariants(c, a, out);
 }
 
+int sph_batch_create(sph_batch **out) {
+    if (!out) return set_error(SPH_ERR_ARG, "sph_batch_create: null out");
+    sph_batch *b = new (std::nothrow) sph_batch();
+    if (!b) return set_error(SPH_ERR_ARG, "sph_batch_create: out of host memory");
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_check(e, "sph_batch_create: stream");
+    }
+    int rc = sph_ctx_create(3, &b->ctx);
+    if (rc) {
+        cudaStreamDestroy(b->stream);
+        delete b;
+        return rc;
+    }
+    b->ctx->stream = b->stream;
+    *out = b;
+    return SPH_OK;
+}
+
+int sph_batch_destroy(sph_batch *b) {
+    if (!b) return SPH_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    sph_ctx_destroy(b->ctx);
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return SPH_OK;
+}
+
+int sph_batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instance *inst,
+                    int ninst, const sph_batch_recipe *recipe) {
+    if (!b) return set_error(SPH_ERR_ARG, "null sph_batch");
+    if (b->ready) return set_error(SPH_ERR_STATE, "sph_batch_setup: batch already set up");
+    return batch_setup(b, all, inst, ninst, recipe);
+}
+
+int sph_batch_step(sph_batch *b, int nsteps, int use_graph) {
+    if (!b) return set_error(SPH_ERR_ARG, "null sph_batch");
+    return batch_step(b, nsteps, use_graph);
+}
+
+int sph_batch_sync(sph_batch *b) {
+    if (!b) return set_error(SPH_ERR_ARG, "null sph_batch");
+    SPH_CUDA(cudaStreamSynchronize(b->stream));
+    return SPH_OK;
+}
+
+int sph_batch_error_word(sph_batch *b, unsigned *out) {
+    if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_error_word: null argument");
+    if (!b->d_err) { *out = 0; return SPH_OK; }
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream);
+    if (e != cudaSuccess) return cuda_check(e, "sph_batch_error_word");
+    *out = h;
+    return SPH_OK;
+}
+
 int sph_error_word(sph_ctx *c, unsigned *out) {
     CHECK_CTX(c);
     if (!out) return set_error(SPH_ERR_ARG, "sph_error_word: null out");

@@ -328,18 +328,6 @@ int ensure(T **p, int64_t &cap, int64_t need) {
     return SPH_OK;
 }
 
-int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
-    int64_t ntiles = (n + kScanTile - 1) / kScanTile;
-    int rc = ensure(&ctx->scan_tmp, ctx->scan_tmp_cap, ntiles);
-    if (rc) return rc;
-    k_scan_tiles<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
-    k_scan_totals<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, ntiles);
-    k_scan_add<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
-    count_launch(3);
-    SPH_LAUNCH_CHECK("scan");
-    return SPH_OK;
-}
-
 int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
     if (n <= A.cap && A.perm && (!nrm || A.nrm)) return SPH_OK;
     cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
@@ -362,6 +350,25 @@ int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
 }
 
 }  // namespace
+
+int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
+    int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    int rc = ensure(&ctx->scan_tmp, ctx->scan_tmp_cap, ntiles);
+    if (rc) return rc;
+    k_scan_tiles<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    k_scan_totals<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, ntiles);
+    k_scan_add<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    count_launch(3);
+    SPH_LAUNCH_CHECK("scan");
+    return SPH_OK;
+}
+
+void launch_counting_sort(cudaStream_t st, int64_t n, int64_t ncells, const int *key, int *cursor,
+                          const int *cstart, int *perm) {
+    k_scatter<<<grid_blocks(n, kThreads), kThreads, 0, st>>>(n, key, cursor, perm);
+    k_cellsort<<<grid_blocks(ncells, kThreads), kThreads, 0, st>>>(ncells, cstart, perm);
+    count_launch(2);
+}
 
 int grid_blocks(int64_t n, int threads, int per_sm) {
     static int sms = 0;

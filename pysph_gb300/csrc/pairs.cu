@@ -31,6 +31,8 @@ namespace {
 struct DestDev {
     const float4 *posm, *velh, *st;
     const int *skey, *perm;
+    const int *sinst;    // batches: instance of each sorted slot
+    const Grid *grids;   // batches: grid of each instance
     const int64_t *tag;
     const double *x, *y, *z, *u, *v, *w, *h, *p;
     int64_t n;
@@ -95,15 +97,22 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
     return true;
 }
 
-// shift table: code -> -(dx, dy, dz) * cs
+// shift table: code -> -(dx, dy, dz) in cells (times the cell size of the
+// destination's grid when used)
 template <int KX>
-__device__ __forceinline__ void fill_shift_table(float4 *tab, const Grid &g) {
+__device__ __forceinline__ void fill_shift_table(float4 *tab) {
     constexpr int W = 2 * KX + 1;
     for (int c = threadIdx.x; c < W * W * W; c += blockDim.x) {
         const int dx = c % W - KX, dy = (c / W) % W - KX, dz = c / (W * W) - KX;
-        tab[c] = make_float4(-(float)dx * g.cs_f, -(float)dy * g.cs_f, -(float)dz * g.cs_f, 0.f);
+        tab[c] = make_float4(-(float)dx, -(float)dy, -(float)dz, 0.f);
     }
     __syncthreads();
+}
+
+// grid of the destination in slot s
+template <bool BATCH>
+__device__ __forceinline__ const Grid &grid_of(const Grid &single, const DestDev &D, int s) {
+    return BATCH ? D.grids[D.sinst[s]] : single;
 }
 
 // Stream the neighbours of dest slot s from the list in batches of B (the
@@ -132,10 +141,11 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
             p[b] = S.posm[e[b] & C::JMASK];
             sh[b] = tab[e[b] >> C::SHIFT];
         }
+        const float csf = g.cs_f;
 #pragma unroll
         for (int b = 0; b < B; ++b)
-            fn(k + b < m, (int)(e[b] & C::JMASK), (d.xi_x - p[b].x) + sh[b].x,
-               (d.xi_y - p[b].y) + sh[b].y, (d.xi_z - p[b].z) + sh[b].z);
+            fn(k + b < m, (int)(e[b] & C::JMASK), fmaf(sh[b].x, csf, d.xi_x - p[b].x),
+               fmaf(sh[b].y, csf, d.xi_y - p[b].y), fmaf(sh[b].z, csf, d.xi_z - p[b].z));
         done();
     }
     if (c > cap) {
@@ -155,18 +165,19 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
 // ---------------------------------------------------------------------------
 // neighbour list (base/nnps.pyx:525-620 FixedDestNbrParticleLocator cache)
 // ---------------------------------------------------------------------------
-template <int KX>
+template <int KX, bool BATCH>
 __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ ListArgs A) {
     using C = Code<KX>;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int c = 0;
     if (s < A.d.n) {
+        const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
         DestPos d;
-        if (load_dest(A.g, A.d, (int)s, d)) {
+        if (load_dest(g, A.d, (int)s, d)) {
             uint32_t *out = A.nbr + s;
             const int cap = A.cap;
             const int64_t stride = A.stride;
-            for_neighbours<KX>(A.g, A.s, d, A.d.x, A.d.y, A.d.z,
+            for_neighbours<KX>(g, A.s, d, A.d.x, A.d.y, A.d.z,
                                [&](int j, float, float, float, int code) {
                                    if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                                    ++c;
@@ -181,14 +192,15 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
-template <int KX, bool UH>
+template <int KX, bool UH, bool BATCH>
 __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ DensityArgs A) {
     __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
-    fill_shift_table<KX>(tab, A.g);
+    fill_shift_table<KX>(tab);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
+    const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
     DestPos d;
-    const bool real = load_dest(A.g, A.d, (int)s, d);
+    const bool real = load_dest(g, A.d, (int)s, d);
     CSum rho;
     if (!real) {
         for (int si = 0; si < A.nsrc; ++si)
@@ -211,7 +223,7 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                 const int cap = A.cap[si];
                 const int64_t stride = A.stride[si];
                 int c = 0;
-                for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                for_neighbours<KX>(g, S, d, A.d.x, A.d.y, A.d.z,
                     [&](int j, float rx, float ry, float rz, int code) {
                         if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                         ++c;
@@ -231,7 +243,7 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                 if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.lmax[si], wmax);
                 continue;
             }
-            for_listed<KX, 4>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+            for_listed<KX, 4>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                     const float mj = S.st[j].w;
                     float ih = ihi, fac = faci;
@@ -286,25 +298,26 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 // SPEC 0: any terms, runtime flags; 1: PGrad + AV, uniform h, one source;
 // 2: PGrad + AV + XSPH, uniform h, one source.
-template <int KX, int SPEC>
+template <int KX, int SPEC, bool BATCH>
 __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ RatesArgs A) {
     constexpr uint32_t SF = SPEC == 1 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC)
                           : (SPEC == 2 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH) : 0u);
     constexpr bool MAY_XSPH = SPEC != 1;
     constexpr bool MAY_BF = SPEC == 0;
     __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
-    fill_shift_table<KX>(tab, A.g);
+    fill_shift_table<KX>(tab);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
+    const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
     DestPos d;
-    const bool real = load_dest(A.g, A.d, (int)s, d);
+    const bool real = load_dest(g, A.d, (int)s, d);
     CSum ax, ay, az, xx, xy, xz;
     if (real) {
         const float4 vi = A.d.velh[s];
         const float4 sti = A.d.st[s];
         const float hi = vi.w, rhoi = sti.x, pri = sti.y, ci = sti.z, mi = sti.w;
         const int dim = A.dim;
-        const bool uh = SPEC != 0 || A.g.uniform_h != 0;
+        const bool uh = SPEC != 0 || g.uniform_h != 0;
         const float ihi = __fdividef(1.f, hi);
         const float faci = cubic_fac(dim, ihi);
         float pax = 0.f, pay = 0.f, paz = 0.f, pxx = 0.f, pxy = 0.f, pxz = 0.f;
@@ -312,7 +325,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         for (int si = 0; si < nsrc; ++si) {
             const SrcDev &S = A.s[si];
             const uint32_t fl = SPEC != 0 ? SF : S.flags;
-            for_listed<KX, (SPEC != 0 ? 4 : 2)>(A.g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+            for_listed<KX, (SPEC != 0 ? 4 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 const float4 vj = S.velh[j];
@@ -415,6 +428,7 @@ DestDev make_dest(const ArraySnap &D) {
     DestDev d;
     d.posm = D.posm; d.velh = D.velh; d.st = D.st;
     d.skey = D.skey; d.perm = D.perm;
+    d.sinst = nullptr; d.grids = nullptr;
     d.tag = D.view.tag;
     d.x = D.view.x; d.y = D.view.y; d.z = D.view.z;
     d.u = D.view.u; d.v = D.view.v; d.w = D.view.w;
@@ -524,9 +538,9 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
         a.stride = L.stride;
         a.cap = L.cap;
         const int b = blocks_for(D.n);
-        if (g.kx == 1) k_nbrlist<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
-        else if (g.kx == 2) k_nbrlist<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
-        else k_nbrlist<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        if (g.kx == 1) k_nbrlist<1, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        else if (g.kx == 2) k_nbrlist<2, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        else k_nbrlist<3, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
         count_launch();
         SPH_LAUNCH_CHECK("k_nbrlist");
     }
@@ -620,8 +634,8 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     const bool uh = a.g.uniform_h != 0;
-#define DLAUNCH(K) (uh ? k_density<K, true><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                       : k_density<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+#define DLAUNCH(K) (uh ? k_density<K, true, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                       : k_density<K, false, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
     if (a.g.kx == 1) DLAUNCH(1);
     else if (a.g.kx == 2) DLAUNCH(2);
     else DLAUNCH(3);
@@ -681,15 +695,109 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
         if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC)) spec = 1;
         else if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
     }
-#define RLAUNCH(K) (spec == 1 ? k_rates<K, 1><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                    : spec == 2 ? k_rates<K, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                                : k_rates<K, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
+#define RLAUNCH(K) (spec == 1 ? k_rates<K, 1, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                    : spec == 2 ? k_rates<K, 2, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                                : k_rates<K, 0, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
     if (a.g.kx == 1) RLAUNCH(1);
     else if (a.g.kx == 2) RLAUNCH(2);
     else RLAUNCH(3);
 #undef RLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_rates");
+    return SPH_OK;
+}
+
+}  // namespace sphgb
+
+// ---------------------------------------------------------------------------
+// batches: the same kernels over all instances, grid per instance
+// ---------------------------------------------------------------------------
+namespace sphgb {
+
+int batch_density(sph_batch *b) {
+    const sph_batch_recipe &r = b->rec;
+    DensityArgs a{};
+    a.g = b->h_grids[0];
+    a.d = make_dest(b->snap);
+    a.d.sinst = b->sinst;
+    a.d.grids = b->d_grids;
+    a.nsrc = 1;
+    a.s[0] = make_src(b->snap);
+    a.s[0].nbr = b->list.nbr;
+    a.s[0].ncnt = b->list.cnt;
+    a.cap[0] = b->list.cap;
+    a.stride[0] = b->list.stride;
+    // every evaluation follows a neighbour build: the density pass writes the lists
+    a.lnbr[0] = b->list.nbr;
+    a.lcnt[0] = b->list.cnt;
+    a.lmax[0] = b->list.maxcnt;
+    a.dim = r.density.dim;
+    a.tait = r.density.tait;
+    a.co = (float)r.density.co; a.ro = (float)r.density.ro; a.gamma = (float)r.density.gamma;
+    a.rho_out = const_cast<double *>(b->view.rho);
+    a.p_out = const_cast<double *>(b->view.p);
+    a.cs_out = const_cast<double *>(b->view.cs);
+    a.st_out = b->snap.st;
+    const int blocks = blocks_for(b->view.n);
+    const bool uh = b->uniform_h != 0;
+    const int K = r.subdiv;
+#define BDL(K_) (uh ? k_density<K_, true, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                    : k_density<K_, false, true><<<blocks, kPairBlock, 0, b->stream>>>(a))
+    if (K == 1) BDL(1);
+    else if (K == 2) BDL(2);
+    else BDL(3);
+#undef BDL
+    count_launch();
+    SPH_LAUNCH_CHECK("k_density (batch)");
+    return SPH_OK;
+}
+
+int batch_rates(sph_batch *b, double *const *acc, double *const *pos) {
+    const sph_batch_recipe &r = b->rec;
+    RatesArgs a{};
+    a.g = b->h_grids[0];
+    a.d = make_dest(b->snap);
+    a.d.sinst = b->sinst;
+    a.d.grids = b->d_grids;
+    a.nsrc = 1;
+    a.s[0] = make_src(b->snap);
+    a.s[0].nbr = b->list.nbr;
+    a.s[0].ncnt = b->list.cnt;
+    a.cap[0] = b->list.cap;
+    a.stride[0] = b->list.stride;
+    a.s[0].flags = r.term.flags;
+    a.s[0].alpha = (float)r.term.alpha;
+    a.s[0].beta = (float)r.term.beta;
+    a.s[0].eta2 = (float)(r.term.eta * r.term.eta);
+    a.s[0].eps = (float)r.term.eps;
+    a.s[0].delp = (float)r.term.delp;
+    if ((r.term.flags & SPH_TERM_BFORCE))
+        return set_error(SPH_ERR_NOTSUP, "batch: boundary force needs a wall array");
+    a.dim = r.rates.dim;
+    a.add_velocity = r.rates.add_velocity;
+    a.add_gravity = r.rates.add_gravity;
+    a.gx = r.rates.gx; a.gy = r.rates.gy; a.gz = r.rates.gz;
+    a.accumulate = 0;
+    for (int c = 0; c < 3; ++c) {
+        a.acc[c] = acc[c];
+        a.pos[c] = pos[c];
+    }
+    const int blocks = blocks_for(b->view.n);
+    int spec = 0;
+    if (b->uniform_h) {
+        if (r.term.flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC)) spec = 1;
+        else if (r.term.flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
+    }
+    const int K = r.subdiv;
+#define BRL(K_) (spec == 1 ? k_rates<K_, 1, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                 : spec == 2 ? k_rates<K_, 2, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                             : k_rates<K_, 0, true><<<blocks, kPairBlock, 0, b->stream>>>(a))
+    if (K == 1) BRL(1);
+    else if (K == 2) BRL(2);
+    else BRL(3);
+#undef BRL
+    count_launch();
+    SPH_LAUNCH_CHECK("k_rates (batch)");
     return SPH_OK;
 }
 

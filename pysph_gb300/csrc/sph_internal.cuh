@@ -38,6 +38,7 @@ struct Grid {
     double radius_scale = 2.0;
     int uniform_h = 0;             // every particle of every array has the same h
     float h_uniform = 1.f;
+    int64_t cell_base = 0;         // first cell of this grid in a shared cell table
 };
 
 struct ArraySnap {
@@ -97,6 +98,28 @@ struct sph_ctx {
     int *h_maxcnt = nullptr;            // pinned scratch for list maxima
 };
 
+struct sph_batch {
+    cudaStream_t stream = nullptr;
+    sph_ctx *ctx = nullptr;      // stream + scan scratch for the shared launchers
+    sph_array_view view{};
+    sph_batch_recipe rec{};
+    int ninst = 0;
+    std::vector<sphgb::Grid> h_grids;
+    sphgb::Grid *d_grids = nullptr;
+    double *d_inv_ref = nullptr; // 1 / reference cell size per instance
+    int *inst_of = nullptr;      // original particle -> instance
+    int *sinst = nullptr;        // sorted slot -> instance
+    int64_t total_cells = 0;
+    int uniform_h = 1;
+    sphgb::ArraySnap snap;
+    sphgb::NbrList list;
+    double *rate1[6] = {nullptr}, *rate2[6] = {nullptr}, *x0[6] = {nullptr};
+    unsigned *d_err = nullptr;
+    long long steps_built = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool ready = false;
+};
+
 namespace sphgb {
 
 // ---------------------------------------------------------------------------
@@ -140,6 +163,16 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
 int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
 int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
 int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc);
+int scan_exclusive(sph_ctx *ctx, int *data, int64_t n);
+void launch_counting_sort(cudaStream_t st, int64_t n, int64_t ncells, const int *key, int *cursor,
+                          const int *cstart, int *perm);
+int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instance *inst,
+                int ninst, const sph_batch_recipe *rec);
+int batch_build(sph_batch *b, int check_jump);
+int batch_density(sph_batch *b);
+int batch_rates(sph_batch *b, double *const *acc, double *const *pos);
+int batch_step(sph_batch *b, int nsteps, int use_graph);
+void batch_free(sph_batch *b);
 int list_maxima_async(sph_ctx *ctx);
 void list_maxima_collect(sph_ctx *ctx);
 void free_lists(sph_ctx *ctx);
@@ -256,6 +289,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
     const float R2 = d.r2hi * 1.0002f;
     const float cxf = (float)d.cx;
     const int rowstride_z = g.nx * g.ny;  // < 2^27 cells: 32-bit indices
+    const int *cst = S.cstart + g.cell_base;
     for (int dz = -g.kz; dz <= g.kz; ++dz) {
         const float ez = fmaxf(0.f, dz > 0 ? (float)dz * csf - d.xi_z
                                            : (dz < 0 ? d.xi_z - (float)(dz + 1) * csf : 0.f));
@@ -273,8 +307,8 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             const int tlo = max(-KX, __float2int_rd((d.xi_x - half) * inv_cs));
             const int thi = min(KX, __float2int_rd((d.xi_x + half) * inv_cs));
             const int c0 = zbase + (d.cy + dy) * g.nx;
-            const int lo = __ldg(S.cstart + c0 + tlo);
-            const int hi = __ldg(S.cstart + c0 + thi + 1);
+            const int lo = __ldg(cst + c0 + tlo);
+            const int hi = __ldg(cst + c0 + thi + 1);
             const float by = d.xi_y - (float)dy * csf;
             const int code_yz = KX + (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
             for (int j = lo; j < hi; ++j) {

@@ -36,6 +36,8 @@ EXPORTS = (
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
     "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
+    "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
+    "sph_batch_sync", "sph_batch_error_word",
 )
 
 
@@ -66,6 +68,23 @@ class AxpyLine(ctypes.Structure):
     _fields_ = [("out", ctypes.c_void_p), ("save", ctypes.c_void_p),
                 ("base", ctypes.c_void_p), ("k1", ctypes.c_void_p),
                 ("k2", ctypes.c_void_p), ("c1", ctypes.c_double), ("mode", ctypes.c_int)]
+
+
+class BatchInstance(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_int64), ("n", ctypes.c_int64),
+                ("cell_size", ctypes.c_double), ("lo", ctypes.c_double * 3),
+                ("hi", ctypes.c_double * 3), ("uniform_h", ctypes.c_int)]
+
+
+class BatchRecipe(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("subdiv", ctypes.c_int), ("scheme", ctypes.c_int),
+                ("list_cap", ctypes.c_int), ("radius_scale", ctypes.c_double),
+                ("dt", ctypes.c_double), ("density", DensityParams), ("term", SourceTerm),
+                ("rates", RatesParams)]
+
+
+SPH_EFLAG_JUMP = 1
+SPH_EFLAG_BOX = 4
 
 
 class NativeError(RuntimeError):
@@ -107,6 +126,12 @@ def load_library(build_if_missing=True):
         L.sph_nnps_fill.argtypes = [vp, i32, i32, d, vp, vp]
         L.sph_refresh_state.argtypes = [vp, i32, P(ArrayView)]
         L.sph_nbr_lists.argtypes = [vp, i32, P(i32), i32]
+        L.sph_batch_create.argtypes = [P(vp)]
+        L.sph_batch_destroy.argtypes = [vp]
+        L.sph_batch_setup.argtypes = [vp, P(ArrayView), P(BatchInstance), i32, P(BatchRecipe)]
+        L.sph_batch_step.argtypes = [vp, i32, i32]
+        L.sph_batch_sync.argtypes = [vp]
+        L.sph_batch_error_word.argtypes = [vp, P(ctypes.c_uint32)]
         L.sph_density.argtypes = [vp, i32, P(i32), i32, P(DensityParams), vp, vp, vp]
         L.sph_rates.argtypes = [vp, i32, P(SourceTerm), i32, P(RatesParams), P(vp), P(vp), i32]
         L.sph_tait.argtypes = [vp, i64, vp, vp, d, d, d, vp, vp]

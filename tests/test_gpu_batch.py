@@ -1,0 +1,85 @@
+"""Batched independent simulations against the same simulations run one by
+one through the solver API, and against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pysph_gb300
+from golden_util import normwise
+from pysph_gb300 import workloads as W
+from pysph_gb300.batch import SimulationBatch
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+API = pysph_gb300.api()
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+
+
+def _drops(count, seed=0):
+    return W.drop_batch(count, seed=seed, max_particles=3000, c0=100.0)
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_matches_single_runs(graph):
+    _need_gpu()
+    drops = _drops(6, seed=1)
+    steps = 5
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0, use_graph=graph)
+    batch.step(steps)
+    for k, props in enumerate(drops):
+        s, particles = W.setup_drop(API, props, c0=100.0)
+        for _ in range(steps):
+            s.integrator.integrate(1e-5)
+        pa = particles.arrays[0]
+        for p in ("x", "y", "u", "v"):
+            got = batch.get(k, p) - props[p]
+            ref = pa.get(p) - props[p]
+            assert normwise(got, ref) < TOL, (k, p, normwise(got, ref))
+        for p in ("rho", "p"):
+            assert normwise(batch.get(k, p), pa.get(p)) < TOL, (k, p)
+
+
+def test_batch_instances_vs_oracle():
+    _need_gpu()
+    drops = _drops(3, seed=2)
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0)
+    batch.step(3)
+    for k, props in enumerate(drops):
+        prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=100.0), dim=2)
+        for _ in range(3):
+            prob.integrate_euler(1e-5)
+        ref = prob.arrays["fluid"]
+        for p in ("x", "v"):
+            assert normwise(batch.get(k, p) - props[p], ref[p] - props[p]) < TOL, (k, p)
+        assert normwise(batch.get(k, "rho"), ref["rho"]) < TOL
+
+
+def test_batch_rk2_from_solvers():
+    _need_gpu()
+    drops = _drops(4, seed=3)
+    solvers = [W.setup_drop(API, p, c0=100.0, integrator="rk2") for p in drops]
+    batch = SimulationBatch.from_solvers(solvers, dt=1e-5)
+    assert batch.recipe.scheme == 1
+    batch.step(2)
+    for k, (s, particles) in enumerate(solvers):
+        for _ in range(2):
+            s.integrator.integrate(1e-5)
+        pa = particles.arrays[0]
+        for p in ("x", "u"):
+            assert normwise(batch.get(k, p) - drops[k][p], pa.get(p) - drops[k][p]) < TOL
+
+
+def test_batch_reports_particles_leaving_their_grid():
+    _need_gpu()
+    drops = _drops(2, seed=4)
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0, margin=0.0)
+    # push instance 1 far outside its region through the device arrays
+    a, b = int(batch.offsets[1]), int(batch.offsets[2])
+    batch.arrays["u"][a:b] = 1e5
+    with pytest.raises(RuntimeError):
+        batch.step(3)
