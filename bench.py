@@ -353,6 +353,203 @@ def run_gpu(args):
         pg.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# batched elliptical drops (many independent simulations per launch)
+# ---------------------------------------------------------------------------
+DROPS_DT = 1e-5
+DROPS_METRIC = "instance steps/s (batched 2D elliptical drops, Euler, SPHRho+Tait+PGrad+AV+XSPH)"
+DROPS_UNIT = "instance-steps/s"
+
+
+def _drops(args):
+    from pysph_gb300 import workloads as W
+    return W.drop_batch(args.drops, seed=0, c0=args.drop_c0)
+
+
+def _drop_sample(drops, count, spread=0.25):
+    """Indices of ``count`` instances spread over the smallest ``spread``
+    fraction of the size range (bounded CPU work)."""
+    import numpy as np
+    sizes = np.array([len(d["x"]) for d in drops])
+    order = np.argsort(sizes)
+    pick = order[np.linspace(0, int((len(order) - 1) * spread), count).astype(int)]
+    return [int(i) for i in pick]
+
+
+def _drop_ref_worker(args):
+    """Reference Cython drop run: (props, steps) -> (seconds, final arrays)."""
+    props, steps, c0 = args
+    import io
+    import contextlib
+    from pysph_gb300 import workloads as W
+    if reference_available():
+        api = _reference_api()
+        with contextlib.redirect_stdout(io.StringIO()):
+            s, particles = W.setup_drop(api, props, c0=c0)
+        step = lambda: s.integrator.integrate(DROPS_DT)  # noqa: E731
+        fetch = lambda: {k: particles.arrays[0].get(k).copy()  # noqa: E731
+                         for k in ("x", "y", "u", "v", "rho", "p")}
+        kind = "reference"
+    else:
+        import oracle
+        prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=c0), dim=2)
+        step = lambda: prob.integrate_euler(DROPS_DT)  # noqa: E731
+        fetch = lambda: {k: prob.arrays["fluid"][k].copy()  # noqa: E731
+                         for k in ("x", "y", "u", "v", "rho", "p")}
+        kind = "port"
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    return kind, time.perf_counter() - t0, fetch()
+
+
+def drops_cpu_baseline(drops, sample, steps, c0, procs=1):
+    import multiprocessing as mp
+    jobs = [(drops[i], steps, c0) for i in sample]
+    if procs == 1:
+        res = [_drop_ref_worker(j) for j in jobs]
+        seconds = sum(r[1] for r in res)
+    else:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_drop_ref_worker, jobs)
+        seconds = max(r[1] for r in res)
+    kind = res[0][0]
+    npart = sum(len(drops[i]["x"]) for i in sample)
+    mean_batch = sum(len(d["x"]) for d in drops) / len(drops)
+    return {"value": len(sample) * steps / seconds, "unit": DROPS_UNIT, "cores": procs,
+            "particle_steps_per_s": npart * steps / seconds,
+            "size_normalised_value": npart * steps / seconds / mean_batch,
+            "kind": kind,
+            "sample": "%d drops of %s particles, %d Euler steps each (%s)" % (
+                len(sample), "/".join(str(len(drops[i]["x"])) for i in sample), steps,
+                "reference PySPH Cython" if kind == "reference" else "oracle C port"),
+            "particles": sum(len(drops[i]["x"]) for i in sample)}, [r[2] for r in res]
+
+
+def run_gpu_drops(args):
+    import numpy as np
+    import torch
+
+    from pysph_gb300 import native, tuning
+    from pysph_gb300.batch import SimulationBatch
+
+    torch.cuda.set_device(0)
+    drops = _drops(args)
+    n = sum(len(d["x"]) for d in drops)
+    recipe = dict(dim=2, dt=DROPS_DT, co=args.drop_c0)
+    best, tune = tuning.autotune_batch(drops, candidates=(1, 2, 3), steps=5, **recipe)
+    batch = SimulationBatch(drops, subdiv=best, **recipe)
+    st = batch.stream()
+    batch.step(args.warmup)
+    pairs = batch.pair_counts()
+    pairs_per_step = 2.0 * float(pairs.sum())       # density + rates pass, Euler
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    launches0 = native.launch_count()
+    step_ms = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(st):
+            flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        batch.step(1, check=False)
+        b.record(st)
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    batch.check()
+    torch.cuda.synchronize()
+    launches = native.launch_count() - launches0
+    clk = clocks.stop()
+    t_total = sum(step_ms) / 1e3
+    steps = args.steps
+
+    # e2e: host state in, one graph step, host state out
+    fin = ("x", "y", "u", "v")
+    fout = ("x", "y", "u", "v", "rho", "p")
+    host = {f: torch.from_numpy(batch.get_all(f)).pin_memory() for f in fin}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.set(**host)
+        batch.step(1, check=False)
+        out = batch.get_all(*fout)
+    e2e_t = time.perf_counter() - t0
+    batch.check()
+    del out
+
+    line = {
+        "metric": DROPS_METRIC, "value": len(drops) * steps / t_total, "unit": DROPS_UNIT,
+        "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": t_total / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pair sums, f64 integration",
+        "data": "synthetic (seeded drop radii and spacings)",
+        "config": {"workload": "%d independent 2D elliptical drops, radius U[0.5,1.5], "
+                               "dx U[0.01,0.04], %d particles in total, c0=%g, Euler dt=%g"
+                               % (len(drops), n, args.drop_c0, DROPS_DT),
+                   "instances": len(drops), "particles": n,
+                   "min_particles": min(len(d["x"]) for d in drops),
+                   "max_particles": max(len(d["x"]) for d in drops),
+                   "subdivision": best, "autotune_ms_per_step": tune,
+                   "cache": "L2 flushed between timed steps (256 MiB write outside the events)",
+                   "launch": "one CUDA graph per step"},
+        "pair_interactions_per_s": pairs_per_step * steps / t_total,
+        "particle_steps_per_s": n * steps / t_total,
+        "gpu_launches": launches,
+        "e2e": {"value": len(drops) * steps / e2e_t, "unit": DROPS_UNIT,
+                "h2d_bytes_per_step": 8 * n * len(fin), "d2h_bytes_per_step": 8 * n * len(fout),
+                "ms_per_step": e2e_t / steps * 1e3},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        sample = _drop_sample(drops, args.drop_sample)
+        cb, ref_states = drops_cpu_baseline(drops, sample, args.cpu_steps, args.drop_c0)
+        # the same instances on the GPU from the initial state, for the error
+        fresh = SimulationBatch(drops, subdiv=best, **recipe)
+        fresh.step(args.cpu_steps)
+        errs = []
+        for i, ref in zip(sample, ref_states):
+            e = {}
+            for p in ("x", "y", "u", "v"):
+                d0 = drops[i][p]
+                got = fresh.get(i, p) - d0
+                want = ref[p] - d0
+                e[p] = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+            for p in ("rho", "p"):
+                got, want = fresh.get(i, p), ref[p]
+                e[p] = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+            errs.append({"instance": i, "particles": len(drops[i]["x"]), "max_rel": max(e.values())})
+        line["cpu_baseline"] = cb
+        line["instance_error_vs_f64"] = {"steps": args.cpu_steps, "norm": "||gpu-ref||/||ref|| "
+                                         "(displacements for x,y,u,v)", "instances": errs}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_drops(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    drops = _drops(args)
+    procs = args.procs or os.cpu_count() or 1
+    sample = _drop_sample(drops, procs, spread=1.0)
+    cb, _ = drops_cpu_baseline(drops, sample, args.steps, args.drop_c0, procs=procs)
+    # the sample's drops are smaller or larger than the batch's mean: report
+    # particle-steps/s divided by the batch's mean drop size
+    cb["value"] = cb["size_normalised_value"]
+    line = {"metric": DROPS_METRIC, "value": cb["value"], "unit": DROPS_UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "impl": "reference", "data": "synthetic (seeded drop radii and spacings)",
+            "config": {"workload": "bounded sample of the %d-drop batch (one drop per process)"
+                                   % len(drops)},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": DROPS_UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -384,10 +581,16 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--procs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="cube", choices=["cube", "drops"])
+    ap.add_argument("--drops", type=int, default=256)
+    ap.add_argument("--drop-c0", type=float, default=100.0)
+    ap.add_argument("--drop-sample", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "drops":
+        (run_reference_drops if args.impl == "reference" else run_gpu_drops)(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

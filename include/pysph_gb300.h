@@ -234,8 +234,15 @@ int sph_batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_ins
 int sph_batch_step(sph_batch *b, int nsteps, int use_graph);
 /* Wait for the batch's stream. */
 int sph_batch_sync(sph_batch *b);
+/* The batch's CUDA stream (cudaStream_t), e.g. to record timing events. */
+int sph_batch_stream(sph_batch *b, void **out);
 /* Read and clear the batch's device error word (SPH_EFLAG_*; synchronises). */
 int sph_batch_error_word(sph_batch *b, uint32_t *out);
+/* Neighbour counts (incl. self) of the batch's last evaluation, summed per
+ * instance into out[ninst] (synchronises).  Used for pair-interaction
+ * counts; the reference has no batch, its per-array counterpart is
+ * NbrParticleLocatorBase.get_nearest_particles (base/nnps.pyx:311). */
+int sph_batch_pair_counts(sph_batch *b, uint64_t *out);
 
 /* Read and clear the device error word (synchronises). */
 int sph_error_word(sph_ctx *ctx, uint32_t *out);

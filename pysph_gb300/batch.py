@@ -18,7 +18,6 @@ import numpy as np
 import torch
 
 from . import native
-from .sph.sph_calc import _kind_of
 
 PROPS = ("x", "y", "z", "u", "v", "w", "m", "h", "rho", "p", "cs")
 
@@ -149,6 +148,18 @@ class SimulationBatch:
         if check:
             self.check()
 
+    def stream(self):
+        """The batch's CUDA stream as a torch stream (for events)."""
+        h = ctypes.c_void_p()
+        native.check(native.lib().sph_batch_stream(self._b, ctypes.byref(h)), "batch stream")
+        return torch.cuda.ExternalStream(h.value)
+
+    def pair_counts(self):
+        """Neighbour pairs (incl. self) per instance in the last evaluation."""
+        out = (ctypes.c_uint64 * self.ninstances)()
+        native.check(native.lib().sph_batch_pair_counts(self._b, out), "pair counts")
+        return np.array(out[:], dtype=np.int64)
+
     def sync(self):
         native.check(native.lib().sph_batch_sync(self._b), "sph_batch_sync")
 
@@ -159,6 +170,23 @@ class SimulationBatch:
             raise RuntimeError("Particle moved by more than one cell width")
         if w.value & native.SPH_EFLAG_BOX:
             raise RuntimeError("a particle left its instance's grid region (raise margin)")
+
+    def set(self, **props):
+        """Overwrite whole concatenated properties (all instances, in
+        instance order) from host or device tensors / arrays."""
+        for name, val in props.items():
+            if name not in self.arrays:
+                raise ValueError("unknown batch property %r" % name)
+            t = torch.as_tensor(val)
+            if t.numel() != self.n:
+                raise ValueError("property %r needs %d values" % (name, self.n))
+            self.arrays[name].copy_(t.reshape(-1), non_blocking=True)
+
+    def get_all(self, *props):
+        """Whole concatenated properties as NumPy arrays (synchronises)."""
+        self.sync()
+        out = [self.arrays[p].cpu().numpy() for p in props]
+        return out[0] if len(out) == 1 else tuple(out)
 
     def get(self, k, *props):
         """Properties of instance ``k`` as NumPy arrays (synchronises)."""

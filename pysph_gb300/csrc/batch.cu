@@ -314,11 +314,50 @@ int batch_step(sph_batch *b, int nsteps, int use_graph) {
             return rc;
         }
         if (e != cudaSuccess) return cuda_check(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
+        // kernels per replay, for the launch counter (the captured launches
+        // were counted at capture but did not run then)
+        size_t nnodes = 0;
+        e = cudaGraphGetNodes(graph, nullptr, &nnodes);
+        std::vector<cudaGraphNode_t> nodes(nnodes);
+        if (e == cudaSuccess && nnodes) e = cudaGraphGetNodes(graph, nodes.data(), &nnodes);
+        int kernels = 0;
+        for (size_t i = 0; e == cudaSuccess && i < nnodes; ++i) {
+            cudaGraphNodeType t;
+            e = cudaGraphNodeGetType(nodes[i], &t);
+            kernels += (e == cudaSuccess && t == cudaGraphNodeTypeKernel);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return cuda_check(e, "cudaGraphInstantiate");
+        b->graph_kernels = kernels;
+        count_launch(-kernels);
     }
-    for (int s = 0; s < nsteps; ++s) SPH_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));
+    for (int s = 0; s < nsteps; ++s) {
+        SPH_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));
+        count_launch(b->graph_kernels);
+    }
+    return SPH_OK;
+}
+
+__global__ void k_inst_pairs(const int *cnt, const int *sinst, int64_t n,
+                             unsigned long long *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(out + sinst[i], (unsigned long long)cnt[i]);
+}
+
+int batch_pair_counts(sph_batch *b, unsigned long long *out) {
+    if (!b->ready || b->steps_built == 0)
+        return set_error(SPH_ERR_STATE, "batch: no evaluation yet");
+    const size_t bytes = sizeof(unsigned long long) * b->ninst;
+    if (!b->d_pairs) SPH_CUDA(cudaMalloc(&b->d_pairs, bytes));
+    SPH_CUDA(cudaMemsetAsync(b->d_pairs, 0, bytes, b->stream));
+    k_inst_pairs<<<grid_blocks(b->view.n, 256, 4), 256, 0, b->stream>>>(
+        b->list.cnt, b->sinst, b->view.n, b->d_pairs);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_inst_pairs");
+    SPH_CUDA(cudaMemcpyAsync(out, b->d_pairs, bytes, cudaMemcpyDeviceToHost, b->stream));
+    SPH_CUDA(cudaStreamSynchronize(b->stream));
     return SPH_OK;
 }
 
@@ -335,6 +374,7 @@ void batch_free(sph_batch *b) {
         cudaFree(b->x0[c]);
     }
     cudaFree(b->d_err);
+    cudaFree(b->d_pairs);
 }
 
 }  // namespace sphgb

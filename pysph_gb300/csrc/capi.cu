@@ -233,6 +233,17 @@ int sph_batch_sync(sph_batch *b) {
     return SPH_OK;
 }
 
+int sph_batch_stream(sph_batch *b, void **out) {
+    if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_stream: null argument");
+    *out = (void *)b->stream;
+    return SPH_OK;
+}
+
+int sph_batch_pair_counts(sph_batch *b, uint64_t *out) {
+    if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_pair_counts: null argument");
+    return batch_pair_counts(b, (unsigned long long *)out);
+}
+
 int sph_batch_error_word(sph_batch *b, unsigned *out) {
     if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_error_word: null argument");
     if (!b->d_err) { *out = 0; return SPH_OK; }

@@ -115,8 +115,10 @@ struct sph_batch {
     sphgb::NbrList list;
     double *rate1[6] = {nullptr}, *rate2[6] = {nullptr}, *x0[6] = {nullptr};
     unsigned *d_err = nullptr;
+    unsigned long long *d_pairs = nullptr;  // per-instance pair counts
     long long steps_built = 0;
     cudaGraphExec_t graph_exec = nullptr;
+    int graph_kernels = 0;       // kernel nodes of one replay
     bool ready = false;
 };
 
@@ -172,6 +174,7 @@ int batch_build(sph_batch *b, int check_jump);
 int batch_density(sph_batch *b);
 int batch_rates(sph_batch *b, double *const *acc, double *const *pos);
 int batch_step(sph_batch *b, int nsteps, int use_graph);
+int batch_pair_counts(sph_batch *b, unsigned long long *out);
 void batch_free(sph_batch *b);
 int list_maxima_async(sph_ctx *ctx);
 void list_maxima_collect(sph_ctx *ctx);

@@ -37,7 +37,8 @@ EXPORTS = (
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
     "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
     "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
-    "sph_batch_sync", "sph_batch_error_word",
+    "sph_batch_sync", "sph_batch_error_word", "sph_batch_stream",
+    "sph_batch_pair_counts",
 )
 
 
@@ -131,6 +132,8 @@ def load_library(build_if_missing=True):
         L.sph_batch_setup.argtypes = [vp, P(ArrayView), P(BatchInstance), i32, P(BatchRecipe)]
         L.sph_batch_step.argtypes = [vp, i32, i32]
         L.sph_batch_sync.argtypes = [vp]
+        L.sph_batch_stream.argtypes = [vp, P(vp)]
+        L.sph_batch_pair_counts.argtypes = [vp, P(ctypes.c_uint64)]
         L.sph_batch_error_word.argtypes = [vp, P(ctypes.c_uint32)]
         L.sph_density.argtypes = [vp, i32, P(i32), i32, P(DensityParams), vp, vp, vp]
         L.sph_rates.argtypes = [vp, i32, P(SourceTerm), i32, P(RatesParams), P(vp), P(vp), i32]

@@ -37,3 +37,33 @@ def choose_subdivision(cell_manager):
     while sub > 1 and nmax >= MAX_PARTICLES[sub]:
         sub -= 1
     return sub
+
+
+def time_batch_steps(batch, steps):
+    """Device time (ms) of ``steps`` batch steps, from CUDA events recorded
+    on the batch's stream."""
+    import torch
+    st = batch.stream()
+    batch.step(1)                       # captures the graph (not timed)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    batch.step(steps, check=False)
+    b.record(st)
+    b.synchronize()
+    batch.check()
+    return a.elapsed_time(b)
+
+
+def autotune_batch(instances, candidates=(1, 2, 3), steps=5, **recipe):
+    """Pick the cell subdivision of a batch by timing every candidate on the
+    batch itself.  Returns ``(best_subdiv, {subdiv: ms_per_step})``."""
+    from .batch import SimulationBatch
+    import copy
+    timings = {}
+    for sub in candidates:
+        b = SimulationBatch(copy.deepcopy(instances), subdiv=sub, **recipe)
+        timings[sub] = time_batch_steps(b, steps) / steps
+        del b
+    best = min(timings, key=timings.get)
+    return best, timings
