@@ -51,6 +51,10 @@ STEP_ALG_BYTES = 694.0
 # FLOPs per neighbour pair: density 24, momentum 72 (FMA = 2)
 PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+# DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md);
+# the traffic grows with the particle count, so it is scaled by n
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 383.0, "RatesStage": 404.0}
 
 
 def measured_peaks():
@@ -332,7 +336,10 @@ def run_gpu(args):
                 "d2h_bytes_per_step": 8 * n * len(fields_out),
                 "ms_per_step": e2e_t / e2e_steps * 1e3},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (NCU_TRAFFIC_PER_PARTICLE[dom] * n
+                                 if dom in NCU_TRAFFIC_PER_PARTICLE else None),
+                     "traffic_source": "ncu capture at 1M particles, scaled by n",
                      "peak_kind": peak_kind,
                      "alg_bytes_per_particle": ALG_BYTES[dom],
                      "note": "pair kernels issue-bound; fp32 context in fp32_context"},
