@@ -50,6 +50,7 @@ extern "C" {
 #define SPH_EFLAG_JUMP 1u
 #define SPH_EFLAG_NONFINITE 2u
 #define SPH_EFLAG_BOX 4u      /* batch: a particle left its instance's grid */
+#define SPH_EFLAG_TIMEOUT 8u  /* a bounded device wait gave up               */
 
 #define SPH_MAX_SOURCES 8
 
@@ -250,6 +251,83 @@ int sph_error_word(sph_ctx *ctx, uint32_t *out);
 /* Mean neighbour count (incl. self) of dst among src from the last build,
  * computed on the device (synchronises).  Used for pair-interaction counts. */
 int sph_mean_neighbours(sph_ctx *ctx, int dst, int src, double *out);
+
+/* ------------------------------------------------------------------------
+ * Learned momentum closure.  None of these has a counterpart in the
+ * reference: the network stands in for the momentum pair loop of a fluid
+ * array on itself (SPHPressureGradient, sph/funcs/pressure_funcs.pyx:40-91,
+ * and MonaghanArtificialVsicosity, sph/funcs/viscosity_funcs.pyx:41-124).
+ *
+ * Network 192 -> 128 -> 128 -> 2, exact GELU on the hidden layers; BF16
+ * weights and matrix-product inputs, FP32 accumulation (tensor memory).
+ * Parameters: one FP32 vector of SPH_MLP_NPARAM values, W row-major
+ * [out][in]; the BF16 copies (w1 [128][192], w2 [128][128], its transpose
+ * w2t, w3 [2][128]) are written by sph_mlp_sync and sph_mlp_adam.
+ * Buffers are device pointers; x, z1, z2, h1, h2 16-byte aligned.
+ * ------------------------------------------------------------------------ */
+#define SPH_MLP_NIN 192
+#define SPH_MLP_NH 128
+#define SPH_MLP_NOUT 2
+#define SPH_MLP_NNBR 32       /* neighbours per feature row                  */
+#define SPH_MLP_NCH 6         /* channels per neighbour                      */
+#define SPH_MLP_OFF_W1 0
+#define SPH_MLP_OFF_B1 (SPH_MLP_OFF_W1 + SPH_MLP_NH * SPH_MLP_NIN)
+#define SPH_MLP_OFF_W2 (SPH_MLP_OFF_B1 + SPH_MLP_NH)
+#define SPH_MLP_OFF_B2 (SPH_MLP_OFF_W2 + SPH_MLP_NH * SPH_MLP_NH)
+#define SPH_MLP_OFF_W3 (SPH_MLP_OFF_B2 + SPH_MLP_NH)
+#define SPH_MLP_OFF_B3 (SPH_MLP_OFF_W3 + SPH_MLP_NOUT * SPH_MLP_NH)
+#define SPH_MLP_NPARAM (SPH_MLP_OFF_B3 + SPH_MLP_NOUT)
+
+typedef struct {
+    float *params;                 /* SPH_MLP_NPARAM FP32 master values */
+    uint16_t *w1, *w2, *w2t, *w3;  /* BF16 copies                        */
+} sph_mlp_model;
+
+typedef struct {
+    double c0;                     /* velocity scale                     */
+    float mean[SPH_MLP_NCH];       /* per-channel standardisation        */
+    float inv_std[SPH_MLP_NCH];
+} sph_mlp_feature_params;
+
+/* Feature rows of every particle of dst (by original index) from its
+ * neighbours in src within radius_scale * h_i: the 32 nearest, self
+ * included, ordered by squared distance then sorted source slot, each
+ * ((x_i-x_j)/h_i, (y_i-y_j)/h_i, (u_j-u_i)/c0, (v_j-v_i)/c0, rho_j, p_j)
+ * minus mean times inv_std; missing neighbours are zero rows.  Reads the
+ * sorted state of the last density pass.  Output BF16 [n][192] and/or FP32
+ * [n][192] (either may be NULL). */
+int sph_mlp_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
+                     uint16_t *out_bf16, float *out_f32);
+/* Write the BF16 copies from the FP32 parameters. */
+int sph_mlp_sync(const sph_mlp_model *m, void *stream);
+/* y[n][2] = network(x[n][192]).  z1, z2 (FP32 [n][128]) and h1, h2 (BF16
+ * [n][128]) save the pre-activations and activations for sph_mlp_backward
+ * (NULL: not saved).  err: device word, SPH_EFLAG_TIMEOUT on a wait that
+ * gave up. */
+int sph_mlp_forward(const sph_mlp_model *m, const uint16_t *x, int64_t n, float *y, float *z1,
+                    float *z2, uint16_t *h1, uint16_t *h2, uint32_t *err, void *stream);
+/* FP32 scratch values sph_mlp_backward needs for a batch of n samples. */
+int sph_mlp_backward_scratch(int64_t n, int64_t *floats);
+/* Gradient of loss = 0.5 * inv_count * sum (y - target)^2 into grad
+ * [SPH_MLP_NPARAM] and the loss into *loss (device), from the saved
+ * forward values.  Deterministic: fixed-order sums of per-CTA partials. */
+int sph_mlp_backward(const sph_mlp_model *m, const uint16_t *x, const uint16_t *h1,
+                     const uint16_t *h2, const float *z1, const float *z2, const float *y,
+                     const float *target, int64_t n, float inv_count, float *grad, float *loss,
+                     float *scratch, uint32_t *err, void *stream);
+/* One Adam step (bias-corrected, step counts from 1) on the FP32
+ * parameters with moment buffers mom, vel; rewrites the BF16 copies. */
+int sph_mlp_adam(const sph_mlp_model *m, const float *grad, float *mom, float *vel, float lr,
+                 float beta1, float beta2, float eps, int step, void *stream);
+/* acc[c][i] = (or +=) (y[i][c] * scale[c] + mean[c]) * c0^2 / h_i for the
+ * LocalReal particles of dst (acc[2], if given, is zeroed when not
+ * accumulating). */
+int sph_mlp_apply(sph_ctx *ctx, int dst, const float *y, double c0, const double *scale,
+                  const double *mean, double *const *acc, int accumulate);
+/* out[i][c] = (a_c[i] * h_i / c0^2 - mean[c]) * inv_std[c]: standardised
+ * training targets from accelerations. */
+int sph_mlp_targets(int64_t n, const double *ax, const double *ay, const double *h, double c0,
+                    const double *mean, const double *inv_std, float *out, void *stream);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,9 @@ class CellManager:
         self.array_indices = {}
         self.coord_x, self.coord_y, self.coord_z = "x", "y", "z"
         self.jump_tolerance = 1
+        # the next build starts afresh (no jump check): set after the
+        # particle state was replaced rather than advanced
+        self.skip_jump_once = False
         self.cell_size = 0.0
         self.periodic_domain = None
         self.is_dirty = True
@@ -151,8 +154,10 @@ class CellManager:
         ctx = self.context()
         views = (native.ArrayView * len(self.arrays_to_bin))(
             *[array_view(pa) for pa in self.arrays_to_bin])
+        check = 0 if self.skip_jump_once else 1
         rc = native.lib().sph_nnps_build(ctx, views, len(self.arrays_to_bin), self.cell_size,
-                                         self.max_radius_scale, self._subdivision(), 1)
+                                         self.max_radius_scale, self._subdivision(), check)
+        self.skip_jump_once = False
         native.check(rc, "CellManager.update")
         self._views = views
         self._snap_versions = [pa.version for pa in self.arrays_to_bin]

@@ -295,4 +295,71 @@ int sph_mean_neighbours(sph_ctx *c, int dst, int src, double *out) {
     return SPH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// learned momentum closure
+// ---------------------------------------------------------------------------
+static bool mlp_model_ok(const sph_mlp_model *m) {
+    return m && m->params && m->w1 && m->w2 && m->w2t && m->w3;
+}
+
+int sph_mlp_features(sph_ctx *c, int dst, int src, const sph_mlp_feature_params *prm,
+                     uint16_t *out_bf16, float *out_f32) {
+    CHECK_CTX(c);
+    return launch_features(c, dst, src, prm, out_bf16, out_f32);
+}
+
+int sph_mlp_sync(const sph_mlp_model *m, void *stream) {
+    if (!mlp_model_ok(m)) return set_error(SPH_ERR_ARG, "sph_mlp_sync: incomplete model");
+    return mlp_sync(m, (cudaStream_t)stream);
+}
+
+int sph_mlp_forward(const sph_mlp_model *m, const uint16_t *x, int64_t n, float *y, float *z1,
+                    float *z2, uint16_t *h1, uint16_t *h2, uint32_t *err, void *stream) {
+    if (!mlp_model_ok(m) || !x || !y || !err || n < 0)
+        return set_error(SPH_ERR_ARG, "sph_mlp_forward: null argument");
+    return mlp_forward(m, x, n, y, z1, z2, h1, h2, err, (cudaStream_t)stream);
+}
+
+int sph_mlp_backward_scratch(int64_t n, int64_t *floats) {
+    if (!floats || n < 0) return set_error(SPH_ERR_ARG, "sph_mlp_backward_scratch: bad argument");
+    *floats = mlp_backward_scratch(n);
+    return SPH_OK;
+}
+
+int sph_mlp_backward(const sph_mlp_model *m, const uint16_t *x, const uint16_t *h1,
+                     const uint16_t *h2, const float *z1, const float *z2, const float *y,
+                     const float *target, int64_t n, float inv_count, float *grad, float *loss,
+                     float *scratch, uint32_t *err, void *stream) {
+    if (!mlp_model_ok(m) || !x || !h1 || !h2 || !z1 || !z2 || !y || !target || !grad ||
+        !scratch || !err)
+        return set_error(SPH_ERR_ARG, "sph_mlp_backward: null argument");
+    return mlp_backward(m, x, h1, h2, z1, z2, y, target, n, inv_count, grad, loss, scratch, err,
+                        (cudaStream_t)stream);
+}
+
+int sph_mlp_adam(const sph_mlp_model *m, const float *grad, float *mom, float *vel, float lr,
+                 float beta1, float beta2, float eps, int step, void *stream) {
+    if (!mlp_model_ok(m) || !grad || !mom || !vel)
+        return set_error(SPH_ERR_ARG, "sph_mlp_adam: null argument");
+    return mlp_adam(m, grad, mom, vel, lr, beta1, beta2, eps, step, (cudaStream_t)stream);
+}
+
+int sph_mlp_apply(sph_ctx *c, int dst, const float *y, double c0, const double *scale,
+                  const double *mean, double *const *acc, int accumulate) {
+    CHECK_CTX(c);
+    if (dst < 0 || dst >= (int)c->arrays.size() || !y || !scale || !mean || !acc)
+        return set_error(SPH_ERR_ARG, "sph_mlp_apply: bad argument");
+    const sph_array_view &v = c->arrays[dst].view;
+    if (!v.h) return set_error(SPH_ERR_ARG, "sph_mlp_apply: destination has no h");
+    return mlp_apply(v.n, y, v.tag, v.h, c0, scale, mean, acc, accumulate, c->stream);
+}
+
+int sph_mlp_targets(int64_t n, const double *ax, const double *ay, const double *h, double c0,
+                    const double *mean, const double *inv_std, float *out, void *stream) {
+    if (!ax || !ay || !h || !mean || !inv_std || !out || c0 <= 0.0)
+        return set_error(SPH_ERR_ARG, "sph_mlp_targets: bad argument");
+    return mlp_targets(n, ax, ay, h, c0, mean, inv_std, out, (cudaStream_t)stream);
+}
+
 }  // extern "C"
+

@@ -1,0 +1,811 @@
+// Learned momentum closure: the per-particle network 192 -> 128 -> 128 -> 2
+// (exact GELU) on the fifth-generation tensor cores.
+//
+// The reference has no learned part; the network stands in for the
+// momentum pair loop (sph/funcs/pressure_funcs.pyx:40-91 and
+// sph/funcs/viscosity_funcs.pyx:41-124) of a fluid array on itself.
+//
+// Operands: BF16, in shared memory in the canonical K-major layout without
+// swizzle -- 8-row x 16-byte core matrices, core matrix (row/8, k/8) at
+// ((row/8) * K/8 + k/8) * 128 bytes, so the leading-dimension offset (next
+// core matrix along K) is 128 B and the stride-dimension offset (next 8
+// rows) is K/8 * 128 B.  One thread issues tcgen05.mma (M = 128 samples or
+// hidden units, kind::f16 with BF16 A and B, FP32 accumulation in tensor
+// memory) and tcgen05.commit signals an mbarrier; the four warps of the
+// CTA read the accumulator rows back with tcgen05.ld (warp w owns lanes
+// 32w..32w+31, thread t owns row t).
+//
+//   k_mlp_fwd   per 128-sample tile: X W1^T -> +b1, GELU -> BF16 H1 (smem)
+//               -> H1 W2^T -> +b2, GELU -> BF16 h2 -> h2 W3^T + b3 on the
+//               CUDA cores.  Training saves z1, z2 (FP32) and h1, h2 (BF16).
+//   k_mlp_bwd   per tile: dy = (y - t) / B; dz2 = (dy W3) * gelu'(z2);
+//               dh1 = dz2 W2 (tensor cores); dW2 += dz2^T h1 and
+//               dW1 += dz1^T x accumulated in tensor memory over the CTA's
+//               tiles; an extra row of ones in the B operand of the weight
+//               gradients yields the bias gradients in the same product.
+//   k_mlp_l3    third-layer gradients (FP32 CUDA cores).
+//   k_mlp_reduce  fixed-order sum of the per-CTA partial gradients.
+//   k_mlp_adam  Adam on the FP32 master parameters and the BF16 copies.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int NIN = SPH_MLP_NIN, NH = SPH_MLP_NH, NOUT = SPH_MLP_NOUT;
+constexpr int OFF_W1 = SPH_MLP_OFF_W1, OFF_B1 = SPH_MLP_OFF_B1, OFF_W2 = SPH_MLP_OFF_W2,
+              OFF_B2 = SPH_MLP_OFF_B2, OFF_W3 = SPH_MLP_OFF_W3, OFF_B3 = SPH_MLP_OFF_B3,
+              NPARAM = SPH_MLP_NPARAM;
+constexpr int TILE = 128;
+constexpr int THREADS = 128;
+constexpr int L3_PART = NOUT * NH + NOUT;   // third-layer partial per block
+constexpr int L3_ROWS = 1024;               // rows per third-layer block
+constexpr int kMaxSpin = 1 << 22;           // bounded mbarrier wait
+
+// ---------------------------------------------------------------------------
+// tcgen05 / mbarrier primitives (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading- and stride-
+// dimension byte offsets (all >> 4), descriptor version 1 (bit 46), no
+// swizzle (bits 61-63 = 0), base offset 0.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+static_assert(idesc_bf16(128, 128) == 0x08200490u, "instruction descriptor layout");
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Wait for phase `parity` of the barrier, at most kMaxSpin polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < kMaxSpin; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of element (r, k) of a K-major operand with kc = K/8 chunks per row
+__device__ __forceinline__ uint32_t core_off(int r, int k, int kc) {
+    return (uint32_t)(((((r >> 3) * kc) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float dgelu(float z) {
+    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) +
+           z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+// Copy a row-major [rows][K] BF16 matrix into the K-major core layout.
+// Eight consecutive threads take the eight rows of one core matrix (one
+// 16-byte chunk each) so their shared stores hit distinct banks.
+__device__ __forceinline__ void load_operand(uint8_t *dst, const uint16_t *src, int rows, int K) {
+    const int kc = K / 8;
+    for (int c = threadIdx.x; c < rows * kc; c += blockDim.x) {
+        const int r8 = c & 7, rest = c >> 3;
+        const int k8 = rest % kc, rg = rest / kc;
+        const int r = rg * 8 + r8;
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (int64_t)r * K + k8 * 8));
+        *reinterpret_cast<uint4 *>(dst + core_off(r, k8 * 8, kc)) = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+constexpr uint32_t F_W1 = 0;
+constexpr uint32_t F_W2 = F_W1 + NH * NIN * 2;      // 49152
+constexpr uint32_t F_X = F_W2 + NH * NH * 2;        // 81920
+constexpr uint32_t F_H1 = F_X + TILE * NIN * 2;     // 131072
+constexpr uint32_t F_W3 = F_H1 + TILE * NH * 2;     // 163840: float [2][128]
+constexpr uint32_t F_B1 = F_W3 + NOUT * NH * 4;     // float [128]
+constexpr uint32_t F_B2 = F_B1 + NH * 4;            // float [128]
+constexpr uint32_t F_B3 = F_B2 + NH * 4;            // float [2] (+pad)
+constexpr uint32_t F_BAR = F_B3 + 16;               // mbarrier (8 B)
+constexpr uint32_t F_SLOT = F_BAR + 8;              // tensor-memory address
+constexpr uint32_t F_BYTES = F_SLOT + 8;
+constexpr uint32_t F_TMEM_COLS = 256;               // z1 at 0, z2 at 128
+
+struct MlpDev {
+    const float *params;
+    const uint16_t *w1, *w2, *w2t, *w3;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_mlp_fwd(const MlpDev W, const uint16_t *__restrict__ x, int64_t n, float *__restrict__ y,
+              float *__restrict__ z1s, float *__restrict__ z2s, uint16_t *__restrict__ h1s,
+              uint16_t *__restrict__ h2s, unsigned *err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int t = threadIdx.x, warp = t >> 5;
+    float *w3f = reinterpret_cast<float *>(sm + F_W3);
+    float *b1f = reinterpret_cast<float *>(sm + F_B1);
+    float *b2f = reinterpret_cast<float *>(sm + F_B2);
+    float *b3f = reinterpret_cast<float *>(sm + F_B3);
+    const uint32_t bar = smem_u32(sm + F_BAR);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + F_SLOT);
+
+    load_operand(sm + F_W1, W.w1, NH, NIN);
+    load_operand(sm + F_W2, W.w2, NH, NH);
+    for (int i = t; i < NOUT * NH; i += THREADS) w3f[i] = __uint_as_float((uint32_t)W.w3[i] << 16);
+    for (int i = t; i < NH; i += THREADS) {
+        b1f[i] = W.params[OFF_B1 + i];
+        b2f[i] = W.params[OFF_B2 + i];
+    }
+    if (t < NOUT) b3f[t] = W.params[OFF_B3 + t];
+    if (warp == 0) tmem_alloc(smem_u32(slot), F_TMEM_COLS);
+    if (t == 0) mbar_init(bar, 1);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *slot;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t sX = smem_u32(sm + F_X), sW1 = smem_u32(sm + F_W1);
+    const uint32_t sH1 = smem_u32(sm + F_H1), sW2 = smem_u32(sm + F_W2);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row0 = tile * TILE;
+        // X tile (rows beyond n are zeros)
+        for (int c = t; c < TILE * (NIN / 8); c += THREADS) {
+            const int r8 = c & 7, rest = c >> 3;
+            const int k8 = rest % (NIN / 8), rg = rest / (NIN / 8);
+            const int r = rg * 8 + r8;
+            const int64_t gr = row0 + r;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (gr < n) v = __ldg(reinterpret_cast<const uint4 *>(x + gr * NIN + k8 * 8));
+            *reinterpret_cast<uint4 *>(sm + F_X + core_off(r, k8 * 8, NIN / 8)) = v;
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int s = 0; s < NIN / 16; ++s)
+                mma_bf16(tbase, sdesc(sX + s * 256, 128, (NIN / 8) * 128),
+                         sdesc(sW1 + s * 256, 128, (NIN / 8) * 128), idesc_bf16(128, NH), s > 0);
+            mma_commit(bar);
+        }
+        ok = mbar_wait(bar, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+
+        const int64_t grow = row0 + t;
+        const bool valid = grow < n;
+#pragma unroll 1
+        for (int c0 = 0; c0 < NH; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + lane_base + c0, v);
+            uint32_t hw[8];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] += b1f[c0 + i];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) hw[i] = pack2(gelu(v[2 * i]), gelu(v[2 * i + 1]));
+            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(t, c0, NH / 8)) =
+                make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(t, c0 + 8, NH / 8)) =
+                make_uint4(hw[4], hw[5], hw[6], hw[7]);
+            if (valid && z1s) {
+                float4 *zp = reinterpret_cast<float4 *>(z1s + grow * NH + c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    zp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+            if (valid && h1s) {
+                uint4 *hp = reinterpret_cast<uint4 *>(h1s + grow * NH + c0);
+                hp[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                hp[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int s = 0; s < NH / 16; ++s)
+                mma_bf16(tbase + 128, sdesc(sH1 + s * 256, 128, (NH / 8) * 128),
+                         sdesc(sW2 + s * 256, 128, (NH / 8) * 128), idesc_bf16(128, NH), s > 0);
+            mma_commit(bar);
+        }
+        ok = mbar_wait(bar, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+
+        float y0 = b3f[0], y1 = b3f[1];
+#pragma unroll 1
+        for (int c0 = 0; c0 < NH; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + 128 + lane_base + c0, v);
+            uint32_t hw[8];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] += b2f[c0 + i];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                hw[i] = pack2(gelu(v[2 * i]), gelu(v[2 * i + 1]));
+                const float ha = bf_lo(hw[i]), hb = bf_hi(hw[i]);
+                const int c = c0 + 2 * i;
+                y0 = fmaf(ha, w3f[c], y0);
+                y0 = fmaf(hb, w3f[c + 1], y0);
+                y1 = fmaf(ha, w3f[NH + c], y1);
+                y1 = fmaf(hb, w3f[NH + c + 1], y1);
+            }
+            if (valid && z2s) {
+                float4 *zp = reinterpret_cast<float4 *>(z2s + grow * NH + c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    zp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+            if (valid && h2s) {
+                uint4 *hp = reinterpret_cast<uint4 *>(h2s + grow * NH + c0);
+                hp[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                hp[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+            }
+        }
+        if (valid) {
+            y[grow * 2] = y0;
+            y[grow * 2 + 1] = y1;
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, F_TMEM_COLS);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// backward
+// ---------------------------------------------------------------------------
+constexpr int H1T_ROWS = NH + 16;    // h1^T plus a row of ones (bias) and zero rows
+constexpr int XT_ROWS = NIN + 16;    // x^T plus a row of ones and zero rows
+constexpr uint32_t B_A1 = 0;                              // dz2 [b][j]
+constexpr uint32_t B_A2 = B_A1 + TILE * NH * 2;           // dz2^T, then dz1^T [j][b]
+constexpr uint32_t B_H1T = B_A2 + NH * TILE * 2;          // [i][b], 144 rows
+constexpr uint32_t B_XT = B_H1T + H1T_ROWS * TILE * 2;    // [m][b], 208 rows
+constexpr uint32_t B_W2T = B_XT + XT_ROWS * TILE * 2;     // W2^T [i][j]
+constexpr uint32_t B_W3 = B_W2T + NH * NH * 2;            // float [2][128]
+constexpr uint32_t B_RED = B_W3 + NOUT * NH * 4;          // float [4] loss per warp
+constexpr uint32_t B_BAR = B_RED + 16;
+constexpr uint32_t B_SLOT = B_BAR + 8;
+constexpr uint32_t B_BYTES = B_SLOT + 8;
+constexpr uint32_t T_DH1 = 0, T_DW2 = 128, T_DW1 = 288;    // tensor-memory columns
+constexpr uint32_t B_TMEM_COLS = 512;
+static_assert(T_DW2 + H1T_ROWS <= T_DW1 && T_DW1 + XT_ROWS <= B_TMEM_COLS, "tensor memory plan");
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_mlp_bwd(const MlpDev W, const uint16_t *__restrict__ x, const uint16_t *__restrict__ h1s,
+              const float *__restrict__ z1s, const float *__restrict__ z2s,
+              const float *__restrict__ y, const float *__restrict__ target, int64_t n,
+              float inv_count, float *__restrict__ dy_out, float *__restrict__ part,
+              float *__restrict__ part_loss, unsigned *err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    float *w3f = reinterpret_cast<float *>(sm + B_W3);
+    float *red = reinterpret_cast<float *>(sm + B_RED);
+    const uint32_t bar = smem_u32(sm + B_BAR);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + B_SLOT);
+
+    load_operand(sm + B_W2T, W.w2t, NH, NH);
+    for (int i = t; i < NOUT * NH; i += THREADS) w3f[i] = __uint_as_float((uint32_t)W.w3[i] << 16);
+    // the constant rows: ones at h1^T row 128 and x^T row 192, zeros below
+    for (int i = t; i < 16 * TILE; i += THREADS) {
+        const int r = i / TILE, b = i % TILE;
+        const __nv_bfloat16 one = __float2bfloat16_rn(r == 0 ? 1.f : 0.f);
+        *reinterpret_cast<__nv_bfloat16 *>(sm + B_H1T + core_off(NH + r, b, TILE / 8)) = one;
+        *reinterpret_cast<__nv_bfloat16 *>(sm + B_XT + core_off(NIN + r, b, TILE / 8)) = one;
+    }
+    if (warp == 0) tmem_alloc(smem_u32(slot), B_TMEM_COLS);
+    if (t == 0) mbar_init(bar, 1);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *slot;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t sA1 = smem_u32(sm + B_A1), sA2 = smem_u32(sm + B_A2);
+    const uint32_t sH1T = smem_u32(sm + B_H1T), sXT = smem_u32(sm + B_XT);
+    const uint32_t sW2T = smem_u32(sm + B_W2T);
+    constexpr uint32_t SBO_T = (TILE / 8) * 128;   // K = 128 samples
+    constexpr uint32_t SBO_H = (NH / 8) * 128;     // K = 128 hidden units
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    float loss = 0.f;
+
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t b = tile * TILE + t;
+        const bool valid = b < n;
+        float d0 = 0.f, d1 = 0.f;
+        if (valid) {
+            const float e0 = y[b * 2] - target[b * 2], e1 = y[b * 2 + 1] - target[b * 2 + 1];
+            loss += e0 * e0 + e1 * e1;
+            d0 = e0 * inv_count;
+            d1 = e1 * inv_count;
+            dy_out[b * 2] = d0;
+            dy_out[b * 2 + 1] = d1;
+        }
+        // dz2 = (dy W3) * gelu'(z2): row t of A1, column t of A2
+#pragma unroll 1
+        for (int j0 = 0; j0 < NH; j0 += 8) {
+            float z[8];
+            if (valid) {
+                const float4 a = *reinterpret_cast<const float4 *>(z2s + b * NH + j0);
+                const float4 c = *reinterpret_cast<const float4 *>(z2s + b * NH + j0 + 4);
+                z[0] = a.x; z[1] = a.y; z[2] = a.z; z[3] = a.w;
+                z[4] = c.x; z[5] = c.y; z[6] = c.z; z[7] = c.w;
+            }
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 8; i += 2) {
+                float g[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int j = j0 + i + q;
+                    g[q] = valid ? (d0 * w3f[j] + d1 * w3f[NH + j]) * dgelu(z[i + q]) : 0.f;
+                }
+                w[i / 2] = pack2(g[0], g[1]);
+            }
+            *reinterpret_cast<uint4 *>(sm + B_A1 + core_off(t, j0, NH / 8)) =
+                make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const uint16_t hv = (uint16_t)((w[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
+                *reinterpret_cast<uint16_t *>(sm + B_A2 + core_off(j0 + i, t, TILE / 8)) = hv;
+            }
+        }
+        // h1^T and x^T: column t
+#pragma unroll 1
+        for (int i0 = 0; i0 < NH; i0 += 8) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (valid) v = __ldg(reinterpret_cast<const uint4 *>(h1s + b * NH + i0));
+            const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                *reinterpret_cast<uint16_t *>(sm + B_H1T + core_off(i0 + i, t, TILE / 8)) =
+                    (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
+        }
+#pragma unroll 1
+        for (int m0 = 0; m0 < NIN; m0 += 8) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (valid) v = __ldg(reinterpret_cast<const uint4 *>(x + b * NIN + m0));
+            const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                *reinterpret_cast<uint16_t *>(sm + B_XT + core_off(m0 + i, t, TILE / 8)) =
+                    (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            // dh1 [b][i] = dz2 [b][j] W2 [j][i]   (B operand W2^T: rows i, K = j)
+#pragma unroll
+            for (int s = 0; s < NH / 16; ++s)
+                mma_bf16(tbase + T_DH1, sdesc(sA1 + s * 256, 128, SBO_H),
+                         sdesc(sW2T + s * 256, 128, SBO_H), idesc_bf16(128, NH), s > 0);
+            // dW2 [j][i] (+ db2 at column 128) += dz2^T [j][b] h1 [b][i]
+#pragma unroll
+            for (int s = 0; s < TILE / 16; ++s)
+                mma_bf16(tbase + T_DW2, sdesc(sA2 + s * 256, 128, SBO_T),
+                         sdesc(sH1T + s * 256, 128, SBO_T), idesc_bf16(128, H1T_ROWS),
+                         (s > 0 || !first) ? 1u : 0u);
+            mma_commit(bar);
+        }
+        ok = mbar_wait(bar, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+
+        // dz1 = dh1 * gelu'(z1) -> column t of A2 (its previous content is consumed)
+#pragma unroll 1
+        for (int c0 = 0; c0 < NH; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + T_DH1 + lane_base + c0, v);
+            float z[16];
+            if (valid) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 a = *reinterpret_cast<const float4 *>(z1s + b * NH + c0 + 4 * q);
+                    z[4 * q] = a.x; z[4 * q + 1] = a.y; z[4 * q + 2] = a.z; z[4 * q + 3] = a.w;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const float g = valid ? v[i] * dgelu(z[i]) : 0.f;
+                *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + core_off(c0 + i, t, TILE / 8)) =
+                    __float2bfloat16_rn(g);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            // dW1 [j][m] (+ db1 at column 192) += dz1^T [j][b] x [b][m]
+#pragma unroll
+            for (int s = 0; s < TILE / 16; ++s)
+                mma_bf16(tbase + T_DW1, sdesc(sA2 + s * 256, 128, SBO_T),
+                         sdesc(sXT + s * 256, 128, SBO_T), idesc_bf16(128, XT_ROWS),
+                         (s > 0 || !first) ? 1u : 0u);
+            mma_commit(bar);
+        }
+        ok = mbar_wait(bar, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+        first = false;
+    }
+
+    if (ok && !first) {
+        // row j = t of the accumulated weight (and bias) gradients
+        float *P = part + (int64_t)blockIdx.x * NPARAM;
+#pragma unroll 1
+        for (int c0 = 0; c0 < H1T_ROWS; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + T_DW2 + lane_base + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int c = c0 + i;
+                if (c < NH) P[OFF_W2 + t * NH + c] = v[i];
+                else if (c == NH) P[OFF_B2 + t] = v[i];
+            }
+        }
+#pragma unroll 1
+        for (int c0 = 0; c0 < XT_ROWS; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + T_DW1 + lane_base + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int c = c0 + i;
+                if (c < NIN) P[OFF_W1 + t * NIN + c] = v[i];
+                else if (c == NIN) P[OFF_B1 + t] = v[i];
+            }
+        }
+    } else if (first) {
+        float *P = part + (int64_t)blockIdx.x * NPARAM;
+        for (int i = t; i < OFF_W3; i += THREADS) P[i] = 0.f;
+    }
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (lane == 0) red[warp] = loss;
+    if (!ok && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (t == 0) part_loss[blockIdx.x] = 0.5f * inv_count * (red[0] + red[1] + red[2] + red[3]);
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, B_TMEM_COLS);
+    }
+}
+
+// third layer: dW3 [o][j] = sum_b dy[b][o] h2[b][j], db3 = sum_b dy
+__global__ void k_mlp_l3(const uint16_t *__restrict__ h2s, const float *__restrict__ dy,
+                         int64_t n, float *__restrict__ part) {
+    const int j = threadIdx.x;   // 128 threads
+    const int64_t r0 = (int64_t)blockIdx.x * L3_ROWS;
+    const int64_t r1 = min(n, r0 + L3_ROWS);
+    float a0 = 0.f, a1 = 0.f, s0 = 0.f, s1 = 0.f;
+    for (int64_t b = r0; b < r1; ++b) {
+        const float h = __uint_as_float((uint32_t)h2s[b * NH + j] << 16);
+        const float d0 = dy[b * 2], d1 = dy[b * 2 + 1];
+        a0 = fmaf(d0, h, a0);
+        a1 = fmaf(d1, h, a1);
+        s0 += d0;
+        s1 += d1;
+    }
+    float *P = part + (int64_t)blockIdx.x * L3_PART;
+    P[j] = a0;
+    P[NH + j] = a1;
+    if (j == 0) {
+        P[2 * NH] = s0;
+        P[2 * NH + 1] = s1;
+    }
+}
+
+// grad[p] = sum over CTAs (fixed order) of the partials
+__global__ void k_mlp_reduce(const float *__restrict__ part, int nparts,
+                             const float *__restrict__ l3, int nl3,
+                             const float *__restrict__ part_loss, float *__restrict__ grad,
+                             float *__restrict__ loss) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < OFF_W3) {
+        float s = 0.f;
+        for (int c = 0; c < nparts; ++c) s += part[(int64_t)c * NPARAM + p];
+        grad[p] = s;
+    } else if (p < NPARAM) {
+        float s = 0.f;
+        for (int c = 0; c < nl3; ++c) s += l3[(int64_t)c * L3_PART + (p - OFF_W3)];
+        grad[p] = s;
+    } else if (p == NPARAM && loss) {
+        float s = 0.f;
+        for (int c = 0; c < nparts; ++c) s += part_loss[c];
+        *loss = s;
+    }
+}
+
+__device__ __forceinline__ void write_copies(const MlpDev &W, uint16_t *w1, uint16_t *w2,
+                                             uint16_t *w2t, uint16_t *w3, int p, float v) {
+    const uint16_t b = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+    if (p < OFF_B1) {
+        w1[p] = b;
+    } else if (p >= OFF_W2 && p < OFF_B2) {
+        const int q = p - OFF_W2, r = q / NH, c = q % NH;
+        w2[q] = b;
+        w2t[c * NH + r] = b;
+    } else if (p >= OFF_W3 && p < OFF_B3) {
+        w3[p - OFF_W3] = b;
+    }
+}
+
+__global__ void k_mlp_sync(const float *__restrict__ params, uint16_t *w1, uint16_t *w2,
+                           uint16_t *w2t, uint16_t *w3) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < NPARAM) write_copies(MlpDev{}, w1, w2, w2t, w3, p, params[p]);
+}
+
+__global__ void k_mlp_adam(float *__restrict__ params, const float *__restrict__ grad,
+                           float *__restrict__ m, float *__restrict__ v, float lr, float beta1,
+                           float beta2, float eps, float c1, float c2, uint16_t *w1,
+                           uint16_t *w2, uint16_t *w2t, uint16_t *w3) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPARAM) return;
+    const float g = grad[p];
+    const float mp = beta1 * m[p] + (1.f - beta1) * g;
+    const float vp = beta2 * v[p] + (1.f - beta2) * g * g;
+    m[p] = mp;
+    v[p] = vp;
+    const float val = params[p] - lr * (mp * c1) / (sqrtf(vp * c2) + eps);
+    params[p] = val;
+    write_copies(MlpDev{}, w1, w2, w2t, w3, p, val);
+}
+
+// acc[c][i] (+)= (y[i][c] * scale[c] + mean[c]) * c0^2 / h_i for real particles
+__global__ void k_mlp_apply(int64_t n, const float *__restrict__ yv, const int64_t *__restrict__ tag,
+                            const double *__restrict__ h, double c0sq, double s0, double s1,
+                            double m0, double m1, double *ax, double *ay, double *az,
+                            int accumulate) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool real = tag == nullptr || tag[i] == SPH_TAG_LOCAL_REAL;
+    const double f = real ? c0sq / h[i] : 0.0;
+    const double a0 = real ? ((double)yv[2 * i] * s0 + m0) * f : 0.0;
+    const double a1 = real ? ((double)yv[2 * i + 1] * s1 + m1) * f : 0.0;
+    if (accumulate) {
+        if (ax) ax[i] += a0;
+        if (ay) ay[i] += a1;
+    } else {
+        if (ax) ax[i] = a0;
+        if (ay) ay[i] = a1;
+        if (az) az[i] = 0.0;
+    }
+}
+
+// out[i] = ((a[i] * h_i / c0^2) - mean) * inv_std, two components
+__global__ void k_mlp_targets(int64_t n, const double *__restrict__ ax, const double *__restrict__ ay,
+                              const double *__restrict__ h, double inv_c0sq, double m0, double m1,
+                              double is0, double is1, float *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double f = h[i] * inv_c0sq;
+    out[2 * i] = (float)((ax[i] * f - m0) * is0);
+    out[2 * i + 1] = (float)((ay[i] * f - m1) * is1);
+}
+
+int g_num_sms = 0;
+std::once_flag g_attr_once;
+cudaError_t g_attr_err = cudaSuccess;
+
+cudaError_t init_attrs() {
+    std::call_once(g_attr_once, [] {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, F_BYTES);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, B_BYTES);
+        g_attr_err = e;
+    });
+    return g_attr_err;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+int mlp_grid(int64_t n) {
+    if (init_attrs() != cudaSuccess) return 0;
+    const int64_t tiles = (n + TILE - 1) / TILE;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, g_num_sms));
+}
+
+int64_t mlp_backward_scratch(int64_t n) {
+    const int grid = mlp_grid(n);
+    const int64_t nl3 = (n + L3_ROWS - 1) / L3_ROWS;
+    return (int64_t)grid * NPARAM + std::max<int64_t>(nl3, 1) * L3_PART + grid + 2 * n + 4;
+}
+
+int mlp_sync(const sph_mlp_model *M, cudaStream_t st) {
+    k_mlp_sync<<<(NPARAM + 255) / 256, 256, 0, st>>>(M->params, M->w1, M->w2, M->w2t, M->w3);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_sync");
+    return SPH_OK;
+}
+
+int mlp_forward(const sph_mlp_model *M, const uint16_t *x, int64_t n, float *y, float *z1,
+                float *z2, uint16_t *h1, uint16_t *h2, unsigned *err, cudaStream_t st) {
+    if (n <= 0) return SPH_OK;
+    if (!aligned16(x) || (z1 && !aligned16(z1)) || (z2 && !aligned16(z2)) || (h1 && !aligned16(h1)) ||
+        (h2 && !aligned16(h2)) || !aligned16(M->w1) || !aligned16(M->w2))
+        return set_error(SPH_ERR_ARG, "mlp forward: buffers must be 16-byte aligned");
+    SPH_CUDA(init_attrs());
+    const MlpDev W{M->params, M->w1, M->w2, M->w2t, M->w3};
+    k_mlp_fwd<<<mlp_grid(n), THREADS, F_BYTES, st>>>(W, x, n, y, z1, z2, h1, h2, err);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_fwd");
+    return SPH_OK;
+}
+
+int mlp_backward(const sph_mlp_model *M, const uint16_t *x, const uint16_t *h1, const uint16_t *h2,
+                 const float *z1, const float *z2, const float *y, const float *target, int64_t n,
+                 float inv_count, float *grad, float *loss, float *scratch, unsigned *err,
+                 cudaStream_t st) {
+    if (n <= 0) return set_error(SPH_ERR_ARG, "mlp backward: empty batch");
+    if (!aligned16(x) || !aligned16(h1) || !aligned16(z1) || !aligned16(z2) || !aligned16(M->w2t))
+        return set_error(SPH_ERR_ARG, "mlp backward: buffers must be 16-byte aligned");
+    SPH_CUDA(init_attrs());
+    const int grid = mlp_grid(n);
+    const int nl3 = (int)std::max<int64_t>(1, (n + L3_ROWS - 1) / L3_ROWS);
+    float *part = scratch;
+    float *l3 = part + (int64_t)grid * NPARAM;
+    float *part_loss = l3 + (int64_t)nl3 * L3_PART;
+    float *dy = part_loss + grid;
+    dy = reinterpret_cast<float *>(((uintptr_t)dy + 15) & ~(uintptr_t)15);
+    const MlpDev W{M->params, M->w1, M->w2, M->w2t, M->w3};
+    k_mlp_bwd<<<grid, THREADS, B_BYTES, st>>>(W, x, h1, z1, z2, y, target, n, inv_count, dy, part,
+                                               part_loss, err);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_bwd");
+    k_mlp_l3<<<nl3, NH, 0, st>>>(h2, dy, n, l3);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_l3");
+    k_mlp_reduce<<<(NPARAM + 1 + 255) / 256, 256, 0, st>>>(part, grid, l3, nl3, part_loss, grad, loss);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_reduce");
+    return SPH_OK;
+}
+
+int mlp_adam(const sph_mlp_model *M, const float *grad, float *m, float *v, float lr, float beta1,
+             float beta2, float eps, int step, cudaStream_t st) {
+    if (step < 1) return set_error(SPH_ERR_ARG, "mlp adam: step counts from 1");
+    const float c1 = (float)(1.0 / (1.0 - std::pow((double)beta1, step)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow((double)beta2, step)));
+    k_mlp_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(M->params, grad, m, v, lr, beta1, beta2, eps,
+                                                      c1, c2, M->w1, M->w2, M->w2t, M->w3);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_adam");
+    return SPH_OK;
+}
+
+int mlp_apply(int64_t n, const float *y, const int64_t *tag, const double *h, double c0,
+              const double *scale, const double *mean, double *const *acc, int accumulate,
+              cudaStream_t st) {
+    if (n <= 0) return SPH_OK;
+    k_mlp_apply<<<(int)((n + 255) / 256), 256, 0, st>>>(n, y, tag, h, c0 * c0, scale[0], scale[1],
+                                                        mean[0], mean[1], acc[0], acc[1], acc[2],
+                                                        accumulate);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_apply");
+    return SPH_OK;
+}
+
+int mlp_targets(int64_t n, const double *ax, const double *ay, const double *h, double c0,
+                const double *mean, const double *inv_std, float *out, cudaStream_t st) {
+    if (n <= 0) return SPH_OK;
+    k_mlp_targets<<<(int)((n + 255) / 256), 256, 0, st>>>(n, ax, ay, h, 1.0 / (c0 * c0), mean[0],
+                                                          mean[1], inv_std[0], inv_std[1], out);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_mlp_targets");
+    return SPH_OK;
+}
+
+}  // namespace sphgb

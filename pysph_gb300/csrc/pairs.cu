@@ -17,6 +17,7 @@
 //
 // Sums are sequential per destination with Neumaier compensation, in the
 // neighbour order of the list (stencil rows, ascending slot).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -424,6 +425,121 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     }
 }
 
+// ---------------------------------------------------------------------------
+// features of the learned momentum closure: the 32 nearest neighbours within
+// the search radius (self included), ordered by squared distance then source
+// slot, each as ((x_i-x_j)/h_i, (y_i-y_j)/h_i, (u_j-u_i)/c0, (v_j-v_i)/c0,
+// rho_j, p_j), standardised per channel; missing neighbours are zero rows.
+// Replaces the inputs of the momentum pair loop (pressure_funcs.pyx:40-91,
+// viscosity_funcs.pyx:41-124) for the network.
+// ---------------------------------------------------------------------------
+struct FeatureArgs {
+    Grid g;
+    DestDev d;
+    SrcDev s;
+    int cap;
+    int64_t stride;
+    float inv_c0;
+    float mean[SPH_MLP_NCH], inv_std[SPH_MLP_NCH];
+    uint16_t *out_bf;   // [n][192] BF16 by original index (or null)
+    float *out_f;       // [n][192] FP32 by original index (or null)
+};
+
+template <int KX>
+__global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__ FeatureArgs A) {
+    constexpr int NN = SPH_MLP_NNBR, NC = SPH_MLP_NCH;
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= A.d.n) return;
+    DestPos d;
+    const bool real = load_dest(A.g, A.d, (int)s, d);
+    float kr2[NN], krx[NN], kry[NN];
+    int kj[NN];
+    int cnt = 0;
+    if (real) {
+        const SrcDev &S = A.s;
+        auto keep = [&](int j, float rx, float ry, float rz) {
+            const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            if (cnt == NN && !(r2 < kr2[NN - 1] || (r2 == kr2[NN - 1] && j < kj[NN - 1]))) return;
+            int k = cnt < NN ? cnt++ : NN - 1;
+            while (k > 0 && (kr2[k - 1] > r2 || (kr2[k - 1] == r2 && kj[k - 1] > j))) {
+                kr2[k] = kr2[k - 1]; krx[k] = krx[k - 1]; kry[k] = kry[k - 1]; kj[k] = kj[k - 1];
+                --k;
+            }
+            kr2[k] = r2; krx[k] = rx; kry[k] = ry; kj[k] = j;
+        };
+        if (S.nbr) {
+            const float csf = A.g.cs_f;
+            using C = Code<KX>;
+            const int c = S.ncnt[s];
+            const int m = min(c, A.cap);
+            for (int k = 0; k < m; ++k) {
+                const uint32_t e = S.nbr[s + (int64_t)k * A.stride];
+                const int j = (int)(e & C::JMASK);
+                const int code = (int)(e >> C::SHIFT);
+                constexpr int W = 2 * KX + 1;
+                const float dx = (float)(code % W - KX), dy = (float)((code / W) % W - KX),
+                            dz = (float)(code / (W * W) - KX);
+                const float4 p = S.posm[j];
+                keep(j, fmaf(-dx, csf, d.xi_x - p.x), fmaf(-dy, csf, d.xi_y - p.y),
+                     fmaf(-dz, csf, d.xi_z - p.z));
+            }
+            if (c > A.cap) {
+                int skip = A.cap;
+                for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                                   [&](int j, float rx, float ry, float rz, int) {
+                                       if (skip > 0) { --skip; return; }
+                                       keep(j, rx, ry, rz);
+                                   });
+            }
+        } else {
+            for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                               [&](int j, float rx, float ry, float rz, int) { keep(j, rx, ry, rz); });
+        }
+    }
+    const float4 vi = A.d.velh[s];
+    const float ih = 1.f / vi.w;
+    const int64_t row = (int64_t)d.orig * (NN * NC);
+#pragma unroll 1
+    for (int k = 0; k < NN; k += 4) {
+        float f[4 * NC];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float raw[NC] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            const bool have = k + q < cnt;
+            if (have) {
+                const int j = kj[k + q];
+                const float4 vj = A.s.velh[j];
+                const float4 st = A.s.st[j];
+                raw[0] = krx[k + q] * ih;
+                raw[1] = kry[k + q] * ih;
+                raw[2] = (vj.x - vi.x) * A.inv_c0;
+                raw[3] = (vj.y - vi.y) * A.inv_c0;
+                raw[4] = st.x;
+                raw[5] = st.y * st.x * st.x;
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) f[q * NC + c] = have ? (raw[c] - A.mean[c]) * A.inv_std[c] : 0.f;
+        }
+        if (A.out_bf) {
+            uint32_t w[12];
+#pragma unroll
+            for (int i = 0; i < 12; ++i) {
+                __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+                w[i] = *reinterpret_cast<uint32_t *>(&h);
+            }
+            uint4 *o = reinterpret_cast<uint4 *>(A.out_bf + row + k * NC);
+            o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+            o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+        }
+        if (A.out_f) {
+            float4 *o = reinterpret_cast<float4 *>(A.out_f + row + k * NC);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) o[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
+        }
+    }
+}
+
 DestDev make_dest(const ArraySnap &D) {
     DestDev d;
     d.posm = D.posm; d.velh = D.velh; d.st = D.st;
@@ -704,6 +820,44 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
 #undef RLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_rates");
+    return SPH_OK;
+}
+
+int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
+                    uint16_t *out_bf, float *out_f) {
+    if (!ctx->built) return set_error(SPH_ERR_STATE, "features: no neighbour build");
+    const int na = (int)ctx->arrays.size();
+    if (dst < 0 || dst >= na || src < 0 || src >= na || !prm || (!out_bf && !out_f))
+        return set_error(SPH_ERR_ARG, "features: bad arguments");
+    if (((uintptr_t)out_bf & 15u) || ((uintptr_t)out_f & 15u))
+        return set_error(SPH_ERR_ARG, "features: outputs must be 16-byte aligned");
+    if (prm->c0 <= 0.0) return set_error(SPH_ERR_ARG, "features: c0 must be positive");
+    ArraySnap &D = ctx->arrays[dst];
+    NbrList *L;
+    const int rc = ensure_list(ctx, dst, src, &L);
+    if (rc) return rc;
+    FeatureArgs a{};
+    a.g = ctx->grid;
+    a.d = make_dest(D);
+    a.s = make_src(ctx->arrays[src]);
+    a.s.nbr = L->nbr;
+    a.s.ncnt = L->cnt;
+    a.cap = L->cap;
+    a.stride = L->stride;
+    a.inv_c0 = (float)(1.0 / prm->c0);
+    for (int c = 0; c < SPH_MLP_NCH; ++c) {
+        a.mean[c] = prm->mean[c];
+        a.inv_std[c] = prm->inv_std[c];
+    }
+    a.out_bf = out_bf;
+    a.out_f = out_f;
+    if (D.n == 0) return SPH_OK;
+    const int b = blocks_for(D.n);
+    if (a.g.kx == 1) k_features<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else if (a.g.kx == 2) k_features<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    else k_features<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_features");
     return SPH_OK;
 }
 

@@ -175,6 +175,26 @@ int batch_density(sph_batch *b);
 int batch_rates(sph_batch *b, double *const *acc, double *const *pos);
 int batch_step(sph_batch *b, int nsteps, int use_graph);
 int batch_pair_counts(sph_batch *b, unsigned long long *out);
+
+// learned momentum closure
+int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
+                    uint16_t *out_bf, float *out_f);
+int mlp_grid(int64_t n);
+int64_t mlp_backward_scratch(int64_t n);
+int mlp_sync(const sph_mlp_model *M, cudaStream_t st);
+int mlp_forward(const sph_mlp_model *M, const uint16_t *x, int64_t n, float *y, float *z1,
+                float *z2, uint16_t *h1, uint16_t *h2, unsigned *err, cudaStream_t st);
+int mlp_backward(const sph_mlp_model *M, const uint16_t *x, const uint16_t *h1, const uint16_t *h2,
+                 const float *z1, const float *z2, const float *y, const float *target, int64_t n,
+                 float inv_count, float *grad, float *loss, float *scratch, unsigned *err,
+                 cudaStream_t st);
+int mlp_adam(const sph_mlp_model *M, const float *grad, float *m, float *v, float lr, float beta1,
+             float beta2, float eps, int step, cudaStream_t st);
+int mlp_apply(int64_t n, const float *y, const int64_t *tag, const double *h, double c0,
+              const double *scale, const double *mean, double *const *acc, int accumulate,
+              cudaStream_t st);
+int mlp_targets(int64_t n, const double *ax, const double *ay, const double *h, double c0,
+                const double *mean, const double *inv_std, float *out, cudaStream_t st);
 void batch_free(sph_batch *b);
 int list_maxima_async(sph_ctx *ctx);
 void list_maxima_collect(sph_ctx *ctx);

@@ -39,7 +39,31 @@ EXPORTS = (
     "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
     "sph_batch_sync", "sph_batch_error_word", "sph_batch_stream",
     "sph_batch_pair_counts",
+    "sph_mlp_features", "sph_mlp_sync", "sph_mlp_forward", "sph_mlp_backward_scratch",
+    "sph_mlp_backward", "sph_mlp_adam", "sph_mlp_apply", "sph_mlp_targets",
 )
+
+# learned momentum closure (include/pysph_gb300.h SPH_MLP_*)
+MLP_NIN, MLP_NH, MLP_NOUT = 192, 128, 2
+MLP_NNBR, MLP_NCH = 32, 6
+MLP_OFF_W1 = 0
+MLP_OFF_B1 = MLP_OFF_W1 + MLP_NH * MLP_NIN
+MLP_OFF_W2 = MLP_OFF_B1 + MLP_NH
+MLP_OFF_B2 = MLP_OFF_W2 + MLP_NH * MLP_NH
+MLP_OFF_W3 = MLP_OFF_B2 + MLP_NH
+MLP_OFF_B3 = MLP_OFF_W3 + MLP_NOUT * MLP_NH
+MLP_NPARAM = MLP_OFF_B3 + MLP_NOUT
+SPH_EFLAG_TIMEOUT = 8
+
+
+class MlpModel(ctypes.Structure):
+    _fields_ = [("params", ctypes.c_void_p), ("w1", ctypes.c_void_p), ("w2", ctypes.c_void_p),
+                ("w2t", ctypes.c_void_p), ("w3", ctypes.c_void_p)]
+
+
+class MlpFeatureParams(ctypes.Structure):
+    _fields_ = [("c0", ctypes.c_double), ("mean", ctypes.c_float * MLP_NCH),
+                ("inv_std", ctypes.c_float * MLP_NCH)]
 
 
 class ArrayView(ctypes.Structure):
@@ -145,6 +169,16 @@ def load_library(build_if_missing=True):
         L.sph_mean_neighbours.argtypes = [vp, i32, i32, P(d)]
         L.sph_launch_count.argtypes = [P(i64)]
         L.sph_invariants_noalloc.argtypes = [P(ArrayView), P(d), vp]
+        f32 = ctypes.c_float
+        L.sph_mlp_features.argtypes = [vp, i32, i32, P(MlpFeatureParams), vp, vp]
+        L.sph_mlp_sync.argtypes = [P(MlpModel), vp]
+        L.sph_mlp_forward.argtypes = [P(MlpModel), vp, i64, vp, vp, vp, vp, vp, vp, vp]
+        L.sph_mlp_backward_scratch.argtypes = [i64, P(i64)]
+        L.sph_mlp_backward.argtypes = [P(MlpModel), vp, vp, vp, vp, vp, vp, vp, i64, f32, vp, vp,
+                                       vp, vp, vp]
+        L.sph_mlp_adam.argtypes = [P(MlpModel), vp, vp, vp, f32, f32, f32, f32, i32, vp]
+        L.sph_mlp_apply.argtypes = [vp, i32, vp, d, P(d), P(d), P(vp), i32]
+        L.sph_mlp_targets.argtypes = [i64, vp, vp, vp, d, P(d), P(d), vp, vp]
         for name in EXPORTS:
             getattr(L, name).restype = ctypes.c_int
         _lib = L

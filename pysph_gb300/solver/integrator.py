@@ -92,6 +92,9 @@ class RatesStage:
         self.gravity = None
         self.add_velocity = False
         self.props = []
+        # objects with before_rates(integ, stage, terms) -> terms and
+        # after_rates(integ, stage, acc) (learned closure, sample recorder)
+        self.hooks = []
         dim = None
         for c in calcs:
             kind = _kind_of(c.funcs[0])
@@ -144,10 +147,15 @@ class RatesStage:
         accumulate = not fresh
         acc = [rate.get(p) if p in self.props else None for p in VEL]
         pos = [rate.get(p) if p in self.props else None for p in POS]
-        if self.terms or self.gravity or self.add_velocity:
-            gpu.rates(cm, self.dest, self.terms, self.dim, acc=acc, pos=pos,
+        terms = self.terms
+        for hk in self.hooks:
+            terms = hk.before_rates(integ, self, terms)
+        if terms or self.gravity or self.add_velocity or (self.hooks and not accumulate):
+            gpu.rates(cm, self.dest, terms, self.dim, acc=acc, pos=pos,
                       accumulate=accumulate, gravity=self.gravity,
                       add_velocity=self.add_velocity)
+        for hk in self.hooks:
+            hk.after_rates(integ, self, acc)
         written.update(self.props)
 
 

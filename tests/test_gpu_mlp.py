@@ -1,0 +1,213 @@
+"""Learned momentum closure on the GPU: the tensor-core network kernels
+against the FP64 oracle (forward, gradients, Adam), the feature gather
+against the oracle's neighbour ordering, and the closure in a solver."""
+import numpy as np
+import pytest
+import torch
+
+import pysph_gb300
+from oracle import mlp as M
+from pysph_gb300 import learned as L
+from pysph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+API = pysph_gb300.api()
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _model(seed, bias=0.1):
+    rng = np.random.default_rng(seed)
+    p = M.init_params(seed)
+    p[M.OFF_B1:M.OFF_W2] = rng.normal(0, bias, M.NH)
+    p[M.OFF_B2:M.OFF_W3] = rng.normal(0, bias, M.NH)
+    p[M.OFF_B3:] = rng.normal(0, bias, M.NOUT)
+    model = L.MomentumMLP(device="cuda")
+    model.set_params(p)
+    return model, model.params.cpu().numpy().astype(np.float64)
+
+
+def _x(n, seed):
+    rng = np.random.default_rng(seed)
+    x = torch.tensor(rng.normal(0, 1, (n, M.NIN)), dtype=torch.float32).to(torch.bfloat16)
+    return x.cuda().contiguous(), x.to(torch.float64).numpy()
+
+
+@pytest.mark.parametrize("n", [1, 128, 300, 5000])
+def test_forward_matches_oracle(n):
+    _need_gpu()
+    model, p = _model(1)
+    xg, xh = _x(n, 2)
+    y, cache = model.forward(xg, save=True)
+    torch.cuda.synchronize()
+    model.check()
+    yr, c = M.forward(p, xh)
+    assert _rel(y.cpu().numpy(), yr) < 1e-3
+    assert _rel(cache["z1"].cpu().numpy(), c["z1"]) < 1e-5
+    assert _rel(cache["z2"].cpu().numpy(), c["z2"]) < 1e-3
+    assert _rel(cache["h1"].float().cpu().numpy(), c["h1"]) < 1e-3
+    # inference without the saved values gives the same outputs
+    y2 = model.forward(xg)
+    assert torch.equal(y, y2)
+
+
+@pytest.mark.parametrize("n", [200, 4096, 20000])
+def test_gradient_matches_oracle(n):
+    """The GPU gradient (tensor-core products, FP32 accumulation) against
+    the FP64 oracle with the same BF16 rounding points."""
+    _need_gpu()
+    model, p = _model(3)
+    xg, xh = _x(n, 4)
+    rng = np.random.default_rng(5)
+    t = rng.normal(0, 1, (n, M.NOUT))
+    tg = torch.tensor(t, dtype=torch.float32, device="cuda")
+    y, cache = model.forward(xg, save=True)
+    g, loss = model.backward(xg, cache, y, tg)
+    torch.cuda.synchronize()
+    model.check()
+    lr, gr = M.backward(p, xh, t.astype(np.float32).astype(np.float64))
+    g = g.cpu().numpy()
+    for name, a, b in (("W1", M.OFF_W1, M.OFF_B1), ("b1", M.OFF_B1, M.OFF_W2),
+                       ("W2", M.OFF_W2, M.OFF_B2), ("b2", M.OFF_B2, M.OFF_W3),
+                       ("W3", M.OFF_W3, M.OFF_B3), ("b3", M.OFF_B3, M.NPARAM)):
+        assert _rel(g[a:b], gr[a:b]) < 5e-3, (name, _rel(g[a:b], gr[a:b]))
+    assert abs(float(loss.item()) - lr) / lr < 1e-4
+
+
+def test_gradient_deterministic():
+    _need_gpu()
+    model, _ = _model(6)
+    xg, _ = _x(3000, 7)
+    tg = torch.randn(3000, 2, device="cuda")
+    y, cache = model.forward(xg, save=True)
+    g1 = model.backward(xg, cache, y, tg)[0].clone()
+    g2 = model.backward(xg, cache, y, tg)[0].clone()
+    assert torch.equal(g1, g2)
+
+
+def test_adam_matches_oracle():
+    _need_gpu()
+    model, p = _model(8)
+    xg, xh = _x(512, 9)
+    tg = torch.randn(512, 2, device="cuda")
+    m = np.zeros(M.NPARAM)
+    v = np.zeros(M.NPARAM)
+    for step in range(1, 4):
+        y, cache = model.forward(xg, save=True)
+        g, _ = model.backward(xg, cache, y, tg)
+        gh = g.cpu().numpy().astype(np.float64)
+        model.adam(1e-3)
+        p, m, v = M.adam(p, gh, m, v, step, 1e-3)
+    got = model.params.cpu().numpy()
+    assert np.max(np.abs(got - p)) < 1e-6
+    # the BF16 copies follow the FP32 parameters
+    w1 = model.w1.float().cpu().numpy()
+    assert np.array_equal(w1, M.bf16(got[M.OFF_W1:M.OFF_B1]).astype(np.float32))
+    w2t = model.w2t.float().cpu().numpy().reshape(M.NH, M.NH)
+    assert np.array_equal(w2t.T.ravel(), model.w2.float().cpu().numpy())
+
+
+def test_training_fits_a_teacher_network():
+    """Train against targets of a fixed random network: the loss falls by
+    well over an order of magnitude."""
+    _need_gpu()
+    teacher, _ = _model(10, bias=0.3)
+    xg, _ = _x(65536, 11)
+    t = teacher.forward(xg)
+    t = (t - t.mean(0)) / t.std(0)
+    model = L.MomentumMLP(seed=12)
+    losses = L.train(model, xg, t.contiguous(), epochs=20, batch=2048, lr=2e-3)
+    assert losses[-1] < 0.1 * losses[0], losses
+
+
+def _jittered_drop(seed=0, dx=0.05):
+    props = W.elliptical_drop(dx=dx, c0=100.0, radius=0.6)
+    rng = np.random.default_rng(seed)
+    n = len(props["x"])
+    props["x"] = props["x"] + rng.uniform(-0.1, 0.1, n) * dx
+    props["y"] = props["y"] + rng.uniform(-0.1, 0.1, n) * dx
+    props["u"] = props["u"] + rng.normal(0, 1, n)
+    return props
+
+
+def test_features_match_oracle():
+    _need_gpu()
+    props = _jittered_drop()
+    s, particles = W.setup_drop(API, props, c0=100.0)
+    integ = s.integrator
+    integ.integrate(1e-5)            # a step, so rho and p are the device's
+    cm = particles.cell_manager
+    pa = particles.arrays[0]
+    norm = L.Normalisation(100.0)
+    # a density pass at the current positions refreshes the sorted state
+    stage = integ.stages[0]
+    integ.cstep = 1
+    stage.run(integ, "k1")
+    raw = L.features(cm, pa, norm, raw=True).cpu().numpy()
+    host = {k: pa.get(k) for k in ("x", "y", "u", "v", "h", "rho", "p")}
+    want = M.features(host, 100.0, np.zeros(6), np.ones(6))
+    assert raw.shape == want.shape
+    np.testing.assert_allclose(raw, want, rtol=1e-5, atol=2e-5)
+    # standardised BF16 rows are the rounded standardised values
+    fm = np.array([0.1, -0.2, 0.01, 0.02, 1.0, 5.0])
+    fs = np.array([0.9, 0.8, 0.3, 0.4, 0.01, 20.0])
+    bf = L.features(cm, pa, L.Normalisation(100.0, fm, fs)).float().cpu().numpy()
+    want_s = M.features(host, 100.0, fm, 1.0 / fs)
+    np.testing.assert_allclose(bf, M.bf16(want_s), rtol=1e-2, atol=1e-3)
+
+
+def _small_dam(dx=0.04):
+    fluid, wall = W.dam_break(dx=dx)
+    c0 = W.dam_break_c0()
+    s, particles = W.setup_dam_break(API, fluid, wall, dx, c0)
+    return s, particles, c0
+
+
+def test_closure_records_trains_and_steps():
+    _need_gpu()
+    s, particles, c0 = _small_dam()
+    fluid = particles.arrays[0]
+    n = fluid.get_number_of_particles()
+    rec = L.SampleRecorder(s.integrator, fluid, c0, capacity=40 * n, every=1)
+    for _ in range(20):
+        s.integrator.integrate(1e-4)
+    rec.detach()
+    x, t, norm = rec.finish()
+    assert rec.count == 40 * n
+    assert torch.isfinite(t).all() and torch.isfinite(x.float()).all()
+    model = L.MomentumMLP(seed=0)
+    losses = L.train(model, x, t, epochs=6, batch=2048, lr=2e-3)
+    assert losses[-1] < losses[0]
+    closure = L.LearnedClosure(s.integrator, fluid, model, norm)
+    runner = L.GuardedRunner(s, particles, closure, k=5, tol=1.0)
+    runner.window(1e-4)
+    runner.window(1e-4)
+    assert runner.checks == 2 and runner.fallbacks == 0
+    assert np.isfinite(fluid.get("u")).all() and np.isfinite(fluid.get("rho")).all()
+    assert np.isfinite(runner.max_err)
+
+
+def test_guarded_runner_restores_exactly():
+    """Re-running a window with the plain pair loop from its saved start
+    reproduces it bit for bit (the density difference of a window whose
+    closure is inactive is exactly zero)."""
+    _need_gpu()
+    import types
+    s, particles, c0 = _small_dam()
+    fluid = particles.arrays[0]
+    for _ in range(5):
+        s.integrator.integrate(1e-4)
+    dummy = types.SimpleNamespace(active=False, dest=fluid)
+    runner = L.GuardedRunner(s, particles, dummy, k=4, tol=0.0)
+    runner.window(1e-4)
+    runner.window(1e-4)
+    assert runner.checks == 2 and runner.max_err == 0.0 and runner.fallbacks == 0
