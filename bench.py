@@ -557,6 +557,129 @@ def run_reference_drops(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# learned momentum closure on the 80,000-particle dam break
+# ---------------------------------------------------------------------------
+CLOSURE_METRIC = "steps/s (2D dam break dx=0.005, RK2, learned closure vs plain)"
+
+
+def run_gpu_closure(args):
+    import numpy as np
+    import torch
+
+    import pysph_gb300
+    from pysph_gb300 import learned as L
+    from pysph_gb300 import native
+    from pysph_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    api = pysph_gb300.api()
+    log = (lambda m: print(m, file=sys.stderr, flush=True))
+    rng = np.random.default_rng(0)
+    aspects = sorted(rng.uniform(0.3, 1.0, 5).tolist())
+    t0 = time.perf_counter()
+    raw, targ, c0 = L.dam_break_samples(api, aspects, dx=0.01, dt=args.train_dt,
+                                        steps=args.train_steps, every=args.every,
+                                        capacity=args.samples, log=log)
+    x, t, norm = L.standardise(raw, targ, c0)
+    del raw, targ
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    model = L.MomentumMLP(seed=0)
+    t0 = time.perf_counter()
+    losses = L.train(model, x, t, epochs=args.epochs, batch=8192, lr=2e-3, log=log)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    # training throughput of the tensor-core kernels: forward + backward
+    nb = x.shape[0] // 8192
+    flops = 6.0 * (192 * 128 + 128 * 128 + 128 * 2) * nb * 8192 * args.epochs
+    del x, t
+
+    dx, dt, nsteps = 0.005, args.dt, args.closure_steps
+    ckpt = max(1, nsteps // 10)
+
+    def fresh():
+        fluid, wall = W.dam_break(dx=dx)
+        return W.setup_dam_break(api, fluid, wall, dx, c0)
+
+    def plain_run():
+        s, particles = fresh()
+        fl = particles.arrays[0]
+        for _ in range(3):
+            s.integrator.integrate(dt)
+        torch.cuda.synchronize()
+        refs = []
+        t1 = time.perf_counter()
+        for k in range(1, nsteps + 1):
+            s.integrator.integrate(dt)
+            if k % ckpt == 0:
+                refs.append(fl.get_device("rho").clone())
+        torch.cuda.synchronize()
+        return time.perf_counter() - t1, refs, fl.get_number_of_particles()
+
+    t_plain, refs, n = plain_run()
+    log("plain: %.3f s for %d steps" % (t_plain, nsteps))
+
+    def surrogate_run(k=None):
+        s, particles = fresh()
+        fl = particles.arrays[0]
+        for _ in range(3):
+            s.integrator.integrate(dt)
+        closure = L.LearnedClosure(s.integrator, fl, model, norm)
+        errs = []
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        runner = None
+        try:
+            if k is None:
+                for j in range(1, nsteps + 1):
+                    s.integrator.integrate(dt)
+                    if j % ckpt == 0:
+                        r = refs[j // ckpt - 1]
+                        errs.append(float(((fl.get_device("rho") - r).abs() / r).max().item()))
+            else:
+                runner = L.GuardedRunner(s, particles, closure, k=k, tol=args.tol)
+                done = 0
+                while done < nsteps:
+                    runner.window(dt)
+                    done += k
+                    if done % ckpt == 0:
+                        r = refs[done // ckpt - 1]
+                        errs.append(float(((fl.get_device("rho") - r).abs() / r).max().item()))
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t1
+            out = {"steps_per_s": nsteps / el, "max_rel_density_error": max(errs) if errs else None,
+                   "rel_density_error_at_checkpoints": errs}
+        except RuntimeError as e:
+            out = {"failed": str(e)[:120]}
+        if runner is not None:
+            out.update(windows=runner.windows, checks=runner.checks, fallbacks=runner.fallbacks)
+        return out
+
+    res = {"surrogate_only": surrogate_run(None)}
+    for k in (5, 10, 20):
+        res["guarded_k%d" % k] = surrogate_run(k)
+        log("k=%d: %s" % (k, res["guarded_k%d" % k]))
+    plain_sps = nsteps / t_plain
+    line = {
+        "metric": CLOSURE_METRIC, "value": plain_sps, "unit": "steps/s", "n_gpus": 1,
+        "steps": nsteps, "warmup": 3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "ms_per_step": 1e3 / plain_sps, "dtype": "bf16 network (fp32 accumulate), f32 pair sums, f64 integration",
+        "data": "synthetic (dam-break lattices)",
+        "config": {"workload": "2D dam break, dx=%g, %d fluid particles, RK2 dt=%g; closure "
+                               "trained on dx=0.01 runs at aspect ratios %s" % (
+                                   dx, n, dt, ["%.3f" % a for a in aspects]),
+                   "tolerance": args.tol, "train_steps": args.train_steps, "every": args.every},
+        "plain_steps_per_s": plain_sps,
+        "closure": res,
+        "training": {"samples": int(nb * 8192), "epochs": args.epochs, "loss_first": losses[0],
+                     "loss_last": losses[-1], "seconds": t_train, "data_seconds": t_data,
+                     "tflops_fwd_bwd": flops / t_train / 1e12},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -588,7 +711,15 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--procs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cube", choices=["cube", "drops"])
+    ap.add_argument("--workload", default="cube", choices=["cube", "drops", "closure"])
+    ap.add_argument("--samples", type=int, default=10_000_000)
+    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--train-dt", type=float, default=2.5e-5)
+    ap.add_argument("--every", type=int, default=20)
+    ap.add_argument("--dt", type=float, default=1.25e-5)
+    ap.add_argument("--tol", type=float, default=1e-3)
+    ap.add_argument("--closure-steps", type=int, default=1000)
     ap.add_argument("--drops", type=int, default=256)
     ap.add_argument("--drop-c0", type=float, default=100.0)
     ap.add_argument("--drop-sample", type=int, default=8)
@@ -597,6 +728,12 @@ def main():
         args.warmup = 3
     if args.workload == "drops":
         (run_reference_drops if args.impl == "reference" else run_gpu_drops)(args)
+    elif args.workload == "closure":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned "
+                              "closure; its plain dam break is the cube/drops reference arm"}))
+        else:
+            run_gpu_closure(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -462,3 +462,37 @@ class GuardedRunner:
         else:
             self._restore(surr)
         self.closure.active = True
+
+
+def dam_break_samples(api, aspects, dx=0.01, dt=1e-4, steps=2000, every=40, capacity=None,
+                      height=2.0, log=None):
+    """Record closure samples from plain dam-break runs, one per column
+    aspect ratio (width / height): the fluid-on-itself pressure gradient +
+    viscosity of every ``every``-th evaluation.  Returns the raw FP32
+    features, raw targets and c0 (samples of all runs concatenated)."""
+    from . import workloads as W
+    c0 = W.dam_break_c0(height=height)
+    raws, targs = [], []
+    left = capacity
+    for a in aspects:
+        fluid, wall = W.dam_break(dx=dx, column=(a * height, height))
+        s, particles = W.setup_dam_break(api, fluid, wall, dx, c0)
+        fl = particles.arrays[0]
+        n = fl.get_number_of_particles()
+        cap = (2 * steps // every + 1) * n
+        if left is not None:
+            cap = min(cap, left // max(1, len(aspects) - len(raws)))
+        rec = SampleRecorder(s.integrator, fl, c0, capacity=cap, every=every)
+        for _ in range(steps):
+            s.integrator.integrate(dt)
+            if rec.full:
+                break
+        rec.detach()
+        raws.append(rec.raw[:rec.count])
+        targs.append(rec.t[:rec.count])
+        if left is not None:
+            left -= rec.count
+        if log:
+            log("aspect %.3f: %d fluid particles, %d samples" % (a, n, rec.count))
+        del s, particles
+    return torch.cat(raws), torch.cat(targs), c0
