@@ -211,6 +211,11 @@ def cpu_baseline(procs, warmup, steps, n=SAMPLE_N):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def _skin():
+    from pysph_gb300.tuning import list_skin
+    return list_skin()
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -273,6 +278,7 @@ def run_gpu(args):
         pg.barrier()
     launches = native.launch_count() - launches0
     clk = clocks.stop()
+    builds = cm.build_stats()
     events = integ.stage_events
     integ.stage_events = None
     t_total = sum(step_ms) / 1e3
@@ -330,6 +336,8 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "steps_per_s": 1.0 / step_s,
         "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
+        "nnps_builds": {"full": builds[0], "light": builds[1],
+                        "skin": "list skin %.3g of the search radius" % _skin()},
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": 8 * n * len(fields_in),

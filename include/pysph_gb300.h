@@ -132,6 +132,26 @@ int sph_launch_count(int64_t *out);
 int sph_nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
                    double radius_scale, int subdiv, int check_jump);
 
+/* Neighbour-list skin as a fraction of the search radius (0 .. 0.5; 0 =
+ * lists hold exactly the neighbours).  With a skin the grid cell is
+ * cell_size (1 + fraction) / subdiv and every list keeps the sources within
+ * radius_scale h + skin; the passes that stream a list keep the exact
+ * neighbours, so results do not depend on the skin.  Takes effect at the
+ * next build.  No reference counterpart (the reference rebuilds its lists
+ * at every update, base/nnps.pyx:581-620). */
+int sph_ctx_set_skin(sph_ctx *ctx, double skin_fraction);
+/* Particles.update() (base/particles.py:159-200 -> cell.pyx:927-1015):
+ * with a skin and the same arrays, refresh the sorted snapshot in the
+ * order of the last full build (one kernel, the reference's jump check
+ * against the previous update) while every particle is within half the
+ * skin of its build position, its h unchanged and no list overflowed;
+ * otherwise a full sph_nnps_build.  *rebuilt (may be NULL) tells which.
+ * Synchronises the stream once. */
+int sph_nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+                    double radius_scale, int subdiv, int check_jump, int *rebuilt);
+/* out[0] = full builds, out[1] = light refreshes of this context. */
+int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
+
 /* Neighbour lists of destination dst among source src (radius
  * radius_scale*h_dst, radius_scale no larger than the build's), as original particle
  * indices: counts[i] (device, int64, n_dst) then, given the exclusive prefix

@@ -125,6 +125,8 @@ class CellManager:
             dim = 3
             h = ctypes.c_void_p()
             native.check(L.sph_ctx_create(dim, ctypes.byref(h)), "sph_ctx_create")
+            from ..tuning import list_skin
+            native.check(L.sph_ctx_set_skin(h, list_skin()), "sph_ctx_set_skin")
             self._ctx = h
         native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
             torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
@@ -155,8 +157,10 @@ class CellManager:
         views = (native.ArrayView * len(self.arrays_to_bin))(
             *[array_view(pa) for pa in self.arrays_to_bin])
         check = 0 if self.skip_jump_once else 1
-        rc = native.lib().sph_nnps_build(ctx, views, len(self.arrays_to_bin), self.cell_size,
-                                         self.max_radius_scale, self._subdivision(), check)
+        rebuilt = ctypes.c_int(1)
+        rc = native.lib().sph_nnps_update(ctx, views, len(self.arrays_to_bin), self.cell_size,
+                                          self.max_radius_scale, self._subdivision(), check,
+                                          ctypes.byref(rebuilt))
         self.skip_jump_once = False
         native.check(rc, "CellManager.update")
         self._views = views
@@ -164,6 +168,27 @@ class CellManager:
         for pa in self.arrays_to_bin:
             pa.set_dirty(False)
         self.is_dirty = False
+        self._build_count += 1
+        return 0
+
+    def rebuild(self, check_jump=True):
+        """A full neighbour build now, sorting afresh (the lists then depend
+        only on the current state, not on the update history)."""
+        if not torch.cuda.is_available():
+            return 0
+        ctx = self.context()
+        views = (native.ArrayView * len(self.arrays_to_bin))(
+            *[array_view(pa) for pa in self.arrays_to_bin])
+        rc = native.lib().sph_nnps_build(ctx, views, len(self.arrays_to_bin), self.cell_size,
+                                         self.max_radius_scale, self._subdivision(),
+                                         1 if check_jump else 0)
+        native.check(rc, "CellManager.rebuild")
+        self._views = views
+        self._snap_versions = [pa.version for pa in self.arrays_to_bin]
+        for pa in self.arrays_to_bin:
+            pa.set_dirty(False)
+        self.is_dirty = False
+        self.skip_jump_once = False
         self._build_count += 1
         return 0
 
@@ -181,6 +206,14 @@ class CellManager:
                 native.check(native.lib().sph_refresh_state(ctx, i, ctypes.byref(v)),
                              "refresh snapshot")
                 self._snap_versions[i] = pa.version
+
+    def build_stats(self):
+        """(full neighbour builds, light refreshes) of this cell manager."""
+        if self._ctx is None:
+            return (0, 0)
+        out = (ctypes.c_int64 * 2)()
+        native.check(native.lib().sph_nnps_stats(self._ctx, out), "sph_nnps_stats")
+        return (int(out[0]), int(out[1]))
 
     def mark_fresh(self, pa):
         """The snapshot of ``pa`` already matches its data (written together)."""

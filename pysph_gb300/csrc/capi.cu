@@ -98,9 +98,9 @@ int sph_ctx_destroy(sph_ctx *c) {
         cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
         cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st);
         cudaFree(A.nrm); cudaFree(A.tan);
-        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell);
+        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0);
     }
-    cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_err);
+    cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_err); cudaFree(c->d_disp);
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);
     if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_red) cudaFreeHost(c->h_red);
@@ -119,6 +119,31 @@ int sph_nnps_build(sph_ctx *c, const sph_array_view *arrays, int narrays, double
                    double radius_scale, int subdiv, int check_jump) {
     CHECK_CTX(c);
     return nnps_build(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
+}
+
+int sph_nnps_update(sph_ctx *c, const sph_array_view *arrays, int narrays, double cell_size,
+                    double radius_scale, int subdiv, int check_jump, int *rebuilt) {
+    CHECK_CTX(c);
+    return nnps_update(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump, rebuilt);
+}
+
+int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
+    CHECK_CTX(c);
+    if (!(skin_fraction >= 0.0) || skin_fraction > 0.5)
+        return set_error(SPH_ERR_ARG, "sph_ctx_set_skin: fraction must be in [0, 0.5]");
+    if (skin_fraction != c->skin_frac) {
+        c->skin_frac = skin_fraction;
+        c->built = false;   // the next update builds afresh
+    }
+    return SPH_OK;
+}
+
+int sph_nnps_stats(sph_ctx *c, int64_t *out) {
+    CHECK_CTX(c);
+    if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_stats: null out");
+    out[0] = c->n_full;
+    out[1] = c->n_light;
+    return SPH_OK;
 }
 
 int sph_nnps_count(sph_ctx *c, int dst, int src, double radius_scale, int64_t *counts) {

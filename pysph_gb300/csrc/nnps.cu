@@ -264,6 +264,74 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
     }
 }
 
+// Light refresh: the snapshot of slot s in the cell of the last full build,
+// the largest squared displacement from the build position, h changes and
+// the jump check against the previous update's cells.
+constexpr unsigned kLightHChanged = 1u << 8;
+
+__global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *perm,
+                        const int *skey, const float4 *posm0, float4 *posm, float4 *velh,
+                        float4 *st, float4 *nrm, float4 *tan, int *refcell, int check_jump,
+                        unsigned *dmax, unsigned *err) {
+    float dm = 0.f;
+    bool jump = false, hch = false;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int i = perm[s];
+        int cx, cy, cz;
+        decode_cell(g, skey[s], cx, cy, cz);
+        const double px = ld0(a.x, i), py = ld0(a.y, i), pz = ld0(a.z, i);
+        const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
+        const float xi = (float)fma(-ox, g.cs, px);
+        const float yi = (float)fma(-oy, g.cs, py);
+        const float zi = (float)fma(-oz, g.cs, pz);
+        const float4 p0 = posm0[s];
+        const float ddx = xi - p0.x, ddy = yi - p0.y, ddz = zi - p0.z;
+        dm = fmaxf(dm, fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)));
+        posm[s] = make_float4(xi, yi, zi, (float)cx);
+        const float hf = (float)a.h[i];
+        if (hf != velh[s].w) hch = true;
+        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), hf);
+        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
+        if (nrm) {
+            nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
+            tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
+        }
+        const double pp[3] = {px, py, pz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int c = floor_cell(pp[d], inv_cs_ref);
+            if (check_jump && abs(c - refcell[3 * i + d]) > 1) jump = true;
+            refcell[3 * i + d] = c;
+        }
+    }
+    // warp, then block, then one atomic per block
+    __shared__ float s_dm[32];
+    __shared__ unsigned s_fl[32];
+    for (int off = 16; off > 0; off >>= 1) dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, off));
+    const unsigned fl = (__any_sync(0xffffffffu, jump) ? SPH_EFLAG_JUMP : 0u) |
+                        (__any_sync(0xffffffffu, hch) ? kLightHChanged : 0u);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        s_dm[wid] = dm;
+        s_fl[wid] = fl;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        float b = lane < nw ? s_dm[lane] : 0.f;
+        unsigned f = lane < nw ? s_fl[lane] : 0u;
+        for (int off = 16; off > 0; off >>= 1) {
+            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, off));
+            f |= __shfl_xor_sync(0xffffffffu, f, off);
+        }
+        if (lane == 0) {
+            if (b > 0.f) atomicMax(dmax, __float_as_uint(b));
+            if (f) atomicOr(err, f);
+        }
+    }
+}
+
 // -------------------------------------------------------------------------
 // neighbour export (exact FP64 test; API / parity path, not the hot loop)
 // -------------------------------------------------------------------------
@@ -400,7 +468,10 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     if (ctx->cell_size_ref != cell_size) same_layout = false;
     ctx->cell_size_ref = cell_size;
 
-    const double cs = cell_size / subdiv;
+    // with a list skin the grid cell is the reference cell grown by the skin
+    // fraction, so the stencil of the subdivision still covers the list radius
+    const double skin_frac = ctx->skin_frac > 0.0 ? ctx->skin_frac : 0.0;
+    const double cs = cell_size * (1.0 + skin_frac) / subdiv;
     const double inv_cs = 1.0 / cs;
     const double inv_cs_ref = 1.0 / cell_size;
 
@@ -458,7 +529,11 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     g.radius_scale = radius_scale;
     g.uniform_h = (hmin == hmax) ? 1 : 0;
     g.h_uniform = (float)hmax;
-    int k = (int)std::ceil(radius_scale * hmax * inv_cs - 1e-9);
+    const double skin = skin_frac * radius_scale * hmax;
+    g.skin = (float)skin;
+    // the list radius over the grid cell, (rs hmax (1 + f)) / (cell (1 + f) / subdiv),
+    // is the subdivision itself when cell = rs hmax; the margin absorbs rounding
+    int k = (int)std::ceil((radius_scale * hmax + skin) * inv_cs - 1e-7);
     if (k < 1) k = 1;
     if (k > 3)
         return set_error(SPH_ERR_NOTSUP,
@@ -521,10 +596,95 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
                                                A.has_nrm ? A.tan : nullptr);
             count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
+            if (g.skin > 0.f) {
+                if (A.posm0_cap < v.n) {
+                    cudaFree(A.posm0);
+                    A.posm0 = nullptr;
+                    SPH_CUDA(cudaMalloc(&A.posm0, sizeof(float4) * v.n));
+                    A.posm0_cap = v.n;
+                }
+                SPH_CUDA(cudaMemcpyAsync(A.posm0, A.posm, sizeof(float4) * v.n,
+                                         cudaMemcpyDeviceToDevice, st));
+            }
         }
     }
     ctx->built = true;
     ctx->build_id += 1;
+    ctx->build_radius_scale = radius_scale;
+    ctx->build_subdiv = subdiv;
+    ctx->n_full += 1;
+    return SPH_OK;
+}
+
+// Refresh the sorted snapshot of moved particles in the order of the last
+// full build (the skin keeps the neighbour lists of that build valid while
+// every particle stays within half the skin of its build position), with
+// the reference's jump check (cell.pyx:1422-1437) against the previous
+// update.  Falls back to a full build when a particle moved too far, an h
+// changed, the array layout changed, or a list overflowed its capacity.
+int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+                double radius_scale, int subdiv, int check_jump, int *rebuilt) {
+    if (rebuilt) *rebuilt = 1;
+    bool light = ctx->built && ctx->grid.skin > 0.f && narrays == (int)ctx->arrays.size() &&
+                 cell_size == ctx->cell_size_ref && radius_scale == ctx->build_radius_scale &&
+                 subdiv == ctx->build_subdiv && arrays != nullptr &&
+                 (int)ctx->lists.size() <= kMaxListSlots;
+    for (int a = 0; light && a < narrays; ++a) {
+        const ArraySnap &A = ctx->arrays[a];
+        const sph_array_view &v = arrays[a];
+        if (v.n != A.n || v.n != A.ref_n || (v.n > 0 && (!v.x || !v.h || !v.m)) ||
+            (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && !A.posm0))
+            light = false;
+    }
+    if (!light)
+        return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
+
+    cudaStream_t st = ctx->stream;
+    if (!ctx->d_disp) SPH_CUDA(cudaMalloc(&ctx->d_disp, sizeof(unsigned)));
+    SPH_CUDA(cudaMemsetAsync(ctx->d_disp, 0, sizeof(unsigned), st));
+    SPH_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), st));
+    const double inv_cs_ref = 1.0 / cell_size;
+    for (int a = 0; a < narrays; ++a) {
+        ArraySnap &A = ctx->arrays[a];
+        const sph_array_view &v = arrays[a];
+        if (v.n == 0) continue;
+        k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
+            v, ctx->grid, inv_cs_ref, A.perm, A.skey, A.posm0, A.posm, A.velh, A.st,
+            A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.refcell, check_jump,
+            ctx->d_disp, ctx->d_err);
+        count_launch();
+        SPH_LAUNCH_CHECK("k_light");
+    }
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 9, ctx->d_disp, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    {
+        const int rcm = list_maxima_async(ctx);
+        if (rcm) return rcm;
+    }
+    SPH_CUDA(cudaStreamSynchronize(st));
+    list_maxima_collect(ctx);
+    // a list that overflowed its capacity completes itself by re-traversal in
+    // the order of its build: it needs the build's positions
+    bool overflow = false;
+    for (int i = 0; i < (int)ctx->lists.size() && i < kMaxListSlots; ++i) {
+        const NbrList &L = ctx->lists[i];
+        if (L.maxcnt && L.build == ctx->build_id && ctx->h_maxcnt[i] > L.cap) overflow = true;
+    }
+    const unsigned err = (unsigned)ctx->h_box[8];
+    if (err & SPH_EFLAG_JUMP) {
+        ctx->built = false;
+        return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
+    }
+    float disp2;
+    memcpy(&disp2, ctx->h_box + 9, sizeof(float));
+    const float half = 0.5f * ctx->grid.skin;
+    if (overflow || (err & kLightHChanged) || !(disp2 < half * half * (1.f - 1e-4f))) {
+        // too far for the lists: the refcells already hold this update's cells
+        return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, 0);
+    }
+    for (int a = 0; a < narrays; ++a) ctx->arrays[a].view = arrays[a];
+    ctx->n_light += 1;
+    if (rebuilt) *rebuilt = 0;
     return SPH_OK;
 }
 

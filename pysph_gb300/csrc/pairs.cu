@@ -95,7 +95,32 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
     const float r2 = (float)d.radius2;
     d.r2lo = r2 * (1.f - 1e-5f);
     d.r2hi = r2 * (1.f + 1e-5f);
+    d.r2list = 0.f;
+    if (g.skin > 0.f) {
+        const float rl = (float)radius + g.skin;
+        d.r2list = rl * rl * (1.f + 2e-5f);
+    }
     return true;
+}
+
+// With a list skin the list holds sources up to the list radius: keep the
+// neighbours (the FP32 band test, then the FP64 test of base/nnps.pyx:
+// 337-353 inside the band).
+__device__ __forceinline__ bool listed_exact_test(const SrcDev &S, const DestDev &D,
+                                                  const DestPos &d, int j, float rx, float ry,
+                                                  float rz) {
+    const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+    if (r2 < d.r2lo) return true;
+    if (r2 > d.r2hi) return false;
+    const int oj = S.perm[j];
+    return exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(D.x, d.orig),
+                        ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
+}
+
+__device__ __forceinline__ bool listed_exact(const Grid &g, const SrcDev &S, const DestDev &D,
+                                             const DestPos &d, int j, float rx, float ry, float rz) {
+    if (g.skin <= 0.f) return true;
+    return listed_exact_test(S, D, d, j, rx, ry, rz);
 }
 
 // shift table: code -> -(dx, dy, dz) in cells (times the cell size of the
@@ -122,11 +147,15 @@ __device__ __forceinline__ const Grid &grid_of(const Grid &single, const DestDev
 // the remaining ones by re-traversal.  fn(ok, j, rx, ry, rz) is called for
 // every slot of a batch; ok is false for the padding of the last batch (its
 // data are those of a valid neighbour, its contribution must be dropped).
-// done() is called after every batch.
+// done() is called after every batch.  With a list skin, filter keeps only
+// the neighbours (ok false for the others); without it a skin entry reaches
+// fn with ok true -- right for terms that vanish beyond the radius (W and
+// grad W of the uniform-h cubic spline are exactly 0 for q >= 2 in FP32).
 template <int KX, int B, class Fn, class Done>
 __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int cap, int64_t stride,
                                            int s, const DestPos &d, const float4 *tab,
-                                           const DestDev &D, Fn &&fn, Done &&done) {
+                                           const DestDev &D, bool filter, Fn &&fn, Done &&done) {
+    filter = filter && g.skin > 0.f;
     using C = Code<KX>;
     const int c = S.ncnt[s];
     const int m = min(c, cap);
@@ -144,19 +173,25 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
         }
         const float csf = g.cs_f;
 #pragma unroll
-        for (int b = 0; b < B; ++b)
-            fn(k + b < m, (int)(e[b] & C::JMASK), fmaf(sh[b].x, csf, d.xi_x - p[b].x),
-               fmaf(sh[b].y, csf, d.xi_y - p[b].y), fmaf(sh[b].z, csf, d.xi_z - p[b].z));
+        for (int b = 0; b < B; ++b) {
+            const int j = (int)(e[b] & C::JMASK);
+            const float rx = fmaf(sh[b].x, csf, d.xi_x - p[b].x);
+            const float ry = fmaf(sh[b].y, csf, d.xi_y - p[b].y);
+            const float rz = fmaf(sh[b].z, csf, d.xi_z - p[b].z);
+            fn(k + b < m && (!filter || listed_exact_test(S, D, d, j, rx, ry, rz)), j, rx, ry, rz);
+        }
         done();
     }
     if (c > cap) {
+        // the list entries past cap, in the order of the list build
         int skip = cap;
         for_neighbours<KX>(g, S, d, D.x, D.y, D.z,
-                           [&](int j, float rx, float ry, float rz, int) {
+                           [&](int j, float rx, float ry, float rz, int, bool exact) {
                                if (skip > 0) {
                                    --skip;
                                    return;
                                }
+                               if (!exact) return;
                                fn(true, j, rx, ry, rz);
                                done();
                            });
@@ -179,7 +214,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
             const int cap = A.cap;
             const int64_t stride = A.stride;
             for_neighbours<KX>(g, A.s, d, A.d.x, A.d.y, A.d.z,
-                               [&](int j, float, float, float, int code) {
+                               [&](int j, float, float, float, int code, bool) {
                                    if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                                    ++c;
                                });
@@ -225,9 +260,10 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                 const int64_t stride = A.stride[si];
                 int c = 0;
                 for_neighbours<KX>(g, S, d, A.d.x, A.d.y, A.d.z,
-                    [&](int j, float rx, float ry, float rz, int code) {
+                    [&](int j, float rx, float ry, float rz, int code, bool exact) {
                         if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                         ++c;
+                        if (!exact) return;
                         const float mj = S.st[j].w;
                         float ih = ihi, fac = faci;
                         if (!uh) {
@@ -244,7 +280,8 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                 if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.lmax[si], wmax);
                 continue;
             }
-            for_listed<KX, 4>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+            // with variable h, W at the mean h can reach past the radius of h_i
+            for_listed<KX, 4>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d, !uh,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                     const float mj = S.st[j].w;
                     float ih = ihi, fac = faci;
@@ -326,7 +363,9 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         for (int si = 0; si < nsrc; ++si) {
             const SrcDev &S = A.s[si];
             const uint32_t fl = SPEC != 0 ? SF : S.flags;
-            for_listed<KX, (SPEC != 0 ? 4 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d,
+            // the boundary force has its own support (normal distance, delp)
+            const bool filt = !uh || (fl & SPH_TERM_BFORCE) != 0;
+            for_listed<KX, (SPEC != 0 ? 4 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d, filt,
                 [&](bool ok, int j, float rx, float ry, float rz) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 const float4 vj = S.velh[j];
@@ -480,20 +519,24 @@ __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__
                 const float dx = (float)(code % W - KX), dy = (float)((code / W) % W - KX),
                             dz = (float)(code / (W * W) - KX);
                 const float4 p = S.posm[j];
-                keep(j, fmaf(-dx, csf, d.xi_x - p.x), fmaf(-dy, csf, d.xi_y - p.y),
-                     fmaf(-dz, csf, d.xi_z - p.z));
+                const float rx = fmaf(-dx, csf, d.xi_x - p.x);
+                const float ry = fmaf(-dy, csf, d.xi_y - p.y);
+                const float rz = fmaf(-dz, csf, d.xi_z - p.z);
+                if (listed_exact(A.g, S, A.d, d, j, rx, ry, rz)) keep(j, rx, ry, rz);
             }
             if (c > A.cap) {
                 int skip = A.cap;
                 for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
-                                   [&](int j, float rx, float ry, float rz, int) {
+                                   [&](int j, float rx, float ry, float rz, int, bool exact) {
                                        if (skip > 0) { --skip; return; }
-                                       keep(j, rx, ry, rz);
+                                       if (exact) keep(j, rx, ry, rz);
                                    });
             }
         } else {
             for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
-                               [&](int j, float rx, float ry, float rz, int) { keep(j, rx, ry, rz); });
+                               [&](int j, float rx, float ry, float rz, int, bool exact) {
+                                   if (exact) keep(j, rx, ry, rz);
+                               });
         }
     }
     const float4 vi = A.d.velh[s];

@@ -39,6 +39,10 @@ struct Grid {
     int uniform_h = 0;             // every particle of every array has the same h
     float h_uniform = 1.f;
     int64_t cell_base = 0;         // first cell of this grid in a shared cell table
+    // neighbour-list skin (absolute): lists hold every source within
+    // radius_scale h + skin of the destination at the build, the passes that
+    // stream a list keep the exact neighbours; 0 = lists are exact
+    float skin = 0.f;
 };
 
 struct ArraySnap {
@@ -55,6 +59,8 @@ struct ArraySnap {
     int64_t cell_cap = 0;
     int *refcell = nullptr; // original order, 3 ints per particle (jump check)
     int64_t ref_n = -1;     // particle count the refcell entries belong to
+    float4 *posm0 = nullptr; // posm at the last full build (skin lists)
+    int64_t posm0_cap = 0;
 };
 
 // Neighbour list of one (destination, source) pair of arrays: entry k of
@@ -96,6 +102,12 @@ struct sph_ctx {
     long long build_id = 0;             // incremented by every neighbour build
     std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
     int *h_maxcnt = nullptr;            // pinned scratch for list maxima
+    // neighbour-list skin as a fraction of the search radius (0 = none)
+    double skin_frac = 0.0;
+    double build_radius_scale = 0.0;    // parameters of the last full build
+    int build_subdiv = 0;
+    unsigned *d_disp = nullptr;         // max squared displacement (float bits)
+    long long n_full = 0, n_light = 0;  // full builds / light refreshes
 };
 
 struct sph_batch {
@@ -148,6 +160,8 @@ void count_launch(int n = 1);
 // launchers implemented in the .cu files
 int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
                double radius_scale, int subdiv, int check_jump);
+int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
+                double radius_scale, int subdiv, int check_jump, int *rebuilt);
 int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *counts);
 int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
               int64_t *index);
@@ -287,6 +301,7 @@ struct DestPos {
     float xi_x, xi_y, xi_z;
     int cx, cy, cz;
     float r2lo, r2hi;   // FP32 accept / reject bands around (radius_scale h)^2
+    float r2list;       // list radius (radius_scale h + skin)^2 with margin; 0 = no skin
     double radius2;     // exact FP64 threshold
     int orig;           // original index (FP64 recheck)
 };
@@ -296,11 +311,14 @@ struct DestPos {
 // row).  Each row is first clipped to the chord of the search sphere: rows
 // farther than the radius in (y, z) are skipped and the x extent of the
 // others is cut to the cells the sphere reaches, so the loop over one row is
-// a single contiguous index range.  fn(j, rx, ry, rz, code) gets
-// r = x_dest - x_src in FP32 and the stencil offset code.  The FP32 distance
-// is trusted outside a +-1e-5 relative band around the threshold; inside it
-// the FP64 test of base/nnps.pyx:337-353 decides, so the set is exactly the
-// reference's.  posm[j].w holds the source's dense-grid x cell.
+// a single contiguous index range.  fn(j, rx, ry, rz, code, exact) gets
+// r = x_dest - x_src in FP32, the stencil offset code and whether the source
+// is a neighbour.  The FP32 distance is trusted outside a +-1e-5 relative
+// band around the threshold; inside it the FP64 test of base/nnps.pyx:
+// 337-353 decides, so the set is exactly the reference's.  With a list skin
+// (d.r2list > 0) the sources within the list radius that are not neighbours
+// are visited too, with exact = false.  posm[j].w holds the source's
+// dense-grid x cell.
 template <int KX, class Fn>
 __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
                                                const double *dx64, const double *dy64,
@@ -309,7 +327,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
     const float inv_cs = 1.f / csf;
     // pruning radius: the accept/recheck threshold plus a relative margin
     // that covers FP32 rounding of the slab distances and cell assignment
-    const float R2 = d.r2hi * 1.0002f;
+    const float R2 = fmaxf(d.r2hi, d.r2list) * 1.0002f;
     const float cxf = (float)d.cx;
     const int rowstride_z = g.nx * g.ny;  // < 2^27 cells: 32-bit indices
     const int *cst = S.cstart + g.cell_base;
@@ -346,7 +364,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
                     hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(dx64, d.orig),
                                        ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
                 }
-                if (hit) fn(j, rx, ry, rz, code_yz + (int)dxc);
+                if (hit || r2 < d.r2list) fn(j, rx, ry, rz, code_yz + (int)dxc, hit);
             }
         }
     }

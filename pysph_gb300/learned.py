@@ -419,8 +419,9 @@ class GuardedRunner:
     def _restore(self, snap):
         for pa, s in zip(self.particles.arrays, snap):
             pa.set(**s)
-        self.particles.cell_manager.skip_jump_once = True
-        self.particles.update()
+        # a full build from the restored state: the replay then depends on
+        # the state alone, exactly as the run it repeats
+        self.particles.cell_manager.rebuild(check_jump=False)
 
     def _steps(self, dt, n):
         for _ in range(n):
@@ -435,6 +436,7 @@ class GuardedRunner:
             self._steps(dt, self.k)
             return
         check = (self.windows - 1) % self.check_every == 0
+        self.particles.cell_manager.rebuild()
         start = self._save()
         self.closure.active = True
         try:

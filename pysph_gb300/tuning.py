@@ -10,6 +10,24 @@ from a per-dimension table measured on GB300 (1 M-particle 3D lattice: 3.18,
 """
 import os
 
+# neighbour-list skin, as a fraction of the search radius: a full neighbour
+# build keeps the sources within (1 + skin) times the radius, and later
+# updates only refresh the sorted state while no particle has moved by half
+# the skin (PYSPH_GB300_SKIN overrides; 0 rebuilds at every update like the
+# reference)
+DEFAULT_SKIN = 0.03
+
+
+def list_skin():
+    env = os.environ.get("PYSPH_GB300_SKIN")
+    if env is not None:
+        v = float(env)
+        if not 0.0 <= v <= 0.5:
+            raise ValueError("PYSPH_GB300_SKIN must be in [0, 0.5]")
+        return v
+    return DEFAULT_SKIN
+
+
 # measured defaults: (dimensions with extent) -> subdivision
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
 # neighbour-list entries hold the source slot in 32 - code bits: at
