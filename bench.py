@@ -688,6 +688,86 @@ def run_gpu_closure(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# the closure network's tensor-core kernels on their own
+# ---------------------------------------------------------------------------
+MLP_FWD_FLOPS = 2.0 * (192 * 128 + 128 * 128 + 128 * 2)            # per sample
+MLP_BWD_FLOPS = 2.0 * (128 * 128 + 128 * 144 + 128 * 208) + 4.0 * 128 * 2
+
+
+def measured_bf16():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def run_gpu_mlp(args):
+    import torch
+
+    from pysph_gb300 import learned as L
+    from pysph_gb300 import native
+
+    torch.cuda.set_device(0)
+    n = args.mlp_n
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    x = torch.randn((n, 192), generator=g, device="cuda").to(torch.bfloat16)
+    t = torch.randn((n, 2), generator=g, device="cuda")
+    model = L.MomentumMLP(seed=0)
+    st = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            fn()
+            b.record(st)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.mean(ms)
+
+    launches0 = native.launch_count()
+    fwd_ms = timed(lambda: model.forward(x), args.steps)
+    y, cache = model.forward(x, save=True)
+    bwd_ms = timed(lambda: model.backward(x, cache, y, t), args.steps)
+    train_ms = timed(lambda: _train_step(model, x, t), args.steps)
+    launches = native.launch_count() - launches0
+    model.check()
+    peak, kind = measured_bf16()
+    fwd_tf = MLP_FWD_FLOPS * n / (fwd_ms / 1e3) / 1e12
+    bwd_tf = MLP_BWD_FLOPS * n / (bwd_ms / 1e3) / 1e12
+    line = {
+        "metric": "closure network samples/s (forward, BF16 tensor cores)",
+        "value": n / (fwd_ms / 1e3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": fwd_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+        "data": "synthetic (seeded normal features)",
+        "config": {"workload": "network 192-128-128-2 GELU, %d samples per launch" % n},
+        "forward": {"ms": fwd_ms, "tflops": fwd_tf},
+        "backward": {"ms": bwd_ms, "tflops": bwd_tf},
+        "train_step_ms": train_ms,
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_fwd", "achieved": fwd_tf, "peak": peak,
+                     "unit": "TFLOP/s", "frac": fwd_tf / peak, "traffic": None,
+                     "peak_kind": kind},
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _train_step(model, x, t):
+    y, cache = model.forward(x, save=True)
+    model.backward(x, cache, y, t)
+    model.adam(1e-4)
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -719,7 +799,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--procs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cube", choices=["cube", "drops", "closure"])
+    ap.add_argument("--workload", default="cube", choices=["cube", "drops", "closure", "mlp"])
+    ap.add_argument("--mlp-n", type=int, default=1 << 20)
     ap.add_argument("--samples", type=int, default=10_000_000)
     ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--train-steps", type=int, default=2000)
@@ -736,6 +817,11 @@ def main():
         args.warmup = 3
     if args.workload == "drops":
         (run_reference_drops if args.impl == "reference" else run_gpu_drops)(args)
+    elif args.workload == "mlp":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no network"}))
+        else:
+            run_gpu_mlp(args)
     elif args.workload == "closure":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned "

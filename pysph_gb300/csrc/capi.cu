@@ -98,7 +98,7 @@ int sph_ctx_destroy(sph_ctx *c) {
         cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
         cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st);
         cudaFree(A.nrm); cudaFree(A.tan);
-        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0);
+        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0); cudaFree(A.inv);
     }
     cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_err); cudaFree(c->d_disp);
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);

@@ -264,22 +264,30 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
     }
 }
 
-// Light refresh: the snapshot of slot s in the cell of the last full build,
-// the largest squared displacement from the build position, h changes and
-// the jump check against the previous update's cells.
+// Light refresh, in original particle order (coalesced FP64 reads, sorted
+// slot from the inverse permutation of the last full build): the snapshot
+// of the particle in the cell of that build, the largest squared
+// displacement from the build position, an h other than the build's
+// uniform h, and the jump check against the previous update's cells.
 constexpr unsigned kLightHChanged = 1u << 8;
 
-__global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *perm,
-                        const int *skey, const float4 *posm0, float4 *posm, float4 *velh,
+__global__ void k_invperm(int64_t n, const int *perm, int *inv) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x)
+        inv[perm[s]] = (int)s;
+}
+
+__global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
+                        const int *key, const float4 *posm0, float4 *posm, float4 *velh,
                         float4 *st, float4 *nrm, float4 *tan, int *refcell, int check_jump,
-                        unsigned *dmax, unsigned *err) {
+                        double build_h, unsigned *dmax, unsigned *err) {
     float dm = 0.f;
     bool jump = false, hch = false;
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
-         s += (int64_t)gridDim.x * blockDim.x) {
-        const int i = perm[s];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int s = inv[i];
         int cx, cy, cz;
-        decode_cell(g, skey[s], cx, cy, cz);
+        decode_cell(g, key[i], cx, cy, cz);
         const double px = ld0(a.x, i), py = ld0(a.y, i), pz = ld0(a.z, i);
         const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
         const float xi = (float)fma(-ox, g.cs, px);
@@ -289,9 +297,9 @@ __global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *
         const float ddx = xi - p0.x, ddy = yi - p0.y, ddz = zi - p0.z;
         dm = fmaxf(dm, fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)));
         posm[s] = make_float4(xi, yi, zi, (float)cx);
-        const float hf = (float)a.h[i];
-        if (hf != velh[s].w) hch = true;
-        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), hf);
+        const double h = a.h[i];
+        if (h != build_h) hch = true;
+        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), (float)h);
         const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
         st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
         if (nrm) {
@@ -599,12 +607,18 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
             if (g.skin > 0.f) {
                 if (A.posm0_cap < v.n) {
                     cudaFree(A.posm0);
+                    cudaFree(A.inv);
                     A.posm0 = nullptr;
+                    A.inv = nullptr;
                     SPH_CUDA(cudaMalloc(&A.posm0, sizeof(float4) * v.n));
+                    SPH_CUDA(cudaMalloc(&A.inv, sizeof(int) * v.n));
                     A.posm0_cap = v.n;
                 }
                 SPH_CUDA(cudaMemcpyAsync(A.posm0, A.posm, sizeof(float4) * v.n,
                                          cudaMemcpyDeviceToDevice, st));
+                k_invperm<<<grid_blocks(v.n, kThreads), kThreads, 0, st>>>(v.n, A.perm, A.inv);
+                count_launch();
+                SPH_LAUNCH_CHECK("k_invperm");
             }
         }
     }
@@ -612,6 +626,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     ctx->build_id += 1;
     ctx->build_radius_scale = radius_scale;
     ctx->build_subdiv = subdiv;
+    ctx->build_h = g.uniform_h ? hmax : 0.0;
     ctx->n_full += 1;
     return SPH_OK;
 }
@@ -628,12 +643,12 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
     bool light = ctx->built && ctx->grid.skin > 0.f && narrays == (int)ctx->arrays.size() &&
                  cell_size == ctx->cell_size_ref && radius_scale == ctx->build_radius_scale &&
                  subdiv == ctx->build_subdiv && arrays != nullptr &&
-                 (int)ctx->lists.size() <= kMaxListSlots;
+                 ctx->build_h > 0.0 && (int)ctx->lists.size() <= kMaxListSlots;
     for (int a = 0; light && a < narrays; ++a) {
         const ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];
         if (v.n != A.n || v.n != A.ref_n || (v.n > 0 && (!v.x || !v.h || !v.m)) ||
-            (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && !A.posm0))
+            (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && (!A.posm0 || !A.inv)))
             light = false;
     }
     if (!light)
@@ -649,9 +664,9 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         const sph_array_view &v = arrays[a];
         if (v.n == 0) continue;
         k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
-            v, ctx->grid, inv_cs_ref, A.perm, A.skey, A.posm0, A.posm, A.velh, A.st,
+            v, ctx->grid, inv_cs_ref, A.inv, A.key, A.posm0, A.posm, A.velh, A.st,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.refcell, check_jump,
-            ctx->d_disp, ctx->d_err);
+            ctx->build_h, ctx->d_disp, ctx->d_err);
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
     }

@@ -60,6 +60,7 @@ struct ArraySnap {
     int *refcell = nullptr; // original order, 3 ints per particle (jump check)
     int64_t ref_n = -1;     // particle count the refcell entries belong to
     float4 *posm0 = nullptr; // posm at the last full build (skin lists)
+    int *inv = nullptr;      // original -> sorted slot of the last full build
     int64_t posm0_cap = 0;
 };
 
@@ -105,6 +106,7 @@ struct sph_ctx {
     // neighbour-list skin as a fraction of the search radius (0 = none)
     double skin_frac = 0.0;
     double build_radius_scale = 0.0;    // parameters of the last full build
+    double build_h = 0.0;               // the uniform h of the last full build (0: not uniform)
     int build_subdiv = 0;
     unsigned *d_disp = nullptr;         // max squared displacement (float bits)
     long long n_full = 0, n_light = 0;  // full builds / light refreshes
