@@ -11,9 +11,11 @@
 // core matrix along K) is 128 B and the stride-dimension offset (next 8
 // rows) is K/8 * 128 B.  One thread issues tcgen05.mma (M = 128 samples or
 // hidden units, kind::f16 with BF16 A and B, FP32 accumulation in tensor
-// memory) and tcgen05.commit signals an mbarrier; the four warps of the
-// CTA read the accumulator rows back with tcgen05.ld (warp w owns lanes
-// 32w..32w+31, thread t owns row t).
+// memory) and tcgen05.commit signals an mbarrier; the eight warps of the
+// CTA read the accumulator rows back with tcgen05.ld: warps w and w + 4 own
+// lanes 32(w%4)..32(w%4)+31 (one tile row per thread) and split the
+// columns, so the FP32 epilogues, which bound these kernels, have two warps
+// per scheduler to hide their latency.
 //
 //   k_mlp_fwd   per 128-sample tile: X W1^T -> +b1, GELU -> BF16 H1 (smem)
 //               -> H1 W2^T -> +b2, GELU -> BF16 h2 -> h2 W3^T + b3 on the
@@ -43,7 +45,7 @@ constexpr int OFF_W1 = SPH_MLP_OFF_W1, OFF_B1 = SPH_MLP_OFF_B1, OFF_W2 = SPH_MLP
               OFF_B2 = SPH_MLP_OFF_B2, OFF_W3 = SPH_MLP_OFF_W3, OFF_B3 = SPH_MLP_OFF_B3,
               NPARAM = SPH_MLP_NPARAM;
 constexpr int TILE = 128;
-constexpr int THREADS = 128;
+constexpr int THREADS = 256;   // two warps per tensor-memory lane quarter
 constexpr int L3_PART = NOUT * NH + NOUT;   // third-layer partial per block
 constexpr int L3_ROWS = 1024;               // rows per third-layer block
 constexpr int kMaxSpin = 1 << 22;           // bounded mbarrier wait
@@ -190,7 +192,8 @@ constexpr uint32_t F_W3 = F_H1 + TILE * NH * 2;     // 163840: float [2][128]
 constexpr uint32_t F_B1 = F_W3 + NOUT * NH * 4;     // float [128]
 constexpr uint32_t F_B2 = F_B1 + NH * 4;            // float [128]
 constexpr uint32_t F_B3 = F_B2 + NH * 4;            // float [2] (+pad)
-constexpr uint32_t F_BAR = F_B3 + 16;               // mbarrier (8 B)
+constexpr uint32_t F_YP = F_B3 + 16;                // float2 [128]: upper-half outputs
+constexpr uint32_t F_BAR = F_YP + TILE * 8;         // mbarrier (8 B)
 constexpr uint32_t F_SLOT = F_BAR + 8;              // tensor-memory address
 constexpr uint32_t F_BYTES = F_SLOT + 8;
 constexpr uint32_t F_TMEM_COLS = 256;               // z1 at 0, z2 at 128
@@ -205,8 +208,14 @@ __global__ void __launch_bounds__(THREADS, 1)
               float *__restrict__ z1s, float *__restrict__ z2s, uint16_t *__restrict__ h1s,
               uint16_t *__restrict__ h2s, unsigned *err) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    const int t = threadIdx.x, warp = t >> 5;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    // warps w and w + 4 read the same 32 tensor-memory lanes (tile rows),
+    // each one half of the accumulator columns
+    const int q = warp & 3, ch = warp >> 2;
+    const int row = q * 32 + lane;
+    const int cbeg = ch * (NH / 2), cend = cbeg + NH / 2;
     float *w3f = reinterpret_cast<float *>(sm + F_W3);
+    float2 *yp = reinterpret_cast<float2 *>(sm + F_YP);
     float *b1f = reinterpret_cast<float *>(sm + F_B1);
     float *b2f = reinterpret_cast<float *>(sm + F_B2);
     float *b3f = reinterpret_cast<float *>(sm + F_B3);
@@ -228,7 +237,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *slot;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     const uint32_t sX = smem_u32(sm + F_X), sW1 = smem_u32(sm + F_W1);
     const uint32_t sH1 = smem_u32(sm + F_H1), sW2 = smem_u32(sm + F_W2);
     uint32_t phase = 0;
@@ -263,10 +272,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!__syncthreads_and(ok)) break;
         tc_fence_after();
 
-        const int64_t grow = row0 + t;
+        const int64_t grow = row0 + row;
         const bool valid = grow < n;
 #pragma unroll 1
-        for (int c0 = 0; c0 < NH; c0 += 16) {
+        for (int c0 = cbeg; c0 < cend; c0 += 16) {
             float v[16];
             tmem_ld16(tbase + lane_base + c0, v);
             uint32_t hw[8];
@@ -274,9 +283,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int i = 0; i < 16; ++i) v[i] += b1f[c0 + i];
 #pragma unroll
             for (int i = 0; i < 8; ++i) hw[i] = pack2(gelu(v[2 * i]), gelu(v[2 * i + 1]));
-            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(t, c0, NH / 8)) =
+            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(row, c0, NH / 8)) =
                 make_uint4(hw[0], hw[1], hw[2], hw[3]);
-            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(t, c0 + 8, NH / 8)) =
+            *reinterpret_cast<uint4 *>(sm + F_H1 + core_off(row, c0 + 8, NH / 8)) =
                 make_uint4(hw[4], hw[5], hw[6], hw[7]);
             if (valid && z1s) {
                 float4 *zp = reinterpret_cast<float4 *>(z1s + grow * NH + c0);
@@ -306,9 +315,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!__syncthreads_and(ok)) break;
         tc_fence_after();
 
-        float y0 = b3f[0], y1 = b3f[1];
+        float y0 = 0.f, y1 = 0.f;
 #pragma unroll 1
-        for (int c0 = 0; c0 < NH; c0 += 16) {
+        for (int c0 = cbeg; c0 < cend; c0 += 16) {
             float v[16];
             tmem_ld16(tbase + 128 + lane_base + c0, v);
             uint32_t hw[8];
@@ -336,9 +345,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 hp[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
             }
         }
-        if (valid) {
-            y[grow * 2] = y0;
-            y[grow * 2 + 1] = y1;
+        if (ch == 1) yp[row] = make_float2(y0, y1);
+        __syncthreads();
+        if (ch == 0 && valid) {
+            const float2 o = yp[row];
+            y[grow * 2] = b3f[0] + (y0 + o.x);
+            y[grow * 2 + 1] = b3f[1] + (y1 + o.y);
         }
         tc_fence_before();
         __syncthreads();
@@ -363,8 +375,8 @@ constexpr uint32_t B_H1T = B_A2 + NH * TILE * 2;          // [i][b], 144 rows
 constexpr uint32_t B_XT = B_H1T + H1T_ROWS * TILE * 2;    // [m][b], 208 rows
 constexpr uint32_t B_W2T = B_XT + XT_ROWS * TILE * 2;     // W2^T [i][j]
 constexpr uint32_t B_W3 = B_W2T + NH * NH * 2;            // float [2][128]
-constexpr uint32_t B_RED = B_W3 + NOUT * NH * 4;          // float [4] loss per warp
-constexpr uint32_t B_BAR = B_RED + 16;
+constexpr uint32_t B_RED = B_W3 + NOUT * NH * 4;          // float [8] loss per warp
+constexpr uint32_t B_BAR = B_RED + 32;
 constexpr uint32_t B_SLOT = B_BAR + 8;
 constexpr uint32_t B_BYTES = B_SLOT + 8;
 constexpr uint32_t T_DH1 = 0, T_DW2 = 128, T_DW1 = 288;    // tensor-memory columns
@@ -379,6 +391,10 @@ __global__ void __launch_bounds__(THREADS, 1)
               float *__restrict__ part_loss, unsigned *err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    // row = sample (and tensor-memory lane); the two warps of a lane quarter
+    // split the columns
+    const int q = warp & 3, ch = warp >> 2;
+    const int row = q * 32 + lane;
     float *w3f = reinterpret_cast<float *>(sm + B_W3);
     float *red = reinterpret_cast<float *>(sm + B_RED);
     const uint32_t bar = smem_u32(sm + B_BAR);
@@ -400,7 +416,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *slot;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     const uint32_t sA1 = smem_u32(sm + B_A1), sA2 = smem_u32(sm + B_A2);
     const uint32_t sH1T = smem_u32(sm + B_H1T), sXT = smem_u32(sm + B_XT);
     const uint32_t sW2T = smem_u32(sm + B_W2T);
@@ -412,21 +428,23 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int64_t ntiles = (n + TILE - 1) / TILE;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t b = tile * TILE + t;
+        const int64_t b = tile * TILE + row;
         const bool valid = b < n;
         float d0 = 0.f, d1 = 0.f;
         if (valid) {
             const float e0 = y[b * 2] - target[b * 2], e1 = y[b * 2 + 1] - target[b * 2 + 1];
-            loss += e0 * e0 + e1 * e1;
             d0 = e0 * inv_count;
             d1 = e1 * inv_count;
-            dy_out[b * 2] = d0;
-            dy_out[b * 2 + 1] = d1;
+            if (ch == 0) {
+                loss += e0 * e0 + e1 * e1;
+                dy_out[b * 2] = d0;
+                dy_out[b * 2 + 1] = d1;
+            }
         }
-        // dz2 = (dy W3) * gelu'(z2): row t of A1, column t of A2
+        // dz2 = (dy W3) * gelu'(z2): row `row` of A1, column `row` of A2
 #pragma unroll 1
-        for (int j0 = 0; j0 < NH; j0 += 8) {
-            float z[8];
+        for (int j0 = ch * (NH / 2); j0 < (ch + 1) * (NH / 2); j0 += 8) {
+            float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (valid) {
                 const float4 a = *reinterpret_cast<const float4 *>(z2s + b * NH + j0);
                 const float4 c = *reinterpret_cast<const float4 *>(z2s + b * NH + j0 + 4);
@@ -444,33 +462,33 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 w[i / 2] = pack2(g[0], g[1]);
             }
-            *reinterpret_cast<uint4 *>(sm + B_A1 + core_off(t, j0, NH / 8)) =
+            *reinterpret_cast<uint4 *>(sm + B_A1 + core_off(row, j0, NH / 8)) =
                 make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const uint16_t hv = (uint16_t)((w[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
-                *reinterpret_cast<uint16_t *>(sm + B_A2 + core_off(j0 + i, t, TILE / 8)) = hv;
+                *reinterpret_cast<uint16_t *>(sm + B_A2 + core_off(j0 + i, row, TILE / 8)) = hv;
             }
         }
-        // h1^T and x^T: column t
+        // h1^T and x^T: column `row`
 #pragma unroll 1
-        for (int i0 = 0; i0 < NH; i0 += 8) {
+        for (int i0 = ch * (NH / 2); i0 < (ch + 1) * (NH / 2); i0 += 8) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (valid) v = __ldg(reinterpret_cast<const uint4 *>(h1s + b * NH + i0));
             const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                *reinterpret_cast<uint16_t *>(sm + B_H1T + core_off(i0 + i, t, TILE / 8)) =
+                *reinterpret_cast<uint16_t *>(sm + B_H1T + core_off(i0 + i, row, TILE / 8)) =
                     (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
         }
 #pragma unroll 1
-        for (int m0 = 0; m0 < NIN; m0 += 8) {
+        for (int m0 = ch * (NIN / 2); m0 < (ch + 1) * (NIN / 2); m0 += 8) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (valid) v = __ldg(reinterpret_cast<const uint4 *>(x + b * NIN + m0));
             const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                *reinterpret_cast<uint16_t *>(sm + B_XT + core_off(m0 + i, t, TILE / 8)) =
+                *reinterpret_cast<uint16_t *>(sm + B_XT + core_off(m0 + i, row, TILE / 8)) =
                     (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
         }
         fence_async_smem();
@@ -496,9 +514,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!__syncthreads_and(ok)) break;
         tc_fence_after();
 
-        // dz1 = dh1 * gelu'(z1) -> column t of A2 (its previous content is consumed)
+        // dz1 = dh1 * gelu'(z1) -> column `row` of A2 (its previous content is consumed)
 #pragma unroll 1
-        for (int c0 = 0; c0 < NH; c0 += 16) {
+        for (int c0 = ch * (NH / 2); c0 < (ch + 1) * (NH / 2); c0 += 16) {
             float v[16];
             tmem_ld16(tbase + T_DH1 + lane_base + c0, v);
             float z[16];
@@ -512,7 +530,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 const float g = valid ? v[i] * dgelu(z[i]) : 0.f;
-                *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + core_off(c0 + i, t, TILE / 8)) =
+                *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + core_off(c0 + i, row, TILE / 8)) =
                     __float2bfloat16_rn(g);
             }
         }
@@ -537,28 +555,32 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 
     if (ok && !first) {
-        // row j = t of the accumulated weight (and bias) gradients
+        // row j = `row` of the accumulated weight (and bias) gradients; the
+        // two warps of a lane quarter split the 16-column chunks
         float *P = part + (int64_t)blockIdx.x * NPARAM;
+        constexpr int C2 = H1T_ROWS / 16, C1 = XT_ROWS / 16;
 #pragma unroll 1
-        for (int c0 = 0; c0 < H1T_ROWS; c0 += 16) {
+        for (int k = ch ? (C2 + 1) / 2 : 0; k < (ch ? C2 : (C2 + 1) / 2); ++k) {
+            const int c0 = 16 * k;
             float v[16];
             tmem_ld16(tbase + T_DW2 + lane_base + c0, v);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 const int c = c0 + i;
-                if (c < NH) P[OFF_W2 + t * NH + c] = v[i];
-                else if (c == NH) P[OFF_B2 + t] = v[i];
+                if (c < NH) P[OFF_W2 + row * NH + c] = v[i];
+                else if (c == NH) P[OFF_B2 + row] = v[i];
             }
         }
 #pragma unroll 1
-        for (int c0 = 0; c0 < XT_ROWS; c0 += 16) {
+        for (int k = ch ? (C1 + 1) / 2 : 0; k < (ch ? C1 : (C1 + 1) / 2); ++k) {
+            const int c0 = 16 * k;
             float v[16];
             tmem_ld16(tbase + T_DW1 + lane_base + c0, v);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 const int c = c0 + i;
-                if (c < NIN) P[OFF_W1 + t * NIN + c] = v[i];
-                else if (c == NIN) P[OFF_B1 + t] = v[i];
+                if (c < NIN) P[OFF_W1 + row * NIN + c] = v[i];
+                else if (c == NIN) P[OFF_B1 + row] = v[i];
             }
         }
     } else if (first) {
@@ -570,7 +592,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (!ok && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
     tc_fence_before();
     __syncthreads();
-    if (t == 0) part_loss[blockIdx.x] = 0.5f * inv_count * (red[0] + red[1] + red[2] + red[3]);
+    if (t == 0) {
+        float sum = 0.f;
+        for (int w = 0; w < THREADS / 32; ++w) sum += red[w];
+        part_loss[blockIdx.x] = 0.5f * inv_count * sum;
+    }
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tbase, B_TMEM_COLS);
