@@ -13,7 +13,8 @@ the closure uses in place of the momentum pair loop of
   by sorted source slot), each as ``((x_i-x_j)/h_i, (y_i-y_j)/h_i,
   (u_j-u_i)/c0, (v_j-v_i)/c0, rho_j, p_j)``, standardised per channel;
   missing neighbours are zero rows;
-* network: 192 -> 128 -> 128 -> 2 with exact GELU, weights and the
+* network: 192 -> 128 -> 128 -> 2 with GELU in its tanh form
+  (Hendrycks & Gimpel 2016), weights and the
   activations that feed a matrix product in BF16 (round to nearest even),
   products accumulated in FP32 on the GPU (FP64 here);
 * loss ``0.5 / B * sum (y - t)^2`` and its gradient, with the kernels'
@@ -25,7 +26,6 @@ the closure uses in place of the momentum pair loop of
 gradient of the FP64 loss, which ``finite_difference`` checks.
 """
 import numpy as np
-from scipy.special import erf
 
 NIN, NH, NOUT = 192, 128, 2
 NNBR, NCH = 32, 6
@@ -37,9 +37,6 @@ OFF_W3 = OFF_B2 + NH
 OFF_B3 = OFF_W3 + NOUT * NH
 NPARAM = OFF_B3 + NOUT
 
-SQRT1_2 = 0.7071067811865476
-INV_SQRT_2PI = 0.3989422804014327
-
 
 def bf16(a):
     """Round to BFloat16 (nearest, ties to even) through FP32; FP64 out."""
@@ -49,12 +46,17 @@ def bf16(a):
     return (u & 0xFFFFFFFF).astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+GELU_C = np.sqrt(2.0 / np.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z * SQRT1_2))
+    """GELU, tanh form (Hendrycks & Gimpel 2016)."""
+    return 0.5 * z * (1.0 + np.tanh(GELU_C * (z + 0.044715 * z ** 3)))
 
 
 def dgelu(z):
-    return 0.5 * (1.0 + erf(z * SQRT1_2)) + z * INV_SQRT_2PI * np.exp(-0.5 * z * z)
+    t = np.tanh(GELU_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def unpack(p):

@@ -1,5 +1,5 @@
 // Learned momentum closure: the per-particle network 192 -> 128 -> 128 -> 2
-// (exact GELU) on the fifth-generation tensor cores.
+// (GELU, tanh form) on the fifth-generation tensor cores.
 //
 // The reference has no learned part; the network stands in for the
 // momentum pair loop (sph/funcs/pressure_funcs.pyx:40-91 and
@@ -153,10 +153,23 @@ __device__ __forceinline__ uint32_t core_off(int r, int k, int kc) {
     return (uint32_t)(((((r >> 3) * kc) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
 }
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel 2016):
+//   gelu(z) = z/2 (1 + tanh(u)),  u = sqrt(2/pi) (z + 0.044715 z^3),
+// with tanh(u) = 1 - 2 / (1 + e^(2u)) (saturates correctly for |u| large).
+__device__ __forceinline__ float tanh_exp(float u) {
+    return 1.f - __fdividef(2.f, 1.f + __expf(2.f * u));
+}
+__device__ __forceinline__ float gelu(float z) {
+    const float u = 0.79788456080286536f * fmaf(0.044715f * z, z * z, z);
+    return 0.5f * z * (1.f + tanh_exp(u));
+}
+// d gelu / dz = (1 + t)/2 + z/2 (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 z^2)
 __device__ __forceinline__ float dgelu(float z) {
-    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) +
-           z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float u = 0.79788456080286536f * fmaf(0.044715f * z, z2, z);
+    const float t = tanh_exp(u);
+    const float du = 0.79788456080286536f * fmaf(0.134145f, z2, 1.f);
+    return fmaf(0.5f * z * (1.f - t * t), du, 0.5f * (1.f + t));
 }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
