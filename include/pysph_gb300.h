@@ -74,6 +74,9 @@ typedef struct {
 #define SPH_TERM_AVISC 2u   /* MonaghanArtificialVsicosity    */
 #define SPH_TERM_XSPH 4u    /* XSPHCorrection                 */
 #define SPH_TERM_BFORCE 8u  /* MonaghanBoundaryForce          */
+#define SPH_TERM_DRHO 16u   /* SPHDensityRate (density_funcs.pyx:89-158): drho += m_j v_ij . grad W */
+/* MomentumEquation (pressure_funcs.pyx:106-252) is PGRAD | AVISC with its own
+ * eta (it stores eta, unlike MonaghanArtificialVsicosity) */
 
 typedef struct {
     int src;           /* array slot of the source (index into the last build) */
@@ -94,6 +97,7 @@ typedef struct {
     int add_velocity;     /* PositionStepping: pos_out += (u, v, w) of the dest */
     double gx, gy, gz;    /* GravityForce: acc_out += g (when add_gravity)      */
     int add_gravity;
+    double *drho_out;     /* density rate of SPH_TERM_DRHO sources (may be NULL) */
 } sph_rates_params;
 
 /* One line of an integrator update, applied elementwise over n particles:

@@ -68,6 +68,8 @@ def lib():
             L.orc_pgrad.argtypes = [P, P, vp, vp, i, i, vp, vp, vp]
             L.orc_avisc.argtypes = [P, P, vp, vp, i, d, d, d, vp, vp, vp]
             L.orc_xsph.argtypes = [P, P, vp, vp, i, d, i, vp, vp, vp]
+            L.orc_momentum.argtypes = [P, P, vp, vp, i, d, d, d, i, vp, vp, vp]
+            L.orc_drho.argtypes = [P, P, vp, vp, i, vp]
             L.orc_bforce.argtypes = [P, P, vp, vp, d, vp, vp, vp]
             L.orc_const3.argtypes = [P, d, d, d, i, vp, vp, vp]
             L.orc_position_stepping.argtypes = [P, i, vp, vp, vp]
@@ -145,11 +147,18 @@ def pair_sum(kind, dst, src, offsets, index, dim, params=None, nout=3):
     if kind == "rho":
         L.orc_sph_rho(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, o[0])
         return outs[:1]
+    if kind == "drho":
+        L.orc_drho(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, o[0])
+        return outs[:1]
     if kind == "pgrad":
         L.orc_pgrad(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, nout, *o)
     elif kind == "avisc":
         L.orc_avisc(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
                     params.get("alpha", 1.0), params.get("beta", 1.0), 0.0, *o)
+    elif kind == "momentum":
+        L.orc_momentum(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
+                       params.get("alpha", 1.0), params.get("beta", 1.0),
+                       params.get("eta", 0.1), nout, *o)
     elif kind == "xsph":
         L.orc_xsph(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
                    params.get("eps", 0.5), nout, *o)
@@ -175,8 +184,9 @@ def tait(dst, co, ro, gamma=7.0):
 # ---------------------------------------------------------------------------
 
 class Op:
-    """One calc: ``kind`` in rho | tait | pgrad | avisc | xsph | bforce |
-    gravity | step, on destination ``dest`` from ``sources``."""
+    """One calc: ``kind`` in rho | tait | pgrad | avisc | momentum | drho |
+    xsph | bforce | gravity | step, on destination ``dest`` from
+    ``sources``."""
 
     def __init__(self, kind, dest, updates, sources=(), integrates=False, **params):
         self.kind = kind
@@ -336,4 +346,17 @@ def cube_ops(c0=1.0, rho0=1.0, alpha=0.1, beta=0.0):
         Op("pgrad", "fluid", ["u", "v", "w"], ["fluid"], integrates=True),
         Op("avisc", "fluid", ["u", "v", "w"], ["fluid"], integrates=True, alpha=alpha, beta=beta),
         Op("step", "fluid", ["x", "y", "z"], integrates=True),
+    ]
+
+
+def fluid_ops(c0=100.0, ro=1.0, alpha=0.01, beta=0.0, eta=0.1, eps=0.1):
+    """solver/fluid_solver.py:51-83 (FluidSolver): Tait, continuity density
+    rate, MomentumEquation, position stepping, XSPH."""
+    return [
+        Op("tait", "fluid", ["p", "cs"], co=c0, ro=ro),
+        Op("drho", "fluid", ["rho"], ["fluid"], integrates=True),
+        Op("momentum", "fluid", ["u", "v", "w"], ["fluid"], integrates=True, alpha=alpha,
+           beta=beta, eta=eta),
+        Op("step", "fluid", ["x", "y"], integrates=True),
+        Op("xsph", "fluid", ["x", "y"], ["fluid"], integrates=True, eps=eps),
     ]

@@ -296,6 +296,77 @@ void orc_avisc(const orc_array *d, const orc_array *s, const int64_t *off,
     }
 }
 
+/* MomentumEquation: sph/funcs/pressure_funcs.pyx:106-252 -- pressure
+ * gradient and Monaghan viscosity in one pair term, eta stored (default
+ * 0.1), hks off; num_outputs = dim.                                       */
+void orc_momentum(const orc_array *d, const orc_array *s, const int64_t *off,
+                  const int64_t *idx, int dim, double alpha, double beta, double eta,
+                  int nout, double *o0, double *o1, double *o2) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < d->n; ++i) {
+        if (!is_real(d, i)) {
+            o0[i] = 0; if (nout > 1) o1[i] = 0; if (nout > 2) o2[i] = 0;
+            continue;
+        }
+        double nr[3] = {0, 0, 0};
+        for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+            int64_t j = idx[k];
+            double ha = d->h[i], hb = s->h[j];
+            double hab = 0.5 * (ha + hb);
+            double rx = get0(d->x, i) - get0(s->x, j), ry = get0(d->y, i) - get0(s->y, j),
+                   rz = get0(d->z, i) - get0(s->z, j);
+            double vx = get0(d->u, i) - get0(s->u, j), vy = get0(d->v, i) - get0(s->v, j),
+                   vz = get0(d->w, i) - get0(s->w, j);
+            double dot = vx * rx + vy * ry + vz * rz;
+            double pa = d->p[i], rhoa = d->rho[i];
+            double pb = s->p[j], rhob = s->rho[j], mb = s->m[j];
+            double tmp = pa / (rhoa * rhoa) + pb / (rhob * rhob);
+            double piab = 0;
+            if (dot < 0) {
+                double cab = 0.5 * (d->cs[i] + s->cs[j]);
+                double rhoab = 0.5 * (rhoa + rhob);
+                double mu = hab * dot;
+                mu /= ((rx * rx + ry * ry + rz * rz) + eta * eta * hab * hab);
+                piab = -alpha * cab * mu + beta * mu * mu;
+                piab /= rhoab;
+            }
+            tmp += piab;
+            tmp *= -mb;
+            double g[3];
+            orc_cubic_grad(dim, get0(d->x, i), get0(d->y, i), get0(d->z, i), get0(s->x, j),
+                           get0(s->y, j), get0(s->z, j), hab, g);
+            nr[0] += tmp * g[0];
+            nr[1] += tmp * g[1];
+            nr[2] += tmp * g[2];
+        }
+        o0[i] += nr[0];
+        if (nout > 1) o1[i] += nr[1];
+        if (nout > 2) o2[i] += nr[2];
+    }
+}
+
+/* SPHDensityRate: sph/funcs/density_funcs.pyx:89-158 -- drho_a +=
+ * m_b (v_a - v_b) . grad W(r_ab, hab), hks off.                           */
+void orc_drho(const orc_array *d, const orc_array *s, const int64_t *off, const int64_t *idx,
+              int dim, double *o0) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < d->n; ++i) {
+        if (!is_real(d, i)) { o0[i] = 0; continue; }
+        double nr = 0;
+        for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+            int64_t j = idx[k];
+            double hab = 0.5 * (d->h[i] + s->h[j]);
+            double vx = get0(d->u, i) - get0(s->u, j), vy = get0(d->v, i) - get0(s->v, j),
+                   vz = get0(d->w, i) - get0(s->w, j);
+            double g[3];
+            orc_cubic_grad(dim, get0(d->x, i), get0(d->y, i), get0(d->z, i), get0(s->x, j),
+                           get0(s->y, j), get0(s->z, j), hab, g);
+            nr += (vx * g[0] + vy * g[1] + vz * g[2]) * s->m[j];
+        }
+        o0[i] += nr;
+    }
+}
+
 /* XSPHCorrection: sph/funcs/xsph_funcs.pyx:31-88 (CSPH, no correction) */
 void orc_xsph(const orc_array *d, const orc_array *s, const int64_t *off,
               const int64_t *idx, int dim, double eps, int nout, double *o0, double *o1,

@@ -28,8 +28,9 @@ __global__ void k_tait(int64_t n, const double *rho, const int64_t *tag, float c
             cs[i] = 0.0;
             continue;
         }
-        float rf = (float)rho[i];
-        float lr = log1pf((rf - ro) / ro);
+        // the density excess in FP64: rho is within ~1e-3 of ro, where its
+        // FP32 rounding would cost p about 1e-5 of its relative accuracy
+        const float lr = log1pf((float)((rho[i] - (double)ro) / (double)ro));
         p[i] = (double)(B * expm1f(gamma * lr));
         cs[i] = (double)(co * expf(0.5f * (gamma - 1.f) * lr));
     }

@@ -80,6 +80,7 @@ struct RatesArgs {
     double gx, gy, gz;
     double *acc[3];
     double *pos[3];
+    double *drho;
 };
 
 // Destination of thread slot s; false for a non-LocalReal particle.
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
             // log1p/expm1 of the density excess so p keeps its relative accuracy
             // as rho -> ro.
             const float B = A.co * A.co * A.ro / A.gamma;
-            const float lr = log1pf((rf - A.ro) / A.ro);
+            const float lr = log1pf((float)((r64 - (double)A.ro) / (double)A.ro));
             pf = B * expm1f(A.gamma * lr);
             cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
         }
@@ -342,6 +343,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                           : (SPEC == 2 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH) : 0u);
     constexpr bool MAY_XSPH = SPEC != 1;
     constexpr bool MAY_BF = SPEC == 0;
+    constexpr bool MAY_DRHO = SPEC == 0;
     __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
     fill_shift_table<KX>(tab);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
     DestPos d;
     const bool real = load_dest(g, A.d, (int)s, d);
-    CSum ax, ay, az, xx, xy, xz;
+    CSum ax, ay, az, xx, xy, xz, dr;
     if (real) {
         const float4 vi = A.d.velh[s];
         const float4 sti = A.d.st[s];
@@ -358,7 +360,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         const bool uh = SPEC != 0 || g.uniform_h != 0;
         const float ihi = __fdividef(1.f, hi);
         const float faci = cubic_fac(dim, ihi);
-        float pax = 0.f, pay = 0.f, paz = 0.f, pxx = 0.f, pxy = 0.f, pxz = 0.f;
+        float pax = 0.f, pay = 0.f, paz = 0.f, pxx = 0.f, pxy = 0.f, pxz = 0.f, pdr = 0.f;
         const int nsrc = SPEC != 0 ? 1 : A.nsrc;
         for (int si = 0; si < nsrc; ++si) {
             const SrcDev &S = A.s[si];
@@ -399,6 +401,11 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                     pay = fmaf(gf, ry, pay);
                     paz = fmaf(gf, rz, paz);
                 }
+                if (MAY_DRHO && (fl & SPH_TERM_DRHO)) {
+                    // drho_i += m_j (v_i - v_j) . grad W(hab)  (density_funcs.pyx:117-158)
+                    const float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+                    pdr = fmaf(cubic_gfac(q, ih, rinv) * fac * mj * okf, dot, pdr);
+                }
                 if (MAY_XSPH && (fl & SPH_TERM_XSPH)) {
                     const float rhoab = 0.5f * (stj.x + rhoi);
                     const float temp = __fdividef(mj * (cubic_w(q) * fac), rhoab) * S.eps * okf;
@@ -437,6 +444,10 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
             [&]() {
                 ax.add(pax); ay.add(pay); az.add(paz);
                 pax = pay = paz = 0.f;
+                if (MAY_DRHO) {
+                    dr.add(pdr);
+                    pdr = 0.f;
+                }
                 if (MAY_XSPH) {
                     xx.add(pxx); xy.add(pxy); xz.add(pxz);
                     pxx = pxy = pxz = 0.f;
@@ -462,6 +473,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         if (A.acc[c]) A.acc[c][orig] = (A.accumulate ? A.acc[c][orig] : 0.0) + a3[c];
         if (A.pos[c]) A.pos[c][orig] = (A.accumulate ? A.pos[c][orig] : 0.0) + p3[c];
     }
+    if (A.drho) A.drho[orig] = (A.accumulate ? A.drho[orig] : 0.0) + (real ? dr.value() : 0.0);
 }
 
 // ---------------------------------------------------------------------------
@@ -847,6 +859,7 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
         a.acc[c] = acc ? acc[c] : nullptr;
         a.pos[c] = pos ? pos[c] : nullptr;
     }
+    a.drho = prm->drho_out;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     int spec = 0;

@@ -22,6 +22,7 @@ TERM_PGRAD = 1
 TERM_AVISC = 2
 TERM_XSPH = 4
 TERM_BFORCE = 8
+TERM_DRHO = 16
 
 MAX_SOURCES = 8
 MAX_AXPY_LINES = 12
@@ -86,7 +87,7 @@ class DensityParams(ctypes.Structure):
 class RatesParams(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int), ("add_velocity", ctypes.c_int),
                 ("gx", ctypes.c_double), ("gy", ctypes.c_double), ("gz", ctypes.c_double),
-                ("add_gravity", ctypes.c_int)]
+                ("add_gravity", ctypes.c_int), ("drho_out", ctypes.c_void_p)]
 
 
 class AxpyLine(ctypes.Structure):

@@ -31,8 +31,10 @@ logger = logging.getLogger()
 
 VEL = ("u", "v", "w")
 POS = ("x", "y", "z")
-VEL_KINDS = ("pgrad", "avisc", "bforce", "gravity")
+RHO = ("rho",)
+VEL_KINDS = ("pgrad", "avisc", "bforce", "gravity", "momentum")
 POS_KINDS = ("xsph", "step")
+RHO_KINDS = ("drho",)
 
 
 class DensityStage:
@@ -100,7 +102,7 @@ class RatesStage:
             kind = _kind_of(c.funcs[0])
             if kind not in RATE_KINDS + ("gravity", "step"):
                 raise NotImplementedError("%s cannot be integrated on the GPU" % kind)
-            allowed = VEL if kind in VEL_KINDS else POS
+            allowed = VEL if kind in VEL_KINDS else (RHO if kind in RHO_KINDS else POS)
             if list(c.updates) != list(allowed[:len(c.updates)]):
                 raise NotImplementedError(
                     "calc %s updates %s; the GPU integrator needs a prefix of %s"
@@ -125,9 +127,15 @@ class RatesStage:
         self.dim = dim or 3
 
     def _add_term(self, t):
-        # merge different kinds on the same source into one traversal
+        # merge different kinds on the same source into one traversal (only
+        # when their term flags are disjoint: MomentumEquation is PGrad + AV)
+        def flags(kinds):
+            f = 0
+            for k in kinds:
+                f |= gpu.RATE_TERM[k]
+            return f
         for e in self.terms:
-            if e["src"] is t["src"] and not (e["kinds"] & t["kinds"]):
+            if e["src"] is t["src"] and not (flags(e["kinds"]) & flags(t["kinds"])):
                 e["kinds"] = e["kinds"] | t["kinds"]
                 for k, v in t.items():
                     if k not in ("src", "kinds"):
@@ -147,13 +155,14 @@ class RatesStage:
         accumulate = not fresh
         acc = [rate.get(p) if p in self.props else None for p in VEL]
         pos = [rate.get(p) if p in self.props else None for p in POS]
+        drho = rate.get("rho") if "rho" in self.props else None
         terms = self.terms
         for hk in self.hooks:
             terms = hk.before_rates(integ, self, terms)
         if terms or self.gravity or self.add_velocity or (self.hooks and not accumulate):
             gpu.rates(cm, self.dest, terms, self.dim, acc=acc, pos=pos,
                       accumulate=accumulate, gravity=self.gravity,
-                      add_velocity=self.add_velocity)
+                      add_velocity=self.add_velocity, drho=drho)
         for hk in self.hooks:
             hk.after_rates(integ, self, acc)
         written.update(self.props)

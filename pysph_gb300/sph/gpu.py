@@ -13,7 +13,8 @@ from .. import native
 from ..base.cell import SNAPSHOT_PROPS, array_view
 
 RATE_TERM = {"pgrad": native.TERM_PGRAD, "avisc": native.TERM_AVISC,
-             "xsph": native.TERM_XSPH, "bforce": native.TERM_BFORCE}
+             "xsph": native.TERM_XSPH, "bforce": native.TERM_BFORCE,
+             "momentum": native.TERM_PGRAD | native.TERM_AVISC, "drho": native.TERM_DRHO}
 
 
 def _p(t):
@@ -59,7 +60,7 @@ def density(cm, dest, sources, dim, rho_out, tait=None, p_out=None, cs_out=None)
 
 
 def rates(cm, dest, terms, dim, acc=(), pos=(), accumulate=False, gravity=None,
-          add_velocity=False):
+          add_velocity=False, drho=None):
     """One launch of the rates kernel.  ``terms``: list of dicts with keys
     src (ParticleArray), kinds (set of pgrad/avisc/xsph/bforce) and the
     function parameters."""
@@ -80,7 +81,8 @@ def rates(cm, dest, terms, dim, acc=(), pos=(), accumulate=False, gravity=None,
                                    delp=t.get("delp", 1.0))
     g = gravity or (0.0, 0.0, 0.0)
     prm = native.RatesParams(dim=int(dim), add_velocity=1 if add_velocity else 0,
-                             gx=g[0], gy=g[1], gz=g[2], add_gravity=1 if gravity else 0)
+                             gx=g[0], gy=g[1], gz=g[2], add_gravity=1 if gravity else 0,
+                             drho_out=None if drho is None else drho.data_ptr())
     native.check(L.sph_rates(ctx, cm.slot(dest), arr, n, ctypes.byref(prm), _vp_array(acc),
                              _vp_array(pos), 1 if accumulate else 0), "rates")
 

@@ -14,8 +14,8 @@ from . import gpu
 
 logger = logging.getLogger()
 
-PAIR_KINDS = ("rho", "pgrad", "avisc", "xsph", "bforce")
-RATE_KINDS = ("pgrad", "avisc", "xsph", "bforce")
+PAIR_KINDS = ("rho", "pgrad", "avisc", "xsph", "bforce", "momentum", "drho")
+RATE_KINDS = ("pgrad", "avisc", "xsph", "bforce", "momentum", "drho")
 
 
 def _kind_of(func):
@@ -27,7 +27,7 @@ def _kind_of(func):
 
 def _term(func, kind):
     t = {"src": func.source, "kinds": {kind}}
-    if kind == "avisc":
+    if kind in ("avisc", "momentum"):
         t.update(alpha=func.alpha, beta=func.beta, eta=func.eta)
     elif kind == "xsph":
         t.update(eps=func.eps)
@@ -72,6 +72,8 @@ def run_functions(particles_cm, dest, funcs, kernel, outs, accumulate=False):
         terms = [_term(f, kind) for f in funcs]
         if kind == "xsph":
             gpu.rates(cm, dest, terms, kernel.dim, pos=targets, accumulate=accumulate)
+        elif kind == "drho":
+            gpu.rates(cm, dest, terms, kernel.dim, drho=targets[0], accumulate=accumulate)
         else:
             gpu.rates(cm, dest, terms, kernel.dim, acc=targets, accumulate=accumulate)
     if targets is not outs:

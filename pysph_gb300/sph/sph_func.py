@@ -184,6 +184,45 @@ class MonaghanArtificialVsicosity(SPHFunctionParticle):
         self.dst_reads = ["x", "y", "z", "h", "p", "u", "v", "w", "cs", "rho", "tag"]
 
 
+class MomentumEquation(SPHFunctionParticle):
+    """sph/funcs/pressure_funcs.pyx:106-252: the pressure gradient and the
+    Monaghan viscosity in one pair term.  Unlike MonaghanArtificialVsicosity
+    it stores ``eta``, so mu's denominator is |r_ab|^2 + eta^2 hab^2."""
+
+    gpu_kind = "momentum"
+
+    def __init__(self, source, dest, setup_arrays=True, alpha=1, beta=1, gamma=1.4, eta=0.1,
+                 dim=3, **kwargs):
+        SPHFunctionParticle.__init__(self, source, dest, setup_arrays, **kwargs)
+        self.alpha = float(alpha)
+        self.beta = float(beta)
+        self.gamma = float(gamma)
+        self.eta = float(eta)
+        self.id = "momentumequation"
+        self.tag = "velocity"
+        self.num_outputs = int(dim)
+
+    def set_src_dst_reads(self):
+        self.src_reads = ["x", "y", "z", "h", "m", "rho", "p", "u", "v", "w", "cs"]
+        self.dst_reads = ["x", "y", "z", "h", "rho", "p", "u", "v", "w", "cs", "tag"]
+
+
+class SPHDensityRate(SPHFunctionParticle):
+    """sph/funcs/density_funcs.pyx:89-158: drho_a/dt = sum_b m_b v_ab . grad W(hab)."""
+
+    gpu_kind = "drho"
+
+    def __init__(self, source, dest, setup_arrays=True, **kwargs):
+        SPHFunctionParticle.__init__(self, source, dest, True, **kwargs)
+        self.id = "densityrate"
+        self.tag = "density"
+        self.num_outputs = 1
+
+    def set_src_dst_reads(self):
+        self.src_reads = ["x", "y", "z", "h", "m", "u", "v", "w"]
+        self.dst_reads = ["x", "y", "z", "h", "tag", "u", "v", "w"]
+
+
 class XSPHCorrection(CSPHFunctionParticle):
     """sph/funcs/xsph_funcs.pyx:8-88."""
 
@@ -258,8 +297,6 @@ def _not_on_gpu(name, ref):
     return _F
 
 
-MomentumEquation = _not_on_gpu("MomentumEquation", "sph/funcs/pressure_funcs.pyx:106")
-SPHDensityRate = _not_on_gpu("SPHDensityRate", "sph/funcs/density_funcs.pyx:89")
 MorrisViscosity = _not_on_gpu("MorrisViscosity", "sph/funcs/viscosity_funcs.pyx:129")
 IdealGasEquation = _not_on_gpu("IdealGasEquation", "sph/funcs/eos_funcs.pyx:13")
 XSPHDensityRate = _not_on_gpu("XSPHDensityRate", "sph/funcs/xsph_funcs.pyx:96")

@@ -48,6 +48,17 @@ def elliptical_drop(dx=0.025, hdx=1.3, rho0=1.0, c0=1400.0, radius=1.0):
     )
 
 
+def circular_patch(dx=0.025, c0=100.0):
+    """The reference FluidSolver's circular patch (solver/fluid_solver.py:15-49):
+    the square lattice of ``elliptical_drop`` with ``m = dx^2``, ``h = 2 dx``,
+    ``rho = 1``, ``p = 0.5 c0^2 (1 - x^2 - y^2)``, ``cs = c0`` and
+    ``(u, v) = (-100 x, 100 y)``."""
+    props = elliptical_drop(dx=dx, hdx=2.0, rho0=1.0, c0=c0)
+    x, y = props["x"], props["y"]
+    props["p"] = 0.5 * 1.0 * c0 * c0 * (1.0 - (x * x + y * y))
+    return props
+
+
 def dam_break(dx=0.01, hdx=1.2, rho0=1000.0, column=(1.0, 2.0), tank=(4.0, 3.0),
               layers=3):
     """Water column in a tank with ``layers`` rows of wall particles.
@@ -185,6 +196,31 @@ def setup_drop(api, props, c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5,
         id="avisc"))
     s.add_operation_step([Fluid])
     s.add_operation_xsph(eps=eps)
+    s.setup_integrator(particles)
+    return s, particles
+
+
+def setup_fluid_solver(api, props, c0=100.0, ro=1.0, alpha=0.01, beta=0.0, eps=0.1,
+                       integrator="rk2"):
+    """The reference FluidSolver's operations (solver/fluid_solver.py:51-83):
+    Tait, continuity density rate, MomentumEquation (eta stored, 0.1),
+    position stepping and XSPH (2D)."""
+    base, sph, solver = api.base, api.sph, api.solver
+    Fluid = base.ParticleType.Fluid
+    pa = base.get_particle_array(name="fluid", type=Fluid, **props)
+    particles = base.Particles(arrays=[pa])
+    s = solver.Solver(dim=2, integrator_type=_integrator(api, integrator))
+    s.add_operation(solver.SPHOperation(
+        sph.TaitEquation.withargs(co=c0, ro=ro), on_types=[Fluid],
+        updates=["p", "cs"], id="eos"))
+    s.add_operation(solver.SPHIntegration(
+        sph.SPHDensityRate.withargs(hks=False), from_types=[Fluid], on_types=[Fluid],
+        updates=["rho"], id="density"))
+    s.add_operation(solver.SPHIntegration(
+        sph.MomentumEquation.withargs(alpha=alpha, beta=beta, hks=False),
+        from_types=[Fluid], on_types=[Fluid], updates=["u", "v", "w"], id="mom"))
+    s.add_operation_step([Fluid])
+    s.add_operation_xsph(eps=eps, hks=False)
     s.setup_integrator(particles)
     return s, particles
 

@@ -167,6 +167,44 @@ def fixture_dam(dx=0.04):
     return out
 
 
+def fixture_fluid(dx=0.05):
+    """The reference FluidSolver recipe (continuity + MomentumEquation) on
+    its circular patch, one RK2 step."""
+    props = W.circular_patch(dx=dx)
+    s, particles = W.setup_fluid_solver(REF, props)
+    out = {}
+    run_step(s, particles, 1e-4, out, nbr_pairs=[(0, 0)])
+    return out
+
+
+def fixture_square4_momentum():
+    """MomentumEquation (alpha = beta = 1, eta = 0.1) and SPHDensityRate on
+    the four-particle square of the reference's function tests."""
+    out = {}
+    x = np.array([0, 0, 1, 1], np.float64)
+    y = np.array([0, 1, 1, 0], np.float64)
+    u = np.array([1, 0, 0, -1], np.float64)
+    v = np.array([0, 1, -1, 0], np.float64)
+    p = np.array([0, 0, 1, 1], np.float64)
+    pa = rbase.get_particle_array(name="test", x=x, y=y, z=np.zeros(4), m=np.ones(4),
+                                  u=u, v=v, p=p, cs=np.ones(4),
+                                  tmpx=np.zeros(4), tmpy=np.zeros(4), tmpz=np.zeros(4))
+    particles = rbase.Particles(arrays=[pa])
+    kern = rbase.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("momentum", rsph.MomentumEquation.withargs(alpha=1.0, beta=1.0, eta=0.1),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("drho", rsph.SPHDensityRate.withargs(), ["tmpx"])):
+        func = fn.get_func(pa, pa)
+        calc = rsph.SPHCalc(particles, [pa], pa, kern, [func], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            out["%s_%d" % (name, k)] = pa.get(upn).copy()
+    for p_ in ("x", "y", "u", "v", "p", "m", "h", "rho", "cs"):
+        out["in_" + p_] = pa.get(p_).copy()
+    return out
+
+
 def fixture_cube(n=4096):
     props = W.cube_lattice(n)
     s, particles = W.setup_cube(REF, props)
@@ -183,7 +221,12 @@ def main():
         "drop_traj10": lambda: fixture_drop(10),
         "dam_step": fixture_dam,
         "cube_step": fixture_cube,
+        "fluid_step": fixture_fluid,
+        "square4_momentum": fixture_square4_momentum,
     }
+    only = sys.argv[1:]
+    if only:
+        fixtures = {k: v for k, v in fixtures.items() if k in only}
     for name, fn in fixtures.items():
         data = fn()
         path = os.path.join(HERE, name + ".npz")

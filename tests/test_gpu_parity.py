@@ -295,3 +295,38 @@ print("ok")
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]
+
+
+def test_square4_momentum_and_density_rate():
+    _need_gpu()
+    g = load("square4_momentum")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    pa = base.get_particle_array(name="test", tmpx=np.zeros(4), tmpy=np.zeros(4),
+                                 tmpz=np.zeros(4), **props)
+    particles = base.Particles(arrays=[pa])
+    kern = base.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("momentum", sph.MomentumEquation.withargs(alpha=1.0, beta=1.0, eta=0.1),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("drho", sph.SPHDensityRate.withargs(), ["tmpx"])):
+        calc = sph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            ref = g["%s_%d" % (name, k)]
+            got = pa.get(upn)
+            assert np.abs(got - ref).max() <= TOL * max(np.abs(ref).max(), 1.0), (name, k)
+
+
+def test_fluid_solver_rk2_step():
+    """The reference FluidSolver recipe: continuity density rate,
+    MomentumEquation, stepping and XSPH in one rates launch per evaluation."""
+    _need_gpu()
+    g = load("fluid_step")
+    p_in = inputs(g, "fluid")
+    s, particles = W.setup_fluid_solver(API, p_in)
+    s.integrator.integrate(float(g["dt"]))
+    pa = particles.arrays[0]
+    _check_step(g, [pa], 2, {"rho": ["density"], "u": ["mom"], "v": ["mom"],
+                             "x": ["step", "xsph"], "y": ["step", "xsph"]})
+    d_ref = g["out_fluid_rho"] - p_in["rho"]
+    assert normwise(pa.get("rho") - p_in["rho"], d_ref) < TOL

@@ -68,7 +68,7 @@ def test_avisc_never_stores_eta():
 def test_unsupported_functions_raise():
     a = _pa()
     with pytest.raises(NotImplementedError):
-        sph.MomentumEquation.withargs().get_func(a, a)
+        sph.XSPHDensityRate.withargs().get_func(a, a)
     with pytest.raises(NotImplementedError):
         base.QuinticSplineKernel(dim=2)
 
@@ -108,3 +108,14 @@ def test_compute_without_gpu_raises():
     s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1))
     with pytest.raises(RuntimeError, match="CUDA device"):
         s.integrator.integrate(1e-5)
+
+
+def test_fluid_solver_plan_integrates_rho():
+    s, particles = W.setup_fluid_solver(API, W.circular_patch(dx=0.2))
+    st = s.integrator.stages
+    assert [type(x).__name__ for x in st] == ["TaitStage", "RatesStage"]
+    rates = st[1]
+    assert set(rates.props) == {"rho", "u", "v", "w", "x", "y"}
+    assert len(rates.terms) == 1
+    assert rates.terms[0]["kinds"] == {"drho", "momentum", "xsph"}
+    assert rates.terms[0]["eta"] == 0.1

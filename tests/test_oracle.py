@@ -138,3 +138,37 @@ def test_cube_rk2_step_matches_reference():
     _cmp_step(g, prob, ["fluid"], 1e-13)
     for c, k in zip("uvw", range(3)):
         assert normwise(prob.k[("k2", 2)][k], g["eval2_k_pgrad_fluid_" + c]) < 1e-13
+
+
+def test_square4_momentum_and_density_rate():
+    """MomentumEquation (eta stored) and SPHDensityRate on the square."""
+    g = load("square4_momentum")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    off, idx = oracle.neighbors(props, props, cell_size=2.0, same=True)
+    res = oracle.pair_sum("momentum", props, props, off, idx, 2,
+                          {"alpha": 1.0, "beta": 1.0, "eta": 0.1}, 3)
+    for k in range(3):
+        np.testing.assert_allclose(res[k], g["momentum_%d" % k], rtol=1e-14, atol=1e-14)
+    dr = oracle.pair_sum("drho", props, props, off, idx, 2)[0]
+    np.testing.assert_allclose(dr, g["drho_0"], rtol=1e-14, atol=1e-14)
+
+
+def test_fluid_solver_pair_sums_bit_exact_with_reference_lists():
+    g = load("fluid_step")
+    p = inputs(g, "fluid")
+    off = g["nbr_fluid_fluid_offsets"]
+    idx = g["nbr_fluid_fluid_index"]
+    pt, ct = oracle.tait(p, 100.0, 1.0)
+    p2 = dict(p, p=pt, cs=ct)
+    dr = oracle.pair_sum("drho", p2, p2, off, idx, 2)[0]
+    np.testing.assert_array_equal(dr, g["eval1_k_density_fluid_rho"])
+    mo = oracle.pair_sum("momentum", p2, p2, off, idx, 2,
+                         {"alpha": 0.01, "beta": 0.0, "eta": 0.1}, 3)
+    for k, c in enumerate("uvw"):
+        np.testing.assert_array_equal(mo[k], g["eval1_k_mom_fluid_" + c])
+
+
+def test_fluid_solver_rk2_step_matches_reference():
+    g = load("fluid_step")
+    prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.fluid_ops(), 2, "rk2")
+    _cmp_step(g, prob, ["fluid"], 1e-13)
