@@ -24,8 +24,9 @@
  *   sph_tait              sph/funcs/eos_funcs.pyx:105-116 TaitEquation.eval_single
  *   sph_const_rates       external_force.pyx:39-45 GravityForce,
  *                         position_funcs.pyx:32-60 PositionStepping
- *   sph_integrate         solver/integrator.py:339-645 set_initial_arrays /
- *                         step / final_step of Euler and RK2
+ *   sph_integrate         solver/integrator.py:339-912 set_initial_arrays /
+ *                         step / final_step of Euler, RK2, RK4,
+ *                         PredictorCorrector and LeapFrog
  *   sph_invariants        (no counterpart: FP64 mass/momentum/energy sums)
  */
 #ifndef PYSPH_GB300_H
@@ -101,11 +102,16 @@ typedef struct {
 } sph_rates_params;
 
 /* One line of an integrator update, applied elementwise over n particles:
- *   tmp = base[i] + c1 * (k1[i] (+ k2[i]))     (k2 may be NULL)
- *   out[i] = tmp;  if (save) save[i] = tmp;
- * With mode 1, tmp = base[i] + k1[i] * c1 (Euler / RK2 predictor form).
+ *   mode 0: t = base + c1 * (k1 (+ k2))          RK2 final (k2 may be NULL)
+ *   mode 1: t = base + k1 * c1                   Euler / predictor step,
+ *                                                LeapFrog position correction
+ *   mode 2: t = base                             copy (set_initial_arrays)
+ *   mode 3: t = 2 * base - k1                    PredictorCorrector final
+ *   mode 4: t = base + c1 * (k2 - k1)            LeapFrog corrector
+ *   mode 5: t = base + c1 * (k1 + 2 k2 + 2 k3 + k4)   RK4 final
+ *   out[i] = t;  if (save) save[i] = t;
  * The FP64 operations are rounded exactly as the NumPy expressions of
- * solver/integrator.py:472-645. */
+ * solver/integrator.py:472-912 (left to right, no FMA contraction). */
 typedef struct {
     double *out;
     double *save;
@@ -113,7 +119,9 @@ typedef struct {
     const double *k1;
     const double *k2;
     double c1;
-    int mode; /* 0: base + c1*(k1+k2); 1: base + k1*c1; 2: copy base */
+    int mode;
+    const double *k3; /* mode 5 only */
+    const double *k4; /* mode 5 only */
 } sph_axpy_line;
 
 #define SPH_MAX_AXPY_LINES 12

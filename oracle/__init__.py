@@ -9,8 +9,8 @@ baseline of ``bench.py`` may import it; the product never does.
 
 Reference routines restated here (paths relative to ``source/pysph``):
 
-* ``solver/integrator.py:229-645`` -- calc bookkeeping, Euler and RK2 steps
-  (``Problem.integrate_euler`` / ``Problem.integrate_rk2``);
+* ``solver/integrator.py:229-912`` -- calc bookkeeping, Euler, RK2, RK4,
+  predictor-corrector and leap-frog steps (``Problem.integrate_*``);
 * ``sph/sph_calc.pyx:223-276`` -- zero the outputs, then sum over sources
   (``Problem._run_op``);
 * the per-function pair sums and the neighbour search -- see the C file.
@@ -188,6 +188,11 @@ class Op:
     xsph | bforce | gravity | step, on destination ``dest`` from
     ``sources``."""
 
+    # the function tags of the reference (sph/funcs/*.pyx ``self.tag``)
+    TAGS = {"rho": "density", "drho": "density", "tait": "state", "pgrad": "velocity",
+            "avisc": "velocity", "momentum": "velocity", "bforce": "velocity",
+            "gravity": "velocity", "step": "position", "xsph": "position"}
+
     def __init__(self, kind, dest, updates, sources=(), integrates=False, **params):
         self.kind = kind
         self.dest = dest
@@ -195,6 +200,7 @@ class Op:
         self.updates = list(updates)
         self.integrates = integrates
         self.params = params
+        self.tag = self.TAGS[kind]
 
 
 class Problem:
@@ -259,8 +265,10 @@ class Problem:
         return outs
 
     # integrator.py:432-470
-    def eval(self, kname):
+    def eval(self, kname, only=None):
         for ci, op in enumerate(self.ops):
+            if only is not None and ci not in only:
+                continue
             res = self._run_op(op)
             if op.integrates:
                 self.k[(kname, ci)] = res
@@ -309,6 +317,77 @@ class Problem:
                 self.arrays[op.dest][upd] = updated
                 init[(op.dest, upd)] = updated
         self._moved()
+
+
+    # integrator.py:369-430 reset_current_arrays + step, for the ops in ``only``
+    def _reset_and_step(self, init, kname, dt, only=None):
+        sel = [(ci, op) for ci, op in self._integrating() if only is None or ci in only]
+        for ci, op in sel:
+            for upd in op.updates:
+                self.arrays[op.dest][upd] = init[(op.dest, upd)].copy()
+        for ci, op in sel:
+            for j, upd in enumerate(op.updates):
+                cur = self.arrays[op.dest][upd]
+                self.arrays[op.dest][upd] = cur + self.k[(kname, ci)][j] * dt
+
+    # integrator.py:650-730
+    def integrate_rk4(self, dt):
+        init = self._set_initial()
+        for kname, h in (("k1", 0.5 * dt), ("k2", 0.5 * dt), ("k3", dt)):
+            self.eval(kname)
+            self._reset_and_step(init, kname, h)
+            self._moved()
+        self.eval("k4")
+        for ci, op in self._integrating():
+            for j, upd in enumerate(op.updates):
+                k1, k2, k3, k4 = (self.k[(kn, ci)][j] for kn in ("k1", "k2", "k3", "k4"))
+                updated = init[(op.dest, upd)] + (dt / 6.0) * (k1 + 2 * k2 + 2 * k3 + k4)
+                self.arrays[op.dest][upd] = updated
+                init[(op.dest, upd)] = updated
+        self._moved()
+
+    # integrator.py:734-796
+    def integrate_pc(self, dt):
+        init = self._set_initial()
+        for kname in ("k1", "k2"):
+            self.eval(kname)
+            self._reset_and_step(init, kname, 0.5 * dt)
+            self._moved()
+        for ci, op in self._integrating():
+            for upd in op.updates:
+                updated = 2 * self.arrays[op.dest][upd] - init[(op.dest, upd)]
+                self.arrays[op.dest][upd] = updated
+                init[(op.dest, upd)] = updated
+        self._moved()
+
+    # integrator.py:802-912
+    def integrate_leapfrog(self, dt):
+        init = self._set_initial()
+        ncalcs = {ci for ci, op in enumerate(self.ops) if op.tag != "position"}
+        pcalcs = [ci for ci, op in enumerate(self.ops) if op.tag == "position"]
+        icalcs = [ci for ci, op in self._integrating() if op.tag != "position"]
+        self.eval("k1", ncalcs)
+        self._reset_and_step(init, "k1", dt, ncalcs)
+        self.eval("k1", set(pcalcs))
+        self._reset_and_step(init, "k1", dt, set(pcalcs))
+        # add_correction_for_position (:841-872)
+        pos = self.ops[pcalcs[0]]
+        for ci in icalcs:
+            op = self.ops[ci]
+            if op.tag != "velocity":
+                continue
+            for j in range(len(op.updates)):
+                upd = pos.updates[j]
+                cur = self.arrays[pos.dest][upd]
+                self.arrays[pos.dest][upd] = cur + 0.5 * dt * dt * self.k[("k1", ci)][j]
+        self._moved()
+        self.eval("k2", ncalcs)
+        for ci in icalcs:
+            op = self.ops[ci]
+            for j, upd in enumerate(op.updates):
+                cur = self.arrays[op.dest][upd]
+                self.arrays[op.dest][upd] = cur + 0.5 * dt * (
+                    self.k[("k2", ci)][j] - self.k[("k1", ci)][j])
 
 
 # ---------------------------------------------------------------------------

@@ -60,8 +60,8 @@ struct AxpyArgs {
     int nl;
 };
 
-// integrator.py:472-645: every line is rounded exactly like the NumPy
-// expression it restates (no FMA contraction).
+// integrator.py:472-912: every line is rounded exactly like the NumPy
+// expression it restates (left to right, no FMA contraction).
 __global__ void k_axpy(int64_t n, const __grid_constant__ AxpyArgs a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -69,12 +69,29 @@ __global__ void k_axpy(int64_t n, const __grid_constant__ AxpyArgs a) {
             const sph_axpy_line &L = a.l[k];
             double b = L.base[i];
             double t;
-            if (L.mode == 0) {
+            switch (L.mode) {
+            case 0: {  // initial + 0.5*dt*(k1 + k2)
                 double s = L.k2 ? __dadd_rn(L.k1[i], L.k2[i]) : L.k1[i];
                 t = __dadd_rn(b, __dmul_rn(L.c1, s));
-            } else if (L.mode == 1) {
+                break;
+            }
+            case 1:  // current + step*dt
                 t = __dadd_rn(b, __dmul_rn(L.k1[i], L.c1));
-            } else {
+                break;
+            case 3:  // 2*current - initial
+                t = __dsub_rn(__dmul_rn(2.0, b), L.k1[i]);
+                break;
+            case 4:  // current + 0.5*dt*(k2 - k1)
+                t = __dadd_rn(b, __dmul_rn(L.c1, __dsub_rn(L.k2[i], L.k1[i])));
+                break;
+            case 5: {  // initial + dt/6*(k1 + 2*k2 + 2*k3 + k4)
+                double s = __dadd_rn(L.k1[i], __dmul_rn(2.0, L.k2[i]));
+                s = __dadd_rn(s, __dmul_rn(2.0, L.k3[i]));
+                s = __dadd_rn(s, L.k4[i]);
+                t = __dadd_rn(b, __dmul_rn(L.c1, s));
+                break;
+            }
+            default:  // 2: copy
                 t = b;
             }
             L.out[i] = t;
@@ -164,7 +181,10 @@ int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nl
     a.nl = nlines;
     for (int k = 0; k < nlines; ++k) {
         a.l[k] = lines[k];
-        if (!lines[k].out || !lines[k].base || (lines[k].mode != 2 && !lines[k].k1))
+        const sph_axpy_line &L = lines[k];
+        if (L.mode < 0 || L.mode > 5) return set_error(SPH_ERR_ARG, "integrate: unknown line mode");
+        if (!L.out || !L.base || (L.mode != 2 && !L.k1) || (L.mode == 4 && !L.k2) ||
+            (L.mode == 5 && (!L.k2 || !L.k3 || !L.k4)))
             return set_error(SPH_ERR_ARG, "integrate: null array in a line");
     }
     if (n == 0 || nlines == 0) return SPH_OK;

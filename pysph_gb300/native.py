@@ -93,7 +93,8 @@ class RatesParams(ctypes.Structure):
 class AxpyLine(ctypes.Structure):
     _fields_ = [("out", ctypes.c_void_p), ("save", ctypes.c_void_p),
                 ("base", ctypes.c_void_p), ("k1", ctypes.c_void_p),
-                ("k2", ctypes.c_void_p), ("c1", ctypes.c_double), ("mode", ctypes.c_int)]
+                ("k2", ctypes.c_void_p), ("c1", ctypes.c_double), ("mode", ctypes.c_int),
+                ("k3", ctypes.c_void_p), ("k4", ctypes.c_void_p)]
 
 
 class BatchInstance(ctypes.Structure):

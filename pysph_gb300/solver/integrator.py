@@ -1,10 +1,12 @@
-"""Euler and RK2 integrators driving the GPU stages.
+"""Euler, RK2, RK4, predictor-corrector and leap-frog integrators driving
+the GPU stages.
 
 Reference: solver/integrator.py.  The reference evaluates its calcs one by
 one (``eval`` :432-470), storing every integrating calc's result in its own
 ``_k<n>_<prop><i><j>`` array, then steps the properties with NumPy
-(``step`` :472-514, Euler ``final_step`` :535-553, RK2 ``final_step``
-:597-619).  Here ``setup_integrator`` compiles the calc list into stages:
+(``step`` :472-514, ``final_step`` of Euler :535-553, RK2 :597-619, RK4
+:669-692, PredictorCorrector :751-765, LeapFrog :874-891).  Here
+``setup_integrator`` compiles the calc list into stages:
 
 * ``DensityStage``  -- SPHRho over all its sources, fused with an
   immediately following TaitEquation on the same destination (the first
@@ -221,7 +223,8 @@ class Integrator:
                         if k_name not in calc.dst_writes[k_num]:
                             calc.dst_writes[k_num].append(k_name)
                         self.k_props[calc.id][k_num].append(k_name)
-        self.stages = self._plan(calcs)
+        self._plans = {}
+        self.stages = self._make_plans()
         self._integrated = {}
         for st in self.stages:
             if isinstance(st, RatesStage):
@@ -235,6 +238,18 @@ class Integrator:
                     dest.add_property({"name": "_rate%d_%s" % (l + 1, p)})
         self.set_rupdate_list()
         self.setup_done = True
+
+    def _make_plans(self):
+        """The stage list of one step (the learned closure hooks its stages)."""
+        return self._plan(self.calcs)
+
+    def _stages_for(self, calcs):
+        if calcs is None or calcs is self.calcs:
+            return self.stages
+        key = tuple(id(c) for c in calcs)
+        if key not in self._plans:
+            self._plans[key] = self._plan(list(calcs))
+        return self._plans[key]
 
     @staticmethod
     def _plan(calcs):
@@ -273,10 +288,11 @@ class Integrator:
 
     # -- the reference's step building blocks ------------------------------------
     def eval(self, calcs=None):
-        """Evaluate every stage for the current ``cstep`` (integrator.py:432-470)."""
+        """Evaluate the stages of ``calcs`` (default: all) for the current
+        ``cstep`` (integrator.py:432-470)."""
         kname = "k" + str(self.cstep)
         self._written = {}
-        for st in self.stages:
+        for st in self._stages_for(calcs):
             if self.stage_events is None:
                 st.run(self, kname)
             else:
@@ -296,30 +312,57 @@ class Integrator:
         else:
             self._timed("NNPSBuild", self.particles.update)
 
-    def _lines(self, mode, dt):
+    def _props_of(self, calcs):
+        """{id(dest): set of integrated properties} of the integrating calcs."""
+        out = {}
+        for c in calcs:
+            if c.integrates:
+                out.setdefault(id(c.dest), set()).update(c.updates)
+        return out
+
+    def _lines(self, mode, dt, level=1, calcs=None):
+        """Integrator lines (``gpu.axpy`` tuples) of every integrated property
+        (of ``calcs`` only, when given), grouped per destination array."""
+        only = None if calcs is None else self._props_of(calcs)
         out = []
         for dest, props in self._integrated.values():
+            if only is not None:
+                props = [p for p in props if p in only.get(id(dest), ())]
+            if not props:
+                continue
             n = dest.get_number_of_particles()
             lines = []
             for p in props:
                 cur = dest.get_device(p)
                 init = dest.get_device("_" + p + "_0")
-                r1 = dest.get_device("_rate1_" + p)
-                if mode == "copy":
+
+                def r(l, p=p):
+                    return dest.get_device("_rate%d_%s" % (l, p))
+
+                if mode == "copy":        # set_initial_arrays
                     lines.append((init, None, cur, None, None, 0.0, 2))
-                elif mode == "euler":
-                    lines.append((cur, init, init, r1, None, dt, 1))
-                elif mode == "predict":
-                    lines.append((cur, None, init, r1, None, dt, 1))
-                elif mode == "rk2":
-                    r2 = dest.get_device("_rate2_" + p)
-                    lines.append((cur, init, init, r1, r2, 0.5 * dt, 0))
+                elif mode == "reset":     # reset_current_arrays
+                    lines.append((cur, None, init, None, None, 0.0, 2))
+                elif mode == "euler":     # X0 + k1 dt, X0 <- X
+                    lines.append((cur, init, init, r(1), None, dt, 1))
+                elif mode == "predict":   # reset + step: X0 + k_level dt
+                    lines.append((cur, None, init, r(level), None, dt, 1))
+                elif mode == "rk2":       # X0 + dt/2 (k1 + k2), X0 <- X
+                    lines.append((cur, init, init, r(1), r(2), 0.5 * dt, 0))
+                elif mode == "rk4":       # X0 + dt/6 (k1 + 2k2 + 2k3 + k4), X0 <- X
+                    lines.append((cur, init, init, r(1), r(2), dt / 6.0, 5, r(3), r(4)))
+                elif mode == "pc":        # 2X - X0, X0 <- X
+                    lines.append((cur, init, cur, init, None, 0.0, 3))
+                elif mode == "leapfrog":  # X + dt/2 (k2 - k1)
+                    lines.append((cur, None, cur, r(1), r(2), 0.5 * dt, 4))
+                else:
+                    raise ValueError(mode)
             out.append((dest, n, props, lines))
         return out
 
-    def _apply(self, mode, dt=0.0):
+    def _apply(self, mode, dt=0.0, level=1, calcs=None):
         cm = self.particles.cell_manager
-        for dest, n, props, lines in self._lines(mode, dt):
+        for dest, n, props, lines in self._lines(mode, dt, level, calcs):
             gpu.axpy(cm, n, lines)
             if mode != "copy":
                 gpu.note_written(cm, dest, props)
@@ -330,21 +373,16 @@ class Integrator:
         self._apply("copy")
 
     def reset_current_arrays(self, calcs=None):
-        cm = self.particles.cell_manager
-        for dest, n, props, _ in self._lines("copy", 0.0):
-            lines = [(dest.get_device(p), None, dest.get_device("_" + p + "_0"), None, None,
-                      0.0, 2) for p in props]
-            gpu.axpy(cm, n, lines)
-            gpu.note_written(cm, dest, props)
-            if any(p in POS for p in props):
-                dest.set_dirty(True)
+        self._apply("reset", calcs=calcs)
 
     def step(self, calcs=None, dt=0.0):
-        """X = X0 + dt k (the reference's reset + step)."""
-        self._apply("predict", dt)
+        """The reference's reset_current_arrays + step: X = X0 + dt k_cstep
+        for the integrating calcs of ``calcs`` (default: all)."""
+        self._apply("predict", dt, level=self.cstep, calcs=calcs)
         self.cstep += 1
 
     def do_step(self, calcs=None, dt=0.0):
+        """integrator.py:380-411: evaluate, then step from the initial arrays."""
         self.eval(calcs)
         self.step(calcs, dt)
 
@@ -381,9 +419,7 @@ class RK2Integrator(Integrator):
             self.setup_integrator()
         self.set_initial_arrays()
         self.cstep = 1
-        self.eval(self.calcs)
-        self._apply("predict", dt)
-        self.cstep = 2
+        self.do_step(self.calcs, dt)
         self._update_particles()
         self.eval(self.calcs)
         self._apply("rk2", dt)
@@ -391,14 +427,117 @@ class RK2Integrator(Integrator):
         self._update_particles()
 
 
-def _not_here(name, ref):
-    class _I(Integrator):
-        def __init__(self, *a, **k):
-            raise NotImplementedError("%s (%s) is not part of this build" % (name, ref))
-    _I.__name__ = name
-    return _I
+class RK4Integrator(Integrator):
+    """X(t+h) = X + h/6 (K1 + 2K2 + 2K3 + K4), integrator.py:650-730.
+
+    K1 = F(X), K2 = F(X + h/2 K1), K3 = F(X + h/2 K2), K4 = F(X + h K3);
+    four pair-loop evaluations and four neighbour builds per step."""
+
+    def __init__(self, particles, calcs=None):
+        Integrator.__init__(self, particles, calcs)
+        self.nsteps = 4
+
+    def integrate(self, dt):
+        if not self.setup_done:
+            self.setup_integrator()
+        self.set_initial_arrays()
+        self.cstep = 1
+        self.do_step(self.calcs, 0.5 * dt)
+        self._update_particles()
+        self.do_step(self.calcs, 0.5 * dt)
+        self._update_particles()
+        self.do_step(self.calcs, dt)
+        self._update_particles()
+        self.eval(self.calcs)
+        self._apply("rk4", dt)
+        self.cstep = 1
+        self._update_particles()
 
 
-RK4Integrator = _not_here("RK4Integrator", "solver/integrator.py:650")
-PredictorCorrectorIntegrator = _not_here("PredictorCorrectorIntegrator", "solver/integrator.py:734")
-LeapFrogIntegrator = _not_here("LeapFrogIntegrator", "solver/integrator.py:802")
+class PredictorCorrectorIntegrator(Integrator):
+    """integrator.py:734-796: X* = X + h/2 F(X); X** = X + h/2 F(X*);
+    X(t+h) = 2 X** - X."""
+
+    def __init__(self, particles, calcs=None):
+        Integrator.__init__(self, particles, calcs)
+        self.nsteps = 2
+
+    def integrate(self, dt):
+        if not self.setup_done:
+            self.setup_integrator()
+        self.set_initial_arrays()
+        self.cstep = 1
+        self.do_step(self.calcs, 0.5 * dt)
+        self._update_particles()
+        self.do_step(self.calcs, 0.5 * dt)
+        self._update_particles()
+        self._apply("pc", dt)
+        self._update_particles()
+        self.cstep = 1
+
+
+class LeapFrogIntegrator(Integrator):
+    """integrator.py:802-912.
+
+    Non-position calcs (tag != "position") and position calcs are evaluated
+    separately: v* = v0 + h F0; then the position calcs see v*, x = x0 + h k_x
+    and every velocity calc adds h^2/2 F0 to the first position calc's
+    properties, component by component (``add_correction_for_position``);
+    after a neighbour update the non-position calcs are evaluated again and
+    v = v* + h/2 (F - F0) (likewise for other integrated non-position
+    properties, e.g. a density rate)."""
+
+    def __init__(self, particles, calcs=None):
+        Integrator.__init__(self, particles, calcs)
+        self.nsteps = 2
+
+    def _make_plans(self):
+        nst = self._plan(self.ncalcs)
+        pst = self._plan(self.pcalcs)
+        self._plans[tuple(id(c) for c in self.ncalcs)] = nst
+        self._plans[tuple(id(c) for c in self.pcalcs)] = pst
+        return nst + pst
+
+    def _correction_lines(self, dt):
+        """add_correction_for_position (integrator.py:841-872)."""
+        if not self.pcalcs:
+            raise IndexError("list index out of range")
+        pos_calc = self.pcalcs[0]
+        pos_updates = list(pos_calc.updates)
+        vel_props = []
+        for calc in self.icalcs:
+            if calc.tag != "velocity":
+                continue
+            if calc.dest is not pos_calc.dest:
+                raise NotImplementedError("LeapFrog position correction across two arrays")
+            for j in range(len(calc.updates)):
+                if j >= len(pos_updates):
+                    raise IndexError("list index out of range")
+                if j >= len(vel_props):
+                    vel_props.append(calc.updates[j])
+        dest = pos_calc.dest
+        c = 0.5 * dt * dt
+        lines = []
+        for j, vp in enumerate(vel_props):
+            x = dest.get_device(pos_updates[j])
+            lines.append((x, None, x, dest.get_device("_rate1_" + vp), None, c, 1))
+        return dest, lines
+
+    def integrate(self, dt):
+        if not self.setup_done:
+            self.setup_integrator()
+        dest, corr = self._correction_lines(dt)
+        self.set_initial_arrays()
+        self.cstep = 1
+        self.do_step(self.ncalcs, dt)
+        self.cstep = 1
+        self.do_step(self.pcalcs, dt)
+        cm = self.particles.cell_manager
+        if corr:
+            gpu.axpy(cm, dest.get_number_of_particles(), corr)
+            gpu.note_written(cm, dest, list(self.pcalcs[0].updates))
+            dest.set_dirty(True)
+        self._update_particles()
+        self.eval(self.ncalcs)
+        self._apply("leapfrog", dt, calcs=self.icalcs)
+        self.cstep = 1

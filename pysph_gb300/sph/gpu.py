@@ -107,19 +107,25 @@ def const_rates(cm, dest, kind, outs, g=None):
 
 
 def axpy(cm, n, lines):
-    """``lines``: list of (out, save, base, k1, k2, c1, mode) device tensors."""
+    """``lines``: list of (out, save, base, k1, k2, c1, mode[, k3, k4]) device
+    tensors (modes as ``sph_axpy_line`` in the C header)."""
     if not lines:
         return
     L = native.lib()
     ctx = cm.context()
+
+    def ptr(t):
+        return None if t is None else t.data_ptr()
+
     for start in range(0, len(lines), native.MAX_AXPY_LINES):
         chunk = lines[start:start + native.MAX_AXPY_LINES]
         arr = (native.AxpyLine * len(chunk))()
-        for i, (out, save, base, k1, k2, c1, mode) in enumerate(chunk):
-            arr[i] = native.AxpyLine(out=out.data_ptr(), save=None if save is None else save.data_ptr(),
-                                     base=base.data_ptr(), k1=None if k1 is None else k1.data_ptr(),
-                                     k2=None if k2 is None else k2.data_ptr(), c1=float(c1),
-                                     mode=int(mode))
+        for i, line in enumerate(chunk):
+            out, save, base, k1, k2, c1, mode = line[:7]
+            k3, k4 = (line[7], line[8]) if len(line) > 7 else (None, None)
+            arr[i] = native.AxpyLine(out=out.data_ptr(), save=ptr(save), base=base.data_ptr(),
+                                     k1=ptr(k1), k2=ptr(k2), c1=float(c1), mode=int(mode),
+                                     k3=ptr(k3), k4=ptr(k4))
         native.check(L.sph_integrate(ctx, n, arr, len(chunk)), "integrate")
 
 

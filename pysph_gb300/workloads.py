@@ -169,7 +169,10 @@ def drop_batch(count=256, seed=0, rmin=0.5, rmax=1.5, dxmin=0.01, dxmax=0.04,
 
 def _integrator(api, name):
     return {"euler": api.solver.EulerIntegrator,
-            "rk2": api.solver.RK2Integrator}[name]
+            "rk2": api.solver.RK2Integrator,
+            "rk4": api.solver.RK4Integrator,
+            "pc": api.solver.PredictorCorrectorIntegrator,
+            "leapfrog": api.solver.LeapFrogIntegrator}[name]
 
 
 def setup_drop(api, props, c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5,

@@ -63,6 +63,7 @@ def run_step(s, particles, dt, out, nbr_pairs=()):
 
     def eval_and_record(calcs):
         e = counter[0] + 1
+        kn = "k%d" % integ.cstep
         for pa in arrays:
             for p in STATE:
                 out["eval%d_pre_%s_%s" % (e, pa.name, p)] = pa.get(p).copy()
@@ -73,7 +74,7 @@ def run_step(s, particles, dt, out, nbr_pairs=()):
         for calc in calcs:
             if calc.integrates:
                 pa = arrays[calc.dnum]
-                names = calc.dst_writes["k%d" % e]
+                names = calc.dst_writes[kn]
                 for j, upd in enumerate(calc.updates):
                     out["eval%d_k_%s_%s" % (e, calc.id, upd)] = pa.get(names[j]).copy()
         counter[0] += 1
@@ -205,11 +206,42 @@ def fixture_square4_momentum():
     return out
 
 
-def fixture_cube(n=4096):
+def fixture_cube(n=4096, integrator="rk2"):
     props = W.cube_lattice(n)
-    s, particles = W.setup_cube(REF, props)
+    s, particles = W.setup_cube(REF, props, integrator=integrator)
     out = {}
     run_step(s, particles, 1e-4, out, nbr_pairs=[(0, 0)])
+    return out
+
+
+def fixture_drop_integrator(integrator, dx=0.05, steps=3):
+    """The elliptical drop stepped by another integrator: the first step
+    recorded evaluation by evaluation, then the state after ``steps``."""
+    props = W.elliptical_drop(dx=dx)
+    s, particles = W.setup_drop(REF, props, integrator=integrator)
+    out = {}
+    run_step(s, particles, 1e-5, out, nbr_pairs=[(0, 0)])
+    for _ in range(steps - 1):
+        s.integrator.integrate(1e-5)
+    pa = particles.arrays[0]
+    for p in ("x", "y", "u", "v", "rho", "p", "cs"):
+        out["final_%s" % p] = pa.get(p).copy()
+    out["steps"] = np.int64(steps)
+    return out
+
+
+def fixture_fluid_integrator(integrator, dx=0.05, steps=3):
+    """The FluidSolver recipe (integrated density) under another integrator."""
+    props = W.circular_patch(dx=dx)
+    s, particles = W.setup_fluid_solver(REF, props, integrator=integrator)
+    out = {}
+    run_step(s, particles, 1e-4, out, nbr_pairs=[(0, 0)])
+    for _ in range(steps - 1):
+        s.integrator.integrate(1e-4)
+    pa = particles.arrays[0]
+    for p in ("x", "y", "u", "v", "rho", "p", "cs"):
+        out["final_%s" % p] = pa.get(p).copy()
+    out["steps"] = np.int64(steps)
     return out
 
 
@@ -223,6 +255,11 @@ def main():
         "cube_step": fixture_cube,
         "fluid_step": fixture_fluid,
         "square4_momentum": fixture_square4_momentum,
+        "drop_rk4": lambda: fixture_drop_integrator("rk4"),
+        "drop_pc": lambda: fixture_drop_integrator("pc"),
+        "fluid_rk4": lambda: fixture_fluid_integrator("rk4"),
+        "fluid_pc": lambda: fixture_fluid_integrator("pc"),
+        "cube_leapfrog": lambda: fixture_cube(1000, "leapfrog"),
     }
     only = sys.argv[1:]
     if only:

@@ -119,3 +119,37 @@ def test_fluid_solver_plan_integrates_rho():
     assert len(rates.terms) == 1
     assert rates.terms[0]["kinds"] == {"drho", "momentum", "xsph"}
     assert rates.terms[0]["eta"] == 0.1
+
+
+def test_multistage_integrators_rate_arrays():
+    for scheme, nsteps in (("rk4", 4), ("pc", 2), ("leapfrog", 2)):
+        s, particles = W.setup_cube(API, W.cube_lattice(512), integrator=scheme)
+        integ = s.integrator
+        assert integ.nsteps == nsteps
+        fluid = particles.arrays[0]
+        for l in range(1, nsteps + 1):
+            for p in ("u", "v", "w", "x", "y", "z"):
+                assert fluid.has_array("_rate%d_%s" % (l, p)), (scheme, l, p)
+        assert not fluid.has_array("_rate%d_u" % (nsteps + 1))
+
+
+def test_leapfrog_plans_velocity_and_position_calcs_apart():
+    """integrator.py:893-912 evaluates non-position and position calcs in
+    separate passes, so they never share a rates launch."""
+    s, _ = W.setup_cube(API, W.cube_lattice(512), integrator="leapfrog")
+    integ = s.integrator
+    assert [type(x).__name__ for x in integ.stages] == ["DensityStage", "RatesStage", "RatesStage"]
+    vel, pos = integ.stages[1], integ.stages[2]
+    assert set(vel.props) == {"u", "v", "w"} and not vel.add_velocity
+    assert set(pos.props) == {"x", "y", "z"} and pos.add_velocity and not pos.terms
+    assert integ._stages_for(integ.ncalcs) == integ.stages[:2]
+    assert integ._stages_for(integ.pcalcs) == integ.stages[2:]
+    # the RK2 plan of the same calcs fuses them into one rates launch
+    s2, _ = W.setup_cube(API, W.cube_lattice(512), integrator="rk2")
+    assert [type(x).__name__ for x in s2.integrator.stages] == ["DensityStage", "RatesStage"]
+
+
+def test_leapfrog_2d_index_error_before_any_work():
+    s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1), integrator="leapfrog")
+    with pytest.raises(IndexError):
+        s.integrator.integrate(1e-5)

@@ -172,3 +172,53 @@ def test_fluid_solver_rk2_step_matches_reference():
     g = load("fluid_step")
     prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.fluid_ops(), 2, "rk2")
     _cmp_step(g, prob, ["fluid"], 1e-13)
+
+
+# -- the other integrators of solver/integrator.py:650-912 -------------------
+
+def _multi_step(g, arrays, ops, dim, scheme, tol_step, tol_final):
+    prob = _step_problem(g, arrays, ops, dim, scheme)
+    _cmp_step(g, prob, list(arrays), tol_step)
+    if "steps" in g:
+        for _ in range(int(g["steps"]) - 1):
+            getattr(prob, "integrate_" + scheme)(float(g["dt"]))
+        for p_ in ("x", "y", "u", "v", "rho", "p", "cs"):
+            assert normwise(prob.arrays["fluid"][p_], g["final_" + p_]) < tol_final, p_
+    return prob
+
+
+@pytest.mark.parametrize("scheme", ["rk4", "pc"])
+def test_drop_step_matches_reference(scheme):
+    g = load("drop_" + scheme)
+    assert int(g["n_evals"]) == {"rk4": 4, "pc": 2}[scheme]
+    _multi_step(g, {"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2, scheme, 1e-13, 1e-12)
+    if scheme == "rk4":
+        prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2, scheme)
+        for c, k in zip("uv", range(2)):
+            assert normwise(prob.k[("k3", 2)][k], g["eval3_k_pgrad_fluid_" + c]) < 1e-13
+
+
+@pytest.mark.parametrize("scheme", ["rk4", "pc"])
+def test_fluid_solver_step_matches_reference(scheme):
+    g = load("fluid_" + scheme)
+    _multi_step(g, {"fluid": inputs(g, "fluid")}, oracle.fluid_ops(), 2, scheme, 1e-13, 1e-12)
+
+
+def test_cube_leapfrog_step_matches_reference():
+    g = load("cube_leapfrog")
+    assert int(g["n_evals"]) == 3
+    prob = _step_problem(g, {"fluid": inputs(g, "fluid")}, oracle.cube_ops(), 3, "leapfrog")
+    _cmp_step(g, prob, ["fluid"], 1e-13)
+    # the position calc was evaluated once, on the predicted velocities
+    for c in "xyz":
+        assert normwise(prob.k[("k1", 4)]["xyz".index(c)], g["eval2_k_step_fluid_" + c]) < 1e-13
+
+
+def test_leapfrog_2d_position_correction_index_error():
+    """2D velocity calcs with three outputs (Monaghan AV) index past the two
+    position updates in add_correction_for_position (integrator.py:861-865);
+    the reference raises IndexError there and so does the oracle."""
+    g = load("drop_step")
+    prob = oracle.Problem({"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2)
+    with pytest.raises(IndexError):
+        prob.integrate_leapfrog(1e-5)
