@@ -152,6 +152,14 @@ int sph_nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, doub
  * next build.  No reference counterpart (the reference rebuilds its lists
  * at every update, base/nnps.pyx:581-620). */
 int sph_ctx_set_skin(sph_ctx *ctx, double skin_fraction);
+
+/* Symmetric neighbour relation for per-particle smoothing lengths
+ * (base/nnps.pyx:654-749 VarHNbrParticleLocator, used when
+ * Particles(variable_h=True)): with on = 1, source j is a neighbour of
+ * destination i when |x_i - x_j| < radius_scale h_i OR < radius_scale h_j
+ * (each test exactly as the reference's FP64 one).  Takes effect at the
+ * next build. */
+int sph_ctx_set_symmetric(sph_ctx *ctx, int on);
 /* Particles.update() (base/particles.py:159-200 -> cell.pyx:927-1015):
  * with a skin and the same arrays, refresh the sorted snapshot in the
  * order of the last full build (one kernel, the reference's jump check

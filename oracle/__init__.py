@@ -63,6 +63,8 @@ def lib():
             i = ctypes.c_int
             L.orc_neighbors.restype = ctypes.c_int64
             L.orc_neighbors.argtypes = [P, P, d, d, i, vp, vp]
+            L.orc_neighbors_varh.restype = ctypes.c_int64
+            L.orc_neighbors_varh.argtypes = [P, P, d, d, i, vp, vp]
             L.orc_sph_rho.argtypes = [P, P, vp, vp, i, vp]
             L.orc_tait.argtypes = [P, d, d, d, vp, vp]
             L.orc_pgrad.argtypes = [P, P, vp, vp, i, i, vp, vp, vp]
@@ -117,17 +119,17 @@ def cubic_grad(dim, a, b, h):
     return g
 
 
-def neighbors(dst, src, cell_size, radius_scale=2.0, same=False):
-    """CSR neighbour lists (ascending source index, self last if ``same``)."""
+def neighbors(dst, src, cell_size, radius_scale=2.0, same=False, variable_h=False):
+    """CSR neighbour lists (ascending source index, self last if ``same``);
+    ``variable_h`` gives the symmetric relation of VarHNbrParticleLocator."""
     D, S = _Arr(dst), _Arr(src)
     n = D.st.n
+    fn = lib().orc_neighbors_varh if variable_h else lib().orc_neighbors
     offsets = np.zeros(n + 1, np.int64)
-    lib().orc_neighbors(D.ref, S.ref, cell_size, radius_scale, int(same),
-                        offsets.ctypes.data, None)
+    fn(D.ref, S.ref, cell_size, radius_scale, int(same), offsets.ctypes.data, None)
     np.cumsum(offsets, out=offsets)
     index = np.zeros(max(int(offsets[-1]), 1), np.int64)
-    lib().orc_neighbors(D.ref, S.ref, cell_size, radius_scale, int(same),
-                        offsets.ctypes.data, index.ctypes.data)
+    fn(D.ref, S.ref, cell_size, radius_scale, int(same), offsets.ctypes.data, index.ctypes.data)
     return offsets, index[: offsets[-1]]
 
 
@@ -204,7 +206,7 @@ class Op:
 
 
 class Problem:
-    def __init__(self, arrays, ops, dim, radius_scale=2.0):
+    def __init__(self, arrays, ops, dim, radius_scale=2.0, variable_h=False):
         # arrays: dict name -> dict of float64 property arrays (copied)
         self.arrays = {}
         for name, props in arrays.items():
@@ -220,6 +222,7 @@ class Problem:
         self.ops = ops
         self.dim = dim
         self.radius_scale = radius_scale
+        self.variable_h = variable_h
         max_h = max(float(a["h"].max()) for a in self.arrays.values() if a["h"].size)
         # CellManager.compute_cell_size: base/cell.pyx:893-925
         self.cell_size = radius_scale * max_h
@@ -231,7 +234,7 @@ class Problem:
         if key not in self.nbr_cache:
             self.nbr_cache[key] = neighbors(self.arrays[dest], self.arrays[src],
                                             self.cell_size, self.radius_scale,
-                                            same=(dest == src))
+                                            same=(dest == src), variable_h=self.variable_h)
         return self.nbr_cache[key]
 
     def _moved(self):

@@ -119,10 +119,19 @@ static int cmp_i64(const void *a, const void *b) {
 }
 
 /* Pass 1 (index == NULL): counts into offsets[1..n]; returns total.
- * Pass 2: fills index given prefix offsets.                              */
-int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_size,
-                      double radius_scale, int same, int64_t *offsets, int64_t *index) {
+ * Pass 2: fills index given prefix offsets.
+ * symmetric = 0: j is a neighbour of i when |x_j - x_i|^2 < (radius_scale h_i)^2
+ *   (FixedDestNbrParticleLocator, base/nnps.pyx:271-356, 525-620);
+ * symmetric = 1: also when |x_i - x_j|^2 < (radius_scale h_j)^2, the union
+ *   VarHNbrParticleLocator builds from its reversed locator (base/nnps.pyx:
+ *   654-749).                                                             */
+static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double cell_size,
+                              double radius_scale, int same, int symmetric, int64_t *offsets,
+                              int64_t *index) {
     int64_t ns = src->n, nd = dst->n;
+    double hmax_src = 0.0;
+    for (int64_t j = 0; j < ns; ++j)
+        if (src->h[j] > hmax_src) hmax_src = src->h[j];
     cell_rec *recs = (cell_rec *)malloc(sizeof(cell_rec) * (ns > 0 ? ns : 1));
     for (int64_t j = 0; j < ns; ++j) {
         recs[j].cx = (int64_t)(int)floor(get0(src->x, j) / cell_size);
@@ -137,7 +146,9 @@ int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_si
         double px = get0(dst->x, i), py = get0(dst->y, i), pz = get0(dst->z, i);
         double radius = dst->h[i] * radius_scale;
         double radius2 = radius * radius;
-        int64_t d = (int64_t)(int)ceil(radius / cell_size);
+        double reach = radius;
+        if (symmetric && hmax_src * radius_scale > reach) reach = hmax_src * radius_scale;
+        int64_t d = (int64_t)(int)ceil(reach / cell_size);
         int64_t cx = (int)floor(px / cell_size), cy = (int)floor(py / cell_size),
                 cz = (int)floor(pz / cell_size);
         int64_t cnt = 0;
@@ -153,7 +164,14 @@ int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_si
                         double sx = get0(src->x, j), sy = get0(src->y, j), sz = get0(src->z, j);
                         double d2 = ((sx - px) * (sx - px) + (sy - py) * (sy - py) +
                                      (sz - pz) * (sz - pz));
-                        if (d2 < radius2) {
+                        int hit = d2 < radius2;
+                        if (!hit && symmetric) {
+                            double rj = src->h[j] * radius_scale;
+                            double e2 = ((px - sx) * (px - sx) + (py - sy) * (py - sy) +
+                                         (pz - sz) * (pz - sz));
+                            hit = e2 < rj * rj;
+                        }
+                        if (hit) {
                             if (index) index[base + cnt] = j;
                             ++cnt;
                         }
@@ -176,6 +194,16 @@ int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_si
     }
     free(recs);
     return total;
+}
+
+int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_size,
+                      double radius_scale, int same, int64_t *offsets, int64_t *index) {
+    return neighbors_impl(dst, src, cell_size, radius_scale, same, 0, offsets, index);
+}
+
+int64_t orc_neighbors_varh(const orc_array *dst, const orc_array *src, double cell_size,
+                           double radius_scale, int same, int64_t *offsets, int64_t *index) {
+    return neighbors_impl(dst, src, cell_size, radius_scale, same, 1, offsets, index);
 }
 
 /* ---------------------------------------------------------------------- */

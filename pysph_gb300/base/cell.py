@@ -61,6 +61,9 @@ class CellManager:
         self.initialized = False
         # internal grid cells per reference cell (1..3); see the autotuner
         self.cell_subdivision = None
+        # variable h: the symmetric neighbour relation of
+        # VarHNbrParticleLocator (set by NNPSManager(variable_h=True))
+        self.symmetric = False
         self._ctx = None
         self._snap_versions = []
         self._build_count = 0
@@ -127,10 +130,22 @@ class CellManager:
             native.check(L.sph_ctx_create(dim, ctypes.byref(h)), "sph_ctx_create")
             from ..tuning import list_skin
             native.check(L.sph_ctx_set_skin(h, list_skin()), "sph_ctx_set_skin")
+            native.check(L.sph_ctx_set_symmetric(h, 1 if self.symmetric else 0),
+                         "sph_ctx_set_symmetric")
             self._ctx = h
         native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
             torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
         return self._ctx
+
+    def set_symmetric(self, on):
+        """Use the variable-h (symmetric) neighbour relation from the next build."""
+        on = bool(on)
+        if on != self.symmetric:
+            self.symmetric = on
+            self.is_dirty = True
+            if self._ctx is not None:
+                native.check(native.lib().sph_ctx_set_symmetric(self._ctx, 1 if on else 0),
+                             "sph_ctx_set_symmetric")
 
     def _subdivision(self):
         if self.cell_subdivision is None:

@@ -162,8 +162,17 @@ class FixedDestNbrParticleLocator(NbrParticleLocatorBase):
 
 
 class VarHNbrParticleLocator(FixedDestNbrParticleLocator):
-    def __init__(self, *args, **kwargs):
-        raise NotImplementedError("variable-h neighbour search is not part of the GPU hot path")
+    """base/nnps.pyx:654-749: neighbours for per-particle smoothing lengths,
+    symmetric -- j is a neighbour of i when i is within the radius of j or j
+    within the radius of i.  The reference builds the union from a reversed
+    locator; here the cell manager's device build applies both tests (its
+    context is switched to the symmetric relation), so every pair pass and
+    exported list of that manager sees the union."""
+
+    def __init__(self, source, dest, radius_scale, cell_manager=None, h="h"):
+        if cell_manager is not None:
+            cell_manager.set_symmetric(True)
+        FixedDestNbrParticleLocator.__init__(self, source, dest, radius_scale, cell_manager)
 
 
 class NNPSManager:
@@ -171,9 +180,9 @@ class NNPSManager:
 
     def __init__(self, cell_manager=None, variable_h=False,
                  locator_type=NeighborLocatorType.SPHNeighborLocator):
-        if variable_h:
-            raise NotImplementedError("variable-h neighbour search is not part of the GPU hot path")
         self.cell_manager = cell_manager
+        if variable_h and cell_manager is not None:
+            cell_manager.set_symmetric(True)
         self.variable_h = variable_h
         self.locator_type = locator_type
         self.particle_locator_cache = {}
@@ -185,7 +194,8 @@ class NNPSManager:
         key = (source.name, dest.name, float(radius_scale))
         loc = self.particle_locator_cache.get(key)
         if loc is None:
-            loc = FixedDestNbrParticleLocator(source, dest, radius_scale, self.cell_manager)
+            cls = VarHNbrParticleLocator if self.variable_h else FixedDestNbrParticleLocator
+            loc = cls(source, dest, radius_scale, self.cell_manager)
             loc.set_locator_type(self.locator_type)
             self.particle_locator_cache[key] = loc
         return loc

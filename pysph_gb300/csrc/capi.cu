@@ -96,7 +96,7 @@ int sph_ctx_destroy(sph_ctx *c) {
     free_lists(c);
     for (auto &A : c->arrays) {
         cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
-        cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st);
+        cudaFree(A.posm); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st);
         cudaFree(A.nrm); cudaFree(A.tan);
         cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0); cudaFree(A.inv);
     }
@@ -133,6 +133,16 @@ int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
         return set_error(SPH_ERR_ARG, "sph_ctx_set_skin: fraction must be in [0, 0.5]");
     if (skin_fraction != c->skin_frac) {
         c->skin_frac = skin_fraction;
+        c->built = false;   // the next update builds afresh
+    }
+    return SPH_OK;
+}
+
+int sph_ctx_set_symmetric(sph_ctx *c, int on) {
+    CHECK_CTX(c);
+    if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_symmetric: on must be 0 or 1");
+    if (on != c->symmetric) {
+        c->symmetric = on;
         c->built = false;   // the next update builds afresh
     }
     return SPH_OK;

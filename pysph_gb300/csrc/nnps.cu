@@ -240,7 +240,8 @@ __global__ void k_cellsort(int64_t ncells, const int *cstart, int *perm) {
 // sorted snapshot
 // -------------------------------------------------------------------------
 __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *key, int *skey,
-                          float4 *posm, float4 *velh, float4 *st, float4 *nrm, float4 *tan) {
+                          float4 *posm, float4 *velh, float4 *st, float4 *nrm, float4 *tan,
+                          float4 *pm) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
          s += (int64_t)gridDim.x * blockDim.x) {
         int i = perm[s];
@@ -255,8 +256,9 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
         posm[s] = make_float4(xi, yi, zi, (float)cx);
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
                               (float)a.h[i]);
-        float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
-        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
+        float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i), m = (float)a.m[i];
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), m);
+        pm[s] = make_float4(xi, yi, zi, m);
         if (nrm) {
             nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
             tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
@@ -279,7 +281,8 @@ __global__ void k_invperm(int64_t n, const int *perm, int *inv) {
 
 __global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
                         const int *key, const float4 *posm0, float4 *posm, float4 *velh,
-                        float4 *st, float4 *nrm, float4 *tan, int *refcell, int check_jump,
+                        float4 *st, float4 *nrm, float4 *tan, float4 *pm, int *refcell,
+                        int check_jump,
                         double build_h, unsigned *dmax, unsigned *err) {
     float dm = 0.f;
     bool jump = false, hch = false;
@@ -300,8 +303,9 @@ __global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *
         const double h = a.h[i];
         if (h != build_h) hch = true;
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), (float)h);
-        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
-        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
+        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i), m = (float)a.m[i];
+        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), m);
+        pm[s] = make_float4(xi, yi, zi, m);
         if (nrm) {
             nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
             tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
@@ -362,7 +366,14 @@ __global__ void k_nbr(sph_array_view d, sph_array_view s, Grid g, const int *dke
                 int rs = scstart[rowbase + cx - g.kx], re = scstart[rowbase + cx + g.kx + 1];
                 for (int t = rs; t < re; ++t) {
                     int j = sperm[t];
-                    if (exact_within(ld0(s.x, j), ld0(s.y, j), ld0(s.z, j), px, py, pz, r2)) {
+                    bool hit = exact_within(ld0(s.x, j), ld0(s.y, j), ld0(s.z, j), px, py, pz, r2);
+                    if (!hit && g.symmetric) {
+                        // VarHNbrParticleLocator: i within the radius of j
+                        const double rj = __dmul_rn(s.h[j], radius_scale);
+                        hit = exact_within(px, py, pz, ld0(s.x, j), ld0(s.y, j), ld0(s.z, j),
+                                           __dmul_rn(rj, rj));
+                    }
+                    if (hit) {
                         if (FILL) index[base + cnt] = j;
                         ++cnt;
                     }
@@ -407,14 +418,16 @@ int ensure(T **p, int64_t &cap, int64_t need) {
 int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
     if (n <= A.cap && A.perm && (!nrm || A.nrm)) return SPH_OK;
     cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
-    cudaFree(A.posm); cudaFree(A.velh); cudaFree(A.st); cudaFree(A.nrm); cudaFree(A.tan);
+    cudaFree(A.posm); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st); cudaFree(A.nrm);
+    cudaFree(A.tan);
     A.key = A.perm = A.skey = nullptr;
-    A.posm = A.velh = A.st = A.nrm = A.tan = nullptr;
+    A.posm = A.pm = A.velh = A.st = A.nrm = A.tan = nullptr;
     int64_t c = std::max<int64_t>(n, 1);
     SPH_CUDA(cudaMalloc(&A.key, sizeof(int) * c));
     SPH_CUDA(cudaMalloc(&A.perm, sizeof(int) * c));
     SPH_CUDA(cudaMalloc(&A.skey, sizeof(int) * c));
     SPH_CUDA(cudaMalloc(&A.posm, sizeof(float4) * c));
+    SPH_CUDA(cudaMalloc(&A.pm, sizeof(float4) * c));
     SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * c));
     SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * c));
     if (nrm) {
@@ -539,6 +552,8 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     g.h_uniform = (float)hmax;
     const double skin = skin_frac * radius_scale * hmax;
     g.skin = (float)skin;
+    g.symmetric = ctx->symmetric;
+    g.reach2 = (float)((radius_scale * hmax + skin) * (radius_scale * hmax + skin) * (1.0 + 1e-4));
     // the list radius over the grid cell, (rs hmax (1 + f)) / (cell (1 + f) / subdiv),
     // is the subdivision itself when cell = rs hmax; the margin absorbs rounding
     int k = (int)std::ceil((radius_scale * hmax + skin) * inv_cs - 1e-7);
@@ -601,7 +616,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
             k_cellsort<<<grid_blocks(g.ncells, kThreads), kThreads, 0, st>>>(g.ncells, A.cstart, A.perm);
             k_reorder<<<nb, kThreads, 0, st>>>(v, g, A.perm, A.key, A.skey, A.posm, A.velh, A.st,
                                                A.has_nrm ? A.nrm : nullptr,
-                                               A.has_nrm ? A.tan : nullptr);
+                                               A.has_nrm ? A.tan : nullptr, A.pm);
             count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
             if (g.skin > 0.f) {
@@ -643,7 +658,8 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
     bool light = ctx->built && ctx->grid.skin > 0.f && narrays == (int)ctx->arrays.size() &&
                  cell_size == ctx->cell_size_ref && radius_scale == ctx->build_radius_scale &&
                  subdiv == ctx->build_subdiv && arrays != nullptr &&
-                 ctx->build_h > 0.0 && (int)ctx->lists.size() <= kMaxListSlots;
+                 ctx->build_h > 0.0 && (int)ctx->lists.size() <= kMaxListSlots &&
+                 ctx->grid.symmetric == ctx->symmetric;
     for (int a = 0; light && a < narrays; ++a) {
         const ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];
@@ -665,7 +681,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         if (v.n == 0) continue;
         k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
             v, ctx->grid, inv_cs_ref, A.inv, A.key, A.posm0, A.posm, A.velh, A.st,
-            A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.refcell, check_jump,
+            A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
             ctx->build_h, ctx->d_disp, ctx->d_err);
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
@@ -717,7 +733,7 @@ int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
     if (A.n == 0) return SPH_OK;
     k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
         A.view, ctx->grid, A.perm, A.key, A.skey, A.posm, A.velh, A.st, nrm ? A.nrm : nullptr,
-        nrm ? A.tan : nullptr);
+        nrm ? A.tan : nullptr, A.pm);
     count_launch();
     SPH_LAUNCH_CHECK("k_reorder (refresh)");
     return SPH_OK;

@@ -107,33 +107,28 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
 // With a list skin the list holds sources up to the list radius: keep the
 // neighbours (the FP32 band test, then the FP64 test of base/nnps.pyx:
 // 337-353 inside the band).
-__device__ __forceinline__ bool listed_exact_test(const SrcDev &S, const DestDev &D,
+__device__ __forceinline__ bool listed_exact_test(const Grid &g, const SrcDev &S, const DestDev &D,
                                                   const DestPos &d, int j, float rx, float ry,
                                                   float rz) {
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
     if (r2 < d.r2lo) return true;
-    if (r2 > d.r2hi) return false;
-    const int oj = S.perm[j];
-    return exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(D.x, d.orig),
-                        ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
+    bool hit = false;
+    if (r2 <= d.r2hi) {
+        const int oj = S.perm[j];
+        hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(D.x, d.orig),
+                           ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
+    }
+    if (!hit && g.symmetric) {
+        bool in_list;
+        hit = reverse_within(g, S, j, r2, D.x, D.y, D.z, d.orig, in_list);
+    }
+    return hit;
 }
 
 __device__ __forceinline__ bool listed_exact(const Grid &g, const SrcDev &S, const DestDev &D,
                                              const DestPos &d, int j, float rx, float ry, float rz) {
     if (g.skin <= 0.f) return true;
-    return listed_exact_test(S, D, d, j, rx, ry, rz);
-}
-
-// shift table: code -> -(dx, dy, dz) in cells (times the cell size of the
-// destination's grid when used)
-template <int KX>
-__device__ __forceinline__ void fill_shift_table(float4 *tab) {
-    constexpr int W = 2 * KX + 1;
-    for (int c = threadIdx.x; c < W * W * W; c += blockDim.x) {
-        const int dx = c % W - KX, dy = (c / W) % W - KX, dz = c / (W * W) - KX;
-        tab[c] = make_float4(-(float)dx, -(float)dy, -(float)dz, 0.f);
-    }
-    __syncthreads();
+    return listed_exact_test(g, S, D, d, j, rx, ry, rz);
 }
 
 // grid of the destination in slot s
@@ -142,46 +137,69 @@ __device__ __forceinline__ const Grid &grid_of(const Grid &single, const DestDev
     return BATCH ? D.grids[D.sinst[s]] : single;
 }
 
-// Stream the neighbours of dest slot s from the list in batches of B (the
-// B list entries and then the B neighbour positions are loaded before any is
-// used, so the dependent loads overlap), then -- if the list overflowed --
-// the remaining ones by re-traversal.  fn(ok, j, rx, ry, rz) is called for
-// every slot of a batch; ok is false for the padding of the last batch (its
-// data are those of a valid neighbour, its contribution must be dropped).
-// done() is called after every batch.  With a list skin, filter keeps only
-// the neighbours (ok false for the others); without it a skin entry reaches
-// fn with ok true -- right for terms that vanish beyond the radius (W and
+// No per-neighbour data beyond the position record.
+struct NoExtra {
+    __device__ __forceinline__ int operator()(int) const { return 0; }
+};
+
+// Stream the neighbours of dest slot s from the list in batches of B.  The
+// list entries of the next batch are requested before the neighbour records
+// of the current one (position offsets and mass, one 16-byte load each, plus
+// whatever extra(j) loads), and all of a batch's records are requested before
+// any is used, so the list stream and the dependent gathers overlap.  Then,
+// if the list overflowed, the remaining neighbours come from a re-traversal.
+// fn(ok, j, rx, ry, rz, mj, x) is called for every slot of a batch (x =
+// extra(j)); ok is false for the padding of the last batch (its data are
+// those of a valid neighbour, its contribution must be dropped).  done() is
+// called after every batch.  With a list skin, filter keeps only the
+// neighbours (ok false for the others); without it a skin entry reaches fn
+// with ok true -- right for terms that vanish beyond the radius (W and
 // grad W of the uniform-h cubic spline are exactly 0 for q >= 2 in FP32).
-template <int KX, int B, class Fn, class Done>
+template <int KX, int B, class Extra, class Fn, class Done>
 __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int cap, int64_t stride,
-                                           int s, const DestPos &d, const float4 *tab,
-                                           const DestDev &D, bool filter, Fn &&fn, Done &&done) {
+                                           int s, const DestPos &d, const DestDev &D, bool filter,
+                                           Extra &&extra, Fn &&fn, Done &&done) {
     filter = filter && g.skin > 0.f;
     using C = Code<KX>;
+    using X = decltype(extra(0));
     const int c = S.ncnt[s];
     const int m = min(c, cap);
     const uint32_t *lst = S.nbr + s;
-    for (int k = 0; k < m; k += B) {
-        uint32_t e[B];
+    auto entries = [&](uint32_t (&e)[B], int k) {
         e[0] = lst[(int64_t)k * stride];
 #pragma unroll
         for (int b = 1; b < B; ++b) e[b] = (k + b < m) ? lst[(int64_t)(k + b) * stride] : e[0];
-        float4 p[B], sh[B];
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            p[b] = S.posm[e[b] & C::JMASK];
-            sh[b] = tab[e[b] >> C::SHIFT];
-        }
-        const float csf = g.cs_f;
+    };
+    uint32_t e[B];
+    if (m > 0) entries(e, 0);
+    const float csf = g.cs_f;
+    for (int k = 0; k < m; k += B) {
+        uint32_t en[B];
+        const bool more = k + B < m;
+        if (more) entries(en, k + B);
+        float4 p[B];
+        X x[B];
 #pragma unroll
         for (int b = 0; b < B; ++b) {
             const int j = (int)(e[b] & C::JMASK);
-            const float rx = fmaf(sh[b].x, csf, d.xi_x - p[b].x);
-            const float ry = fmaf(sh[b].y, csf, d.xi_y - p[b].y);
-            const float rz = fmaf(sh[b].z, csf, d.xi_z - p[b].z);
-            fn(k + b < m && (!filter || listed_exact_test(S, D, d, j, rx, ry, rz)), j, rx, ry, rz);
+            p[b] = S.pm[j];
+            x[b] = extra(j);
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int j = (int)(e[b] & C::JMASK);
+            const float3 sh = neg_cell_offset<KX>(e[b]);
+            const float rx = fmaf(sh.x, csf, d.xi_x - p[b].x);
+            const float ry = fmaf(sh.y, csf, d.xi_y - p[b].y);
+            const float rz = fmaf(sh.z, csf, d.xi_z - p[b].z);
+            fn(k + b < m && (!filter || listed_exact_test(g, S, D, d, j, rx, ry, rz)), j, rx, ry, rz,
+               p[b].w, x[b]);
         }
         done();
+        if (more) {
+#pragma unroll
+            for (int b = 0; b < B; ++b) e[b] = en[b];
+        }
     }
     if (c > cap) {
         // the list entries past cap, in the order of the list build
@@ -193,7 +211,7 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
                                    return;
                                }
                                if (!exact) return;
-                               fn(true, j, rx, ry, rz);
+                               fn(true, j, rx, ry, rz, S.pm[j].w, extra(j));
                                done();
                            });
     }
@@ -230,9 +248,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
 template <int KX, bool UH, bool BATCH>
-__global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ DensityArgs A) {
-    __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
-    fill_shift_table<KX>(tab);
+__global__ void __launch_bounds__(kPairBlock, (UH && !BATCH) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
     const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
@@ -265,7 +281,7 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                         if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                         ++c;
                         if (!exact) return;
-                        const float mj = S.st[j].w;
+                        const float mj = S.pm[j].w;
                         float ih = ihi, fac = faci;
                         if (!uh) {
                             ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
@@ -282,9 +298,8 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
                 continue;
             }
             // with variable h, W at the mean h can reach past the radius of h_i
-            for_listed<KX, 4>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d, !uh,
-                [&](bool ok, int j, float rx, float ry, float rz) {
-                    const float mj = S.st[j].w;
+            for_listed<KX, (UH && !BATCH) ? 6 : 4>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, !uh, NoExtra(),
+                [&](bool ok, int j, float rx, float ry, float rz, float mj, int) {
                     float ih = ihi, fac = faci;
                     if (!uh) {
                         ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
@@ -335,6 +350,11 @@ __global__ void __launch_bounds__(kPairBlock) k_density(const __grid_constant__ 
 // 41-124), XSPH (xsph_funcs.pyx:31-88), Monaghan BF (boundary_funcs.pyx:
 // 54-110), gravity (external_force.pyx:39-45), stepping (position_funcs.pyx)
 // ---------------------------------------------------------------------------
+// velocity (+h) and state records of one neighbour
+struct VelState {
+    float4 v, st;
+};
+
 // SPEC 0: any terms, runtime flags; 1: PGrad + AV, uniform h, one source;
 // 2: PGrad + AV + XSPH, uniform h, one source.
 template <int KX, int SPEC, bool BATCH>
@@ -344,8 +364,6 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     constexpr bool MAY_XSPH = SPEC != 1;
     constexpr bool MAY_BF = SPEC == 0;
     constexpr bool MAY_DRHO = SPEC == 0;
-    __shared__ float4 tab[(2 * KX + 1) * (2 * KX + 1) * (2 * KX + 1)];
-    fill_shift_table<KX>(tab);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
     const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
@@ -367,12 +385,12 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
             const uint32_t fl = SPEC != 0 ? SF : S.flags;
             // the boundary force has its own support (normal distance, delp)
             const bool filt = !uh || (fl & SPH_TERM_BFORCE) != 0;
-            for_listed<KX, (SPEC != 0 ? 4 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, tab, A.d, filt,
-                [&](bool ok, int j, float rx, float ry, float rz) {
+            for_listed<KX, (SPEC != 0 ? 3 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, filt,
+                [&](int j) { return VelState{S.velh[j], S.st[j]}; },
+                [&](bool ok, int j, float rx, float ry, float rz, float mj, const VelState &vs) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                const float4 vj = S.velh[j];
-                const float4 stj = S.st[j];
-                const float mj = stj.w;
+                const float4 vj = vs.v;
+                const float4 stj = vs.st;
                 float hab = hi, ih = ihi, fac = faci;
                 if (!uh) {
                     hab = 0.5f * (hi + vj.w);
@@ -526,14 +544,11 @@ __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__
             for (int k = 0; k < m; ++k) {
                 const uint32_t e = S.nbr[s + (int64_t)k * A.stride];
                 const int j = (int)(e & C::JMASK);
-                const int code = (int)(e >> C::SHIFT);
-                constexpr int W = 2 * KX + 1;
-                const float dx = (float)(code % W - KX), dy = (float)((code / W) % W - KX),
-                            dz = (float)(code / (W * W) - KX);
-                const float4 p = S.posm[j];
-                const float rx = fmaf(-dx, csf, d.xi_x - p.x);
-                const float ry = fmaf(-dy, csf, d.xi_y - p.y);
-                const float rz = fmaf(-dz, csf, d.xi_z - p.z);
+                const float3 sh = neg_cell_offset<KX>(e);
+                const float4 p = S.pm[j];
+                const float rx = fmaf(sh.x, csf, d.xi_x - p.x);
+                const float ry = fmaf(sh.y, csf, d.xi_y - p.y);
+                const float rz = fmaf(sh.z, csf, d.xi_z - p.z);
                 if (listed_exact(A.g, S, A.d, d, j, rx, ry, rz)) keep(j, rx, ry, rz);
             }
             if (c > A.cap) {
@@ -611,9 +626,9 @@ DestDev make_dest(const ArraySnap &D) {
 
 SrcDev make_src(const ArraySnap &S) {
     SrcDev s{};
-    s.posm = S.posm; s.velh = S.velh; s.st = S.st; s.nrm = S.nrm; s.tan = S.tan;
+    s.posm = S.posm; s.velh = S.velh; s.st = S.st; s.nrm = S.nrm; s.tan = S.tan; s.pm = S.pm;
     s.cstart = S.cstart; s.perm = S.perm;
-    s.x = S.view.x; s.y = S.view.y; s.z = S.view.z;
+    s.x = S.view.x; s.y = S.view.y; s.z = S.view.z; s.h = S.view.h;
     return s;
 }
 

@@ -6,6 +6,8 @@
 //     perm[s]  -> original index of sorted slot s          int32
 //     skey[s]  -> dense-grid cell of slot s                int32
 //     posm[s]  =  (xi_x, xi_y, xi_z, cx)  cell-local FP32 offsets, dense x cell
+//     pm[s]    =  (xi_x, xi_y, xi_z, m)   the same offsets with the mass: the
+//                 one 16-byte record per neighbour of the list-streaming passes
 //     velh[s]  =  (u, v, w, h)                              FP32
 //     st[s]    =  (rho, p/rho^2, cs, m)                     FP32
 //     nrm[s], tan[s] (walls only)
@@ -43,6 +45,11 @@ struct Grid {
     // radius_scale h + skin of the destination at the build, the passes that
     // stream a list keep the exact neighbours; 0 = lists are exact
     float skin = 0.f;
+    // variable h (VarHNbrParticleLocator): j is also a neighbour of i when
+    // i lies within the radius of j; reach2 is the squared largest list
+    // radius (radius_scale max h + skin, with a margin), the pruning radius
+    int symmetric = 0;
+    float reach2 = 0.f;
 };
 
 struct ArraySnap {
@@ -54,6 +61,7 @@ struct ArraySnap {
     int *perm = nullptr;  // sorted -> original
     int *skey = nullptr;  // sorted: cell
     float4 *posm = nullptr, *velh = nullptr, *st = nullptr, *nrm = nullptr, *tan = nullptr;
+    float4 *pm = nullptr;
     int *cstart = nullptr; // ncells + 1
     int *cursor = nullptr; // ncells
     int64_t cell_cap = 0;
@@ -108,6 +116,7 @@ struct sph_ctx {
     double build_radius_scale = 0.0;    // parameters of the last full build
     double build_h = 0.0;               // the uniform h of the last full build (0: not uniform)
     int build_subdiv = 0;
+    int symmetric = 0;                  // variable-h neighbour relation (next build)
     unsigned *d_disp = nullptr;         // max squared displacement (float bits)
     long long n_full = 0, n_light = 0;  // full builds / light refreshes
 };
@@ -277,26 +286,68 @@ __device__ __forceinline__ bool exact_within(double sx, double sy, double sz, do
 __device__ __forceinline__ double ld0(const double *p, int64_t i) { return p ? p[i] : 0.0; }
 
 // Per-source view used by the pair kernels.
+
 struct SrcDev {
-    const float4 *posm, *velh, *st, *nrm, *tan;
+    const float4 *posm, *velh, *st, *nrm, *tan, *pm;
     const int *cstart, *perm;
-    const double *x, *y, *z;
+    const double *x, *y, *z, *h;
     const uint32_t *nbr;   // k-major neighbour list of (dest, this source)
     const int *ncnt;       // neighbour count per dest slot
     uint32_t flags;
     float alpha, beta, eta2, eps, delp;
 };
 
-// Neighbour-list entry: source slot j in the low bits, stencil offset code
-// (dx+K) + (2K+1)((dy+K) + (2K+1)(dz+K)) in the high CODE_BITS bits.
+// Neighbour-list entry: source slot j in the low bits, the stencil offset
+// of the source's cell in the high BITS bits as three fields of FB bits,
+// (dx+K) | (dy+K) << FB | (dz+K) << 2 FB, so the passes that stream a list
+// decode the offset with shifts and masks (no table lookup).
 template <int K>
 struct Code {
     static constexpr int W = 2 * K + 1;
-    static constexpr int N = W * W * W;
-    static constexpr int BITS = (N <= 32) ? 5 : (N <= 128 ? 7 : 9);
+    static constexpr int FB = K == 1 ? 2 : 3;
+    static constexpr int BITS = 3 * FB;
     static constexpr int SHIFT = 32 - BITS;
     static constexpr uint32_t JMASK = (1u << SHIFT) - 1u;
+    static constexpr uint32_t FMASK = (1u << FB) - 1u;
+    // code of a row (dy, dz) with dx = 0; adding dx gives the full code
+    __host__ __device__ static constexpr int row(int dy, int dz) {
+        return K | ((dy + K) << FB) | ((dz + K) << (2 * FB));
+    }
 };
+
+// Minus the cell offset (dx, dy, dz) of list entry e, as exact floats: a
+// field v becomes 2^23 + v by OR-ing it into the bits of 2^23, and
+// (2^23 + K) - (2^23 + v) = -(v - K).
+template <int K>
+__device__ __forceinline__ float3 neg_cell_offset(uint32_t e) {
+    using C = Code<K>;
+    const uint32_t c = e >> C::SHIFT;
+    constexpr float base = 8388608.f + (float)K;
+    return make_float3(base - __uint_as_float((c & C::FMASK) | 0x4B000000u),
+                       base - __uint_as_float(((c >> C::FB) & C::FMASK) | 0x4B000000u),
+                       base - __uint_as_float(((c >> (2 * C::FB)) & C::FMASK) | 0x4B000000u));
+}
+
+// The reverse test of the variable-h relation: destination (original index
+// oi, FP64 position dx64..) lies within the radius of source slot j, i.e.
+// |x_i - x_j|^2 < (radius_scale h_j)^2.  FP32 outside a +-1e-5 relative band
+// around the threshold, the FP64 test of base/nnps.pyx:337-353 inside it.
+// in_list: within the list radius of j (radius_scale h_j + skin).
+template <class Src>
+__device__ __forceinline__ bool reverse_within(const Grid &g, const Src &S, int j, float r2,
+                                               const double *dx64, const double *dy64,
+                                               const double *dz64, int oi, bool &in_list) {
+    const float rj = (float)g.radius_scale * S.velh[j].w;
+    const float rj2 = rj * rj;
+    const float rl = rj + g.skin;
+    in_list = g.skin > 0.f && r2 < rl * rl * (1.f + 2e-5f);
+    if (r2 < rj2 * (1.f - 1e-5f)) return true;
+    if (r2 > rj2 * (1.f + 1e-5f)) return false;
+    const int oj = S.perm[j];
+    const double radius = __dmul_rn(S.h[oj], g.radius_scale);
+    return exact_within(ld0(dx64, oi), ld0(dy64, oi), ld0(dz64, oi), ld0(S.x, oj), ld0(S.y, oj),
+                        ld0(S.z, oj), __dmul_rn(radius, radius));
+}
 
 // Destination state of one thread (cell-local FP32 offsets, dense cell).
 struct DestPos {
@@ -329,7 +380,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
     const float inv_cs = 1.f / csf;
     // pruning radius: the accept/recheck threshold plus a relative margin
     // that covers FP32 rounding of the slab distances and cell assignment
-    const float R2 = fmaxf(d.r2hi, d.r2list) * 1.0002f;
+    const float R2 = fmaxf(fmaxf(d.r2hi, d.r2list), g.symmetric ? g.reach2 : 0.f) * 1.0002f;
     const float cxf = (float)d.cx;
     const int rowstride_z = g.nx * g.ny;  // < 2^27 cells: 32-bit indices
     const int *cst = S.cstart + g.cell_base;
@@ -353,7 +404,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             const int lo = __ldg(cst + c0 + tlo);
             const int hi = __ldg(cst + c0 + thi + 1);
             const float by = d.xi_y - (float)dy * csf;
-            const int code_yz = KX + (2 * KX + 1) * ((dy + KX) + (2 * KX + 1) * (dz + KX));
+            const int code_yz = Code<KX>::row(dy, dz);
             for (int j = lo; j < hi; ++j) {
                 const float4 pj = __ldg(S.posm + j);
                 const float dxc = pj.w - cxf;  // exact: small integers in FP32
@@ -366,7 +417,13 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
                     hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(dx64, d.orig),
                                        ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
                 }
-                if (hit || r2 < d.r2list) fn(j, rx, ry, rz, code_yz + (int)dxc, hit);
+                bool listed = hit || r2 < d.r2list;
+                if (g.symmetric && !hit && r2 <= g.reach2) {
+                    bool in_list;
+                    hit = reverse_within(g, S, j, r2, dx64, dy64, dz64, d.orig, in_list);
+                    listed = listed || hit || in_list;
+                }
+                if (listed) fn(j, rx, ry, rz, code_yz + (int)dxc, hit);
             }
         }
     }

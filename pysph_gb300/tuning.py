@@ -30,9 +30,10 @@ def list_skin():
 
 # measured defaults: (dimensions with extent) -> subdivision
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
-# neighbour-list entries hold the source slot in 32 - code bits: at
-# subdivision 3 (343 stencil codes, 9 bits) at most 2^23 source particles
-MAX_PARTICLES = {1: 1 << 27, 2: 1 << 25, 3: 1 << 23}
+# neighbour-list entries hold the source slot in 32 - code bits (three
+# fields of 2 bits at subdivision 1, of 3 bits at 2 and 3): at most 2^26
+# source particles at subdivision 1, 2^23 at 2 and 3
+MAX_PARTICLES = {1: 1 << 26, 2: 1 << 23, 3: 1 << 23}
 
 
 def choose_subdivision(cell_manager):

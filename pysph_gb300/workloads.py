@@ -48,6 +48,15 @@ def elliptical_drop(dx=0.025, hdx=1.3, rho0=1.0, c0=1400.0, radius=1.0):
     )
 
 
+def jitter_h(props, frac=0.25, seed=0):
+    """Copy of ``props`` with every h scaled by 1 + U(-frac, frac) (seeded):
+    smoothing lengths that differ from particle to particle."""
+    rng = np.random.default_rng(seed)
+    out = dict(props)
+    out["h"] = props["h"] * (1.0 + rng.uniform(-frac, frac, size=props["h"].shape))
+    return out
+
+
 def circular_patch(dx=0.025, c0=100.0):
     """The reference FluidSolver's circular patch (solver/fluid_solver.py:15-49):
     the square lattice of ``elliptical_drop`` with ``m = dx^2``, ``h = 2 dx``,
@@ -176,13 +185,14 @@ def _integrator(api, name):
 
 
 def setup_drop(api, props, c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5,
-               integrator="euler", name="fluid"):
+               integrator="euler", name="fluid", variable_h=False):
     """Elliptical drop operations: SPHRho, Tait, PGrad, Monaghan AV,
-    position stepping and XSPH, in that order (2D)."""
+    position stepping and XSPH, in that order (2D).  ``variable_h`` makes
+    the neighbour relation symmetric (``Particles(variable_h=True)``)."""
     base, sph, solver = api.base, api.sph, api.solver
     Fluid = base.ParticleType.Fluid
     pa = base.get_particle_array(name=name, type=Fluid, **props)
-    particles = base.Particles(arrays=[pa])
+    particles = base.Particles(arrays=[pa], variable_h=variable_h)
     s = solver.Solver(dim=2, integrator_type=_integrator(api, integrator))
     s.add_operation(solver.SPHOperation(
         sph.SPHRho.withargs(), on_types=[Fluid], from_types=[Fluid],

@@ -245,6 +245,17 @@ def fixture_fluid_integrator(integrator, dx=0.05, steps=3):
     return out
 
 
+def fixture_drop_varh(dx=0.05):
+    """The elliptical drop with per-particle h (U(-25 %, 25 %) about 1.3 dx)
+    and Particles(variable_h=True): symmetric neighbour lists
+    (VarHNbrParticleLocator) and one Euler step."""
+    props = W.jitter_h(W.elliptical_drop(dx=dx))
+    s, particles = W.setup_drop(REF, props, variable_h=True)
+    out = {}
+    run_step(s, particles, 1e-5, out, nbr_pairs=[(0, 0)])
+    return out
+
+
 def main():
     fixtures = {
         "kernel": fixture_kernel,
@@ -260,6 +271,7 @@ def main():
         "fluid_rk4": lambda: fixture_fluid_integrator("rk4"),
         "fluid_pc": lambda: fixture_fluid_integrator("pc"),
         "cube_leapfrog": lambda: fixture_cube(1000, "leapfrog"),
+        "drop_varh": fixture_drop_varh,
     }
     only = sys.argv[1:]
     if only:

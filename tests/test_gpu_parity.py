@@ -409,3 +409,37 @@ def test_leapfrog_2d_drop_raises_index_error():
     with pytest.raises(IndexError):
         s.integrator.integrate(1e-5)
     np.testing.assert_array_equal(particles.arrays[0].get("x"), x0)
+
+
+# -- variable h: Particles(variable_h=True), VarHNbrParticleLocator ------------
+
+def test_variable_h_neighbour_sets_bit_exact():
+    """The symmetric union (base/nnps.pyx:654-749) as index sets, from the
+    exported lists of the device build."""
+    _need_gpu()
+    g = load("drop_varh")
+    pa = base.get_particle_array(name="fluid", type=base.ParticleType.Fluid,
+                                 **inputs(g, "fluid"))
+    particles = base.Particles(arrays=[pa], variable_h=True)
+    off, idx = _locator_sets(particles, pa, pa)
+    ro, ri = g["nbr_fluid_fluid_offsets"], g["nbr_fluid_fluid_index"]
+    assert csr_sets(off, idx) == csr_sets(ro, ri)
+    loc = particles.nnps_manager.get_neighbor_particle_locator(pa, pa, 2.0)
+    assert type(loc).__name__ == "VarHNbrParticleLocator"
+    # fixed-h lists of the same particles are a strict subset
+    pb = base.get_particle_array(name="fluid", type=base.ParticleType.Fluid,
+                                 **inputs(g, "fluid"))
+    o2, i2 = _locator_sets(base.Particles(arrays=[pb]), pb, pb)
+    assert o2[-1] < off[-1]
+
+
+@pytest.mark.parametrize("skin", ["0", "0.03"])
+def test_variable_h_euler_step(skin, monkeypatch):
+    """One Euler step of the drop with per-particle h over the symmetric
+    neighbour relation (pair sums at the mean h of each pair)."""
+    _need_gpu()
+    monkeypatch.setenv("PYSPH_GB300_SKIN", skin)
+    g = load("drop_varh")
+    s, particles = W.setup_drop(API, inputs(g, "fluid"), variable_h=True)
+    s.integrator.integrate(float(g["dt"]))
+    _check_step(g, particles.arrays, 1, DROP_K)

@@ -153,3 +153,12 @@ def test_leapfrog_2d_index_error_before_any_work():
     s, _ = W.setup_drop(API, W.elliptical_drop(dx=0.1), integrator="leapfrog")
     with pytest.raises(IndexError):
         s.integrator.integrate(1e-5)
+
+
+def test_variable_h_switches_the_cell_manager_to_the_symmetric_relation():
+    props = W.jitter_h(W.elliptical_drop(dx=0.1))
+    pa = base.get_particle_array(name="fluid", **props)
+    particles = base.Particles(arrays=[pa], variable_h=True, update_particles=False)
+    assert particles.cell_manager.symmetric
+    pb = base.get_particle_array(name="fluid", **props)
+    assert not base.Particles(arrays=[pb], update_particles=False).cell_manager.symmetric

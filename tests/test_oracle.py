@@ -222,3 +222,25 @@ def test_leapfrog_2d_position_correction_index_error():
     prob = oracle.Problem({"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2)
     with pytest.raises(IndexError):
         prob.integrate_leapfrog(1e-5)
+
+
+def test_variable_h_neighbour_sets_match_reference():
+    """Particles(variable_h=True): the symmetric union of VarHNbrParticleLocator
+    (base/nnps.pyx:654-749), a strict superset of the fixed-h sets here."""
+    g = load("drop_varh")
+    p = inputs(g, "fluid")
+    off, idx = oracle.neighbors(p, p, 2 * p["h"].max(), 2.0, same=True, variable_h=True)
+    ref = csr_sets(g["nbr_fluid_fluid_offsets"], g["nbr_fluid_fluid_index"])
+    assert csr_sets(off, idx) == ref
+    o2, i2 = oracle.neighbors(p, p, 2 * p["h"].max(), 2.0, same=True)
+    assert o2[-1] < off[-1]
+    # symmetric: j in N(i) <=> i in N(j)
+    pairs = {(i, j) for i, s in enumerate(ref) for j in s}
+    assert all((j, i) in pairs for (i, j) in pairs)
+
+
+def test_variable_h_euler_step_matches_reference():
+    g = load("drop_varh")
+    prob = oracle.Problem({"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2, variable_h=True)
+    prob.integrate_euler(float(g["dt"]))
+    _cmp_step(g, prob, ["fluid"], 1e-13)
