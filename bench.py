@@ -52,9 +52,9 @@ STEP_ALG_BYTES = 694.0
 PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md);
-# the traffic grows with the particle count, so it is scaled by n
-NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 383.0, "RatesStage": 404.0}
+# of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md,
+# list-streaming passes); the traffic grows with the particle count, so it is scaled by n
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 420.0, "RatesStage": 451.0}
 
 
 def measured_peaks():
@@ -75,25 +75,38 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=50):
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines = []
+        self.window = None
 
-    def start(self):
+    def start(self, wait_s=5.0):
+        """Start sampling and wait (up to wait_s) for the first sample."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.monotonic()
+        while not self.lines and time.monotonic() - t0 < wait_s and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark(self, begin, end):
+        """The timed region (time.monotonic() values): samples inside it are
+        the ones reported (the nearest one when the region is shorter than
+        the sampling interval)."""
+        self.window = (begin, end)
 
     def stop(self):
         if self.proc is None:
@@ -106,7 +119,14 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, smax, reasons = [], None, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        lines = self.lines
+        if self.window is not None and lines:
+            b, e = self.window
+            inside = [x for x in lines if b <= x[0] <= e]
+            if not inside:
+                inside = [min(lines, key=lambda x: abs(x[0] - 0.5 * (b + e)))]
+            lines = inside
+        for _, ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -118,8 +138,12 @@ class ClockSampler:
             for nm, v in zip(names, f[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+               "reasons": sorted(reasons), "samples": len(sm),
+               "interval_ms": self.interval_ms}
+        if self.window is not None:
+            out["timed_s"] = round(self.window[1] - self.window[0], 3)
+        return out
 
 
 # ---------------------------------------------------------------------------
@@ -264,6 +288,7 @@ def run_gpu(args):
     launches0 = native.launch_count()
     integ.stage_events = []
     step_ms = []
+    t_begin = time.monotonic()
     for _ in range(args.steps):
         flush.fill_(1.0)
         a = torch.cuda.Event(enable_timing=True)
@@ -277,6 +302,7 @@ def run_gpu(args):
     if pg:
         pg.barrier()
     launches = native.launch_count() - launches0
+    clocks.mark(t_begin, time.monotonic())
     clk = clocks.stop()
     builds = cm.build_stats()
     events = integ.stage_events
@@ -350,7 +376,8 @@ def run_gpu(args):
                      "traffic_source": "ncu capture at 1M particles, scaled by n",
                      "peak_kind": peak_kind,
                      "alg_bytes_per_particle": ALG_BYTES[dom],
-                     "note": "pair kernels issue-bound; fp32 context in fp32_context"},
+                     "note": "pair kernels bound by issue (density) and the L1 data pipe "
+                             "(rates gathers), not HBM; fp32 context in fp32_context"},
         "fp32_context": {"kernel": dom, "achieved_tflops": flops,
                          "nominal_peak_tflops": FP32_NOMINAL_TFLOPS,
                          "frac_of_nominal": flops / FP32_NOMINAL_TFLOPS},
@@ -464,6 +491,7 @@ def run_gpu_drops(args):
     torch.cuda.synchronize()
     launches0 = native.launch_count()
     step_ms = []
+    t_begin = time.monotonic()
     for _ in range(args.steps):
         with torch.cuda.stream(st):
             flush.fill_(1.0)
@@ -477,6 +505,7 @@ def run_gpu_drops(args):
     batch.check()
     torch.cuda.synchronize()
     launches = native.launch_count() - launches0
+    clocks.mark(t_begin, time.monotonic())
     clk = clocks.stop()
     t_total = sum(step_ms) / 1e3
     steps = args.steps
@@ -792,7 +821,9 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # default: 300 timed GPU steps of the 1M-particle lattice (about half a
+    # second, long enough for several clock samples), 20 elsewhere
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
@@ -813,6 +844,8 @@ def main():
     ap.add_argument("--drop-c0", type=float, default=100.0)
     ap.add_argument("--drop-sample", type=int, default=8)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 300 if (args.workload == "cube" and args.impl == "gb300") else 20
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.workload == "drops":
