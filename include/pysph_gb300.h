@@ -160,6 +160,18 @@ int sph_ctx_set_skin(sph_ctx *ctx, double skin_fraction);
  * (each test exactly as the reference's FP64 one).  Takes effect at the
  * next build. */
 int sph_ctx_set_symmetric(sph_ctx *ctx, int on);
+
+/* Periodic x axis (base/cell.pyx:1277-1376 CellManager.create_ghost_cells,
+ * cell.pyx:392-398 binning of the PeriodicDomain, which the reference
+ * applies along x only): with on = 1, every neighbour search treats x as
+ * periodic on [xmin, xmax).  Instead of appending ghost copies of the cells
+ * near either end to the particle arrays, a particle is binned at its image
+ * in the period and a stencil row that leaves the period continues at the
+ * other end, where the sources are the images shifted by -+(xmax - xmin)
+ * (added in FP64 exactly as the reference shifts its ghost copies); the
+ * images carry the state of the particle they copy.  The period must span
+ * at least 2K+1 grid cells.  Takes effect at the next build. */
+int sph_ctx_set_periodic(sph_ctx *ctx, int on, double xmin, double xmax);
 /* Particles.update() (base/particles.py:159-200 -> cell.pyx:927-1015):
  * with a skin and the same arrays, refresh the sorted snapshot in the
  * order of the last full build (one kernel, the reference's jump check

@@ -180,6 +180,35 @@ def tait(dst, co, ro, gamma=7.0):
     return p, cs
 
 
+def periodic_images(src, xmin, xmax, reach):
+    """Ghost copies for a domain periodic in x (base/cell.pyx:1277-1376): the
+    particles within ``reach`` of either end, copied with x shifted by
+    +-(xmax - xmin) (FP64 adds, as the reference shifts its ghosts) and the
+    rest of their state unchanged.  Returns (extended property dict, origin
+    index of every ghost).  The reference copies whole cells of size 2 max h
+    whose faces lie within reach; the extra copies lie beyond every search
+    radius, so the neighbour sets are the same.  Particles that have left
+    the period (x is never wrapped) widen the reach by their overshoot, so
+    every particle sees the nearest image of every other (the reference's
+    binning wraps such particles once and misses images beyond its cells)."""
+    L = xmax - xmin
+    x = np.asarray(src["x"], np.float64)
+    if x.size:
+        reach = reach + max(0.0, float(x.max()) - xmax, xmin - float(x.min()))
+    lo = np.nonzero(x - xmin < reach)[0]
+    hi = np.nonzero(xmax - x < reach)[0]
+    origin = np.concatenate([lo, hi]).astype(np.int64)
+    shift = np.concatenate([np.full(lo.size, L), np.full(hi.size, -L)])
+    ext = {}
+    for k, v in src.items():
+        v = np.asarray(v)
+        ext[k] = np.concatenate([v, v[origin]])
+    ext["x"] = np.concatenate([x, x[origin] + shift])
+    if "tag" in ext:
+        ext["tag"][len(x):] = 0
+    return ext, origin
+
+
 # ---------------------------------------------------------------------------
 # Problem: a set of particle arrays plus an ordered list of operations,
 # stepped exactly like solver/integrator.py steps its calcs.
@@ -206,7 +235,7 @@ class Op:
 
 
 class Problem:
-    def __init__(self, arrays, ops, dim, radius_scale=2.0, variable_h=False):
+    def __init__(self, arrays, ops, dim, radius_scale=2.0, variable_h=False, periodic=None):
         # arrays: dict name -> dict of float64 property arrays (copied)
         self.arrays = {}
         for name, props in arrays.items():
@@ -223,18 +252,30 @@ class Problem:
         self.dim = dim
         self.radius_scale = radius_scale
         self.variable_h = variable_h
+        # (xmin, xmax) of a domain periodic in x, or None
+        self.periodic = periodic
         max_h = max(float(a["h"].max()) for a in self.arrays.values() if a["h"].size)
         # CellManager.compute_cell_size: base/cell.pyx:893-925
         self.cell_size = radius_scale * max_h
         self.k = {}
         self.nbr_cache = {}
 
+    def _source(self, src):
+        """The source arrays a pair pass sees: with a periodic domain, the
+        particles plus their ghost images (state as it is now)."""
+        a = self.arrays[src]
+        if self.periodic is None:
+            return a, None
+        reach = self.radius_scale * max(float(b["h"].max()) for b in self.arrays.values())
+        return periodic_images(a, self.periodic[0], self.periodic[1], reach * (1 + 1e-12))
+
     def neighbours(self, dest, src):
         key = (dest, src)
         if key not in self.nbr_cache:
-            self.nbr_cache[key] = neighbors(self.arrays[dest], self.arrays[src],
-                                            self.cell_size, self.radius_scale,
-                                            same=(dest == src), variable_h=self.variable_h)
+            ext, _ = self._source(src)
+            self.nbr_cache[key] = neighbors(self.arrays[dest], ext, self.cell_size,
+                                            self.radius_scale, same=(dest == src),
+                                            variable_h=self.variable_h)
         return self.nbr_cache[key]
 
     def _moved(self):
@@ -262,7 +303,7 @@ class Problem:
             return tmp[:nout]
         for s in op.sources:
             off, idx = self.neighbours(op.dest, s)
-            res = pair_sum(op.kind, d, self.arrays[s], off, idx, self.dim, op.params, nout)
+            res = pair_sum(op.kind, d, self._source(s)[0], off, idx, self.dim, op.params, nout)
             for o, r in zip(outs, res):
                 o += r
         return outs

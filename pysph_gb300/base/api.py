@@ -1,6 +1,6 @@
 """Names of ``pysph.base.api`` (the reference's base package)."""
 from .carray import DoubleArray, FloatArray, IntArray, LongArray  # noqa: F401
-from .cell import CellManager  # noqa: F401
+from .cell import CellManager, PeriodicDomain  # noqa: F401
 from .kernels import (CubicSplineKernel, DummyKernel, GaussianKernel,  # noqa: F401
                       HarmonicKernel, KernelBase, M6SplineKernel, Poly6Kernel,
                       QuinticSplineKernel, W8Kernel, W10Kernel,

@@ -37,13 +37,32 @@ def array_view(pa):
     return v
 
 
+class PeriodicDomain:
+    """base/cell.pyx:1568-1598: limits of a periodic box.  An axis whose
+    limits span exactly 2000 (the default -1000 .. 1000) is not periodic
+    (translate 0); the others translate by max - min."""
+
+    def __init__(self, xmin=-1000.0, xmax=1000.0, ymin=-1000.0, ymax=1000.0, zmin=-1000.0,
+                 zmax=1000.0):
+        self.xmin, self.xmax = xmin, xmax
+        self.ymin, self.ymax = ymin, ymax
+        self.zmin, self.zmax = zmin, zmax
+        self.xtranslate = 0.0 if (xmax - xmin) == 2000 else xmax - xmin
+        self.ytranslate = 0.0 if (ymax - ymin) == 2000 else ymax - ymin
+        self.ztranslate = 0.0 if (zmax - zmin) == 2000 else zmax - zmin
+
+
 class CellManager:
     """Dense-grid cell structure over ``arrays_to_bin``."""
 
     def __init__(self, arrays_to_bin=None, min_cell_size=-1.0, max_cell_size=0,
                  periodic_domain=None, initialize=True, max_radius_scale=2.0):
-        if periodic_domain is not None:
-            raise NotImplementedError("periodic domains are not part of the GPU hot path")
+        if periodic_domain is not None and (periodic_domain.ytranslate != 0.0
+                                            or periodic_domain.ztranslate != 0.0):
+            # the reference replicates ghost cells along x only
+            # (cell.pyx:1308-1352); y and z periodicity have no reference
+            raise NotImplementedError("periodic domains are periodic along x only "
+                                      "(as the reference's ghost cells)")
         self.max_radius_scale = max_radius_scale
         self.min_cell_size = min_cell_size
         self.max_cell_size = max_cell_size
@@ -56,7 +75,7 @@ class CellManager:
         # particle state was replaced rather than advanced
         self.skip_jump_once = False
         self.cell_size = 0.0
-        self.periodic_domain = None
+        self.periodic_domain = periodic_domain
         self.is_dirty = True
         self.initialized = False
         # internal grid cells per reference cell (1..3); see the autotuner
@@ -132,6 +151,10 @@ class CellManager:
             native.check(L.sph_ctx_set_skin(h, list_skin()), "sph_ctx_set_skin")
             native.check(L.sph_ctx_set_symmetric(h, 1 if self.symmetric else 0),
                          "sph_ctx_set_symmetric")
+            dom = self.periodic_domain
+            if dom is not None and dom.xtranslate != 0.0:
+                native.check(L.sph_ctx_set_periodic(h, 1, float(dom.xmin), float(dom.xmax)),
+                             "sph_ctx_set_periodic")
             self._ctx = h
         native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
             torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
@@ -171,7 +194,8 @@ class CellManager:
         ctx = self.context()
         views = (native.ArrayView * len(self.arrays_to_bin))(
             *[array_view(pa) for pa in self.arrays_to_bin])
-        check = 0 if self.skip_jump_once else 1
+        # no jump check with a periodic domain (cell.pyx:404-407)
+        check = 0 if (self.skip_jump_once or self.periodic_domain is not None) else 1
         rebuilt = ctypes.c_int(1)
         rc = native.lib().sph_nnps_update(ctx, views, len(self.arrays_to_bin), self.cell_size,
                                           self.max_radius_scale, self._subdivision(), check,
@@ -196,7 +220,7 @@ class CellManager:
             *[array_view(pa) for pa in self.arrays_to_bin])
         rc = native.lib().sph_nnps_build(ctx, views, len(self.arrays_to_bin), self.cell_size,
                                          self.max_radius_scale, self._subdivision(),
-                                         1 if check_jump else 0)
+                                         1 if (check_jump and self.periodic_domain is None) else 0)
         native.check(rc, "CellManager.rebuild")
         self._views = views
         self._snap_versions = [pa.version for pa in self.arrays_to_bin]

@@ -148,6 +148,20 @@ int sph_ctx_set_symmetric(sph_ctx *c, int on) {
     return SPH_OK;
 }
 
+int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
+    CHECK_CTX(c);
+    if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_periodic: on must be 0 or 1");
+    if (on && !(xmax > xmin))
+        return set_error(SPH_ERR_ARG, "sph_ctx_set_periodic: xmax must exceed xmin");
+    if (on != c->periodic || (on && (xmin != c->pxmin || xmax != c->pxmax))) {
+        c->periodic = on;
+        c->pxmin = on ? xmin : 0.0;
+        c->pxmax = on ? xmax : 0.0;
+        c->built = false;   // the next update builds afresh
+    }
+    return SPH_OK;
+}
+
 int sph_nnps_stats(sph_ctx *c, int64_t *out) {
     CHECK_CTX(c);
     if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_stats: null out");

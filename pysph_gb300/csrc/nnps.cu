@@ -37,7 +37,8 @@ __device__ __forceinline__ int floor_cell(double x, double inv_cs) {
 // bounding box / max h / jump check
 // -------------------------------------------------------------------------
 __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *refcell,
-                      int check_jump, int *box, unsigned long long *hmax, unsigned *err) {
+                      int check_jump, int *box, unsigned long long *hmax, unsigned *err,
+                      Grid pg) {
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX};
     int mx[3] = {INT_MIN, INT_MIN, INT_MIN};
     double hm = 0.0, hn = 1.0e308;
@@ -45,9 +46,10 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         double p[3] = {ld0(a.x, i), ld0(a.y, i), ld0(a.z, i)};
+        const double pb[3] = {bin_x(pg, p[0]), p[1], p[2]};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            int c = floor_cell(p[d], inv_cs);
+            int c = floor_cell(pb[d], inv_cs);
             mn[d] = min(mn[d], c);
             mx[d] = max(mx[d], c);
         }
@@ -131,7 +133,7 @@ __global__ void k_box_init(int *box, unsigned long long *hmax) {
 __global__ void k_keys(sph_array_view a, Grid g, int *key, int *count) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        int cx = floor_cell(ld0(a.x, i), g.inv_cs) - g.bx0;
+        int cx = bin_cell_x(g, bin_x(g, ld0(a.x, i)));
         int cy = floor_cell(ld0(a.y, i), g.inv_cs) - g.by0;
         int cz = floor_cell(ld0(a.z, i), g.inv_cs) - g.bz0;
         int k = cx + g.nx * (cy + g.ny * cz);
@@ -250,7 +252,7 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
         int cx, cy, cz;
         decode_cell(g, k, cx, cy, cz);
         double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
-        float xi = (float)fma(-ox, g.cs, ld0(a.x, i));
+        float xi = (float)fma(-ox, g.cs, bin_x(g, ld0(a.x, i)));
         float yi = (float)fma(-oy, g.cs, ld0(a.y, i));
         float zi = (float)fma(-oz, g.cs, ld0(a.z, i));
         posm[s] = make_float4(xi, yi, zi, (float)cx);
@@ -293,7 +295,7 @@ __global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *
         decode_cell(g, key[i], cx, cy, cz);
         const double px = ld0(a.x, i), py = ld0(a.y, i), pz = ld0(a.z, i);
         const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
-        const float xi = (float)fma(-ox, g.cs, px);
+        const float xi = (float)fma(-ox, g.cs, bin_x(g, px));
         const float yi = (float)fma(-oy, g.cs, py);
         const float zi = (float)fma(-oz, g.cs, pz);
         const float4 p0 = posm0[s];
@@ -363,20 +365,34 @@ __global__ void k_nbr(sph_array_view d, sph_array_view s, Grid g, const int *dke
         for (int dz = -g.kz; dz <= g.kz; ++dz)
             for (int dy = -g.ky; dy <= g.ky; ++dy) {
                 int64_t rowbase = (int64_t)g.nx * ((cy + dy) + (int64_t)g.ny * (cz + dz));
-                int rs = scstart[rowbase + cx - g.kx], re = scstart[rowbase + cx + g.kx + 1];
+                // x cells [cx - kx, cx + kx]; on a periodic axis the cells past
+                // either end wrap around and hold the images at x -+ period
+                int pieces = 1, plo[3] = {cx - g.kx, 0, 0}, phi[3] = {cx + g.kx, 0, 0};
+                double pshift[3] = {0.0, 0.0, 0.0};
+                if (g.periodic) {
+                    const int a0 = cx - g.kx, a1 = cx + g.kx;
+                    pieces = 0;
+                    if (a0 < 0) { plo[pieces] = a0 + g.nx; phi[pieces] = g.nx - 1; pshift[pieces++] = -g.plen; }
+                    plo[pieces] = max(a0, 0); phi[pieces] = min(a1, g.nx - 1); pshift[pieces++] = 0.0;
+                    if (a1 >= g.nx) { plo[pieces] = 0; phi[pieces] = a1 - g.nx; pshift[pieces++] = g.plen; }
+                }
+                for (int pc = 0; pc < pieces; ++pc) {
+                int rs = scstart[rowbase + plo[pc]], re = scstart[rowbase + phi[pc] + 1];
                 for (int t = rs; t < re; ++t) {
                     int j = sperm[t];
-                    bool hit = exact_within(ld0(s.x, j), ld0(s.y, j), ld0(s.z, j), px, py, pz, r2);
+                    const double sx = pshift[pc] == 0.0 ? ld0(s.x, j) : __dadd_rn(ld0(s.x, j), pshift[pc]);
+                    bool hit = exact_within(sx, ld0(s.y, j), ld0(s.z, j), px, py, pz, r2);
                     if (!hit && g.symmetric) {
                         // VarHNbrParticleLocator: i within the radius of j
                         const double rj = __dmul_rn(s.h[j], radius_scale);
-                        hit = exact_within(px, py, pz, ld0(s.x, j), ld0(s.y, j), ld0(s.z, j),
+                        hit = exact_within(px, py, pz, sx, ld0(s.y, j), ld0(s.z, j),
                                            __dmul_rn(rj, rj));
                     }
                     if (hit) {
                         if (FILL) index[base + cnt] = j;
                         ++cnt;
                     }
+                }
                 }
             }
         if (FILL) {
@@ -492,7 +508,19 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     // with a list skin the grid cell is the reference cell grown by the skin
     // fraction, so the stencil of the subdivision still covers the list radius
     const double skin_frac = ctx->skin_frac > 0.0 ? ctx->skin_frac : 0.0;
-    const double cs = cell_size * (1.0 + skin_frac) / subdiv;
+    double cs = cell_size * (1.0 + skin_frac) / subdiv;
+    // periodic x: the period holds a whole number of (slightly larger) cells
+    Grid pg;
+    int pnx = 0;
+    if (ctx->periodic) {
+        const double plen = ctx->pxmax - ctx->pxmin;
+        pnx = (int)std::floor(plen / cs);
+        if (pnx < 1) return set_error(SPH_ERR_NOTSUP, "nnps_build: periodic domain shorter than a cell");
+        cs = plen / pnx;
+        pg.periodic = 1;
+        pg.pxmin = ctx->pxmin;
+        pg.plen = plen;
+    }
     const double inv_cs = 1.0 / cs;
     const double inv_cs_ref = 1.0 / cell_size;
 
@@ -515,7 +543,8 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         if (v.n == 0) continue;
         int jb = (check_jump && same_layout) ? 1 : 0;
         k_box<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(v, inv_cs, inv_cs_ref, A.refcell, jb,
-                                                               ctx->d_box, ctx->d_hmax, ctx->d_err);
+                                                               ctx->d_box, ctx->d_hmax, ctx->d_err,
+                                                               pg);
         count_launch();
         SPH_LAUNCH_CHECK("k_box");
     }
@@ -544,6 +573,9 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     memcpy(&hmax, ctx->h_box + 6, sizeof(hmax));
     memcpy(&hmin, ctx->h_box + 10, sizeof(hmin));
     Grid g;
+    g.periodic = pg.periodic;
+    g.pxmin = pg.pxmin;
+    g.plen = pg.plen;
     g.cs = cs;
     g.inv_cs = inv_cs;
     g.cs_f = (float)cs;
@@ -570,6 +602,14 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     g.by0 = mn[1] - g.ky;
     g.bz0 = mn[2] - g.kz;
     int64_t nx = (int64_t)mx[0] - mn[0] + 1 + 2 * g.kx;
+    if (g.periodic) {
+        // the grid is the period: a stencil row wraps at most once
+        if (pnx < 2 * k + 1)
+            return set_error(SPH_ERR_NOTSUP,
+                             "nnps_build: periodic domain narrower than the neighbour stencil");
+        g.bx0 = 0;
+        nx = pnx;
+    }
     int64_t ny = (int64_t)mx[1] - mn[1] + 1 + 2 * g.ky;
     int64_t nz = (int64_t)mx[2] - mn[2] + 1 + 2 * g.kz;
     const int64_t kMaxCells = (int64_t)1 << 27;
@@ -659,7 +699,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
                  cell_size == ctx->cell_size_ref && radius_scale == ctx->build_radius_scale &&
                  subdiv == ctx->build_subdiv && arrays != nullptr &&
                  ctx->build_h > 0.0 && (int)ctx->lists.size() <= kMaxListSlots &&
-                 ctx->grid.symmetric == ctx->symmetric;
+                 ctx->grid.symmetric == ctx->symmetric && ctx->grid.periodic == ctx->periodic;
     for (int a = 0; light && a < narrays; ++a) {
         const ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];

@@ -115,12 +115,13 @@ __device__ __forceinline__ bool listed_exact_test(const Grid &g, const SrcDev &S
     bool hit = false;
     if (r2 <= d.r2hi) {
         const int oj = S.perm[j];
-        hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(D.x, d.orig),
+        const double xi = ld0(D.x, d.orig);
+        hit = exact_within(image_x(g, ld0(S.x, oj), xi, rx), ld0(S.y, oj), ld0(S.z, oj), xi,
                            ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
     }
     if (!hit && g.symmetric) {
         bool in_list;
-        hit = reverse_within(g, S, j, r2, D.x, D.y, D.z, d.orig, in_list);
+        hit = reverse_within(g, S, j, r2, rx, D.x, D.y, D.z, d.orig, in_list);
     }
     return hit;
 }

@@ -50,7 +50,40 @@ struct Grid {
     // radius (radius_scale max h + skin, with a margin), the pruning radius
     int symmetric = 0;
     float reach2 = 0.f;
+    // periodic x axis (the reference's PeriodicDomain, cell.pyx:1277-1376):
+    // particles are binned at their image in [pxmin, pxmin + plen), measured
+    // from pxmin; the grid spans exactly the period (bx0 = 0, nx cells of
+    // size plen / nx) and a stencil row that leaves it continues at the other
+    // end, where the sources are the images shifted by -+plen
+    int periodic = 0;
+    double pxmin = 0.0, plen = 0.0;
 };
+
+// Binning coordinate along x: the position, or on a periodic axis the offset
+// of its image in [pxmin, pxmin + plen) from pxmin.
+__device__ __forceinline__ double bin_x(const Grid &g, double x) {
+    if (!g.periodic) return x;
+    double t = x - g.pxmin;
+    t -= g.plen * floor(t / g.plen);
+    return t;
+}
+
+// Grid x cell of binning coordinate xb (clamped into the period, where
+// rounding can put xb on its upper end).
+__device__ __forceinline__ int bin_cell_x(const Grid &g, double xb) {
+    int c = (int)floor(xb * g.inv_cs) - g.bx0;
+    if (g.periodic) c = min(max(c, 0), g.nx - 1);
+    return c;
+}
+
+// The image of source coordinate xj that destination coordinate xi sees,
+// given the FP32 separation rx = x_i - x_j(image): xj itself, or on a periodic
+// axis xj +- plen (added in FP64 like the reference's ghost copies).
+__device__ __forceinline__ double image_x(const Grid &g, double xj, double xi, float rx) {
+    if (!g.periodic) return xj;
+    const double s = rint((xi - xj - (double)rx) / g.plen);
+    return s == 0.0 ? xj : __dadd_rn(xj, s * g.plen);
+}
 
 struct ArraySnap {
     int64_t n = 0;
@@ -117,6 +150,8 @@ struct sph_ctx {
     double build_h = 0.0;               // the uniform h of the last full build (0: not uniform)
     int build_subdiv = 0;
     int symmetric = 0;                  // variable-h neighbour relation (next build)
+    int periodic = 0;                   // periodic x axis (next build)
+    double pxmin = 0.0, pxmax = 0.0;
     unsigned *d_disp = nullptr;         // max squared displacement (float bits)
     long long n_full = 0, n_light = 0;  // full builds / light refreshes
 };
@@ -334,7 +369,7 @@ __device__ __forceinline__ float3 neg_cell_offset(uint32_t e) {
 // around the threshold, the FP64 test of base/nnps.pyx:337-353 inside it.
 // in_list: within the list radius of j (radius_scale h_j + skin).
 template <class Src>
-__device__ __forceinline__ bool reverse_within(const Grid &g, const Src &S, int j, float r2,
+__device__ __forceinline__ bool reverse_within(const Grid &g, const Src &S, int j, float r2, float rx,
                                                const double *dx64, const double *dy64,
                                                const double *dz64, int oi, bool &in_list) {
     const float rj = (float)g.radius_scale * S.velh[j].w;
@@ -345,8 +380,9 @@ __device__ __forceinline__ bool reverse_within(const Grid &g, const Src &S, int 
     if (r2 > rj2 * (1.f + 1e-5f)) return false;
     const int oj = S.perm[j];
     const double radius = __dmul_rn(S.h[oj], g.radius_scale);
-    return exact_within(ld0(dx64, oi), ld0(dy64, oi), ld0(dz64, oi), ld0(S.x, oj), ld0(S.y, oj),
-                        ld0(S.z, oj), __dmul_rn(radius, radius));
+    const double xi = ld0(dx64, oi);
+    return exact_within(xi, ld0(dy64, oi), ld0(dz64, oi), image_x(g, ld0(S.x, oj), xi, rx),
+                        ld0(S.y, oj), ld0(S.z, oj), __dmul_rn(radius, radius));
 }
 
 // Destination state of one thread (cell-local FP32 offsets, dense cell).
@@ -401,29 +437,46 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             const int tlo = max(-KX, __float2int_rd((d.xi_x - half) * inv_cs));
             const int thi = min(KX, __float2int_rd((d.xi_x + half) * inv_cs));
             const int c0 = zbase + (d.cy + dy) * g.nx;
-            const int lo = __ldg(cst + c0 + tlo);
-            const int hi = __ldg(cst + c0 + thi + 1);
             const float by = d.xi_y - (float)dy * csf;
             const int code_yz = Code<KX>::row(dy, dz);
+            // the row's x cells [cx + tlo, cx + thi]: one index range, or on a
+            // periodic axis up to three (cells past either end wrap around;
+            // wrap = -1 / +1 marks sources whose cell index is nx more / less
+            // than the unwrapped one)
+            int pieces = 1, plo[3], phi[3], pwrap[3];
+            plo[0] = tlo; phi[0] = thi; pwrap[0] = 0;
+            if (g.periodic) {
+                const int a0 = d.cx + tlo, a1 = d.cx + thi;
+                pieces = 0;
+                if (a0 < 0) { plo[pieces] = a0 + g.nx - d.cx; phi[pieces] = min(a1, -1) + g.nx - d.cx; pwrap[pieces++] = -1; }
+                if (a1 >= 0 && a0 < g.nx) { plo[pieces] = max(a0, 0) - d.cx; phi[pieces] = min(a1, g.nx - 1) - d.cx; pwrap[pieces++] = 0; }
+                if (a1 >= g.nx) { plo[pieces] = max(a0, g.nx) - g.nx - d.cx; phi[pieces] = a1 - g.nx - d.cx; pwrap[pieces++] = 1; }
+            }
+            for (int pc = 0; pc < pieces; ++pc) {
+            const int lo = __ldg(cst + c0 + plo[pc]);
+            const int hi = __ldg(cst + c0 + phi[pc] + 1);
+            const float wshift = (float)(pwrap[pc] * g.nx);
             for (int j = lo; j < hi; ++j) {
                 const float4 pj = __ldg(S.posm + j);
-                const float dxc = pj.w - cxf;  // exact: small integers in FP32
+                const float dxc = (pj.w + wshift) - cxf;  // exact: small integers in FP32
                 const float rx = fmaf(-dxc, csf, d.xi_x - pj.x);
                 const float ry = by - pj.y, rz = bz - pj.z;
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                 bool hit = r2 < d.r2lo;
                 if (!hit && r2 <= d.r2hi) {
                     const int oj = S.perm[j];
-                    hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(dx64, d.orig),
-                                       ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
+                    const double xi = ld0(dx64, d.orig);
+                    hit = exact_within(image_x(g, ld0(S.x, oj), xi, rx), ld0(S.y, oj), ld0(S.z, oj),
+                                       xi, ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
                 }
                 bool listed = hit || r2 < d.r2list;
                 if (g.symmetric && !hit && r2 <= g.reach2) {
                     bool in_list;
-                    hit = reverse_within(g, S, j, r2, dx64, dy64, dz64, d.orig, in_list);
+                    hit = reverse_within(g, S, j, r2, rx, dx64, dy64, dz64, d.orig, in_list);
                     listed = listed || hit || in_list;
                 }
                 if (listed) fn(j, rx, ry, rz, code_yz + (int)dxc, hit);
+            }
             }
         }
     }

@@ -57,6 +57,31 @@ def jitter_h(props, frac=0.25, seed=0):
     return out
 
 
+def periodic_strip(dx=0.05, nx=20, ny=10, rho0=1.0, c0=10.0, vel_std=1.0, seed=0,
+                   rho_jitter=0.01, jitter=0.0):
+    """A 2D lattice strip [0, nx dx) x [0, ny dx) meant to be periodic in x
+    (domain xmin = 0, xmax = nx dx): points at cell centres (moved by
+    U(-jitter, jitter) dx per coordinate), h = 1.3 dx, m = rho0 dx^2,
+    velocities N(0, vel_std^2), rho = rho0 (1 + U(-j, j)) and the Tait p, cs
+    of that density (gamma = 7) -- a state where every pair term is
+    non-trivial.  Seeded."""
+    rng = np.random.default_rng(seed)
+    xs, ys = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dx)
+    x = xs.ravel()
+    y = ys.ravel()
+    n = x.size
+    if jitter:
+        jr = np.random.default_rng(seed + 1)
+        x = x + jr.uniform(-jitter, jitter, n) * dx
+        y = y + jr.uniform(-jitter, jitter, n) * dx
+    rho = rho0 * (1.0 + rng.uniform(-rho_jitter, rho_jitter, n))
+    B = c0 * c0 * rho0 / 7.0
+    return dict(x=x, y=y, z=np.zeros(n), u=rng.normal(0.0, vel_std, n),
+                v=rng.normal(0.0, vel_std, n), m=np.full(n, rho0 * dx * dx),
+                h=np.full(n, 1.3 * dx), rho=rho, p=B * ((rho / rho0) ** 7 - 1.0),
+                cs=c0 * (rho / rho0) ** 3)
+
+
 def circular_patch(dx=0.025, c0=100.0):
     """The reference FluidSolver's circular patch (solver/fluid_solver.py:15-49):
     the square lattice of ``elliptical_drop`` with ``m = dx^2``, ``h = 2 dx``,
@@ -185,14 +210,15 @@ def _integrator(api, name):
 
 
 def setup_drop(api, props, c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5,
-               integrator="euler", name="fluid", variable_h=False):
+               integrator="euler", name="fluid", variable_h=False, periodic_domain=None):
     """Elliptical drop operations: SPHRho, Tait, PGrad, Monaghan AV,
     position stepping and XSPH, in that order (2D).  ``variable_h`` makes
     the neighbour relation symmetric (``Particles(variable_h=True)``)."""
     base, sph, solver = api.base, api.sph, api.solver
     Fluid = base.ParticleType.Fluid
     pa = base.get_particle_array(name=name, type=Fluid, **props)
-    particles = base.Particles(arrays=[pa], variable_h=variable_h)
+    particles = base.Particles(arrays=[pa], variable_h=variable_h,
+                               periodic_domain=periodic_domain)
     s = solver.Solver(dim=2, integrator_type=_integrator(api, integrator))
     s.add_operation(solver.SPHOperation(
         sph.SPHRho.withargs(), on_types=[Fluid], from_types=[Fluid],

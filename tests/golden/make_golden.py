@@ -256,6 +256,54 @@ def fixture_drop_varh(dx=0.05):
     return out
 
 
+def fixture_periodic(dx=0.05, nx=20, ny=10):
+    """Particles(periodic_domain=PeriodicDomain(0, nx dx)) on a lattice strip:
+    the ghost copies the reference appends (cell.pyx:1277-1376), the
+    neighbour lists over real and ghost particles, and each pair function
+    evaluated on the initial state (where the ghosts still carry their
+    originals' state; a calc zeroes them as non-LocalReal destinations)."""
+    props = W.periodic_strip(dx=dx, nx=nx, ny=ny)
+    n = len(props["x"])
+    extra = {k: np.zeros(n) for k in ("tmpx", "tmpy", "tmpz")}
+    pa = rbase.get_particle_array(name="fluid", type=rbase.ParticleType.Fluid,
+                                  **props, **extra)
+    dom = rbase.PeriodicDomain(xmin=0.0, xmax=nx * dx)
+    particles = rbase.Particles(arrays=[pa], periodic_domain=dom)
+    out = {"xmin": np.float64(0.0), "xmax": np.float64(nx * dx), "n_real": np.int64(n)}
+    for p_ in props:
+        out["in_" + p_] = props[p_].copy()
+    xa = pa.get("x", only_real_particles=False)
+    ya = pa.get("y", only_real_particles=False)
+    ng = len(xa) - n
+    origin = np.full(ng, -1, np.int64)
+    shift = np.zeros(ng)
+    L = nx * dx
+    for g in range(ng):
+        for s in (L, -L):
+            hit = np.nonzero((xa[:n] + s == xa[n + g]) & (ya[:n] == ya[n + g]))[0]
+            if hit.size:
+                origin[g], shift[g] = hit[0], s
+                break
+    assert (origin >= 0).all()
+    out["ghost_origin"] = origin
+    out["ghost_shift"] = shift
+    o, ix = neighbours_csr(particles, pa, pa)
+    out["nbr_offsets"] = o[: n + 1]
+    out["nbr_index"] = ix[: o[n]]
+    kern = rbase.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("pgrad", rsph.SPHPressureGradient.withargs(dim=2), ["tmpx", "tmpy"]),
+            ("avisc", rsph.MonaghanArtificialVsicosity.withargs(alpha=1.0, beta=1.0),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("xsph", rsph.XSPHCorrection.withargs(eps=0.5, dim=2), ["tmpx", "tmpy"]),
+            ("rho", rsph.SPHRho.withargs(), ["tmpx"])):
+        calc = rsph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            out["%s_%d" % (name, k)] = pa.get(upn)[:n].copy()
+    return out
+
+
 def main():
     fixtures = {
         "kernel": fixture_kernel,
@@ -272,6 +320,7 @@ def main():
         "fluid_pc": lambda: fixture_fluid_integrator("pc"),
         "cube_leapfrog": lambda: fixture_cube(1000, "leapfrog"),
         "drop_varh": fixture_drop_varh,
+        "periodic": fixture_periodic,
     }
     only = sys.argv[1:]
     if only:

@@ -443,3 +443,98 @@ def test_variable_h_euler_step(skin, monkeypatch):
     s, particles = W.setup_drop(API, inputs(g, "fluid"), variable_h=True)
     s.integrator.integrate(float(g["dt"]))
     _check_step(g, particles.arrays, 1, DROP_K)
+
+
+# -- periodic x (PeriodicDomain, base/cell.pyx:1277-1376) ---------------------
+
+def _periodic_particles(g):
+    n = int(g["n_real"])
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    pa = base.get_particle_array(name="fluid", type=base.ParticleType.Fluid,
+                                 tmpx=np.zeros(n), tmpy=np.zeros(n), tmpz=np.zeros(n), **props)
+    dom = base.PeriodicDomain(xmin=float(g["xmin"]), xmax=float(g["xmax"]))
+    return pa, base.Particles(arrays=[pa], periodic_domain=dom)
+
+
+def test_periodic_neighbour_sets_bit_exact():
+    """The reference's lists over real and ghost particles, ghosts mapped to
+    the particle they copy, against the device build's images."""
+    _need_gpu()
+    g = load("periodic")
+    n = int(g["n_real"])
+    pa, particles = _periodic_particles(g)
+    assert pa.get_number_of_particles() == n     # no ghost particles appended
+    origin = g["ghost_origin"]
+    ref = [{(j if j < n else int(origin[j - n])) for j in s}
+           for s in csr_sets(g["nbr_offsets"], g["nbr_index"])]
+    off, idx = _locator_sets(particles, pa, pa)
+    assert csr_sets(off, idx) == ref
+
+
+def test_periodic_pair_functions():
+    """Every pair function on the initial state (the reference's ghosts
+    still carry their originals' state there)."""
+    _need_gpu()
+    g = load("periodic")
+    pa, particles = _periodic_particles(g)
+    kern = base.CubicSplineKernel(dim=2)
+    for name, fn, ups in (
+            ("pgrad", sph.SPHPressureGradient.withargs(dim=2), ["tmpx", "tmpy"]),
+            ("avisc", sph.MonaghanArtificialVsicosity.withargs(alpha=1.0, beta=1.0),
+             ["tmpx", "tmpy", "tmpz"]),
+            ("xsph", sph.XSPHCorrection.withargs(eps=0.5, dim=2), ["tmpx", "tmpy"]),
+            ("rho", sph.SPHRho.withargs(), ["tmpx"])):
+        calc = sph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+        calc.sph(*ups)
+        for k, upn in enumerate(ups):
+            ref = g["%s_%d" % (name, k)]
+            assert normwise(pa.get(upn), ref) < TOL, (name, k, normwise(pa.get(upn), ref))
+
+
+def test_periodic_step_after_crossing_vs_oracle():
+    """Ten Euler steps of the drop operations on a jittered strip with a
+    uniform drift that carries the last column across the periodic end; then one
+    more step from that shared state, GPU against the oracle's periodic
+    images (per-step parity, 1e-5).  The reference itself cannot run this:
+    its ghosts are re-appended at every update and zeroed by every calc."""
+    _need_gpu()
+    # jittered lattice: on the exact lattice the pressure forces cancel to
+    # ~1e-4 of their terms and FP32 sums cannot carry the x rate to 1e-5
+    props = W.periodic_strip(vel_std=0.1, jitter=0.1)
+    props["u"] = props["u"] + 50.0
+    dom = (0.0, 1.0)
+    s, particles = W.setup_drop(API, props, c0=10.0,
+                                periodic_domain=base.PeriodicDomain(xmin=dom[0], xmax=dom[1]))
+    dt = 1e-4
+    for _ in range(10):
+        s.integrator.integrate(dt)
+    pa = particles.arrays[0]
+    assert pa.get("x").max() > dom[1]             # some particles left the period
+    state = {k: pa.get(k).copy() for k in props}
+    prob = oracle.Problem({"fluid": state}, oracle.drop_ops(c0=10.0), 2, periodic=dom)
+    prob.integrate_euler(dt)
+    s.integrator.integrate(dt)
+    for p in ("x", "y", "u", "v"):
+        d_ref = prob.arrays["fluid"][p] - state[p]
+        assert normwise(pa.get(p) - state[p], d_ref) < TOL, (p, normwise(pa.get(p) - state[p], d_ref))
+    for p in ("rho", "p"):
+        assert normwise(pa.get(p), prob.arrays["fluid"][p]) < TOL, p
+
+
+def test_periodic_trajectory_vs_oracle():
+    """A gentle strip (c0 = 1, small velocities, drift across the end):
+    ten Euler steps against the oracle within 1e-4."""
+    _need_gpu()
+    props = W.periodic_strip(vel_std=0.1, c0=1.0, jitter=0.1)
+    props["u"] = props["u"] + 50.0
+    dom = (0.0, 1.0)
+    s, particles = W.setup_drop(API, props, c0=1.0,
+                                periodic_domain=base.PeriodicDomain(xmin=dom[0], xmax=dom[1]))
+    prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=1.0), 2, periodic=dom)
+    for _ in range(10):
+        s.integrator.integrate(1e-4)
+        prob.integrate_euler(1e-4)
+    pa = particles.arrays[0]
+    for p in ("x", "y", "u", "v"):
+        d_ref = prob.arrays["fluid"][p] - props[p]
+        assert normwise(pa.get(p) - props[p], d_ref) < 1e-4, (p, normwise(pa.get(p) - props[p], d_ref))

@@ -162,3 +162,13 @@ def test_variable_h_switches_the_cell_manager_to_the_symmetric_relation():
     assert particles.cell_manager.symmetric
     pb = base.get_particle_array(name="fluid", **props)
     assert not base.Particles(arrays=[pb], update_particles=False).cell_manager.symmetric
+
+
+def test_periodic_domain_translate_rules():
+    """base/cell.pyx:1568-1598: an axis spanning exactly 2000 is not periodic."""
+    d = base.PeriodicDomain(xmin=-0.2, xmax=1.0)
+    assert d.xtranslate == pytest.approx(1.2) and d.ytranslate == 0.0 and d.ztranslate == 0.0
+    pa = base.get_particle_array(name="f", x=np.linspace(0, 1, 5), h=np.full(5, 0.1))
+    with pytest.raises(NotImplementedError):
+        base.CellManager(arrays_to_bin=[pa], periodic_domain=base.PeriodicDomain(ymin=0, ymax=1),
+                         initialize=False)

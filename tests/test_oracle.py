@@ -244,3 +244,61 @@ def test_variable_h_euler_step_matches_reference():
     prob = oracle.Problem({"fluid": inputs(g, "fluid")}, oracle.drop_ops(), 2, variable_h=True)
     prob.integrate_euler(float(g["dt"]))
     _cmp_step(g, prob, ["fluid"], 1e-13)
+
+
+def _periodic_case():
+    g = load("periodic")
+    n = int(g["n_real"])
+    p = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    return g, n, p
+
+
+def test_periodic_neighbour_sets_match_reference():
+    """PeriodicDomain along x: the reference's lists over real particles and
+    the ghost copies it appends (cell.pyx:1277-1376), ghosts mapped to the
+    particle they copy, equal the oracle's lists over periodic images."""
+    g, n, p = _periodic_case()
+    origin = g["ghost_origin"]
+    ref = csr_sets(g["nbr_offsets"], g["nbr_index"])
+    ref = [{(j if j < n else int(origin[j - n])) for j in s} for s in ref]
+    prob = oracle.Problem({"fluid": p}, [], 2, periodic=(float(g["xmin"]), float(g["xmax"])))
+    off, idx = prob.neighbours("fluid", "fluid")
+    _, gor = prob._source("fluid")
+    got = [{(j if j < n else int(gor[j - n])) for j in s} for s in csr_sets(off, idx)]
+    assert got == ref
+    # the boundary rows see images: particle 0 has as many neighbours as an interior one
+    assert len(ref[0]) == len(ref[5])
+
+
+def test_periodic_pair_sums_bit_exact_with_reference_lists():
+    """Given the reference's lists and ghost positions, every pair function
+    sums to the same FP64 bits (ghosts carrying their originals' state)."""
+    g, n, p = _periodic_case()
+    origin, shift = g["ghost_origin"], g["ghost_shift"]
+    ext = {k: np.concatenate([v, v[origin]]) for k, v in p.items()}
+    ext["x"] = np.concatenate([p["x"], p["x"][origin] + shift])
+    off, idx = g["nbr_offsets"], g["nbr_index"]
+    for name, params, nout in (("pgrad", {}, 2), ("avisc", {"alpha": 1.0, "beta": 1.0}, 3),
+                               ("xsph", {"eps": 0.5}, 2), ("rho", {}, 1)):
+        res = oracle.pair_sum(name, p, ext, off, idx, 2, params, nout)
+        for k in range(nout):
+            np.testing.assert_array_equal(res[k], g["%s_%d" % (name, k)])
+
+
+def test_periodic_images_are_the_minimum_images():
+    """With particles past the end of the period (x is never wrapped), the
+    oracle's lists are exactly the sources within radius among every
+    particle's images x_j + {-L, 0, L} (brute force)."""
+    from pysph_gb300 import workloads as W
+    props = W.periodic_strip(vel_std=1.0)
+    props["x"] = props["x"] + 0.07
+    prob = oracle.Problem({"fluid": props}, [], 2, periodic=(0.0, 1.0))
+    off, idx = prob.neighbours("fluid", "fluid")
+    _, gor = prob._source("fluid")
+    n = len(props["x"])
+    x, y, h = props["x"], props["y"], props["h"]
+    for i in range(n):
+        got = sorted(int(j) if j < n else int(gor[j - n]) for j in idx[off[i]:off[i + 1]])
+        ref = sorted(j for j in range(n) for s in (-1.0, 0.0, 1.0)
+                     if ((x[j] + s if s else x[j]) - x[i]) ** 2 + (y[j] - y[i]) ** 2 < (2 * h[i]) ** 2)
+        assert got == ref, i
