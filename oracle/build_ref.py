@@ -119,6 +119,7 @@ def _fix_py(text, local_modules):
     text = re.sub(r"^import thread\b", "import _thread as thread", text, flags=re.M)
     text = re.sub(r"^import threading, thread$", "import threading, _thread as thread", text, flags=re.M)
     text = text.replace("sys.maxint", "sys.maxsize")
+    text = re.sub(r"\bbasestring\b", "str", text)
     return text
 
 

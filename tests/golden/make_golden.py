@@ -304,6 +304,34 @@ def fixture_periodic(dx=0.05, nx=20, ny=10):
     return out
 
 
+def fixture_drop_output(dx=0.1, steps=3):
+    """Solver.solve of the drop with output every step (solver.py:457-538):
+    the names of the .npz files it writes and their contents."""
+    import tempfile
+    props = W.elliptical_drop(dx=dx)
+    s, particles = W.setup_drop(REF, props)
+    s.set_time_step(1e-5)
+    s.set_final_time(steps * 1e-5 * (1 - 1e-9))
+    s.set_print_freq(1)
+    # the reference's Solver reads detailed_output, which only this setter
+    # creates (solver.py:520)
+    s.set_output_printing_level(False)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        s.set_output_directory(d)
+        s.set_output_fname("drop")
+        s.solve()
+        names = sorted(os.listdir(d))
+        out["files"] = np.array(names)
+        for k, f in enumerate(names):
+            with np.load(os.path.join(d, f)) as z:
+                for key in z.files:
+                    out["f%d_%s" % (k, key)] = z[key]
+    for p_ in props:
+        out["in_" + p_] = np.asarray(props[p_]).copy()
+    return out
+
+
 def main():
     fixtures = {
         "kernel": fixture_kernel,
@@ -321,6 +349,7 @@ def main():
         "cube_leapfrog": lambda: fixture_cube(1000, "leapfrog"),
         "drop_varh": fixture_drop_varh,
         "periodic": fixture_periodic,
+        "drop_output": fixture_drop_output,
     }
     only = sys.argv[1:]
     if only:

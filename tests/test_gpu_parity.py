@@ -538,3 +538,36 @@ def test_periodic_trajectory_vs_oracle():
     for p in ("x", "y", "u", "v"):
         d_ref = prob.arrays["fluid"][p] - props[p]
         assert normwise(pa.get(p) - props[p], d_ref) < 1e-4, (p, normwise(pa.get(p) - props[p], d_ref))
+
+
+# -- Solver.solve output (solver.py:457-538) ------------------------------------
+
+def test_solver_output_files_match_reference(tmp_path):
+    """The .npz files Solver.solve writes: the same names, keys and values
+    as the reference's (dt, cell_size, np and the print properties)."""
+    _need_gpu()
+    g = load("drop_output")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    s, particles = W.setup_drop(API, props)
+    s.set_time_step(1e-5)
+    s.set_final_time(3 * 1e-5 * (1 - 1e-9))
+    s.set_print_freq(1)
+    s.set_output_printing_level(False)
+    s.set_output_directory(str(tmp_path))
+    s.set_output_fname("drop")
+    s.solve()
+    names = sorted(p.name for p in tmp_path.iterdir())
+    assert names == list(g["files"])
+    for k, f in enumerate(names):
+        with np.load(tmp_path / f) as z:
+            ref_keys = sorted(key[len("f%d_" % k):] for key in g if key.startswith("f%d_" % k))
+            assert sorted(z.files) == ref_keys
+            for key in ref_keys:
+                ref = g["f%d_%s" % (k, key)]
+                got = z[key]
+                if key in ("dt", "cell_size", "np", "m", "h"):
+                    np.testing.assert_array_equal(got, ref)
+                elif key in ("x", "y", "u", "v"):
+                    assert normwise(got - props[key], ref - props[key]) < 1e-4, (f, key)
+                else:
+                    assert normwise(got, ref) < 1e-4, (f, key)
