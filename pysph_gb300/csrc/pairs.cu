@@ -107,6 +107,7 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
 // With a list skin the list holds sources up to the list radius: keep the
 // neighbours (the FP32 band test, then the FP64 test of base/nnps.pyx:
 // 337-353 inside the band).
+template <bool EXT>
 __device__ __forceinline__ bool listed_exact_test(const Grid &g, const SrcDev &S, const DestDev &D,
                                                   const DestPos &d, int j, float rx, float ry,
                                                   float rz) {
@@ -116,20 +117,21 @@ __device__ __forceinline__ bool listed_exact_test(const Grid &g, const SrcDev &S
     if (r2 <= d.r2hi) {
         const int oj = S.perm[j];
         const double xi = ld0(D.x, d.orig);
-        hit = exact_within(image_x(g, ld0(S.x, oj), xi, rx), ld0(S.y, oj), ld0(S.z, oj), xi,
-                           ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
+        hit = exact_within(EXT ? image_x(g, ld0(S.x, oj), xi, rx) : ld0(S.x, oj), ld0(S.y, oj),
+                           ld0(S.z, oj), xi, ld0(D.y, d.orig), ld0(D.z, d.orig), d.radius2);
     }
-    if (!hit && g.symmetric) {
+    if (EXT && !hit && g.symmetric) {
         bool in_list;
         hit = reverse_within(g, S, j, r2, rx, D.x, D.y, D.z, d.orig, in_list);
     }
     return hit;
 }
 
+template <bool EXT>
 __device__ __forceinline__ bool listed_exact(const Grid &g, const SrcDev &S, const DestDev &D,
                                              const DestPos &d, int j, float rx, float ry, float rz) {
     if (g.skin <= 0.f) return true;
-    return listed_exact_test(g, S, D, d, j, rx, ry, rz);
+    return listed_exact_test<EXT>(g, S, D, d, j, rx, ry, rz);
 }
 
 // grid of the destination in slot s
@@ -156,7 +158,7 @@ struct NoExtra {
 // neighbours (ok false for the others); without it a skin entry reaches fn
 // with ok true -- right for terms that vanish beyond the radius (W and
 // grad W of the uniform-h cubic spline are exactly 0 for q >= 2 in FP32).
-template <int KX, int B, class Extra, class Fn, class Done>
+template <int KX, int B, bool EXT, class Extra, class Fn, class Done>
 __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int cap, int64_t stride,
                                            int s, const DestPos &d, const DestDev &D, bool filter,
                                            Extra &&extra, Fn &&fn, Done &&done) {
@@ -193,7 +195,7 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
             const float rx = fmaf(sh.x, csf, d.xi_x - p[b].x);
             const float ry = fmaf(sh.y, csf, d.xi_y - p[b].y);
             const float rz = fmaf(sh.z, csf, d.xi_z - p[b].z);
-            fn(k + b < m && (!filter || listed_exact_test(g, S, D, d, j, rx, ry, rz)), j, rx, ry, rz,
+            fn(k + b < m && (!filter || listed_exact_test<EXT>(g, S, D, d, j, rx, ry, rz)), j, rx, ry, rz,
                p[b].w, x[b]);
         }
         done();
@@ -205,7 +207,7 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
     if (c > cap) {
         // the list entries past cap, in the order of the list build
         int skip = cap;
-        for_neighbours<KX>(g, S, d, D.x, D.y, D.z,
+        for_neighbours<KX, EXT>(g, S, d, D.x, D.y, D.z,
                            [&](int j, float rx, float ry, float rz, int, bool exact) {
                                if (skip > 0) {
                                    --skip;
@@ -221,19 +223,19 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
 // ---------------------------------------------------------------------------
 // neighbour list (base/nnps.pyx:525-620 FixedDestNbrParticleLocator cache)
 // ---------------------------------------------------------------------------
-template <int KX, bool BATCH>
+template <int KX, int MODE>
 __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ ListArgs A) {
     using C = Code<KX>;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int c = 0;
     if (s < A.d.n) {
-        const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
+        const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
         DestPos d;
         if (load_dest(g, A.d, (int)s, d)) {
             uint32_t *out = A.nbr + s;
             const int cap = A.cap;
             const int64_t stride = A.stride;
-            for_neighbours<KX>(g, A.s, d, A.d.x, A.d.y, A.d.z,
+            for_neighbours<KX, MODE == 2>(g, A.s, d, A.d.x, A.d.y, A.d.z,
                                [&](int j, float, float, float, int code, bool) {
                                    if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                                    ++c;
@@ -248,11 +250,14 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
-template <int KX, bool UH, bool BATCH>
-__global__ void __launch_bounds__(kPairBlock, (UH && !BATCH) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
+// MODE 0: one simulation; 1: a batch of simulations (per-instance grids);
+// 2: one simulation with the extended search (periodic x or variable-h
+// symmetric lists), kept apart so the other modes carry none of its state.
+template <int KX, bool UH, int MODE>
+__global__ void __launch_bounds__(kPairBlock, (UH && MODE == 0) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
-    const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
+    const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
     const bool real = load_dest(g, A.d, (int)s, d);
     CSum rho;
@@ -277,7 +282,7 @@ __global__ void __launch_bounds__(kPairBlock, (UH && !BATCH) ? 8 : 1) k_density(
                 const int cap = A.cap[si];
                 const int64_t stride = A.stride[si];
                 int c = 0;
-                for_neighbours<KX>(g, S, d, A.d.x, A.d.y, A.d.z,
+                for_neighbours<KX, MODE == 2>(g, S, d, A.d.x, A.d.y, A.d.z,
                     [&](int j, float rx, float ry, float rz, int code, bool exact) {
                         if (c < cap) out[(int64_t)c * stride] = (uint32_t)j | ((uint32_t)code << C::SHIFT);
                         ++c;
@@ -299,7 +304,7 @@ __global__ void __launch_bounds__(kPairBlock, (UH && !BATCH) ? 8 : 1) k_density(
                 continue;
             }
             // with variable h, W at the mean h can reach past the radius of h_i
-            for_listed<KX, (UH && !BATCH) ? 6 : 4>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, !uh, NoExtra(),
+            for_listed<KX, (UH && MODE == 0) ? 6 : 4, MODE == 2>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, !uh, NoExtra(),
                 [&](bool ok, int j, float rx, float ry, float rz, float mj, int) {
                     float ih = ihi, fac = faci;
                     if (!uh) {
@@ -358,7 +363,7 @@ struct VelState {
 
 // SPEC 0: any terms, runtime flags; 1: PGrad + AV, uniform h, one source;
 // 2: PGrad + AV + XSPH, uniform h, one source.
-template <int KX, int SPEC, bool BATCH>
+template <int KX, int SPEC, int MODE>
 __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ RatesArgs A) {
     constexpr uint32_t SF = SPEC == 1 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC)
                           : (SPEC == 2 ? (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH) : 0u);
@@ -367,7 +372,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     constexpr bool MAY_DRHO = SPEC == 0;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
-    const Grid &g = grid_of<BATCH>(A.g, A.d, (int)s);
+    const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
     const bool real = load_dest(g, A.d, (int)s, d);
     CSum ax, ay, az, xx, xy, xz, dr;
@@ -386,7 +391,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
             const uint32_t fl = SPEC != 0 ? SF : S.flags;
             // the boundary force has its own support (normal distance, delp)
             const bool filt = !uh || (fl & SPH_TERM_BFORCE) != 0;
-            for_listed<KX, (SPEC != 0 ? 3 : 2)>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, filt,
+            for_listed<KX, (SPEC != 0 ? 3 : 2), MODE == 2>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, filt,
                 [&](int j) { return VelState{S.velh[j], S.st[j]}; },
                 [&](bool ok, int j, float rx, float ry, float rz, float mj, const VelState &vs) {
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
@@ -515,7 +520,7 @@ struct FeatureArgs {
     float *out_f;       // [n][192] FP32 by original index (or null)
 };
 
-template <int KX>
+template <int KX, bool EXT>
 __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__ FeatureArgs A) {
     constexpr int NN = SPH_MLP_NNBR, NC = SPH_MLP_NCH;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -550,18 +555,18 @@ __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__
                 const float rx = fmaf(sh.x, csf, d.xi_x - p.x);
                 const float ry = fmaf(sh.y, csf, d.xi_y - p.y);
                 const float rz = fmaf(sh.z, csf, d.xi_z - p.z);
-                if (listed_exact(A.g, S, A.d, d, j, rx, ry, rz)) keep(j, rx, ry, rz);
+                if (listed_exact<EXT>(A.g, S, A.d, d, j, rx, ry, rz)) keep(j, rx, ry, rz);
             }
             if (c > A.cap) {
                 int skip = A.cap;
-                for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                for_neighbours<KX, EXT>(A.g, S, d, A.d.x, A.d.y, A.d.z,
                                    [&](int j, float rx, float ry, float rz, int, bool exact) {
                                        if (skip > 0) { --skip; return; }
                                        if (exact) keep(j, rx, ry, rz);
                                    });
             }
         } else {
-            for_neighbours<KX>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+            for_neighbours<KX, EXT>(A.g, S, d, A.d.x, A.d.y, A.d.z,
                                [&](int j, float rx, float ry, float rz, int, bool exact) {
                                    if (exact) keep(j, rx, ry, rz);
                                });
@@ -725,9 +730,13 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
         a.stride = L.stride;
         a.cap = L.cap;
         const int b = blocks_for(D.n);
-        if (g.kx == 1) k_nbrlist<1, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
-        else if (g.kx == 2) k_nbrlist<2, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
-        else k_nbrlist<3, false><<<b, kPairBlock, 0, ctx->stream>>>(a);
+        const bool ext = g.periodic || g.symmetric;
+#define LLAUNCH(K) (ext ? k_nbrlist<K, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                        : k_nbrlist<K, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
+        if (g.kx == 1) LLAUNCH(1);
+        else if (g.kx == 2) LLAUNCH(2);
+        else LLAUNCH(3);
+#undef LLAUNCH
         count_launch();
         SPH_LAUNCH_CHECK("k_nbrlist");
     }
@@ -821,8 +830,11 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     const bool uh = a.g.uniform_h != 0;
-#define DLAUNCH(K) (uh ? k_density<K, true, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                       : k_density<K, false, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+    const bool ext = a.g.periodic || a.g.symmetric;
+#define DLAUNCH(K) (ext ? (uh ? k_density<K, true, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                              : k_density<K, false, 2><<<b, kPairBlock, 0, ctx->stream>>>(a)) \
+                        : (uh ? k_density<K, true, 0><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                              : k_density<K, false, 0><<<b, kPairBlock, 0, ctx->stream>>>(a)))
     if (a.g.kx == 1) DLAUNCH(1);
     else if (a.g.kx == 2) DLAUNCH(2);
     else DLAUNCH(3);
@@ -883,9 +895,13 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
         if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC)) spec = 1;
         else if (terms[0].flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
     }
-#define RLAUNCH(K) (spec == 1 ? k_rates<K, 1, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                    : spec == 2 ? k_rates<K, 2, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                                : k_rates<K, 0, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+    // the extended search (periodic x, variable-h lists) has its own
+    // instantiation of the general kernel; the specialised ones need neither
+    if (a.g.periodic || a.g.symmetric) spec = 3;
+#define RLAUNCH(K) (spec == 1 ? k_rates<K, 1, 0><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                    : spec == 2 ? k_rates<K, 2, 0><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                    : spec == 3 ? k_rates<K, 0, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                                : k_rates<K, 0, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
     if (a.g.kx == 1) RLAUNCH(1);
     else if (a.g.kx == 2) RLAUNCH(2);
     else RLAUNCH(3);
@@ -925,9 +941,13 @@ int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params
     a.out_f = out_f;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
-    if (a.g.kx == 1) k_features<1><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else if (a.g.kx == 2) k_features<2><<<b, kPairBlock, 0, ctx->stream>>>(a);
-    else k_features<3><<<b, kPairBlock, 0, ctx->stream>>>(a);
+    const bool ext = a.g.periodic || a.g.symmetric;
+#define FLAUNCH(K) (ext ? k_features<K, true><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                        : k_features<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+    if (a.g.kx == 1) FLAUNCH(1);
+    else if (a.g.kx == 2) FLAUNCH(2);
+    else FLAUNCH(3);
+#undef FLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_features");
     return SPH_OK;
@@ -967,8 +987,8 @@ int batch_density(sph_batch *b) {
     const int blocks = blocks_for(b->view.n);
     const bool uh = b->uniform_h != 0;
     const int K = r.subdiv;
-#define BDL(K_) (uh ? k_density<K_, true, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
-                    : k_density<K_, false, true><<<blocks, kPairBlock, 0, b->stream>>>(a))
+#define BDL(K_) (uh ? k_density<K_, true, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                    : k_density<K_, false, 1><<<blocks, kPairBlock, 0, b->stream>>>(a))
     if (K == 1) BDL(1);
     else if (K == 2) BDL(2);
     else BDL(3);
@@ -1015,9 +1035,9 @@ int batch_rates(sph_batch *b, double *const *acc, double *const *pos) {
         else if (r.term.flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
     }
     const int K = r.subdiv;
-#define BRL(K_) (spec == 1 ? k_rates<K_, 1, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
-                 : spec == 2 ? k_rates<K_, 2, true><<<blocks, kPairBlock, 0, b->stream>>>(a) \
-                             : k_rates<K_, 0, true><<<blocks, kPairBlock, 0, b->stream>>>(a))
+#define BRL(K_) (spec == 1 ? k_rates<K_, 1, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                 : spec == 2 ? k_rates<K_, 2, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
+                             : k_rates<K_, 0, 1><<<blocks, kPairBlock, 0, b->stream>>>(a))
     if (K == 1) BRL(1);
     else if (K == 2) BRL(2);
     else BRL(3);

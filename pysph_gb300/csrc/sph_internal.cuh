@@ -408,7 +408,7 @@ struct DestPos {
 // (d.r2list > 0) the sources within the list radius that are not neighbours
 // are visited too, with exact = false.  posm[j].w holds the source's
 // dense-grid x cell.
-template <int KX, class Fn>
+template <int KX, bool EXT, class Fn>
 __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
                                                const double *dx64, const double *dy64,
                                                const double *dz64, Fn &&fn) {
@@ -416,7 +416,7 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
     const float inv_cs = 1.f / csf;
     // pruning radius: the accept/recheck threshold plus a relative margin
     // that covers FP32 rounding of the slab distances and cell assignment
-    const float R2 = fmaxf(fmaxf(d.r2hi, d.r2list), g.symmetric ? g.reach2 : 0.f) * 1.0002f;
+    const float R2 = fmaxf(fmaxf(d.r2hi, d.r2list), (EXT && g.symmetric) ? g.reach2 : 0.f) * 1.0002f;
     const float cxf = (float)d.cx;
     const int rowstride_z = g.nx * g.ny;  // < 2^27 cells: 32-bit indices
     const int *cst = S.cstart + g.cell_base;
@@ -439,23 +439,14 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             const int c0 = zbase + (d.cy + dy) * g.nx;
             const float by = d.xi_y - (float)dy * csf;
             const int code_yz = Code<KX>::row(dy, dz);
-            // the row's x cells [cx + tlo, cx + thi]: one index range, or on a
-            // periodic axis up to three (cells past either end wrap around;
-            // wrap = -1 / +1 marks sources whose cell index is nx more / less
-            // than the unwrapped one)
-            int pieces = 1, plo[3], phi[3], pwrap[3];
-            plo[0] = tlo; phi[0] = thi; pwrap[0] = 0;
-            if (g.periodic) {
-                const int a0 = d.cx + tlo, a1 = d.cx + thi;
-                pieces = 0;
-                if (a0 < 0) { plo[pieces] = a0 + g.nx - d.cx; phi[pieces] = min(a1, -1) + g.nx - d.cx; pwrap[pieces++] = -1; }
-                if (a1 >= 0 && a0 < g.nx) { plo[pieces] = max(a0, 0) - d.cx; phi[pieces] = min(a1, g.nx - 1) - d.cx; pwrap[pieces++] = 0; }
-                if (a1 >= g.nx) { plo[pieces] = max(a0, g.nx) - g.nx - d.cx; phi[pieces] = a1 - g.nx - d.cx; pwrap[pieces++] = 1; }
-            }
-            for (int pc = 0; pc < pieces; ++pc) {
-            const int lo = __ldg(cst + c0 + plo[pc]);
-            const int hi = __ldg(cst + c0 + phi[pc] + 1);
-            const float wshift = (float)(pwrap[pc] * g.nx);
+            // the row's x cells [cx + tlo, cx + thi] (relative): one index
+            // range, or on a periodic axis up to three -- the cells past the
+            // low / high end wrap to the other end, where the sources' cell
+            // index is nx more / less than the unwrapped one (wrap -1 / +1)
+            auto visit = [&](int rlo, int rhi, int wrap) {
+            const int lo = __ldg(cst + c0 + rlo);
+            const int hi = __ldg(cst + c0 + rhi + 1);
+            const float wshift = (float)(wrap * g.nx);
             for (int j = lo; j < hi; ++j) {
                 const float4 pj = __ldg(S.posm + j);
                 const float dxc = (pj.w + wshift) - cxf;  // exact: small integers in FP32
@@ -466,17 +457,26 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
                 if (!hit && r2 <= d.r2hi) {
                     const int oj = S.perm[j];
                     const double xi = ld0(dx64, d.orig);
-                    hit = exact_within(image_x(g, ld0(S.x, oj), xi, rx), ld0(S.y, oj), ld0(S.z, oj),
-                                       xi, ld0(dy64, d.orig), ld0(dz64, d.orig), d.radius2);
+                    hit = exact_within(EXT ? image_x(g, ld0(S.x, oj), xi, rx) : ld0(S.x, oj),
+                                       ld0(S.y, oj), ld0(S.z, oj), xi, ld0(dy64, d.orig),
+                                       ld0(dz64, d.orig), d.radius2);
                 }
                 bool listed = hit || r2 < d.r2list;
-                if (g.symmetric && !hit && r2 <= g.reach2) {
+                if (EXT && g.symmetric && !hit && r2 <= g.reach2) {
                     bool in_list;
                     hit = reverse_within(g, S, j, r2, rx, dx64, dy64, dz64, d.orig, in_list);
                     listed = listed || hit || in_list;
                 }
                 if (listed) fn(j, rx, ry, rz, code_yz + (int)dxc, hit);
             }
+            };
+            if (!EXT || !g.periodic) {
+                visit(tlo, thi, 0);
+            } else {
+                const int a0 = d.cx + tlo, a1 = d.cx + thi;
+                if (a0 < 0) visit(a0 + g.nx - d.cx, min(a1, -1) + g.nx - d.cx, -1);
+                visit(max(a0, 0) - d.cx, min(a1, g.nx - 1) - d.cx, 0);
+                if (a1 >= g.nx) visit(max(a0, g.nx) - g.nx - d.cx, a1 - g.nx - d.cx, 1);
             }
         }
     }
