@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // 2: one simulation with the extended search (periodic x or variable-h
 // symmetric lists), kept apart so the other modes carry none of its state.
 template <int KX, bool UH, int MODE>
-__global__ void __launch_bounds__(kPairBlock, (UH && MODE == 0) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
+__global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n) return;
     const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
