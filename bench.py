@@ -286,6 +286,7 @@ def run_gpu(args):
         pg.barrier()
     torch.cuda.synchronize()
     launches0 = native.launch_count()
+    builds0 = cm.build_stats()
     integ.stage_events = []
     step_ms = []
     t_begin = time.monotonic()
@@ -305,6 +306,7 @@ def run_gpu(args):
     clocks.mark(t_begin, time.monotonic())
     clk = clocks.stop()
     builds = cm.build_stats()
+    builds = (builds[0] - builds0[0], builds[1] - builds0[1])
     events = integ.stage_events
     integ.stage_events = None
     t_total = sum(step_ms) / 1e3
@@ -362,7 +364,7 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "steps_per_s": 1.0 / step_s,
         "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
-        "nnps_builds": {"full": builds[0], "light": builds[1],
+        "nnps_builds": {"timed_full": builds[0], "timed_light": builds[1],
                         "skin": "list skin %.3g of the search radius" % _skin()},
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT,

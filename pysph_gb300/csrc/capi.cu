@@ -77,15 +77,17 @@ int sph_ctx_create(int dim, sph_ctx **out) {
     cudaError_t e;
     if ((e = cudaMalloc(&c->d_box, 8 * sizeof(int))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_hmax, 2 * sizeof(unsigned long long))) != cudaSuccess ||
-        (e = cudaMalloc(&c->d_err, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_status, kStatusWords * sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess ||
-        (e = cudaMallocHost(&c->h_maxcnt, kMaxListSlots * sizeof(int))) != cudaSuccess) {
+        (e = cudaMallocHost(&c->h_status, kStatusWords * sizeof(unsigned))) != cudaSuccess) {
         sph_ctx_destroy(c);
         return cuda_check(e, "sph_ctx_create");
     }
-    cudaMemset(c->d_err, 0, sizeof(unsigned));
+    cudaMemset(c->d_status, 0, kStatusWords * sizeof(unsigned));
+    c->d_err = c->d_status;
+    c->d_disp = c->d_status + 1;
     *out = c;
     return SPH_OK;
 }
@@ -100,11 +102,11 @@ int sph_ctx_destroy(sph_ctx *c) {
         cudaFree(A.nrm); cudaFree(A.tan);
         cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0); cudaFree(A.inv);
     }
-    cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_err); cudaFree(c->d_disp);
+    cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_status);
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);
     if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_red) cudaFreeHost(c->h_red);
-    if (c->h_maxcnt) cudaFreeHost(c->h_maxcnt);
+    if (c->h_status) cudaFreeHost(c->h_status);
     delete c;
     return SPH_OK;
 }

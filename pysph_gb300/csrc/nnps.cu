@@ -281,7 +281,7 @@ __global__ void k_invperm(int64_t n, const int *perm, int *inv) {
         inv[perm[s]] = (int)s;
 }
 
-__global__ void k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
+__global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
                         const int *key, const float4 *posm0, float4 *posm, float4 *velh,
                         float4 *st, float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
@@ -553,14 +553,13 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
                              cudaMemcpyDeviceToHost, st));
     SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 10, ctx->d_hmax + 1, sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     {
-        const int rcm = list_maxima_async(ctx);
+        const int rcm = list_maxima_async(ctx);   // with the error word
         if (rcm) return rcm;
     }
     SPH_CUDA(cudaStreamSynchronize(st));
     list_maxima_collect(ctx);
-    unsigned err = (unsigned)ctx->h_box[8];
+    unsigned err = ctx->h_status[0];
     if (err & SPH_EFLAG_JUMP) {
         ctx->built = false;
         return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
@@ -711,9 +710,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
 
     cudaStream_t st = ctx->stream;
-    if (!ctx->d_disp) SPH_CUDA(cudaMalloc(&ctx->d_disp, sizeof(unsigned)));
-    SPH_CUDA(cudaMemsetAsync(ctx->d_disp, 0, sizeof(unsigned), st));
-    SPH_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), st));
+    SPH_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(unsigned), st));  // error word, displacement
     const double inv_cs_ref = 1.0 / cell_size;
     for (int a = 0; a < narrays; ++a) {
         ArraySnap &A = ctx->arrays[a];
@@ -726,10 +723,8 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
     }
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 8, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 9, ctx->d_disp, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     {
-        const int rcm = list_maxima_async(ctx);
+        const int rcm = list_maxima_async(ctx);   // with the error word and displacement
         if (rcm) return rcm;
     }
     SPH_CUDA(cudaStreamSynchronize(st));
@@ -739,15 +734,15 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
     bool overflow = false;
     for (int i = 0; i < (int)ctx->lists.size() && i < kMaxListSlots; ++i) {
         const NbrList &L = ctx->lists[i];
-        if (L.maxcnt && L.build == ctx->build_id && ctx->h_maxcnt[i] > L.cap) overflow = true;
+        if (L.maxcnt && L.build == ctx->build_id && (int)ctx->h_status[2 + i] > L.cap) overflow = true;
     }
-    const unsigned err = (unsigned)ctx->h_box[8];
+    const unsigned err = ctx->h_status[0];
     if (err & SPH_EFLAG_JUMP) {
         ctx->built = false;
         return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
     }
     float disp2;
-    memcpy(&disp2, ctx->h_box + 9, sizeof(float));
+    memcpy(&disp2, ctx->h_status + 1, sizeof(float));
     const float half = 0.5f * ctx->grid.skin;
     if (overflow || (err & kLightHChanged) || !(disp2 < half * half * (1.f - 1e-4f))) {
         // too far for the lists: the refcells already hold this update's cells

@@ -681,7 +681,13 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
         return set_error(SPH_ERR_NOTSUP, "neighbour list: too many source particles for this "
                                          "cell subdivision (use a smaller subdivision)");
     if (!L.maxcnt) {
-        SPH_CUDA(cudaMalloc(&L.maxcnt, sizeof(int)));
+        const int slot = dst * na + src;
+        if (slot < kMaxListSlots) {
+            L.maxcnt = (int *)(ctx->d_status + 2 + slot);
+        } else {
+            SPH_CUDA(cudaMalloc(&L.maxcnt, sizeof(int)));
+            L.own_maxcnt = true;
+        }
         SPH_CUDA(cudaMemsetAsync(L.maxcnt, 0, sizeof(int), ctx->stream));
     }
     // capacity: largest count seen so far plus headroom (dests beyond it are
@@ -747,12 +753,11 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
 }  // namespace
 
 // Queue copies of the lists' largest counts (read at the next build's sync).
+// One copy of the status block (error word, displacement, list maxima).
 int list_maxima_async(sph_ctx *ctx) {
-    const int nl = (int)ctx->lists.size();
-    for (int i = 0; i < nl && i < kMaxListSlots; ++i)
-        if (ctx->lists[i].maxcnt)
-            SPH_CUDA(cudaMemcpyAsync(ctx->h_maxcnt + i, ctx->lists[i].maxcnt, sizeof(int),
-                                     cudaMemcpyDeviceToHost, ctx->stream));
+    const int nl = std::min((int)ctx->lists.size(), kMaxListSlots);
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned) * (2 + nl),
+                             cudaMemcpyDeviceToHost, ctx->stream));
     return SPH_OK;
 }
 
@@ -760,14 +765,14 @@ void list_maxima_collect(sph_ctx *ctx) {
     const int nl = (int)ctx->lists.size();
     for (int i = 0; i < nl && i < kMaxListSlots; ++i)
         if (ctx->lists[i].maxcnt)
-            ctx->lists[i].seen_max = std::max(ctx->lists[i].seen_max, ctx->h_maxcnt[i]);
+            ctx->lists[i].seen_max = std::max(ctx->lists[i].seen_max, (int)ctx->h_status[2 + i]);
 }
 
 void free_lists(sph_ctx *ctx) {
     for (auto &L : ctx->lists) {
         cudaFree(L.nbr);
         cudaFree(L.cnt);
-        cudaFree(L.maxcnt);
+        if (L.own_maxcnt) cudaFree(L.maxcnt);
     }
     ctx->lists.clear();
 }

@@ -28,6 +28,9 @@ namespace sphgb {
 
 constexpr int kPairBlock = 128; // threads per block of the pair kernels
 constexpr int kMaxListSlots = 64; // (dst, src) lists whose maxima are tracked
+// device status block read back with one copy: [0] error word, [1] largest
+// squared displacement (float bits), [2 + i] largest count of list slot i
+constexpr int kStatusWords = 2 + kMaxListSlots;
 
 struct Grid {
     int bx0 = 0, by0 = 0, bz0 = 0; // origin of the dense grid (internal cell coords)
@@ -113,6 +116,7 @@ struct NbrList {
     uint32_t *nbr = nullptr;
     int *cnt = nullptr;
     int *maxcnt = nullptr;   // device: largest count of the last list build
+    bool own_maxcnt = false; // maxcnt allocated apart (lists past the status block)
     int64_t entries = 0;     // allocated entries
     int64_t stride = 0;
     int64_t stride_cap = 0;  // allocated count slots
@@ -143,7 +147,8 @@ struct sph_ctx {
     double cell_size_ref = 0;           // reference cell size of the jump check
     long long build_id = 0;             // incremented by every neighbour build
     std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
-    int *h_maxcnt = nullptr;            // pinned scratch for list maxima
+    unsigned *d_status = nullptr;       // kStatusWords: d_err, d_disp, list maxima
+    unsigned *h_status = nullptr;       // pinned mirror of d_status
     // neighbour-list skin as a fraction of the search radius (0 = none)
     double skin_frac = 0.0;
     double build_radius_scale = 0.0;    // parameters of the last full build
