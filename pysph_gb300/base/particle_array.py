@@ -282,18 +282,32 @@ class ParticleArray:
         return self._props[name][: self.num_real_particles].detach().cpu().numpy()
 
     def get(self, *args, only_real_particles=True):
+        """Host copies of properties (numpy arrays the caller owns).  Device
+        properties are copied into page-locked host buffers on the current
+        stream, all of them before one synchronisation."""
         if len(args) == 0:
             return None
         out = []
+        pending = False
         for a in args:
             self._check_property(a)
             if a in self._props:
                 t = self._props[a]
                 if only_real_particles:
                     t = t[: self.num_real_particles]
-                out.append(t.detach().cpu().numpy())
+                t = t.detach()
+                if t.is_cuda:
+                    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                    h.copy_(t, non_blocking=True)
+                    pending = True
+                    out.append(h)
+                else:
+                    out.append(t)
             else:
                 out.append(self.constants[a])
+        if pending:
+            torch.cuda.current_stream().synchronize()
+        out = [o.numpy() if isinstance(o, torch.Tensor) else o for o in out]
         return out[0] if len(out) == 1 else tuple(out)
 
     def get_device(self, name):
@@ -302,22 +316,34 @@ class ParticleArray:
         return self._props[name]
 
     def set(self, **props):
+        """Copy values into properties.  Host sources in page-locked memory
+        are copied asynchronously on the current stream, all of them before
+        one synchronisation (the caller may reuse its buffers on return)."""
         for p in props:
             self._check_property(p)
+        pending = False
         for p, val in props.items():
             if p in self._props:
                 t = self._props[p]
                 src = val if isinstance(val, torch.Tensor) else torch.as_tensor(
                     np.asarray(val, dtype=_NP[t.dtype]))
-                src = src.to(device=t.device, dtype=t.dtype).reshape(-1)
+                src = src.reshape(-1)
                 if src.numel() != t.numel():
                     raise ValueError("size mismatch setting %s: %d != %d" %
                                      (p, src.numel(), t.numel()))
-                t.copy_(src)
+                if src.device == t.device:
+                    t.copy_(src)
+                elif (not src.is_cuda) and t.is_cuda and src.is_pinned() and src.dtype == t.dtype:
+                    t.copy_(src, non_blocking=True)
+                    pending = True
+                else:
+                    t.copy_(src.to(dtype=t.dtype))
             if p == "tag":
                 self.align_particles()
             if p in ("x", "y", "z"):
                 self.set_dirty(True)
+        if pending:
+            torch.cuda.current_stream().synchronize()
         self.touch()
 
     def get_carray(self, prop):
