@@ -823,8 +823,9 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    # default: 300 timed GPU steps of the 1M-particle lattice (about half a
-    # second, long enough for several clock samples), 20 elsewhere
+    # default: 300 timed GPU steps of the 1M-particle lattice or of the drops
+    # batch (a third to half a second, long enough for several clock
+    # samples), 20 elsewhere
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -847,7 +848,7 @@ def main():
     ap.add_argument("--drop-sample", type=int, default=8)
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 300 if (args.workload == "cube" and args.impl == "gb300") else 20
+        args.steps = 300 if (args.workload in ("cube", "drops") and args.impl == "gb300") else 20
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.workload == "drops":

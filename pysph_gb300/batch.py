@@ -173,7 +173,11 @@ class SimulationBatch:
 
     def set(self, **props):
         """Overwrite whole concatenated properties (all instances, in
-        instance order) from host or device tensors / arrays."""
+        instance order) from host or device tensors / arrays.  Waits for the
+        batch's own stream first (a step may still be using the arrays);
+        copies from page-locked host memory run asynchronously, all of them
+        before one synchronisation."""
+        self.sync()
         for name, val in props.items():
             if name not in self.arrays:
                 raise ValueError("unknown batch property %r" % name)
@@ -181,18 +185,29 @@ class SimulationBatch:
             if t.numel() != self.n:
                 raise ValueError("property %r needs %d values" % (name, self.n))
             self.arrays[name].copy_(t.reshape(-1), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    def _host(self, tensors):
+        """Host copies through page-locked buffers, one synchronisation."""
+        out = []
+        for t in tensors:
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h.copy_(t, non_blocking=True)
+            out.append(h)
+        torch.cuda.current_stream().synchronize()
+        return [h.numpy() for h in out]
 
     def get_all(self, *props):
         """Whole concatenated properties as NumPy arrays (synchronises)."""
         self.sync()
-        out = [self.arrays[p].cpu().numpy() for p in props]
+        out = self._host([self.arrays[p] for p in props])
         return out[0] if len(out) == 1 else tuple(out)
 
     def get(self, k, *props):
         """Properties of instance ``k`` as NumPy arrays (synchronises)."""
         self.sync()
         a, b = int(self.offsets[k]), int(self.offsets[k + 1])
-        out = [self.arrays[p][a:b].cpu().numpy() for p in props]
+        out = self._host([self.arrays[p][a:b] for p in props])
         return out[0] if len(out) == 1 else tuple(out)
 
     @property
