@@ -187,6 +187,8 @@ class Integrator:
         self.stages = []
         self._rates = {}
         self._written = {}
+        # array versions right after a final update that left X0 = X
+        self._x0_versions = None
         # when a list, CUDA events (name, start, end) are recorded around
         # every stage and neighbour build on the current stream
         self.stage_events = None
@@ -224,6 +226,7 @@ class Integrator:
                             calc.dst_writes[k_num].append(k_name)
                         self.k_props[calc.id][k_num].append(k_name)
         self._plans = {}
+        self._x0_versions = None
         self.stages = self._make_plans()
         self._integrated = {}
         for st in self.stages:
@@ -370,7 +373,18 @@ class Integrator:
                     dest.set_dirty(True)
 
     def set_initial_arrays(self):
+        """X0 = X for every integrated property (integrator.py:339-367).
+        Skipped when the last step's final update already left X0 = X and
+        no array changed since."""
+        if self._x0_versions is not None and all(
+                self._x0_versions.get(id(dest)) == dest.version
+                for dest, _ in self._integrated.values()):
+            return
         self._apply("copy")
+
+    def _saved_initial(self):
+        """The final update just wrote X0 = X (its lines save the result)."""
+        self._x0_versions = {id(dest): dest.version for dest, _ in self._integrated.values()}
 
     def reset_current_arrays(self, calcs=None):
         self._apply("reset", calcs=calcs)
@@ -404,6 +418,7 @@ class EulerIntegrator(Integrator):
         self.cstep = 1
         self.eval(self.calcs)
         self._apply("euler", dt)
+        self._saved_initial()
         self._update_particles()
 
 
@@ -423,6 +438,7 @@ class RK2Integrator(Integrator):
         self._update_particles()
         self.eval(self.calcs)
         self._apply("rk2", dt)
+        self._saved_initial()
         self.cstep = 1
         self._update_particles()
 
@@ -450,6 +466,7 @@ class RK4Integrator(Integrator):
         self._update_particles()
         self.eval(self.calcs)
         self._apply("rk4", dt)
+        self._saved_initial()
         self.cstep = 1
         self._update_particles()
 
@@ -472,6 +489,7 @@ class PredictorCorrectorIntegrator(Integrator):
         self.do_step(self.calcs, 0.5 * dt)
         self._update_particles()
         self._apply("pc", dt)
+        self._saved_initial()
         self._update_particles()
         self.cstep = 1
 
