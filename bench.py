@@ -247,6 +247,26 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(value, pg):
+    """The largest of one float per rank (all ranks get it): whole-job time
+    is the slowest replica's.  ``pg`` is torch.distributed or None (one
+    process); the reduction runs on the device of the process group's
+    backend (CUDA for NCCL, the host for gloo)."""
+    if pg is None:
+        return float(value)
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], device=dev, dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(units_per_rank, world, seconds):
+    """Whole-job throughput of independent replicas (weak scaling): the units
+    all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def run_gpu(args):
     import torch
 
@@ -309,11 +329,7 @@ def run_gpu(args):
     builds = (builds[0] - builds0[0], builds[1] - builds0[1])
     events = integ.stage_events
     integ.stage_events = None
-    t_total = sum(step_ms) / 1e3
-    if pg:
-        t = torch.tensor([t_total], device="cuda", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_total = float(t.item())
+    t_total = max_over_ranks(sum(step_ms) / 1e3, pg)
     stage_ms = {}
     for name, a, b in events:
         stage_ms.setdefault(name, []).append(a.elapsed_time(b))
@@ -333,16 +349,12 @@ def run_gpu(args):
         integ.integrate(DT)
         out = pa.get(*fields_out)
     torch.cuda.synchronize()
-    e2e_t = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = max_over_ranks(time.perf_counter() - t0, pg)
     del out
 
     steps = args.steps
-    value = world * pairs_per_step * steps / t_total
-    e2e_value = world * pairs_per_step * e2e_steps / e2e_t
+    value = replicas_value(pairs_per_step * steps, world, t_total)
+    e2e_value = replicas_value(pairs_per_step * e2e_steps, world, e2e_t)
     peak, peak_kind = measured_peaks()
     # dominant kernel by device time
     dom = max(ALG_BYTES, key=lambda k: sum(stage_ms.get(k, [0.0])))
