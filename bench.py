@@ -307,6 +307,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     launches0 = native.launch_count()
     builds0 = cm.build_stats()
+    deferred0 = cm.deferred_stats()
     integ.stage_events = []
     step_ms = []
     t_begin = time.monotonic()
@@ -327,6 +328,8 @@ def run_gpu(args):
     clk = clocks.stop()
     builds = cm.build_stats()
     builds = (builds[0] - builds0[0], builds[1] - builds0[1])
+    deferred = cm.deferred_stats()
+    deferred = (deferred[0] - deferred0[0], deferred[1] - deferred0[1])
     events = integ.stage_events
     integ.stage_events = None
     t_total = max_over_ranks(sum(step_ms) / 1e3, pg)
@@ -377,6 +380,7 @@ def run_gpu(args):
         "steps_per_s": 1.0 / step_s,
         "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
         "nnps_builds": {"timed_full": builds[0], "timed_light": builds[1],
+                        "deferred": deferred[0], "deferred_stale": deferred[1],
                         "skin": "list skin %.3g of the search radius" % _skin()},
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT,

@@ -178,9 +178,25 @@ int sph_ctx_set_periodic(sph_ctx *ctx, int on, double xmin, double xmax);
  * against the previous update) while every particle is within half the
  * skin of its build position, its h unchanged and no list overflowed;
  * otherwise a full sph_nnps_build.  *rebuilt (may be NULL) tells which.
- * Synchronises the stream once. */
+ * Synchronises the stream once, unless the check is deferred (below). */
 int sph_nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
                     double radius_scale, int subdiv, int check_jump, int *rebuilt);
+/* Deferred check of light refreshes (on = 1): sph_nnps_update queues the
+ * refresh and the copy of its status and returns without synchronising
+ * (*rebuilt = 0).  The next sph_density / sph_rates / sph_features launches
+ * its pass first, with a device test that makes the pass return at once
+ * when the refresh found a particle past half the skin, a changed h, a
+ * jump or a list past its capacity; it then reads the status (long since copied) and, in that case,
+ * makes the full build and launches the pass again, or returns
+ * SPH_ERR_JUMP.  Every other entry point of the context reads a pending
+ * status first, synchronously.  Results are those of the synchronous
+ * update; a jump is reported by the first pass after the update instead of
+ * by the update itself.  No reference counterpart (the reference's update
+ * runs on the host, base/cell.pyx:927-962). */
+int sph_ctx_set_deferred(sph_ctx *ctx, int on);
+/* out[0] = deferred light refreshes, out[1] = those of them found stale
+ * (replaced by a full build at their first pass). */
+int sph_nnps_deferred_stats(sph_ctx *ctx, int64_t *out);
 /* out[0] = full builds, out[1] = light refreshes of this context. */
 int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
 

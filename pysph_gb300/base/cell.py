@@ -83,6 +83,10 @@ class CellManager:
         # variable h: the symmetric neighbour relation of
         # VarHNbrParticleLocator (set by NNPSManager(variable_h=True))
         self.symmetric = False
+        # deferred check of light refreshes (set by the integrators): the
+        # update returns without waiting for the device, the next pair pass
+        # reads its verdict
+        self.deferred_check = False
         self._ctx = None
         self._snap_versions = []
         self._build_count = 0
@@ -155,6 +159,8 @@ class CellManager:
             if dom is not None and dom.xtranslate != 0.0:
                 native.check(L.sph_ctx_set_periodic(h, 1, float(dom.xmin), float(dom.xmax)),
                              "sph_ctx_set_periodic")
+            if self.deferred_check:
+                native.check(L.sph_ctx_set_deferred(h, 1), "sph_ctx_set_deferred")
             self._ctx = h
         native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
             torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
@@ -169,6 +175,17 @@ class CellManager:
             if self._ctx is not None:
                 native.check(native.lib().sph_ctx_set_symmetric(self._ctx, 1 if on else 0),
                              "sph_ctx_set_symmetric")
+
+    def set_deferred_check(self, on):
+        """Let updates return before the device has checked a light refresh
+        (a jump is then reported by the next pair pass instead of by the
+        update; results are unchanged)."""
+        on = bool(on)
+        if on != self.deferred_check:
+            self.deferred_check = on
+            if self._ctx is not None:
+                native.check(native.lib().sph_ctx_set_deferred(self._ctx, 1 if on else 0),
+                             "sph_ctx_set_deferred")
 
     def _subdivision(self):
         if self.cell_subdivision is None:
@@ -252,6 +269,15 @@ class CellManager:
             return (0, 0)
         out = (ctypes.c_int64 * 2)()
         native.check(native.lib().sph_nnps_stats(self._ctx, out), "sph_nnps_stats")
+        return (int(out[0]), int(out[1]))
+
+    def deferred_stats(self):
+        """(deferred light refreshes, those found stale at their first pass)."""
+        if self._ctx is None:
+            return (0, 0)
+        out = (ctypes.c_int64 * 2)()
+        native.check(native.lib().sph_nnps_deferred_stats(self._ctx, out),
+                     "sph_nnps_deferred_stats")
         return (int(out[0]), int(out[1]))
 
     def mark_fresh(self, pa):

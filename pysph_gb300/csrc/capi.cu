@@ -81,7 +81,8 @@ int sph_ctx_create(int dim, sph_ctx **out) {
         (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess ||
-        (e = cudaMallocHost(&c->h_status, kStatusWords * sizeof(unsigned))) != cudaSuccess) {
+        (e = cudaMallocHost(&c->h_status, kStatusWords * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->pending_event, cudaEventDisableTiming)) != cudaSuccess) {
         sph_ctx_destroy(c);
         return cuda_check(e, "sph_ctx_create");
     }
@@ -107,19 +108,34 @@ int sph_ctx_destroy(sph_ctx *c) {
     if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_red) cudaFreeHost(c->h_red);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->pending_event) cudaEventDestroy(c->pending_event);
     delete c;
     return SPH_OK;
 }
 
 int sph_ctx_set_stream(sph_ctx *c, void *stream) {
     CHECK_CTX(c);
+    // a gated pass must follow its refresh on the same stream
+    if (c->pending && (cudaStream_t)stream != c->stream) {
+        const int rc = resolve_pending(c);
+        if (rc) return rc;
+    }
     c->stream = (cudaStream_t)stream;
     return SPH_OK;
 }
 
+// Entry points that use the neighbour structure (or move particles) read a
+// pending deferred refresh first.
+#define RESOLVE(c)                              \
+    do {                                        \
+        const int rc_ = resolve_pending(c);     \
+        if (rc_) return rc_;                    \
+    } while (0)
+
 int sph_nnps_build(sph_ctx *c, const sph_array_view *arrays, int narrays, double cell_size,
                    double radius_scale, int subdiv, int check_jump) {
     CHECK_CTX(c);
+    RESOLVE(c);
     return nnps_build(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
 }
 
@@ -129,8 +145,17 @@ int sph_nnps_update(sph_ctx *c, const sph_array_view *arrays, int narrays, doubl
     return nnps_update(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump, rebuilt);
 }
 
+int sph_ctx_set_deferred(sph_ctx *c, int on) {
+    CHECK_CTX(c);
+    if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_deferred: on must be 0 or 1");
+    RESOLVE(c);
+    c->deferred = on;
+    return SPH_OK;
+}
+
 int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
     CHECK_CTX(c);
+    RESOLVE(c);
     if (!(skin_fraction >= 0.0) || skin_fraction > 0.5)
         return set_error(SPH_ERR_ARG, "sph_ctx_set_skin: fraction must be in [0, 0.5]");
     if (skin_fraction != c->skin_frac) {
@@ -142,6 +167,7 @@ int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
 
 int sph_ctx_set_symmetric(sph_ctx *c, int on) {
     CHECK_CTX(c);
+    RESOLVE(c);
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_symmetric: on must be 0 or 1");
     if (on != c->symmetric) {
         c->symmetric = on;
@@ -152,6 +178,7 @@ int sph_ctx_set_symmetric(sph_ctx *c, int on) {
 
 int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
     CHECK_CTX(c);
+    RESOLVE(c);
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_periodic: on must be 0 or 1");
     if (on && !(xmax > xmin))
         return set_error(SPH_ERR_ARG, "sph_ctx_set_periodic: xmax must exceed xmin");
@@ -167,14 +194,25 @@ int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
 int sph_nnps_stats(sph_ctx *c, int64_t *out) {
     CHECK_CTX(c);
     if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_stats: null out");
+    RESOLVE(c);
     out[0] = c->n_full;
     out[1] = c->n_light;
+    return SPH_OK;
+}
+
+int sph_nnps_deferred_stats(sph_ctx *c, int64_t *out) {
+    CHECK_CTX(c);
+    if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_deferred_stats: null out");
+    RESOLVE(c);
+    out[0] = c->n_deferred;
+    out[1] = c->n_deferred_stale;
     return SPH_OK;
 }
 
 int sph_nnps_count(sph_ctx *c, int dst, int src, double radius_scale, int64_t *counts) {
     CHECK_CTX(c);
     if (!counts) return set_error(SPH_ERR_ARG, "sph_nnps_count: null counts");
+    RESOLVE(c);
     return nnps_count(c, dst, src, radius_scale, counts);
 }
 
@@ -182,17 +220,20 @@ int sph_nnps_fill(sph_ctx *c, int dst, int src, double radius_scale, const int64
                   int64_t *index) {
     CHECK_CTX(c);
     if (!offsets || !index) return set_error(SPH_ERR_ARG, "sph_nnps_fill: null output");
+    RESOLVE(c);
     return nnps_fill(c, dst, src, radius_scale, offsets, index);
 }
 
 int sph_nbr_lists(sph_ctx *c, int dst, const int *srcs, int nsrc) {
     CHECK_CTX(c);
+    RESOLVE(c);
     return build_lists(c, dst, srcs, nsrc);
 }
 
 int sph_refresh_state(sph_ctx *c, int array, const sph_array_view *view) {
     CHECK_CTX(c);
     if (!view) return set_error(SPH_ERR_ARG, "sph_refresh_state: null view");
+    RESOLVE(c);
     return refresh_state(c, array, view);
 }
 
@@ -228,11 +269,13 @@ int sph_const_rates(sph_ctx *c, int kind, int64_t n, const int64_t *tag, const d
 
 int sph_integrate(sph_ctx *c, int64_t n, const sph_axpy_line *lines, int nlines) {
     CHECK_CTX(c);
+    RESOLVE(c);
     return launch_integrate(c, n, lines, nlines);
 }
 
 int sph_invariants(sph_ctx *c, const sph_array_view *a, double *out) {
     CHECK_CTX(c);
+    RESOLVE(c);
     return invariants(c, a, out);
 }
 
@@ -310,6 +353,7 @@ int sph_batch_error_word(sph_batch *b, unsigned *out) {
 int sph_error_word(sph_ctx *c, unsigned *out) {
     CHECK_CTX(c);
     if (!out) return set_error(SPH_ERR_ARG, "sph_error_word: null out");
+    RESOLVE(c);
     unsigned h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -322,6 +366,7 @@ int sph_error_word(sph_ctx *c, unsigned *out) {
 int sph_mean_neighbours(sph_ctx *c, int dst, int src, double *out) {
     CHECK_CTX(c);
     if (!out) return set_error(SPH_ERR_ARG, "sph_mean_neighbours: null out");
+    RESOLVE(c);
     if (!c->built || dst < 0 || dst >= (int)c->arrays.size())
         return set_error(SPH_ERR_STATE, "sph_mean_neighbours: no neighbour build");
     int64_t n = c->arrays[dst].n;

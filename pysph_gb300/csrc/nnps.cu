@@ -273,6 +273,17 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
 // of the particle in the cell of that build, the largest squared
 // displacement from the build position, an h other than the build's
 // uniform h, and the jump check against the previous update's cells.
+// status[0] |= flags, status[1] = max(displacement^2 bits), and
+// status[kStaleWord] = kStaleLists when some block saw a displacement of
+// at least stale_thr^(1/2), an h change or a jump (the lists no longer hold
+// every neighbour), or when a list of this build holds more neighbours than
+// its capacity (the re-traversal that completes it needs the build's
+// positions).
+struct ListCaps {
+    int n;                      // lists to check (0: none)
+    int cap[kMaxListSlots];     // capacity, INT_MAX for a list of an older build
+};
+
 constexpr unsigned kLightHChanged = 1u << 8;
 
 __global__ void k_invperm(int64_t n, const int *perm, int *inv) {
@@ -285,9 +296,14 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
                         const int *key, const float4 *posm0, float4 *posm, float4 *velh,
                         float4 *st, float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
-                        double build_h, unsigned *dmax, unsigned *err) {
+                        double build_h, float stale_thr, const __grid_constant__ ListCaps caps,
+                        unsigned *status) {
     float dm = 0.f;
     bool jump = false, hch = false;
+    // list maxima: written by the passes before this launch
+    if (blockIdx.x == 0 && threadIdx.x < caps.n &&
+        (int)status[kListWord0 + threadIdx.x] > caps.cap[threadIdx.x])
+        atomicOr(status + kStaleWord, kStaleLists);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int s = inv[i];
@@ -340,8 +356,9 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
             f |= __shfl_xor_sync(0xffffffffu, f, off);
         }
         if (lane == 0) {
-            if (b > 0.f) atomicMax(dmax, __float_as_uint(b));
-            if (f) atomicOr(err, f);
+            if (b > 0.f) atomicMax(status + 1, __float_as_uint(b));
+            if (f) atomicOr(status, f);
+            if (f || !(b < stale_thr)) atomicOr(status + kStaleWord, kStaleLists);
         }
     }
 }
@@ -691,10 +708,62 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
 // the reference's jump check (cell.pyx:1422-1437) against the previous
 // update.  Falls back to a full build when a particle moved too far, an h
 // changed, the array layout changed, or a list overflowed its capacity.
+namespace {
+
+// Verdict of a light refresh from its status block on the host: an error
+// for a jump; *stale: the lists miss neighbours or a list outgrew its
+// capacity (the word the gated passes test); *overflow: the host's own
+// reading of the capacities (implies *stale, which k_light also sets).
+int light_verdict(sph_ctx *ctx, bool *stale, bool *overflow) {
+    *overflow = false;
+    for (int i = 0; i < (int)ctx->lists.size() && i < kMaxListSlots; ++i) {
+        const NbrList &L = ctx->lists[i];
+        if (L.maxcnt && L.build == ctx->build_id && (int)ctx->h_status[kListWord0 + i] > L.cap)
+            *overflow = true;
+    }
+    *stale = (ctx->h_status[kStaleWord] & kStaleLists) != 0;
+    if (ctx->h_status[0] & SPH_EFLAG_JUMP) {
+        ctx->built = false;
+        return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+int resolve_pending(sph_ctx *ctx, bool *rebuilt) {
+    *rebuilt = false;
+    if (!ctx->pending) return SPH_OK;
+    ctx->pending = false;
+    SPH_CUDA(cudaEventSynchronize(ctx->pending_event));
+    list_maxima_collect(ctx);
+    bool stale, overflow;
+    const int rc = light_verdict(ctx, &stale, &overflow);
+    if (rc) return rc;
+    if (stale) {
+        // the refcells already hold the update's cells
+        ctx->n_deferred_stale += 1;
+        const int rb = nnps_build(ctx, ctx->pending_views.data(), (int)ctx->pending_views.size(),
+                                  ctx->pending_cell_size, ctx->pending_radius_scale,
+                                  ctx->pending_subdiv, 0);
+        if (rb) return rb;
+        *rebuilt = true;
+        return SPH_OK;
+    }
+    // the gated pass has run on valid lists
+    ctx->n_light += 1;
+    return SPH_OK;
+}
+
 int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double cell_size,
                 double radius_scale, int subdiv, int check_jump, int *rebuilt) {
     if (rebuilt) *rebuilt = 1;
-    bool light = ctx->built && ctx->grid.skin > 0.f && narrays == (int)ctx->arrays.size() &&
+    {
+        const int rc = resolve_pending(ctx);
+        if (rc) return rc;
+    }
+    bool light = ctx->built && ctx->grid.skin > 0.f &&
+                 narrays == (int)ctx->arrays.size() &&
                  cell_size == ctx->cell_size_ref && radius_scale == ctx->build_radius_scale &&
                  subdiv == ctx->build_subdiv && arrays != nullptr &&
                  ctx->build_h > 0.0 && (int)ctx->lists.size() <= kMaxListSlots &&
@@ -710,8 +779,17 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
 
     cudaStream_t st = ctx->stream;
-    SPH_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(unsigned), st));  // error word, displacement
+    // error word, displacement, stale flag
+    SPH_CUDA(cudaMemsetAsync(ctx->d_status, 0, 3 * sizeof(unsigned), st));
     const double inv_cs_ref = 1.0 / cell_size;
+    const float half = 0.5f * ctx->grid.skin;
+    const float stale_thr = half * half * (1.f - 1e-4f);
+    ListCaps caps;
+    caps.n = std::min((int)ctx->lists.size(), kMaxListSlots);
+    for (int i = 0; i < caps.n; ++i) {
+        const NbrList &L = ctx->lists[i];
+        caps.cap[i] = (L.maxcnt && L.build == ctx->build_id) ? L.cap : INT_MAX;
+    }
     for (int a = 0; a < narrays; ++a) {
         ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];
@@ -719,7 +797,8 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
             v, ctx->grid, inv_cs_ref, A.inv, A.key, A.posm0, A.posm, A.velh, A.st,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
-            ctx->build_h, ctx->d_disp, ctx->d_err);
+            ctx->build_h, stale_thr, caps, ctx->d_status);
+        caps.n = 0;   // checked once
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
     }
@@ -727,28 +806,29 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         const int rcm = list_maxima_async(ctx);   // with the error word and displacement
         if (rcm) return rcm;
     }
+    for (int a = 0; a < narrays; ++a) ctx->arrays[a].view = arrays[a];
+    if (ctx->deferred) {
+        SPH_CUDA(cudaEventRecord(ctx->pending_event, st));
+        ctx->pending = true;
+        ctx->pending_views.assign(arrays, arrays + narrays);
+        ctx->pending_cell_size = cell_size;
+        ctx->pending_radius_scale = radius_scale;
+        ctx->pending_subdiv = subdiv;
+        ctx->n_deferred += 1;
+        if (rebuilt) *rebuilt = 0;
+        return SPH_OK;
+    }
     SPH_CUDA(cudaStreamSynchronize(st));
     list_maxima_collect(ctx);
     // a list that overflowed its capacity completes itself by re-traversal in
     // the order of its build: it needs the build's positions
-    bool overflow = false;
-    for (int i = 0; i < (int)ctx->lists.size() && i < kMaxListSlots; ++i) {
-        const NbrList &L = ctx->lists[i];
-        if (L.maxcnt && L.build == ctx->build_id && (int)ctx->h_status[2 + i] > L.cap) overflow = true;
-    }
-    const unsigned err = ctx->h_status[0];
-    if (err & SPH_EFLAG_JUMP) {
-        ctx->built = false;
-        return set_error(SPH_ERR_JUMP, "Particle moved by more than one cell width");
-    }
-    float disp2;
-    memcpy(&disp2, ctx->h_status + 1, sizeof(float));
-    const float half = 0.5f * ctx->grid.skin;
-    if (overflow || (err & kLightHChanged) || !(disp2 < half * half * (1.f - 1e-4f))) {
+    bool stale, overflow;
+    const int rc = light_verdict(ctx, &stale, &overflow);
+    if (rc) return rc;
+    if (stale || overflow) {
         // too far for the lists: the refcells already hold this update's cells
         return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, 0);
     }
-    for (int a = 0; a < narrays; ++a) ctx->arrays[a].view = arrays[a];
     ctx->n_light += 1;
     if (rebuilt) *rebuilt = 0;
     return SPH_OK;

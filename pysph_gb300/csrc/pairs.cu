@@ -48,6 +48,7 @@ struct ListArgs {
     int *maxcnt;
     int64_t stride;
     int cap;
+    const unsigned *gate;   // non-null: return at once if *gate (stale lists)
 };
 
 struct DensityArgs {
@@ -66,6 +67,7 @@ struct DensityArgs {
     float co, ro, gamma;
     double *rho_out, *p_out, *cs_out;
     float4 *st_out; // sorted state of the destination (may be null)
+    const unsigned *gate;
 };
 
 struct RatesArgs {
@@ -81,6 +83,7 @@ struct RatesArgs {
     double *acc[3];
     double *pos[3];
     double *drho;
+    const unsigned *gate;
 };
 
 // Destination of thread slot s; false for a non-LocalReal particle.
@@ -138,6 +141,12 @@ __device__ __forceinline__ bool listed_exact(const Grid &g, const SrcDev &S, con
 template <bool BATCH>
 __device__ __forceinline__ const Grid &grid_of(const Grid &single, const DestDev &D, int s) {
     return BATCH ? D.grids[D.sinst[s]] : single;
+}
+
+// A pass launched after a deferred light refresh does nothing when the
+// refresh found the lists stale (the host repeats it after a full build).
+__device__ __forceinline__ bool gated_off(const unsigned *gate) {
+    return gate != nullptr && __ldg(gate) != 0u;
 }
 
 // No per-neighbour data beyond the position record.
@@ -226,6 +235,7 @@ __device__ __forceinline__ void for_listed(const Grid &g, const SrcDev &S, int c
 template <int KX, int MODE>
 __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ ListArgs A) {
     using C = Code<KX>;
+    if (gated_off(A.gate)) return;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int c = 0;
     if (s < A.d.n) {
@@ -256,7 +266,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 template <int KX, bool UH, int MODE>
 __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= A.d.n) return;
+    if (s >= A.d.n || gated_off(A.gate)) return;
     const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
     const bool real = load_dest(g, A.d, (int)s, d);
@@ -371,7 +381,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     constexpr bool MAY_BF = SPEC == 0;
     constexpr bool MAY_DRHO = SPEC == 0;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= A.d.n) return;
+    if (s >= A.d.n || gated_off(A.gate)) return;
     const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
     const bool real = load_dest(g, A.d, (int)s, d);
@@ -518,13 +528,14 @@ struct FeatureArgs {
     float mean[SPH_MLP_NCH], inv_std[SPH_MLP_NCH];
     uint16_t *out_bf;   // [n][192] BF16 by original index (or null)
     float *out_f;       // [n][192] FP32 by original index (or null)
+    const unsigned *gate;
 };
 
 template <int KX, bool EXT>
 __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__ FeatureArgs A) {
     constexpr int NN = SPH_MLP_NNBR, NC = SPH_MLP_NCH;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= A.d.n) return;
+    if (s >= A.d.n || gated_off(A.gate)) return;
     DestPos d;
     const bool real = load_dest(A.g, A.d, (int)s, d);
     float kr2[NN], krx[NN], kry[NN];
@@ -683,7 +694,7 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
     if (!L.maxcnt) {
         const int slot = dst * na + src;
         if (slot < kMaxListSlots) {
-            L.maxcnt = (int *)(ctx->d_status + 2 + slot);
+            L.maxcnt = (int *)(ctx->d_status + kListWord0 + slot);
         } else {
             SPH_CUDA(cudaMalloc(&L.maxcnt, sizeof(int)));
             L.own_maxcnt = true;
@@ -735,6 +746,7 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
         a.maxcnt = L.maxcnt;
         a.stride = L.stride;
         a.cap = L.cap;
+        a.gate = ctx->gate;
         const int b = blocks_for(D.n);
         const bool ext = g.periodic || g.symmetric;
 #define LLAUNCH(K) (ext ? k_nbrlist<K, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
@@ -756,7 +768,7 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
 // One copy of the status block (error word, displacement, list maxima).
 int list_maxima_async(sph_ctx *ctx) {
     const int nl = std::min((int)ctx->lists.size(), kMaxListSlots);
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned) * (2 + nl),
+    SPH_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned) * (kListWord0 + nl),
                              cudaMemcpyDeviceToHost, ctx->stream));
     return SPH_OK;
 }
@@ -765,7 +777,7 @@ void list_maxima_collect(sph_ctx *ctx) {
     const int nl = (int)ctx->lists.size();
     for (int i = 0; i < nl && i < kMaxListSlots; ++i)
         if (ctx->lists[i].maxcnt)
-            ctx->lists[i].seen_max = std::max(ctx->lists[i].seen_max, (int)ctx->h_status[2 + i]);
+            ctx->lists[i].seen_max = std::max(ctx->lists[i].seen_max, (int)ctx->h_status[kListWord0 + i]);
 }
 
 void free_lists(sph_ctx *ctx) {
@@ -791,8 +803,26 @@ int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc) {
     return SPH_OK;
 }
 
-int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
-                   double *rho, double *p, double *cs) {
+namespace {
+
+// A pair pass after a deferred light refresh: launched gated, then the
+// refresh's status is read; if the lists were stale the gated launch did
+// nothing and the pass runs again on the full build that replaced them.
+template <class Pass>
+int gated_pass(sph_ctx *ctx, Pass &&pass) {
+    if (!ctx->pending) return pass();
+    ctx->gate = ctx->d_status + kStaleWord;
+    const int rc = pass();
+    ctx->gate = nullptr;
+    bool rebuilt = false;
+    const int rr = resolve_pending(ctx, &rebuilt);
+    if (rr) return rr;
+    if (rc) return rc;
+    return rebuilt ? pass() : SPH_OK;
+}
+
+int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
+                 double *rho, double *p, double *cs) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "density: no neighbour build");
     const int na = (int)ctx->arrays.size();
     if (dst < 0 || dst >= na || nsrc < 0 || nsrc > SPH_MAX_SOURCES || !prm)
@@ -832,6 +862,7 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     const bool own = rho != nullptr && rho == D.view.rho &&
                      (!prm->tait || (p == D.view.p && cs == D.view.cs));
     a.st_out = own ? D.st : nullptr;
+    a.gate = ctx->gate;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     const bool uh = a.g.uniform_h != 0;
@@ -851,9 +882,9 @@ int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_d
     return SPH_OK;
 }
 
-int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
-                 const sph_rates_params *prm, double *const *acc, double *const *pos,
-                 int accumulate) {
+int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+               const sph_rates_params *prm, double *const *acc, double *const *pos,
+               int accumulate) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "rates: no neighbour build");
     const int na = (int)ctx->arrays.size();
     if (dst < 0 || dst >= na || nterms < 0 || nterms > SPH_MAX_SOURCES || !prm)
@@ -893,6 +924,7 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
         a.pos[c] = pos ? pos[c] : nullptr;
     }
     a.drho = prm->drho_out;
+    a.gate = ctx->gate;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     int spec = 0;
@@ -916,8 +948,8 @@ int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms
     return SPH_OK;
 }
 
-int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
-                    uint16_t *out_bf, float *out_f) {
+int features_pass(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
+                  uint16_t *out_bf, float *out_f) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "features: no neighbour build");
     const int na = (int)ctx->arrays.size();
     if (dst < 0 || dst >= na || src < 0 || src >= na || !prm || (!out_bf && !out_f))
@@ -944,6 +976,7 @@ int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params
     }
     a.out_bf = out_bf;
     a.out_f = out_f;
+    a.gate = ctx->gate;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     const bool ext = a.g.periodic || a.g.symmetric;
@@ -956,6 +989,26 @@ int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params
     count_launch();
     SPH_LAUNCH_CHECK("k_features");
     return SPH_OK;
+}
+
+}  // namespace
+
+int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
+                   double *rho, double *p, double *cs) {
+    return gated_pass(ctx, [&] { return density_pass(ctx, dst, srcs, nsrc, prm, rho, p, cs); });
+}
+
+int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+                 const sph_rates_params *prm, double *const *acc, double *const *pos,
+                 int accumulate) {
+    return gated_pass(ctx, [&] {
+        return rates_pass(ctx, dst, terms, nterms, prm, acc, pos, accumulate);
+    });
+}
+
+int launch_features(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *prm,
+                    uint16_t *out_bf, float *out_f) {
+    return gated_pass(ctx, [&] { return features_pass(ctx, dst, src, prm, out_bf, out_f); });
 }
 
 }  // namespace sphgb

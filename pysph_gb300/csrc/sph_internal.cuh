@@ -29,8 +29,15 @@ namespace sphgb {
 constexpr int kPairBlock = 128; // threads per block of the pair kernels
 constexpr int kMaxListSlots = 64; // (dst, src) lists whose maxima are tracked
 // device status block read back with one copy: [0] error word, [1] largest
-// squared displacement (float bits), [2 + i] largest count of list slot i
-constexpr int kStatusWords = 2 + kMaxListSlots;
+// squared displacement (float bits), [2] stale-list flags of the last light
+// refresh, [3] spare, [kListWord0 + i] largest count of list slot i
+constexpr int kListWord0 = 4;
+constexpr int kStatusWords = kListWord0 + kMaxListSlots;
+// [2]: the lists cannot serve the last light refresh (a particle moved by
+// half the skin, an h changed, a jump, or a list outgrew its capacity);
+// a gated pair pass returns at once
+constexpr unsigned kStaleLists = 1u;
+constexpr int kStaleWord = 2;
 
 struct Grid {
     int bx0 = 0, by0 = 0, bz0 = 0; // origin of the dense grid (internal cell coords)
@@ -147,8 +154,20 @@ struct sph_ctx {
     double cell_size_ref = 0;           // reference cell size of the jump check
     long long build_id = 0;             // incremented by every neighbour build
     std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
-    unsigned *d_status = nullptr;       // kStatusWords: d_err, d_disp, list maxima
+    unsigned *d_status = nullptr;       // kStatusWords: d_err, d_disp, stale, list maxima
     unsigned *h_status = nullptr;       // pinned mirror of d_status
+    // deferred check of a light refresh (sph_ctx_set_deferred): the status
+    // of the refresh is read at the next pair pass, which is launched first
+    // with gate = &d_status[2] (the pass returns at once when the word is
+    // set) and launched again after a full build if it was
+    int deferred = 0;
+    bool pending = false;               // a refresh whose status is not read yet
+    cudaEvent_t pending_event = nullptr; // recorded after the status copy
+    std::vector<sph_array_view> pending_views;
+    double pending_cell_size = 0.0, pending_radius_scale = 0.0;
+    int pending_subdiv = 1;
+    const unsigned *gate = nullptr;     // set while a gated pass is launched
+    long long n_deferred = 0, n_deferred_stale = 0;
     // neighbour-list skin as a fraction of the search radius (0 = none)
     double skin_frac = 0.0;
     double build_radius_scale = 0.0;    // parameters of the last full build
@@ -217,6 +236,13 @@ int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *cou
 int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
               int64_t *index);
 int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view);
+// read the status of a deferred light refresh; *rebuilt: it was stale and a
+// full build replaced it (a gated pass launched since then did nothing)
+int resolve_pending(sph_ctx *ctx, bool *rebuilt);
+inline int resolve_pending(sph_ctx *ctx) {
+    bool rebuilt;
+    return resolve_pending(ctx, &rebuilt);
+}
 int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc,
                    const sph_density_params *prm, double *rho, double *p, double *cs);
 int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,

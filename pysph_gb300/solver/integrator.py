@@ -199,6 +199,10 @@ class Integrator:
     def setup_integrator(self):
         """integrator.py:229-337 bookkeeping plus the stage plan."""
         self.arrays = self.particles.arrays
+        cm = getattr(self.particles, "cell_manager", None)
+        if cm is not None:
+            # every update of a step is followed by its pair passes
+            cm.set_deferred_check(True)
         calcs = self.calcs
         self.pcalcs = [c for c in calcs if c.tag == "position"]
         self.ncalcs = [c for c in calcs if not c.tag == "position"]
