@@ -74,7 +74,7 @@ __global__ void k_bkeys(sph_array_view a, const Grid *grids, const double *inv_c
 }
 
 __global__ void k_breorder(sph_array_view a, const Grid *grids, const int *inst_of,
-                           const int *perm, const int *key, int *skey, int *sinst, float4 *posm,
+                           const int *perm, const int *key, int *skey, int *sinst, float *scx,
                            float4 *velh, float4 *st, float4 *pm) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
          s += (int64_t)gridDim.x * blockDim.x) {
@@ -89,7 +89,7 @@ __global__ void k_breorder(sph_array_view a, const Grid *grids, const int *inst_
         const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
         const float xi = (float)fma(-ox, g.cs, ld0(a.x, i)), yi = (float)fma(-oy, g.cs, ld0(a.y, i)),
                     zi = (float)fma(-oz, g.cs, ld0(a.z, i));
-        posm[s] = make_float4(xi, yi, zi, (float)cx);
+        scx[s] = (float)cx;
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
                               (float)a.h[i]);
         const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i), m = (float)a.m[i];
@@ -117,7 +117,7 @@ int batch_build(sph_batch *b, int check_jump) {
                              cudaMemcpyDeviceToDevice, st));
     launch_counting_sort(st, n, b->total_cells, A.key, A.cursor, A.cstart, A.perm);
     k_breorder<<<nb, kThreads, 0, st>>>(b->view, b->d_grids, b->inst_of, A.perm, A.key, A.skey,
-                                        b->sinst, A.posm, A.velh, A.st, A.pm);
+                                        b->sinst, A.scx, A.velh, A.st, A.pm);
     count_launch();
     SPH_LAUNCH_CHECK("k_breorder");
     b->steps_built += 1;
@@ -201,7 +201,7 @@ int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instanc
     SPH_CUDA(cudaMalloc(&A.key, sizeof(int) * n));
     SPH_CUDA(cudaMalloc(&A.perm, sizeof(int) * n));
     SPH_CUDA(cudaMalloc(&A.skey, sizeof(int) * n));
-    SPH_CUDA(cudaMalloc(&A.posm, sizeof(float4) * n));
+    SPH_CUDA(cudaMalloc(&A.scx, sizeof(float) * n));
     SPH_CUDA(cudaMalloc(&A.pm, sizeof(float4) * n));
     SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * n));
     SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * n));
@@ -367,7 +367,7 @@ int batch_pair_counts(sph_batch *b, unsigned long long *out) {
 void batch_free(sph_batch *b) {
     if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
     ArraySnap &A = b->snap;
-    cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey); cudaFree(A.posm); cudaFree(A.pm); cudaFree(A.velh);
+    cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey); cudaFree(A.scx); cudaFree(A.pm); cudaFree(A.velh);
     cudaFree(A.st); cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell);
     cudaFree(b->d_grids); cudaFree(b->d_inv_ref); cudaFree(b->inst_of); cudaFree(b->sinst);
     cudaFree(b->list.nbr); cudaFree(b->list.cnt); cudaFree(b->list.maxcnt);

@@ -99,9 +99,9 @@ int sph_ctx_destroy(sph_ctx *c) {
     free_lists(c);
     for (auto &A : c->arrays) {
         cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
-        cudaFree(A.posm); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st);
+        cudaFree(A.scx); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st);
         cudaFree(A.nrm); cudaFree(A.tan);
-        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.posm0); cudaFree(A.inv);
+        cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.pm0); cudaFree(A.inv);
     }
     cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_status);
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);

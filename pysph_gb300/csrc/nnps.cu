@@ -242,7 +242,7 @@ __global__ void k_cellsort(int64_t ncells, const int *cstart, int *perm) {
 // sorted snapshot
 // -------------------------------------------------------------------------
 __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *key, int *skey,
-                          float4 *posm, float4 *velh, float4 *st, float4 *nrm, float4 *tan,
+                          float *scx, float4 *velh, float4 *st, float4 *nrm, float4 *tan,
                           float4 *pm) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
          s += (int64_t)gridDim.x * blockDim.x) {
@@ -255,7 +255,7 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
         float xi = (float)fma(-ox, g.cs, bin_x(g, ld0(a.x, i)));
         float yi = (float)fma(-oy, g.cs, ld0(a.y, i));
         float zi = (float)fma(-oz, g.cs, ld0(a.z, i));
-        posm[s] = make_float4(xi, yi, zi, (float)cx);
+        scx[s] = (float)cx;
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i),
                               (float)a.h[i]);
         float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i), m = (float)a.m[i];
@@ -293,7 +293,7 @@ __global__ void k_invperm(int64_t n, const int *perm, int *inv) {
 }
 
 __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
-                        const int *key, const float4 *posm0, float4 *posm, float4 *velh,
+                        const int *key, const float4 *pm0, float4 *velh,
                         float4 *st, float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
                         double build_h, float stale_thr, const __grid_constant__ ListCaps caps,
@@ -314,10 +314,9 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         const float xi = (float)fma(-ox, g.cs, bin_x(g, px));
         const float yi = (float)fma(-oy, g.cs, py);
         const float zi = (float)fma(-oz, g.cs, pz);
-        const float4 p0 = posm0[s];
+        const float4 p0 = pm0[s];
         const float ddx = xi - p0.x, ddy = yi - p0.y, ddz = zi - p0.z;
         dm = fmaxf(dm, fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)));
-        posm[s] = make_float4(xi, yi, zi, (float)cx);
         const double h = a.h[i];
         if (h != build_h) hch = true;
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), (float)h);
@@ -331,9 +330,12 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         const double pp[3] = {px, py, pz};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
+            // the reference cell rarely changes between updates: store only
+            // a change (no write-back of unchanged lines)
             const int c = floor_cell(pp[d], inv_cs_ref);
-            if (check_jump && abs(c - refcell[3 * i + d]) > 1) jump = true;
-            refcell[3 * i + d] = c;
+            const int c0 = refcell[3 * i + d];
+            if (check_jump && abs(c - c0) > 1) jump = true;
+            if (c != c0) refcell[3 * i + d] = c;
         }
     }
     // warp, then block, then one atomic per block
@@ -451,15 +453,16 @@ int ensure(T **p, int64_t &cap, int64_t need) {
 int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
     if (n <= A.cap && A.perm && (!nrm || A.nrm)) return SPH_OK;
     cudaFree(A.key); cudaFree(A.perm); cudaFree(A.skey);
-    cudaFree(A.posm); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st); cudaFree(A.nrm);
+    cudaFree(A.scx); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st); cudaFree(A.nrm);
     cudaFree(A.tan);
     A.key = A.perm = A.skey = nullptr;
-    A.posm = A.pm = A.velh = A.st = A.nrm = A.tan = nullptr;
+    A.scx = nullptr;
+    A.pm = A.velh = A.st = A.nrm = A.tan = nullptr;
     int64_t c = std::max<int64_t>(n, 1);
     SPH_CUDA(cudaMalloc(&A.key, sizeof(int) * c));
     SPH_CUDA(cudaMalloc(&A.perm, sizeof(int) * c));
     SPH_CUDA(cudaMalloc(&A.skey, sizeof(int) * c));
-    SPH_CUDA(cudaMalloc(&A.posm, sizeof(float4) * c));
+    SPH_CUDA(cudaMalloc(&A.scx, sizeof(float) * c));
     SPH_CUDA(cudaMalloc(&A.pm, sizeof(float4) * c));
     SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * c));
     SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * c));
@@ -670,22 +673,22 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
             int nb = grid_blocks(v.n, kThreads);
             k_scatter<<<nb, kThreads, 0, st>>>(v.n, A.key, A.cursor, A.perm);
             k_cellsort<<<grid_blocks(g.ncells, kThreads), kThreads, 0, st>>>(g.ncells, A.cstart, A.perm);
-            k_reorder<<<nb, kThreads, 0, st>>>(v, g, A.perm, A.key, A.skey, A.posm, A.velh, A.st,
+            k_reorder<<<nb, kThreads, 0, st>>>(v, g, A.perm, A.key, A.skey, A.scx, A.velh, A.st,
                                                A.has_nrm ? A.nrm : nullptr,
                                                A.has_nrm ? A.tan : nullptr, A.pm);
             count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
             if (g.skin > 0.f) {
-                if (A.posm0_cap < v.n) {
-                    cudaFree(A.posm0);
+                if (A.pm0_cap < v.n) {
+                    cudaFree(A.pm0);
                     cudaFree(A.inv);
-                    A.posm0 = nullptr;
+                    A.pm0 = nullptr;
                     A.inv = nullptr;
-                    SPH_CUDA(cudaMalloc(&A.posm0, sizeof(float4) * v.n));
+                    SPH_CUDA(cudaMalloc(&A.pm0, sizeof(float4) * v.n));
                     SPH_CUDA(cudaMalloc(&A.inv, sizeof(int) * v.n));
-                    A.posm0_cap = v.n;
+                    A.pm0_cap = v.n;
                 }
-                SPH_CUDA(cudaMemcpyAsync(A.posm0, A.posm, sizeof(float4) * v.n,
+                SPH_CUDA(cudaMemcpyAsync(A.pm0, A.pm, sizeof(float4) * v.n,
                                          cudaMemcpyDeviceToDevice, st));
                 k_invperm<<<grid_blocks(v.n, kThreads), kThreads, 0, st>>>(v.n, A.perm, A.inv);
                 count_launch();
@@ -772,7 +775,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         const ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];
         if (v.n != A.n || v.n != A.ref_n || (v.n > 0 && (!v.x || !v.h || !v.m)) ||
-            (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && (!A.posm0 || !A.inv)))
+            (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && (!A.pm0 || !A.inv)))
             light = false;
     }
     if (!light)
@@ -795,7 +798,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         const sph_array_view &v = arrays[a];
         if (v.n == 0) continue;
         k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
-            v, ctx->grid, inv_cs_ref, A.inv, A.key, A.posm0, A.posm, A.velh, A.st,
+            v, ctx->grid, inv_cs_ref, A.inv, A.key, A.pm0, A.velh, A.st,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
             ctx->build_h, stale_thr, caps, ctx->d_status);
         caps.n = 0;   // checked once
@@ -847,7 +850,7 @@ int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
     A.has_nrm = nrm;
     if (A.n == 0) return SPH_OK;
     k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
-        A.view, ctx->grid, A.perm, A.key, A.skey, A.posm, A.velh, A.st, nrm ? A.nrm : nullptr,
+        A.view, ctx->grid, A.perm, A.key, A.skey, A.scx, A.velh, A.st, nrm ? A.nrm : nullptr,
         nrm ? A.tan : nullptr, A.pm);
     count_launch();
     SPH_LAUNCH_CHECK("k_reorder (refresh)");

@@ -30,7 +30,7 @@ namespace sphgb {
 namespace {
 
 struct DestDev {
-    const float4 *posm, *velh, *st;
+    const float4 *pm, *velh, *st;
     const int *skey, *perm;
     const int *sinst;    // batches: instance of each sorted slot
     const Grid *grids;   // batches: grid of each instance
@@ -91,7 +91,7 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
     const int orig = D.perm[s];
     d.orig = orig;
     if (D.tag != nullptr && D.tag[orig] != SPH_TAG_LOCAL_REAL) return false;
-    const float4 p = D.posm[s];
+    const float4 p = D.pm[s];
     d.xi_x = p.x; d.xi_y = p.y; d.xi_z = p.z;
     decode_cell(g, D.skey[s], d.cx, d.cy, d.cz);
     const double radius = __dmul_rn(D.h[orig], g.radius_scale);
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__
 
 DestDev make_dest(const ArraySnap &D) {
     DestDev d;
-    d.posm = D.posm; d.velh = D.velh; d.st = D.st;
+    d.pm = D.pm; d.velh = D.velh; d.st = D.st;
     d.skey = D.skey; d.perm = D.perm;
     d.sinst = nullptr; d.grids = nullptr;
     d.tag = D.view.tag;
@@ -643,7 +643,7 @@ DestDev make_dest(const ArraySnap &D) {
 
 SrcDev make_src(const ArraySnap &S) {
     SrcDev s{};
-    s.posm = S.posm; s.velh = S.velh; s.st = S.st; s.nrm = S.nrm; s.tan = S.tan; s.pm = S.pm;
+    s.velh = S.velh; s.st = S.st; s.nrm = S.nrm; s.tan = S.tan; s.pm = S.pm; s.scx = S.scx;
     s.cstart = S.cstart; s.perm = S.perm;
     s.x = S.view.x; s.y = S.view.y; s.z = S.view.z; s.h = S.view.h;
     return s;

@@ -5,9 +5,10 @@
 //   sorted order (context-owned, cell-major, deterministic within a cell):
 //     perm[s]  -> original index of sorted slot s          int32
 //     skey[s]  -> dense-grid cell of slot s                int32
-//     posm[s]  =  (xi_x, xi_y, xi_z, cx)  cell-local FP32 offsets, dense x cell
-//     pm[s]    =  (xi_x, xi_y, xi_z, m)   the same offsets with the mass: the
-//                 one 16-byte record per neighbour of the list-streaming passes
+//     pm[s]    =  (xi_x, xi_y, xi_z, m)   cell-local FP32 offsets and mass: the
+//                 one 16-byte record per neighbour of the pair passes
+//     scx[s]   =  cx                       dense x cell (FP32, exact), fixed
+//                 between full builds
 //     velh[s]  =  (u, v, w, h)                              FP32
 //     st[s]    =  (rho, p/rho^2, cs, m)                     FP32
 //     nrm[s], tan[s] (walls only)
@@ -103,16 +104,17 @@ struct ArraySnap {
     int *key = nullptr;   // original order, dense cell index
     int *perm = nullptr;  // sorted -> original
     int *skey = nullptr;  // sorted: cell
-    float4 *posm = nullptr, *velh = nullptr, *st = nullptr, *nrm = nullptr, *tan = nullptr;
+    float4 *velh = nullptr, *st = nullptr, *nrm = nullptr, *tan = nullptr;
     float4 *pm = nullptr;
+    float *scx = nullptr;   // sorted: dense x cell
     int *cstart = nullptr; // ncells + 1
     int *cursor = nullptr; // ncells
     int64_t cell_cap = 0;
     int *refcell = nullptr; // original order, 3 ints per particle (jump check)
     int64_t ref_n = -1;     // particle count the refcell entries belong to
-    float4 *posm0 = nullptr; // posm at the last full build (skin lists)
+    float4 *pm0 = nullptr; // pm at the last full build (skin lists)
     int *inv = nullptr;      // original -> sorted slot of the last full build
-    int64_t posm0_cap = 0;
+    int64_t pm0_cap = 0;
 };
 
 // Neighbour list of one (destination, source) pair of arrays: entry k of
@@ -354,7 +356,8 @@ __device__ __forceinline__ double ld0(const double *p, int64_t i) { return p ? p
 // Per-source view used by the pair kernels.
 
 struct SrcDev {
-    const float4 *posm, *velh, *st, *nrm, *tan, *pm;
+    const float4 *velh, *st, *nrm, *tan, *pm;
+    const float *scx;
     const int *cstart, *perm;
     const double *x, *y, *z, *h;
     const uint32_t *nbr;   // k-major neighbour list of (dest, this source)
@@ -437,7 +440,7 @@ struct DestPos {
 // band around the threshold; inside it the FP64 test of base/nnps.pyx:
 // 337-353 decides, so the set is exactly the reference's.  With a list skin
 // (d.r2list > 0) the sources within the list radius that are not neighbours
-// are visited too, with exact = false.  posm[j].w holds the source's
+// are visited too, with exact = false.  scx[j] holds the source's
 // dense-grid x cell.
 template <int KX, bool EXT, class Fn>
 __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
@@ -479,8 +482,8 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             const int hi = __ldg(cst + c0 + rhi + 1);
             const float wshift = (float)(wrap * g.nx);
             for (int j = lo; j < hi; ++j) {
-                const float4 pj = __ldg(S.posm + j);
-                const float dxc = (pj.w + wshift) - cxf;  // exact: small integers in FP32
+                const float4 pj = __ldg(S.pm + j);
+                const float dxc = (__ldg(S.scx + j) + wshift) - cxf;  // exact: small integers in FP32
                 const float rx = fmaf(-dxc, csf, d.xi_x - pj.x);
                 const float ry = by - pj.y, rz = bz - pj.z;
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
