@@ -15,6 +15,7 @@ import itertools
 import numpy as np
 import torch
 
+from . import transfer
 from .carray import BaseArray, DoubleArray, IntArray, LongArray
 from .particle_types import ParticleType
 
@@ -345,6 +346,27 @@ class ParticleArray:
         if pending:
             torch.cuda.current_stream().synchronize()
         self.touch()
+
+    # -- staged host transfers (overlap the link with stepping) ----------------
+    def upload(self, **props):
+        """Start copying host values (page-locked tensors or arrays; others
+        are staged through a page-locked copy) to device buffers on a copy
+        stream and return a ``StagedUpload`` at once.  Page-locked sources
+        must stay unchanged until ``set_staged`` has been called with it."""
+        return transfer.upload(self, props)
+
+    def set_staged(self, up):
+        """``set`` with the values of an earlier ``upload``: the current
+        stream waits for its copies, then copies them into the properties on
+        the device (no host synchronisation)."""
+        transfer.set_staged(self, up)
+
+    def download(self, *names, only_real_particles=True):
+        """Start reading properties back: a device snapshot on the current
+        stream, copied to page-locked host buffers on a copy stream.  Returns
+        a ``StagedDownload``; its ``result()`` waits for those copies and
+        returns NumPy arrays as ``get`` does."""
+        return transfer.download(self, names, only_real_particles)
 
     def get_carray(self, prop):
         if prop in self._props:

@@ -79,9 +79,12 @@ int sph_ctx_create(int dim, sph_ctx **out) {
         (e = cudaMalloc(&c->d_hmax, 2 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_status, kStatusWords * sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&c->d_part, sizeof(double) * red_part_doubles())) != cudaSuccess ||
-        (e = cudaMallocHost(&c->h_box, 16 * sizeof(int))) != cudaSuccess ||
+        (e = cudaHostAlloc(&c->h_box, 16 * sizeof(int), cudaHostAllocMapped)) != cudaSuccess ||
         (e = cudaMallocHost(&c->h_red, 16 * sizeof(double))) != cudaSuccess ||
-        (e = cudaMallocHost(&c->h_status, kStatusWords * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaHostAlloc(&c->h_status, kStatusWords * sizeof(unsigned), cudaHostAllocMapped)) !=
+            cudaSuccess ||
+        (e = cudaHostGetDevicePointer((void **)&c->hd_box, c->h_box, 0)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer((void **)&c->hd_status, c->h_status, 0)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->pending_event, cudaEventDisableTiming)) != cudaSuccess) {
         sph_ctx_destroy(c);
         return cuda_check(e, "sph_ctx_create");

@@ -116,6 +116,11 @@ __global__ void k_box(sph_array_view a, double inv_cs, double inv_cs_ref, int *r
     }
 }
 
+__global__ void k_publish(const unsigned *src, unsigned *dst, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+    __threadfence_system();
+}
+
 __global__ void k_box_init(int *box, unsigned long long *hmax) {
     if (threadIdx.x < 3) {
         box[threadIdx.x] = INT_MAX;
@@ -476,6 +481,14 @@ int alloc_array(ArraySnap &A, int64_t n, bool nrm) {
 
 }  // namespace
 
+int publish_words(sph_ctx *ctx, const void *src, void *dst, int nwords) {
+    if (nwords <= 0) return SPH_OK;
+    k_publish<<<1, 128, 0, ctx->stream>>>((const unsigned *)src, (unsigned *)dst, nwords);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_publish");
+    return SPH_OK;
+}
+
 int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
     int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     int rc = ensure(&ctx->scan_tmp, ctx->scan_tmp_cap, ntiles);
@@ -568,11 +581,11 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
         count_launch();
         SPH_LAUNCH_CHECK("k_box");
     }
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box, ctx->d_box, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 6, ctx->d_hmax, sizeof(unsigned long long),
-                             cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_box + 10, ctx->d_hmax + 1, sizeof(unsigned long long),
-                             cudaMemcpyDeviceToHost, st));
+    {
+        int rcp = publish_words(ctx, ctx->d_box, ctx->hd_box, 6);
+        if (!rcp) rcp = publish_words(ctx, ctx->d_hmax, ctx->hd_box + 6, 4);   // hmax, hmin
+        if (rcp) return rcp;
+    }
     {
         const int rcm = list_maxima_async(ctx);   // with the error word
         if (rcm) return rcm;
@@ -590,7 +603,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
 
     double hmax, hmin;
     memcpy(&hmax, ctx->h_box + 6, sizeof(hmax));
-    memcpy(&hmin, ctx->h_box + 10, sizeof(hmin));
+    memcpy(&hmin, ctx->h_box + 8, sizeof(hmin));
     Grid g;
     g.periodic = pg.periodic;
     g.pxmin = pg.pxmin;

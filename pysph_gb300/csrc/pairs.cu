@@ -764,13 +764,12 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
 
 }  // namespace
 
-// Queue copies of the lists' largest counts (read at the next build's sync).
-// One copy of the status block (error word, displacement, list maxima).
+// Queue the publication of the status block (error word, displacement,
+// stale flag, list maxima) to its mapped host mirror, read after the next
+// synchronisation.
 int list_maxima_async(sph_ctx *ctx) {
     const int nl = std::min((int)ctx->lists.size(), kMaxListSlots);
-    SPH_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned) * (kListWord0 + nl),
-                             cudaMemcpyDeviceToHost, ctx->stream));
-    return SPH_OK;
+    return publish_words(ctx, ctx->d_status, ctx->hd_status, kListWord0 + nl);
 }
 
 void list_maxima_collect(sph_ctx *ctx) {

@@ -146,7 +146,11 @@ struct sph_ctx {
     int *d_box = nullptr;               // [6] internal-cell min xyz, max xyz
     unsigned long long *d_hmax = nullptr;
     unsigned *d_err = nullptr;
-    int *h_box = nullptr;               // pinned mirror: box[6], hmax bits (2 ints), err
+    // host mirrors written by kernels through mapped page-locked memory (no
+    // copy engine: a read-back of the caller's data on a copy stream cannot
+    // delay them): box[6], hmax bits (2 words), hmin bits (2 words)
+    int *h_box = nullptr;
+    int *hd_box = nullptr;              // device address of h_box
     int *scan_tmp = nullptr;
     int64_t scan_tmp_cap = 0;
     double *d_part = nullptr;           // reduction partials
@@ -157,7 +161,8 @@ struct sph_ctx {
     long long build_id = 0;             // incremented by every neighbour build
     std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
     unsigned *d_status = nullptr;       // kStatusWords: d_err, d_disp, stale, list maxima
-    unsigned *h_status = nullptr;       // pinned mirror of d_status
+    unsigned *h_status = nullptr;       // mapped mirror of d_status
+    unsigned *hd_status = nullptr;      // device address of h_status
     // deferred check of a light refresh (sph_ctx_set_deferred): the status
     // of the refresh is read at the next pair pass, which is launched first
     // with gate = &d_status[2] (the pass returns at once when the word is
@@ -290,6 +295,9 @@ int mlp_targets(int64_t n, const double *ax, const double *ay, const double *h, 
                 const double *mean, const double *inv_std, float *out, cudaStream_t st);
 void batch_free(sph_batch *b);
 int list_maxima_async(sph_ctx *ctx);
+// copy nwords 32-bit words from device memory to a mapped host mirror
+// (device address dst) with a one-block kernel on the context's stream
+int publish_words(sph_ctx *ctx, const void *src, void *dst, int nwords);
 void list_maxima_collect(sph_ctx *ctx);
 void free_lists(sph_ctx *ctx);
 

@@ -2,6 +2,7 @@
 expansion, calc validation errors, the integrator's stage plan."""
 import numpy as np
 import pytest
+import torch
 
 import pysph_gb300
 from pysph_gb300 import workloads as W
@@ -172,3 +173,19 @@ def test_periodic_domain_translate_rules():
     with pytest.raises(NotImplementedError):
         base.CellManager(arrays_to_bin=[pa], periodic_domain=base.PeriodicDomain(ymin=0, ymax=1),
                          initialize=False)
+
+
+def test_staged_transfers_check_their_arguments():
+    pa = base.get_particle_array(name="f", x=np.zeros(4), y=np.zeros(4))
+    with pytest.raises(ValueError):
+        pa.upload()
+    with pytest.raises(ValueError):
+        pa.download()
+    with pytest.raises(AttributeError):
+        pa.upload(q=np.zeros(4))
+    if not torch.cuda.is_available():
+        # host-resident arrays (no GPU): the staged forms need device arrays
+        with pytest.raises(RuntimeError):
+            pa.upload(x=np.ones(4))
+        with pytest.raises(RuntimeError):
+            pa.download("x")
