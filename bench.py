@@ -45,9 +45,9 @@ DT = 1e-4
 
 # Algorithmic bytes per particle per launch (FP32 snapshot reads + FP64
 # outputs the interface requires; neighbour re-reads excluded):
-#   rates:   posm+velh+st 48 B read, FP64 velocity 24 B read (position
+#   rates:   pm+velh+st 48 B read, FP64 velocity 24 B read (position
 #            stepping), FP64 rates 48 B written                    = 120 B
-#   density: posm+velh 32 B read, FP64 rho,p,cs 24 B + st 16 B written = 72 B
+#   density: pm+velh 32 B read, FP64 rho,p,cs 24 B + st 16 B written = 72 B
 ALG_BYTES = {"RatesStage": 120.0, "DensityStage": 72.0, "ListStage": 8.0}
 # Survey algorithmic bytes of a whole RK2 step per particle (3D)
 STEP_ALG_BYTES = 694.0
@@ -57,7 +57,7 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
 # of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md,
 # list-streaming passes); the traffic grows with the particle count, so it is scaled by n
-NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 420.0, "RatesStage": 451.0}
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 405.0, "RatesStage": 436.0}
 
 
 def measured_peaks():
