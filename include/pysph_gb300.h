@@ -76,6 +76,10 @@ typedef struct {
 #define SPH_TERM_XSPH 4u    /* XSPHCorrection                 */
 #define SPH_TERM_BFORCE 8u  /* MonaghanBoundaryForce          */
 #define SPH_TERM_DRHO 16u   /* SPHDensityRate (density_funcs.pyx:89-158): drho += m_j v_ij . grad W */
+/* SPHVelocityDivergence (adke_funcs.pyx:152-226, hks off): div_i = (1/rho_i)
+ * sum m_j (v_j - v_i) . grad W(r_ij, (h_i + h_j)/2), written to drho_out;
+ * not combined with SPH_TERM_DRHO in one launch */
+#define SPH_TERM_VDIV 32u
 /* MomentumEquation (pressure_funcs.pyx:106-252) is PGRAD | AVISC with its own
  * eta (it stores eta, unlike MonaghanArtificialVsicosity) */
 
@@ -91,6 +95,10 @@ typedef struct {
     int dim;              /* kernel dimension 1..3                              */
     int tait;             /* 1: also compute p, cs by the Tait equation           */
     double co, ro, gamma; /* Tait parameters                                    */
+    double h0;            /* > 0: W at this fixed h for every pair, over the
+                           * neighbours of the particles' own radius
+                           * (ADKEPilotRho, adke_funcs.pyx:15-73); 0: the
+                           * particles' own h (SPHRho)                          */
 } sph_density_params;
 
 typedef struct {
@@ -233,6 +241,22 @@ int sph_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
 
 int sph_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, double co,
              double ro, double gamma, double *p_out, double *cs_out);
+
+/* ADKESmoothingUpdate.eval (sph/funcs/adke_funcs.pyx:118-147): over the
+ * LocalReal particles among the first n, log g = (sum of log rhop) / nreal,
+ * then h_out = h0 k (g / rhop)^eps for each of them (others untouched).  The
+ * logarithms are summed in FP64 in a fixed order, so the result does not
+ * depend on the launch; every step is rounded as the reference's C (no
+ * fused multiply-add). */
+int sph_adke_smoothing(sph_ctx *ctx, int64_t n, int64_t nreal, const int64_t *tag,
+                       const double *rhop, double h0, double k, double eps, double *h_out);
+
+/* ADKEConductionCoeffUpdate.eval (adke_funcs.pyx:256-291): for the
+ * LocalReal particles among the first nreal, q_out = (g1 cs + g2 h
+ * (|div| - div)) h (others untouched), rounded as the reference's C. */
+int sph_adke_conduction(sph_ctx *ctx, int64_t nreal, const int64_t *tag, const double *cs,
+                        const double *h, const double *div, double g1, double g2,
+                        double *q_out);
 
 /* kind 0: out_k = g_k (GravityForce); kind 1: out_k = (u, v, w)_k of src
  * (PositionStepping).  nout outputs, non-LocalReal get 0. */

@@ -16,6 +16,7 @@ Reference routines restated here (paths relative to ``source/pysph``):
 * the per-function pair sums and the neighbour search -- see the C file.
 """
 import ctypes
+import math
 import os
 import platform
 import subprocess
@@ -72,6 +73,8 @@ def lib():
             L.orc_xsph.argtypes = [P, P, vp, vp, i, d, i, vp, vp, vp]
             L.orc_momentum.argtypes = [P, P, vp, vp, i, d, d, d, i, vp, vp, vp]
             L.orc_drho.argtypes = [P, P, vp, vp, i, vp]
+            L.orc_pilot_rho.argtypes = [P, P, vp, vp, i, d, vp]
+            L.orc_vdiv.argtypes = [P, P, vp, vp, i, vp]
             L.orc_bforce.argtypes = [P, P, vp, vp, d, vp, vp, vp]
             L.orc_const3.argtypes = [P, d, d, d, i, vp, vp, vp]
             L.orc_position_stepping.argtypes = [P, i, vp, vp, vp]
@@ -152,6 +155,13 @@ def pair_sum(kind, dst, src, offsets, index, dim, params=None, nout=3):
     if kind == "drho":
         L.orc_drho(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, o[0])
         return outs[:1]
+    if kind == "pilotrho":
+        L.orc_pilot_rho(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim,
+                        ctypes.c_double(params["h0"]), o[0])
+        return outs[:1]
+    if kind == "vdiv":
+        L.orc_vdiv(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, o[0])
+        return outs[:1]
     if kind == "pgrad":
         L.orc_pgrad(D.ref, S.ref, off.ctypes.data, idx.ctypes.data, dim, nout, *o)
     elif kind == "avisc":
@@ -170,6 +180,45 @@ def pair_sum(kind, dst, src, offsets, index, dim, params=None, nout=3):
     else:
         raise ValueError(kind)
     return outs[:nout]
+
+
+def adke_smoothing(dst, h0, k=1.0, eps=0.0, nreal=None):
+    """ADKESmoothingUpdate.eval (sph/funcs/adke_funcs.pyx:118-147): new h of
+    the LocalReal particles (0 for the others, which SPHCalc.sph zeroes);
+    the logarithms are summed in index order as the reference's loop does."""
+    rhop = np.asarray(dst["rhop"], np.float64)
+    n = rhop.size
+    tag = np.asarray(dst.get("tag", np.zeros(n, np.int64)))
+    nreal = n if nreal is None else nreal
+    log_g = 0.0
+    for i in range(n):
+        if tag[i] == 0:
+            log_g += math.log(rhop[i])
+    log_g /= nreal
+    g = math.exp(log_g)
+    out = np.zeros(n)
+    for i in range(n):
+        if tag[i] == 0:
+            out[i] = h0 * k * (g / rhop[i]) ** eps
+    return out
+
+
+def adke_conduction(dst, g1, g2, nreal=None):
+    """ADKEConductionCoeffUpdate.eval (adke_funcs.pyx:256-291):
+    q = (g1 cs + g2 h (|div| - div)) h over the LocalReal particles among the
+    first nreal (0 for the others)."""
+    h = np.asarray(dst["h"], np.float64)
+    n = h.size
+    tag = np.asarray(dst.get("tag", np.zeros(n, np.int64)))
+    cs = np.asarray(dst["cs"], np.float64)
+    div = np.asarray(dst["div"], np.float64)
+    nreal = n if nreal is None else nreal
+    out = np.zeros(n)
+    for i in range(nreal):
+        if tag[i] == 0:
+            o = g1 * cs[i] + (g2 * h[i] * (abs(div[i]) - div[i]))
+            out[i] = o * h[i]
+    return out
 
 
 def tait(dst, co, ro, gamma=7.0):
@@ -222,7 +271,8 @@ class Op:
     # the function tags of the reference (sph/funcs/*.pyx ``self.tag``)
     TAGS = {"rho": "density", "drho": "density", "tait": "state", "pgrad": "velocity",
             "avisc": "velocity", "momentum": "velocity", "bforce": "velocity",
-            "gravity": "velocity", "step": "position", "xsph": "position"}
+            "gravity": "velocity", "step": "position", "xsph": "position",
+            "pilotrho": "pilotrho", "adke_h": "h", "vdiv": "vdivergence", "adke_q": "q"}
 
     def __init__(self, kind, dest, updates, sources=(), integrates=False, **params):
         self.kind = kind
@@ -290,6 +340,11 @@ class Problem:
         if op.kind == "tait":
             p, cs = tait(d, op.params["co"], op.params["ro"], op.params.get("gamma", 7.0))
             return [p, cs]
+        if op.kind == "adke_h":
+            return [adke_smoothing(d, op.params["h0"], op.params.get("k", 1.0),
+                                   op.params.get("eps", 0.0))]
+        if op.kind == "adke_q":
+            return [adke_conduction(d, op.params.get("g1", 0.0), op.params.get("g2", 0.0))]
         if op.kind == "gravity":
             D = _Arr(d)
             tmp = [np.zeros(n) for _ in range(3)]
@@ -319,6 +374,10 @@ class Problem:
             else:
                 for upd, r in zip(op.updates, res):
                     self.arrays[op.dest][upd] = r
+                if "h" in op.updates:
+                    # new smoothing lengths: the calc re-bins (sph_calc.pyx:
+                    # 262-263 after adke_funcs.pyx:145-147)
+                    self._moved()
 
     def _integrating(self):
         return [(ci, op) for ci, op in enumerate(self.ops) if op.integrates]

@@ -395,6 +395,46 @@ void orc_drho(const orc_array *d, const orc_array *s, const int64_t *off, const 
     }
 }
 
+/* ADKEPilotRho: sph/funcs/adke_funcs.pyx:41-73 -- rhop_a += m_b W(r_ab, h0)
+ * over the neighbours of the destination's own radius (CSPH, no correction) */
+void orc_pilot_rho(const orc_array *d, const orc_array *s, const int64_t *off,
+                   const int64_t *idx, int dim, double h0, double *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < d->n; ++i) {
+        if (!is_real(d, i)) { out[i] = 0; continue; }
+        double nr = 0.0;
+        for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+            int64_t j = idx[k];
+            double w = orc_cubic_w(dim, get0(d->x, i), get0(d->y, i), get0(d->z, i),
+                                   get0(s->x, j), get0(s->y, j), get0(s->z, j), h0);
+            nr += w * s->m[j];
+        }
+        out[i] += nr;
+    }
+}
+
+/* SPHVelocityDivergence: sph/funcs/adke_funcs.pyx:175-226 (hks off) --
+ * div_a += (1/rho_a) m_b (v_b - v_a) . grad W(r_ab, (h_a + h_b)/2)          */
+void orc_vdiv(const orc_array *d, const orc_array *s, const int64_t *off, const int64_t *idx,
+              int dim, double *o0) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < d->n; ++i) {
+        if (!is_real(d, i)) { o0[i] = 0; continue; }
+        double nr = 0;
+        for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+            int64_t j = idx[k];
+            double hab = 0.5 * (d->h[i] + s->h[j]);
+            double vx = get0(s->u, j) - get0(d->u, i), vy = get0(s->v, j) - get0(d->v, i),
+                   vz = get0(s->w, j) - get0(d->w, i);
+            double g[3];
+            orc_cubic_grad(dim, get0(d->x, i), get0(d->y, i), get0(d->z, i), get0(s->x, j),
+                           get0(s->y, j), get0(s->z, j), hab, g);
+            nr += (1.0 / d->rho[i]) * s->m[j] * (g[0] * vx + g[1] * vy + g[2] * vz);
+        }
+        o0[i] += nr;
+    }
+}
+
 /* XSPHCorrection: sph/funcs/xsph_funcs.pyx:31-88 (CSPH, no correction) */
 void orc_xsph(const orc_array *d, const orc_array *s, const int64_t *off,
               const int64_t *idx, int dim, double eps, int nout, double *o0, double *o1,

@@ -132,6 +132,10 @@ int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instanc
     if (rec->subdiv < 1 || rec->subdiv > 3) return set_error(SPH_ERR_ARG, "batch: subdiv must be 1..3");
     if (rec->scheme != 0 && rec->scheme != 1) return set_error(SPH_ERR_ARG, "batch: scheme 0 (Euler) or 1 (RK2)");
     if (rec->dim < 1 || rec->dim > 3) return set_error(SPH_ERR_ARG, "batch: dim must be 1..3");
+    if (rec->density.h0 != 0.0)
+        return set_error(SPH_ERR_NOTSUP, "batch: the density pass runs at the particles' own h");
+    if (rec->term.flags & SPH_TERM_VDIV)
+        return set_error(SPH_ERR_NOTSUP, "batch: no velocity divergence term");
     int64_t covered = 0;
     for (int k = 0; k < ninst; ++k) {
         if (inst[k].offset != covered || inst[k].n <= 0)

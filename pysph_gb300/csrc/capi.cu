@@ -263,6 +263,19 @@ int sph_tait(sph_ctx *c, int64_t n, const double *rho, const int64_t *tag, doubl
     return launch_tait(c, n, rho, tag, co, ro, gamma, p_out, cs_out);
 }
 
+int sph_adke_smoothing(sph_ctx *c, int64_t n, int64_t nreal, const int64_t *tag,
+                       const double *rhop, double h0, double k, double eps, double *h_out) {
+    CHECK_CTX(c);
+    return launch_adke_smoothing(c, n, nreal, tag, rhop, h0, k, eps, h_out);
+}
+
+int sph_adke_conduction(sph_ctx *c, int64_t nreal, const int64_t *tag, const double *cs,
+                        const double *h, const double *div, double g1, double g2,
+                        double *q_out) {
+    CHECK_CTX(c);
+    return launch_adke_conduction(c, nreal, tag, cs, h, div, g1, g2, q_out);
+}
+
 int sph_const_rates(sph_ctx *c, int kind, int64_t n, const int64_t *tag, const double *g3,
                     const double *u, const double *v, const double *w, int nout,
                     double *const *out) {

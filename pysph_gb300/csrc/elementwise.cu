@@ -140,7 +140,81 @@ __global__ void k_invariants_final(const double *part, int nb, double *out) {
     }
 }
 
+// ADKESmoothingUpdate.eval (adke_funcs.pyx:118-147), first pass: per-block
+// FP64 sums of log(rhop) over LocalReal particles (fixed grid, fixed order).
+__global__ void k_adke_logsum(int64_t n, const int64_t *tag, const double *rhop, double *part) {
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (real_tag(tag, i)) s = __dadd_rn(s, log(rhop[i]));
+    __shared__ double sh[kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, off));
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x = __dadd_rn(x, sh[w]);
+        part[blockIdx.x] = x;
+    }
+}
+
+// second pass: every block sums the partials in the same order (the same g
+// everywhere), then h = h0 k (g / rhop)^eps
+__global__ void k_adke_h(int64_t n, const int64_t *tag, const double *rhop, const double *part,
+                         int nb, double nreal, double h0k, double eps, double *h) {
+    __shared__ double g_s;
+    if (threadIdx.x == 0) {
+        double x = 0.0;
+        for (int b = 0; b < nb; ++b) x = __dadd_rn(x, part[b]);
+        g_s = exp(__ddiv_rn(x, nreal));
+    }
+    __syncthreads();
+    const double g = g_s;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (real_tag(tag, i)) h[i] = __dmul_rn(h0k, pow(__ddiv_rn(g, rhop[i]), eps));
+}
+
+// ADKEConductionCoeffUpdate.eval (adke_funcs.pyx:256-291)
+__global__ void k_adke_q(int64_t nreal, const int64_t *tag, const double *cs, const double *h,
+                         const double *div, double g1, double g2, double *q) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nreal;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (!real_tag(tag, i)) continue;
+        const double ha = h[i], d = div[i];
+        const double t = __dmul_rn(__dmul_rn(g2, ha), __dsub_rn(fabs(d), d));
+        q[i] = __dmul_rn(__dadd_rn(__dmul_rn(g1, cs[i]), t), ha);
+    }
+}
+
 }  // namespace
+
+int launch_adke_smoothing(sph_ctx *ctx, int64_t n, int64_t nreal, const int64_t *tag,
+                          const double *rhop, double h0, double k, double eps, double *h) {
+    if (n < 0 || nreal < 0 || nreal > n || (n > 0 && (!rhop || !h)))
+        return set_error(SPH_ERR_ARG, "adke_smoothing: bad arguments");
+    if (n == 0) return SPH_OK;
+    k_adke_logsum<<<kRedBlocks, kThreads, 0, ctx->stream>>>(n, tag, rhop, ctx->d_part);
+    k_adke_h<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(
+        n, tag, rhop, ctx->d_part, kRedBlocks, (double)nreal, h0 * k, eps, h);
+    count_launch(2);
+    SPH_LAUNCH_CHECK("k_adke_h");
+    return SPH_OK;
+}
+
+int launch_adke_conduction(sph_ctx *ctx, int64_t nreal, const int64_t *tag, const double *cs,
+                           const double *h, const double *div, double g1, double g2,
+                           double *q) {
+    if (nreal < 0 || (nreal > 0 && (!cs || !h || !div || !q)))
+        return set_error(SPH_ERR_ARG, "adke_conduction: bad arguments");
+    if (nreal == 0) return SPH_OK;
+    k_adke_q<<<grid_blocks(nreal, kThreads), kThreads, 0, ctx->stream>>>(nreal, tag, cs, h, div,
+                                                                       g1, g2, q);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_adke_q");
+    return SPH_OK;
+}
 
 int launch_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, double co,
                 double ro, double gamma, double *p, double *cs) {

@@ -35,7 +35,7 @@ struct DestDev {
     const int *sinst;    // batches: instance of each sorted slot
     const Grid *grids;   // batches: grid of each instance
     const int64_t *tag;
-    const double *x, *y, *z, *u, *v, *w, *h, *p;
+    const double *x, *y, *z, *u, *v, *w, *h, *p, *rho;
     int64_t n;
 };
 
@@ -68,6 +68,7 @@ struct DensityArgs {
     double *rho_out, *p_out, *cs_out;
     float4 *st_out; // sorted state of the destination (may be null)
     const unsigned *gate;
+    float ih0;      // > 0: 1 / the fixed h of every pair (pilot density)
 };
 
 struct RatesArgs {
@@ -84,6 +85,7 @@ struct RatesArgs {
     double *pos[3];
     double *drho;
     const unsigned *gate;
+    int vdiv;       // the drho sum is a velocity divergence: store -sum / rho_i
 };
 
 // Destination of thread slot s; false for a non-LocalReal particle.
@@ -279,7 +281,9 @@ __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_densi
         const float hi = A.d.velh[s].w;
         const int dim = A.dim;
         const bool uh = UH;
-        const float ihi = __fdividef(1.f, hi);
+        // a fixed h for every pair (pilot density): the variable-h kernels only
+        const bool fixed = !UH && A.ih0 > 0.f;
+        const float ihi = fixed ? A.ih0 : __fdividef(1.f, hi);
         const float faci = cubic_fac(dim, ihi);
         float part = 0.f;
         for (int si = 0; si < A.nsrc; ++si) {
@@ -299,7 +303,7 @@ __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_densi
                         if (!exact) return;
                         const float mj = S.pm[j].w;
                         float ih = ihi, fac = faci;
-                        if (!uh) {
+                        if (!uh && !fixed) {
                             ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
                             fac = cubic_fac(dim, ih);
                         }
@@ -313,11 +317,11 @@ __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_densi
                 if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.lmax[si], wmax);
                 continue;
             }
-            // with variable h, W at the mean h can reach past the radius of h_i
+            // with variable h (or a fixed h), W can reach past the radius of h_i
             for_listed<KX, (UH && MODE == 0) ? 6 : 4, MODE == 2>(g, S, A.cap[si], A.stride[si], (int)s, d, A.d, !uh, NoExtra(),
                 [&](bool ok, int j, float rx, float ry, float rz, float mj, int) {
                     float ih = ihi, fac = faci;
-                    if (!uh) {
+                    if (!uh && !fixed) {
                         ih = __fdividef(1.f, 0.5f * (hi + S.velh[j].w));
                         fac = cubic_fac(dim, ih);
                     }
@@ -435,8 +439,9 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
                     pay = fmaf(gf, ry, pay);
                     paz = fmaf(gf, rz, paz);
                 }
-                if (MAY_DRHO && (fl & SPH_TERM_DRHO)) {
-                    // drho_i += m_j (v_i - v_j) . grad W(hab)  (density_funcs.pyx:117-158)
+                if (MAY_DRHO && (fl & (SPH_TERM_DRHO | SPH_TERM_VDIV))) {
+                    // drho_i += m_j (v_i - v_j) . grad W(hab)  (density_funcs.pyx:117-158);
+                    // the velocity divergence is -sum / rho_i (adke_funcs.pyx:175-226)
                     const float dot = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
                     pdr = fmaf(cubic_gfac(q, ih, rinv) * fac * mj * okf, dot, pdr);
                 }
@@ -507,7 +512,11 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
         if (A.acc[c]) A.acc[c][orig] = (A.accumulate ? A.acc[c][orig] : 0.0) + a3[c];
         if (A.pos[c]) A.pos[c][orig] = (A.accumulate ? A.pos[c][orig] : 0.0) + p3[c];
     }
-    if (A.drho) A.drho[orig] = (A.accumulate ? A.drho[orig] : 0.0) + (real ? dr.value() : 0.0);
+    if (A.drho) {
+        double r = real ? dr.value() : 0.0;
+        if (A.vdiv && real) r = -r / A.d.rho[orig];
+        A.drho[orig] = (A.accumulate ? A.drho[orig] : 0.0) + r;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -637,6 +646,7 @@ DestDev make_dest(const ArraySnap &D) {
     d.u = D.view.u; d.v = D.view.v; d.w = D.view.w;
     d.h = D.view.h;
     d.p = D.view.p;
+    d.rho = D.view.rho;
     d.n = D.n;
     return d;
 }
@@ -862,9 +872,12 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
                      (!prm->tait || (p == D.view.p && cs == D.view.cs));
     a.st_out = own ? D.st : nullptr;
     a.gate = ctx->gate;
+    if (prm->h0 < 0.0) return set_error(SPH_ERR_ARG, "density: h0 must be >= 0");
+    a.ih0 = prm->h0 > 0.0 ? (float)(1.0 / prm->h0) : 0.f;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
-    const bool uh = a.g.uniform_h != 0;
+    // a fixed h (pilot density) runs in the variable-h kernels
+    const bool uh = a.g.uniform_h != 0 && a.ih0 == 0.f;
     const bool ext = a.g.periodic || a.g.symmetric;
 #define DLAUNCH(K) (ext ? (uh ? k_density<K, true, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                               : k_density<K, false, 2><<<b, kPairBlock, 0, ctx->stream>>>(a)) \
@@ -924,6 +937,18 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
     }
     a.drho = prm->drho_out;
     a.gate = ctx->gate;
+    {
+        bool drho = false, vdiv = false;
+        for (int i = 0; i < nterms; ++i) {
+            drho = drho || (terms[i].flags & SPH_TERM_DRHO);
+            vdiv = vdiv || (terms[i].flags & SPH_TERM_VDIV);
+        }
+        if (drho && vdiv)
+            return set_error(SPH_ERR_ARG, "rates: density rate and velocity divergence in one launch");
+        if (vdiv && !D.view.rho)
+            return set_error(SPH_ERR_ARG, "rates: velocity divergence needs the destination's rho");
+        a.vdiv = vdiv ? 1 : 0;
+    }
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     int spec = 0;

@@ -250,6 +250,11 @@ inline int resolve_pending(sph_ctx *ctx) {
     bool rebuilt;
     return resolve_pending(ctx, &rebuilt);
 }
+int launch_adke_smoothing(sph_ctx *ctx, int64_t n, int64_t nreal, const int64_t *tag,
+                          const double *rhop, double h0, double k, double eps, double *h);
+int launch_adke_conduction(sph_ctx *ctx, int64_t nreal, const int64_t *tag, const double *cs,
+                           const double *h, const double *div, double g1, double g2,
+                           double *q);
 int launch_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc,
                    const sph_density_params *prm, double *rho, double *p, double *cs);
 int launch_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,

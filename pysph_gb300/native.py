@@ -23,6 +23,7 @@ TERM_AVISC = 2
 TERM_XSPH = 4
 TERM_BFORCE = 8
 TERM_DRHO = 16
+TERM_VDIV = 32
 
 MAX_SOURCES = 8
 MAX_AXPY_LINES = 12
@@ -35,6 +36,7 @@ EXPORTS = (
     "sph_ctx_create", "sph_ctx_destroy", "sph_ctx_set_stream", "sph_last_error",
     "sph_version", "sph_nnps_build", "sph_nnps_count", "sph_nnps_fill",
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
+    "sph_adke_smoothing", "sph_adke_conduction",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
     "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
     "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
@@ -83,7 +85,7 @@ class SourceTerm(ctypes.Structure):
 
 class DensityParams(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int), ("tait", ctypes.c_int), ("co", ctypes.c_double),
-                ("ro", ctypes.c_double), ("gamma", ctypes.c_double)]
+                ("ro", ctypes.c_double), ("gamma", ctypes.c_double), ("h0", ctypes.c_double)]
 
 
 class RatesParams(ctypes.Structure):
@@ -173,6 +175,8 @@ def load_library(build_if_missing=True):
         L.sph_density.argtypes = [vp, i32, P(i32), i32, P(DensityParams), vp, vp, vp]
         L.sph_rates.argtypes = [vp, i32, P(SourceTerm), i32, P(RatesParams), P(vp), P(vp), i32]
         L.sph_tait.argtypes = [vp, i64, vp, vp, d, d, d, vp, vp]
+        L.sph_adke_smoothing.argtypes = [vp, i64, i64, vp, vp, d, d, d, vp]
+        L.sph_adke_conduction.argtypes = [vp, i64, vp, vp, vp, vp, d, d, vp]
         L.sph_const_rates.argtypes = [vp, i32, i64, vp, P(d), vp, vp, vp, i32, P(vp)]
         L.sph_integrate.argtypes = [vp, i64, P(AxpyLine), i32]
         L.sph_invariants.argtypes = [vp, P(ArrayView), P(d)]

@@ -14,7 +14,8 @@ from ..base.cell import SNAPSHOT_PROPS, array_view
 
 RATE_TERM = {"pgrad": native.TERM_PGRAD, "avisc": native.TERM_AVISC,
              "xsph": native.TERM_XSPH, "bforce": native.TERM_BFORCE,
-             "momentum": native.TERM_PGRAD | native.TERM_AVISC, "drho": native.TERM_DRHO}
+             "momentum": native.TERM_PGRAD | native.TERM_AVISC, "drho": native.TERM_DRHO,
+             "vdiv": native.TERM_VDIV}
 
 
 def _p(t):
@@ -45,16 +46,17 @@ def nbr_lists(cm, dest, sources):
     native.check(L.sph_nbr_lists(cm.context(), cm.slot(dest), srcs, len(sources)), "lists")
 
 
-def density(cm, dest, sources, dim, rho_out, tait=None, p_out=None, cs_out=None):
+def density(cm, dest, sources, dim, rho_out, tait=None, p_out=None, cs_out=None, h0=0.0):
     """Summation density of ``dest`` from ``sources`` into ``rho_out``;
-    with ``tait=(co, ro, gamma)`` also p and cs."""
+    with ``tait=(co, ro, gamma)`` also p and cs; with ``h0 > 0`` the kernel
+    at that fixed h (the ADKE pilot density)."""
     cm.ensure_current()
     L = native.lib()
     ctx = cm.context()
     srcs = (ctypes.c_int * max(1, len(sources)))(*[cm.slot(s) for s in sources])
     prm = native.DensityParams(dim=int(dim), tait=1 if tait else 0,
                                co=tait[0] if tait else 0.0, ro=tait[1] if tait else 1.0,
-                               gamma=tait[2] if tait else 7.0)
+                               gamma=tait[2] if tait else 7.0, h0=float(h0))
     native.check(L.sph_density(ctx, cm.slot(dest), srcs, len(sources), ctypes.byref(prm),
                                _p(rho_out), _p(p_out), _p(cs_out)), "SPHRho")
 
@@ -93,6 +95,30 @@ def tait(cm, dest, co, ro, gamma, p_out, cs_out):
     native.check(L.sph_tait(ctx, dest.get_number_of_particles(), _p(dest.get_device("rho")),
                             _p(dest.get_device("tag")), co, ro, gamma, _p(p_out), _p(cs_out)),
                  "TaitEquation")
+
+
+def _prop(pa, name, why):
+    if not pa.has_array(name):
+        raise AttributeError("%s needs property %s of %s" % (why, name, pa.name))
+    return pa.get_device(name)
+
+
+def adke_smoothing(cm, dest, h0, k, eps, h_out):
+    """ADKESmoothingUpdate: h_out of the LocalReal particles from ``rhop``."""
+    ctx = cm.context()
+    rhop = _prop(dest, "rhop", "ADKESmoothingUpdate")
+    native.check(native.lib().sph_adke_smoothing(
+        ctx, dest.get_number_of_particles(), dest.num_real_particles,
+        _p(dest.get_device("tag")), _p(rhop), h0, k, eps, _p(h_out)), "ADKESmoothingUpdate")
+
+
+def adke_conduction(cm, dest, g1, g2, q_out):
+    """ADKEConductionCoeffUpdate: q_out of the LocalReal particles."""
+    ctx = cm.context()
+    args = [_prop(dest, p, "ADKEConductionCoeffUpdate") for p in ("cs", "h", "div")]
+    native.check(native.lib().sph_adke_conduction(
+        ctx, dest.num_real_particles, _p(dest.get_device("tag")), *[_p(a) for a in args],
+        g1, g2, _p(q_out)), "ADKEConductionCoeffUpdate")
 
 
 def const_rates(cm, dest, kind, outs, g=None):

@@ -14,7 +14,7 @@ from . import gpu
 
 logger = logging.getLogger()
 
-PAIR_KINDS = ("rho", "pgrad", "avisc", "xsph", "bforce", "momentum", "drho")
+PAIR_KINDS = ("rho", "pgrad", "avisc", "xsph", "bforce", "momentum", "drho", "pilotrho", "vdiv")
 RATE_KINDS = ("pgrad", "avisc", "xsph", "bforce", "momentum", "drho")
 
 
@@ -54,10 +54,26 @@ def run_functions(particles_cm, dest, funcs, kernel, outs, accumulate=False):
     nout = funcs[0].num_outputs
     outs = list(outs[:nout]) + [None] * (3 - min(3, nout))
     targets = outs
-    if accumulate and kind in ("rho", "tait", "gravity", "step"):
+    if accumulate and kind in ("rho", "pilotrho", "tait", "gravity", "step"):
         targets = [None if o is None else torch.empty_like(o) for o in outs]
     if kind == "rho":
         gpu.density(cm, dest, [f.source for f in funcs], kernel.dim, targets[0])
+    elif kind == "pilotrho":
+        gpu.density(cm, dest, [f.source for f in funcs], kernel.dim, targets[0],
+                    h0=funcs[0].h0)
+    elif kind in ("adke_h", "adke_q"):
+        # the reference's eval assigns the LocalReal entries; SPHCalc.sph has
+        # zeroed the outputs first
+        f = funcs[0]
+        if targets[0] is None:
+            raise ValueError("%s needs one output" % type(f).__name__)
+        if not accumulate:
+            targets[0].zero_()
+        if kind == "adke_h":
+            gpu.adke_smoothing(cm, dest, f.h0, f.k, f.eps, targets[0])
+            dest.set_dirty(True)    # new neighbours are needed (adke_funcs.pyx:145-147)
+        else:
+            gpu.adke_conduction(cm, dest, f.g1, f.g2, targets[0])
     elif kind == "tait":
         f = funcs[0]
         if targets[0] is None or targets[1] is None:
@@ -72,8 +88,12 @@ def run_functions(particles_cm, dest, funcs, kernel, outs, accumulate=False):
         terms = [_term(f, kind) for f in funcs]
         if kind == "xsph":
             gpu.rates(cm, dest, terms, kernel.dim, pos=targets, accumulate=accumulate)
-        elif kind == "drho":
+        elif kind in ("drho", "vdiv"):
             gpu.rates(cm, dest, terms, kernel.dim, drho=targets[0], accumulate=accumulate)
+            if not accumulate:
+                for o in targets[1:nout]:
+                    if o is not None:
+                        o.zero_()
         else:
             gpu.rates(cm, dest, terms, kernel.dim, acc=targets, accumulate=accumulate)
     if targets is not outs:

@@ -289,6 +289,92 @@ class GravityForce(SPHFunction):
         self.gz = float(gz)
 
 
+# ---------------------------------------------------------------------------
+# ADKE: Sigalotti's adaptive kernel estimation (sph/funcs/adke_funcs.pyx)
+# ---------------------------------------------------------------------------
+
+class ADKEPilotRho(CSPHFunctionParticle):
+    """Pilot density sum m_b W(x_a - x_b, h0) at a fixed h0, over the
+    neighbours of the destination's own radius (adke_funcs.pyx:15-73)."""
+
+    gpu_kind = "pilotrho"
+
+    def __init__(self, source, dest, setup_arrays=True, h0=1.0, **kwargs):
+        SPHFunctionParticle.__init__(self, source, dest, True, **kwargs)
+        self.h0 = float(h0)
+        if not self.h0 > 0.0:
+            raise ValueError("ADKEPilotRho: h0 must be positive")
+        self.id = "pilotrho"
+        self.tag = "pilotrho"
+        self.num_outputs = 1
+
+    def set_src_dst_reads(self):
+        self.src_reads = ["x", "y", "z", "m", "rho"]
+        self.dst_reads = ["x", "y", "z", "tag"]
+
+
+class ADKESmoothingUpdate(SPHFunction):
+    """h_a = h0 k (g / rhop_a)^eps with log g the mean of log rhop over the
+    LocalReal particles (adke_funcs.pyx:78-147); marks the array dirty, since
+    new neighbours are needed."""
+
+    gpu_kind = "adke_h"
+
+    def __init__(self, source, dest, setup_arrays=True, k=1.0, eps=0.0, h0=1.0, **kwargs):
+        SPHFunction.__init__(self, source, dest, setup_arrays)
+        self.dest = dest if dest is not None else source
+        self.k = float(k)
+        self.eps = float(eps)
+        self.h0 = float(h0)
+        self.id = "adke_smoothing_update"
+        self.tag = "h"
+        self.num_outputs = 1
+
+    def set_src_dst_reads(self):
+        self.src_reads = []
+        self.dst_reads = ["rhop"]
+
+
+class SPHVelocityDivergence(SPHFunctionParticle):
+    """(1/rho_a) sum m_b (v_b - v_a) . grad W(r_ab, (h_a + h_b)/2)
+    (adke_funcs.pyx:152-226).  Like the reference class it keeps
+    SPHFunction's three outputs (the second and third stay zero)."""
+
+    gpu_kind = "vdiv"
+
+    def __init__(self, source, dest, setup_arrays=True, **kwargs):
+        SPHFunctionParticle.__init__(self, source, dest, True, **kwargs)
+        self.id = "vdivergence"
+        self.tag = "vdivergence"
+
+    def set_src_dst_reads(self):
+        self.src_reads = ["x", "y", "z", "h", "u", "v", "w", "m"]
+        self.dst_reads = ["x", "y", "z", "h", "u", "v", "w", "rho", "tag"]
+
+
+VelocityDivergence = SPHVelocityDivergence
+
+
+class ADKEConductionCoeffUpdate(SPHFunction):
+    """q_a = (g1 c_a + g2 h_a (|div_a| - div_a)) h_a over the LocalReal
+    particles (adke_funcs.pyx:231-291)."""
+
+    gpu_kind = "adke_q"
+
+    def __init__(self, source, dest, setup_arrays=True, g1=0.0, g2=0.0, **kwargs):
+        SPHFunction.__init__(self, source, dest, setup_arrays)
+        self.dest = dest if dest is not None else source
+        self.g1 = float(g1)
+        self.g2 = float(g2)
+        self.id = "adke_conduction"
+        self.tag = "q"
+        self.num_outputs = 1
+
+    def set_src_dst_reads(self):
+        self.src_reads = ["x", "y", "z", "h", "u", "v", "w", "m"]
+        self.dst_reads = ["x", "y", "z", "h", "u", "v", "w", "rho", "cs", "tag"]
+
+
 def _not_on_gpu(name, ref):
     class _F(SPHFunctionParticle):
         def __init__(self, *a, **k):

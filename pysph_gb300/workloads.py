@@ -210,16 +210,28 @@ def _integrator(api, name):
 
 
 def setup_drop(api, props, c0=1400.0, rho0=1.0, alpha=0.01, beta=0.0, eps=0.5,
-               integrator="euler", name="fluid", variable_h=False, periodic_domain=None):
+               integrator="euler", name="fluid", variable_h=False, periodic_domain=None,
+               adke=None):
     """Elliptical drop operations: SPHRho, Tait, PGrad, Monaghan AV,
     position stepping and XSPH, in that order (2D).  ``variable_h`` makes
-    the neighbour relation symmetric (``Particles(variable_h=True)``)."""
+    the neighbour relation symmetric (``Particles(variable_h=True)``).
+    ``adke=(h0, k, eps)`` puts the ADKE pilot density and smoothing-length
+    update first, as examples/shock-tube/sigalotti_shock_tube.py:44-56 does
+    (``props`` needs ``rhop``)."""
     base, sph, solver = api.base, api.sph, api.solver
     Fluid = base.ParticleType.Fluid
     pa = base.get_particle_array(name=name, type=Fluid, **props)
     particles = base.Particles(arrays=[pa], variable_h=variable_h,
                                periodic_domain=periodic_domain)
     s = solver.Solver(dim=2, integrator_type=_integrator(api, integrator))
+    if adke is not None:
+        h0, k, e = adke
+        s.add_operation(solver.SPHOperation(
+            sph.ADKEPilotRho.withargs(h0=h0), on_types=[Fluid], from_types=[Fluid],
+            updates=["rhop"], id="adke_rho"))
+        s.add_operation(solver.SPHOperation(
+            sph.ADKESmoothingUpdate.withargs(h0=h0, k=k, eps=e), on_types=[Fluid],
+            updates=["h"], id="adke"))
     s.add_operation(solver.SPHOperation(
         sph.SPHRho.withargs(), on_types=[Fluid], from_types=[Fluid],
         updates=["rho"], id="density"))

@@ -304,6 +304,57 @@ def fixture_periodic(dx=0.05, nx=20, ny=10):
     return out
 
 
+ADKE = {"h0_dx": 1.2, "k": 1.0, "eps": 0.5, "g1": 0.2, "g2": 0.4}
+
+
+def fixture_adke(dx=0.05):
+    """ADKE (Sigalotti's adaptive kernel estimation, sph/funcs/adke_funcs.pyx)
+    on the elliptical drop with per-particle h, a seeded velocity
+    perturbation and Particles(variable_h=True), each function through an
+    SPHCalc as the reference's shock-tube example chains them: the pilot
+    density at the fixed h0, the smoothing-length update from it (the calc
+    marks the array dirty and re-bins), then the velocity divergence and the
+    conduction coefficient on the new h; with the neighbour lists before and
+    after the update."""
+    props = W.jitter_h(W.elliptical_drop(dx=dx, c0=100.0))
+    n = len(props["x"])
+    rng = np.random.default_rng(11)
+    props["u"] = props["u"] + rng.normal(0.0, 5.0, n)
+    props["v"] = props["v"] + rng.normal(0.0, 5.0, n)
+    extra = {k: np.zeros(n) for k in ("rhop", "div", "q", "tmpx", "tmpy")}
+    pa = rbase.get_particle_array(name="fluid", type=rbase.ParticleType.Fluid,
+                                  **props, **extra)
+    particles = rbase.Particles(arrays=[pa], variable_h=True)
+    kern = rbase.CubicSplineKernel(dim=2)
+    h0 = ADKE["h0_dx"] * dx
+    out = {"h0": np.float64(h0), "k": np.float64(ADKE["k"]), "eps": np.float64(ADKE["eps"]),
+           "g1": np.float64(ADKE["g1"]), "g2": np.float64(ADKE["g2"])}
+    for p_ in props:
+        out["in_" + p_] = np.asarray(props[p_]).copy()
+    o, ix = neighbours_csr(particles, pa, pa)
+    out["nbr0_offsets"], out["nbr0_index"] = o, ix
+
+    def run(fn, ups):
+        calc = rsph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+        calc.sph(*ups)
+
+    run(rsph.ADKEPilotRho.withargs(h0=h0), ["rhop"])
+    out["rhop"] = pa.get("rhop").copy()
+    run(rsph.ADKESmoothingUpdate.withargs(h0=h0, k=ADKE["k"], eps=ADKE["eps"]), ["h"])
+    out["h_new"] = pa.get("h").copy()
+    o, ix = neighbours_csr(particles, pa, pa)
+    out["nbr1_offsets"], out["nbr1_index"] = o, ix
+    # three outputs: the class keeps SPHFunction's num_outputs (a one-update
+    # calc, as in examples/shock-tube/sigalotti_shock_tube.py, raises)
+    run(rsph.VelocityDivergence.withargs(), ["div", "tmpx", "tmpy"])
+    out["div"] = pa.get("div").copy()
+    out["div_1"] = pa.get("tmpx").copy()
+    out["div_2"] = pa.get("tmpy").copy()
+    run(rsph.ADKEConductionCoeffUpdate.withargs(g1=ADKE["g1"], g2=ADKE["g2"]), ["q"])
+    out["q"] = pa.get("q").copy()
+    return out
+
+
 def fixture_drop_output(dx=0.1, steps=3):
     """Solver.solve of the drop with output every step (solver.py:457-538):
     the names of the .npz files it writes and their contents."""
@@ -350,6 +401,7 @@ def main():
         "drop_varh": fixture_drop_varh,
         "periodic": fixture_periodic,
         "drop_output": fixture_drop_output,
+        "adke": fixture_adke,
     }
     only = sys.argv[1:]
     if only:

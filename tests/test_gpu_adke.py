@@ -1,0 +1,132 @@
+"""ADKE (adaptive kernel estimation, sph/funcs/adke_funcs.pyx) on the GPU
+against the reference's outputs and the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pysph_gb300
+from golden_util import csr_sets, load, normwise
+from pysph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+API = pysph_gb300.api()
+base, sph, solver = API.base, API.sph, API.solver
+TOL = 1e-5
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+
+
+def _calc(particles, pa, fn, ups):
+    kern = base.CubicSplineKernel(dim=2)
+    calc = sph.SPHCalc(particles, [pa], pa, kern, [fn.get_func(pa, pa)], ups)
+    calc.sph(*ups)
+
+
+def test_adke_chain_matches_reference():
+    """The reference's chain on the jittered-h drop with variable-h lists:
+    pilot density at h0, smoothing update (the calc re-bins), neighbour
+    sets on the new h, velocity divergence, conduction coefficient."""
+    _need_gpu()
+    g = load("adke")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    n = len(props["x"])
+    extra = {k: np.zeros(n) for k in ("rhop", "div", "q", "tmpx", "tmpy")}
+    pa = base.get_particle_array(name="fluid", type=base.ParticleType.Fluid, **props, **extra)
+    particles = base.Particles(arrays=[pa], variable_h=True)
+    h0 = float(g["h0"])
+    _calc(particles, pa, sph.ADKEPilotRho.withargs(h0=h0), ["rhop"])
+    assert normwise(pa.get("rhop"), g["rhop"]) < TOL
+    # the update from the reference's pilot density is FP64 throughout
+    pa.set(rhop=g["rhop"])
+    _calc(particles, pa, sph.ADKESmoothingUpdate.withargs(h0=h0, k=float(g["k"]),
+                                                          eps=float(g["eps"])), ["h"])
+    np.testing.assert_allclose(pa.get("h"), g["h_new"], rtol=1e-14, atol=0)
+    loc = particles.nnps_manager.get_neighbor_particle_locator(pa, pa, 2.0)
+    off, idx = loc.neighbour_csr()
+    assert csr_sets(off, idx) == csr_sets(g["nbr1_offsets"], g["nbr1_index"])
+    _calc(particles, pa, sph.VelocityDivergence.withargs(), ["div", "tmpx", "tmpy"])
+    assert normwise(pa.get("div"), g["div"]) < TOL
+    assert not pa.get("tmpx").any() and not pa.get("tmpy").any()
+    # the conduction coefficient from the reference's inputs, bit for bit
+    # (the GPU's h differs from the reference's in the last bit here and
+    # there: CUDA's pow against the host's)
+    pa.set(div=g["div"], h=g["h_new"])
+    _calc(particles, pa, sph.ADKEConductionCoeffUpdate.withargs(g1=float(g["g1"]),
+                                                                g2=float(g["g2"])), ["q"])
+    np.testing.assert_array_equal(pa.get("q"), g["q"])
+
+
+def test_velocity_divergence_keeps_three_outputs():
+    """As the reference's class: one update raises from check_internals."""
+    _need_gpu()
+    props = W.elliptical_drop(dx=0.1)
+    pa = base.get_particle_array(name="fluid", div=np.zeros(len(props["x"])), **props)
+    particles = base.Particles(arrays=[pa])
+    with pytest.raises(ValueError, match="num_outputs"):
+        sph.SPHCalc(particles, [pa], pa, base.CubicSplineKernel(dim=2),
+                    [sph.VelocityDivergence.get_func(pa, pa)], ["div"])
+
+
+def test_pilot_density_uniform_h_and_divergence_match_oracle():
+    """Uniform h (the list-streaming kernels of one h), a 3D lattice:
+    pilot density at h0 = 0.8 h and h0 = 1.1 h (support past the lists'
+    radius: only the listed neighbours count, as in the reference), and
+    the velocity divergence."""
+    _need_gpu()
+    props = W.cube_lattice(4096, seed=2, vel_std=0.3)
+    n = len(props["x"])
+    pa = base.get_particle_array(name="fluid", rhop=np.zeros(n), div=np.zeros(n),
+                                 t1=np.zeros(n), t2=np.zeros(n), **props)
+    particles = base.Particles(arrays=[pa])
+    kern = base.CubicSplineKernel(dim=3)
+    off, idx = oracle.neighbors(props, props, 2.0 * props["h"].max(), same=True)
+    for f in (0.8, 1.1):
+        h0 = f * float(props["h"][0])
+        calc = sph.SPHCalc(particles, [pa], pa, kern,
+                           [sph.ADKEPilotRho.withargs(h0=h0).get_func(pa, pa)], ["rhop"])
+        calc.sph("rhop")
+        ref = oracle.pair_sum("pilotrho", props, props, off, idx, 3, {"h0": h0}, nout=1)[0]
+        assert normwise(pa.get("rhop"), ref) < TOL, f
+    calc = sph.SPHCalc(particles, [pa], pa, kern, [sph.VelocityDivergence.get_func(pa, pa)],
+                       ["div", "t1", "t2"])
+    calc.sph("div", "t1", "t2")
+    ref = oracle.pair_sum("vdiv", props, props, off, idx, 3, nout=1)[0]
+    assert normwise(pa.get("div"), ref) < TOL
+
+
+def _adke_drop_ops(h0, k, eps):
+    return [oracle.Op("pilotrho", "fluid", ["rhop"], ["fluid"], h0=h0),
+            oracle.Op("adke_h", "fluid", ["h"], ["fluid"], h0=h0, k=k, eps=eps)
+            ] + oracle.drop_ops(c0=100.0)
+
+
+def test_adke_in_solver_matches_oracle():
+    """The drop with the example's ADKE operations ahead of the density
+    (examples/shock-tube/sigalotti_shock_tube.py:44-56): pilot density and
+    smoothing update, then SPHRho, Tait, PGrad, AV, stepping, XSPH; three
+    Euler steps, every evaluation re-binning on the new h."""
+    _need_gpu()
+    dx = 0.05
+    h0, k, eps = 1.3 * dx, 1.0, 0.5
+    props = W.elliptical_drop(dx=dx, c0=100.0)
+    n = len(props["x"])
+    props["rhop"] = np.ones(n)
+    s, particles = W.setup_drop(API, dict(props), c0=100.0, variable_h=True,
+                                adke=(h0, k, eps))
+    for _ in range(3):
+        s.integrator.integrate(1e-5)
+    pa = particles.arrays[0]
+    prob = oracle.Problem({"fluid": props}, _adke_drop_ops(h0, k, eps), dim=2,
+                          variable_h=True)
+    for _ in range(3):
+        prob.integrate_euler(1e-5)
+    ref = prob.arrays["fluid"]
+    assert np.ptp(ref["h"]) > 0.05 * h0        # h really varies
+    for p in ("h", "rhop", "rho", "p"):
+        assert normwise(pa.get(p), ref[p]) < TOL, p
+    for p in ("x", "y", "u", "v"):
+        assert normwise(pa.get(p) - props[p], ref[p] - props[p]) < 1e-4, p

@@ -302,3 +302,31 @@ def test_periodic_images_are_the_minimum_images():
         ref = sorted(j for j in range(n) for s in (-1.0, 0.0, 1.0)
                      if ((x[j] + s if s else x[j]) - x[i]) ** 2 + (y[j] - y[i]) ** 2 < (2 * h[i]) ** 2)
         assert got == ref, i
+
+
+def test_adke_functions_match_reference():
+    """ADKE (adke_funcs.pyx) on the jittered-h drop, variable-h lists: the
+    reference's neighbour sets before and after the smoothing update, the
+    pilot density and the divergence over the reference's lists bit for bit,
+    the smoothing update and the conduction coefficient to FP64 round-off."""
+    g = load("adke")
+    props = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    cell = 2.0 * props["h"].max()
+    off, idx = oracle.neighbors(props, props, cell, same=True, variable_h=True)
+    assert csr_sets(off, idx) == csr_sets(g["nbr0_offsets"], g["nbr0_index"])
+    h0 = float(g["h0"])
+    rhop = oracle.pair_sum("pilotrho", props, props, g["nbr0_offsets"], g["nbr0_index"], 2,
+                           {"h0": h0}, nout=1)[0]
+    np.testing.assert_array_equal(rhop, g["rhop"])
+    st = dict(props, rhop=g["rhop"])
+    h = oracle.adke_smoothing(st, h0, float(g["k"]), float(g["eps"]))
+    np.testing.assert_allclose(h, g["h_new"], rtol=1e-15, atol=0)
+    st["h"] = g["h_new"]
+    off1, idx1 = oracle.neighbors(st, st, 2.0 * st["h"].max(), same=True, variable_h=True)
+    assert csr_sets(off1, idx1) == csr_sets(g["nbr1_offsets"], g["nbr1_index"])
+    div = oracle.pair_sum("vdiv", st, st, g["nbr1_offsets"], g["nbr1_index"], 2, nout=1)[0]
+    np.testing.assert_array_equal(div, g["div"])
+    assert not g["div_1"].any() and not g["div_2"].any()
+    st["div"] = g["div"]
+    q = oracle.adke_conduction(st, float(g["g1"]), float(g["g2"]))
+    np.testing.assert_array_equal(q, g["q"])
