@@ -130,3 +130,35 @@ def test_adke_in_solver_matches_oracle():
         assert normwise(pa.get(p), ref[p]) < TOL, p
     for p in ("x", "y", "u", "v"):
         assert normwise(pa.get(p) - props[p], ref[p] - props[p]) < 1e-4, p
+
+
+def test_update_after_h_change_finds_new_neighbours():
+    """sph/tests/test_update_smoothing.py:62-107: 11 particles on [0, 1],
+    h = dx; doubling h[5] and marking the array dirty gives particle 5 the
+    neighbours 1..9 at the next particles.update(); with the ADKE defaults
+    (k = 1, eps = 0) the update leaves h = h0."""
+    _need_gpu()
+    x = np.linspace(0, 1, 11)
+    dx = x[1] - x[0]
+    h = np.ones_like(x) * (dx + 1e-10)
+    pa = base.get_particle_array(name="test", type=base.ParticleType.Fluid, x=x, h=h,
+                                 rho=np.ones_like(x), m=np.ones_like(x) * dx,
+                                 rhop=np.ones_like(x))
+    particles = base.Particles(arrays=[pa], variable_h=True)
+    adke = solver.SPHOperation(sph.ADKESmoothingUpdate.withargs(h0=dx, k=1.0, eps=0.0),
+                               from_types=[base.ParticleType.Fluid],
+                               on_types=[base.ParticleType.Fluid], updates=["h"],
+                               id="adke_smoothing")
+    calcs = adke.get_calcs(particles, base.CubicSplineKernel(dim=1))
+    loc = calcs[0].nbr_locators[0]
+    nbrs = np.sort(loc.py_get_nearest_particles(5).get_npy_array())
+    assert nbrs.tolist() == [3, 4, 5, 6, 7]
+    hh = pa.get("h")
+    hh[5] *= 2
+    pa.set(h=hh)
+    pa.set_dirty(True)
+    particles.update()
+    nbrs = np.sort(loc.py_get_nearest_particles(5).get_npy_array())
+    assert nbrs.tolist() == [1, 2, 3, 4, 5, 6, 7, 8, 9]
+    calcs[0].sph("h")
+    np.testing.assert_array_equal(pa.get("h"), np.full(11, dx))
