@@ -810,7 +810,9 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         ArraySnap &A = ctx->arrays[a];
         const sph_array_view &v = arrays[a];
         if (v.n == 0) continue;
-        k_light<<<grid_blocks(v.n, kThreads, 8), kThreads, 0, st>>>(
+        // one thread per particle (more loads in flight than a grid-stride
+        // loop over a resident grid: 55 against 61 us at 1 M particles)
+        k_light<<<grid_blocks(v.n, kThreads, 64), kThreads, 0, st>>>(
             v, ctx->grid, inv_cs_ref, A.inv, A.key, A.pm0, A.velh, A.st,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
             ctx->build_h, stale_thr, caps, ctx->d_status);
