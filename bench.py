@@ -174,10 +174,45 @@ def reference_available():
         return False
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the ISA)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def _pin(core):
+    """Pin this process to one core (returns the previous set, or None)."""
+    if not hasattr(os, "sched_setaffinity"):
+        return None
+    try:
+        prev = os.sched_getaffinity(0)
+        os.sched_setaffinity(0, {core % (os.cpu_count() or 1)})
+        return prev
+    except OSError:
+        return None
+
+
 def _cpu_worker(args):
-    """Time ``steps`` RK2 steps of the sample after ``warmup`` (one process)."""
-    kind, n, warmup, steps, seed = args
+    """Time ``steps`` RK2 steps of the sample after ``warmup`` (one process,
+    pinned to its own core)."""
+    kind, n, warmup, steps, seed, core = args
     import numpy as np
+    # the reference's Cython is single-threaded; the oracle port uses OpenMP
+    prev = _pin(core) if kind == "reference" else None
 
     from pysph_gb300 import workloads as W
     props = W.cube_lattice(n, seed=seed)
@@ -200,13 +235,15 @@ def _cpu_worker(args):
     for _ in range(steps):
         step()
     dt = time.perf_counter() - t0
+    if prev is not None:
+        os.sched_setaffinity(0, prev)
     return {"pairs": 4.0 * kbar * n * steps, "seconds": dt, "kbar": kbar}
 
 
 def cpu_baseline(procs, warmup, steps, n=SAMPLE_N):
     kind = "reference" if reference_available() else "port"
     import multiprocessing as mp
-    jobs = [(kind, n, warmup, steps, 100 + i) for i in range(procs)]
+    jobs = [(kind, n, warmup, steps, 100 + i, i) for i in range(procs)]
     if procs == 1:
         res = [_cpu_worker(jobs[0])]
     else:
@@ -226,7 +263,8 @@ def cpu_baseline(procs, warmup, steps, n=SAMPLE_N):
         import oracle
         cores = procs * oracle.num_threads()
     return {
-        "value": value, "unit": UNIT, "cores": cores, "kind": kind,
+        "value": value, "unit": UNIT, "cores": cores, "kind": kind, "cpu": cpu_model(),
+        "pinning": "process i on core i" if kind == "reference" else "none (OpenMP)",
         "sample": "%d independent %s processes, each %d RK2 steps of a %d-particle "
                   "jittered lattice (h=1.2dx, same physics), after %d warm-up steps; "
                   "mean neighbours %.1f" % (procs, "reference PySPH Cython" if kind == "reference"
