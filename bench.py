@@ -445,6 +445,10 @@ def run_gpu(args):
                    "cache": "L2 flushed between timed steps (256 MiB write outside the events)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "steps_per_s": 1.0 / step_s,
+        # the reference counts each SPHFunction's pair loop separately:
+        # SPHRho, PGrad and AV over every neighbour, twice per RK2 step
+        "reference_equivalent": {"value": value * 6.0 / 4.0, "unit": UNIT,
+                                 "per_step": "6 K N (SPHRho, PGrad, AV x 2 evaluations)"},
         "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
         "nnps_builds": {"timed_full": builds[0], "timed_light": builds[1],
                         "deferred": deferred[0], "deferred_stale": deferred[1],
