@@ -211,8 +211,9 @@ int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
 /* Neighbour lists of destination dst among source src (radius
  * radius_scale*h_dst, radius_scale no larger than the build's), as original particle
  * indices: counts[i] (device, int64, n_dst) then, given the exclusive prefix
- * offsets (device, n_dst+1), the index lists, each sorted ascending with the
- * destination itself moved last when dst == src. */
+ * offsets (device, n_dst+1), the index lists, each sorted ascending and then,
+ * when dst == src, the destination itself swapped with the last entry (as
+ * the reference's cache update does, base/nnps.pyx:609-616). */
 int sph_nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *counts);
 int sph_nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
                   int64_t *index);

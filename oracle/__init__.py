@@ -123,7 +123,8 @@ def cubic_grad(dim, a, b, h):
 
 
 def neighbors(dst, src, cell_size, radius_scale=2.0, same=False, variable_h=False):
-    """CSR neighbour lists (ascending source index, self last if ``same``);
+    """CSR neighbour lists (ascending source index, then with ``same`` the
+    destination swapped with the last entry, nnps.pyx:609-616);
     ``variable_h`` gives the symmetric relation of VarHNbrParticleLocator."""
     D, S = _Arr(dst), _Arr(src)
     n = D.st.n

@@ -90,7 +90,8 @@ static inline double get0(const double *a, int64_t i) { return a ? a[i] : 0.0; }
 /* stencil :93-116 / :1106-1142 (distance = ceil(radius/cell_size)),       */
 /* distance test base/nnps.pyx:271-356 (d2 = |src-dst|^2 < radius^2, with  */
 /* radius = radius_scale * h_dst, :525-559), self moved last :596-620.      */
-/* Lists are returned in ascending source index (self last when src==dst). */
+/* Lists are returned in ascending source index, then (src == dst) the      */
+/* destination swapped with the last entry, as nnps.pyx:609-616 does.       */
 /* ---------------------------------------------------------------------- */
 
 typedef struct { int64_t cx, cy, cz; int64_t idx; } cell_rec;

@@ -6,7 +6,8 @@ array moved.  The GPU pair kernels need no such cache: they walk the sorted
 cell rows directly.  The locator here serves the API: its neighbour lists
 are exported from the device on first query after a rebuild (FP64 distance
 test ``|x_j - x_i|^2 < (radius_scale h_i)^2`` as in :337-353, each list in
-ascending index order with the particle itself moved last, :611-618).
+ascending index order with the particle itself then swapped with the last
+entry, as the reference's cache update does, :609-616).
 """
 import ctypes
 

@@ -420,7 +420,8 @@ __global__ void k_nbr(sph_array_view d, sph_array_view s, Grid g, const int *dke
                 }
             }
         if (FILL) {
-            // ascending, self last (base/nnps.pyx:611-618 keeps self last)
+            // ascending, then self swapped with the last entry (the
+            // reference's cache update, base/nnps.pyx:609-616)
             for (int64_t a2 = base + 1; a2 < base + cnt; ++a2) {
                 int64_t v = index[a2];
                 int64_t b = a2 - 1;
@@ -433,7 +434,7 @@ __global__ void k_nbr(sph_array_view d, sph_array_view s, Grid g, const int *dke
             if (same) {
                 for (int64_t t = base; t + 1 < base + cnt; ++t)
                     if (index[t] == i) {
-                        for (int64_t u = t; u + 1 < base + cnt; ++u) index[u] = index[u + 1];
+                        index[t] = index[base + cnt - 1];
                         index[base + cnt - 1] = i;
                         break;
                     }
