@@ -64,3 +64,27 @@ def test_bench_workload_conserves_mass_and_momentum():
     assert dp / scale < 1e-6, dp / scale
     full, light = particles.cell_manager.build_stats()
     assert light > 0
+
+
+def test_dam_break_full_size_matches_oracle():
+    """The dam break at its full size (20 000 fluid particles at dx = 0.01,
+    three layers of walls, gravity, boundary force), five RK2 steps at the
+    stable dt of this configuration (2.5e-5) against the FP64 oracle."""
+    _need_gpu()
+    dx = 0.01
+    fluid, wall = W.dam_break(dx=dx)
+    assert len(fluid["x"]) == 20000
+    c0 = W.dam_break_c0()
+    s, particles = W.setup_dam_break(API, fluid, wall, dx, c0)
+    prob = oracle.Problem({"fluid": fluid, "boundary": wall}, oracle.dam_ops(dx, c0), dim=2)
+    for _ in range(5):
+        s.integrator.integrate(2.5e-5)
+        prob.integrate_rk2(2.5e-5)
+    pa = particles.arrays[0]
+    ref = prob.arrays["fluid"]
+    for p in ("rho", "p"):
+        assert normwise(pa.get(p), ref[p]) < TOL, p
+    n = len(fluid["x"])
+    for p in ("x", "y", "u", "v"):
+        init = fluid.get(p, np.zeros(n))      # the column starts at rest
+        assert normwise(pa.get(p) - init, ref[p] - init) < 1e-4, p
