@@ -91,7 +91,6 @@ int sph_ctx_create(int dim, sph_ctx **out) {
     }
     cudaMemset(c->d_status, 0, kStatusWords * sizeof(unsigned));
     c->d_err = c->d_status;
-    c->d_disp = c->d_status + 1;
     *out = c;
     return SPH_OK;
 }

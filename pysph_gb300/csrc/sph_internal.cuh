@@ -160,7 +160,7 @@ struct sph_ctx {
     double cell_size_ref = 0;           // reference cell size of the jump check
     long long build_id = 0;             // incremented by every neighbour build
     std::vector<sphgb::NbrList> lists;  // narrays x narrays (dst-major)
-    unsigned *d_status = nullptr;       // kStatusWords: d_err, d_disp, stale, list maxima
+    unsigned *d_status = nullptr;       // kStatusWords: error word, displacement, stale, list maxima
     unsigned *h_status = nullptr;       // mapped mirror of d_status
     unsigned *hd_status = nullptr;      // device address of h_status
     // deferred check of a light refresh (sph_ctx_set_deferred): the status
@@ -183,7 +183,6 @@ struct sph_ctx {
     int symmetric = 0;                  // variable-h neighbour relation (next build)
     int periodic = 0;                   // periodic x axis (next build)
     double pxmin = 0.0, pxmax = 0.0;
-    unsigned *d_disp = nullptr;         // max squared displacement (float bits)
     long long n_full = 0, n_light = 0;  // full builds / light refreshes
 };
 
