@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "sph_internal.cuh"
@@ -654,6 +655,19 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
     g.ncells = nx * ny * nz;
     ctx->grid = g;
+    // stencil half-width 2 with more source particles than three 3-bit
+    // offset fields leave slot bits for: base-5 offsets (environment
+    // SPH_WIDE_CODES=1 forces them, to test them on small sets)
+    {
+        static int force = -1;
+        if (force < 0) {
+            const char *e = getenv("SPH_WIDE_CODES");
+            force = (e && atoi(e) > 0) ? 1 : 0;
+        }
+        int64_t nmax = 0;
+        for (int a = 0; a < narrays; ++a) nmax = std::max<int64_t>(nmax, arrays[a].n);
+        ctx->wide_codes = k == 2 && (force || nmax >= ((int64_t)1 << 23));
+    }
 
     for (int a = 0; a < narrays; ++a) {
         ArraySnap &A = ctx->arrays[a];

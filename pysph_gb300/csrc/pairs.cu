@@ -682,8 +682,19 @@ int default_cap(const Grid &g) {
     return 16;
 }
 
-int64_t code_limit(int kx) {
-    return kx == 1 ? (1ll << Code<1>::SHIFT) : (kx == 2 ? (1ll << Code<2>::SHIFT) : (1ll << Code<3>::SHIFT));
+// code variant of the context's build: the stencil half-width, or 4 for
+// half-width 2 with base-5 offsets
+int code_variant(const sph_ctx *ctx) {
+    return (ctx->grid.kx == 2 && ctx->wide_codes) ? 4 : ctx->grid.kx;
+}
+
+int64_t code_limit(int variant) {
+    switch (variant) {
+        case 1: return 1ll << Code<1>::SHIFT;
+        case 2: return 1ll << Code<2>::SHIFT;
+        case 4: return 1ll << Code<4>::SHIFT;
+        default: return 1ll << Code<3>::SHIFT;
+    }
 }
 
 // Allocate / size the neighbour list of (dst, src) for the current build
@@ -698,7 +709,7 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
     ArraySnap &D = ctx->arrays[dst];
     ArraySnap &S = ctx->arrays[src];
     const Grid &g = ctx->grid;
-    if (S.n >= code_limit(g.kx))
+    if (S.n >= code_limit(code_variant(ctx)))
         return set_error(SPH_ERR_NOTSUP, "neighbour list: too many source particles for this "
                                          "cell subdivision (use a smaller subdivision)");
     if (!L.maxcnt) {
@@ -761,9 +772,12 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
         const bool ext = g.periodic || g.symmetric;
 #define LLAUNCH(K) (ext ? k_nbrlist<K, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                         : k_nbrlist<K, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
-        if (g.kx == 1) LLAUNCH(1);
-        else if (g.kx == 2) LLAUNCH(2);
-        else LLAUNCH(3);
+        switch (code_variant(ctx)) {
+            case 1: LLAUNCH(1); break;
+            case 2: LLAUNCH(2); break;
+            case 4: LLAUNCH(4); break;
+            default: LLAUNCH(3); break;
+        }
 #undef LLAUNCH
         count_launch();
         SPH_LAUNCH_CHECK("k_nbrlist");
@@ -883,9 +897,12 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
                               : k_density<K, false, 2><<<b, kPairBlock, 0, ctx->stream>>>(a)) \
                         : (uh ? k_density<K, true, 0><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                               : k_density<K, false, 0><<<b, kPairBlock, 0, ctx->stream>>>(a)))
-    if (a.g.kx == 1) DLAUNCH(1);
-    else if (a.g.kx == 2) DLAUNCH(2);
-    else DLAUNCH(3);
+    switch (code_variant(ctx)) {
+        case 1: DLAUNCH(1); break;
+        case 2: DLAUNCH(2); break;
+        case 4: DLAUNCH(4); break;
+        default: DLAUNCH(3); break;
+    }
 #undef DLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
@@ -963,9 +980,12 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
                     : spec == 2 ? k_rates<K, 2, 0><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                     : spec == 3 ? k_rates<K, 0, 2><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                                 : k_rates<K, 0, 0><<<b, kPairBlock, 0, ctx->stream>>>(a))
-    if (a.g.kx == 1) RLAUNCH(1);
-    else if (a.g.kx == 2) RLAUNCH(2);
-    else RLAUNCH(3);
+    switch (code_variant(ctx)) {
+        case 1: RLAUNCH(1); break;
+        case 2: RLAUNCH(2); break;
+        case 4: RLAUNCH(4); break;
+        default: RLAUNCH(3); break;
+    }
 #undef RLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_rates");
@@ -1006,9 +1026,12 @@ int features_pass(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *
     const bool ext = a.g.periodic || a.g.symmetric;
 #define FLAUNCH(K) (ext ? k_features<K, true><<<b, kPairBlock, 0, ctx->stream>>>(a) \
                         : k_features<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
-    if (a.g.kx == 1) FLAUNCH(1);
-    else if (a.g.kx == 2) FLAUNCH(2);
-    else FLAUNCH(3);
+    switch (code_variant(ctx)) {
+        case 1: FLAUNCH(1); break;
+        case 2: FLAUNCH(2); break;
+        case 4: FLAUNCH(4); break;
+        default: FLAUNCH(3); break;
+    }
 #undef FLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_features");

@@ -169,6 +169,9 @@ struct sph_ctx {
     // set) and launched again after a full build if it was
     int deferred = 0;
     bool pending = false;               // a refresh whose status is not read yet
+    // list entries of this build use code variant 4 (base-5 offsets, 25
+    // slot bits): stencil half-width 2 with more than 2^23 source particles
+    bool wide_codes = false;
     cudaEvent_t pending_event = nullptr; // recorded after the status copy
     std::vector<sph_array_view> pending_views;
     double pending_cell_size = 0.0, pending_radius_scale = 0.0;
@@ -396,6 +399,24 @@ struct Code {
     }
 };
 
+// Code variant 4: stencil half-width 2 with the offset in base 5,
+// (dx+2) + 5 (dy+2) + 25 (dz+2) (125 values, 7 bits), so the slot keeps 25
+// bits (2^25 source particles instead of the 2^23 of three 3-bit fields).
+// Linear in dx like the bit fields: a row code plus dx is the full code.
+template <>
+struct Code<4> {
+    static constexpr int BITS = 7;
+    static constexpr int SHIFT = 32 - BITS;
+    static constexpr uint32_t JMASK = (1u << SHIFT) - 1u;
+    __host__ __device__ static constexpr int row(int dy, int dz) {
+        return 2 + 5 * (dy + 2) + 25 * (dz + 2);
+    }
+};
+
+// stencil half-width K of a code variant
+template <int KX>
+__host__ __device__ constexpr int stencil_k() { return KX == 4 ? 2 : KX; }
+
 // Minus the cell offset (dx, dy, dz) of list entry e, as exact floats: a
 // field v becomes 2^23 + v by OR-ing it into the bits of 2^23, and
 // (2^23 + K) - (2^23 + v) = -(v - K).
@@ -407,6 +428,21 @@ __device__ __forceinline__ float3 neg_cell_offset(uint32_t e) {
     return make_float3(base - __uint_as_float((c & C::FMASK) | 0x4B000000u),
                        base - __uint_as_float(((c >> C::FB) & C::FMASK) | 0x4B000000u),
                        base - __uint_as_float(((c >> (2 * C::FB)) & C::FMASK) | 0x4B000000u));
+}
+
+// base 5: c / 25 = (c 1311) >> 15 for c < 125 and r / 5 = (r 13) >> 6 for
+// r < 25 (exact on those ranges; checked for every value by the tests)
+template <>
+__device__ __forceinline__ float3 neg_cell_offset<4>(uint32_t e) {
+    const uint32_t c = e >> Code<4>::SHIFT;
+    const uint32_t z = (c * 1311u) >> 15;
+    const uint32_t r = c - 25u * z;
+    const uint32_t y = (r * 13u) >> 6;
+    const uint32_t x = r - 5u * y;
+    constexpr float base = 8388608.f + 2.f;
+    return make_float3(base - __uint_as_float(x | 0x4B000000u),
+                       base - __uint_as_float(y | 0x4B000000u),
+                       base - __uint_as_float(z | 0x4B000000u));
 }
 
 // The reverse test of the variable-h relation: destination (original index
@@ -458,6 +494,7 @@ template <int KX, bool EXT, class Fn>
 __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, const DestPos &d,
                                                const double *dx64, const double *dy64,
                                                const double *dz64, Fn &&fn) {
+    constexpr int K = stencil_k<KX>();
     const float csf = g.cs_f;
     const float inv_cs = 1.f / csf;
     // pruning radius: the accept/recheck threshold plus a relative margin
@@ -480,8 +517,8 @@ __device__ __forceinline__ void for_neighbours(const Grid &g, const SrcDev &S, c
             if (rem < 0.f) continue;
             // chord half-width with a relative margin (covers the rsqrt error)
             const float half = fmaf(rem * rsqrtf(fmaxf(rem, 1e-30f)), 1.0001f, 1e-5f * csf);
-            const int tlo = max(-KX, __float2int_rd((d.xi_x - half) * inv_cs));
-            const int thi = min(KX, __float2int_rd((d.xi_x + half) * inv_cs));
+            const int tlo = max(-K, __float2int_rd((d.xi_x - half) * inv_cs));
+            const int thi = min(K, __float2int_rd((d.xi_x + half) * inv_cs));
             const int c0 = zbase + (d.cy + dy) * g.nx;
             const float by = d.xi_y - (float)dy * csf;
             const int code_yz = Code<KX>::row(dy, dz);

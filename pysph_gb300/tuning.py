@@ -31,9 +31,10 @@ def list_skin():
 # measured defaults: (dimensions with extent) -> subdivision
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
 # neighbour-list entries hold the source slot in 32 - code bits (three
-# fields of 2 bits at subdivision 1, of 3 bits at 2 and 3): at most 2^26
-# source particles at subdivision 1, 2^23 at 2 and 3
-MAX_PARTICLES = {1: 1 << 26, 2: 1 << 23, 3: 1 << 23}
+# fields of 2 bits at subdivision 1, of 3 bits at 3; at subdivision 2 three
+# 3-bit fields up to 2^23 particles, above that the offset in base 5 in 7
+# bits): at most 2^26 source particles at subdivision 1, 2^25 at 2, 2^23 at 3
+MAX_PARTICLES = {1: 1 << 26, 2: 1 << 25, 3: 1 << 23}
 
 
 def choose_subdivision(cell_manager):

@@ -571,3 +571,48 @@ def test_solver_output_files_match_reference(tmp_path):
                     assert normwise(got - props[key], ref - props[key]) < 1e-4, (f, key)
                 else:
                     assert normwise(got, ref) < 1e-4, (f, key)
+
+
+def test_base5_list_codes_match_oracle():
+    """Lists with base-5 cell offsets (used at subdivision 2 above 2^23
+    particles), forced on small sets: a 3D lattice RK2 step and a 2D drop
+    Euler step against the oracle."""
+    _need_gpu()
+    import subprocess
+    import sys
+    code = r'''
+import sys
+sys.path.insert(0, ".")
+import oracle, pysph_gb300
+from pysph_gb300 import workloads as W
+from tests.golden_util import normwise
+api = pysph_gb300.api()
+props = W.cube_lattice(32768, seed=4)
+s, particles = W.setup_cube(api, props)
+assert particles.cell_manager._subdivision() == 2
+s.integrator.integrate(1e-4)
+pa = particles.arrays[0]
+prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+prob.integrate_rk2(1e-4)
+for p in ("rho", "p"):
+    assert normwise(pa.get(p), prob.arrays["fluid"][p]) < 1e-5, p
+for p in ("x", "u", "w"):
+    assert normwise(pa.get(p) - props[p], prob.arrays["fluid"][p] - props[p]) < 1e-5, p
+props = W.elliptical_drop(dx=0.025, c0=100.0)
+s, particles = W.setup_drop(api, props, c0=100.0)
+s.integrator.integrate(1e-5)
+pa = particles.arrays[0]
+prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=100.0), dim=2)
+prob.integrate_euler(1e-5)
+for p in ("rho", "p"):
+    assert normwise(pa.get(p), prob.arrays["fluid"][p]) < 1e-5, p
+for p in ("x", "y", "u", "v"):
+    assert normwise(pa.get(p) - props[p], prob.arrays["fluid"][p] - props[p]) < 1e-5, p
+print("ok")
+'''
+    import os
+    env = dict(os.environ, SPH_WIDE_CODES="1", PYSPH_GB300_SUBDIV="2")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]

@@ -189,3 +189,23 @@ def test_staged_transfers_check_their_arguments():
             pa.upload(x=np.ones(4))
         with pytest.raises(RuntimeError):
             pa.download("x")
+
+
+def test_base5_cell_offset_decode_is_exact():
+    """The base-5 list-entry code (stencil half-width 2 above 2^23 source
+    particles): (dx+2) + 5 (dy+2) + 25 (dz+2), decoded with c / 25 =
+    (c 1311) >> 15 and r / 5 = (r 13) >> 6 -- exact for every code."""
+    seen = set()
+    for dz in range(-2, 3):
+        for dy in range(-2, 3):
+            for dx in range(-2, 3):
+                row = 2 + 5 * (dy + 2) + 25 * (dz + 2)     # Code<4>::row
+                c = row + dx
+                assert 0 <= c < 128
+                z = (c * 1311) >> 15
+                r = c - 25 * z
+                y = (r * 13) >> 6
+                x = r - 5 * y
+                assert (x - 2, y - 2, z - 2) == (dx, dy, dz)
+                seen.add(c)
+    assert len(seen) == 125
