@@ -275,10 +275,12 @@ __global__ void k_reorder(sph_array_view a, Grid g, const int *perm, const int *
 }
 
 // Light refresh, in original particle order (coalesced FP64 reads, sorted
-// slot from the inverse permutation of the last full build): the snapshot
-// of the particle in the cell of that build, the largest squared
-// displacement from the build position, an h other than the build's
-// uniform h, and the jump check against the previous update's cells.
+// slot from the inverse permutation of the last full build): the position
+// and velocity records of the particle in the cell of that build (the
+// state record waits for the next density pass, which rewrites it, or for
+// k_state before a pass that reads it), the largest squared displacement
+// from the build position, an h other than the build's uniform h, and the
+// jump check against the previous update's cells.
 // status[0] |= flags, status[1] = max(displacement^2 bits), and
 // status[kStaleWord] = kStaleLists when some block saw a displacement of
 // at least stale_thr^(1/2), an h change or a jump (the lists no longer hold
@@ -300,7 +302,7 @@ __global__ void k_invperm(int64_t n, const int *perm, int *inv) {
 
 __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
                         const int *key, const float4 *pm0, float4 *velh,
-                        float4 *st, float4 *nrm, float4 *tan, float4 *pm, int *refcell,
+                        float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
                         double build_h, float stale_thr, const __grid_constant__ ListCaps caps,
                         unsigned *status) {
@@ -326,9 +328,7 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         const double h = a.h[i];
         if (h != build_h) hch = true;
         velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), (float)h);
-        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i), m = (float)a.m[i];
-        st[s] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), m);
-        pm[s] = make_float4(xi, yi, zi, m);
+        pm[s] = make_float4(xi, yi, zi, (float)a.m[i]);
         if (nrm) {
             nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
             tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
@@ -368,6 +368,17 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
             if (f) atomicOr(status, f);
             if (f || !(b < stale_thr)) atomicOr(status + kStaleWord, kStaleLists);
         }
+    }
+}
+
+// State record (rho, p / rho^2, cs, m) of every particle in the slots of
+// the last full build, after light refreshes that left it (in original
+// order, as k_light).
+__global__ void k_state(sph_array_view a, const int *inv, float4 *st) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float rho = (float)ld0(a.rho, i), p = (float)ld0(a.p, i);
+        st[inv[i]] = make_float4(rho, p / (rho * rho), (float)ld0(a.cs, i), (float)a.m[i]);
     }
 }
 
@@ -706,6 +717,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
                                                A.has_nrm ? A.tan : nullptr, A.pm);
             count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
+            A.st_fresh = true;
             if (g.skin > 0.f) {
                 if (A.pm0_cap < v.n) {
                     cudaFree(A.pm0);
@@ -828,10 +840,11 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         // one thread per particle (more loads in flight than a grid-stride
         // loop over a resident grid: 55 against 61 us at 1 M particles)
         k_light<<<grid_blocks(v.n, kThreads, 64), kThreads, 0, st>>>(
-            v, ctx->grid, inv_cs_ref, A.inv, A.key, A.pm0, A.velh, A.st,
+            v, ctx->grid, inv_cs_ref, A.inv, A.key, A.pm0, A.velh,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
             ctx->build_h, stale_thr, caps, ctx->d_status);
         caps.n = 0;   // checked once
+        A.st_fresh = false;
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
     }
@@ -867,6 +880,18 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
     return SPH_OK;
 }
 
+int ensure_state(sph_ctx *ctx, int a) {
+    ArraySnap &A = ctx->arrays[a];
+    if (A.st_fresh) return SPH_OK;
+    A.st_fresh = true;
+    if (A.n == 0) return SPH_OK;
+    if (!A.inv) return set_error(SPH_ERR_STATE, "state refresh without a light-refresh order");
+    k_state<<<grid_blocks(A.n, kThreads, 64), kThreads, 0, ctx->stream>>>(A.view, A.inv, A.st);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_state");
+    return SPH_OK;
+}
+
 int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
     if (!ctx->built || a < 0 || a >= (int)ctx->arrays.size())
         return set_error(SPH_ERR_STATE, "refresh_state: no neighbour build for this array");
@@ -878,6 +903,7 @@ int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
         return set_error(SPH_ERR_STATE, "refresh_state: normals added; rebuild needed");
     A.view = *view;
     A.has_nrm = nrm;
+    A.st_fresh = true;
     if (A.n == 0) return SPH_OK;
     k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
         A.view, ctx->grid, A.perm, A.key, A.skey, A.scx, A.velh, A.st, nrm ? A.nrm : nullptr,

@@ -35,7 +35,7 @@ struct DestDev {
     const int *sinst;    // batches: instance of each sorted slot
     const Grid *grids;   // batches: grid of each instance
     const int64_t *tag;
-    const double *x, *y, *z, *u, *v, *w, *h, *p, *rho;
+    const double *x, *y, *z, *u, *v, *w, *h, *p, *rho, *cs;
     int64_t n;
 };
 
@@ -355,12 +355,14 @@ __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_densi
         A.cs_out[orig] = (double)cf;
     }
     if (A.st_out) {
-        const float4 old = A.st_out[s];
+        // the whole state record from this pass and the FP64 arrays (the
+        // mass from the position record): fresh whatever it held before
+        const float mi = A.d.pm[s].w;
         if (A.tait) {
-            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, old.w);
+            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, mi);
         } else {
             const float pold = (float)ld0(A.d.p, orig);
-            A.st_out[s] = make_float4(rf, pold / (rf * rf), old.z, old.w);
+            A.st_out[s] = make_float4(rf, pold / (rf * rf), (float)ld0(A.d.cs, orig), mi);
         }
     }
 }
@@ -647,6 +649,7 @@ DestDev make_dest(const ArraySnap &D) {
     d.h = D.view.h;
     d.p = D.view.p;
     d.rho = D.view.rho;
+    d.cs = D.view.cs;
     d.n = D.n;
     return d;
 }
@@ -906,6 +909,7 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
 #undef DLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
+    if (a.st_out) D.st_fresh = true;   // every slot's state record rewritten
     for (int i = 0; i < nsrc; ++i)
         if (built[i]) built[i]->build = ctx->build_id;
     return SPH_OK;
@@ -919,6 +923,12 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
     if (dst < 0 || dst >= na || nterms < 0 || nterms > SPH_MAX_SOURCES || !prm)
         return set_error(SPH_ERR_ARG, "rates: bad destination / sources");
     ArraySnap &D = ctx->arrays[dst];
+    {
+        int rc = ensure_state(ctx, dst);
+        for (int i = 0; !rc && i < nterms; ++i)
+            if (terms[i].src >= 0 && terms[i].src < na) rc = ensure_state(ctx, terms[i].src);
+        if (rc) return rc;
+    }
     RatesArgs a{};
     a.g = ctx->grid;
     a.d = make_dest(D);
@@ -1003,7 +1013,8 @@ int features_pass(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *
     if (prm->c0 <= 0.0) return set_error(SPH_ERR_ARG, "features: c0 must be positive");
     ArraySnap &D = ctx->arrays[dst];
     NbrList *L;
-    const int rc = ensure_list(ctx, dst, src, &L);
+    int rc = ensure_state(ctx, src);
+    if (!rc) rc = ensure_list(ctx, dst, src, &L);
     if (rc) return rc;
     FeatureArgs a{};
     a.g = ctx->grid;

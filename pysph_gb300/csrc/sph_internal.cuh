@@ -101,6 +101,10 @@ struct ArraySnap {
     int64_t cap = 0;
     sph_array_view view{};
     bool has_nrm = false;
+    // st holds the arrays' current rho, p, cs (a light refresh leaves it
+    // to the next density pass, or to a state refresh before a pass that
+    // reads it)
+    bool st_fresh = true;
     int *key = nullptr;   // original order, dense cell index
     int *perm = nullptr;  // sorted -> original
     int *skey = nullptr;  // sorted: cell
@@ -245,6 +249,8 @@ int nnps_count(sph_ctx *ctx, int dst, int src, double radius_scale, int64_t *cou
 int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t *offsets,
               int64_t *index);
 int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view);
+// bring the state record st of array a up to date if a light refresh left it
+int ensure_state(sph_ctx *ctx, int a);
 // read the status of a deferred light refresh; *rebuilt: it was stale and a
 // full build replaced it (a gated pass launched since then did nothing)
 int resolve_pending(sph_ctx *ctx, bool *rebuilt);
