@@ -57,7 +57,7 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
 # of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md,
 # list-streaming passes); the traffic grows with the particle count, so it is scaled by n
-NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 405.0, "RatesStage": 436.0}
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 388.0, "RatesStage": 436.0}
 
 
 def measured_peaks():
