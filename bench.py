@@ -49,7 +49,9 @@ DT = 1e-4
 #            stepping), FP64 rates 48 B written                    = 120 B
 #   density: pm+velh 32 B read, FP64 rho,p,cs 24 B + st 16 B written = 72 B
 ALG_BYTES = {"RatesStage": 120.0, "DensityStage": 72.0, "ListStage": 8.0}
-# Survey algorithmic bytes of a whole RK2 step per particle (3D)
+# Compulsory HBM bytes of a whole RK2 step per particle (3D): cell keys,
+# counting sort, reorder, density + Tait, momentum, per evaluation, plus the
+# predictor and final integrator updates
 STEP_ALG_BYTES = 694.0
 # FLOPs per neighbour pair: density 24, momentum 72 (FMA = 2)
 PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}

@@ -1,5 +1,5 @@
 """Deferred check of light neighbour refreshes: the integrators' updates
-return before the device has judged the refresh, the next pair pass is
+return before the device has checked the refresh, the next pair pass is
 launched gated and repeated after a full build when the lists were stale.
 Results must be those of the synchronous update, bit for bit."""
 import numpy as np
