@@ -60,6 +60,15 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md,
 # list-streaming passes); the traffic grows with the particle count, so it is scaled by n
 NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 388.0, "RatesStage": 436.0}
+# The unit that bounds each pair kernel in the same capture, as a fraction of
+# that unit's peak: the rates pass is bound by the L1 data pipe that feeds its
+# neighbour gathers, the density pass by instruction issue
+NCU_LIMITER = {
+    "RatesStage": {"kernel": "k_rates", "unit": "L1 data-pipe wavefronts", "frac": 0.726,
+                   "issue_frac": 0.671, "dram_frac": 0.158},
+    "DensityStage": {"kernel": "k_density", "unit": "instruction issue", "frac": 0.724,
+                     "l1_frac": 0.490, "dram_frac": 0.254},
+}
 
 
 def measured_peaks():
@@ -473,7 +482,10 @@ def run_gpu(args):
                      "peak_kind": peak_kind,
                      "alg_bytes_per_particle": ALG_BYTES[dom],
                      "note": "pair kernels bound by issue (density) and the L1 data pipe "
-                             "(rates gathers), not HBM; fp32 context in fp32_context"},
+                             "(rates gathers), not HBM; fp32 context in fp32_context",
+                     "limiter": dict(NCU_LIMITER.get(dom, {}),
+                                     source="ncu --set full capture at 1M particles "
+                                            "(profiles/ncu_k_density_k_rates_cube_1M.md)")},
         "fp32_context": {"kernel": dom, "achieved_tflops": flops,
                          "nominal_peak_tflops": FP32_NOMINAL_TFLOPS,
                          "frac_of_nominal": flops / FP32_NOMINAL_TFLOPS},
