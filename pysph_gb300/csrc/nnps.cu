@@ -148,9 +148,13 @@ __global__ void k_keys(sph_array_view a, Grid g, int *key, int *count) {
     }
 }
 
-// exclusive scan, 3 phases: per-tile scan + tile totals, scan of totals, add
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kThreads * kScanItems;
+// exclusive scan, 3 phases over tiles of kScanTile counts: tile totals
+// (read only), exclusive scan of the totals, then each tile re-read, scanned
+// and written with its offset.  Every thread moves one int4 per step, so a
+// warp's accesses are 512 contiguous bytes.
+constexpr int kScanV = 4;                                   // counts per thread per step
+constexpr int kScanSteps = 8;
+constexpr int kScanTile = kThreads * kScanV * kScanSteps;   // 8192 counts
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int *smem, int &total) {
     // warp inclusive scan
@@ -180,23 +184,27 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *smem, int &total
     return warp_prefix + x - v;
 }
 
-__global__ void k_scan_tiles(int *data, int64_t n, int *tile_tot) {
+// the four counts of step st of this thread (0 past n)
+__device__ __forceinline__ int4 scan_load(const int *data, int64_t n, int64_t i) {
+    if (i + kScanV <= n) return *reinterpret_cast<const int4 *>(data + i);
+    int4 v = make_int4(0, 0, 0, 0);
+    if (i < n) v.x = data[i];
+    if (i + 1 < n) v.y = data[i + 1];
+    if (i + 2 < n) v.z = data[i + 2];
+    return v;
+}
+
+__global__ void k_scan_reduce(const int *data, int64_t n, int *tile_tot) {
     __shared__ int smem[32];
-    int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
-    int v[kScanItems];
+    const int64_t base = blockIdx.x * (int64_t)kScanTile;
     int s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = (base + k < n) ? data[base + k] : 0;
-        s += v[k];
+    for (int st = 0; st < kScanSteps; ++st) {
+        const int4 v = scan_load(data, n, base + ((int64_t)st * kThreads + threadIdx.x) * kScanV);
+        s += v.x + v.y + v.z + v.w;
     }
     int total;
-    int pre = block_exclusive_scan(s, smem, total);
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) data[base + k] = pre;
-        pre += v[k];
-    }
+    block_exclusive_scan(s, smem, total);
     if (threadIdx.x == 0) tile_tot[blockIdx.x] = total;
 }
 
@@ -213,11 +221,25 @@ __global__ void k_scan_totals(int *tot, int64_t ntiles) {
     }
 }
 
-__global__ void k_scan_add(int *data, int64_t n, const int *tile_off) {
-    int add = tile_off[blockIdx.x];
-    int64_t base = blockIdx.x * (int64_t)kScanTile;
-    for (int k = threadIdx.x; k < kScanTile; k += blockDim.x)
-        if (base + k < n) data[base + k] += add;
+__global__ void k_scan_apply(int *data, int64_t n, const int *tile_off) {
+    __shared__ int smem[32];
+    const int64_t base = blockIdx.x * (int64_t)kScanTile;
+    int carry = tile_off[blockIdx.x];
+    for (int st = 0; st < kScanSteps; ++st) {
+        const int64_t i = base + ((int64_t)st * kThreads + threadIdx.x) * kScanV;
+        const int4 v = scan_load(data, n, i);
+        int total;
+        const int pre = carry + block_exclusive_scan(v.x + v.y + v.z + v.w, smem, total);
+        const int4 o = make_int4(pre, pre + v.x, pre + v.x + v.y, pre + v.x + v.y + v.z);
+        if (i + kScanV <= n) {
+            *reinterpret_cast<int4 *>(data + i) = o;
+        } else {
+            if (i < n) data[i] = o.x;
+            if (i + 1 < n) data[i + 1] = o.y;
+            if (i + 2 < n) data[i + 2] = o.z;
+        }
+        carry += total;
+    }
 }
 
 __global__ void k_scatter(int64_t n, const int *key, int *cursor, int *perm) {
@@ -506,9 +528,9 @@ int scan_exclusive(sph_ctx *ctx, int *data, int64_t n) {
     int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     int rc = ensure(&ctx->scan_tmp, ctx->scan_tmp_cap, ntiles);
     if (rc) return rc;
-    k_scan_tiles<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    k_scan_reduce<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
     k_scan_totals<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, ntiles);
-    k_scan_add<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
+    k_scan_apply<<<(unsigned)ntiles, kThreads, 0, ctx->stream>>>(data, n, ctx->scan_tmp);
     count_launch(3);
     SPH_LAUNCH_CHECK("scan");
     return SPH_OK;
