@@ -618,17 +618,39 @@ def run_gpu_drops(args):
     t_total = sum(step_ms) / 1e3
     steps = args.steps
 
-    # e2e: host state in, one graph step, host state out
+    # e2e: host state in, one graph step, host state out -- staged (the
+    # upload of step k+1 and the read-back of step k on copy streams beside
+    # the steps), and serial (set -> step -> get_all) for comparison
     fin = ("x", "y", "u", "v")
     fout = ("x", "y", "u", "v", "rho", "p")
     host = {f: torch.from_numpy(batch.get_all(f)).pin_memory() for f in fin}
+
+    def staged_loop(nsteps):
+        up = batch.upload(**host)
+        pending = None
+        for k in range(nsteps):
+            batch.set_staged(up)
+            if k + 1 < nsteps:
+                up = batch.upload(**host)
+            batch.step(1, check=False)
+            dl = batch.download(*fout)
+            if pending is not None:
+                pending.result()
+            pending = dl
+        return pending.result()
+
+    staged_loop(max(1, args.warmup))     # untimed: first use of the copy streams
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = staged_loop(steps)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(steps):
         batch.set(**host)
         batch.step(1, check=False)
         out = batch.get_all(*fout)
-    e2e_t = time.perf_counter() - t0
+    e2e_serial_t = time.perf_counter() - t0
     batch.check()
     del out
 
@@ -652,7 +674,11 @@ def run_gpu_drops(args):
         "gpu_launches": launches,
         "e2e": {"value": len(drops) * steps / e2e_t, "unit": DROPS_UNIT,
                 "h2d_bytes_per_step": 8 * n * len(fin), "d2h_bytes_per_step": 8 * n * len(fout),
-                "ms_per_step": e2e_t / steps * 1e3},
+                "ms_per_step": e2e_t / steps * 1e3,
+                "transfers": "staged: SimulationBatch.upload / set_staged / download",
+                "serial": {"value": len(drops) * steps / e2e_serial_t,
+                           "ms_per_step": e2e_serial_t / steps * 1e3,
+                           "transfers": "SimulationBatch.set -> step -> get_all"}},
         "clocks": clk,
     }
     if not args.no_cpu_baseline:

@@ -38,7 +38,8 @@ def copy_stream(kind):
 
 
 class StagedUpload:
-    """Host values in flight to a particle array (``ParticleArray.upload``)."""
+    """Host values in flight to a particle array (``ParticleArray.upload``)
+    or a batch of simulations (``SimulationBatch.upload``)."""
 
     def __init__(self, pa, groups, ready):
         self.pa = pa
@@ -102,6 +103,72 @@ def _copy_all(dst, src):
             d.copy_(s)
 
 
+def upload_tensors(targets, props, n):
+    """Start the host-to-device copies of ``props`` (name -> host values)
+    for the device tensors ``targets`` (name -> tensor of ``n`` values) on
+    the copy stream; returns a ``StagedUpload`` (its ``pa`` left unset)."""
+    srcs = {}
+    for p, val in props.items():
+        src = _host_source(val, targets[p].dtype)
+        if src.numel() != n:
+            raise ValueError("size mismatch uploading %s: %d != %d" % (p, src.numel(), n))
+        srcs[p] = src
+    cs = copy_stream("h2d")
+    groups = []
+    with torch.cuda.stream(cs):
+        for names in _by_dtype(targets, list(props)):
+            # one device buffer per dtype, allocated for the copy stream
+            buf = torch.empty((len(names), n), dtype=targets[names[0]].dtype,
+                              device=targets[names[0]].device)
+            for r, p in enumerate(names):
+                buf[r].copy_(srcs[p], non_blocking=True)
+            groups.append((names, buf))
+        ready = torch.cuda.Event()
+        ready.record(cs)
+    return StagedUpload(None, groups, ready)
+
+
+def apply_staged(targets, up, stream):
+    """Make ``stream`` wait for the upload's copies and copy its rows into
+    ``targets`` there (one multi-tensor copy per dtype)."""
+    if up.applied:
+        raise ValueError("set_staged: upload already applied")
+    stream.wait_event(up.ready)
+    with torch.cuda.stream(stream):
+        for names, buf in up.groups:
+            buf.record_stream(stream)
+            _copy_all([targets[p] for p in names], list(buf.unbind(0)))
+    up.applied = True
+    names = [p for names, _ in up.groups for p in names]
+    up.groups = None
+    return names
+
+
+def download_tensors(tensors, names, stream):
+    """Stack ``tensors`` (name -> device tensor, same length) on ``stream``
+    and copy the stack to page-locked host memory on the copy stream."""
+    cs = copy_stream("d2h")
+    snaps = []
+    with torch.cuda.stream(stream):
+        for group in _by_dtype(tensors, list(dict.fromkeys(names))):
+            s = torch.stack([tensors[a] for a in group])
+            s.record_stream(cs)                # read there by the copy
+            snaps.append((group, s))
+        snapped = torch.cuda.Event()
+        snapped.record(stream)
+    where = {}
+    with torch.cuda.stream(cs):
+        cs.wait_event(snapped)
+        for group, s in snaps:
+            h = torch.empty(s.shape, dtype=s.dtype, pin_memory=True)
+            h.copy_(s, non_blocking=True)
+            for r, a in enumerate(group):
+                where[a] = (h, r)
+        done = torch.cuda.Event()
+        done.record(cs)
+    return StagedDownload(tuple(names), [where[a] for a in names], done)
+
+
 def upload(pa, props):
     if not props:
         raise ValueError("upload: no properties")
@@ -111,44 +178,19 @@ def upload(pa, props):
             raise ValueError("upload: %s is not a numeric property" % p)
         if not pa._props[p].is_cuda:
             raise RuntimeError("upload needs the arrays on a GPU")
-    n = pa.get_number_of_particles()
-    srcs = {}
-    for p, val in props.items():
-        src = _host_source(val, pa._props[p].dtype)
-        if src.numel() != n:
-            raise ValueError("size mismatch uploading %s: %d != %d" % (p, src.numel(), n))
-        srcs[p] = src
-    main = torch.cuda.current_stream()
-    cs = copy_stream("h2d")
-    groups = []
-    with torch.cuda.stream(cs):
-        for names in _by_dtype(pa._props, list(props)):
-            # one device buffer per dtype, allocated for the copy stream
-            buf = torch.empty((len(names), n), dtype=pa._props[names[0]].dtype,
-                              device=pa._props[names[0]].device)
-            for r, p in enumerate(names):
-                buf[r].copy_(srcs[p], non_blocking=True)
-            buf.record_stream(main)            # read there by set_staged
-            groups.append((names, buf))
-        ready = torch.cuda.Event()
-        ready.record(cs)
-    return StagedUpload(pa, groups, ready)
+    up = upload_tensors(pa._props, props, pa.get_number_of_particles())
+    up.pa = pa
+    return up
 
 
 def set_staged(pa, up):
     if not isinstance(up, StagedUpload) or up.pa is not pa:
         raise ValueError("set_staged takes an upload of this particle array")
-    if up.applied:
-        raise ValueError("set_staged: upload already applied")
     if up.groups and up.groups[0][1].shape[1] != pa.get_number_of_particles():
         raise ValueError("set_staged: the particle count changed since the upload")
-    torch.cuda.current_stream().wait_event(up.ready)
-    for names, buf in up.groups:
-        _copy_all([pa._props[p] for p in names], list(buf.unbind(0)))
-        if any(p in ("x", "y", "z") for p in names):
-            pa.set_dirty(True)
-    up.applied = True
-    up.groups = None
+    names = apply_staged(pa._props, up, torch.cuda.current_stream())
+    if any(p in ("x", "y", "z") for p in names):
+        pa.set_dirty(True)
     pa.touch()
 
 
@@ -161,25 +203,6 @@ def download(pa, names, only_real_particles=True):
             raise ValueError("download: %s is not a property" % a)
         if not pa._props[a].is_cuda:
             raise RuntimeError("download needs the arrays on a GPU")
-    main = torch.cuda.current_stream()
-    cs = copy_stream("d2h")
     m = pa.num_real_particles if only_real_particles else pa.get_number_of_particles()
-    snaps = []
-    for group in _by_dtype(pa._props, list(dict.fromkeys(names))):
-        # one snapshot kernel per dtype, on the compute stream
-        s = torch.stack([pa._props[a][:m] for a in group])
-        s.record_stream(cs)                    # read there by the copy
-        snaps.append((group, s))
-    snapped = torch.cuda.Event()
-    snapped.record(main)
-    where = {}
-    with torch.cuda.stream(cs):
-        cs.wait_event(snapped)
-        for group, s in snaps:
-            h = torch.empty(s.shape, dtype=s.dtype, pin_memory=True)
-            h.copy_(s, non_blocking=True)
-            for r, a in enumerate(group):
-                where[a] = (h, r)
-        done = torch.cuda.Event()
-        done.record(cs)
-    return StagedDownload(tuple(names), [where[a] for a in names], done)
+    tensors = {a: pa._props[a][:m] for a in dict.fromkeys(names)}
+    return download_tensors(tensors, names, torch.cuda.current_stream())

@@ -18,6 +18,7 @@ import numpy as np
 import torch
 
 from . import native
+from .base import transfer
 
 PROPS = ("x", "y", "z", "u", "v", "w", "m", "h", "rho", "p", "cs")
 
@@ -186,6 +187,43 @@ class SimulationBatch:
                 raise ValueError("property %r needs %d values" % (name, self.n))
             self.arrays[name].copy_(t.reshape(-1), non_blocking=True)
         torch.cuda.current_stream().synchronize()
+
+    # -- staged host transfers (see pysph_gb300.base.transfer) -----------------
+    def _torch_stream(self):
+        s = getattr(self, "_tstream", None)
+        if s is None:
+            s = self._tstream = self.stream()
+        return s
+
+    def upload(self, **props):
+        """Start copying whole concatenated properties from host memory
+        (page-locked for an asynchronous copy) on a copy stream; returns at
+        once.  Page-locked sources must stay unchanged until ``set_staged``."""
+        for name in props:
+            if name not in self.arrays:
+                raise ValueError("unknown batch property %r" % name)
+        up = transfer.upload_tensors(self.arrays, props, self.n)
+        up.pa = self
+        return up
+
+    def set_staged(self, up):
+        """``set`` with the values of an earlier ``upload``: the batch's
+        stream waits for its copies and takes them over on the device (no
+        host synchronisation)."""
+        if not isinstance(up, transfer.StagedUpload) or up.pa is not self:
+            raise ValueError("set_staged takes an upload of this batch")
+        transfer.apply_staged(self.arrays, up, self._torch_stream())
+
+    def download(self, *props):
+        """Start reading whole concatenated properties back: a device
+        snapshot on the batch's stream, copied to page-locked host memory on
+        a copy stream.  ``result()`` of the returned object waits for those
+        copies only."""
+        for name in props:
+            if name not in self.arrays:
+                raise ValueError("unknown batch property %r" % name)
+        return transfer.download_tensors({p: self.arrays[p] for p in props}, props,
+                                         self._torch_stream())
 
     def _host(self, tensors):
         """Host copies through page-locked buffers, one synchronisation."""

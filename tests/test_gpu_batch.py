@@ -83,3 +83,41 @@ def test_batch_reports_particles_leaving_their_grid():
     batch.arrays["u"][a:b] = 1e5
     with pytest.raises(RuntimeError):
         batch.step(3)
+
+
+def test_batch_staged_transfers_match_set_and_get():
+    """SimulationBatch.upload / set_staged / download: the same state and
+    results as set / step / get_all, with the copies on copy streams."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from pysph_gb300 import workloads as W
+    from pysph_gb300.batch import SimulationBatch
+    drops = [W.elliptical_drop(dx=0.05, radius=r, c0=100.0) for r in (0.6, 1.0, 1.3)]
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0)
+    batch.step(2)
+    fin = ("x", "y", "u", "v")
+    fout = ("x", "y", "u", "v", "rho", "p")
+    host = {f: torch.from_numpy(batch.get_all(f)).pin_memory() for f in fin}
+    serial = []
+    for _ in range(3):
+        batch.set(**host)
+        batch.step(1)
+        serial.append(batch.get_all(*fout))
+    staged = []
+    up = batch.upload(**host)
+    pending = None
+    for k in range(3):
+        batch.set_staged(up)
+        if k < 2:
+            up = batch.upload(**host)
+        batch.step(1)
+        dl = batch.download(*fout)
+        if pending is not None:
+            staged.append(pending.result())
+        pending = dl
+    staged.append(pending.result())
+    for a, b in zip(serial, staged):
+        for p, x, y in zip(fout, a, b):
+            assert np.array_equal(x, y), p
+    with pytest.raises(ValueError):
+        batch.upload(q=np.zeros(batch.n))
