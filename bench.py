@@ -57,8 +57,8 @@ STEP_ALG_BYTES = 694.0
 PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture of the 1M-particle lattice, profiles/ncu_k_density_k_rates_cube_1M.md,
-# list-streaming passes); the traffic grows with the particle count, so it is scaled by n
+# of one ncu capture of the 1M-particle lattice, list-streaming passes); the
+# traffic grows with the particle count, so it is scaled by n
 NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 388.0, "RatesStage": 436.0}
 # The unit that bounds each pair kernel in the same capture, as a fraction of
 # that unit's peak: the rates pass is bound by the L1 data pipe that feeds its
@@ -69,6 +69,18 @@ NCU_LIMITER = {
     "DensityStage": {"kernel": "k_density", "unit": "instruction issue", "frac": 0.724,
                      "l1_frac": 0.490, "dram_frac": 0.254},
 }
+
+
+def fp32_peak_tflops():
+    """FP32 FMA peak: 152 SMs x 128 lanes x 2 FLOP x the maximum SM clock
+    measured on this machine (MEASURED_PEAKS.json sm_max_mhz), else 2070 MHz."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            mhz = float(json.load(fh)["sm_max_mhz"])
+        kind = "nominal lanes x measured max SM clock"
+    except (OSError, KeyError, ValueError):
+        mhz, kind = 2070.0, "nominal"
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12, kind
 
 
 def measured_peaks():
@@ -275,6 +287,8 @@ def cpu_baseline(procs, warmup, steps, n=SAMPLE_N):
         cores = procs * oracle.num_threads()
     return {
         "value": value, "unit": UNIT, "cores": cores, "kind": kind, "cpu": cpu_model(),
+        "ms_per_step": max(r["seconds"] for r in res) / steps * 1e3,
+        "particles_per_process": n,
         "pinning": "process i on core i" if kind == "reference" else "none (OpenMP)",
         "sample": "%d independent %s processes, each %d RK2 steps of a %d-particle "
                   "jittered lattice (h=1.2dx, same physics), after %d warm-up steps; "
@@ -319,6 +333,64 @@ def replicas_value(units_per_rank, world, seconds):
     return world * units_per_rank / seconds
 
 
+def _timed_window(integ, cm, steps, flush):
+    """Time ``steps`` integrator steps with CUDA events on the current
+    stream, L2 flushed (outside the events) before each.  Returns the step
+    times (ms), the per-stage times (ms lists), the full builds / light
+    refreshes in the window and the library launches."""
+    import torch
+    from pysph_gb300 import native
+    torch.cuda.synchronize()
+    launches0 = native.launch_count()
+    builds0 = cm.build_stats()
+    integ.stage_events = []
+    step_ms = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        integ.integrate(DT)
+        b.record()
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    launches = native.launch_count() - launches0
+    events = integ.stage_events
+    integ.stage_events = None
+    stage_ms = {}
+    for name, a, b in events:
+        stage_ms.setdefault(name, []).append(a.elapsed_time(b))
+    builds = cm.build_stats()
+    return step_ms, stage_ms, (builds[0] - builds0[0], builds[1] - builds0[1]), launches
+
+
+def _full_rebuild_leg(api, props, steps, warmup, flush, pairs_per_step):
+    """The same step with no neighbour-list skin: every update is a full
+    neighbour build (box, counting sort, reorder, the density pass that
+    writes the lists), as the reference rebuilds at every
+    ``particles.update()`` (base/nnps.pyx:581-620)."""
+    from pysph_gb300 import workloads as W
+    prev = os.environ.get("PYSPH_GB300_SKIN")
+    os.environ["PYSPH_GB300_SKIN"] = "0"
+    try:
+        s, particles = W.setup_cube(api, props)
+    finally:
+        if prev is None:
+            os.environ.pop("PYSPH_GB300_SKIN", None)
+        else:
+            os.environ["PYSPH_GB300_SKIN"] = prev
+    integ = s.integrator
+    for _ in range(warmup):
+        integ.integrate(DT)
+    step_ms, stage_ms, builds, launches = _timed_window(integ, particles.cell_manager, steps, flush)
+    ms = statistics.mean(step_ms)
+    return {"value": pairs_per_step / (ms / 1e3), "unit": UNIT, "steps": steps,
+            "ms_per_step": ms, "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
+            "timed_full": builds[0], "timed_light": builds[1], "gpu_launches": launches,
+            "skin": 0.0}
+
+
 def run_gpu(args):
     import torch
 
@@ -352,42 +424,29 @@ def run_gpu(args):
     pairs_per_step = 4.0 * kbar * n
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, interval_ms=20)
     clocks.start()
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
-    launches0 = native.launch_count()
-    builds0 = cm.build_stats()
     deferred0 = cm.deferred_stats()
-    integ.stage_events = []
-    step_ms = []
     t_begin = time.monotonic()
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record()
-        integ.integrate(DT)
-        b.record()
-        b.synchronize()
-        step_ms.append(a.elapsed_time(b))
-    torch.cuda.synchronize()
+    step_ms, stage_ms, builds, launches = _timed_window(integ, cm, args.steps, flush)
     if pg:
         pg.barrier()
-    launches = native.launch_count() - launches0
-    clocks.mark(t_begin, time.monotonic())
-    clk = clocks.stop()
-    builds = cm.build_stats()
-    builds = (builds[0] - builds0[0], builds[1] - builds0[1])
+    t_end = time.monotonic()
     deferred = cm.deferred_stats()
     deferred = (deferred[0] - deferred0[0], deferred[1] - deferred0[1])
-    events = integ.stage_events
-    integ.stage_events = None
     t_total = max_over_ranks(sum(step_ms) / 1e3, pg)
-    stage_ms = {}
-    for name, a, b in events:
-        stage_ms.setdefault(name, []).append(a.elapsed_time(b))
+    life = cm.build_stats()          # every update of this context so far
+    # the reference-equivalent step: a full neighbour build at every update
+    full_leg = None
+    if not args.no_full_rebuild_leg:
+        t_fb = time.monotonic()
+        full_leg = _full_rebuild_leg(api, props, min(args.steps, 20), 3, flush, pairs_per_step)
+        full_leg["clock_window_s"] = round(time.monotonic() - t_fb, 3)
+    clocks.mark(t_begin, t_end)
+    clk = clocks.stop()
 
     # e2e through the public API with host buffers: every step uploads the
     # state from page-locked memory and reads its results back.  Staged: the
@@ -443,7 +502,14 @@ def run_gpu(args):
     avg_ms = statistics.mean(stage_ms[dom]) if launches_dom else float("nan")
     achieved = ALG_BYTES[dom] * n / (avg_ms / 1e3) / 1e9
     flops = PAIR_FLOPS[dom] * kbar * n / (avg_ms / 1e3) / 1e12
+    fp32_peak, fp32_src = fp32_peak_tflops()
     step_s = t_total / steps
+    # whole-step rooflines: B_alg = 694 B and F_alg = 2 K (24 + 72) FLOP per
+    # particle per RK2 step (compulsory bytes; density + momentum pair FLOPs)
+    f_alg = 2.0 * kbar * (PAIR_FLOPS["DensityStage"] + PAIR_FLOPS["RatesStage"])
+    hbm_frac = STEP_ALG_BYTES * n / step_s / 1e9 / peak
+    fp32_frac = f_alg * n / step_s / 1e12 / fp32_peak
+    rebuild_frac = life[0] / max(1, life[0] + life[1])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
@@ -484,16 +550,32 @@ def run_gpu(args):
                      "note": "pair kernels bound by issue (density) and the L1 data pipe "
                              "(rates gathers), not HBM; fp32 context in fp32_context",
                      "limiter": dict(NCU_LIMITER.get(dom, {}),
-                                     source="ncu --set full capture at 1M particles "
-                                            "(profiles/ncu_k_density_k_rates_cube_1M.md)")},
+                                     source="ncu --set full capture at 1M particles")},
         "fp32_context": {"kernel": dom, "achieved_tflops": flops,
                          "nominal_peak_tflops": FP32_NOMINAL_TFLOPS,
                          "frac_of_nominal": flops / FP32_NOMINAL_TFLOPS},
         "step_roofline": {"alg_bytes_per_particle_step": STEP_ALG_BYTES,
+                          "alg_flops_per_particle_step": f_alg,
                           "achieved_gbs": STEP_ALG_BYTES * n / step_s / 1e9,
-                          "frac": STEP_ALG_BYTES * n / step_s / 1e9 / peak},
+                          "achieved_tflops": f_alg * n / step_s / 1e12,
+                          "frac": hbm_frac,
+                          "hbm": hbm_frac, "fp32": fp32_frac,
+                          "achieved": max(hbm_frac, fp32_frac),
+                          "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind,
+                          "fp32_peak_tflops": fp32_peak, "fp32_peak_kind": fp32_src},
         "clocks": clk,
     }
+    line["roofline"]["fp32"] = {"achieved_tflops": flops, "peak_tflops": fp32_peak,
+                                "frac": flops / fp32_peak, "peak_kind": fp32_src,
+                                "flops_per_pair": PAIR_FLOPS[dom]}
+    line["nnps_builds"]["rebuild_fraction_all_updates"] = rebuild_frac
+    line["nnps_builds"]["updates_all"] = life[0] + life[1]
+    if full_leg is not None:
+        line["full_rebuild"] = full_leg
+        # amortised step at the rebuild rate this context has seen so far
+        ms_skin = step_s * 1e3
+        line["nnps_builds"]["amortised_ms_per_step"] = (
+            ms_skin + rebuild_frac * (full_leg["ms_per_step"] - ms_skin))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(1, 1, args.cpu_steps)
     if rank == 0:
@@ -960,9 +1042,23 @@ def run_reference(args):
         return
     procs = args.procs or os.cpu_count() or 1
     cb = cpu_baseline(procs, args.warmup, args.steps)
+    # the bench's own size on one pinned core: whole RK2 steps of the
+    # 1,000,000-particle lattice (each rebuilds the neighbour cache)
+    full = None
+    if args.ref_1m_steps > 0:
+        if reference_available():
+            r = _cpu_worker(("reference", 1_000_000, 0, args.ref_1m_steps, 0, 0))
+            full = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": 1,
+                    "particles": 1_000_000, "steps": args.ref_1m_steps,
+                    "ms_per_step": r["seconds"] / args.ref_1m_steps * 1e3,
+                    "mean_neighbours": r["kbar"], "pinning": "core 0",
+                    "kind": "reference"}
+        else:
+            full = {"unavailable": "the compiled reference is not built on this host"}
     line = {
         "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "ms_per_step": cb["ms_per_step"],
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
         "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": "3D jittered lattice, h=1.2dx, RK2, NNPS+SPHRho+Tait+PGrad+"
@@ -971,7 +1067,11 @@ def run_reference(args):
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "ms_per_step_note": "wall time per RK2 step of the slowest process (its %d-particle "
+                            "sample)" % SAMPLE_N,
     }
+    if full is not None:
+        line["single_core_1M"] = full
     print(json.dumps(line), flush=True)
 
 
@@ -988,6 +1088,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--procs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-rebuild-leg", action="store_true")
+    ap.add_argument("--ref-1m-steps", type=int, default=3)
     ap.add_argument("--workload", default="cube", choices=["cube", "drops", "closure", "mlp"])
     ap.add_argument("--mlp-n", type=int, default=1 << 20)
     ap.add_argument("--samples", type=int, default=10_000_000)

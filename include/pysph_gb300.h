@@ -273,16 +273,17 @@ int sph_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nline
 int sph_invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
 
 /* Allocation-free variant of sph_invariants (no counterpart in the
- * reference).  For callers that cannot allocate device memory: code running
- * under CUDA stream capture, loops that forbid allocation after start-up,
- * hosts whose allocator owns all device memory.  Needs no context; its
- * scratch is a fixed file-scope device array (192 KiB per GPU that loads
- * the library, held until exit) that every call shares, so calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on a device looks up the scratch's device address; make it before
- * any stream capture.  Rejects arrays of more than 16777216 particles with
- * SPH_ERR_ARG.  stream: a cudaStream_t (NULL = default stream).  out: 6
- * host doubles as for sph_invariants.  Synchronises the stream. */
+ * reference).  For callers that cannot allocate device memory: real-time
+ * loops that forbid allocation after start-up (a cudaMalloc can block or
+ * fail mid-run), and host applications whose own allocator reserves all
+ * device memory up front.  Needs no context; its scratch is a fixed
+ * file-scope device array (192 KiB per GPU that loads the library, held
+ * until exit) that every call shares, so calls that overlap on the GPU race
+ * and must be serialised by the caller.  The first call on a device looks
+ * up the scratch's device address.  Rejects arrays of more than 16777216
+ * particles with SPH_ERR_ARG.  stream: a cudaStream_t (NULL = default
+ * stream).  out: 6 host doubles as for sph_invariants; the call copies them
+ * to the host and synchronises the stream before it returns. */
 int sph_invariants_noalloc(const sph_array_view *a, double *out, void *stream);
 
 /* ---------------------------------------------------------------------

@@ -289,7 +289,8 @@ def _recipe_id():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PYSPH_REFERENCE_TREE", "/root/reference"),
+                    help="the reference's source tree (default: environment PYSPH_REFERENCE_TREE)")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--cythonize-only", action="store_true")
     ap.add_argument("--compile", action="store_true",

@@ -1,11 +1,14 @@
 // Allocation-free FP64 invariant sums (sph_invariants_noalloc).
 //
 // For callers that cannot allocate device memory themselves or let a library
-// do it: code running while a stream is being captured into a CUDA graph
-// (cudaMalloc is not allowed then), real-time loops that forbid allocation
-// after start-up, and host applications whose allocator owns all device
-// memory.  The variant needs no context: its scratch is the file-scope
-// device array below, sized for at most kNoAllocMaxParticles particles.
+// do it: real-time loops that forbid any allocation after start-up (a
+// cudaMalloc can block on the device or fail in the middle of a run), and
+// host applications whose own allocator reserves all device memory up front
+// (an allocation by a library then fails or escapes the host's accounting).
+// The variant needs no context: its scratch is the file-scope device array
+// below, sized for at most kNoAllocMaxParticles particles.  Each call copies
+// the six sums into the caller's host buffer and synchronises the stream
+// before it returns.
 //
 // Every GPU that loads the library holds the scratch until the process
 // exits.  All calls share it: two calls that overlap on the GPU (different

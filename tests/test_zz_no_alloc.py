@@ -1,10 +1,11 @@
 """The allocation-free invariant sums against the context-based ones.
 
 ``sph_invariants_noalloc`` serves callers that cannot allocate device
-memory (stream capture, allocation-free loops, hosts owning all device
-memory): it keeps its scratch in a fixed device array inside the library.
-This file is collected last so that a failure here comes after every other
-test has run; it also passes on its own in a fresh process.
+memory: real-time loops that forbid allocation after start-up, and hosts
+whose own allocator reserves all device memory.  It keeps its scratch in a
+fixed device array inside the library.  This file is collected last so that
+a failure here comes after every other test has run; it also passes on its
+own in a fresh process.
 """
 import ctypes
 
@@ -76,3 +77,38 @@ def test_noalloc_rejects_arrays_beyond_its_scratch():
     rc = native.lib().sph_invariants_noalloc(ctypes.byref(v), out, None)
     assert rc == native.SPH_ERR_ARG
     assert "16777216" in native.last_error()
+
+
+def test_noalloc_counts_only_local_real_particles():
+    """Non-LocalReal particles (ghosts, remote copies) are left out of every
+    sum, as in sph_invariants."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    pa, particles = _setup(8000, seed=13)
+    tag = np.zeros(8000, dtype=np.int64)
+    tag[::7] = 1
+    tag[3::11] = 2
+    pa.set(tag=tag)              # align_particles moves the non-real ones to the end
+    real = pa.get("tag") == 0
+    m, u, v, w = (pa.get(k) for k in ("m", "u", "v", "w"))
+    want = np.array([m[real].sum(), (m * u)[real].sum(), (m * v)[real].sum(),
+                     (m * w)[real].sum(), (0.5 * m * (u * u + v * v + w * w))[real].sum(),
+                     float(real.sum())])
+    got = _noalloc(pa)
+    ref = _context(particles)
+    assert got[5] == real.sum() and ref[5] == real.sum()
+    assert _close(got, ref), (got, ref)
+    assert _close(got, want), (got, want)
+
+
+def test_noalloc_empty_array_gives_zeros():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from pysph_gb300 import native
+    v = native.ArrayView()
+    v.n = 0
+    out = (ctypes.c_double * 6)(*([7.0] * 6))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    native.check(native.lib().sph_invariants_noalloc(ctypes.byref(v), out, stream),
+                 "sph_invariants_noalloc")
+    assert list(out) == [0.0] * 6
