@@ -208,6 +208,20 @@ int sph_nnps_deferred_stats(sph_ctx *ctx, int64_t *out);
 /* out[0] = full builds, out[1] = light refreshes of this context. */
 int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
 
+/* Brick-staged pair passes (on = 1, the default): for one source of uniform
+ * h without a periodic axis or the variable-h relation, sph_density
+ * (SPHRho, + Tait) and sph_rates with the terms PGRAD | AVISC (+ XSPH) run
+ * kernels that stage, per brick of grid cells, the records of every source
+ * within the stencil of the brick in shared memory once, and stream a
+ * neighbour list of 16-bit indices into that staging.  Results are those of
+ * the list-streaming kernels within FP32 rounding (positions relative to the
+ * brick centre instead of the particle's cell); neighbour sets are the same.
+ * on = 0 selects the list-streaming kernels everywhere.  Takes effect at the
+ * next build.  The same reference routines as sph_density / sph_rates. */
+int sph_ctx_set_bricks(sph_ctx *ctx, int on);
+/* out[0] = pair passes run by the brick-staged kernels in this context. */
+int sph_pair_pass_stats(sph_ctx *ctx, int64_t *out);
+
 /* Neighbour lists of destination dst among source src (radius
  * radius_scale*h_dst, radius_scale no larger than the build's), as original particle
  * indices: counts[i] (device, int64, n_dst) then, given the exclusive prefix

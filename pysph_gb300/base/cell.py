@@ -161,6 +161,8 @@ class CellManager:
                              "sph_ctx_set_periodic")
             if self.deferred_check:
                 native.check(L.sph_ctx_set_deferred(h, 1), "sph_ctx_set_deferred")
+            from ..tuning import brick_passes
+            native.check(L.sph_ctx_set_bricks(h, 1 if brick_passes() else 0), "sph_ctx_set_bricks")
             self._ctx = h
         native.check(L.sph_ctx_set_stream(self._ctx, ctypes.c_void_p(
             torch.cuda.current_stream().cuda_stream)), "sph_ctx_set_stream")
@@ -270,6 +272,14 @@ class CellManager:
         out = (ctypes.c_int64 * 2)()
         native.check(native.lib().sph_nnps_stats(self._ctx, out), "sph_nnps_stats")
         return (int(out[0]), int(out[1]))
+
+    def brick_pass_count(self):
+        """Pair passes the brick-staged kernels have run for this cell manager."""
+        if self._ctx is None:
+            return 0
+        out = (ctypes.c_int64 * 1)()
+        native.check(native.lib().sph_pair_pass_stats(self._ctx, out), "sph_pair_pass_stats")
+        return int(out[0])
 
     def deferred_stats(self):
         """(deferred light refreshes, those found stale at their first pass)."""

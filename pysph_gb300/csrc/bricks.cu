@@ -1,0 +1,1027 @@
+// Brick-staged pair passes (sm_103a): the uniform-h summation density
+// (+ Tait) and the PGrad + Monaghan AV (+ XSPH) rates of one simulation.
+//
+// Replaces, for the configurations it covers, the same reference routines
+// as the list-streaming kernels of pairs.cu: SPHCalc.sph -> SPHFunction.eval
+// -> eval_nbr over density_funcs.pyx:38-74 (SPHRho), eos_funcs.pyx:105-116
+// (TaitEquation), pressure_funcs.pyx:40-91 (SPHPressureGradient),
+// viscosity_funcs.pyx:41-124 (MonaghanArtificialVsicosity) and
+// xsph_funcs.pyx:31-88 (XSPHCorrection), and the neighbour cache of
+// base/nnps.pyx:566-620.
+//
+// One block owns one brick of bx * by * bz grid cells.  It copies the
+// records of every source particle within the stencil half-width K of the
+// brick -- the particles of the brick's rows of cells grown by K cells on
+// every side -- once into shared memory, with positions relative to the
+// brick's centre cell (FP32, |x| < ~12 cells, so |r_ab| keeps ~2e-7 of
+// relative accuracy).  A destination's neighbour list then holds 16-bit
+// indices into that staging, fixed between full builds (the sorted order and
+// the cell table do not change), so a pair costs one list entry, shared-
+// memory records and the pair arithmetic: no cell-offset decoding and no
+// global gathers.
+//
+// The neighbour relation is the reference's: strict r^2 < (radius_scale
+// h)^2, decided in FP32 outside a +-1e-5 relative band around the threshold
+// and by the FP64 test of base/nnps.pyx:337-353 inside it.  Neighbours are
+// visited in the order of the list-streaming kernels (stencil rows in (dz,
+// dy) order, ascending sorted slot within a row), and every destination's
+// sums are Neumaier-compensated FP32 over plain batch partials.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+// destination threads per block are chosen per build (the largest brick
+// population rounded to warps); the kernels are compiled for at most this
+constexpr int kBrickMaxThreads = 512;
+
+struct BrickSrcDev {
+    const float4 *pm, *velh, *st;
+    const float *scx;
+    const int *cstart, *perm;
+    const double *x, *y, *z;
+};
+
+struct BrickDstDev {
+    const float4 *pm, *velh, *st;
+    const float *scx;
+    const int *cstart, *perm;
+    const int *bdst;       // exclusive prefix of the destinations per brick
+    const int64_t *tag;
+    const double *x, *y, *z, *h, *u, *v, *w, *p, *cs;
+};
+
+// shared-memory layout of a block (byte offsets into the dynamic array)
+struct BrickSmem {
+    int stage_cap;   // staged records (0: records are read from global memory)
+    int off_v, off_s;             // rates: velocity / state records
+    int off_rlo, off_roff, off_dlo, off_doff, off_scell;
+};
+
+struct BrickDensityArgs {
+    Grid g;
+    BrickGeom bk;
+    BrickDstDev d;
+    BrickSrcDev s;
+    BrickSmem sm;
+    uint16_t *nbr;      // list entries: nbr[bdst[b] * cap + k * D_b + d]
+    int *cnt;           // neighbour count per destination, brick order
+    int *maxcnt;
+    int cap;
+    int build;          // 1: traverse the stencil and write the list
+    int write_out;      // 0: list build only
+    int dim, tait;
+    float co, ro, gamma;
+    double *rho_out, *p_out, *cs_out;
+    float4 *st_out;
+    const unsigned *gate;
+};
+
+struct BrickRatesArgs {
+    Grid g;
+    BrickGeom bk;
+    BrickDstDev d;
+    BrickSrcDev s;
+    BrickSmem sm;
+    const uint16_t *nbr;
+    const int *cnt;
+    int cap;
+    int dim;
+    float alpha, beta, eta2, eps;
+    int add_velocity, add_gravity, accumulate;
+    double gx, gy, gz;
+    double *acc[3];
+    double *pos[3];
+    const unsigned *gate;
+};
+
+// The block's cells: brick [x0, x1) x [y0, y1) x [z0, z1), the staged
+// region [xs0, xs1) x ... (the brick grown by the stencil half-widths,
+// clipped to the grid) and the origin cell of the staged positions.
+struct BlockGeo {
+    int x0, x1, y0, y1, z0, z1;
+    int xs0, xs1, ys0, ys1, zs0, zs1;
+    int lx, ry, nr, dry, ndr;
+    int cxc, cyc, czc;
+};
+
+__device__ __forceinline__ BlockGeo block_geo(const Grid &g, const BrickGeom &bk, int b) {
+    BlockGeo G;
+    const int ibx = b % bk.nbx;
+    const int rest = b / bk.nbx;
+    const int iby = rest % bk.nby;
+    const int ibz = rest / bk.nby;
+    G.x0 = ibx * bk.bx; G.x1 = min(g.nx, G.x0 + bk.bx);
+    G.y0 = iby * bk.by; G.y1 = min(g.ny, G.y0 + bk.by);
+    G.z0 = ibz * bk.bz; G.z1 = min(g.nz, G.z0 + bk.bz);
+    G.xs0 = max(0, G.x0 - g.kx); G.xs1 = min(g.nx, G.x1 + g.kx);
+    G.ys0 = max(0, G.y0 - g.ky); G.ys1 = min(g.ny, G.y1 + g.ky);
+    G.zs0 = max(0, G.z0 - g.kz); G.zs1 = min(g.nz, G.z1 + g.kz);
+    G.lx = G.xs1 - G.xs0;
+    G.ry = G.ys1 - G.ys0;
+    G.nr = G.ry * (G.zs1 - G.zs0);
+    G.dry = G.y1 - G.y0;
+    G.ndr = G.dry * (G.z1 - G.z0);
+    G.cxc = G.x0 + bk.bx / 2;
+    G.cyc = G.y0 + bk.by / 2;
+    G.czc = G.z0 + bk.bz / 2;
+    return G;
+}
+
+// In-place inclusive scan of a[1..n] by one warp (a[0] = 0 on return).
+__device__ __forceinline__ void warp_scan_inplace(int *a, int n) {
+    const int lane = threadIdx.x & 31;
+    int carry = 0;
+    for (int base = 1; base <= n; base += 32) {
+        const int i = base + lane;
+        int x = i <= n ? a[i] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (i <= n) a[i] = x + carry;
+        carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) a[0] = 0;
+}
+
+// Largest r in [0, n) with off[r] <= t (off[n] > t): the row holding index t.
+__device__ __forceinline__ int row_of(const int *off, int n, int t) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= t) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Position record (brick-relative x, y, z and the mass) of sorted slot j of
+// row (cy, cz): the same FP32 operations for destinations and sources.
+__device__ __forceinline__ float4 rel_pos(const float4 *pm, const float *scx, int j, int cy,
+                                          int cz, const BlockGeo &G, float csf) {
+    const float4 p = pm[j];
+    return make_float4(fmaf(scx[j] - (float)G.cxc, csf, p.x),
+                       fmaf((float)(cy - G.cyc), csf, p.y),
+                       fmaf((float)(cz - G.czc), csf, p.z), p.w);
+}
+
+// Tables of a block: source rows (slot of the row's first staged cell and
+// the staging offset of each row) and destination rows (the brick's rows of
+// the destination array).  Returns the staged count and the destinations.
+__device__ __forceinline__ void block_tables(const Grid &g, const BlockGeo &G, const int *scst,
+                                             const int *dcst, int *rlo, int *roff, int *dlo,
+                                             int *doff, int &T, int &D) {
+    const int nt = blockDim.x;
+    const int rowz = g.nx * g.ny;
+    for (int r = threadIdx.x; r < G.nr; r += nt) {
+        const int cy = G.ys0 + r % G.ry, cz = G.zs0 + r / G.ry;
+        const int c = cz * rowz + cy * g.nx + G.xs0;
+        const int lo = scst[c];
+        rlo[r] = lo;
+        roff[r + 1] = scst[c + G.lx] - lo;
+    }
+    for (int q = threadIdx.x; q < G.ndr; q += nt) {
+        const int cy = G.y0 + q % G.dry, cz = G.z0 + q / G.dry;
+        const int c = cz * rowz + cy * g.nx + G.x0;
+        const int lo = dcst[c];
+        dlo[q] = lo;
+        doff[q + 1] = dcst[c + (G.x1 - G.x0)] - lo;
+    }
+    __syncthreads();
+    const int wid = threadIdx.x >> 5;
+    if (wid == 0) warp_scan_inplace(roff, G.nr);
+    if (wid == (nt > 32 ? 1 : 0)) warp_scan_inplace(doff, G.ndr);
+    __syncthreads();
+    T = roff[G.nr];
+    D = doff[G.ndr];
+}
+
+// Staging offset of the first particle of every cell of every source row
+// (scell[r * (lx + 1) + i], i = 0 .. lx): the ranges a stencil traversal
+// visits.
+__device__ __forceinline__ void cell_table(const Grid &g, const BlockGeo &G, const int *scst,
+                                           const int *rlo, const int *roff, int *scell) {
+    const int w = G.lx + 1;
+    const int rowz = g.nx * g.ny;
+    for (int idx = threadIdx.x; idx < G.nr * w; idx += blockDim.x) {
+        const int r = idx / w, i = idx - r * w;
+        const int cy = G.ys0 + r % G.ry, cz = G.zs0 + r / G.ry;
+        scell[idx] = roff[r] + (scst[cz * rowz + cy * g.nx + G.xs0 + i] - rlo[r]);
+    }
+}
+
+// Sorted slot and row of staging index t (records read from global memory).
+__device__ __forceinline__ int staged_slot(const BlockGeo &G, const int *rlo, const int *roff,
+                                           int t, int &cy, int &cz) {
+    const int r = row_of(roff, G.nr, t);
+    cy = G.ys0 + r % G.ry;
+    cz = G.zs0 + r / G.ry;
+    return rlo[r] + (t - roff[r]);
+}
+
+// Source records: staged in shared memory, or (STAGED = false, a brick
+// more populous than the shared memory holds) recomputed from the sorted
+// arrays with the same operations.
+template <bool STAGED>
+struct SrcRecords {
+    const float4 *P, *V;
+    const float2 *S;
+    const BrickSrcDev *src;
+    const BlockGeo *G;
+    const int *rlo, *roff;
+    float csf;
+    __device__ __forceinline__ float4 pos(int t) const {
+        if (STAGED) return P[t];
+        int cy, cz;
+        const int j = staged_slot(*G, rlo, roff, t, cy, cz);
+        return rel_pos(src->pm, src->scx, j, cy, cz, *G, csf);
+    }
+    // (u, v, w, p / rho^2) and (rho, cs)
+    __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
+        if (STAGED) {
+            v = V[t];
+            s = S[t];
+            return;
+        }
+        int cy, cz;
+        const int j = staged_slot(*G, rlo, roff, t, cy, cz);
+        const float4 vh = src->velh[j], st = src->st[j];
+        v = make_float4(vh.x, vh.y, vh.z, st.y);
+        s = make_float2(st.x, st.z);
+    }
+};
+
+// Copy the block's source records into shared memory.
+template <bool RATES>
+__device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
+                                      const int *roff, int T, float csf, float4 *P, float4 *V,
+                                      float2 *SS) {
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        int cy, cz;
+        const int j = staged_slot(G, rlo, roff, t, cy, cz);
+        P[t] = rel_pos(S.pm, S.scx, j, cy, cz, G, csf);
+        if (RATES) {
+            const float4 vh = S.velh[j], st = S.st[j];
+            V[t] = make_float4(vh.x, vh.y, vh.z, st.y);
+            SS[t] = make_float2(st.x, st.z);
+        }
+    }
+}
+
+// One destination of the block.
+struct BrickDest {
+    int s;          // sorted slot
+    int orig;       // original index
+    int cx, cy, cz; // build cell
+    float xi_x, xi_y, xi_z;     // cell-local offsets (stencil pruning)
+    float4 P;       // brick-relative position, mass
+    float r2lo, r2hi, r2list;
+    double radius2;
+};
+
+__device__ __forceinline__ bool brick_dest(const Grid &g, const BrickDstDev &D, const BlockGeo &G,
+                                           const int *dlo, const int *doff, int d, BrickDest &q) {
+    const int r = row_of(doff, G.ndr, d);
+    q.s = dlo[r] + (d - doff[r]);
+    q.cy = G.y0 + r % G.dry;
+    q.cz = G.z0 + r / G.dry;
+    q.orig = D.perm[q.s];
+    const float4 p = D.pm[q.s];
+    q.xi_x = p.x; q.xi_y = p.y; q.xi_z = p.z;
+    q.cx = (int)D.scx[q.s];
+    q.P = rel_pos(D.pm, D.scx, q.s, q.cy, q.cz, G, g.cs_f);
+    if (D.tag != nullptr && D.tag[q.orig] != SPH_TAG_LOCAL_REAL) return false;
+    const double radius = __dmul_rn(D.h[q.orig], g.radius_scale);
+    q.radius2 = __dmul_rn(radius, radius);
+    const float r2 = (float)q.radius2;
+    q.r2lo = r2 * (1.f - 1e-5f);
+    q.r2hi = r2 * (1.f + 1e-5f);
+    q.r2list = 0.f;
+    if (g.skin > 0.f) {
+        const float rl = (float)radius + g.skin;
+        q.r2list = rl * rl * (1.f + 2e-5f);
+    }
+    return true;
+}
+
+// Visit the listed sources of destination q in the staged records, in the
+// order of the list-streaming kernels: stencil rows in (dz, dy) order, each
+// clipped to the chord of the search sphere, ascending slot within a row.
+// fn(t, rx, ry, rz, hit): staging index, r = x_dest - x_src, neighbour or
+// (with a list skin) only within the list radius.  The ranges come from the
+// block's cell table (scell) or, without one, from the grid's cell table.
+template <int K, bool STAGED, class Fn>
+__device__ __forceinline__ void brick_traverse(const Grid &g, const BlockGeo &G, const BrickSrcDev &S,
+                                               const BrickDstDev &D, const SrcRecords<STAGED> &R,
+                                               const int *rlo, const int *roff, const int *scell,
+                                               const BrickDest &q, Fn &&fn) {
+    const float csf = g.cs_f;
+    const float inv_cs = 1.f / csf;
+    const float R2 = fmaxf(q.r2hi, q.r2list) * 1.0002f;
+    const int w = G.lx + 1;
+#pragma unroll 1
+    for (int dz = -g.kz; dz <= g.kz; ++dz) {
+        const int czz = q.cz + dz;
+        if (czz < G.zs0 || czz >= G.zs1) continue;
+        const float ez = fmaxf(0.f, dz > 0 ? (float)dz * csf - q.xi_z
+                                           : (dz < 0 ? q.xi_z - (float)(dz + 1) * csf : 0.f));
+        const float ez2 = ez * ez;
+        if (ez2 > R2) continue;
+#pragma unroll 1
+        for (int dy = -g.ky; dy <= g.ky; ++dy) {
+            const int cyy = q.cy + dy;
+            if (cyy < G.ys0 || cyy >= G.ys1) continue;
+            const float ey = fmaxf(0.f, dy > 0 ? (float)dy * csf - q.xi_y
+                                               : (dy < 0 ? q.xi_y - (float)(dy + 1) * csf : 0.f));
+            const float rem = R2 - fmaf(ey, ey, ez2);
+            if (rem < 0.f) continue;
+            const float half = fmaf(rem * rsqrtf(fmaxf(rem, 1e-30f)), 1.0001f, 1e-5f * csf);
+            const int tlo = max(-K, __float2int_rd((q.xi_x - half) * inv_cs));
+            const int thi = min(K, __float2int_rd((q.xi_x + half) * inv_cs));
+            const int clo = max(q.cx + tlo, G.xs0);
+            const int chi = min(q.cx + thi, G.xs1 - 1);
+            if (clo > chi) continue;
+            const int rr = (cyy - G.ys0) + G.ry * (czz - G.zs0);
+            int ta, tb;
+            if (scell != nullptr) {
+                ta = scell[rr * w + (clo - G.xs0)];
+                tb = scell[rr * w + (chi + 1 - G.xs0)];
+            } else {
+                const int c = (czz * g.ny + cyy) * g.nx;
+                ta = roff[rr] + (__ldg(S.cstart + c + clo) - rlo[rr]);
+                tb = roff[rr] + (__ldg(S.cstart + c + chi + 1) - rlo[rr]);
+            }
+            for (int t = ta; t < tb; ++t) {
+                const float4 pj = R.pos(t);
+                const float rx = q.P.x - pj.x, ry = q.P.y - pj.y, rz = q.P.z - pj.z;
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                bool hit = r2 < q.r2lo;
+                if (!hit && r2 <= q.r2hi) {
+                    const int oj = S.perm[rlo[rr] + (t - roff[rr])];
+                    hit = exact_within(ld0(S.x, oj), ld0(S.y, oj), ld0(S.z, oj), ld0(D.x, q.orig),
+                                       ld0(D.y, q.orig), ld0(D.z, q.orig), q.radius2);
+                }
+                if (hit || r2 < q.r2list) fn(t, rx, ry, rz, hit);
+            }
+        }
+    }
+}
+
+// Staging pointers of the dynamic shared memory.
+struct SmemPtrs {
+    float4 *P, *V;
+    float2 *S;
+    int *rlo, *roff, *dlo, *doff, *scell;
+};
+
+__device__ __forceinline__ SmemPtrs smem_ptrs(unsigned char *base, const BrickSmem &sm) {
+    SmemPtrs p;
+    p.P = reinterpret_cast<float4 *>(base);
+    p.V = reinterpret_cast<float4 *>(base + sm.off_v);
+    p.S = reinterpret_cast<float2 *>(base + sm.off_s);
+    p.rlo = reinterpret_cast<int *>(base + sm.off_rlo);
+    p.roff = reinterpret_cast<int *>(base + sm.off_roff);
+    p.dlo = reinterpret_cast<int *>(base + sm.off_dlo);
+    p.doff = reinterpret_cast<int *>(base + sm.off_doff);
+    p.scell = reinterpret_cast<int *>(base + sm.off_scell);
+    return p;
+}
+
+__device__ __forceinline__ bool gate_off(const unsigned *gate) {
+    return gate != nullptr && __ldg(gate) != 0u;
+}
+
+// Neighbours of a destination past its list's capacity (skipping the cap
+// listed ones, in the order of the list build), added to its density sum.
+// Out of line: rare, and it would raise the register count of the stream.
+template <int K, bool STAGED>
+__device__ __noinline__ void density_overflow(const Grid &g, const BlockGeo &G,
+                                              const BrickSrcDev &S, const BrickDstDev &D,
+                                              const SrcRecords<STAGED> &R, const int *rlo,
+                                              const int *roff, const int *dlo, const int *doff,
+                                              int d, int cap, float ih, float fac, CSum &rho) {
+    BrickDest q;
+    brick_dest(g, D, G, dlo, doff, d, q);
+    int skip = cap;
+    brick_traverse<K, STAGED>(g, G, S, D, R, rlo, roff, nullptr, q,
+        [&](int t, float rx, float ry, float rz, bool hit) {
+            if (skip > 0) { --skip; return; }
+            if (!hit) return;
+            const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+            rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
+        });
+}
+
+// ---------------------------------------------------------------------------
+// summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
+// ---------------------------------------------------------------------------
+template <int K, bool BUILD, bool STAGED>
+__global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (gate_off(A.gate)) return;
+    const int b = blockIdx.x;
+    const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
+    if (nd == 0) return;
+    const Grid &g = A.g;
+    const BlockGeo G = block_geo(g, A.bk, b);
+    SmemPtrs sp = smem_ptrs(smem, A.sm);
+    int T, D;
+    block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
+    const int dbase = A.d.bdst[b];
+    const int cap = A.cap;
+    // the stencil cell table of a list build (a destination whose neighbours
+    // outgrew the list reads the grid's table instead)
+    int *scell = BUILD ? sp.scell : nullptr;
+    if (BUILD) cell_table(g, G, A.s.cstart, sp.rlo, sp.roff, sp.scell);
+    if (STAGED) stage<false>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, nullptr, nullptr);
+    __syncthreads();
+    SrcRecords<STAGED> R{sp.P, nullptr, nullptr, &A.s, &G, sp.rlo, sp.roff, g.cs_f};
+    const float ih = __fdividef(1.f, g.h_uniform);
+    const float fac = cubic_fac(A.dim, ih);
+    const uint16_t *lbase = A.nbr + (size_t)dbase * cap;
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        BrickDest q;
+        const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
+        CSum rho;
+        int c = 0;
+        if (real) {
+            if (BUILD) {
+                uint16_t *out = A.nbr + (size_t)dbase * cap + d;
+                brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, scell, q,
+                    [&](int t, float rx, float ry, float rz, bool hit) {
+                        if (c < cap) out[(size_t)c * D] = (uint16_t)t;
+                        ++c;
+                        if (!hit) return;
+                        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                        const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                        rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
+                    });
+            } else {
+                // stream the list in batches of 6 (entries of the next batch
+                // requested before the records of this one are used)
+                constexpr int B = 6;
+                c = A.cnt[dbase + d];
+                const int m = min(c, cap);
+                const uint16_t *lst = lbase + d;
+                int e[B];
+                auto entries = [&](int (&o)[B], int k) {
+                    o[0] = lst[(size_t)k * D];
+#pragma unroll
+                    for (int i = 1; i < B; ++i) o[i] = (k + i < m) ? lst[(size_t)(k + i) * D] : o[0];
+                };
+                if (m > 0) entries(e, 0);
+                for (int k = 0; k < m; k += B) {
+                    int en[B];
+                    const bool more = k + B < m;
+                    if (more) entries(en, k + B);
+                    float4 pj[B];
+#pragma unroll
+                    for (int i = 0; i < B; ++i) pj[i] = R.pos(e[i]);
+                    float part = 0.f;
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        const float rx = q.P.x - pj[i].x, ry = q.P.y - pj[i].y, rz = q.P.z - pj[i].z;
+                        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                        const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                        const float wv = cubic_w(r * ih) * fac * pj[i].w;
+                        part += (k + i < m) ? wv : 0.f;
+                    }
+                    rho.add(part);
+                    if (more) {
+#pragma unroll
+                        for (int i = 0; i < B; ++i) e[i] = en[i];
+                    }
+                }
+                if (c > cap)
+                    density_overflow<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, sp.dlo, sp.doff, d,
+                                                cap, ih, fac, rho);
+            }
+        }
+        if (BUILD) {
+            A.cnt[dbase + d] = c;
+            const unsigned act = __activemask();
+            const int wmax = __reduce_max_sync(act, c);
+            if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.maxcnt, wmax);
+        }
+        if (!A.write_out) continue;
+        const int orig = q.orig;
+        const double r64 = real ? rho.value() : 0.0;
+        if (A.rho_out) A.rho_out[orig] = r64;
+        const float rf = (float)r64;
+        float pf = 0.f, cf = 0.f;
+        if (A.tait) {
+            if (real) {
+                // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), through
+                // log1p/expm1 of the density excess (relative accuracy of p as rho -> ro)
+                const float Bt = A.co * A.co * A.ro / A.gamma;
+                const float lr = log1pf((float)((r64 - (double)A.ro) / (double)A.ro));
+                pf = Bt * expm1f(A.gamma * lr);
+                cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
+            }
+            A.p_out[orig] = (double)pf;
+            A.cs_out[orig] = (double)cf;
+        }
+        if (A.st_out) {
+            const float mi = A.d.pm[q.s].w;
+            if (A.tait) {
+                A.st_out[q.s] = make_float4(rf, pf / (rf * rf), cf, mi);
+            } else {
+                const float pold = (float)ld0(A.d.p, orig);
+                A.st_out[q.s] = make_float4(rf, pold / (rf * rf), (float)ld0(A.d.cs, orig), mi);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// rates: PGrad (pressure_funcs.pyx:40-91) + Monaghan AV (viscosity_funcs.pyx:
+// 41-124) [+ XSPH (xsph_funcs.pyx:31-88)], uniform h, one source, with
+// gravity (external_force.pyx:39-45) and position stepping
+// (position_funcs.pyx:32-60) folded into the store
+// ---------------------------------------------------------------------------
+struct RatesConst {
+    float h, ih, fac, alpha, beta, eta2, eps;
+};
+
+// destination state and the sums: plain FP32 partials of a batch, merged
+// into the Neumaier-compensated totals by flush()
+struct RatesAcc {
+    float4 vi;
+    float rhoi, pri, ci;
+    float pax, pay, paz, pxx, pxy, pxz;
+    CSum ax, ay, az, xx, xy, xz;
+};
+
+template <bool XSPH>
+__device__ __forceinline__ void rates_pair(RatesAcc &a, const RatesConst &k, float okf, float rx,
+                                           float ry, float rz, const float4 &pj, const float4 &vj,
+                                           const float2 &sj) {
+    const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+    const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+    const float qq = r2 * rinv * k.ih;
+    const float mj = pj.w;
+    float t = -mj * (a.pri + vj.w);
+    // Pi_ab only for approaching pairs (v_ab . r_ab < 0), as a select
+    const float dot = (a.vi.x - vj.x) * rx + (a.vi.y - vj.y) * ry + (a.vi.z - vj.z) * rz;
+    const bool neg = dot < 0.f;
+    const float den = neg ? fmaf(k.eta2 * k.h, k.h, r2) : 1.f;
+    const float mu = neg ? __fdividef(k.h * dot, den) : 0.f;
+    const float cab = 0.5f * (a.ci + sj.y);
+    const float rhoab = 0.5f * (a.rhoi + sj.x);
+    const float piab = __fdividef(fmaf(k.beta * mu, mu, -k.alpha * cab * mu), rhoab);
+    t -= mj * (neg ? piab : 0.f);
+    const float gf = cubic_gfac(qq, k.ih, rinv) * k.fac * t * okf;
+    a.pax = fmaf(gf, rx, a.pax);
+    a.pay = fmaf(gf, ry, a.pay);
+    a.paz = fmaf(gf, rz, a.paz);
+    if (XSPH) {
+        const float rhox = 0.5f * (sj.x + a.rhoi);
+        const float temp = __fdividef(mj * (cubic_w(qq) * k.fac), rhox) * k.eps * okf;
+        a.pxx = fmaf(temp, vj.x - a.vi.x, a.pxx);
+        a.pxy = fmaf(temp, vj.y - a.vi.y, a.pxy);
+        a.pxz = fmaf(temp, vj.z - a.vi.z, a.pxz);
+    }
+}
+
+template <bool XSPH>
+__device__ __forceinline__ void rates_flush(RatesAcc &a) {
+    a.ax.add(a.pax); a.ay.add(a.pay); a.az.add(a.paz);
+    a.pax = a.pay = a.paz = 0.f;
+    if (XSPH) {
+        a.xx.add(a.pxx); a.xy.add(a.pxy); a.xz.add(a.pxz);
+        a.pxx = a.pxy = a.pxz = 0.f;
+    }
+}
+
+// Neighbours past the list's capacity (out of line, as density_overflow).
+template <int K, bool XSPH, bool STAGED>
+__device__ __noinline__ void rates_overflow(const Grid &g, const BlockGeo &G, const BrickSrcDev &S,
+                                            const BrickDstDev &D, const SrcRecords<STAGED> &R,
+                                            const int *rlo, const int *roff, const int *dlo,
+                                            const int *doff, int d, int cap, const RatesConst &k,
+                                            RatesAcc &a) {
+    BrickDest q;
+    brick_dest(g, D, G, dlo, doff, d, q);
+    int skip = cap;
+    brick_traverse<K, STAGED>(g, G, S, D, R, rlo, roff, nullptr, q,
+        [&](int t, float rx, float ry, float rz, bool hit) {
+            if (skip > 0) { --skip; return; }
+            if (!hit) return;
+            float4 vj;
+            float2 sj;
+            R.state(t, vj, sj);
+            rates_pair<XSPH>(a, k, 1.f, rx, ry, rz, R.pos(t), vj, sj);
+            rates_flush<XSPH>(a);
+        });
+}
+
+template <int K, bool XSPH, bool STAGED>
+__global__ void __maxnreg__(80) k_brates(const __grid_constant__ BrickRatesArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (gate_off(A.gate)) return;
+    const int b = blockIdx.x;
+    const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
+    if (nd == 0) return;
+    const Grid &g = A.g;
+    const BlockGeo G = block_geo(g, A.bk, b);
+    SmemPtrs sp = smem_ptrs(smem, A.sm);
+    int T, D;
+    block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
+    const int dbase = A.d.bdst[b];
+    const int cap = A.cap;
+    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, sp.V, sp.S);
+    __syncthreads();
+    SrcRecords<STAGED> R{sp.P, sp.V, sp.S, &A.s, &G, sp.rlo, sp.roff, g.cs_f};
+    RatesConst kc;
+    kc.h = g.h_uniform;
+    kc.ih = __fdividef(1.f, kc.h);
+    kc.fac = cubic_fac(A.dim, kc.ih);
+    kc.alpha = A.alpha; kc.beta = A.beta; kc.eta2 = A.eta2; kc.eps = A.eps;
+    const uint16_t *lbase = A.nbr + (size_t)dbase * cap;
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        BrickDest q;
+        const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
+        RatesAcc acc;
+        acc.pax = acc.pay = acc.paz = acc.pxx = acc.pxy = acc.pxz = 0.f;
+        if (real) {
+            acc.vi = A.d.velh[q.s];
+            const float4 sti = A.d.st[q.s];
+            acc.rhoi = sti.x; acc.pri = sti.y; acc.ci = sti.z;
+            // stream the list in batches of 3 (entries of the next batch
+            // requested before the records of this one are used)
+            constexpr int B = 3;
+            const int c = A.cnt[dbase + d];
+            const int m = min(c, cap);
+            const uint16_t *lst = lbase + d;
+            int e[B];
+            auto entries = [&](int (&o)[B], int k) {
+                o[0] = lst[(size_t)k * D];
+#pragma unroll
+                for (int i = 1; i < B; ++i) o[i] = (k + i < m) ? lst[(size_t)(k + i) * D] : o[0];
+            };
+            if (m > 0) entries(e, 0);
+            for (int k = 0; k < m; k += B) {
+                int en[B];
+                const bool more = k + B < m;
+                if (more) entries(en, k + B);
+                float4 pj[B], vj[B];
+                float2 sj[B];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    pj[i] = R.pos(e[i]);
+                    R.state(e[i], vj[i], sj[i]);
+                }
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+                    rates_pair<XSPH>(acc, kc, k + i < m ? 1.f : 0.f, q.P.x - pj[i].x,
+                                     q.P.y - pj[i].y, q.P.z - pj[i].z, pj[i], vj[i], sj[i]);
+                rates_flush<XSPH>(acc);
+                if (more) {
+#pragma unroll
+                    for (int i = 0; i < B; ++i) e[i] = en[i];
+                }
+            }
+            if (c > cap)
+                rates_overflow<K, XSPH, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, sp.dlo, sp.doff, d,
+                                                cap, kc, acc);
+        }
+        const int orig = q.orig;
+        double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
+        if (real) {
+            a3[0] = acc.ax.value(); a3[1] = acc.ay.value(); a3[2] = acc.az.value();
+            p3[0] = acc.xx.value(); p3[1] = acc.xy.value(); p3[2] = acc.xz.value();
+            if (A.add_gravity) { a3[0] += A.gx; a3[1] += A.gy; a3[2] += A.gz; }
+            if (A.add_velocity) {
+                // exact FP64 velocity of the destination (position_funcs.pyx:47-50)
+                p3[0] += ld0(A.d.u, orig);
+                p3[1] += ld0(A.d.v, orig);
+                p3[2] += ld0(A.d.w, orig);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (A.acc[k]) A.acc[k][orig] = (A.accumulate ? A.acc[k][orig] : 0.0) + a3[k];
+            if (A.pos[k]) A.pos[k][orig] = (A.accumulate ? A.pos[k][orig] : 0.0) + p3[k];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-brick tables of one array: destinations per brick (then scanned into
+// bdst) and the largest count of source particles a brick stages
+// ---------------------------------------------------------------------------
+__global__ void k_brick_tables(Grid g, BrickGeom bk, const int *cstart, int *dcount,
+                               unsigned *stats) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    unsigned tmax = 0, dmax = 0;
+    if (b < bk.nbricks) {
+        const BlockGeo G = block_geo(g, bk, (int)b);
+        const int rowz = g.nx * g.ny;
+        int D = 0;
+        for (int cz = G.z0; cz < G.z1; ++cz)
+            for (int cy = G.y0; cy < G.y1; ++cy) {
+                const int c = cz * rowz + cy * g.nx;
+                D += cstart[c + G.x1] - cstart[c + G.x0];
+            }
+        // every brick: as a source this array is staged by the bricks that
+        // hold destinations of any array
+        int T = 0;
+        for (int cz = G.zs0; cz < G.zs1; ++cz)
+            for (int cy = G.ys0; cy < G.ys1; ++cy) {
+                const int c = cz * rowz + cy * g.nx;
+                T += cstart[c + G.xs1] - cstart[c + G.xs0];
+            }
+        dcount[b] = D;
+        tmax = (unsigned)T;
+        dmax = (unsigned)D;
+    }
+    if (b == bk.nbricks) dcount[b] = 0;
+    tmax = __reduce_max_sync(0xffffffffu, tmax);
+    dmax = __reduce_max_sync(0xffffffffu, dmax);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(stats, tmax);
+        atomicMax(stats + 1, dmax);
+    }
+}
+
+// the largest source staging of any brick over every source array, as the
+// staged-record capacity, if it fits the shared memory of a block
+constexpr int kBrickSmemLimit = 200 * 1024;
+
+// Shared-memory layout of a pass over destination array D from source S.
+int brick_layout(const sph_ctx *ctx, const ArraySnap &S, bool rates, bool cells, BrickSmem *sm,
+                 size_t *bytes) {
+    const BrickGeom &bk = ctx->bricks;
+    const Grid &g = ctx->grid;
+    const int lx = bk.bx + 2 * g.kx, ry = bk.by + 2 * g.ky, rz = bk.bz + 2 * g.kz;
+    const int nr = ry * rz;
+    const int ndr = bk.by * bk.bz;
+    // tables (ints): rlo[nr], roff[nr + 1], dlo[ndr], doff[ndr + 1], and for
+    // a list build scell[nr (lx + 1)]
+    const size_t ncell = cells ? (size_t)nr * (lx + 1) : 0;
+    const size_t tables = sizeof(int) * ((size_t)nr + nr + 1 + ndr + ndr + 1 + ncell);
+    const size_t rec = rates ? (16 + 16 + 8) : 16;
+    size_t cap = (size_t)std::max(S.b_tmax, 1);
+    // environment SPH_BRICK_UNSTAGED=1 reads every record from global memory
+    // (the path of bricks too populous for shared memory), to test it on
+    // small sets
+    static int unstaged = -1;
+    if (unstaged < 0) {
+        const char *e = getenv("SPH_BRICK_UNSTAGED");
+        unstaged = (e && atoi(e) > 0) ? 1 : 0;
+    }
+    bool staged = !unstaged && tables + cap * rec + 64 <= (size_t)kBrickSmemLimit;
+    if (!staged) cap = 0;
+    size_t off = 0;
+    sm->stage_cap = (int)cap;
+    off += cap * 16;
+    sm->off_v = (int)off;
+    if (rates) off += cap * 16;
+    sm->off_s = (int)off;
+    if (rates) off += cap * 8;
+    off = (off + 15) & ~(size_t)15;
+    sm->off_rlo = (int)off; off += sizeof(int) * nr;
+    sm->off_roff = (int)off; off += sizeof(int) * (nr + 1);
+    sm->off_dlo = (int)off; off += sizeof(int) * ndr;
+    sm->off_doff = (int)off; off += sizeof(int) * (ndr + 1);
+    sm->off_scell = (int)off; off += sizeof(int) * ncell;
+    *bytes = off;
+    return staged ? 1 : 0;
+}
+
+BrickSrcDev make_bsrc(const ArraySnap &S) {
+    BrickSrcDev s;
+    s.pm = S.pm; s.velh = S.velh; s.st = S.st; s.scx = S.scx;
+    s.cstart = S.cstart; s.perm = S.perm;
+    s.x = S.view.x; s.y = S.view.y; s.z = S.view.z;
+    return s;
+}
+
+BrickDstDev make_bdst(const ArraySnap &D) {
+    BrickDstDev d;
+    d.pm = D.pm; d.velh = D.velh; d.st = D.st; d.scx = D.scx;
+    d.cstart = D.cstart; d.perm = D.perm; d.bdst = D.bdst;
+    d.tag = D.view.tag;
+    d.x = D.view.x; d.y = D.view.y; d.z = D.view.z; d.h = D.view.h;
+    d.u = D.view.u; d.v = D.view.v; d.w = D.view.w;
+    d.p = D.view.p; d.cs = D.view.cs;
+    return d;
+}
+
+int brick_threads(const ArraySnap &D) {
+    const int want = (std::max(D.b_dmax, 1) + 31) / 32 * 32;
+    return std::min(std::max(want, 64), kBrickMaxThreads);
+}
+
+template <class Kern>
+int allow_smem(Kern *k, size_t bytes) {
+    // raise each kernel's dynamic shared-memory limit to the largest layout,
+    // once per kernel and device
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> done;
+    if (bytes <= 48 * 1024) return SPH_OK;
+    int dev = 0;
+    SPH_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &d : done)
+        if (d.first == (const void *)k && d.second == dev) return SPH_OK;
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               kBrickSmemLimit);
+    if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute (brick shared memory)");
+    done.emplace_back((const void *)k, dev);
+    return SPH_OK;
+}
+
+}  // namespace
+
+// Brick geometry of the current grid: edge lengths (cells) per stencil
+// half-width, chosen so a brick holds a few hundred destinations and its
+// staging ~5-8 times as many sources.
+void brick_geometry(sph_ctx *ctx) {
+    const Grid &g = ctx->grid;
+    BrickGeom &bk = ctx->bricks;
+    const int K = g.kx;
+    if (g.kz > 0) {
+        const int e = K == 1 ? 3 : (K == 2 ? 5 : 8);
+        bk.bx = bk.by = bk.bz = e;
+    } else if (g.ky > 0) {
+        const int e = K == 1 ? 8 : (K == 2 ? 12 : 16);
+        bk.bx = bk.by = e;
+        bk.bz = 1;
+    } else {
+        bk.bx = 64;
+        bk.by = bk.bz = 1;
+    }
+    bk.nbx = (g.nx + bk.bx - 1) / bk.bx;
+    bk.nby = (g.ny + bk.by - 1) / bk.by;
+    bk.nbz = (g.nz + bk.bz - 1) / bk.bz;
+    bk.nbricks = (int64_t)bk.nbx * bk.nby * bk.nbz;
+}
+
+// Per-array brick tables for the current build (queued on the context's
+// stream); the statistics land in stats[2 a], stats[2 a + 1].
+int brick_tables(sph_ctx *ctx, int a, unsigned *stats) {
+    ArraySnap &A = ctx->arrays[a];
+    const BrickGeom &bk = ctx->bricks;
+    const int64_t need = bk.nbricks + 1;
+    if (need > A.bdst_cap || !A.bdst) {
+        cudaFree(A.bdst);
+        A.bdst = nullptr;
+        SPH_CUDA(cudaMalloc(&A.bdst, sizeof(int) * need));
+        A.bdst_cap = need;
+    }
+    const int th = 128;
+    const int blocks = (int)((need + th - 1) / th);
+    k_brick_tables<<<blocks, th, 0, ctx->stream>>>(ctx->grid, bk, A.cstart, A.bdst, stats);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_brick_tables");
+    return scan_exclusive(ctx, A.bdst, need);
+}
+
+bool brick_density_eligible(const sph_ctx *ctx, int dst, const int *srcs, int nsrc,
+                            const sph_density_params *prm) {
+    const Grid &g = ctx->grid;
+    if (!ctx->bricks_on || !ctx->bricks_ready || nsrc != 1 || !g.uniform_h || g.periodic ||
+        g.symmetric || prm->h0 != 0.0)
+        return false;
+    const ArraySnap &S = ctx->arrays[srcs[0]];
+    const ArraySnap &D = ctx->arrays[dst];
+    return S.n > 0 && D.n > 0 && S.b_tmax <= 65535;
+}
+
+bool brick_rates_eligible(const sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+                          const sph_rates_params *prm) {
+    const Grid &g = ctx->grid;
+    if (!ctx->bricks_on || !ctx->bricks_ready || nterms != 1 || !g.uniform_h || g.periodic ||
+        g.symmetric || prm->drho_out != nullptr)
+        return false;
+    const uint32_t f = terms[0].flags;
+    if (f != (SPH_TERM_PGRAD | SPH_TERM_AVISC) && f != (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH))
+        return false;
+    const ArraySnap &S = ctx->arrays[terms[0].src];
+    const ArraySnap &D = ctx->arrays[dst];
+    return S.n > 0 && D.n > 0 && S.b_tmax <= 65535;
+}
+
+// Density pass (and, with build, the list build) of destination dst among
+// source src; write_out = 0 builds the list only.
+int brick_density(sph_ctx *ctx, int dst, int src, NbrList &L, bool build, bool write_out,
+                  const sph_density_params *prm, double *rho, double *p, double *cs,
+                  float4 *st_out) {
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[src];
+    BrickDensityArgs a{};
+    a.g = ctx->grid;
+    a.bk = ctx->bricks;
+    a.d = make_bdst(D);
+    a.s = make_bsrc(S);
+    size_t bytes = 0;
+    const bool staged = brick_layout(ctx, S, false, build, &a.sm, &bytes) != 0;
+    a.nbr = L.nbr16;
+    a.cnt = L.cnt;
+    a.maxcnt = L.maxcnt;
+    a.cap = L.cap;
+    a.build = build ? 1 : 0;
+    a.write_out = write_out ? 1 : 0;
+    if (prm) {
+        a.dim = prm->dim;
+        a.tait = prm->tait;
+        a.co = (float)prm->co; a.ro = (float)prm->ro; a.gamma = (float)prm->gamma;
+    } else {
+        a.dim = ctx->dim;
+    }
+    a.rho_out = rho; a.p_out = p; a.cs_out = cs;
+    a.st_out = st_out;
+    a.gate = ctx->gate;
+    if (D.n == 0) return SPH_OK;
+    const int nt = brick_threads(D);
+    const int blocks = (int)ctx->bricks.nbricks;
+    const int K = ctx->grid.kx;
+#define BDL2(K_, B_, S_)                                                                  \
+    do {                                                                                  \
+        int rc_ = allow_smem(k_bdensity<K_, B_, S_>, bytes);                              \
+        if (rc_) return rc_;                                                              \
+        k_bdensity<K_, B_, S_><<<blocks, nt, bytes, ctx->stream>>>(a);                    \
+    } while (0)
+#define BDL1(K_, B_) do { if (staged) BDL2(K_, B_, true); else BDL2(K_, B_, false); } while (0)
+#define BDL(K_) do { if (build) BDL1(K_, true); else BDL1(K_, false); } while (0)
+    if (K == 1) BDL(1);
+    else if (K == 2) BDL(2);
+    else BDL(3);
+#undef BDL
+#undef BDL1
+#undef BDL2
+    count_launch();
+    SPH_LAUNCH_CHECK("k_bdensity");
+    return SPH_OK;
+}
+
+int brick_rates(sph_ctx *ctx, int dst, const sph_source_term &term, NbrList &L,
+                const sph_rates_params *prm, double *const *acc, double *const *pos,
+                int accumulate) {
+    ArraySnap &D = ctx->arrays[dst];
+    ArraySnap &S = ctx->arrays[term.src];
+    BrickRatesArgs a{};
+    a.g = ctx->grid;
+    a.bk = ctx->bricks;
+    a.d = make_bdst(D);
+    a.s = make_bsrc(S);
+    size_t bytes = 0;
+    const bool staged = brick_layout(ctx, S, true, false, &a.sm, &bytes) != 0;
+    a.nbr = L.nbr16;
+    a.cnt = L.cnt;
+    a.cap = L.cap;
+    a.dim = prm->dim;
+    a.alpha = (float)term.alpha;
+    a.beta = (float)term.beta;
+    a.eta2 = (float)(term.eta * term.eta);
+    a.eps = (float)term.eps;
+    a.add_velocity = prm->add_velocity;
+    a.add_gravity = prm->add_gravity;
+    a.accumulate = accumulate;
+    a.gx = prm->gx; a.gy = prm->gy; a.gz = prm->gz;
+    for (int c = 0; c < 3; ++c) {
+        a.acc[c] = acc ? acc[c] : nullptr;
+        a.pos[c] = pos ? pos[c] : nullptr;
+    }
+    a.gate = ctx->gate;
+    if (D.n == 0) return SPH_OK;
+    const bool xsph = (term.flags & SPH_TERM_XSPH) != 0;
+    const int nt = brick_threads(D);
+    const int blocks = (int)ctx->bricks.nbricks;
+    const int K = ctx->grid.kx;
+#define BRL2(K_, X_)                                                                      \
+    do {                                                                                  \
+        if (staged) {                                                                     \
+            int rc_ = allow_smem(k_brates<K_, X_, true>, bytes);                          \
+            if (rc_) return rc_;                                                          \
+            k_brates<K_, X_, true><<<blocks, nt, bytes, ctx->stream>>>(a);                \
+        } else {                                                                          \
+            int rc_ = allow_smem(k_brates<K_, X_, false>, bytes);                         \
+            if (rc_) return rc_;                                                          \
+            k_brates<K_, X_, false><<<blocks, nt, bytes, ctx->stream>>>(a);               \
+        }                                                                                 \
+    } while (0)
+#define BRL(K_) do { if (xsph) BRL2(K_, true); else BRL2(K_, false); } while (0)
+    if (K == 1) BRL(1);
+    else if (K == 2) BRL(2);
+    else BRL(3);
+#undef BRL
+#undef BRL2
+    count_launch();
+    SPH_LAUNCH_CHECK("k_brates");
+    return SPH_OK;
+}
+
+}  // namespace sphgb

@@ -85,6 +85,10 @@ int sph_ctx_create(int dim, sph_ctx **out) {
             cudaSuccess ||
         (e = cudaHostGetDevicePointer((void **)&c->hd_box, c->h_box, 0)) != cudaSuccess ||
         (e = cudaHostGetDevicePointer((void **)&c->hd_status, c->h_status, 0)) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_bstats, 2 * kMaxBrickArrays * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaHostAlloc(&c->h_bstats, 2 * kMaxBrickArrays * sizeof(unsigned),
+                           cudaHostAllocMapped)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer((void **)&c->hd_bstats, c->h_bstats, 0)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->pending_event, cudaEventDisableTiming)) != cudaSuccess) {
         sph_ctx_destroy(c);
         return cuda_check(e, "sph_ctx_create");
@@ -104,12 +108,15 @@ int sph_ctx_destroy(sph_ctx *c) {
         cudaFree(A.scx); cudaFree(A.pm); cudaFree(A.velh); cudaFree(A.st);
         cudaFree(A.nrm); cudaFree(A.tan);
         cudaFree(A.cstart); cudaFree(A.cursor); cudaFree(A.refcell); cudaFree(A.pm0); cudaFree(A.inv);
+        cudaFree(A.bdst);
     }
     cudaFree(c->d_box); cudaFree(c->d_hmax); cudaFree(c->d_status);
     cudaFree(c->scan_tmp); cudaFree(c->d_part); cudaFree(c->d_cnt);
     if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_red) cudaFreeHost(c->h_red);
     if (c->h_status) cudaFreeHost(c->h_status);
+    cudaFree(c->d_bstats);
+    if (c->h_bstats) cudaFreeHost(c->h_bstats);
     if (c->pending_event) cudaEventDestroy(c->pending_event);
     delete c;
     return SPH_OK;
@@ -190,6 +197,24 @@ int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
         c->pxmax = on ? xmax : 0.0;
         c->built = false;   // the next update builds afresh
     }
+    return SPH_OK;
+}
+
+int sph_ctx_set_bricks(sph_ctx *c, int on) {
+    CHECK_CTX(c);
+    RESOLVE(c);
+    if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_bricks: on must be 0 or 1");
+    if (on != c->bricks_on) {
+        c->bricks_on = on;
+        c->built = false;   // the next update builds afresh
+    }
+    return SPH_OK;
+}
+
+int sph_pair_pass_stats(sph_ctx *c, int64_t *out) {
+    CHECK_CTX(c);
+    if (!out) return set_error(SPH_ERR_ARG, "sph_pair_pass_stats: null out");
+    out[0] = c->n_brick_passes;
     return SPH_OK;
 }
 

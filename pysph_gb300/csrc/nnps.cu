@@ -764,6 +764,29 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
     ctx->build_subdiv = subdiv;
     ctx->build_h = g.uniform_h ? hmax : 0.0;
     ctx->n_full += 1;
+    // brick tables of the brick-staged pair passes (uniform h, no periodic
+    // axis or symmetric relation): their largest populations size the
+    // launches, so they are read back once per full build
+    ctx->bricks_ready = false;
+    if (ctx->bricks_on && g.uniform_h && !g.periodic && !g.symmetric &&
+        narrays <= kMaxBrickArrays) {
+        brick_geometry(ctx);
+        SPH_CUDA(cudaMemsetAsync(ctx->d_bstats, 0, 2 * narrays * sizeof(unsigned), st));
+        for (int a = 0; a < narrays; ++a) {
+            if (arrays[a].n == 0) continue;
+            const int rc = brick_tables(ctx, a, ctx->d_bstats + 2 * a);
+            if (rc) return rc;
+        }
+        const int rp = publish_words(ctx, ctx->d_bstats, ctx->hd_bstats, 2 * narrays);
+        if (rp) return rp;
+        SPH_CUDA(cudaStreamSynchronize(st));
+        for (int a = 0; a < narrays; ++a) {
+            ArraySnap &A = ctx->arrays[a];
+            A.b_tmax = arrays[a].n > 0 ? (int)ctx->h_bstats[2 * a] : 0;
+            A.b_dmax = arrays[a].n > 0 ? (int)ctx->h_bstats[2 * a + 1] : 0;
+        }
+        ctx->bricks_ready = true;
+    }
     return SPH_OK;
 }
 

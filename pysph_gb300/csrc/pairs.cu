@@ -702,21 +702,24 @@ int64_t code_limit(int variant) {
 
 // Allocate / size the neighbour list of (dst, src) for the current build
 // (no launch).  *stale tells whether its contents must be (re)built.
-int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
+// brick: the brick-staged list of the pair (16-bit staging indices), kept
+// apart from the list-streaming one.
+int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale, bool brick = false) {
     const int na = (int)ctx->arrays.size();
-    if ((int)ctx->lists.size() < na * na) ctx->lists.resize((size_t)na * na);
-    NbrList &L = ctx->lists[(size_t)dst * na + src];
+    if ((int)ctx->lists.size() < 2 * na * na) ctx->lists.resize((size_t)2 * na * na);
+    const int slot = (brick ? na * na : 0) + dst * na + src;
+    NbrList &L = ctx->lists[(size_t)slot];
+    L.brick = brick;
     *out = &L;
     *stale = L.build != ctx->build_id;
     if (!*stale) return SPH_OK;
     ArraySnap &D = ctx->arrays[dst];
     ArraySnap &S = ctx->arrays[src];
     const Grid &g = ctx->grid;
-    if (S.n >= code_limit(code_variant(ctx)))
+    if (!brick && S.n >= code_limit(code_variant(ctx)))
         return set_error(SPH_ERR_NOTSUP, "neighbour list: too many source particles for this "
                                          "cell subdivision (use a smaller subdivision)");
     if (!L.maxcnt) {
-        const int slot = dst * na + src;
         if (slot < kMaxListSlots) {
             L.maxcnt = (int *)(ctx->d_status + kListWord0 + slot);
         } else {
@@ -735,12 +738,16 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale) {
     if (cap_override() > 0) cap = cap_override();
     const int64_t stride = std::max<int64_t>(D.n, 1);
     const int64_t need = stride * cap;
-    if (need > L.entries || !L.nbr || !L.cnt || stride > L.stride_cap) {
+    const bool have = brick ? L.nbr16 != nullptr : L.nbr != nullptr;
+    if (need > L.entries || !have || !L.cnt || stride > L.stride_cap) {
         cudaFree(L.nbr);
+        cudaFree(L.nbr16);
         cudaFree(L.cnt);
         L.nbr = nullptr;
+        L.nbr16 = nullptr;
         L.cnt = nullptr;
-        SPH_CUDA(cudaMalloc(&L.nbr, sizeof(uint32_t) * need));
+        if (brick) SPH_CUDA(cudaMalloc(&L.nbr16, sizeof(uint16_t) * need));
+        else SPH_CUDA(cudaMalloc(&L.nbr, sizeof(uint32_t) * need));
         SPH_CUDA(cudaMalloc(&L.cnt, sizeof(int) * stride));
         L.entries = need;
         L.stride_cap = stride;
@@ -809,6 +816,7 @@ void list_maxima_collect(sph_ctx *ctx) {
 void free_lists(sph_ctx *ctx) {
     for (auto &L : ctx->lists) {
         cudaFree(L.nbr);
+        cudaFree(L.nbr16);
         cudaFree(L.cnt);
         if (L.own_maxcnt) cudaFree(L.maxcnt);
     }
@@ -854,6 +862,24 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
     if (dst < 0 || dst >= na || nsrc < 0 || nsrc > SPH_MAX_SOURCES || !prm)
         return set_error(SPH_ERR_ARG, "density: bad destination / sources");
     ArraySnap &D = ctx->arrays[dst];
+    if (prm->h0 < 0.0) return set_error(SPH_ERR_ARG, "density: h0 must be >= 0");
+    for (int i = 0; i < nsrc; ++i)
+        if (srcs[i] < 0 || srcs[i] >= na) return set_error(SPH_ERR_ARG, "density: bad source");
+    if (brick_density_eligible(ctx, dst, srcs, nsrc, prm)) {
+        NbrList *L;
+        bool stale = false;
+        const int rc = prepare_list(ctx, dst, srcs[0], &L, &stale, true);
+        if (rc) return rc;
+        const bool own = rho != nullptr && rho == D.view.rho &&
+                         (!prm->tait || (p == D.view.p && cs == D.view.cs));
+        const int rb = brick_density(ctx, dst, srcs[0], *L, stale, true, prm, rho, p, cs,
+                                     own ? D.st : nullptr);
+        if (rb) return rb;
+        if (own) D.st_fresh = true;
+        if (stale) L->build = ctx->build_id;
+        ctx->n_brick_passes += 1;
+        return SPH_OK;
+    }
     DensityArgs a{};
     a.g = ctx->grid;
     a.d = make_dest(D);
@@ -928,6 +954,25 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
         for (int i = 0; !rc && i < nterms; ++i)
             if (terms[i].src >= 0 && terms[i].src < na) rc = ensure_state(ctx, terms[i].src);
         if (rc) return rc;
+    }
+    for (int i = 0; i < nterms; ++i)
+        if (terms[i].src < 0 || terms[i].src >= na) return set_error(SPH_ERR_ARG, "rates: bad source");
+    if (brick_rates_eligible(ctx, dst, terms, nterms, prm)) {
+        NbrList *L;
+        bool stale = false;
+        int rc = prepare_list(ctx, dst, terms[0].src, &L, &stale, true);
+        if (rc) return rc;
+        if (stale) {
+            // no density pass of this build wrote the list: build it alone
+            rc = brick_density(ctx, dst, terms[0].src, *L, true, false, nullptr, nullptr, nullptr,
+                               nullptr, nullptr);
+            if (rc) return rc;
+            L->build = ctx->build_id;
+        }
+        rc = brick_rates(ctx, dst, terms[0], *L, prm, acc, pos, accumulate);
+        if (rc) return rc;
+        ctx->n_brick_passes += 1;
+        return SPH_OK;
     }
     RatesArgs a{};
     a.g = ctx->grid;

@@ -28,7 +28,9 @@
 namespace sphgb {
 
 constexpr int kPairBlock = 128; // threads per block of the pair kernels
-constexpr int kMaxListSlots = 64; // (dst, src) lists whose maxima are tracked
+// (dst, src) lists whose maxima are tracked: the list-streaming lists of
+// slots [0, na^2) and the brick-staged lists of slots [na^2, 2 na^2)
+constexpr int kMaxListSlots = 128;
 // device status block read back with one copy: [0] error word, [1] largest
 // squared displacement (float bits), [2] stale-list flags of the last light
 // refresh, [3] spare, [kListWord0 + i] largest count of list slot i
@@ -96,6 +98,14 @@ __device__ __forceinline__ double image_x(const Grid &g, double xj, double xi, f
     return s == 0.0 ? xj : __dadd_rn(xj, s * g.plen);
 }
 
+// Bricks of grid cells, the unit of work of the brick-staged pair passes:
+// bx * by * bz cells per brick, nbx * nby * nbz bricks over the grid.
+struct BrickGeom {
+    int bx = 1, by = 1, bz = 1;
+    int nbx = 1, nby = 1, nbz = 1;
+    int64_t nbricks = 0;
+};
+
 struct ArraySnap {
     int64_t n = 0;
     int64_t cap = 0;
@@ -119,6 +129,12 @@ struct ArraySnap {
     float4 *pm0 = nullptr; // pm at the last full build (skin lists)
     int *inv = nullptr;      // original -> sorted slot of the last full build
     int64_t pm0_cap = 0;
+    // brick tables of the last full build: exclusive prefix of the
+    // destinations per brick (nbricks + 1), the largest count of source
+    // particles a brick stages and of destinations in one brick
+    int *bdst = nullptr;
+    int64_t bdst_cap = 0;
+    int b_tmax = 0, b_dmax = 0;
 };
 
 // Neighbour list of one (destination, source) pair of arrays: entry k of
@@ -127,6 +143,11 @@ struct ArraySnap {
 // cap neighbours keep the first cap and are completed by a re-traversal.
 struct NbrList {
     uint32_t *nbr = nullptr;
+    // brick-staged list: entry k of destination d of brick b at
+    // nbr16[bdst[b] * cap + k * D_b + d] (an index into the brick's staged
+    // sources), count in cnt[bdst[b] + d]
+    uint16_t *nbr16 = nullptr;
+    bool brick = false;
     int *cnt = nullptr;
     int *maxcnt = nullptr;   // device: largest count of the last list build
     bool own_maxcnt = false; // maxcnt allocated apart (lists past the status block)
@@ -191,6 +212,15 @@ struct sph_ctx {
     int periodic = 0;                   // periodic x axis (next build)
     double pxmin = 0.0, pxmax = 0.0;
     long long n_full = 0, n_light = 0;  // full builds / light refreshes
+    // brick-staged pair passes (sph_ctx_set_bricks): on by default; ready
+    // once the brick tables of the current build are known on the host
+    int bricks_on = 1;
+    bool bricks_ready = false;
+    sphgb::BrickGeom bricks;
+    unsigned *d_bstats = nullptr;       // 2 words per array: staged max, destinations max
+    unsigned *h_bstats = nullptr;       // mapped mirror
+    unsigned *hd_bstats = nullptr;
+    long long n_brick_passes = 0;       // pair passes run by the brick kernels
 };
 
 struct sph_batch {
@@ -276,6 +306,20 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
 int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
 int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
 int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc);
+// brick-staged pair passes (bricks.cu)
+constexpr int kMaxBrickArrays = 16;
+void brick_geometry(sph_ctx *ctx);
+int brick_tables(sph_ctx *ctx, int a, unsigned *stats);
+bool brick_density_eligible(const sph_ctx *ctx, int dst, const int *srcs, int nsrc,
+                            const sph_density_params *prm);
+bool brick_rates_eligible(const sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+                          const sph_rates_params *prm);
+int brick_density(sph_ctx *ctx, int dst, int src, NbrList &L, bool build, bool write_out,
+                  const sph_density_params *prm, double *rho, double *p, double *cs,
+                  float4 *st_out);
+int brick_rates(sph_ctx *ctx, int dst, const sph_source_term &term, NbrList &L,
+                const sph_rates_params *prm, double *const *acc, double *const *pos,
+                int accumulate);
 int scan_exclusive(sph_ctx *ctx, int *data, int64_t n);
 void launch_counting_sort(cudaStream_t st, int64_t n, int64_t ncells, const int *key, int *cursor,
                           const int *cstart, int *perm);

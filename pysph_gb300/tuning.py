@@ -28,6 +28,19 @@ def list_skin():
     return DEFAULT_SKIN
 
 
+def brick_passes():
+    """Whether the pair passes that qualify (one source of uniform h, no
+    periodic axis or variable-h relation) run the brick-staged kernels, which
+    stage each brick of cells' neighbour records in shared memory
+    (PYSPH_GB300_BRICKS=0 selects the list-streaming kernels everywhere)."""
+    env = os.environ.get("PYSPH_GB300_BRICKS")
+    if env is not None:
+        if env not in ("0", "1"):
+            raise ValueError("PYSPH_GB300_BRICKS must be 0 or 1")
+        return env == "1"
+    return True
+
+
 # measured defaults: (dimensions with extent) -> subdivision
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
 # neighbour-list entries hold the source slot in 32 - code bits (three

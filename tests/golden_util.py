@@ -28,3 +28,16 @@ def normwise(a, ref):
     if scale == 0:
         return float(np.abs(a).max())
     return float(np.abs(a - ref).max() / scale)
+
+
+def rel_percentiles(a, ref, floor=1e-3):
+    """Per-particle relative error |a - ref| / |ref| over the particles with
+    |ref| above floor * max |ref|: (p50, p99, max, particles counted)."""
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = np.abs(ref).max()
+    keep = np.abs(ref) > floor * scale
+    if not keep.any():
+        return 0.0, 0.0, 0.0, 0
+    r = np.abs(a[keep] - ref[keep]) / np.abs(ref[keep])
+    return float(np.percentile(r, 50)), float(np.percentile(r, 99)), float(r.max()), int(keep.sum())

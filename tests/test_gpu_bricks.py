@@ -1,0 +1,175 @@
+"""The brick-staged pair passes against the list-streaming ones and the oracle.
+
+With one source of uniform h, ``sph_density`` (SPHRho + Tait) and
+``sph_rates`` (PGrad + Monaghan AV, + XSPH) stage each brick of cells'
+neighbour records in shared memory and stream 16-bit lists into that
+staging.  The same step must match the list-streaming kernels
+(``PYSPH_GB300_BRICKS=0``) within FP32 rounding and the FP64 oracle within
+the 1e-5 normwise tolerance of every step-parity test, for every cell
+subdivision, in 2D and 3D, with non-real destinations, and on the paths for
+over-full lists and for bricks whose sources are read from global memory.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pysph_gb300
+from golden_util import normwise, rel_percentiles
+from pysph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+API = pysph_gb300.api()
+TOL = 1e-5          # normwise, against the FP64 oracle
+SAME = 2e-6         # normwise, brick-staged against list-streaming kernels
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+
+
+def _cube_step(props, bricks, monkeypatch, steps=1, dt=1e-4):
+    monkeypatch.setenv("PYSPH_GB300_BRICKS", "1" if bricks else "0")
+    s, particles = W.setup_cube(API, props)
+    for _ in range(steps):
+        s.integrator.integrate(dt)
+    pa = particles.arrays[0]
+    out = {p: pa.get(p) for p in ("x", "y", "z", "u", "v", "w", "rho", "p", "cs")}
+    return out, particles.cell_manager.brick_pass_count()
+
+
+@pytest.mark.parametrize("n,subdiv", [(32768, 1), (32768, 2), (64000, 3)])
+def test_cube_step_bricks_match_lists_and_oracle(n, subdiv, monkeypatch):
+    _need_gpu()
+    monkeypatch.setenv("PYSPH_GB300_SUBDIV", str(subdiv))
+    props = W.cube_lattice(n, seed=21)
+    got, nb = _cube_step(props, True, monkeypatch)
+    ref_list, nl = _cube_step(props, False, monkeypatch)
+    assert nb == 4 and nl == 0          # 2 density + 2 rates passes per RK2 step
+    prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+    prob.integrate_rk2(1e-4)
+    ref = prob.arrays["fluid"]
+    for p in ("rho", "p", "cs"):
+        assert normwise(got[p], ref_list[p]) < SAME, p
+        assert normwise(got[p], ref[p]) < TOL, p
+    for p in ("x", "y", "z", "u", "v", "w"):
+        assert normwise(got[p] - props[p], ref_list[p] - props[p]) < SAME, p
+        assert normwise(got[p] - props[p], ref[p] - props[p]) < TOL, p
+    p50, p99, mx, cnt = rel_percentiles(got["rho"], ref["rho"])
+    print("rho per-particle relative error p50 %.2e p99 %.2e max %.2e over %d" % (p50, p99, mx, cnt))
+    assert mx < 1e-5
+
+
+def test_drop_euler_step_with_xsph(monkeypatch):
+    """2D: PGrad + AV + XSPH in one brick-staged rates pass (the drop)."""
+    _need_gpu()
+    props = W.elliptical_drop(dx=0.0125, c0=100.0)
+    outs = {}
+    for bricks in (True, False):
+        monkeypatch.setenv("PYSPH_GB300_BRICKS", "1" if bricks else "0")
+        s, particles = W.setup_drop(API, props, c0=100.0)
+        s.integrator.integrate(1e-5)
+        pa = particles.arrays[0]
+        outs[bricks] = {p: pa.get(p) for p in ("x", "y", "u", "v", "rho", "p")}
+        assert (particles.cell_manager.brick_pass_count() > 0) == bricks
+    prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=100.0), dim=2)
+    prob.integrate_euler(1e-5)
+    ref = prob.arrays["fluid"]
+    for p in ("rho", "p"):
+        assert normwise(outs[True][p], outs[False][p]) < SAME, p
+        assert normwise(outs[True][p], ref[p]) < TOL, p
+    for p in ("x", "y", "u", "v"):
+        assert normwise(outs[True][p] - props[p], outs[False][p] - props[p]) < SAME, p
+        assert normwise(outs[True][p] - props[p], ref[p] - props[p]) < TOL, p
+
+
+def test_light_refresh_trajectory_matches_list_kernels(monkeypatch):
+    """Twenty RK2 steps with the list skin (light refreshes between full
+    builds): the brick-staged and list-streaming trajectories agree."""
+    _need_gpu()
+    props = W.cube_lattice(32768, seed=22)
+    a, _ = _cube_step(props, True, monkeypatch, steps=20)
+    b, _ = _cube_step(props, False, monkeypatch, steps=20)
+    for p in ("rho", "p"):
+        assert normwise(a[p], b[p]) < 1e-5, p
+    for p in ("x", "y", "z", "u", "v", "w"):
+        assert normwise(a[p] - props[p], b[p] - props[p]) < 1e-5, p
+
+
+def test_non_real_destinations_get_zero_in_bricks(monkeypatch):
+    _need_gpu()
+    monkeypatch.setenv("PYSPH_GB300_BRICKS", "1")
+    base, sph = API.base, API.sph
+    props = W.cube_lattice(8000, seed=23)
+    n = len(props["x"])
+    tag = np.zeros(n, np.int64)
+    tag[::5] = 1
+    pa = base.get_particle_array(name="fluid", **props)
+    pa.add_property({"name": "tag", "data": tag, "type": "long"})
+    pa.align_particles()
+    particles = base.Particles(arrays=[pa])
+    k3 = base.CubicSplineKernel(dim=3)
+    sph.SPHCalc(particles, [pa], pa, k3, [sph.SPHRho.get_func(pa, pa)], ["rho"]).sph("rho")
+    assert particles.cell_manager.brick_pass_count() == 1
+    rho = pa.get("rho", only_real_particles=False)
+    t = pa.get("tag", only_real_particles=False)
+    assert np.all(rho[t != 0] == 0)
+    host = {k: pa.get(k, only_real_particles=False) for k in ("x", "y", "z", "h", "m")}
+    host["tag"] = t
+    off, idx = oracle.neighbors(host, host, particles.cell_manager.cell_size, same=True)
+    ref = oracle.pair_sum("rho", host, host, off, idx, 3)[0]
+    assert normwise(rho, ref) < TOL
+
+
+_SUB = r'''
+import sys
+sys.path.insert(0, ".")
+import oracle, pysph_gb300
+from pysph_gb300 import workloads as W
+from tests.golden_util import normwise
+api = pysph_gb300.api()
+props = W.cube_lattice(32768, seed=24)
+s, particles = W.setup_cube(api, props)
+s.integrator.integrate(1e-4)
+assert particles.cell_manager.brick_pass_count() == 4
+pa = particles.arrays[0]
+prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+prob.integrate_rk2(1e-4)
+for p in ("rho", "p"):
+    assert normwise(pa.get(p), prob.arrays["fluid"][p]) < 1e-5, p
+for p in ("x", "u", "w"):
+    assert normwise(pa.get(p) - props[p], prob.arrays["fluid"][p] - props[p]) < 1e-5, p
+props = W.elliptical_drop(dx=0.025, c0=100.0)
+s, particles = W.setup_drop(api, props, c0=100.0)
+s.integrator.integrate(1e-5)
+assert particles.cell_manager.brick_pass_count() > 0
+pa = particles.arrays[0]
+prob = oracle.Problem({"fluid": props}, oracle.drop_ops(c0=100.0), dim=2)
+prob.integrate_euler(1e-5)
+for p in ("rho", "p"):
+    assert normwise(pa.get(p), prob.arrays["fluid"][p]) < 1e-5, p
+for p in ("x", "y", "u", "v"):
+    assert normwise(pa.get(p) - props[p], prob.arrays["fluid"][p] - props[p]) < 1e-5, p
+print("ok")
+'''
+
+
+@pytest.mark.parametrize("env", [{"SPH_BRICK_UNSTAGED": "1"}, {"SPH_LIST_CAP": "9"},
+                                 {"SPH_BRICK_UNSTAGED": "1", "SPH_LIST_CAP": "9"}],
+                         ids=["global-records", "over-full-lists", "both"])
+def test_brick_fallback_paths_match_oracle(env):
+    """Records read from global memory (bricks too populous for shared
+    memory) and lists shorter than the neighbour counts (completed by
+    re-traversal), forced on small sets in a fresh process."""
+    _need_gpu()
+    e = dict(os.environ, PYSPH_GB300_BRICKS="1", **env)
+    r = subprocess.run([sys.executable, "-c", _SUB], cwd=ROOT, env=e, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]

@@ -290,11 +290,13 @@ for p in ("x", "u", "w"):
 print("ok")
 '''
     import os
-    env = dict(os.environ, SPH_LIST_CAP="7")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
-                       text=True, timeout=600)
-    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]
+    # both kernel families: the list-streaming passes and the brick-staged ones
+    for bricks in ("0", "1"):
+        env = dict(os.environ, SPH_LIST_CAP="7", PYSPH_GB300_BRICKS=bricks)
+        r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0 and "ok" in r.stdout, (bricks, r.stderr[-3000:])
 
 
 def test_square4_momentum_and_density_rate():
@@ -611,7 +613,8 @@ for p in ("x", "y", "u", "v"):
 print("ok")
 '''
     import os
-    env = dict(os.environ, SPH_WIDE_CODES="1", PYSPH_GB300_SUBDIV="2")
+    # the list-streaming kernels carry the cell-offset codes
+    env = dict(os.environ, SPH_WIDE_CODES="1", PYSPH_GB300_SUBDIV="2", PYSPH_GB300_BRICKS="0")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
                        text=True, timeout=600)

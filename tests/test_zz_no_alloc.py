@@ -89,8 +89,9 @@ def test_noalloc_counts_only_local_real_particles():
     tag[::7] = 1
     tag[3::11] = 2
     pa.set(tag=tag)              # align_particles moves the non-real ones to the end
-    real = pa.get("tag") == 0
-    m, u, v, w = (pa.get(k) for k in ("m", "u", "v", "w"))
+    real = pa.get("tag", only_real_particles=False) == 0
+    assert real.size == 8000 and 0 < real.sum() < 8000
+    m, u, v, w = (pa.get(k, only_real_particles=False) for k in ("m", "u", "v", "w"))
     want = np.array([m[real].sum(), (m * u)[real].sum(), (m * v)[real].sum(),
                      (m * w)[real].sum(), (0.5 * m * (u * u + v * v + w * w))[real].sum(),
                      float(real.sum())])
