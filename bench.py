@@ -763,6 +763,8 @@ def run_gpu_drops(args):
                            "transfers": "SimulationBatch.set -> step -> get_all"}},
         "clocks": clk,
     }
+    if args.drop_error_steps > 0:
+        line["instance_error_vs_f64"] = drops_long_error(drops, best, recipe, args)
     if not args.no_cpu_baseline:
         sample = _drop_sample(drops, args.drop_sample)
         cb, ref_states = drops_cpu_baseline(drops, sample, args.cpu_steps, args.drop_c0)
@@ -782,9 +784,52 @@ def run_gpu_drops(args):
                 e[p] = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
             errs.append({"instance": i, "particles": len(drops[i]["x"]), "max_rel": max(e.values())})
         line["cpu_baseline"] = cb
-        line["instance_error_vs_f64"] = {"steps": args.cpu_steps, "norm": "||gpu-ref||/||ref|| "
-                                         "(displacements for x,y,u,v)", "instances": errs}
+        line["instance_error_vs_reference"] = {"steps": args.cpu_steps,
+                                               "norm": "||gpu-ref||/||ref|| (displacements for "
+                                                       "x,y,u,v)", "instances": errs}
     print(json.dumps(line), flush=True)
+
+
+def normwise(a, ref):
+    """max |a - ref| / max |ref| (the per-field parity metric)."""
+    import numpy as np
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = np.abs(ref).max()
+    return float(np.abs(a - ref).max() / scale) if scale > 0 else float(np.abs(a).max())
+
+
+def drops_long_error(drops, subdiv, recipe, args):
+    """Per-instance error after ``args.drop_error_steps`` batch steps against
+    FP64 runs of each drop alone (the oracle's C restatement, OpenMP), for a
+    sample stratified over the size range (smallest, largest, evenly
+    between)."""
+    import numpy as np
+
+    import oracle
+    from pysph_gb300.batch import SimulationBatch
+    sizes = np.array([len(d["x"]) for d in drops])
+    order = np.argsort(sizes)
+    pick = [int(order[i]) for i in np.linspace(0, len(order) - 1, args.drop_error_sample).astype(int)]
+    fresh = SimulationBatch(drops, subdiv=subdiv, **recipe)
+    fresh.step(args.drop_error_steps)
+    fresh.check()
+    out = []
+    for i in pick:
+        d = drops[i]
+        prob = oracle.Problem({"fluid": d}, oracle.drop_ops(c0=args.drop_c0), dim=2)
+        for _ in range(args.drop_error_steps):
+            prob.integrate_euler(DROPS_DT)
+        ref = prob.arrays["fluid"]
+        e = {p: normwise(fresh.get(i, p) - d[p], ref[p] - d[p]) for p in ("x", "y")}
+        e.update({p: normwise(fresh.get(i, p), ref[p]) for p in ("u", "v", "rho", "p")})
+        out.append({"instance": i, "particles": len(d["x"]), "errors": e,
+                    "max": max(e.values())})
+    return {"steps": args.drop_error_steps, "reference": "oracle C restatement, FP64",
+            "norm": "max|gpu-ref|/max|ref| per field (x, y as displacements)",
+            "sample": "stratified over the size range, %d of %d instances"
+                      % (len(pick), len(drops)),
+            "instances": out}
 
 
 def run_reference_drops(args):
@@ -1103,6 +1148,8 @@ def main():
     ap.add_argument("--drops", type=int, default=256)
     ap.add_argument("--drop-c0", type=float, default=100.0)
     ap.add_argument("--drop-sample", type=int, default=8)
+    ap.add_argument("--drop-error-steps", type=int, default=1000)
+    ap.add_argument("--drop-error-sample", type=int, default=8)
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 300 if (args.workload in ("cube", "drops") and args.impl == "gb300") else 20

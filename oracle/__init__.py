@@ -64,6 +64,8 @@ def lib():
             i = ctypes.c_int
             L.orc_neighbors.restype = ctypes.c_int64
             L.orc_neighbors.argtypes = [P, P, d, d, i, vp, vp]
+            L.orc_neighbor_digest.restype = ctypes.c_int64
+            L.orc_neighbor_digest.argtypes = [P, P, d, d, vp, vp]
             L.orc_neighbors_varh.restype = ctypes.c_int64
             L.orc_neighbors_varh.argtypes = [P, P, d, d, i, vp, vp]
             L.orc_sph_rho.argtypes = [P, P, vp, vp, i, vp]
@@ -135,6 +137,27 @@ def neighbors(dst, src, cell_size, radius_scale=2.0, same=False, variable_h=Fals
     index = np.zeros(max(int(offsets[-1]), 1), np.int64)
     fn(D.ref, S.ref, cell_size, radius_scale, int(same), offsets.ctypes.data, index.ctypes.data)
     return offsets, index[: offsets[-1]]
+
+
+def mix64(j):
+    """The splitmix64 finaliser of sph_oracle.c, elementwise over uint64."""
+    z = np.asarray(j).astype(np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def neighbor_digest(dst, src, cell_size, radius_scale=2.0):
+    """Per destination: neighbour count and the wrap-around sum of mix64 over
+    its source indices (an order-independent digest of the set), without
+    storing the lists."""
+    D, S = _Arr(dst), _Arr(src)
+    n = D.st.n
+    counts = np.zeros(n + 1, np.int64)
+    digest = np.zeros(max(n, 1), np.uint64)
+    lib().orc_neighbor_digest(D.ref, S.ref, cell_size, radius_scale, counts.ctypes.data,
+                              digest.ctypes.data)
+    return counts[1:], digest[:n]
 
 
 def pair_sum(kind, dst, src, offsets, index, dim, params=None, nout=3):

@@ -126,9 +126,20 @@ static int cmp_i64(const void *a, const void *b) {
  * symmetric = 1: also when |x_i - x_j|^2 < (radius_scale h_j)^2, the union
  *   VarHNbrParticleLocator builds from its reversed locator (base/nnps.pyx:
  *   654-749).                                                             */
+/* splitmix64 finaliser: an order-independent digest of a neighbour set is
+ * the wrap-around sum of mix(j) over its source indices j. */
+static inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* digest (pass 1 only, may be NULL): per destination, the sum of mix64(j)
+ * over its neighbours -- the set without storing it. */
 static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double cell_size,
                               double radius_scale, int same, int symmetric, int64_t *offsets,
-                              int64_t *index) {
+                              int64_t *index, uint64_t *digest) {
     int64_t ns = src->n, nd = dst->n;
     double hmax_src = 0.0;
     for (int64_t j = 0; j < ns; ++j)
@@ -153,6 +164,7 @@ static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double
         int64_t cx = (int)floor(px / cell_size), cy = (int)floor(py / cell_size),
                 cz = (int)floor(pz / cell_size);
         int64_t cnt = 0;
+        uint64_t dig = 0;
         int64_t base = index ? offsets[i] : 0;
         for (int64_t a = -d; a <= d; ++a)
             for (int64_t b = -d; b <= d; ++b)
@@ -174,6 +186,7 @@ static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double
                         }
                         if (hit) {
                             if (index) index[base + cnt] = j;
+                            if (digest) dig += mix64((uint64_t)j);
                             ++cnt;
                         }
                     }
@@ -190,6 +203,7 @@ static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double
             }
         } else {
             offsets[i + 1] = cnt;
+            if (digest) digest[i] = dig;
         }
         total += cnt;
     }
@@ -199,12 +213,20 @@ static int64_t neighbors_impl(const orc_array *dst, const orc_array *src, double
 
 int64_t orc_neighbors(const orc_array *dst, const orc_array *src, double cell_size,
                       double radius_scale, int same, int64_t *offsets, int64_t *index) {
-    return neighbors_impl(dst, src, cell_size, radius_scale, same, 0, offsets, index);
+    return neighbors_impl(dst, src, cell_size, radius_scale, same, 0, offsets, index, NULL);
 }
 
 int64_t orc_neighbors_varh(const orc_array *dst, const orc_array *src, double cell_size,
                            double radius_scale, int same, int64_t *offsets, int64_t *index) {
-    return neighbors_impl(dst, src, cell_size, radius_scale, same, 1, offsets, index);
+    return neighbors_impl(dst, src, cell_size, radius_scale, same, 1, offsets, index, NULL);
+}
+
+/* Neighbour counts (counts[i + 1], as pass 1 of orc_neighbors) and set
+ * digests (digest[i]) of every destination, in memory linear in the
+ * particle count: for sets too large to hold as lists. */
+int64_t orc_neighbor_digest(const orc_array *dst, const orc_array *src, double cell_size,
+                            double radius_scale, int64_t *counts, uint64_t *digest) {
+    return neighbors_impl(dst, src, cell_size, radius_scale, 0, 0, counts, NULL, digest);
 }
 
 /* ---------------------------------------------------------------------- */

@@ -18,7 +18,11 @@
 // indices into that staging, fixed between full builds (the sorted order and
 // the cell table do not change), so a pair costs one list entry, shared-
 // memory records and the pair arithmetic: no cell-offset decoding and no
-// global gathers.
+// global gathers.  The entries of a destination are grouped by eight (one
+// 16-byte load), groups of consecutive destinations adjacent, and the last
+// group is padded with the index of a zero-mass record placed far away
+// (index T, just past the staged records): the pair loop needs no bounds
+// predicates.
 //
 // The neighbour relation is the reference's: strict r^2 < (radius_scale
 // h)^2, decided in FP32 outside a +-1e-5 relative band around the threshold
@@ -73,7 +77,8 @@ struct BrickDensityArgs {
     BrickDstDev d;
     BrickSrcDev s;
     BrickSmem sm;
-    uint16_t *nbr;      // list entries: nbr[bdst[b] * cap + k * D_b + d]
+    uint16_t *nbr;      // list: 8-entry group g of destination d of brick b is
+                        // the uint4 (bdst[b] * cap / 8 + g * D_b + d)
     int *cnt;           // neighbour count per destination, brick order
     int *maxcnt;
     int cap;
@@ -232,40 +237,101 @@ __device__ __forceinline__ int staged_slot(const BlockGeo &G, const int *rlo, co
 // Source records: staged in shared memory, or (STAGED = false, a brick
 // more populous than the shared memory holds) recomputed from the sorted
 // arrays with the same operations.
+// Staging pointers of the dynamic shared memory.
+struct SmemPtrs {
+    float4 *P, *V;
+    float2 *S;
+    int *rlo, *roff, *dlo, *doff, *scell;
+};
+
+__device__ __forceinline__ SmemPtrs smem_ptrs(unsigned char *base, const BrickSmem &sm) {
+    SmemPtrs p;
+    p.P = reinterpret_cast<float4 *>(base);
+    p.V = reinterpret_cast<float4 *>(base + sm.off_v);
+    p.S = reinterpret_cast<float2 *>(base + sm.off_s);
+    p.rlo = reinterpret_cast<int *>(base + sm.off_rlo);
+    p.roff = reinterpret_cast<int *>(base + sm.off_roff);
+    p.dlo = reinterpret_cast<int *>(base + sm.off_dlo);
+    p.doff = reinterpret_cast<int *>(base + sm.off_doff);
+    p.scell = reinterpret_cast<int *>(base + sm.off_scell);
+    return p;
+}
+
+// The padding record (index T): far away, zero mass, at rest -- every pair
+// term with it is exactly 0.
+__device__ __forceinline__ float4 pad_pos() { return make_float4(1e15f, 1e15f, 1e15f, 0.f); }
+__device__ __forceinline__ float4 pad_vel() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ float2 pad_state() { return make_float2(0.5f, 0.f); }
+
 template <bool STAGED>
-struct SrcRecords {
+struct SrcRecords;
+
+// staged in shared memory
+template <>
+struct SrcRecords<true> {
     const float4 *P, *V;
     const float2 *S;
-    const BrickSrcDev *src;
-    const BlockGeo *G;
-    const int *rlo, *roff;
-    float csf;
-    __device__ __forceinline__ float4 pos(int t) const {
-        if (STAGED) return P[t];
-        int cy, cz;
-        const int j = staged_slot(*G, rlo, roff, t, cy, cz);
-        return rel_pos(src->pm, src->scx, j, cy, cz, *G, csf);
-    }
+    __device__ __forceinline__ float4 pos(int t) const { return P[t]; }
     // (u, v, w, p / rho^2) and (rho, cs)
     __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
-        if (STAGED) {
-            v = V[t];
-            s = S[t];
-            return;
-        }
-        int cy, cz;
-        const int j = staged_slot(*G, rlo, roff, t, cy, cz);
-        const float4 vh = src->velh[j], st = src->st[j];
-        v = make_float4(vh.x, vh.y, vh.z, st.y);
-        s = make_float2(st.x, st.z);
+        v = V[t];
+        s = S[t];
     }
 };
 
+// recomputed from the sorted arrays with the staging's operations
+template <>
+struct SrcRecords<false> {
+    const BrickSrcDev *src;
+    BlockGeo G;
+    const int *rlo, *roff;
+    float csf;
+    int T;
+    float halpha;
+    __device__ __forceinline__ float4 pos(int t) const {
+        if (t >= T) return pad_pos();
+        int cy, cz;
+        const int j = staged_slot(G, rlo, roff, t, cy, cz);
+        return rel_pos(src->pm, src->scx, j, cy, cz, G, csf);
+    }
+    __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
+        if (t >= T) {
+            v = pad_vel();
+            s = pad_state();
+            return;
+        }
+        int cy, cz;
+        const int j = staged_slot(G, rlo, roff, t, cy, cz);
+        const float4 vh = src->velh[j], st = src->st[j];
+        v = make_float4(vh.x, vh.y, vh.z, st.y);
+        s = make_float2(0.5f * st.x, halpha * st.z);
+    }
+};
+
+template <bool STAGED>
+__device__ __forceinline__ SrcRecords<STAGED> make_records(const SmemPtrs &sp, const BrickSrcDev &S,
+                                                           const BlockGeo &G, float csf, int T,
+                                                           float halpha);
+template <>
+__device__ __forceinline__ SrcRecords<true> make_records<true>(const SmemPtrs &sp, const BrickSrcDev &,
+                                                               const BlockGeo &, float, int, float) {
+    return SrcRecords<true>{sp.P, sp.V, sp.S};
+}
+template <>
+__device__ __forceinline__ SrcRecords<false> make_records<false>(const SmemPtrs &sp,
+                                                                 const BrickSrcDev &S,
+                                                                 const BlockGeo &G, float csf,
+                                                                 int T, float halpha) {
+    return SrcRecords<false>{&S, G, sp.rlo, sp.roff, csf, T, halpha};
+}
+
 // Copy the block's source records into shared memory.
+// Rates records: (u, v, w, p / rho^2) and (rho / 2, alpha cs / 2), the
+// halves that the pair averages of the artificial viscosity add.
 template <bool RATES>
 __device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
                                       const int *roff, int T, float csf, float4 *P, float4 *V,
-                                      float2 *SS) {
+                                      float2 *SS, float halpha = 0.f) {
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         int cy, cz;
         const int j = staged_slot(G, rlo, roff, t, cy, cz);
@@ -273,9 +339,22 @@ __device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, c
         if (RATES) {
             const float4 vh = S.velh[j], st = S.st[j];
             V[t] = make_float4(vh.x, vh.y, vh.z, st.y);
-            SS[t] = make_float2(st.x, st.z);
+            SS[t] = make_float2(0.5f * st.x, halpha * st.z);
         }
     }
+    if (threadIdx.x == 0) {
+        P[T] = pad_pos();
+        if (RATES) {
+            V[T] = pad_vel();
+            SS[T] = pad_state();
+        }
+    }
+}
+
+// The 16-bit entry i (0..7) of a group.
+__device__ __forceinline__ int group_entry(const uint4 &q, int i) {
+    const unsigned w = i < 2 ? q.x : (i < 4 ? q.y : (i < 6 ? q.z : q.w));
+    return (int)((i & 1) ? (w >> 16) : (w & 0xffffu));
 }
 
 // One destination of the block.
@@ -377,57 +456,72 @@ __device__ __forceinline__ void brick_traverse(const Grid &g, const BlockGeo &G,
     }
 }
 
-// Staging pointers of the dynamic shared memory.
-struct SmemPtrs {
-    float4 *P, *V;
-    float2 *S;
-    int *rlo, *roff, *dlo, *doff, *scell;
-};
-
-__device__ __forceinline__ SmemPtrs smem_ptrs(unsigned char *base, const BrickSmem &sm) {
-    SmemPtrs p;
-    p.P = reinterpret_cast<float4 *>(base);
-    p.V = reinterpret_cast<float4 *>(base + sm.off_v);
-    p.S = reinterpret_cast<float2 *>(base + sm.off_s);
-    p.rlo = reinterpret_cast<int *>(base + sm.off_rlo);
-    p.roff = reinterpret_cast<int *>(base + sm.off_roff);
-    p.dlo = reinterpret_cast<int *>(base + sm.off_dlo);
-    p.doff = reinterpret_cast<int *>(base + sm.off_doff);
-    p.scell = reinterpret_cast<int *>(base + sm.off_scell);
-    return p;
-}
-
 __device__ __forceinline__ bool gate_off(const unsigned *gate) {
     return gate != nullptr && __ldg(gate) != 0u;
-}
-
-// Neighbours of a destination past its list's capacity (skipping the cap
-// listed ones, in the order of the list build), added to its density sum.
-// Out of line: rare, and it would raise the register count of the stream.
-template <int K, bool STAGED>
-__device__ __noinline__ void density_overflow(const Grid &g, const BlockGeo &G,
-                                              const BrickSrcDev &S, const BrickDstDev &D,
-                                              const SrcRecords<STAGED> &R, const int *rlo,
-                                              const int *roff, const int *dlo, const int *doff,
-                                              int d, int cap, float ih, float fac, CSum &rho) {
-    BrickDest q;
-    brick_dest(g, D, G, dlo, doff, d, q);
-    int skip = cap;
-    brick_traverse<K, STAGED>(g, G, S, D, R, rlo, roff, nullptr, q,
-        [&](int t, float rx, float ry, float rz, bool hit) {
-            if (skip > 0) { --skip; return; }
-            if (!hit) return;
-            const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-            const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-            rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
-        });
 }
 
 // ---------------------------------------------------------------------------
 // summation density (density_funcs.pyx:38-74) + Tait (eos_funcs.pyx:105-116)
 // ---------------------------------------------------------------------------
+// fac W(q) of the cubic spline (base/kernels.pyx:351-374), the normalisation
+// (and any constant factor) folded into the coefficients: fac (1 - 1.5 q^2
+// + 0.75 q^3) for q <= 1, fac / 4 (2 - q)^3 for 1 < q <= 2, else 0.
+struct WCoef {
+    float i0, i1, i2, o;
+};
+
+__device__ __forceinline__ WCoef w_coef(float fac, float scale) {
+    const float f = fac * scale;
+    return WCoef{f, -1.5f * f, 0.75f * f, 0.25f * f};
+}
+
+__device__ __forceinline__ float w_of(float q, const WCoef &c) {
+    const float inner = fmaf(q * q, fmaf(c.i2, q, c.i1), c.i0);
+    const float t = 2.f - q;
+    const float outer = c.o * (t * t) * t;
+    return q > 2.f ? 0.f : (q > 1.f ? outer : inner);
+}
+
+__device__ __forceinline__ float density_term(const float4 &pi, const float4 &pj, float ih,
+                                              const WCoef &wc) {
+    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+    const float r = r2 * rsqrtf(fmaxf(r2, 1e-30f));
+    return w_of(r * ih, wc) * pj.w;
+}
+
+// Density of one destination and, with Tait, its p and cs; the sorted
+// state record when the pass writes the destination's own properties.
+__device__ __forceinline__ void density_store(const BrickDensityArgs &A, int s, int orig, bool real,
+                                              double r64) {
+    if (A.rho_out) A.rho_out[orig] = r64;
+    const float rf = (float)r64;
+    float pf = 0.f, cf = 0.f;
+    if (A.tait) {
+        if (real) {
+            // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), through
+            // log1p/expm1 of the density excess (relative accuracy of p as rho -> ro)
+            const float Bt = A.co * A.co * A.ro / A.gamma;
+            const float lr = log1pf((float)((r64 - (double)A.ro) / (double)A.ro));
+            pf = Bt * expm1f(A.gamma * lr);
+            cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
+        }
+        A.p_out[orig] = (double)pf;
+        A.cs_out[orig] = (double)cf;
+    }
+    if (A.st_out) {
+        const float mi = A.d.pm[s].w;
+        if (A.tait) {
+            A.st_out[s] = make_float4(rf, pf / (rf * rf), cf, mi);
+        } else {
+            const float pold = (float)ld0(A.d.p, orig);
+            A.st_out[s] = make_float4(rf, pold / (rf * rf), (float)ld0(A.d.cs, orig), mi);
+        }
+    }
+}
+
 template <int K, bool BUILD, bool STAGED>
-__global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityArgs A) {
+__global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (gate_off(A.gate)) return;
     const int b = blockIdx.x;
@@ -439,17 +533,19 @@ __global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityA
     int T, D;
     block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
     const int dbase = A.d.bdst[b];
-    const int cap = A.cap;
+    const int cap = A.cap;            // a multiple of 8
+    const int ng_cap = cap >> 3;
     // the stencil cell table of a list build (a destination whose neighbours
     // outgrew the list reads the grid's table instead)
     int *scell = BUILD ? sp.scell : nullptr;
     if (BUILD) cell_table(g, G, A.s.cstart, sp.rlo, sp.roff, sp.scell);
     if (STAGED) stage<false>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, nullptr, nullptr);
     __syncthreads();
-    SrcRecords<STAGED> R{sp.P, nullptr, nullptr, &A.s, &G, sp.rlo, sp.roff, g.cs_f};
+    const SrcRecords<STAGED> R = make_records<STAGED>(sp, A.s, G, g.cs_f, T, 0.f);
     const float ih = __fdividef(1.f, g.h_uniform);
     const float fac = cubic_fac(A.dim, ih);
-    const uint16_t *lbase = A.nbr + (size_t)dbase * cap;
+    const WCoef wc = w_coef(fac, 1.f);
+    const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * ng_cap;
     for (int d = threadIdx.x; d < D; d += blockDim.x) {
         BrickDest q;
         const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
@@ -457,55 +553,44 @@ __global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityA
         int c = 0;
         if (real) {
             if (BUILD) {
-                uint16_t *out = A.nbr + (size_t)dbase * cap + d;
+                uint16_t *out = A.nbr + ((size_t)dbase * ng_cap + d) * 8;
+                const size_t gstride = (size_t)D * 8;
                 brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, scell, q,
                     [&](int t, float rx, float ry, float rz, bool hit) {
-                        if (c < cap) out[(size_t)c * D] = (uint16_t)t;
+                        if (c < cap) out[(size_t)(c >> 3) * gstride + (c & 7)] = (uint16_t)t;
                         ++c;
                         if (!hit) return;
                         const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                         const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
                         rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
                     });
+                // pad the last group with the zero record
+                for (int k = c; k < cap && (k & 7); ++k)
+                    out[(size_t)(k >> 3) * gstride + (k & 7)] = (uint16_t)T;
             } else {
-                // stream the list in batches of 6 (entries of the next batch
-                // requested before the records of this one are used)
-                constexpr int B = 6;
+                // stream the groups of 8 entries, two groups requested ahead
                 c = A.cnt[dbase + d];
-                const int m = min(c, cap);
-                const uint16_t *lst = lbase + d;
-                int e[B];
-                auto entries = [&](int (&o)[B], int k) {
-                    o[0] = lst[(size_t)k * D];
-#pragma unroll
-                    for (int i = 1; i < B; ++i) o[i] = (k + i < m) ? lst[(size_t)(k + i) * D] : o[0];
-                };
-                if (m > 0) entries(e, 0);
-                for (int k = 0; k < m; k += B) {
-                    int en[B];
-                    const bool more = k + B < m;
-                    if (more) entries(en, k + B);
-                    float4 pj[B];
-#pragma unroll
-                    for (int i = 0; i < B; ++i) pj[i] = R.pos(e[i]);
+                const int ng = (min(c, cap) + 7) >> 3;
+                const uint4 *lst = lgrp + d;
+                uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
+                if (ng > 0) cur = lst[0];
+                if (ng > 1) nxt = lst[D];
+                for (int gi = 0; gi < ng; ++gi) {
+                    uint4 fut = nxt;
+                    if (gi + 2 < ng) fut = lst[(size_t)(gi + 2) * D];
                     float part = 0.f;
 #pragma unroll
-                    for (int i = 0; i < B; ++i) {
-                        const float rx = q.P.x - pj[i].x, ry = q.P.y - pj[i].y, rz = q.P.z - pj[i].z;
-                        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                        const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                        const float wv = cubic_w(r * ih) * fac * pj[i].w;
-                        part += (k + i < m) ? wv : 0.f;
+                    for (int h = 0; h < 2; ++h) {
+                        float4 pj[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) pj[i] = R.pos(group_entry(cur, 4 * h + i));
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) part += density_term(q.P, pj[i], ih, wc);
                     }
                     rho.add(part);
-                    if (more) {
-#pragma unroll
-                        for (int i = 0; i < B; ++i) e[i] = en[i];
-                    }
+                    cur = nxt;
+                    nxt = fut;
                 }
-                if (c > cap)
-                    density_overflow<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, sp.dlo, sp.doff, d,
-                                                cap, ih, fac, rho);
             }
         }
         if (BUILD) {
@@ -514,33 +599,27 @@ __global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityA
             const int wmax = __reduce_max_sync(act, c);
             if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.maxcnt, wmax);
         }
-        if (!A.write_out) continue;
-        const int orig = q.orig;
-        const double r64 = real ? rho.value() : 0.0;
-        if (A.rho_out) A.rho_out[orig] = r64;
-        const float rf = (float)r64;
-        float pf = 0.f, cf = 0.f;
-        if (A.tait) {
-            if (real) {
-                // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), through
-                // log1p/expm1 of the density excess (relative accuracy of p as rho -> ro)
-                const float Bt = A.co * A.co * A.ro / A.gamma;
-                const float lr = log1pf((float)((r64 - (double)A.ro) / (double)A.ro));
-                pf = Bt * expm1f(A.gamma * lr);
-                cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
-            }
-            A.p_out[orig] = (double)pf;
-            A.cs_out[orig] = (double)cf;
-        }
-        if (A.st_out) {
-            const float mi = A.d.pm[q.s].w;
-            if (A.tait) {
-                A.st_out[q.s] = make_float4(rf, pf / (rf * rf), cf, mi);
-            } else {
-                const float pold = (float)ld0(A.d.p, orig);
-                A.st_out[q.s] = make_float4(rf, pold / (rf * rf), (float)ld0(A.d.cs, orig), mi);
-            }
-        }
+        if (A.write_out) density_store(A, q.s, q.orig, real, real ? rho.value() : 0.0);
+    }
+    if (BUILD || !A.write_out || A.rho_out == nullptr) return;
+    // destinations with more neighbours than their list holds: the rest
+    // come from a traversal that skips the listed ones (in the order of
+    // the list build), added to the stored partial density
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        if (A.cnt[dbase + d] <= cap) continue;
+        BrickDest q;
+        if (!brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q)) continue;
+        CSum rest;
+        int skip = cap;
+        brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, nullptr, q,
+            [&](int t, float rx, float ry, float rz, bool hit) {
+                if (skip > 0) { --skip; return; }
+                if (!hit) return;
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                rest.add(cubic_w(r * ih) * fac * R.pos(t).w);
+            });
+        density_store(A, q.s, q.orig, true, A.rho_out[q.orig] + rest.value());
     }
 }
 
@@ -551,43 +630,64 @@ __global__ void __maxnreg__(80) k_bdensity(const __grid_constant__ BrickDensityA
 // (position_funcs.pyx:32-60) folded into the store
 // ---------------------------------------------------------------------------
 struct RatesConst {
-    float h, ih, fac, alpha, beta, eta2, eps;
+    float h, ih, beta, eta2h2;
+    float gin0, gin1, gout;     // fac dW/dr / r: gin1 q + gin0 (q < 1), gout (2-q)^2 / r (q < 2)
+    WCoef wx;                   // eps fac W(q) (XSPH)
 };
+
+__device__ __forceinline__ RatesConst rates_const(float h, float fac, float beta, float eta2,
+                                                  float eps) {
+    RatesConst k;
+    k.h = h;
+    k.ih = __fdividef(1.f, h);
+    k.beta = beta;
+    k.eta2h2 = eta2 * h * h;
+    // fac 3 (0.75 q - 1) / h^2 and -0.75 fac (2 - q)^2 / (h r) (base/kernels.pyx:376-413)
+    k.gin1 = 2.25f * fac * k.ih * k.ih;
+    k.gin0 = -3.f * fac * k.ih * k.ih;
+    k.gout = -0.75f * fac * k.ih;
+    k.wx = w_coef(fac, eps);
+    return k;
+}
 
 // destination state and the sums: plain FP32 partials of a batch, merged
 // into the Neumaier-compensated totals by flush()
 struct RatesAcc {
     float4 vi;
-    float rhoi, pri, ci;
+    float hrhoi, pri, haci;     // rho_i / 2, p_i / rho_i^2, alpha cs_i / 2
     float pax, pay, paz, pxx, pxy, pxz;
     CSum ax, ay, az, xx, xy, xz;
 };
 
-template <bool XSPH>
-__device__ __forceinline__ void rates_pair(RatesAcc &a, const RatesConst &k, float okf, float rx,
-                                           float ry, float rz, const float4 &pj, const float4 &vj,
+// One pair: pressure gradient -m_j (p_i/rho_i^2 + p_j/rho_j^2) grad W
+// (pressure_funcs.pyx:67-91), Monaghan viscosity -m_j Pi_ab grad W with
+// mu = h v_ab.r_ab / (r^2 + eta^2 h^2) for approaching pairs
+// (viscosity_funcs.pyx:72-124; min(v.r, 0) gives mu = 0 otherwise, and
+// with eta = 0, as the reference's class always has, 1/r^2 comes from the
+// rsqrt already taken), and XSPH eps m_j W (v_j - v_i) / rho_ab
+// (xsph_funcs.pyx:44-88), sharing 1 / rho_ab.
+template <bool XSPH, bool ETA0>
+__device__ __forceinline__ void rates_pair(RatesAcc &a, const RatesConst &k, float rx, float ry,
+                                           float rz, const float4 &pj, const float4 &vj,
                                            const float2 &sj) {
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
-    const float qq = r2 * rinv * k.ih;
+    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float q = r2 * rinv * k.ih;
     const float mj = pj.w;
-    float t = -mj * (a.pri + vj.w);
-    // Pi_ab only for approaching pairs (v_ab . r_ab < 0), as a select
     const float dot = (a.vi.x - vj.x) * rx + (a.vi.y - vj.y) * ry + (a.vi.z - vj.z) * rz;
-    const bool neg = dot < 0.f;
-    const float den = neg ? fmaf(k.eta2 * k.h, k.h, r2) : 1.f;
-    const float mu = neg ? __fdividef(k.h * dot, den) : 0.f;
-    const float cab = 0.5f * (a.ci + sj.y);
-    const float rhoab = 0.5f * (a.rhoi + sj.x);
-    const float piab = __fdividef(fmaf(k.beta * mu, mu, -k.alpha * cab * mu), rhoab);
-    t -= mj * (neg ? piab : 0.f);
-    const float gf = cubic_gfac(qq, k.ih, rinv) * k.fac * t * okf;
+    const float hdot = k.h * fminf(dot, 0.f);
+    const float mu = ETA0 ? hdot * rinv * rinv : __fdividef(hdot, r2 + k.eta2h2);
+    const float inv_rhoab = __fdividef(1.f, a.hrhoi + sj.x);
+    const float piab = mu * fmaf(k.beta, mu, -(a.haci + sj.y)) * inv_rhoab;
+    const float t = -mj * ((a.pri + vj.w) + piab);
+    const float tq = 2.f - q;
+    const float g = q > 2.f ? 0.f : (q >= 1.f ? k.gout * (tq * tq) * rinv : fmaf(k.gin1, q, k.gin0));
+    const float gf = g * t;
     a.pax = fmaf(gf, rx, a.pax);
     a.pay = fmaf(gf, ry, a.pay);
     a.paz = fmaf(gf, rz, a.paz);
     if (XSPH) {
-        const float rhox = 0.5f * (sj.x + a.rhoi);
-        const float temp = __fdividef(mj * (cubic_w(qq) * k.fac), rhox) * k.eps * okf;
+        const float temp = mj * w_of(q, k.wx) * inv_rhoab;
         a.pxx = fmaf(temp, vj.x - a.vi.x, a.pxx);
         a.pxy = fmaf(temp, vj.y - a.vi.y, a.pxy);
         a.pxz = fmaf(temp, vj.z - a.vi.z, a.pxz);
@@ -604,15 +704,47 @@ __device__ __forceinline__ void rates_flush(RatesAcc &a) {
     }
 }
 
-// Neighbours past the list's capacity (out of line, as density_overflow).
-template <int K, bool XSPH, bool STAGED>
-__device__ __noinline__ void rates_overflow(const Grid &g, const BlockGeo &G, const BrickSrcDev &S,
-                                            const BrickDstDev &D, const SrcRecords<STAGED> &R,
-                                            const int *rlo, const int *roff, const int *dlo,
-                                            const int *doff, int d, int cap, const RatesConst &k,
-                                            RatesAcc &a) {
-    BrickDest q;
-    brick_dest(g, D, G, dlo, doff, d, q);
+// The sums of one destination: its list streamed in groups of 8 entries
+// (two groups requested ahead), records two at a time, flushed every 4.
+template <bool XSPH, bool ETA0, bool STAGED>
+__device__ __forceinline__ void rates_stream(RatesAcc &acc, const RatesConst &kc,
+                                             const SrcRecords<STAGED> &R, const uint4 *lst, int D,
+                                             int ng, const float4 &Pi) {
+    uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
+    if (ng > 0) cur = lst[0];
+    if (ng > 1) nxt = lst[D];
+    for (int gi = 0; gi < ng; ++gi) {
+        uint4 fut = nxt;
+        if (gi + 2 < ng) fut = lst[(size_t)(gi + 2) * D];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            float4 pj[2], vj[2];
+            float2 sj[2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int t = group_entry(cur, 2 * h + i);
+                pj[i] = R.pos(t);
+                R.state(t, vj[i], sj[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+                rates_pair<XSPH, ETA0>(acc, kc, Pi.x - pj[i].x, Pi.y - pj[i].y, Pi.z - pj[i].z,
+                                       pj[i], vj[i], sj[i]);
+            if (h & 1) rates_flush<XSPH>(acc);
+        }
+        cur = nxt;
+        nxt = fut;
+    }
+}
+
+// Neighbours of destination q past its list's capacity: a traversal that
+// skips the listed ones (in the order of the list build).
+template <int K, bool XSPH, bool ETA0, bool STAGED>
+__device__ __forceinline__ void rates_rest(RatesAcc &acc, const RatesConst &kc, const Grid &g,
+                                           const BlockGeo &G, const BrickSrcDev &S,
+                                           const BrickDstDev &D, const SrcRecords<STAGED> &R,
+                                           const int *rlo, const int *roff, const BrickDest &q,
+                                           int cap) {
     int skip = cap;
     brick_traverse<K, STAGED>(g, G, S, D, R, rlo, roff, nullptr, q,
         [&](int t, float rx, float ry, float rz, bool hit) {
@@ -621,80 +753,36 @@ __device__ __noinline__ void rates_overflow(const Grid &g, const BlockGeo &G, co
             float4 vj;
             float2 sj;
             R.state(t, vj, sj);
-            rates_pair<XSPH>(a, k, 1.f, rx, ry, rz, R.pos(t), vj, sj);
-            rates_flush<XSPH>(a);
+            rates_pair<XSPH, ETA0>(acc, kc, rx, ry, rz, R.pos(t), vj, sj);
+            rates_flush<XSPH>(acc);
         });
 }
 
-template <int K, bool XSPH, bool STAGED>
-__global__ void __maxnreg__(80) k_brates(const __grid_constant__ BrickRatesArgs A) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    if (gate_off(A.gate)) return;
-    const int b = blockIdx.x;
-    const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
-    if (nd == 0) return;
-    const Grid &g = A.g;
-    const BlockGeo G = block_geo(g, A.bk, b);
-    SmemPtrs sp = smem_ptrs(smem, A.sm);
-    int T, D;
-    block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
-    const int dbase = A.d.bdst[b];
+__device__ __forceinline__ void rates_acc_init(RatesAcc &acc, const float4 &vi, const float4 &st,
+                                               float halpha) {
+    acc.pax = acc.pay = acc.paz = acc.pxx = acc.pxy = acc.pxz = 0.f;
+    acc.vi = vi;
+    acc.hrhoi = 0.5f * st.x;
+    acc.pri = st.y;
+    acc.haci = halpha * st.z;
+}
+
+template <int K, bool XSPH, bool ETA0, bool STAGED>
+__device__ __forceinline__ void rates_block(const BrickRatesArgs &A, const Grid &g,
+                                            const BlockGeo &G, const SmemPtrs &sp,
+                                            const SrcRecords<STAGED> &R, const RatesConst &kc,
+                                            int D, int dbase) {
     const int cap = A.cap;
-    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, sp.V, sp.S);
-    __syncthreads();
-    SrcRecords<STAGED> R{sp.P, sp.V, sp.S, &A.s, &G, sp.rlo, sp.roff, g.cs_f};
-    RatesConst kc;
-    kc.h = g.h_uniform;
-    kc.ih = __fdividef(1.f, kc.h);
-    kc.fac = cubic_fac(A.dim, kc.ih);
-    kc.alpha = A.alpha; kc.beta = A.beta; kc.eta2 = A.eta2; kc.eps = A.eps;
-    const uint16_t *lbase = A.nbr + (size_t)dbase * cap;
+    const float halpha = 0.5f * A.alpha;
+    const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * (cap >> 3);
     for (int d = threadIdx.x; d < D; d += blockDim.x) {
         BrickDest q;
         const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
         RatesAcc acc;
-        acc.pax = acc.pay = acc.paz = acc.pxx = acc.pxy = acc.pxz = 0.f;
+        rates_acc_init(acc, A.d.velh[q.s], A.d.st[q.s], halpha);
         if (real) {
-            acc.vi = A.d.velh[q.s];
-            const float4 sti = A.d.st[q.s];
-            acc.rhoi = sti.x; acc.pri = sti.y; acc.ci = sti.z;
-            // stream the list in batches of 3 (entries of the next batch
-            // requested before the records of this one are used)
-            constexpr int B = 3;
             const int c = A.cnt[dbase + d];
-            const int m = min(c, cap);
-            const uint16_t *lst = lbase + d;
-            int e[B];
-            auto entries = [&](int (&o)[B], int k) {
-                o[0] = lst[(size_t)k * D];
-#pragma unroll
-                for (int i = 1; i < B; ++i) o[i] = (k + i < m) ? lst[(size_t)(k + i) * D] : o[0];
-            };
-            if (m > 0) entries(e, 0);
-            for (int k = 0; k < m; k += B) {
-                int en[B];
-                const bool more = k + B < m;
-                if (more) entries(en, k + B);
-                float4 pj[B], vj[B];
-                float2 sj[B];
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    pj[i] = R.pos(e[i]);
-                    R.state(e[i], vj[i], sj[i]);
-                }
-#pragma unroll
-                for (int i = 0; i < B; ++i)
-                    rates_pair<XSPH>(acc, kc, k + i < m ? 1.f : 0.f, q.P.x - pj[i].x,
-                                     q.P.y - pj[i].y, q.P.z - pj[i].z, pj[i], vj[i], sj[i]);
-                rates_flush<XSPH>(acc);
-                if (more) {
-#pragma unroll
-                    for (int i = 0; i < B; ++i) e[i] = en[i];
-                }
-            }
-            if (c > cap)
-                rates_overflow<K, XSPH, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, sp.dlo, sp.doff, d,
-                                                cap, kc, acc);
+            rates_stream<XSPH, ETA0, STAGED>(acc, kc, R, lgrp + d, D, (min(c, cap) + 7) >> 3, q.P);
         }
         const int orig = q.orig;
         double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
@@ -715,6 +803,48 @@ __global__ void __maxnreg__(80) k_brates(const __grid_constant__ BrickRatesArgs 
             if (A.pos[k]) A.pos[k][orig] = (A.accumulate ? A.pos[k][orig] : 0.0) + p3[k];
         }
     }
+    // destinations with more neighbours than their list holds: the rest
+    // added to the stored sums
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        if (A.cnt[dbase + d] <= cap) continue;
+        BrickDest q;
+        if (!brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q)) continue;
+        RatesAcc acc;
+        rates_acc_init(acc, A.d.velh[q.s], A.d.st[q.s], halpha);
+        rates_rest<K, XSPH, ETA0, STAGED>(acc, kc, g, G, A.s, A.d, R, sp.rlo, sp.roff, q, cap);
+        const double a3[3] = {acc.ax.value(), acc.ay.value(), acc.az.value()};
+        const double p3[3] = {acc.xx.value(), acc.xy.value(), acc.xz.value()};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (A.acc[k]) A.acc[k][q.orig] += a3[k];
+            if (A.pos[k]) A.pos[k][q.orig] += p3[k];
+        }
+    }
+}
+
+template <int K, bool XSPH, bool STAGED>
+__global__ void __maxnreg__(XSPH ? 80 : 64) k_brates(const __grid_constant__ BrickRatesArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (gate_off(A.gate)) return;
+    const int b = blockIdx.x;
+    const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
+    if (nd == 0) return;
+    const Grid &g = A.g;
+    const BlockGeo G = block_geo(g, A.bk, b);
+    SmemPtrs sp = smem_ptrs(smem, A.sm);
+    int T, D;
+    block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
+    const float halpha = 0.5f * A.alpha;
+    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, sp.V, sp.S, halpha);
+    __syncthreads();
+    const SrcRecords<STAGED> R = make_records<STAGED>(sp, A.s, G, g.cs_f, T, halpha);
+    const float ih = __fdividef(1.f, g.h_uniform);
+    const RatesConst kc = rates_const(g.h_uniform, cubic_fac(A.dim, ih), A.beta, A.eta2, A.eps);
+    const int dbase = A.d.bdst[b];
+    if (A.eta2 == 0.f)
+        rates_block<K, XSPH, true, STAGED>(A, g, G, sp, R, kc, D, dbase);
+    else
+        rates_block<K, XSPH, false, STAGED>(A, g, G, sp, R, kc, D, dbase);
 }
 
 // ---------------------------------------------------------------------------
@@ -772,7 +902,8 @@ int brick_layout(const sph_ctx *ctx, const ArraySnap &S, bool rates, bool cells,
     const size_t ncell = cells ? (size_t)nr * (lx + 1) : 0;
     const size_t tables = sizeof(int) * ((size_t)nr + nr + 1 + ndr + ndr + 1 + ncell);
     const size_t rec = rates ? (16 + 16 + 8) : 16;
-    size_t cap = (size_t)std::max(S.b_tmax, 1);
+    // the staged records and the padding record after them
+    size_t cap = (size_t)std::max(S.b_tmax, 0) + 1;
     // environment SPH_BRICK_UNSTAGED=1 reads every record from global memory
     // (the path of bricks too populous for shared memory), to test it on
     // small sets
@@ -819,9 +950,12 @@ BrickDstDev make_bdst(const ArraySnap &D) {
     return d;
 }
 
+// Threads per block: the largest brick population rounded to warps, at
+// most 320 (three blocks of 64-register threads per SM); a brick with more
+// destinations takes them in rounds.
 int brick_threads(const ArraySnap &D) {
     const int want = (std::max(D.b_dmax, 1) + 31) / 32 * 32;
-    return std::min(std::max(want, 64), kBrickMaxThreads);
+    return std::min(std::max(want, 64), 320);
 }
 
 template <class Kern>
@@ -852,8 +986,15 @@ void brick_geometry(sph_ctx *ctx) {
     const Grid &g = ctx->grid;
     BrickGeom &bk = ctx->bricks;
     const int K = g.kx;
+    // environment SPH_BRICK_EDGE: the brick edge in cells (3D), to measure
+    // other brick sizes
+    static int edge = -1;
+    if (edge < 0) {
+        const char *e = getenv("SPH_BRICK_EDGE");
+        edge = e ? std::max(1, atoi(e)) : 0;
+    }
     if (g.kz > 0) {
-        const int e = K == 1 ? 3 : (K == 2 ? 5 : 8);
+        const int e = edge > 0 ? edge : (K == 1 ? 3 : (K == 2 ? 5 : 8));
         bk.bx = bk.by = bk.bz = e;
     } else if (g.ky > 0) {
         const int e = K == 1 ? 8 : (K == 2 ? 12 : 16);
@@ -897,7 +1038,7 @@ bool brick_density_eligible(const sph_ctx *ctx, int dst, const int *srcs, int ns
         return false;
     const ArraySnap &S = ctx->arrays[srcs[0]];
     const ArraySnap &D = ctx->arrays[dst];
-    return S.n > 0 && D.n > 0 && S.b_tmax <= 65535;
+    return S.n > 0 && D.n > 0 && S.b_tmax < 65535;
 }
 
 bool brick_rates_eligible(const sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
@@ -911,7 +1052,7 @@ bool brick_rates_eligible(const sph_ctx *ctx, int dst, const sph_source_term *te
         return false;
     const ArraySnap &S = ctx->arrays[terms[0].src];
     const ArraySnap &D = ctx->arrays[dst];
-    return S.n > 0 && D.n > 0 && S.b_tmax <= 65535;
+    return S.n > 0 && D.n > 0 && S.b_tmax < 65535;
 }
 
 // Density pass (and, with build, the list build) of destination dst among

@@ -736,6 +736,8 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale, boo
         if (want > cap || want < cap / 2) cap = want;
     }
     if (cap_override() > 0) cap = cap_override();
+    // brick lists hold their entries in groups of 8
+    if (brick) cap = (cap + 7) / 8 * 8;
     const int64_t stride = std::max<int64_t>(D.n, 1);
     const int64_t need = stride * cap;
     const bool have = brick ? L.nbr16 != nullptr : L.nbr != nullptr;
@@ -752,7 +754,6 @@ int prepare_list(sph_ctx *ctx, int dst, int src, NbrList **out, bool *stale, boo
         L.entries = need;
         L.stride_cap = stride;
     }
-    if (cap_override() > 0) cap = cap_override();
     L.cap = cap;
     L.stride = stride;
     return SPH_OK;
