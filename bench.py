@@ -333,17 +333,19 @@ def replicas_value(units_per_rank, world, seconds):
     return world * units_per_rank / seconds
 
 
-def _timed_window(integ, cm, steps, flush):
+def _timed_window(integ, cm, steps, flush, stages=False):
     """Time ``steps`` integrator steps with CUDA events on the current
     stream, L2 flushed (outside the events) before each.  Returns the step
-    times (ms), the per-stage times (ms lists), the full builds / light
-    refreshes in the window and the library launches."""
+    times (ms), the per-stage times (ms lists, with ``stages``: CUDA events
+    around every stage, which runs the steps call by call instead of as
+    recorded step graphs), the full builds / light refreshes in the window
+    and the library launches."""
     import torch
     from pysph_gb300 import native
     torch.cuda.synchronize()
     launches0 = native.launch_count()
     builds0 = cm.build_stats()
-    integ.stage_events = []
+    integ.stage_events = [] if stages else None
     step_ms = []
     for _ in range(steps):
         flush.fill_(1.0)
@@ -356,7 +358,7 @@ def _timed_window(integ, cm, steps, flush):
         step_ms.append(a.elapsed_time(b))
     torch.cuda.synchronize()
     launches = native.launch_count() - launches0
-    events = integ.stage_events
+    events = integ.stage_events or []
     integ.stage_events = None
     stage_ms = {}
     for name, a, b in events:
@@ -384,6 +386,8 @@ def _full_rebuild_leg(api, props, steps, warmup, flush, pairs_per_step):
     for _ in range(warmup):
         integ.integrate(DT)
     step_ms, stage_ms, builds, launches = _timed_window(integ, particles.cell_manager, steps, flush)
+    _, stage_ms, _, _ = _timed_window(integ, particles.cell_manager, min(steps, 5), flush,
+                                      stages=True)
     ms = statistics.mean(step_ms)
     return {"value": pairs_per_step / (ms / 1e3), "unit": UNIT, "steps": steps,
             "ms_per_step": ms, "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
@@ -431,10 +435,14 @@ def run_gpu(args):
     torch.cuda.synchronize()
     deferred0 = cm.deferred_stats()
     t_begin = time.monotonic()
-    step_ms, stage_ms, builds, launches = _timed_window(integ, cm, args.steps, flush)
+    step_ms, _, builds, launches = _timed_window(integ, cm, args.steps, flush)
     if pg:
         pg.barrier()
     t_end = time.monotonic()
+    replay_stats = integ.step_stats()
+    # the per-stage breakdown: a few steps call by call with events around
+    # every stage (outside the headline window)
+    eager_ms, stage_ms, _, _ = _timed_window(integ, cm, min(args.steps, 10), flush, stages=True)
     deferred = cm.deferred_stats()
     deferred = (deferred[0] - deferred0[0], deferred[1] - deferred0[1])
     t_total = max_over_ranks(sum(step_ms) / 1e3, pg)
@@ -527,6 +535,8 @@ def run_gpu(args):
         "reference_equivalent": {"value": value * 6.0 / 4.0, "unit": UNIT,
                                  "per_step": "6 K N (SPHRho, PGrad, AV x 2 evaluations)"},
         "stage_ms": {k: statistics.mean(v) for k, v in stage_ms.items()},
+        "step_graphs": replay_stats,
+        "eager_ms_per_step": statistics.mean(eager_ms),
         "nnps_builds": {"timed_full": builds[0], "timed_light": builds[1],
                         "deferred": deferred[0], "deferred_stale": deferred[1],
                         "skin": "list skin %.3g of the search radius" % _skin()},
@@ -1081,6 +1091,81 @@ def _train_step(model, x, t):
     model.adam(1e-4)
 
 
+# ---------------------------------------------------------------------------
+# single small simulations: host-bound call by call, one graph per step
+# ---------------------------------------------------------------------------
+SMALL_METRIC = "steps/s (single small simulations: 2D drop 5k Euler, 2D dam break 20k/80k RK2)"
+
+
+def run_gpu_small(args):
+    """Wall-clock and device time per step of the small single-simulation
+    configurations, their steps replayed as one CUDA graph each (the default
+    below 500 000 particles) and run call by call (PYSPH_GB300_GRAPHS=0).
+    Device time: CUDA events around the timed steps on the stream the steps
+    run on, i.e. the device timeline including any idle gaps the host
+    leaves; device-bound means wall ~ device."""
+    import torch
+
+    import pysph_gb300
+    from pysph_gb300 import native
+    from pysph_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    api = pysph_gb300.api()
+
+    def drop():
+        props = W.elliptical_drop(dx=0.025, c0=100.0)
+        return W.setup_drop(api, props, c0=100.0), 1e-5, len(props["x"])
+
+    def dam(dx, dt):
+        def make():
+            fluid, wall = W.dam_break(dx=dx)
+            return (W.setup_dam_break(api, fluid, wall, dx, W.dam_break_c0()), dt,
+                    len(fluid["x"]) + len(wall["x"]))
+        return make
+
+    cases = [("2D elliptical drop dx=0.025, Euler, c0=100", drop),
+             ("2D dam break dx=0.01 (20k fluid + walls), RK2 dt=2.5e-5", dam(0.01, 2.5e-5)),
+             ("2D dam break dx=0.005 (80k fluid + walls), RK2 dt=1.25e-5", dam(0.005, 1.25e-5))]
+    out = []
+    for name, make in cases:
+        row = {"case": name}
+        for mode in ("graphs", "calls"):
+            os.environ["PYSPH_GB300_GRAPHS"] = "1" if mode == "graphs" else "0"
+            (s, particles), dt, n = make()
+            integ = s.integrator
+            for _ in range(args.warmup + 2):
+                integ.integrate(dt)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            l0 = native.launch_count()
+            t0 = time.perf_counter()
+            a.record()
+            for _ in range(args.steps):
+                integ.integrate(dt)
+            b.record()
+            b.synchronize()
+            wall = (time.perf_counter() - t0) / args.steps * 1e3
+            dev = a.elapsed_time(b) / args.steps
+            row["particles"] = n
+            row[mode] = {"wall_ms_per_step": wall, "device_ms_per_step": dev,
+                         "steps_per_s": 1e3 / wall,
+                         "launches_per_step": (native.launch_count() - l0) / args.steps,
+                         "step_graphs": integ.step_stats()}
+        os.environ.pop("PYSPH_GB300_GRAPHS", None)
+        row["speedup_graphs"] = row["calls"]["wall_ms_per_step"] / row["graphs"]["wall_ms_per_step"]
+        out.append(row)
+    line = {"metric": SMALL_METRIC, "value": out[0]["graphs"]["steps_per_s"], "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out[0]["graphs"]["wall_ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair sums, f64 integration",
+            "data": "synthetic (drop and dam-break lattices)",
+            "config": {"workload": "single small simulations", "cases": [c for c, _ in cases]},
+            "cases": out, "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -1135,7 +1220,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-full-rebuild-leg", action="store_true")
     ap.add_argument("--ref-1m-steps", type=int, default=3)
-    ap.add_argument("--workload", default="cube", choices=["cube", "drops", "closure", "mlp"])
+    ap.add_argument("--workload", default="cube",
+                    choices=["cube", "drops", "closure", "mlp", "small"])
     ap.add_argument("--mlp-n", type=int, default=1 << 20)
     ap.add_argument("--samples", type=int, default=10_000_000)
     ap.add_argument("--epochs", type=int, default=10)
@@ -1148,7 +1234,9 @@ def main():
     ap.add_argument("--drops", type=int, default=256)
     ap.add_argument("--drop-c0", type=float, default=100.0)
     ap.add_argument("--drop-sample", type=int, default=8)
-    ap.add_argument("--drop-error-steps", type=int, default=1000)
+    # the supersonic drops (c0 = 100, |v| up to 150) blow up in FP64 within
+    # ~770 steps for the largest ones: the error is compared at 500
+    ap.add_argument("--drop-error-steps", type=int, default=500)
     ap.add_argument("--drop-error-sample", type=int, default=8)
     args = ap.parse_args()
     if args.steps is None:
@@ -1157,6 +1245,12 @@ def main():
         args.warmup = 3
     if args.workload == "drops":
         (run_reference_drops if args.impl == "reference" else run_gpu_drops)(args)
+    elif args.workload == "small":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the small cases' reference "
+                              "timings are the cube and drops reference arms"}))
+        else:
+            run_gpu_small(args)
     elif args.workload == "mlp":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no network"}))

@@ -208,6 +208,32 @@ int sph_nnps_deferred_stats(sph_ctx *ctx, int64_t *out);
 /* out[0] = full builds, out[1] = light refreshes of this context. */
 int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
 
+/* Step programs (no reference counterpart: the reference advances a
+ * simulation by Python calls per calc and per NumPy update,
+ * solver/integrator.py:432-645).  Between sph_step_begin and sph_step_end
+ * the calls a time step is made of -- sph_nnps_update / sph_nnps_build,
+ * sph_density, sph_rates, sph_tait, sph_const_rates, sph_integrate,
+ * sph_refresh_state -- are recorded (with their pointers and parameters)
+ * instead of run; the other entry points of the context fail with
+ * SPH_ERR_STATE meanwhile.  sph_step_run runs the recorded step nsteps
+ * times: while the neighbour build stays the same (light refreshes), as one
+ * CUDA graph per step in which every launch after a light refresh returns
+ * at once when the refresh found the lists stale; after each step it reads
+ * the step's status (synchronises), reports a jump as the calls do, and
+ * resumes a step whose refresh was stale with a full build and the rest of
+ * the step's calls run eagerly.  Results equal the recorded calls run one by
+ * one.  Runs on the context's stream (on a stream of its own, ordered with
+ * the legacy default stream, when the context's is that stream). */
+typedef struct sph_step sph_step;
+int sph_step_begin(sph_ctx *ctx);
+int sph_step_end(sph_ctx *ctx, sph_step **out);
+int sph_step_run(sph_step *step, int nsteps);
+/* out[0] graph replays, out[1] eager steps, out[2] steps resumed after a
+ * stale refresh, out[3] graph captures, out[4] recorded calls, out[5]
+ * kernels of one replay. */
+int sph_step_stats(sph_step *step, int64_t *out);
+int sph_step_destroy(sph_step *step);
+
 /* Brick-staged pair passes (on = 1, the default): for one source of uniform
  * h without a periodic axis or the variable-h relation, sph_density
  * (SPHRho, + Tait) and sph_rates with the terms PGRAD | AVISC (+ XSPH) run

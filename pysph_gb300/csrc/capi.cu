@@ -141,9 +141,19 @@ int sph_ctx_set_stream(sph_ctx *c, void *stream) {
         if (rc_) return rc_;                    \
     } while (0)
 
+// While a step program records (sph_step_begin), the calls a step is made
+// of are recorded instead of run; the others are refused.
+#define NOT_RECORDING(c, name)                                                          \
+    do {                                                                                \
+        if ((c)->recording)                                                             \
+            return set_error(SPH_ERR_STATE, name ": not recordable in a step program"); \
+    } while (0)
+
 int sph_nnps_build(sph_ctx *c, const sph_array_view *arrays, int narrays, double cell_size,
                    double radius_scale, int subdiv, int check_jump) {
     CHECK_CTX(c);
+    if (c->recording)
+        return record_update(c, true, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
     RESOLVE(c);
     return nnps_build(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
 }
@@ -151,11 +161,16 @@ int sph_nnps_build(sph_ctx *c, const sph_array_view *arrays, int narrays, double
 int sph_nnps_update(sph_ctx *c, const sph_array_view *arrays, int narrays, double cell_size,
                     double radius_scale, int subdiv, int check_jump, int *rebuilt) {
     CHECK_CTX(c);
+    if (c->recording) {
+        if (rebuilt) *rebuilt = 0;
+        return record_update(c, false, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
+    }
     return nnps_update(c, arrays, narrays, cell_size, radius_scale, subdiv, check_jump, rebuilt);
 }
 
 int sph_ctx_set_deferred(sph_ctx *c, int on) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_ctx_set_deferred");
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_deferred: on must be 0 or 1");
     RESOLVE(c);
     c->deferred = on;
@@ -164,6 +179,7 @@ int sph_ctx_set_deferred(sph_ctx *c, int on) {
 
 int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_ctx_set_skin");
     RESOLVE(c);
     if (!(skin_fraction >= 0.0) || skin_fraction > 0.5)
         return set_error(SPH_ERR_ARG, "sph_ctx_set_skin: fraction must be in [0, 0.5]");
@@ -176,6 +192,7 @@ int sph_ctx_set_skin(sph_ctx *c, double skin_fraction) {
 
 int sph_ctx_set_symmetric(sph_ctx *c, int on) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_ctx_set_symmetric");
     RESOLVE(c);
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_symmetric: on must be 0 or 1");
     if (on != c->symmetric) {
@@ -187,6 +204,7 @@ int sph_ctx_set_symmetric(sph_ctx *c, int on) {
 
 int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_ctx_set_periodic");
     RESOLVE(c);
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_periodic: on must be 0 or 1");
     if (on && !(xmax > xmin))
@@ -202,6 +220,7 @@ int sph_ctx_set_periodic(sph_ctx *c, int on, double xmin, double xmax) {
 
 int sph_ctx_set_bricks(sph_ctx *c, int on) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_ctx_set_bricks");
     RESOLVE(c);
     if (on != 0 && on != 1) return set_error(SPH_ERR_ARG, "sph_ctx_set_bricks: on must be 0 or 1");
     if (on != c->bricks_on) {
@@ -220,6 +239,7 @@ int sph_pair_pass_stats(sph_ctx *c, int64_t *out) {
 
 int sph_nnps_stats(sph_ctx *c, int64_t *out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_nnps_stats");
     if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_stats: null out");
     RESOLVE(c);
     out[0] = c->n_full;
@@ -229,6 +249,7 @@ int sph_nnps_stats(sph_ctx *c, int64_t *out) {
 
 int sph_nnps_deferred_stats(sph_ctx *c, int64_t *out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_nnps_deferred_stats");
     if (!out) return set_error(SPH_ERR_ARG, "sph_nnps_deferred_stats: null out");
     RESOLVE(c);
     out[0] = c->n_deferred;
@@ -238,6 +259,7 @@ int sph_nnps_deferred_stats(sph_ctx *c, int64_t *out) {
 
 int sph_nnps_count(sph_ctx *c, int dst, int src, double radius_scale, int64_t *counts) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_nnps_count");
     if (!counts) return set_error(SPH_ERR_ARG, "sph_nnps_count: null counts");
     RESOLVE(c);
     return nnps_count(c, dst, src, radius_scale, counts);
@@ -246,6 +268,7 @@ int sph_nnps_count(sph_ctx *c, int dst, int src, double radius_scale, int64_t *c
 int sph_nnps_fill(sph_ctx *c, int dst, int src, double radius_scale, const int64_t *offsets,
                   int64_t *index) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_nnps_fill");
     if (!offsets || !index) return set_error(SPH_ERR_ARG, "sph_nnps_fill: null output");
     RESOLVE(c);
     return nnps_fill(c, dst, src, radius_scale, offsets, index);
@@ -253,6 +276,7 @@ int sph_nnps_fill(sph_ctx *c, int dst, int src, double radius_scale, const int64
 
 int sph_nbr_lists(sph_ctx *c, int dst, const int *srcs, int nsrc) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_nbr_lists");
     RESOLVE(c);
     return build_lists(c, dst, srcs, nsrc);
 }
@@ -260,6 +284,7 @@ int sph_nbr_lists(sph_ctx *c, int dst, const int *srcs, int nsrc) {
 int sph_refresh_state(sph_ctx *c, int array, const sph_array_view *view) {
     CHECK_CTX(c);
     if (!view) return set_error(SPH_ERR_ARG, "sph_refresh_state: null view");
+    if (c->recording) return record_refresh(c, array, view);
     RESOLVE(c);
     return refresh_state(c, array, view);
 }
@@ -270,6 +295,7 @@ int sph_density(sph_ctx *c, int dst, const int *srcs, int nsrc, const sph_densit
     if (nsrc > 0 && !srcs) return set_error(SPH_ERR_ARG, "sph_density: null sources");
     if (prm && prm->tait && (!p_out || !cs_out))
         return set_error(SPH_ERR_ARG, "sph_density: Tait needs p and cs outputs");
+    if (c->recording) return record_density(c, dst, srcs, nsrc, prm, rho_out, p_out, cs_out);
     return launch_density(c, dst, srcs, nsrc, prm, rho_out, p_out, cs_out);
 }
 
@@ -278,18 +304,21 @@ int sph_rates(sph_ctx *c, int dst, const sph_source_term *terms, int nterms,
               int accumulate) {
     CHECK_CTX(c);
     if (nterms > 0 && !terms) return set_error(SPH_ERR_ARG, "sph_rates: null terms");
+    if (c->recording) return record_rates(c, dst, terms, nterms, prm, acc_out, pos_out, accumulate);
     return launch_rates(c, dst, terms, nterms, prm, acc_out, pos_out, accumulate);
 }
 
 int sph_tait(sph_ctx *c, int64_t n, const double *rho, const int64_t *tag, double co, double ro,
              double gamma, double *p_out, double *cs_out) {
     CHECK_CTX(c);
+    if (c->recording) return record_tait(c, n, rho, tag, co, ro, gamma, p_out, cs_out);
     return launch_tait(c, n, rho, tag, co, ro, gamma, p_out, cs_out);
 }
 
 int sph_adke_smoothing(sph_ctx *c, int64_t n, int64_t nreal, const int64_t *tag,
                        const double *rhop, double h0, double k, double eps, double *h_out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_adke_smoothing");
     return launch_adke_smoothing(c, n, nreal, tag, rhop, h0, k, eps, h_out);
 }
 
@@ -297,6 +326,7 @@ int sph_adke_conduction(sph_ctx *c, int64_t nreal, const int64_t *tag, const dou
                         const double *h, const double *div, double g1, double g2,
                         double *q_out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_adke_conduction");
     return launch_adke_conduction(c, nreal, tag, cs, h, div, g1, g2, q_out);
 }
 
@@ -304,17 +334,20 @@ int sph_const_rates(sph_ctx *c, int kind, int64_t n, const int64_t *tag, const d
                     const double *u, const double *v, const double *w, int nout,
                     double *const *out) {
     CHECK_CTX(c);
+    if (c->recording) return record_const(c, kind, n, tag, g3, u, v, w, nout, out);
     return launch_const_rates(c, kind, n, tag, g3, u, v, w, nout, out);
 }
 
 int sph_integrate(sph_ctx *c, int64_t n, const sph_axpy_line *lines, int nlines) {
     CHECK_CTX(c);
+    if (c->recording) return record_integrate(c, n, lines, nlines);
     RESOLVE(c);
     return launch_integrate(c, n, lines, nlines);
 }
 
 int sph_invariants(sph_ctx *c, const sph_array_view *a, double *out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_invariants");
     RESOLVE(c);
     return invariants(c, a, out);
 }
@@ -392,6 +425,7 @@ int sph_batch_error_word(sph_batch *b, unsigned *out) {
 
 int sph_error_word(sph_ctx *c, unsigned *out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_error_word");
     if (!out) return set_error(SPH_ERR_ARG, "sph_error_word: null out");
     RESOLVE(c);
     unsigned h = 0;
@@ -405,6 +439,7 @@ int sph_error_word(sph_ctx *c, unsigned *out) {
 
 int sph_mean_neighbours(sph_ctx *c, int dst, int src, double *out) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_mean_neighbours");
     if (!out) return set_error(SPH_ERR_ARG, "sph_mean_neighbours: null out");
     RESOLVE(c);
     if (!c->built || dst < 0 || dst >= (int)c->arrays.size())
@@ -441,6 +476,7 @@ static bool mlp_model_ok(const sph_mlp_model *m) {
 int sph_mlp_features(sph_ctx *c, int dst, int src, const sph_mlp_feature_params *prm,
                      uint16_t *out_bf16, float *out_f32) {
     CHECK_CTX(c);
+    NOT_RECORDING(c, "sph_mlp_features");
     return launch_features(c, dst, src, prm, out_bf16, out_f32);
 }
 

@@ -18,8 +18,16 @@ __device__ __forceinline__ bool real_tag(const int64_t *tag, int64_t i) {
 
 // TaitEquation.eval_single (eos_funcs.pyx:105-116) in FP32 through
 // log1p/expm1 of the density excess (relative accuracy kept as rho -> ro).
+// gate: a launch inside a replayed step returns at once when a light
+// refresh of that step found the neighbour lists stale (the host resumes the
+// step after a full build)
+__device__ __forceinline__ bool gated(const unsigned *gate) {
+    return gate != nullptr && __ldg(gate) != 0u;
+}
+
 __global__ void k_tait(int64_t n, const double *rho, const int64_t *tag, float co, float ro,
-                       float gamma, double *p, double *cs) {
+                       float gamma, double *p, double *cs, const unsigned *gate) {
+    if (gated(gate)) return;
     float B = co * co * ro / gamma;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -44,7 +52,8 @@ struct ConstArgs {
 };
 
 // GravityForce (external_force.pyx:39-45) / PositionStepping (position_funcs.pyx:32-60)
-__global__ void k_const(int64_t n, const int64_t *tag, ConstArgs a) {
+__global__ void k_const(int64_t n, const int64_t *tag, ConstArgs a, const unsigned *gate) {
+    if (gated(gate)) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         bool r = real_tag(tag, i);
@@ -62,7 +71,8 @@ struct AxpyArgs {
 
 // integrator.py:472-912: every line is rounded exactly like the NumPy
 // expression it restates (left to right, no FMA contraction).
-__global__ void k_axpy(int64_t n, const __grid_constant__ AxpyArgs a) {
+__global__ void k_axpy(int64_t n, const __grid_constant__ AxpyArgs a, const unsigned *gate) {
+    if (gated(gate)) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         for (int k = 0; k < a.nl; ++k) {
@@ -221,7 +231,7 @@ int launch_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, 
     if (n < 0 || (n > 0 && (!rho || !p || !cs))) return set_error(SPH_ERR_ARG, "tait: bad arguments");
     if (n == 0) return SPH_OK;
     k_tait<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, rho, tag, (float)co, (float)ro,
-                                                                  (float)gamma, p, cs);
+                                                                  (float)gamma, p, cs, ctx->gate);
     count_launch();
     SPH_LAUNCH_CHECK("k_tait");
     return SPH_OK;
@@ -242,7 +252,7 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
     }
     a.vel[0] = u; a.vel[1] = v; a.vel[2] = w;
     if (n == 0) return SPH_OK;
-    k_const<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, tag, a);
+    k_const<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, tag, a, ctx->gate);
     count_launch();
     SPH_LAUNCH_CHECK("k_const");
     return SPH_OK;
@@ -262,7 +272,7 @@ int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nl
             return set_error(SPH_ERR_ARG, "integrate: null array in a line");
     }
     if (n == 0 || nlines == 0) return SPH_OK;
-    k_axpy<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, a);
+    k_axpy<<<grid_blocks(n, kThreads), kThreads, 0, ctx->stream>>>(n, a, ctx->gate);
     count_launch();
     SPH_LAUNCH_CHECK("k_axpy");
     return SPH_OK;

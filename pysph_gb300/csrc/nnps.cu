@@ -327,13 +327,15 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
                         float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
                         double build_h, float stale_thr, const __grid_constant__ ListCaps caps,
-                        unsigned *status) {
+                        unsigned *status, unsigned stale_bit) {
     float dm = 0.f;
     bool jump = false, hch = false;
     // list maxima: written by the passes before this launch
     if (blockIdx.x == 0 && threadIdx.x < caps.n &&
-        (int)status[kListWord0 + threadIdx.x] > caps.cap[threadIdx.x])
+        (int)status[kListWord0 + threadIdx.x] > caps.cap[threadIdx.x]) {
         atomicOr(status + kStaleWord, kStaleLists);
+        if (stale_bit) atomicOr(status + kStaleBitsWord, stale_bit);
+    }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int s = inv[i];
@@ -388,7 +390,10 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         if (lane == 0) {
             if (b > 0.f) atomicMax(status + 1, __float_as_uint(b));
             if (f) atomicOr(status, f);
-            if (f || !(b < stale_thr)) atomicOr(status + kStaleWord, kStaleLists);
+            if (f || !(b < stale_thr)) {
+                atomicOr(status + kStaleWord, kStaleLists);
+                if (stale_bit) atomicOr(status + kStaleBitsWord, stale_bit);
+            }
         }
     }
 }
@@ -863,12 +868,19 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
             (bool)(v.nx || v.ny || v.nz) != A.has_nrm || (v.n > 0 && (!A.pm0 || !A.inv)))
             light = false;
     }
-    if (!light)
+    if (!light) {
+        // a full build needs the host: no step graph for this build
+        if (ctx->capturing) {
+            ctx->capture_failed = true;
+            return SPH_OK;
+        }
         return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);
+    }
 
     cudaStream_t st = ctx->stream;
-    // error word, displacement, stale flag
-    SPH_CUDA(cudaMemsetAsync(ctx->d_status, 0, 3 * sizeof(unsigned), st));
+    // error word, displacement, stale flag (a captured step clears them once,
+    // at its start, so that a stale refresh gates the rest of the step)
+    if (!ctx->capturing) SPH_CUDA(cudaMemsetAsync(ctx->d_status, 0, 3 * sizeof(unsigned), st));
     const double inv_cs_ref = 1.0 / cell_size;
     const float half = 0.5f * ctx->grid.skin;
     const float stale_thr = half * half * (1.f - 1e-4f);
@@ -887,17 +899,22 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         k_light<<<grid_blocks(v.n, kThreads, 64), kThreads, 0, st>>>(
             v, ctx->grid, inv_cs_ref, A.inv, A.key, A.pm0, A.velh,
             A.has_nrm ? A.nrm : nullptr, A.has_nrm ? A.tan : nullptr, A.pm, A.refcell, check_jump,
-            ctx->build_h, stale_thr, caps, ctx->d_status);
+            ctx->build_h, stale_thr, caps, ctx->d_status, ctx->capture_stale_bit);
         caps.n = 0;   // checked once
         A.st_fresh = false;
         count_launch();
         SPH_LAUNCH_CHECK("k_light");
     }
+    for (int a = 0; a < narrays; ++a) ctx->arrays[a].view = arrays[a];
+    if (ctx->capturing) {
+        // the graph publishes the status block once, at the end of the step
+        if (rebuilt) *rebuilt = 0;
+        return SPH_OK;
+    }
     {
         const int rcm = list_maxima_async(ctx);   // with the error word and displacement
         if (rcm) return rcm;
     }
-    for (int a = 0; a < narrays; ++a) ctx->arrays[a].view = arrays[a];
     if (ctx->deferred) {
         SPH_CUDA(cudaEventRecord(ctx->pending_event, st));
         ctx->pending = true;

@@ -764,6 +764,11 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
     bool stale = false;
     int rc = prepare_list(ctx, dst, src, out, &stale);
     if (rc || !stale) return rc;
+    if (ctx->capturing) {
+        // lists are built at the positions of the build, not inside a step graph
+        ctx->capture_failed = true;
+        return SPH_OK;
+    }
     NbrList &L = **out;
     ArraySnap &D = ctx->arrays[dst];
     ArraySnap &S = ctx->arrays[src];
@@ -871,6 +876,10 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
         bool stale = false;
         const int rc = prepare_list(ctx, dst, srcs[0], &L, &stale, true);
         if (rc) return rc;
+        if (stale && ctx->capturing) {
+            ctx->capture_failed = true;
+            return SPH_OK;
+        }
         const bool own = rho != nullptr && rho == D.view.rho &&
                          (!prm->tait || (p == D.view.p && cs == D.view.cs));
         const int rb = brick_density(ctx, dst, srcs[0], *L, stale, true, prm, rho, p, cs,
@@ -894,6 +903,10 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
         bool stale = false;
         const int rc = prepare_list(ctx, dst, srcs[i], &L, &stale);
         if (rc) return rc;
+        if (stale && ctx->capturing) {
+            ctx->capture_failed = true;
+            return SPH_OK;
+        }
         a.s[i] = make_src(ctx->arrays[srcs[i]]);
         a.s[i].nbr = L->nbr;
         a.s[i].ncnt = L->cnt;
@@ -963,6 +976,10 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
         bool stale = false;
         int rc = prepare_list(ctx, dst, terms[0].src, &L, &stale, true);
         if (rc) return rc;
+        if (stale && ctx->capturing) {
+            ctx->capture_failed = true;
+            return SPH_OK;
+        }
         if (stale) {
             // no density pass of this build wrote the list: build it alone
             rc = brick_density(ctx, dst, terms[0].src, *L, true, false, nullptr, nullptr, nullptr,

@@ -33,7 +33,8 @@ constexpr int kPairBlock = 128; // threads per block of the pair kernels
 constexpr int kMaxListSlots = 128;
 // device status block read back with one copy: [0] error word, [1] largest
 // squared displacement (float bits), [2] stale-list flags of the last light
-// refresh, [3] spare, [kListWord0 + i] largest count of list slot i
+// refresh, [3] stale bits of a replayed step, [kListWord0 + i] largest count
+// of list slot i
 constexpr int kListWord0 = 4;
 constexpr int kStatusWords = kListWord0 + kMaxListSlots;
 // [2]: the lists cannot serve the last light refresh (a particle moved by
@@ -41,6 +42,9 @@ constexpr int kStatusWords = kListWord0 + kMaxListSlots;
 // a gated pair pass returns at once
 constexpr unsigned kStaleLists = 1u;
 constexpr int kStaleWord = 2;
+// [3]: in a replayed step, bit u set when the u-th light refresh of the
+// step found the lists stale (the step resumes after the first such one)
+constexpr int kStaleBitsWord = 3;
 
 struct Grid {
     int bx0 = 0, by0 = 0, bz0 = 0; // origin of the dense grid (internal cell coords)
@@ -161,6 +165,8 @@ struct NbrList {
 
 }  // namespace sphgb
 
+struct sph_step;
+
 struct sph_ctx {
     int dim = 3;
     cudaStream_t stream = 0;
@@ -221,6 +227,13 @@ struct sph_ctx {
     unsigned *h_bstats = nullptr;       // mapped mirror
     unsigned *hd_bstats = nullptr;
     long long n_brick_passes = 0;       // pair passes run by the brick kernels
+    // step programs (sph_step_*): calls recorded instead of run, and the
+    // capture of a recorded step into a CUDA graph (every launch gated on
+    // the stale word, no host synchronisation)
+    struct sph_step *recording = nullptr;
+    bool capturing = false;
+    bool capture_failed = false;
+    unsigned capture_stale_bit = 0;     // stale bit of the light refresh being captured
 };
 
 struct sph_batch {
@@ -306,6 +319,20 @@ int launch_const_rates(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, co
 int launch_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
 int invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
 int build_lists(sph_ctx *ctx, int dst, const int *srcs, int nsrc);
+// step programs (program.cu): recording of the calls of one step
+int record_update(sph_ctx *ctx, bool build, const sph_array_view *arrays, int narrays,
+                  double cell_size, double radius_scale, int subdiv, int check_jump);
+int record_density(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
+                   double *rho, double *p, double *cs);
+int record_rates(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
+                 const sph_rates_params *prm, double *const *acc, double *const *pos,
+                 int accumulate);
+int record_tait(sph_ctx *ctx, int64_t n, const double *rho, const int64_t *tag, double co,
+                double ro, double gamma, double *p, double *cs);
+int record_const(sph_ctx *ctx, int kind, int64_t n, const int64_t *tag, const double *g3,
+                 const double *u, const double *v, const double *w, int nout, double *const *out);
+int record_integrate(sph_ctx *ctx, int64_t n, const sph_axpy_line *lines, int nlines);
+int record_refresh(sph_ctx *ctx, int array, const sph_array_view *view);
 // brick-staged pair passes (bricks.cu)
 constexpr int kMaxBrickArrays = 16;
 void brick_geometry(sph_ctx *ctx);

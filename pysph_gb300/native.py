@@ -44,6 +44,7 @@ EXPORTS = (
     "sph_batch_pair_counts", "sph_ctx_set_skin", "sph_nnps_update", "sph_nnps_stats",
     "sph_ctx_set_symmetric", "sph_ctx_set_periodic", "sph_ctx_set_deferred",
     "sph_nnps_deferred_stats", "sph_ctx_set_bricks", "sph_pair_pass_stats",
+    "sph_step_begin", "sph_step_end", "sph_step_run", "sph_step_stats", "sph_step_destroy",
     "sph_mlp_features", "sph_mlp_sync", "sph_mlp_forward", "sph_mlp_backward_scratch",
     "sph_mlp_backward", "sph_mlp_adam", "sph_mlp_apply", "sph_mlp_targets",
 )
@@ -159,6 +160,11 @@ def load_library(build_if_missing=True):
         L.sph_ctx_set_periodic.argtypes = [vp, i32, d, d]
         L.sph_ctx_set_deferred.argtypes = [vp, i32]
         L.sph_ctx_set_bricks.argtypes = [vp, i32]
+        L.sph_step_begin.argtypes = [vp]
+        L.sph_step_end.argtypes = [vp, P(vp)]
+        L.sph_step_run.argtypes = [vp, i32]
+        L.sph_step_stats.argtypes = [vp, P(i64)]
+        L.sph_step_destroy.argtypes = [vp]
         L.sph_pair_pass_stats.argtypes = [vp, P(i64)]
         L.sph_nnps_update.argtypes = [vp, P(ArrayView), i32, d, d, i32, i32, P(i32)]
         L.sph_nnps_stats.argtypes = [vp, P(i64)]

@@ -22,6 +22,7 @@ run of them changes nothing but the order of the FP64 additions (the
 reference adds each calc's ``k*dt`` in turn).  The state update is one FP64
 kernel per array with the rounding of the reference's NumPy expressions.
 """
+import ctypes
 import logging
 
 import torch
@@ -151,6 +152,8 @@ class RatesStage:
         written = integ._written.setdefault(id(self.dest), set())
         fresh = [p for p in self.props if p not in written]
         if fresh and len(fresh) != len(self.props):
+            if getattr(cm, "recording", False):
+                raise RuntimeError("a partly written rate array cannot be recorded")
             for p in fresh:
                 rate[p].zero_()
             fresh = []
@@ -192,6 +195,9 @@ class Integrator:
         # when a list, CUDA events (name, start, end) are recorded around
         # every stage and neighbour build on the current stream
         self.stage_events = None
+        self._replay = None
+        self._steps_done = 0
+        self._saved_count = 0
 
     def set_rupdate_list(self):
         self.rupdate_list = [[] for _ in self.particles.arrays]
@@ -389,6 +395,7 @@ class Integrator:
     def _saved_initial(self):
         """The final update just wrote X0 = X (its lines save the result)."""
         self._x0_versions = {id(dest): dest.version for dest, _ in self._integrated.values()}
+        self._saved_count += 1
 
     def reset_current_arrays(self, calcs=None):
         self._apply("reset", calcs=calcs)
@@ -404,8 +411,60 @@ class Integrator:
         self.eval(calcs)
         self.step(calcs, dt)
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         raise NotImplementedError
+
+    def integrate(self, dt):
+        """One time step.  From the second step on, the step's calls of the
+        C ABI are recorded once into a step program (``sph_step_*``), which
+        then runs each later step as one CUDA graph while the arrays, dt
+        and the stage plan stay as they were (any change, or the learned
+        closure's hooks, or per-stage timing, runs the step call by call
+        and records afresh).  Results are those of the calls run one by
+        one."""
+        if not self.setup_done:
+            self.setup_integrator()
+        rp = self._replay
+        if rp is not None:
+            if rp.usable(self, dt):
+                rp.run()
+                return
+            self._drop_replay()
+        if self._steps_done >= 1 and self._may_record():
+            rp = StepReplay.record(self, dt)
+            if rp is not None:
+                self._replay = rp
+                rp.run()
+                self._steps_done += 1
+                return
+        self._integrate(dt)
+        self._steps_done += 1
+
+    def _may_record(self):
+        from ..tuning import step_graphs
+        n = sum(pa.get_number_of_particles() for pa in self.particles.arrays)
+        if not step_graphs(n) or self.stage_events is not None:
+            return False
+        cm = getattr(self.particles, "cell_manager", None)
+        if cm is None or not torch.cuda.is_available():
+            return False
+        for st in self.stages + [s for p in self._plans.values() for s in p]:
+            # the learned closure's hooks and calcs evaluated on their own
+            # (SPHCalc.sph) run torch operations that a program does not record
+            if isinstance(st, CalcStage) or (isinstance(st, RatesStage) and st.hooks):
+                return False
+        return True
+
+    def _drop_replay(self):
+        if self._replay is not None:
+            self._replay.close()
+            self._replay = None
+
+    def step_stats(self):
+        """Counters of the recorded step (graph replays, eager steps,
+        resumed steps, captures, recorded calls, kernels per replay), or
+        None."""
+        return None if self._replay is None else self._replay.stats()
 
 
 class EulerIntegrator(Integrator):
@@ -415,7 +474,7 @@ class EulerIntegrator(Integrator):
         Integrator.__init__(self, particles, calcs)
         self.nsteps = 1
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         if not self.setup_done:
             self.setup_integrator()
         self.set_initial_arrays()
@@ -433,7 +492,7 @@ class RK2Integrator(Integrator):
         Integrator.__init__(self, particles, calcs)
         self.nsteps = 2
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         if not self.setup_done:
             self.setup_integrator()
         self.set_initial_arrays()
@@ -457,7 +516,7 @@ class RK4Integrator(Integrator):
         Integrator.__init__(self, particles, calcs)
         self.nsteps = 4
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         if not self.setup_done:
             self.setup_integrator()
         self.set_initial_arrays()
@@ -483,7 +542,7 @@ class PredictorCorrectorIntegrator(Integrator):
         Integrator.__init__(self, particles, calcs)
         self.nsteps = 2
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         if not self.setup_done:
             self.setup_integrator()
         self.set_initial_arrays()
@@ -545,7 +604,7 @@ class LeapFrogIntegrator(Integrator):
             lines.append((x, None, x, dest.get_device("_rate1_" + vp), None, c, 1))
         return dest, lines
 
-    def integrate(self, dt):
+    def _integrate(self, dt):
         if not self.setup_done:
             self.setup_integrator()
         dest, corr = self._correction_lines(dt)
@@ -563,3 +622,101 @@ class LeapFrogIntegrator(Integrator):
         self.eval(self.ncalcs)
         self._apply("leapfrog", dt, calcs=self.icalcs)
         self.cstep = 1
+
+
+class StepReplay:
+    """A step recorded as a step program of the C ABI and its replay
+    conditions: the same dt and the same arrays (sizes and device buffers).
+    Values written into the arrays between steps are taken as an eager step
+    takes them: X0 = X for the integrated properties and a neighbour update
+    (or snapshot refresh) of the changed arrays run before the replay."""
+
+    def __init__(self, integ, dt, handle):
+        self.integ = integ
+        self.dt = dt
+        self.handle = handle
+        self.cm = integ.particles.cell_manager
+        self.ctx = self.cm.context()
+        self.signature = self._signature(integ)
+        self.builds_per_step = 0
+
+    @staticmethod
+    def _arrays(integ):
+        return list(integ.particles.arrays)
+
+    @classmethod
+    def _signature(cls, integ):
+        sig = []
+        for pa in cls._arrays(integ):
+            sig.append((id(pa), pa.get_number_of_particles(),
+                        tuple((k, t.data_ptr()) for k, t in sorted(pa.properties.items()))))
+        return tuple(sig)
+
+    @classmethod
+    def record(cls, integ, dt):
+        """Record one step (nothing runs on the device); None when a call of
+        the step cannot be recorded."""
+        from .. import native
+        cm = integ.particles.cell_manager
+        ctx = cm.context()
+        L = native.lib()
+        native.check(L.sph_step_begin(ctx), "sph_step_begin")
+        b0 = cm._build_count
+        s0 = integ._saved_count
+        handle = ctypes.c_void_p()
+        cm.recording = True
+        try:
+            integ._integrate(dt)
+        except Exception:
+            cm.recording = False
+            L.sph_step_end(ctx, ctypes.byref(handle))
+            L.sph_step_destroy(handle)
+            # the recorded calls never ran: the next step updates afresh
+            for pa in integ.particles.arrays:
+                pa.set_dirty(True)
+            cm.is_dirty = True
+            integ._may_record = lambda: False
+            return None
+        cm.recording = False
+        native.check(L.sph_step_end(ctx, ctypes.byref(handle)), "sph_step_end")
+        rp = cls(integ, dt, handle)
+        rp.builds_per_step = cm._build_count - b0
+        # the step's final lines save X0 = X (not the leap-frog's)
+        rp.saves_initial = integ._saved_count != s0
+        rp.recorded = True
+        return rp
+
+    def usable(self, integ, dt):
+        return (dt == self.dt and self.cm.context().value == self.ctx.value
+                and integ.stage_events is None and self._signature(integ) == self.signature)
+
+    def run(self):
+        from .. import native
+        integ, cm = self.integ, self.cm
+        if self.recorded:
+            # the step just recorded: its bookkeeping ran while recording
+            self.recorded = False
+        else:
+            # what the eager step does first when arrays changed since the
+            # last step: X0 = X, and snapshots of changed arrays
+            integ.set_initial_arrays()
+            cm.ensure_current()
+        cm.context()   # the current stream
+        native.check(native.lib().sph_step_run(self.handle, 1), "step")
+        if self.saves_initial:
+            integ._saved_initial()
+        # locators compare the build count with their cached lists
+        cm._build_count += self.builds_per_step
+
+    def stats(self):
+        from .. import native
+        out = (ctypes.c_int64 * 6)()
+        native.check(native.lib().sph_step_stats(self.handle, out), "sph_step_stats")
+        return {"graph_steps": out[0], "eager_steps": out[1], "resumed_steps": out[2],
+                "captures": out[3], "calls": out[4], "kernels_per_replay": out[5]}
+
+    def close(self):
+        from .. import native
+        if self.handle:
+            native.lib().sph_step_destroy(self.handle)
+            self.handle = None

@@ -41,6 +41,25 @@ def brick_passes():
     return True
 
 
+# below this many particles a step is shorter than the host's calls for it,
+# and replaying it as one graph pays; above it the step is device-bound (1 M
+# particles: 1.222 ms per replayed step against 1.214 call by call) and the
+# calls' deferred checks keep host transfers overlapped with the steps
+GRAPH_MAX_PARTICLES = 500_000
+
+
+def step_graphs(nparticles=0):
+    """Whether integrators record their step once and replay it as one CUDA
+    graph per step: PYSPH_GB300_GRAPHS=1 always, 0 never, unset (auto) for
+    simulations of fewer than GRAPH_MAX_PARTICLES particles."""
+    env = os.environ.get("PYSPH_GB300_GRAPHS")
+    if env is not None:
+        if env not in ("0", "1"):
+            raise ValueError("PYSPH_GB300_GRAPHS must be 0 or 1")
+        return env == "1"
+    return nparticles < GRAPH_MAX_PARTICLES
+
+
 # measured defaults: (dimensions with extent) -> subdivision
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
 # neighbour-list entries hold the source slot in 32 - code bits (three
