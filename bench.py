@@ -903,91 +903,112 @@ def run_gpu_closure(args):
     flops = 6.0 * (192 * 128 + 128 * 128 + 128 * 2) * nb * 8192 * args.epochs
     del x, t
 
-    dx, dt, nsteps = 0.005, args.dt, args.closure_steps
+    nsteps = args.closure_steps
     ckpt = max(1, nsteps // 10)
 
-    def fresh():
-        fluid, wall = W.dam_break(dx=dx)
-        return W.setup_dam_break(api, fluid, wall, dx, c0)
+    def errs_of(a, r):
+        d = (a - r).abs()
+        return float((d.max() / r.abs().max()).item()), float((d / r.abs()).max().item())
 
-    def plain_run():
-        s, particles = fresh()
-        fl = particles.arrays[0]
-        for _ in range(3):
-            s.integrator.integrate(dt)
-        torch.cuda.synchronize()
-        refs = []
-        t1 = time.perf_counter()
-        for k in range(1, nsteps + 1):
-            s.integrator.integrate(dt)
-            if k % ckpt == 0:
-                refs.append(fl.get_device("rho").clone())
-        torch.cuda.synchronize()
-        return time.perf_counter() - t1, refs, fl.get_number_of_particles()
+    def deploy(dx, dt, column):
+        """Plain, surrogate-only and guarded runs of one dam break."""
+        def fresh():
+            fluid, wall = W.dam_break(dx=dx, column=column)
+            return W.setup_dam_break(api, fluid, wall, dx, c0)
 
-    def rel_err(a, r):
-        return float(((a - r).abs() / r).max().item())
-
-    # The comparison runs rebuild the neighbour lists at every update (no
-    # list skin): the FP32 summation order then depends on the state alone,
-    # so a guarded window that falls back reproduces the plain run bit for
-    # bit.  With a skin the order follows the rebuild history, and this
-    # free-surface flow amplifies the rounding differences of two equally
-    # exact orders to O(0.1) in the maximum relative density difference
-    # within 1000 steps (``plain_noise_floor``).
-    skin_env = os.environ.get("PYSPH_GB300_SKIN")
-    os.environ["PYSPH_GB300_SKIN"] = "0.03"
-    _, refs_skin, _ = plain_run()
-    os.environ["PYSPH_GB300_SKIN"] = "0"
-    t_plain, refs, n = plain_run()
-    log("plain: %.3f s for %d steps" % (t_plain, nsteps))
-    noise_floor = [rel_err(a, r) for a, r in zip(refs_skin, refs)]
-
-    def surrogate_run(k=None):
-        s, particles = fresh()
-        fl = particles.arrays[0]
-        for _ in range(3):
-            s.integrator.integrate(dt)
-        closure = L.LearnedClosure(s.integrator, fl, model, norm)
-        errs = []
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        runner = None
-        try:
-            if k is None:
-                for j in range(1, nsteps + 1):
-                    s.integrator.integrate(dt)
-                    if j % ckpt == 0:
-                        r = refs[j // ckpt - 1]
-                        errs.append(float(((fl.get_device("rho") - r).abs() / r).max().item()))
-            else:
-                runner = L.GuardedRunner(s, particles, closure, k=k, tol=args.tol)
-                done = 0
-                while done < nsteps:
-                    runner.window(dt)
-                    done += k
-                    if done % ckpt == 0:
-                        r = refs[done // ckpt - 1]
-                        errs.append(float(((fl.get_device("rho") - r).abs() / r).max().item()))
+        def plain_run():
+            s, particles = fresh()
+            fl = particles.arrays[0]
+            for _ in range(3):
+                s.integrator.integrate(dt)
             torch.cuda.synchronize()
-            el = time.perf_counter() - t1
-            out = {"steps_per_s": nsteps / el, "max_rel_density_error": max(errs) if errs else None,
-                   "rel_density_error_at_checkpoints": errs}
-        except RuntimeError as e:
-            out = {"failed": str(e)[:120]}
-        if runner is not None:
-            out.update(windows=runner.windows, checks=runner.checks, fallbacks=runner.fallbacks)
-        return out
+            refs = []
+            t1 = time.perf_counter()
+            for k in range(1, nsteps + 1):
+                s.integrator.integrate(dt)
+                if k % ckpt == 0:
+                    refs.append(fl.get_device("rho").clone())
+            torch.cuda.synchronize()
+            return time.perf_counter() - t1, refs, fl.get_number_of_particles()
 
-    res = {"surrogate_only": surrogate_run(None)}
-    for k in (5, 10, 20):
-        res["guarded_k%d" % k] = surrogate_run(k)
-    if skin_env is None:
-        os.environ.pop("PYSPH_GB300_SKIN", None)
-    else:
-        os.environ["PYSPH_GB300_SKIN"] = skin_env
-        log("k=%d: %s" % (k, res["guarded_k%d" % k]))
-    plain_sps = nsteps / t_plain
+        # The comparison runs rebuild the neighbour lists at every update
+        # (no list skin): the FP32 summation order then depends on the state
+        # alone, so a guarded window that falls back reproduces the plain
+        # run bit for bit.  With a skin the order follows the rebuild
+        # history; the difference of the two plain runs is the noise floor
+        # of each metric in this free-surface flow.
+        skin_env = os.environ.get("PYSPH_GB300_SKIN")
+        os.environ["PYSPH_GB300_SKIN"] = "0.03"
+        _, refs_skin, _ = plain_run()
+        os.environ["PYSPH_GB300_SKIN"] = "0"
+        t_plain, refs, n = plain_run()
+        log("dx %g plain: %.3f s for %d steps" % (dx, t_plain, nsteps))
+        floor = [errs_of(a, r) for a, r in zip(refs_skin, refs)]
+
+        def surrogate_run(k=None):
+            s, particles = fresh()
+            fl = particles.arrays[0]
+            for _ in range(3):
+                s.integrator.integrate(dt)
+            closure = L.LearnedClosure(s.integrator, fl, model, norm)
+            errs = []
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            runner = None
+            try:
+                if k is None:
+                    for j in range(1, nsteps + 1):
+                        s.integrator.integrate(dt)
+                        if j % ckpt == 0:
+                            errs.append(errs_of(fl.get_device("rho"), refs[j // ckpt - 1]))
+                else:
+                    runner = L.GuardedRunner(s, particles, closure, k=k, tol=args.tol)
+                    done = 0
+                    while done < nsteps:
+                        runner.window(dt)
+                        done += k
+                        if done % ckpt == 0:
+                            errs.append(errs_of(fl.get_device("rho"), refs[done // ckpt - 1]))
+                torch.cuda.synchronize()
+                el = time.perf_counter() - t1
+                out = {"steps_per_s": nsteps / el, "vs_plain": (nsteps / el) / (nsteps / t_plain),
+                       "max_normwise_density_error": max(e[0] for e in errs) if errs else None,
+                       "max_relative_density_error": max(e[1] for e in errs) if errs else None,
+                       "normwise_at_checkpoints": [e[0] for e in errs],
+                       "max_relative_at_checkpoints": [e[1] for e in errs]}
+            except RuntimeError as e:
+                out = {"failed": str(e)[:120]}
+            if runner is not None:
+                out["guard"] = runner.stats()
+            closure.detach()
+            return out
+
+        res = {"surrogate_only": surrogate_run(None)}
+        for k in (5, 10, 20):
+            res["guarded_k%d" % k] = surrogate_run(k)
+            log("dx %g k=%d: %s" % (dx, k, {q: v for q, v in res["guarded_k%d" % k].items()
+                                            if not q.endswith("checkpoints")}))
+        if skin_env is None:
+            os.environ.pop("PYSPH_GB300_SKIN", None)
+        else:
+            os.environ["PYSPH_GB300_SKIN"] = skin_env
+        return {"dx": dx, "dt": dt, "column": list(column), "fluid_particles": n,
+                "plain_steps_per_s": nsteps / t_plain,
+                "plain_noise_floor": {
+                    "what": "density difference between the plain run with and without a "
+                            "neighbour-list skin (two exact summation orders)",
+                    "normwise_at_checkpoints": [f[0] for f in floor],
+                    "max_relative_at_checkpoints": [f[1] for f in floor]},
+                "closure": res}
+
+    # cross-resolution (trained at dx = 0.01, deployed at dx = 0.005, the
+    # 80,000-particle case) and in-distribution (trained and deployed at
+    # dx = 0.01; the column's aspect ratio 0.5 lies inside the training
+    # range but is not one of the training runs)
+    cross = deploy(0.005, args.dt, (1.0, 2.0))
+    indist = deploy(0.01, args.train_dt, (1.0, 2.0))
+    plain_sps = cross["plain_steps_per_s"]
+    n, dx, dt = cross["fluid_particles"], cross["dx"], cross["dt"]
     line = {
         "metric": CLOSURE_METRIC, "value": plain_sps, "unit": "steps/s", "n_gpus": 1,
         "steps": nsteps, "warmup": 3, "higher_is_better": True, "scaling": "weak",
@@ -996,13 +1017,12 @@ def run_gpu_closure(args):
         "config": {"workload": "2D dam break, dx=%g, %d fluid particles, RK2 dt=%g; closure "
                                "trained on dx=0.01 runs at aspect ratios %s" % (
                                    dx, n, dt, ["%.3f" % a for a in aspects]),
-                   "tolerance": args.tol, "train_steps": args.train_steps, "every": args.every,
+                   "tolerance": args.tol, "tolerance_metric": "normwise max|d rho|/max|rho|",
+                   "train_steps": args.train_steps, "every": args.every,
                    "lists": "rebuilt at every update (no skin) in the timed comparison runs"},
         "plain_steps_per_s": plain_sps,
-        "plain_noise_floor": {"what": "max relative density difference between the plain run with "
-                                      "and without a neighbour-list skin (two exact summation orders)",
-                              "at_checkpoints": noise_floor},
-        "closure": res,
+        "cross_resolution": cross,
+        "in_distribution": indist,
         "training": {"samples": int(nb * 8192), "epochs": args.epochs, "loss_first": losses[0],
                      "loss_last": losses[-1], "seconds": t_train, "data_seconds": t_data,
                      "tflops_fwd_bwd": flops / t_train / 1e12},

@@ -553,11 +553,23 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
         int c = 0;
         if (real) {
             if (BUILD) {
-                uint16_t *out = A.nbr + ((size_t)dbase * ng_cap + d) * 8;
-                const size_t gstride = (size_t)D * 8;
+                // entries collected eight at a time in a 128-bit shift
+                // register (the newest enters at the top) and written as
+                // one 16-byte store per group
+                uint4 *out = reinterpret_cast<uint4 *>(A.nbr) + (size_t)dbase * ng_cap + d;
+                uint4 grp = make_uint4(0, 0, 0, 0);
+                auto push = [&](unsigned t) {
+                    grp.x = __funnelshift_r(grp.x, grp.y, 16);
+                    grp.y = __funnelshift_r(grp.y, grp.z, 16);
+                    grp.z = __funnelshift_r(grp.z, grp.w, 16);
+                    grp.w = (grp.w >> 16) | (t << 16);
+                };
                 brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, scell, q,
                     [&](int t, float rx, float ry, float rz, bool hit) {
-                        if (c < cap) out[(size_t)(c >> 3) * gstride + (c & 7)] = (uint16_t)t;
+                        if (c < cap) {
+                            push((unsigned)t);
+                            if ((c & 7) == 7) out[(size_t)(c >> 3) * D] = grp;
+                        }
                         ++c;
                         if (!hit) return;
                         const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
@@ -565,8 +577,10 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
                         rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
                     });
                 // pad the last group with the zero record
-                for (int k = c; k < cap && (k & 7); ++k)
-                    out[(size_t)(k >> 3) * gstride + (k & 7)] = (uint16_t)T;
+                if (c < cap && (c & 7)) {
+                    for (int k = c; k & 7; ++k) push((unsigned)T);
+                    out[(size_t)(c >> 3) * D] = grp;
+                }
             } else {
                 // stream the groups of 8 entries, two groups requested ahead
                 c = A.cnt[dbase + d];

@@ -16,6 +16,7 @@
 // step's calls eagerly -- with results identical to the eager step.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -77,6 +78,13 @@ struct sph_step {
     // with the default stream's work
     cudaStream_t stream = nullptr;
     long long n_graph = 0, n_eager = 0, n_resumed = 0, n_captures = 0;
+    // capture back-off: a flow whose lists go stale within a step or two of
+    // every full build spends a capture per build for no replay; after a
+    // graph that never ran a whole step the next 1, 2, 4 .. 64 capture
+    // opportunities are skipped (reset by a graph that ran two steps)
+    int lifetime = 0;              // whole-step replays of the current graph
+    bool judged = true;            // the last graph's lifetime was taken into account
+    int backoff = 0, skip = 0;
 };
 
 namespace sphgb {
@@ -250,6 +258,7 @@ int replay(sph_step *s) {
     if (!bits) {
         ctx->n_light += s->updates;
         s->n_graph += 1;
+        s->lifetime += 1;
         return SPH_OK;
     }
     // the first stale light refresh: a full build in its place, then the
@@ -428,8 +437,22 @@ int run_steps(sph_step *s, int nsteps) {
         if (ctx->built && !ctx->pending && s->settled && s->graph_build != ctx->build_id &&
             s->attempt_build != ctx->build_id && !s->ops.empty()) {
             s->attempt_build = ctx->build_id;
-            rc = capture(s);
-            if (rc) return rc;
+            if (!s->judged) {
+                s->judged = true;
+                if (s->lifetime == 0) s->backoff = std::min(64, std::max(1, 2 * s->backoff));
+                else if (s->lifetime >= 2) s->backoff = 0;
+                s->skip = s->backoff;
+            }
+            if (s->skip > 0) {
+                --s->skip;
+            } else {
+                rc = capture(s);
+                if (rc) return rc;
+                if (s->exec) {
+                    s->judged = false;
+                    s->lifetime = 0;
+                }
+            }
         }
         const long long full0 = ctx->n_full;
         if (s->exec && s->graph_build == ctx->build_id && !ctx->pending) {

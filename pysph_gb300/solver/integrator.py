@@ -448,12 +448,16 @@ class Integrator:
         cm = getattr(self.particles, "cell_manager", None)
         if cm is None or not torch.cuda.is_available():
             return False
+        return not self._unrecordable_stages()
+
+    def _unrecordable_stages(self):
+        """Whether a stage runs work a step program does not record: the
+        learned closure's hooks and calcs evaluated on their own
+        (SPHCalc.sph) run torch operations."""
         for st in self.stages + [s for p in self._plans.values() for s in p]:
-            # the learned closure's hooks and calcs evaluated on their own
-            # (SPHCalc.sph) run torch operations that a program does not record
             if isinstance(st, CalcStage) or (isinstance(st, RatesStage) and st.hooks):
-                return False
-        return True
+                return True
+        return False
 
     def _drop_replay(self):
         if self._replay is not None:
@@ -687,8 +691,11 @@ class StepReplay:
         return rp
 
     def usable(self, integ, dt):
+        # hooks attached after the recording (a learned closure) change the
+        # step: it runs call by call again
         return (dt == self.dt and self.cm.context().value == self.ctx.value
-                and integ.stage_events is None and self._signature(integ) == self.signature)
+                and integ.stage_events is None and self._signature(integ) == self.signature
+                and not integ._unrecordable_stages())
 
     def run(self):
         from .. import native

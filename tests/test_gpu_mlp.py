@@ -211,6 +211,7 @@ def test_guarded_runner_restores_exactly():
     runner.window(1e-4)
     runner.window(1e-4)
     assert runner.checks == 2 and runner.max_err == 0.0 and runner.fallbacks == 0
+    assert runner.kept == 2 and runner.stats()["fallback_rate"] == 0.0
 
 
 def test_trained_network_beats_no_network():

@@ -157,3 +157,43 @@ def test_locators_see_replayed_steps(monkeypatch):
     off, idx = oracle.neighbors(host, host, particles.cell_manager.cell_size, same=True)
     goff, gidx = loc.neighbour_csr()
     assert np.array_equal(goff, off) and np.array_equal(gidx, idx)
+
+
+def test_hooks_attached_after_recording_run_every_step(monkeypatch):
+    """A rates hook (the learned closure's interface) attached after the
+    step was recorded is called at every later step: the recorded step is
+    not replayed while hooks are attached, and is recorded afresh once they
+    are gone."""
+    _need_gpu()
+    monkeypatch.setenv("PYSPH_GB300_GRAPHS", "1")
+    props = W.cube_lattice(8000, seed=36)
+    s, particles = W.setup_cube(API, props)
+    integ = s.integrator
+    for _ in range(4):
+        integ.integrate(1e-4)
+    assert integ.step_stats() is not None
+
+    class Counter:
+        calls = 0
+
+        def before_rates(self, integ, stage, terms):
+            Counter.calls += 1
+            return terms
+
+        def after_rates(self, integ, stage, acc):
+            pass
+
+    stage = next(st for st in integ.stages if getattr(st, "hooks", None) is not None)
+    hook = Counter()
+    stage.hooks.append(hook)
+    for _ in range(3):
+        before = Counter.calls
+        integ.integrate(1e-4)
+        assert Counter.calls > before
+    assert integ.step_stats() is None
+    stage.hooks.remove(hook)
+    done = Counter.calls
+    for _ in range(3):
+        integ.integrate(1e-4)
+    assert Counter.calls == done
+    assert integ.step_stats() is not None
