@@ -57,17 +57,19 @@ STEP_ALG_BYTES = 694.0
 PAIR_FLOPS = {"RatesStage": 72.0, "DensityStage": 24.0, "ListStage": 12.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per particle per launch (dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture of the 1M-particle lattice, list-streaming passes); the
-# traffic grows with the particle count, so it is scaled by n
-NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 388.0, "RatesStage": 436.0}
+# of one ncu capture of the 1M-particle lattice, brick-staged passes at cell
+# subdivision 2); the traffic grows with the particle count, so it is scaled
+# by n
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 222.3, "RatesStage": 285.5}
 # The unit that bounds each pair kernel in the same capture, as a fraction of
-# that unit's peak: the rates pass is bound by the L1 data pipe that feeds its
-# neighbour gathers, the density pass by instruction issue
+# that unit's peak: the rates pass is bound by the L1 / shared-memory pipe
+# that serves its staged-record reads (and their latency), the density pass
+# by instruction issue
 NCU_LIMITER = {
-    "RatesStage": {"kernel": "k_rates", "unit": "L1 data-pipe wavefronts", "frac": 0.726,
-                   "issue_frac": 0.671, "dram_frac": 0.158},
-    "DensityStage": {"kernel": "k_density", "unit": "instruction issue", "frac": 0.724,
-                     "l1_frac": 0.490, "dram_frac": 0.254},
+    "RatesStage": {"kernel": "k_brates", "unit": "L1 / shared-memory pipe", "frac": 0.795,
+                   "issue_frac": 0.579, "dram_frac": 0.132},
+    "DensityStage": {"kernel": "k_bdensity", "unit": "instruction issue", "frac": 0.646,
+                     "l1_frac": 0.603, "dram_frac": 0.179},
 }
 
 
@@ -557,8 +559,9 @@ def run_gpu(args):
                      "traffic_source": "ncu capture at 1M particles, scaled by n",
                      "peak_kind": peak_kind,
                      "alg_bytes_per_particle": ALG_BYTES[dom],
-                     "note": "pair kernels bound by issue (density) and the L1 data pipe "
-                             "(rates gathers), not HBM; fp32 context in fp32_context",
+                     "note": "brick-staged pair kernels bound by issue (density) and the "
+                             "L1 / shared-memory pipe (rates: staged-record reads), not HBM; "
+                             "fp32 context in fp32_context",
                      "limiter": dict(NCU_LIMITER.get(dom, {}),
                                      source="ncu --set full capture at 1M particles")},
         "fp32_context": {"kernel": dom, "achieved_tflops": flops,
@@ -681,6 +684,7 @@ def run_gpu_drops(args):
     recipe = dict(dim=2, dt=DROPS_DT, co=args.drop_c0)
     best, tune = tuning.autotune_batch(drops, candidates=(1, 2, 3), steps=5, **recipe)
     batch = SimulationBatch(drops, subdiv=best, **recipe)
+    stats0 = batch.stats()
     st = batch.stream()
     batch.step(args.warmup)
     pairs = batch.pair_counts()
@@ -758,7 +762,12 @@ def run_gpu_drops(args):
                    "instances": len(drops), "particles": n,
                    "min_particles": min(len(d["x"]) for d in drops),
                    "max_particles": max(len(d["x"]) for d in drops),
-                   "subdivision": best, "autotune_ms_per_step": tune,
+                   "subdivision": {str(k): int(sum(1 for v in best if v == k)) for k in (1, 2, 3)},
+                   "autotune": tune,
+                   "regions": {"margin": 0.25, "cells_at_setup": stats0["cells"],
+                               "cells_now": batch.stats()["cells"],
+                               "regrids": batch.stats()["regrids"],
+                               "pair_launch_groups": stats0["groups"]},
                    "cache": "L2 flushed between timed steps (256 MiB write outside the events)",
                    "launch": "one CUDA graph per step"},
         "pair_interactions_per_s": pairs_per_step * steps / t_total,

@@ -221,8 +221,11 @@ int sph_nnps_stats(sph_ctx *ctx, int64_t *out);
  * at once when the refresh found the lists stale; after each step it reads
  * the step's status (synchronises), reports a jump as the calls do, and
  * resumes a step whose refresh was stale with a full build and the rest of
- * the step's calls run eagerly.  Results equal the recorded calls run one by
- * one.  Runs on the context's stream (on a stream of its own, ordered with
+ * the step's calls run eagerly.  A graph is captured once per build, after a
+ * step that needed no full build; after a graph that never ran a whole step
+ * the next 1, 2, 4 .. 64 capture chances are skipped (the flow's lists go
+ * stale too soon for a graph to pay).  Results equal the recorded calls run
+ * one by one.  Runs on the context's stream (on a stream of its own, ordered with
  * the legacy default stream, when the context's is that stream). */
 typedef struct sph_step sph_step;
 int sph_step_begin(sph_ctx *ctx);
@@ -332,17 +335,20 @@ int sph_invariants_noalloc(const sph_array_view *a, double *out, void *stream);
  * operation recipe -- SPHRho (+Tait) of each instance on itself, one set of
  * rate terms among its own particles, gravity / position stepping, Euler or
  * RK2 -- and their particles are concatenated in one set of arrays.  Every
- * instance gets its own dense grid, fixed at set-up over [lo, hi] with a
- * margin, so a time step needs no host synchronisation and no allocation:
- * the step is captured once into a CUDA graph and replayed.
+ * instance gets its own dense grid (its own cell size and subdivision) over
+ * a region around its particles, so a time step needs no host
+ * synchronisation and no allocation: the step is captured into a CUDA graph
+ * and replayed; the regions follow the instances as they deform.
  * --------------------------------------------------------------------- */
 typedef struct sph_batch sph_batch;
 
 typedef struct {
     int64_t offset, n;    /* particle range of the instance (instances tile [0, n) in order) */
     double cell_size;     /* reference cell size: radius_scale * max h of the instance */
-    double lo[3], hi[3];  /* region the instance's particles may occupy */
+    double lo[3], hi[3];  /* region the instance's particles may occupy at set-up */
     int uniform_h;        /* 1 if every particle of the instance has the same h */
+    int subdiv;           /* grid cells per reference cell of this instance, 1..3
+                             (0: the recipe's) */
 } sph_batch_instance;
 
 typedef struct {
@@ -355,6 +361,11 @@ typedef struct {
     sph_density_params density;  /* SPHRho (+ Tait when density.tait) */
     sph_source_term term;        /* rate terms among an instance's particles (src unused) */
     sph_rates_params rates;      /* gravity and position stepping */
+    double margin;        /* > 0: when a particle leaves its instance's region the
+                             step is undone, every region is re-derived from the
+                             current extent e as [lo - m e - 4 c, hi + m e + 4 c]
+                             (c the instance's reference cell) and the step is
+                             repeated; 0: leaving the region is an error */
 } sph_batch_recipe;
 
 int sph_batch_create(sph_batch **out);
@@ -363,9 +374,15 @@ int sph_batch_destroy(sph_batch *b);
  * (synchronises).  all: the concatenated particle arrays (device). */
 int sph_batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instance *inst,
                     int ninst, const sph_batch_recipe *recipe);
-/* Advance every instance by nsteps time steps on the batch's own stream
- * (asynchronous).  use_graph: capture the step into a CUDA graph on the
- * first call and replay it. */
+/* Advance every instance by nsteps time steps on the batch's own stream.
+ * use_graph: capture the step into a CUDA graph on the first call (and after
+ * the regions change) and replay it.  Every launch of a step that writes
+ * the state is gated on the error word: when a particle leaves its
+ * instance's region the step stops there, an RK2 step returns to the state
+ * it started from, the regions are re-derived from the current extents
+ * (recipe.margin) and the step is repeated.  Synchronises once at the end
+ * (and once per re-derivation).  A jump leaves the state at the start of
+ * the failing step and the error word set. */
 int sph_batch_step(sph_batch *b, int nsteps, int use_graph);
 /* Wait for the batch's stream. */
 int sph_batch_sync(sph_batch *b);
@@ -373,6 +390,10 @@ int sph_batch_sync(sph_batch *b);
 int sph_batch_stream(sph_batch *b, void **out);
 /* Read and clear the batch's device error word (SPH_EFLAG_*; synchronises). */
 int sph_batch_error_word(sph_batch *b, uint32_t *out);
+/* out[0] regions re-derived so far, out[1] cells of the current grids,
+ * out[2] steps completed, out[3] groups of instances of equal subdivision
+ * (one pair launch each).  No reference counterpart. */
+int sph_batch_stats(sph_batch *b, int64_t *out);
 /* Neighbour counts (incl. self) of the batch's last evaluation, summed per
  * instance into out[ninst] (synchronises).  Used for pair-interaction
  * counts; the reference has no batch, its per-array counterpart is

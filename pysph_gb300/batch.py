@@ -8,9 +8,12 @@ artificial viscosity, XSPH), gravity, position stepping, Euler or RK2 -- and
 advances all of them with one fixed sequence of launches per step, captured
 in a CUDA graph (``sph_batch_*`` in ``include/pysph_gb300.h``).
 
-Each instance keeps its own smoothing length and cell size (its own dense
-grid, fixed over a region around its initial extent), so instances of very
-different resolution share the launches without sharing cells.
+Each instance keeps its own smoothing length, cell size and cell
+subdivision (its own dense grid over a region around its particles), so
+instances of very different resolution share the launches without sharing
+cells.  The regions follow the instances: a step in which a particle leaves
+its instance's region is undone on the device and repeated on regions
+re-derived from the current extents (``margin``).
 """
 import ctypes
 
@@ -28,12 +31,18 @@ class SimulationBatch:
     ``get_particle_array``).  Physics: SPHRho, Tait(co, ro, gamma), then
     the rate terms named by ``terms`` (subset of pgrad, avisc, xsph) with
     ``alpha``, ``beta``, ``eps``, optional ``gravity`` and position stepping,
-    integrated with ``integrator`` ('euler' or 'rk2') at ``dt``."""
+    integrated with ``integrator`` ('euler' or 'rk2') at ``dt``.
+
+    ``subdiv``: the cell subdivision (1..3), one for all instances or a
+    sequence with one per instance (``tuning.autotune_batch`` chooses them);
+    ``margin``: the regions are the instances' extents grown by ``margin``
+    times the extent plus four reference cells on every side (0: fixed
+    regions, leaving one is an error)."""
 
     def __init__(self, instances, dim=2, dt=1e-5, co=100.0, ro=1.0, gamma=7.0,
                  terms=("pgrad", "avisc", "xsph"), alpha=0.01, beta=0.0, eps=0.5,
                  gravity=None, step_positions=True, integrator="euler", radius_scale=2.0,
-                 margin=1.0, subdiv=None, list_cap=0, use_graph=True):
+                 margin=0.25, subdiv=None, list_cap=0, use_graph=True):
         if not instances:
             raise ValueError("a batch needs at least one instance")
         if not torch.cuda.is_available():
@@ -66,6 +75,13 @@ class SimulationBatch:
         self._view = view
 
         ninst = len(instances)
+        from .tuning import DEFAULT_SUBDIVISION
+        if subdiv is None:
+            subdiv = DEFAULT_SUBDIVISION[self.dim]
+        per_inst = [int(subdiv)] * ninst if np.isscalar(subdiv) else [int(v) for v in subdiv]
+        if len(per_inst) != ninst or any(v not in (1, 2, 3) for v in per_inst):
+            raise ValueError("subdiv: 1, 2 or 3, or one such value per instance")
+        self.subdiv = per_inst
         inst = (native.BatchInstance * ninst)()
         for k in range(ninst):
             a, b = int(self.offsets[k]), int(self.offsets[k + 1])
@@ -74,6 +90,7 @@ class SimulationBatch:
             inst[k].n = b - a
             inst[k].cell_size = radius_scale * float(h.max())
             inst[k].uniform_h = int(h.min() == h.max())
+            inst[k].subdiv = per_inst[k]
             for d, c in enumerate(("x", "y", "z")):
                 lo, hi = float(host[c][a:b].min()), float(host[c][a:b].max())
                 ext = hi - lo
@@ -88,10 +105,8 @@ class SimulationBatch:
                       "xsph": native.TERM_XSPH}[t]
         rec = native.BatchRecipe()
         rec.dim = self.dim
-        if subdiv is None:
-            from .tuning import DEFAULT_SUBDIVISION
-            subdiv = DEFAULT_SUBDIVISION[self.dim]
-        rec.subdiv = int(subdiv)
+        rec.subdiv = per_inst[0]
+        rec.margin = float(margin)
         rec.scheme = {"euler": 0, "rk2": 1}[integrator]
         rec.list_cap = int(list_cap)
         rec.radius_scale = radius_scale
@@ -149,6 +164,13 @@ class SimulationBatch:
         if check:
             self.check()
 
+    def stats(self):
+        """Regions re-derived so far, cells of the current grids, steps
+        completed, groups of equal subdivision."""
+        out = (ctypes.c_int64 * 4)()
+        native.check(native.lib().sph_batch_stats(self._b, out), "sph_batch_stats")
+        return {"regrids": out[0], "cells": out[1], "steps": out[2], "groups": out[3]}
+
     def stream(self):
         """The batch's CUDA stream as a torch stream (for events)."""
         h = ctypes.c_void_p()
@@ -170,7 +192,7 @@ class SimulationBatch:
         if w.value & native.SPH_EFLAG_JUMP:
             raise RuntimeError("Particle moved by more than one cell width")
         if w.value & native.SPH_EFLAG_BOX:
-            raise RuntimeError("a particle left its instance's grid region (raise margin)")
+            raise RuntimeError("a particle left its instance's grid region (margin 0)")
 
     def set(self, **props):
         """Overwrite whole concatenated properties (all instances, in

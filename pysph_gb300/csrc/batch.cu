@@ -98,7 +98,157 @@ __global__ void k_breorder(sph_array_view a, const Grid *grids, const int *inst_
     }
 }
 
+// Bounding box of every instance's current positions (instance k owns the
+// original indices [off[k], off[k + 1])), one block per instance.
+__global__ void k_inst_box(sph_array_view a, const int64_t *off, double *box) {
+    const int k = blockIdx.x;
+    const int64_t i0 = off[k], i1 = off[k + 1];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const double p[3] = {ld0(a.x, i), ld0(a.y, i), ld0(a.z, i)};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], p[d]);
+            hi[d] = fmax(hi[d], p[d]);
+        }
+    }
+    __shared__ double red[6][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+        if (lane == 0) {
+            red[d][wid] = lo[d];
+            red[3 + d][wid] = hi[d];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int q = threadIdx.x;
+        double v = red[q][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            v = q < 3 ? fmin(v, red[q][w]) : fmax(v, red[q][w]);
+        box[6 * k + q] = v;
+    }
+}
+
+// Count of the steps that completed (a step whose launches were gated off
+// by the error word is not counted).
+__global__ void k_step_done(const unsigned *err, unsigned long long *steps) {
+    if (*err == 0u) *steps += 1ull;
+}
+
 }  // namespace
+
+// Lay out the per-instance grids over the regions [lo, hi] (3 doubles per
+// instance each): cell size from the instance's own reference cell and
+// subdivision, the cells of the instances of subdivision 1, then 2, then 3
+// one after another in the shared cell table (so the sorted slots come in
+// the same groups), the cell table (re)allocated when it grows.
+int batch_place(sph_batch *b, const double *lo, const double *hi) {
+    const int ninst = b->ninst;
+    b->h_grids.assign(ninst, Grid());
+    b->groups.clear();
+    int64_t cells = 0, slot = 0;
+    for (int K = 1; K <= 3; ++K) {
+        BatchGroup grp;
+        grp.K = K;
+        grp.s0 = slot;
+        for (int k = 0; k < ninst; ++k) {
+            if (b->inst_subdiv[k] != K) continue;
+            Grid &g = b->h_grids[k];
+            const double *l = lo + 3 * k, *h = hi + 3 * k;
+            g.cs = b->inst_cell[k] / K;
+            g.inv_cs = 1.0 / g.cs;
+            g.cs_f = (float)g.cs;
+            g.radius_scale = b->rec.radius_scale;
+            g.kx = K;
+            g.ky = (h[1] > l[1]) ? K : 0;
+            g.kz = (h[2] > l[2]) ? K : 0;
+            int c0[3], c1[3];
+            for (int d = 0; d < 3; ++d) {
+                c0[d] = (int)std::floor(l[d] * g.inv_cs);
+                c1[d] = (int)std::floor(h[d] * g.inv_cs);
+            }
+            g.bx0 = c0[0] - g.kx;
+            g.by0 = c0[1] - g.ky;
+            g.bz0 = c0[2] - g.kz;
+            const int64_t nx = (int64_t)c1[0] - c0[0] + 1 + 2 * g.kx;
+            const int64_t ny = (int64_t)c1[1] - c0[1] + 1 + 2 * g.ky;
+            const int64_t nz = (int64_t)c1[2] - c0[2] + 1 + 2 * g.kz;
+            if (nx * ny * nz > ((int64_t)1 << 26) || nx > (1 << 24))
+                return set_error(SPH_ERR_GRID, "batch: an instance's region needs too many cells");
+            g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
+            g.ncells = nx * ny * nz;
+            g.cell_base = cells;
+            g.uniform_h = b->h_uniform_inst[k];
+            cells += g.ncells;
+            slot += b->inst_off[k + 1] - b->inst_off[k];
+        }
+        grp.s1 = slot;
+        if (grp.s1 > grp.s0) b->groups.push_back(grp);
+    }
+    if (cells >= ((int64_t)1 << 30)) return set_error(SPH_ERR_GRID, "batch: too many cells in total");
+    b->total_cells = cells;
+    cudaStream_t st = b->stream;
+    ArraySnap &A = b->snap;
+    if (cells + 1 > b->cell_cap) {
+        cudaFree(A.cstart);
+        cudaFree(A.cursor);
+        A.cstart = A.cursor = nullptr;
+        const int64_t cap = cells + 1 + (cells + 1) / 4;
+        SPH_CUDA(cudaMalloc(&A.cstart, sizeof(int) * cap));
+        SPH_CUDA(cudaMalloc(&A.cursor, sizeof(int) * cap));
+        b->cell_cap = cap;
+        // scan scratch (sized now: nothing is allocated while a step is captured)
+        const int64_t ntiles = (cap + 2047) / 2048 + 1;
+        if (ntiles > b->ctx->scan_tmp_cap) {
+            cudaFree(b->ctx->scan_tmp);
+            b->ctx->scan_tmp = nullptr;
+            SPH_CUDA(cudaMalloc(&b->ctx->scan_tmp, sizeof(int) * ntiles));
+            b->ctx->scan_tmp_cap = ntiles;
+        }
+    }
+    SPH_CUDA(cudaMemcpyAsync(b->d_grids, b->h_grids.data(), sizeof(Grid) * ninst,
+                             cudaMemcpyHostToDevice, st));
+    // the host vector must outlive the copy
+    SPH_CUDA(cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+// New regions from the instances' current extents (grown by the margin),
+// the grids laid out again and the step graph dropped (re-captured at the
+// next step).
+int batch_regrid(sph_batch *b) {
+    cudaStream_t st = b->stream;
+    const int ninst = b->ninst;
+    k_inst_box<<<ninst, 256, 0, st>>>(b->view, b->d_off, b->d_ibox);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_inst_box");
+    std::vector<double> box(6 * (size_t)ninst), lo(3 * (size_t)ninst), hi(3 * (size_t)ninst);
+    SPH_CUDA(cudaMemcpyAsync(box.data(), b->d_ibox, sizeof(double) * box.size(),
+                             cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < ninst; ++k)
+        for (int d = 0; d < 3; ++d) {
+            const double l = box[6 * k + d], h = box[6 * k + 3 + d];
+            const double ext = h - l;
+            const double pad = ext > 0 ? b->margin * ext + 4.0 * b->inst_cell[k] : 0.0;
+            lo[3 * k + d] = l - pad;
+            hi[3 * k + d] = h + pad;
+        }
+    const int rc = batch_place(b, lo.data(), hi.data());
+    if (rc) return rc;
+    if (b->graph_exec) {
+        cudaGraphExecDestroy(b->graph_exec);
+        b->graph_exec = nullptr;
+    }
+    b->regrids += 1;
+    return SPH_OK;
+}
 
 int batch_build(sph_batch *b, int check_jump) {
     cudaStream_t st = b->stream;
@@ -148,51 +298,45 @@ int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instanc
     b->view = *all;
     b->rec = *rec;
     b->ninst = ninst;
-    const int K = rec->subdiv;
-    b->h_grids.assign(ninst, Grid());
-    std::vector<double> inv_ref(ninst);
-    int64_t cells = 0;
+    b->margin = rec->margin > 0 ? rec->margin : 0.0;
+    b->inst_subdiv.assign(ninst, rec->subdiv);
+    b->inst_cell.assign(ninst, 0.0);
+    b->h_uniform_inst.assign(ninst, 0);
+    b->inst_off.assign(ninst + 1, 0);
+    std::vector<double> lo(3 * (size_t)ninst), hi(3 * (size_t)ninst);
     for (int k = 0; k < ninst; ++k) {
-        Grid &g = b->h_grids[k];
-        g.cs = inst[k].cell_size / K;
-        g.inv_cs = 1.0 / g.cs;
-        g.cs_f = (float)g.cs;
-        g.radius_scale = rec->radius_scale;
-        g.kx = K;
-        g.ky = (inst[k].hi[1] > inst[k].lo[1]) ? K : 0;
-        g.kz = (inst[k].hi[2] > inst[k].lo[2]) ? K : 0;
-        int lo[3], hi[3];
+        if (inst[k].subdiv < 0 || inst[k].subdiv > 3)
+            return set_error(SPH_ERR_ARG, "batch: an instance's subdiv must be 0..3");
+        if (inst[k].subdiv > 0) b->inst_subdiv[k] = inst[k].subdiv;
+        b->inst_cell[k] = inst[k].cell_size;
+        b->h_uniform_inst[k] = inst[k].uniform_h ? 1 : 0;
+        b->inst_off[k + 1] = inst[k].offset + inst[k].n;
         for (int d = 0; d < 3; ++d) {
-            lo[d] = (int)std::floor(inst[k].lo[d] * g.inv_cs);
-            hi[d] = (int)std::floor(inst[k].hi[d] * g.inv_cs);
+            lo[3 * k + d] = inst[k].lo[d];
+            hi[3 * k + d] = inst[k].hi[d];
         }
-        g.bx0 = lo[0] - g.kx;
-        g.by0 = lo[1] - g.ky;
-        g.bz0 = lo[2] - g.kz;
-        const int64_t nx = (int64_t)hi[0] - lo[0] + 1 + 2 * g.kx;
-        const int64_t ny = (int64_t)hi[1] - lo[1] + 1 + 2 * g.ky;
-        const int64_t nz = (int64_t)hi[2] - lo[2] + 1 + 2 * g.kz;
-        if (nx * ny * nz > ((int64_t)1 << 26) || nx > (1 << 24))
-            return set_error(SPH_ERR_GRID, "batch: an instance's region needs too many cells");
-        g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
-        g.ncells = nx * ny * nz;
-        g.cell_base = cells;
-        g.uniform_h = inst[k].uniform_h ? 1 : 0;
-        cells += g.ncells;
-        inv_ref[k] = 1.0 / inst[k].cell_size;
     }
-    if (cells >= ((int64_t)1 << 30)) return set_error(SPH_ERR_GRID, "batch: too many cells in total");
-    b->total_cells = cells;
     b->uniform_h = 1;
-    for (auto &g : b->h_grids) b->uniform_h &= g.uniform_h;
+    for (int k = 0; k < ninst; ++k) b->uniform_h &= b->h_uniform_inst[k];
     cudaStream_t st = b->stream;
     const int64_t n = all->n;
+    std::vector<double> inv_ref(ninst);
+    for (int k = 0; k < ninst; ++k) inv_ref[k] = 1.0 / inst[k].cell_size;
     SPH_CUDA(cudaMalloc(&b->d_grids, sizeof(Grid) * ninst));
-    SPH_CUDA(cudaMemcpyAsync(b->d_grids, b->h_grids.data(), sizeof(Grid) * ninst,
-                             cudaMemcpyHostToDevice, st));
     SPH_CUDA(cudaMalloc(&b->d_inv_ref, sizeof(double) * ninst));
     SPH_CUDA(cudaMemcpyAsync(b->d_inv_ref, inv_ref.data(), sizeof(double) * ninst,
                              cudaMemcpyHostToDevice, st));
+    SPH_CUDA(cudaMalloc(&b->d_off, sizeof(int64_t) * (ninst + 1)));
+    SPH_CUDA(cudaMemcpyAsync(b->d_off, b->inst_off.data(), sizeof(int64_t) * (ninst + 1),
+                             cudaMemcpyHostToDevice, st));
+    SPH_CUDA(cudaMalloc(&b->d_ibox, sizeof(double) * 6 * ninst));
+    SPH_CUDA(cudaMalloc(&b->d_steps, sizeof(unsigned long long)));
+    SPH_CUDA(cudaMemsetAsync(b->d_steps, 0, sizeof(unsigned long long), st));
+    b->h_steps = 0;
+    {
+        const int rc = batch_place(b, lo.data(), hi.data());
+        if (rc) return rc;
+    }
     SPH_CUDA(cudaMalloc(&b->inst_of, sizeof(int) * n));
     SPH_CUDA(cudaMalloc(&b->sinst, sizeof(int) * n));
     for (int k = 0; k < ninst; ++k) {
@@ -209,16 +353,8 @@ int batch_setup(sph_batch *b, const sph_array_view *all, const sph_batch_instanc
     SPH_CUDA(cudaMalloc(&A.pm, sizeof(float4) * n));
     SPH_CUDA(cudaMalloc(&A.velh, sizeof(float4) * n));
     SPH_CUDA(cudaMalloc(&A.st, sizeof(float4) * n));
-    SPH_CUDA(cudaMalloc(&A.cstart, sizeof(int) * (cells + 1)));
-    SPH_CUDA(cudaMalloc(&A.cursor, sizeof(int) * (cells + 1)));
     SPH_CUDA(cudaMalloc(&A.refcell, sizeof(int) * 3 * n));
     A.view = *all;
-    // scan scratch (sized now: nothing is allocated while a step is captured)
-    {
-        const int64_t ntiles = (cells + 1 + 2047) / 2048 + 1;
-        SPH_CUDA(cudaMalloc(&b->ctx->scan_tmp, sizeof(int) * ntiles));
-        b->ctx->scan_tmp_cap = ntiles;
-    }
     // neighbour list (built by every first density pass)
     NbrList &L = b->list;
     L.cap = rec->list_cap > 0 ? rec->list_cap : (rec->dim == 3 ? 96 : (rec->dim == 2 ? 40 : 16));
@@ -263,8 +399,24 @@ static double *state_ptr(sph_batch *b, int c) {
     return const_cast<double *>(p[c < d ? c : 3 + (c - d)]);
 }
 
-// one time step as a fixed launch sequence (captured into the graph)
+// one time step as a fixed launch sequence (captured into the graph); every
+// launch that writes the state, and the completed-step count, is gated on
+// the error word, so a step in which a particle left its region or jumped
+// changes nothing after that point
+static int batch_step_launches_gated(sph_batch *b);
+
 static int batch_step_launches(sph_batch *b) {
+    b->ctx->gate = b->d_err;
+    const int rc = batch_step_launches_gated(b);
+    b->ctx->gate = nullptr;
+    if (rc) return rc;
+    k_step_done<<<1, 1, 0, b->stream>>>(b->d_err, b->d_steps);
+    count_launch();
+    SPH_LAUNCH_CHECK("k_step_done");
+    return SPH_OK;
+}
+
+static int batch_step_launches_gated(sph_batch *b) {
     const int nc = 2 * b->rec.dim;
     const double dt = b->rec.dt;
     sph_axpy_line lines[SPH_MAX_AXPY_LINES];
@@ -294,9 +446,9 @@ static int batch_step_launches(sph_batch *b) {
     return launch_integrate(b->ctx, b->view.n, lines, nc);
 }
 
-int batch_step(sph_batch *b, int nsteps, int use_graph) {
-    if (!b->ready) return set_error(SPH_ERR_STATE, "batch: not set up");
-    if (nsteps < 0) return set_error(SPH_ERR_ARG, "batch: negative step count");
+// Launch nsteps steps: replays of the captured step graph, or eager
+// launches.
+static int batch_launch_steps(sph_batch *b, int nsteps, int use_graph) {
     if (!use_graph) {
         for (int s = 0; s < nsteps; ++s) {
             const int rc = batch_step_launches(b);
@@ -346,6 +498,48 @@ int batch_step(sph_batch *b, int nsteps, int use_graph) {
     return SPH_OK;
 }
 
+int batch_step(sph_batch *b, int nsteps, int use_graph) {
+    if (!b->ready) return set_error(SPH_ERR_STATE, "batch: not set up");
+    if (nsteps < 0) return set_error(SPH_ERR_ARG, "batch: negative step count");
+    int left = nsteps, stuck = 0;
+    while (left > 0) {
+        int rc = batch_launch_steps(b, left, use_graph);
+        if (rc) return rc;
+        // the steps completed and the error word
+        struct {
+            unsigned long long steps;
+            unsigned err;
+        } h{0, 0};
+        SPH_CUDA(cudaMemcpyAsync(&h.steps, b->d_steps, sizeof(h.steps), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        SPH_CUDA(cudaMemcpyAsync(&h.err, b->d_err, sizeof(h.err), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        SPH_CUDA(cudaStreamSynchronize(b->stream));
+        const int done = (int)(h.steps - b->h_steps);
+        b->h_steps = h.steps;
+        if (h.err == 0u) break;
+        // the failing step stopped where the error was raised; an RK2 step
+        // may have stepped to its midpoint: back to the state it started from
+        if (b->rec.scheme == 1) {
+            for (int c = 0; c < 2 * b->rec.dim; ++c)
+                SPH_CUDA(cudaMemcpyAsync(const_cast<double *>(state_ptr(b, c)), b->x0[c],
+                                         sizeof(double) * b->view.n, cudaMemcpyDeviceToDevice,
+                                         b->stream));
+        }
+        // a jump (or no margin to grow the regions by) is the caller's error
+        // (the error word stays set for sph_batch_error_word)
+        if ((h.err & ~SPH_EFLAG_BOX) != 0u || b->margin <= 0.0) break;
+        stuck = done == 0 ? stuck + 1 : 0;
+        if (stuck >= 3)
+            return set_error(SPH_ERR_GRID, "batch: a particle keeps leaving its instance's region");
+        rc = batch_regrid(b);
+        if (rc) return rc;
+        SPH_CUDA(cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream));
+        left -= done;
+    }
+    return SPH_OK;
+}
+
 __global__ void k_inst_pairs(const int *cnt, const int *sinst, int64_t n,
                              unsigned long long *out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -382,6 +576,9 @@ void batch_free(sph_batch *b) {
     }
     cudaFree(b->d_err);
     cudaFree(b->d_pairs);
+    cudaFree(b->d_off);
+    cudaFree(b->d_ibox);
+    cudaFree(b->d_steps);
 }
 
 }  // namespace sphgb

@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <mutex>
 #include <utility>
@@ -71,12 +72,21 @@ struct BrickSmem {
     int off_rlo, off_roff, off_dlo, off_doff, off_scell;
 };
 
+// The neighbour radius of a uniform h, computed on the host with the
+// operations of the per-destination test: radius2 = (h rs)^2 in FP64, its
+// FP32 band [r2lo, r2hi] and the list radius r2list (0 without a skin).
+struct BrickRadius {
+    double radius2;
+    float r2lo, r2hi, r2list;
+};
+
 struct BrickDensityArgs {
     Grid g;
     BrickGeom bk;
     BrickDstDev d;
     BrickSrcDev s;
     BrickSmem sm;
+    BrickRadius rad;
     uint16_t *nbr;      // list: 8-entry group g of destination d of brick b is
                         // the uint4 (bdst[b] * cap / 8 + g * D_b + d)
     int *cnt;           // neighbour count per destination, brick order
@@ -97,6 +107,7 @@ struct BrickRatesArgs {
     BrickDstDev d;
     BrickSrcDev s;
     BrickSmem sm;
+    BrickRadius rad;
     const uint16_t *nbr;
     const int *cnt;
     int cap;
@@ -234,21 +245,20 @@ __device__ __forceinline__ int staged_slot(const BlockGeo &G, const int *rlo, co
     return rlo[r] + (t - roff[r]);
 }
 
-// Source records: staged in shared memory, or (STAGED = false, a brick
-// more populous than the shared memory holds) recomputed from the sorted
-// arrays with the same operations.
-// Staging pointers of the dynamic shared memory.
+// The dynamic shared memory of the brick kernels: the staged records from
+// byte 0, then the block's tables.
+extern __shared__ __align__(16) unsigned char brick_smem[];
+
+// Table pointers and the state records' offset in the dynamic shared memory.
 struct SmemPtrs {
-    float4 *P, *V;
-    float2 *S;
+    uint32_t voff, soff;
     int *rlo, *roff, *dlo, *doff, *scell;
 };
 
 __device__ __forceinline__ SmemPtrs smem_ptrs(unsigned char *base, const BrickSmem &sm) {
     SmemPtrs p;
-    p.P = reinterpret_cast<float4 *>(base);
-    p.V = reinterpret_cast<float4 *>(base + sm.off_v);
-    p.S = reinterpret_cast<float2 *>(base + sm.off_s);
+    p.voff = (uint32_t)sm.off_v;
+    p.soff = (uint32_t)sm.off_s;
     p.rlo = reinterpret_cast<int *>(base + sm.off_rlo);
     p.roff = reinterpret_cast<int *>(base + sm.off_roff);
     p.dlo = reinterpret_cast<int *>(base + sm.off_dlo);
@@ -263,25 +273,34 @@ __device__ __forceinline__ float4 pad_pos() { return make_float4(1e15f, 1e15f, 1
 __device__ __forceinline__ float4 pad_vel() { return make_float4(0.f, 0.f, 0.f, 0.f); }
 __device__ __forceinline__ float2 pad_state() { return make_float2(0.5f, 0.f); }
 
-template <bool STAGED>
+// Source records: staged in shared memory, or (STAGED = false, a brick
+// more populous than the shared memory holds) recomputed from the sorted
+// arrays with the same operations.
+template <bool STAGED, int PSH>
 struct SrcRecords;
 
-// staged in shared memory
-template <>
-struct SrcRecords<true> {
-    const float4 *P, *V;
-    const float2 *S;
-    __device__ __forceinline__ float4 pos(int t) const { return P[t]; }
-    // (u, v, w, p / rho^2) and (rho, cs)
+// Staged: the position record (x, y, z from the brick's centre cell, m) of
+// source t at byte 16 t of the shared memory, in the rates pass the velocity
+// record (u, v, w, p / rho^2) at voff + 16 t and the state record (rho / 2,
+// alpha cs / 2) at soff + 8 t: 32-bit offsets into the shared array, so a
+// record costs one address operation.  (Position and velocity interleaved
+// in 32-byte records took 11 % longer: twice the bank conflicts of the
+// random reads.)
+template <int PSH>
+struct SrcRecords<true, PSH> {
+    uint32_t voff, soff;
+    __device__ __forceinline__ float4 pos(int t) const {
+        return *reinterpret_cast<const float4 *>(brick_smem + ((uint32_t)t << 4));
+    }
     __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
-        v = V[t];
-        s = S[t];
+        v = *reinterpret_cast<const float4 *>(brick_smem + voff + ((uint32_t)t << 4));
+        s = *reinterpret_cast<const float2 *>(brick_smem + soff + ((uint32_t)t << 3));
     }
 };
 
 // recomputed from the sorted arrays with the staging's operations
-template <>
-struct SrcRecords<false> {
+template <int PSH>
+struct SrcRecords<false, PSH> {
     const BrickSrcDev *src;
     BlockGeo G;
     const int *rlo, *roff;
@@ -308,45 +327,45 @@ struct SrcRecords<false> {
     }
 };
 
-template <bool STAGED>
-__device__ __forceinline__ SrcRecords<STAGED> make_records(const SmemPtrs &sp, const BrickSrcDev &S,
-                                                           const BlockGeo &G, float csf, int T,
-                                                           float halpha);
-template <>
-__device__ __forceinline__ SrcRecords<true> make_records<true>(const SmemPtrs &sp, const BrickSrcDev &,
-                                                               const BlockGeo &, float, int, float) {
-    return SrcRecords<true>{sp.P, sp.V, sp.S};
-}
-template <>
-__device__ __forceinline__ SrcRecords<false> make_records<false>(const SmemPtrs &sp,
-                                                                 const BrickSrcDev &S,
-                                                                 const BlockGeo &G, float csf,
-                                                                 int T, float halpha) {
-    return SrcRecords<false>{&S, G, sp.rlo, sp.roff, csf, T, halpha};
+template <bool STAGED, int PSH>
+__device__ __forceinline__ SrcRecords<STAGED, PSH> make_records(const SmemPtrs &sp,
+                                                                const BrickSrcDev &S,
+                                                                const BlockGeo &G, float csf,
+                                                                int T, float halpha) {
+    if constexpr (STAGED)
+        return SrcRecords<true, PSH>{sp.voff, sp.soff};
+    else
+        return SrcRecords<false, PSH>{&S, G, sp.rlo, sp.roff, csf, T, halpha};
 }
 
-// Copy the block's source records into shared memory.
-// Rates records: (u, v, w, p / rho^2) and (rho / 2, alpha cs / 2), the
-// halves that the pair averages of the artificial viscosity add.
+// Copy the block's source records into shared memory (the layout of
+// SrcRecords<true, .>).  Rates records: (u, v, w, p / rho^2) and (rho / 2,
+// alpha cs / 2), the halves that the pair averages of the artificial
+// viscosity add.
 template <bool RATES>
 __device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
-                                      const int *roff, int T, float csf, float4 *P, float4 *V,
-                                      float2 *SS, float halpha = 0.f) {
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+                                      const int *roff, int T, float csf, uint32_t voff,
+                                      uint32_t soff, float halpha = 0.f) {
+    for (int t = threadIdx.x; t <= T; t += blockDim.x) {
+        float4 *prec = reinterpret_cast<float4 *>(brick_smem + ((uint32_t)t << 4));
+        float4 *vrec = reinterpret_cast<float4 *>(brick_smem + voff + ((uint32_t)t << 4));
+        float2 *srec = reinterpret_cast<float2 *>(brick_smem + soff + ((uint32_t)t << 3));
+        if (t == T) {
+            // the padding record after the staged ones
+            *prec = pad_pos();
+            if (RATES) {
+                *vrec = pad_vel();
+                *srec = pad_state();
+            }
+            continue;
+        }
         int cy, cz;
         const int j = staged_slot(G, rlo, roff, t, cy, cz);
-        P[t] = rel_pos(S.pm, S.scx, j, cy, cz, G, csf);
+        *prec = rel_pos(S.pm, S.scx, j, cy, cz, G, csf);
         if (RATES) {
             const float4 vh = S.velh[j], st = S.st[j];
-            V[t] = make_float4(vh.x, vh.y, vh.z, st.y);
-            SS[t] = make_float2(0.5f * st.x, halpha * st.z);
-        }
-    }
-    if (threadIdx.x == 0) {
-        P[T] = pad_pos();
-        if (RATES) {
-            V[T] = pad_vel();
-            SS[T] = pad_state();
+            *vrec = make_float4(vh.x, vh.y, vh.z, st.y);
+            *srec = make_float2(0.5f * st.x, halpha * st.z);
         }
     }
 }
@@ -369,7 +388,8 @@ struct BrickDest {
 };
 
 __device__ __forceinline__ bool brick_dest(const Grid &g, const BrickDstDev &D, const BlockGeo &G,
-                                           const int *dlo, const int *doff, int d, BrickDest &q) {
+                                           const BrickRadius &rad, const int *dlo,
+                                           const int *doff, int d, BrickDest &q) {
     const int r = row_of(doff, G.ndr, d);
     q.s = dlo[r] + (d - doff[r]);
     q.cy = G.y0 + r % G.dry;
@@ -379,18 +399,11 @@ __device__ __forceinline__ bool brick_dest(const Grid &g, const BrickDstDev &D, 
     q.xi_x = p.x; q.xi_y = p.y; q.xi_z = p.z;
     q.cx = (int)D.scx[q.s];
     q.P = rel_pos(D.pm, D.scx, q.s, q.cy, q.cz, G, g.cs_f);
-    if (D.tag != nullptr && D.tag[q.orig] != SPH_TAG_LOCAL_REAL) return false;
-    const double radius = __dmul_rn(D.h[q.orig], g.radius_scale);
-    q.radius2 = __dmul_rn(radius, radius);
-    const float r2 = (float)q.radius2;
-    q.r2lo = r2 * (1.f - 1e-5f);
-    q.r2hi = r2 * (1.f + 1e-5f);
-    q.r2list = 0.f;
-    if (g.skin > 0.f) {
-        const float rl = (float)radius + g.skin;
-        q.r2list = rl * rl * (1.f + 2e-5f);
-    }
-    return true;
+    q.radius2 = rad.radius2;
+    q.r2lo = rad.r2lo;
+    q.r2hi = rad.r2hi;
+    q.r2list = rad.r2list;
+    return D.tag == nullptr || D.tag[q.orig] == SPH_TAG_LOCAL_REAL;
 }
 
 // Visit the listed sources of destination q in the staged records, in the
@@ -399,9 +412,9 @@ __device__ __forceinline__ bool brick_dest(const Grid &g, const BrickDstDev &D, 
 // fn(t, rx, ry, rz, hit): staging index, r = x_dest - x_src, neighbour or
 // (with a list skin) only within the list radius.  The ranges come from the
 // block's cell table (scell) or, without one, from the grid's cell table.
-template <int K, bool STAGED, class Fn>
+template <int K, bool STAGED, int PSH, class Fn>
 __device__ __forceinline__ void brick_traverse(const Grid &g, const BlockGeo &G, const BrickSrcDev &S,
-                                               const BrickDstDev &D, const SrcRecords<STAGED> &R,
+                                               const BrickDstDev &D, const SrcRecords<STAGED, PSH> &R,
                                                const int *rlo, const int *roff, const int *scell,
                                                const BrickDest &q, Fn &&fn) {
     const float csf = g.cs_f;
@@ -456,6 +469,20 @@ __device__ __forceinline__ void brick_traverse(const Grid &g, const BlockGeo &G,
     }
 }
 
+// Reciprocal square root and reciprocal, flushing subnormal inputs to zero
+// (the pair terms' inputs are bounded away from the subnormal range: r^2 is
+// clamped to 1e-30, the density sums are near the rest density).
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ bool gate_off(const unsigned *gate) {
     return gate != nullptr && __ldg(gate) != 0u;
 }
@@ -486,23 +513,26 @@ __device__ __forceinline__ float density_term(const float4 &pi, const float4 &pj
                                               const WCoef &wc) {
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float r = r2 * rsqrtf(fmaxf(r2, 1e-30f));
+    const float r = r2 * rsqrt_ftz(fmaxf(r2, 1e-30f));
     return w_of(r * ih, wc) * pj.w;
 }
 
-// Density of one destination and, with Tait, its p and cs; the sorted
-// state record when the pass writes the destination's own properties.
+// Density of one destination (the compensated sum hi + lo) and, with
+// Tait, its p and cs; the sorted state record when the pass writes the
+// destination's own properties.
 __device__ __forceinline__ void density_store(const BrickDensityArgs &A, int s, int orig, bool real,
-                                              double r64) {
+                                              float hi, float lo) {
+    const double r64 = (double)hi + (double)lo;
     if (A.rho_out) A.rho_out[orig] = r64;
-    const float rf = (float)r64;
+    const float rf = hi + lo;
     float pf = 0.f, cf = 0.f;
     if (A.tait) {
         if (real) {
             // p = B((rho/ro)^gamma - 1), cs = co (rho/ro)^((gamma-1)/2), through
-            // log1p/expm1 of the density excess (relative accuracy of p as rho -> ro)
+            // log1p/expm1 of the density excess (relative accuracy of p as
+            // rho -> ro); hi - ro is exact for hi within a factor 2 of ro
             const float Bt = A.co * A.co * A.ro / A.gamma;
-            const float lr = log1pf((float)((r64 - (double)A.ro) / (double)A.ro));
+            const float lr = log1pf(((hi - A.ro) + lo) * (1.f / A.ro));
             pf = Bt * expm1f(A.gamma * lr);
             cf = A.co * expf(0.5f * (A.gamma - 1.f) * lr);
         }
@@ -520,9 +550,78 @@ __device__ __forceinline__ void density_store(const BrickDensityArgs &A, int s, 
     }
 }
 
+// What a destination's sums start from: its slot and records, its count
+// and the first two groups of its list.  The first destination of every
+// thread requests these before the block stages its sources, so their
+// latency overlaps the staging.
+struct DestPre {
+    int s, orig;    // sorted slot, original index
+    bool real;
+    float4 P;       // brick-relative position, mass
+    int c;
+    uint4 b0, b1;
+};
+
+__device__ __forceinline__ void dest_prefetch(const BrickDstDev &Dd, const Grid &g,
+                                              const BlockGeo &G, const BrickRadius &rad,
+                                              const SmemPtrs &sp, const int *cnt,
+                                              const uint4 *lgrp, int cap, int D, int dbase,
+                                              int d, DestPre &p) {
+    BrickDest q;
+    p.real = brick_dest(g, Dd, G, rad, sp.dlo, sp.doff, d, q);
+    p.s = q.s;
+    p.orig = q.orig;
+    p.P = q.P;
+    p.c = cnt[dbase + d];
+    // every destination owns cap / 8 groups: the first two are read whatever
+    // the count (used only as far as it reaches)
+    const uint4 *lst = lgrp + d;
+    p.b0 = lst[0];
+    p.b1 = cap >= 16 ? lst[D] : make_uint4(0, 0, 0, 0);
+}
+
+// The density sum of one destination over its list: groups of 8 entries,
+// each requested two groups ahead into one of three rotating buffers.
+template <bool STAGED, int PSH>
+__device__ __forceinline__ void density_group(CSum &rho, const SrcRecords<STAGED, PSH> &R,
+                                              const uint4 &grp, const float4 &Pi, float ih,
+                                              const WCoef &wc) {
+    float part = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float4 pj[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pj[i] = R.pos(group_entry(grp, 4 * h + i));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) part += density_term(Pi, pj[i], ih, wc);
+    }
+    rho.add(part);
+}
+
+template <bool STAGED, int PSH>
+__device__ __forceinline__ void density_stream(CSum &rho, const SrcRecords<STAGED, PSH> &R,
+                                               const uint4 *lst, int D, int ng, const float4 &Pi,
+                                               float ih, const WCoef &wc, uint4 b0, uint4 b1) {
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    const size_t step = (size_t)D;
+    uint4 b2;
+    for (int gi = 0;;) {
+        if (gi >= ng) break;
+        b2 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        density_group<STAGED>(rho, R, b0, Pi, ih, wc);
+        if (++gi >= ng) break;
+        b0 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        density_group<STAGED>(rho, R, b1, Pi, ih, wc);
+        if (++gi >= ng) break;
+        b1 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        density_group<STAGED>(rho, R, b2, Pi, ih, wc);
+        ++gi;
+    }
+}
+
 template <int K, bool BUILD, bool STAGED>
 __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityArgs A) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char *smem = brick_smem;
     if (gate_off(A.gate)) return;
     const int b = blockIdx.x;
     const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
@@ -538,17 +637,27 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
     // the stencil cell table of a list build (a destination whose neighbours
     // outgrew the list reads the grid's table instead)
     int *scell = BUILD ? sp.scell : nullptr;
+    const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * ng_cap;
+    // the first destination of this thread, requested before the staging
+    DestPre pre;
+    if (!BUILD && (int)threadIdx.x < D)
+        dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, cap, D, dbase, threadIdx.x, pre);
     if (BUILD) cell_table(g, G, A.s.cstart, sp.rlo, sp.roff, sp.scell);
-    if (STAGED) stage<false>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, nullptr, nullptr);
+    if (STAGED) stage<false>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.voff, sp.soff);
     __syncthreads();
-    const SrcRecords<STAGED> R = make_records<STAGED>(sp, A.s, G, g.cs_f, T, 0.f);
+    const SrcRecords<STAGED, 4> R = make_records<STAGED, 4>(sp, A.s, G, g.cs_f, T, 0.f);
     const float ih = __fdividef(1.f, g.h_uniform);
     const float fac = cubic_fac(A.dim, ih);
     const WCoef wc = w_coef(fac, 1.f);
-    const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * ng_cap;
-    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    // destination d from its record p (for a list build, the traversal fills it)
+    auto one = [&](int d, DestPre &p) {
         BrickDest q;
-        const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
+        if (BUILD) {
+            p.real = brick_dest(g, A.d, G, A.rad, sp.dlo, sp.doff, d, q);
+            p.s = q.s;
+            p.orig = q.orig;
+        }
+        const bool real = p.real;
         CSum rho;
         int c = 0;
         if (real) {
@@ -564,6 +673,10 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
                     grp.z = __funnelshift_r(grp.z, grp.w, 16);
                     grp.w = (grp.w >> 16) | (t << 16);
                 };
+                // neighbours summed in plain FP32 batches of 8 hits, each
+                // batch folded into the compensated sum
+                float part = 0.f;
+                int nb = 0;
                 brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, scell, q,
                     [&](int t, float rx, float ry, float rz, bool hit) {
                         if (c < cap) {
@@ -573,38 +686,24 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
                         ++c;
                         if (!hit) return;
                         const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                        const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                        rho.add(cubic_w(r * ih) * fac * R.pos(t).w);
+                        const float r = r2 * rsqrt_ftz(fmaxf(r2, 1e-30f));
+                        part += w_of(r * ih, wc) * R.pos(t).w;
+                        if (++nb == 8) {
+                            rho.add(part);
+                            part = 0.f;
+                            nb = 0;
+                        }
                     });
+                rho.add(part);
                 // pad the last group with the zero record
                 if (c < cap && (c & 7)) {
                     for (int k = c; k & 7; ++k) push((unsigned)T);
                     out[(size_t)(c >> 3) * D] = grp;
                 }
             } else {
-                // stream the groups of 8 entries, two groups requested ahead
-                c = A.cnt[dbase + d];
-                const int ng = (min(c, cap) + 7) >> 3;
-                const uint4 *lst = lgrp + d;
-                uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
-                if (ng > 0) cur = lst[0];
-                if (ng > 1) nxt = lst[D];
-                for (int gi = 0; gi < ng; ++gi) {
-                    uint4 fut = nxt;
-                    if (gi + 2 < ng) fut = lst[(size_t)(gi + 2) * D];
-                    float part = 0.f;
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        float4 pj[4];
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) pj[i] = R.pos(group_entry(cur, 4 * h + i));
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) part += density_term(q.P, pj[i], ih, wc);
-                    }
-                    rho.add(part);
-                    cur = nxt;
-                    nxt = fut;
-                }
+                c = p.c;
+                density_stream<STAGED>(rho, R, lgrp + d, D, (min(c, cap) + 7) >> 3, p.P, ih, wc,
+                                       p.b0, p.b1);
             }
         }
         if (BUILD) {
@@ -613,16 +712,23 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
             const int wmax = __reduce_max_sync(act, c);
             if ((threadIdx.x & 31) == (__ffs(act) - 1)) atomicMax(A.maxcnt, wmax);
         }
-        if (A.write_out) density_store(A, q.s, q.orig, real, real ? rho.value() : 0.0);
+        if (A.write_out)
+            density_store(A, p.s, p.orig, real, real ? rho.hi : 0.f, real ? rho.lo : 0.f);
+    };
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        if (!BUILD && d != (int)threadIdx.x)
+            dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, cap, D, dbase, d, pre);
+        one(d, pre);
     }
-    if (BUILD || !A.write_out || A.rho_out == nullptr) return;
+    if constexpr (BUILD) return;
+    if (!A.write_out || A.rho_out == nullptr) return;
     // destinations with more neighbours than their list holds: the rest
     // come from a traversal that skips the listed ones (in the order of
     // the list build), added to the stored partial density
     for (int d = threadIdx.x; d < D; d += blockDim.x) {
         if (A.cnt[dbase + d] <= cap) continue;
         BrickDest q;
-        if (!brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q)) continue;
+        if (!brick_dest(g, A.d, G, A.rad, sp.dlo, sp.doff, d, q)) continue;
         CSum rest;
         int skip = cap;
         brick_traverse<K, STAGED>(g, G, A.s, A.d, R, sp.rlo, sp.roff, nullptr, q,
@@ -633,7 +739,13 @@ __global__ void __maxnreg__(64) k_bdensity(const __grid_constant__ BrickDensityA
                 const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
                 rest.add(cubic_w(r * ih) * fac * R.pos(t).w);
             });
-        density_store(A, q.s, q.orig, true, A.rho_out[q.orig] + rest.value());
+        // the stored partial density (hi + lo of the listed part, in FP64)
+        // plus the rest, as a compensated FP32 pair
+        CSum tot = rest;
+        const double part = A.rho_out[q.orig];
+        const float phi = (float)part;
+        tot.merge(phi, (float)(part - (double)phi));
+        density_store(A, q.s, q.orig, true, tot.hi, tot.lo);
     }
 }
 
@@ -685,17 +797,18 @@ __device__ __forceinline__ void rates_pair(RatesAcc &a, const RatesConst &k, flo
                                            float rz, const float4 &pj, const float4 &vj,
                                            const float2 &sj) {
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float rinv = rsqrt_ftz(fmaxf(r2, 1e-30f));
     const float q = r2 * rinv * k.ih;
     const float mj = pj.w;
     const float dot = (a.vi.x - vj.x) * rx + (a.vi.y - vj.y) * ry + (a.vi.z - vj.z) * rz;
     const float hdot = k.h * fminf(dot, 0.f);
     const float mu = ETA0 ? hdot * rinv * rinv : __fdividef(hdot, r2 + k.eta2h2);
-    const float inv_rhoab = __fdividef(1.f, a.hrhoi + sj.x);
+    const float inv_rhoab = rcp_ftz(a.hrhoi + sj.x);
     const float piab = mu * fmaf(k.beta, mu, -(a.haci + sj.y)) * inv_rhoab;
     const float t = -mj * ((a.pri + vj.w) + piab);
-    const float tq = 2.f - q;
-    const float g = q > 2.f ? 0.f : (q >= 1.f ? k.gout * (tq * tq) * rinv : fmaf(k.gin1, q, k.gin0));
+    // (2 - q) clamped at 0: the outer branch is 0 beyond q = 2
+    const float tq = fmaxf(2.f - q, 0.f);
+    const float g = q >= 1.f ? k.gout * (tq * tq) * rinv : fmaf(k.gin1, q, k.gin0);
     const float gf = g * t;
     a.pax = fmaf(gf, rx, a.pax);
     a.pay = fmaf(gf, ry, a.pay);
@@ -718,45 +831,61 @@ __device__ __forceinline__ void rates_flush(RatesAcc &a) {
     }
 }
 
-// The sums of one destination: its list streamed in groups of 8 entries
-// (two groups requested ahead), records two at a time, flushed every 4.
-template <bool XSPH, bool ETA0, bool STAGED>
-__device__ __forceinline__ void rates_stream(RatesAcc &acc, const RatesConst &kc,
-                                             const SrcRecords<STAGED> &R, const uint4 *lst, int D,
-                                             int ng, const float4 &Pi) {
-    uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
-    if (ng > 0) cur = lst[0];
-    if (ng > 1) nxt = lst[D];
-    for (int gi = 0; gi < ng; ++gi) {
-        uint4 fut = nxt;
-        if (gi + 2 < ng) fut = lst[(size_t)(gi + 2) * D];
+// The pairs of one group of 8 list entries, records two at a time, then
+// the batch's partial sums folded into the compensated ones.
+template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+__device__ __forceinline__ void rates_group(RatesAcc &acc, const RatesConst &kc,
+                                            const SrcRecords<STAGED, PSH> &R, const uint4 &grp,
+                                            const float4 &Pi) {
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            float4 pj[2], vj[2];
-            float2 sj[2];
+    for (int h = 0; h < 4; ++h) {
+        float4 pj[2], vj[2];
+        float2 sj[2];
 #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const int t = group_entry(cur, 2 * h + i);
-                pj[i] = R.pos(t);
-                R.state(t, vj[i], sj[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < 2; ++i)
-                rates_pair<XSPH, ETA0>(acc, kc, Pi.x - pj[i].x, Pi.y - pj[i].y, Pi.z - pj[i].z,
-                                       pj[i], vj[i], sj[i]);
-            if (h & 1) rates_flush<XSPH>(acc);
+        for (int i = 0; i < 2; ++i) {
+            const int t = group_entry(grp, 2 * h + i);
+            pj[i] = R.pos(t);
+            R.state(t, vj[i], sj[i]);
         }
-        cur = nxt;
-        nxt = fut;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+            rates_pair<XSPH, ETA0>(acc, kc, Pi.x - pj[i].x, Pi.y - pj[i].y, Pi.z - pj[i].z,
+                                   pj[i], vj[i], sj[i]);
+    }
+    rates_flush<XSPH>(acc);
+}
+
+// The sums of one destination: its list streamed in groups of 8 entries,
+// each group requested two groups ahead into one of three rotating
+// buffers (the loop body is unrolled over the three, so no buffer is
+// copied).
+template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+__device__ __forceinline__ void rates_stream(RatesAcc &acc, const RatesConst &kc,
+                                             const SrcRecords<STAGED, PSH> &R, const uint4 *lst, int D,
+                                             int ng, const float4 &Pi, uint4 b0, uint4 b1) {
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    uint4 b2;
+    const size_t step = (size_t)D;
+    for (int gi = 0;;) {
+        if (gi >= ng) break;
+        b2 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b0, Pi);
+        if (++gi >= ng) break;
+        b0 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b1, Pi);
+        if (++gi >= ng) break;
+        b1 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
+        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b2, Pi);
+        ++gi;
     }
 }
 
 // Neighbours of destination q past its list's capacity: a traversal that
 // skips the listed ones (in the order of the list build).
-template <int K, bool XSPH, bool ETA0, bool STAGED>
+template <int K, bool XSPH, bool ETA0, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_rest(RatesAcc &acc, const RatesConst &kc, const Grid &g,
                                            const BlockGeo &G, const BrickSrcDev &S,
-                                           const BrickDstDev &D, const SrcRecords<STAGED> &R,
+                                           const BrickDstDev &D, const SrcRecords<STAGED, PSH> &R,
                                            const int *rlo, const int *roff, const BrickDest &q,
                                            int cap) {
     int skip = cap;
@@ -781,53 +910,73 @@ __device__ __forceinline__ void rates_acc_init(RatesAcc &acc, const float4 &vi, 
     acc.haci = halpha * st.z;
 }
 
-template <int K, bool XSPH, bool ETA0, bool STAGED>
+// The sums of destination d (listed part) and their store.
+template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+__device__ __forceinline__ void rates_dest(const BrickRatesArgs &A, const SrcRecords<STAGED, PSH> &R,
+                                           const RatesConst &kc, const uint4 *lgrp, int D, int d,
+                                           const DestPre &pre) {
+    const int cap = A.cap;
+    const bool real = pre.real;
+    RatesAcc acc;
+    rates_acc_init(acc, A.d.velh[pre.s], A.d.st[pre.s], 0.5f * A.alpha);
+    if (real)
+        rates_stream<XSPH, ETA0, STAGED>(acc, kc, R, lgrp + d, D, (min(pre.c, cap) + 7) >> 3,
+                                         pre.P, pre.b0, pre.b1);
+    const int orig = pre.orig;
+    double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
+    if (real) {
+        // the compensated sums rounded once to FP32 (far below the pair
+        // terms' own FP32 error), one conversion each
+        a3[0] = (double)acc.ax.fvalue(); a3[1] = (double)acc.ay.fvalue();
+        a3[2] = (double)acc.az.fvalue();
+        if (XSPH) {
+            p3[0] = (double)acc.xx.fvalue(); p3[1] = (double)acc.xy.fvalue();
+            p3[2] = (double)acc.xz.fvalue();
+        }
+        if (A.add_gravity) { a3[0] += A.gx; a3[1] += A.gy; a3[2] += A.gz; }
+        if (A.add_velocity) {
+            // exact FP64 velocity of the destination (position_funcs.pyx:47-50)
+            p3[0] += ld0(A.d.u, orig);
+            p3[1] += ld0(A.d.v, orig);
+            p3[2] += ld0(A.d.w, orig);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (A.acc[k]) A.acc[k][orig] = (A.accumulate ? A.acc[k][orig] : 0.0) + a3[k];
+        if (A.pos[k]) A.pos[k][orig] = (A.accumulate ? A.pos[k][orig] : 0.0) + p3[k];
+    }
+}
+
+template <int K, bool XSPH, bool ETA0, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_block(const BrickRatesArgs &A, const Grid &g,
                                             const BlockGeo &G, const SmemPtrs &sp,
-                                            const SrcRecords<STAGED> &R, const RatesConst &kc,
-                                            int D, int dbase) {
+                                            const SrcRecords<STAGED, PSH> &R, const RatesConst &kc,
+                                            int D, int dbase, const DestPre &first) {
     const int cap = A.cap;
     const float halpha = 0.5f * A.alpha;
     const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * (cap >> 3);
-    for (int d = threadIdx.x; d < D; d += blockDim.x) {
-        BrickDest q;
-        const bool real = brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q);
-        RatesAcc acc;
-        rates_acc_init(acc, A.d.velh[q.s], A.d.st[q.s], halpha);
-        if (real) {
-            const int c = A.cnt[dbase + d];
-            rates_stream<XSPH, ETA0, STAGED>(acc, kc, R, lgrp + d, D, (min(c, cap) + 7) >> 3, q.P);
-        }
-        const int orig = q.orig;
-        double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
-        if (real) {
-            a3[0] = acc.ax.value(); a3[1] = acc.ay.value(); a3[2] = acc.az.value();
-            p3[0] = acc.xx.value(); p3[1] = acc.xy.value(); p3[2] = acc.xz.value();
-            if (A.add_gravity) { a3[0] += A.gx; a3[1] += A.gy; a3[2] += A.gz; }
-            if (A.add_velocity) {
-                // exact FP64 velocity of the destination (position_funcs.pyx:47-50)
-                p3[0] += ld0(A.d.u, orig);
-                p3[1] += ld0(A.d.v, orig);
-                p3[2] += ld0(A.d.w, orig);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            if (A.acc[k]) A.acc[k][orig] = (A.accumulate ? A.acc[k][orig] : 0.0) + a3[k];
-            if (A.pos[k]) A.pos[k][orig] = (A.accumulate ? A.pos[k][orig] : 0.0) + p3[k];
-        }
+    // the first destination of the thread from its prefetched record, the
+    // others (bricks with more destinations than threads) as they come
+    if ((int)threadIdx.x < D) rates_dest<XSPH, ETA0, STAGED>(A, R, kc, lgrp, D, threadIdx.x, first);
+    for (int d = threadIdx.x + blockDim.x; d < D; d += blockDim.x) {
+        DestPre pre;
+        dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, cap, D, dbase, d, pre);
+        rates_dest<XSPH, ETA0, STAGED>(A, R, kc, lgrp, D, d, pre);
     }
     // destinations with more neighbours than their list holds: the rest
     // added to the stored sums
     for (int d = threadIdx.x; d < D; d += blockDim.x) {
         if (A.cnt[dbase + d] <= cap) continue;
         BrickDest q;
-        if (!brick_dest(g, A.d, G, sp.dlo, sp.doff, d, q)) continue;
+        if (!brick_dest(g, A.d, G, A.rad, sp.dlo, sp.doff, d, q)) continue;
         RatesAcc acc;
         rates_acc_init(acc, A.d.velh[q.s], A.d.st[q.s], halpha);
         rates_rest<K, XSPH, ETA0, STAGED>(acc, kc, g, G, A.s, A.d, R, sp.rlo, sp.roff, q, cap);
-        const double a3[3] = {acc.ax.value(), acc.ay.value(), acc.az.value()};
-        const double p3[3] = {acc.xx.value(), acc.xy.value(), acc.xz.value()};
+        const double a3[3] = {(double)acc.ax.fvalue(), (double)acc.ay.fvalue(),
+                              (double)acc.az.fvalue()};
+        const double p3[3] = {(double)acc.xx.fvalue(), (double)acc.xy.fvalue(),
+                              (double)acc.xz.fvalue()};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             if (A.acc[k]) A.acc[k][q.orig] += a3[k];
@@ -838,7 +987,7 @@ __device__ __forceinline__ void rates_block(const BrickRatesArgs &A, const Grid 
 
 template <int K, bool XSPH, bool STAGED>
 __global__ void __maxnreg__(XSPH ? 80 : 64) k_brates(const __grid_constant__ BrickRatesArgs A) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char *smem = brick_smem;
     if (gate_off(A.gate)) return;
     const int b = blockIdx.x;
     const int nd = A.d.bdst[b + 1] - A.d.bdst[b];
@@ -848,17 +997,22 @@ __global__ void __maxnreg__(XSPH ? 80 : 64) k_brates(const __grid_constant__ Bri
     SmemPtrs sp = smem_ptrs(smem, A.sm);
     int T, D;
     block_tables(g, G, A.s.cstart, A.d.cstart, sp.rlo, sp.roff, sp.dlo, sp.doff, T, D);
+    const int dbase = A.d.bdst[b];
+    DestPre pre;
+    if ((int)threadIdx.x < D) {
+        const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * (A.cap >> 3);
+        dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, A.cap, D, dbase, threadIdx.x, pre);
+    }
     const float halpha = 0.5f * A.alpha;
-    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.P, sp.V, sp.S, halpha);
+    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.voff, sp.soff, halpha);
     __syncthreads();
-    const SrcRecords<STAGED> R = make_records<STAGED>(sp, A.s, G, g.cs_f, T, halpha);
+    const SrcRecords<STAGED, 5> R = make_records<STAGED, 5>(sp, A.s, G, g.cs_f, T, halpha);
     const float ih = __fdividef(1.f, g.h_uniform);
     const RatesConst kc = rates_const(g.h_uniform, cubic_fac(A.dim, ih), A.beta, A.eta2, A.eps);
-    const int dbase = A.d.bdst[b];
     if (A.eta2 == 0.f)
-        rates_block<K, XSPH, true, STAGED>(A, g, G, sp, R, kc, D, dbase);
+        rates_block<K, XSPH, true, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
     else
-        rates_block<K, XSPH, false, STAGED>(A, g, G, sp, R, kc, D, dbase);
+        rates_block<K, XSPH, false, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
 }
 
 // ---------------------------------------------------------------------------
@@ -930,6 +1084,7 @@ int brick_layout(const sph_ctx *ctx, const ArraySnap &S, bool rates, bool cells,
     if (!staged) cap = 0;
     size_t off = 0;
     sm->stage_cap = (int)cap;
+    // position records, then (rates) velocity and state records
     off += cap * 16;
     sm->off_v = (int)off;
     if (rates) off += cap * 16;
@@ -943,6 +1098,22 @@ int brick_layout(const sph_ctx *ctx, const ArraySnap &S, bool rates, bool cells,
     sm->off_scell = (int)off; off += sizeof(int) * ncell;
     *bytes = off;
     return staged ? 1 : 0;
+}
+
+BrickRadius brick_radius(const sph_ctx *ctx) {
+    const Grid &g = ctx->grid;
+    BrickRadius r;
+    const double radius = ctx->build_h * g.radius_scale;
+    r.radius2 = radius * radius;
+    const float r2 = (float)r.radius2;
+    r.r2lo = r2 * (1.f - 1e-5f);
+    r.r2hi = r2 * (1.f + 1e-5f);
+    r.r2list = 0.f;
+    if (g.skin > 0.f) {
+        const float rl = (float)radius + g.skin;
+        r.r2list = rl * rl * (1.f + 2e-5f);
+    }
+    return r;
 }
 
 BrickSrcDev make_bsrc(const ArraySnap &S) {
@@ -968,8 +1139,16 @@ BrickDstDev make_bdst(const ArraySnap &D) {
 // most 320 (three blocks of 64-register threads per SM); a brick with more
 // destinations takes them in rounds.
 int brick_threads(const ArraySnap &D) {
+    // environment SPH_BRICK_MAX_THREADS: another ceiling (a multiple of 32
+    // up to 512), to measure it
+    static int ceiling = -1;
+    if (ceiling < 0) {
+        const char *e = getenv("SPH_BRICK_MAX_THREADS");
+        const int v = e ? atoi(e) : 0;
+        ceiling = (v >= 64 && v <= kBrickMaxThreads && v % 32 == 0) ? v : 320;
+    }
     const int want = (std::max(D.b_dmax, 1) + 31) / 32 * 32;
-    return std::min(std::max(want, 64), 320);
+    return std::min(std::max(want, 64), ceiling);
 }
 
 template <class Kern>
@@ -1003,13 +1182,27 @@ void brick_geometry(sph_ctx *ctx) {
     // environment SPH_BRICK_EDGE: the brick edge in cells (3D), to measure
     // other brick sizes
     static int edge = -1;
+    // environment SPH_BRICK_SHAPE=bx,by,bz: a 3D brick shape, to measure it
+    static int shape[3] = {0, 0, 0};
     if (edge < 0) {
         const char *e = getenv("SPH_BRICK_EDGE");
         edge = e ? std::max(1, atoi(e)) : 0;
+        const char *sh = getenv("SPH_BRICK_SHAPE");
+        int a = 0, b = 0, c = 0;
+        if (sh && sscanf(sh, "%d,%d,%d", &a, &b, &c) == 3 && a > 0 && b > 0 && c > 0 && a <= 16 &&
+            b <= 16 && c <= 16) {
+            shape[0] = a; shape[1] = b; shape[2] = c;
+        }
     }
     if (g.kz > 0) {
         const int e = edge > 0 ? edge : (K == 1 ? 3 : (K == 2 ? 5 : 8));
         bk.bx = bk.by = bk.bz = e;
+        // stencil half-width 2: 6 x 5 x 5 cells (1 M-particle lattice, rates
+        // pass 0.276 ms against 0.283 ms with 5^3 cells)
+        if (K == 2 && edge <= 0) bk.bx = 6;
+        if (shape[0] > 0) {
+            bk.bx = shape[0]; bk.by = shape[1]; bk.bz = shape[2];
+        }
     } else if (g.ky > 0) {
         const int e = K == 1 ? 8 : (K == 2 ? 12 : 16);
         bk.bx = bk.by = e;
@@ -1079,6 +1272,7 @@ int brick_density(sph_ctx *ctx, int dst, int src, NbrList &L, bool build, bool w
     BrickDensityArgs a{};
     a.g = ctx->grid;
     a.bk = ctx->bricks;
+    a.rad = brick_radius(ctx);
     a.d = make_bdst(D);
     a.s = make_bsrc(S);
     size_t bytes = 0;
@@ -1130,6 +1324,7 @@ int brick_rates(sph_ctx *ctx, int dst, const sph_source_term &term, NbrList &L,
     BrickRatesArgs a{};
     a.g = ctx->grid;
     a.bk = ctx->bricks;
+    a.rad = brick_radius(ctx);
     a.d = make_bdst(D);
     a.s = make_bsrc(S);
     size_t bytes = 0;

@@ -411,6 +411,15 @@ int sph_batch_pair_counts(sph_batch *b, uint64_t *out) {
     return batch_pair_counts(b, (unsigned long long *)out);
 }
 
+int sph_batch_stats(sph_batch *b, int64_t *out) {
+    if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_stats: null argument");
+    out[0] = b->regrids;
+    out[1] = b->total_cells;
+    out[2] = (int64_t)b->h_steps;
+    out[3] = (int64_t)b->groups.size();
+    return SPH_OK;
+}
+
 int sph_batch_error_word(sph_batch *b, unsigned *out) {
     if (!b || !out) return set_error(SPH_ERR_ARG, "sph_batch_error_word: null argument");
     if (!b->d_err) { *out = 0; return SPH_OK; }

@@ -37,6 +37,7 @@ struct DestDev {
     const int64_t *tag;
     const double *x, *y, *z, *u, *v, *w, *h, *p, *rho, *cs;
     int64_t n;
+    int64_t s0;          // batches: first slot of the launch (slots [s0, n))
 };
 
 struct ListArgs {
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kPairBlock) k_nbrlist(const __grid_constant__ 
 // symmetric lists), kept apart so the other modes carry none of its state.
 template <int KX, bool UH, int MODE>
 __global__ void __launch_bounds__(kPairBlock, (UH && MODE != 2) ? 8 : 1) k_density(const __grid_constant__ DensityArgs A) {
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t s = (MODE == 1 ? A.d.s0 : 0) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n || gated_off(A.gate)) return;
     const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(kPairBlock) k_rates(const __grid_constant__ Ra
     constexpr bool MAY_XSPH = SPEC != 1;
     constexpr bool MAY_BF = SPEC == 0;
     constexpr bool MAY_DRHO = SPEC == 0;
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t s = (MODE == 1 ? A.d.s0 : 0) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= A.d.n || gated_off(A.gate)) return;
     const Grid &g = grid_of<MODE == 1>(A.g, A.d, (int)s);
     DestPos d;
@@ -651,6 +652,7 @@ DestDev make_dest(const ArraySnap &D) {
     d.rho = D.view.rho;
     d.cs = D.view.cs;
     d.n = D.n;
+    d.s0 = 0;
     return d;
 }
 
@@ -1163,17 +1165,23 @@ int batch_density(sph_batch *b) {
     a.p_out = const_cast<double *>(b->view.p);
     a.cs_out = const_cast<double *>(b->view.cs);
     a.st_out = b->snap.st;
-    const int blocks = blocks_for(b->view.n);
+    a.gate = b->d_err;
     const bool uh = b->uniform_h != 0;
-    const int K = r.subdiv;
+    // one launch per group of instances of equal subdivision (their sorted
+    // slots are contiguous)
+    for (const BatchGroup &grp : b->groups) {
+        a.d.s0 = grp.s0;
+        a.d.n = grp.s1;
+        const int blocks = blocks_for(grp.s1 - grp.s0);
 #define BDL(K_) (uh ? k_density<K_, true, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
                     : k_density<K_, false, 1><<<blocks, kPairBlock, 0, b->stream>>>(a))
-    if (K == 1) BDL(1);
-    else if (K == 2) BDL(2);
-    else BDL(3);
+        if (grp.K == 1) BDL(1);
+        else if (grp.K == 2) BDL(2);
+        else BDL(3);
 #undef BDL
-    count_launch();
-    SPH_LAUNCH_CHECK("k_density (batch)");
+        count_launch();
+        SPH_LAUNCH_CHECK("k_density (batch)");
+    }
     return SPH_OK;
 }
 
@@ -1207,22 +1215,26 @@ int batch_rates(sph_batch *b, double *const *acc, double *const *pos) {
         a.acc[c] = acc[c];
         a.pos[c] = pos[c];
     }
-    const int blocks = blocks_for(b->view.n);
+    a.gate = b->d_err;
     int spec = 0;
     if (b->uniform_h) {
         if (r.term.flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC)) spec = 1;
         else if (r.term.flags == (SPH_TERM_PGRAD | SPH_TERM_AVISC | SPH_TERM_XSPH)) spec = 2;
     }
-    const int K = r.subdiv;
+    for (const BatchGroup &grp : b->groups) {
+        a.d.s0 = grp.s0;
+        a.d.n = grp.s1;
+        const int blocks = blocks_for(grp.s1 - grp.s0);
 #define BRL(K_) (spec == 1 ? k_rates<K_, 1, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
                  : spec == 2 ? k_rates<K_, 2, 1><<<blocks, kPairBlock, 0, b->stream>>>(a) \
                              : k_rates<K_, 0, 1><<<blocks, kPairBlock, 0, b->stream>>>(a))
-    if (K == 1) BRL(1);
-    else if (K == 2) BRL(2);
-    else BRL(3);
+        if (grp.K == 1) BRL(1);
+        else if (grp.K == 2) BRL(2);
+        else BRL(3);
 #undef BRL
-    count_launch();
-    SPH_LAUNCH_CHECK("k_rates (batch)");
+        count_launch();
+        SPH_LAUNCH_CHECK("k_rates (batch)");
+    }
     return SPH_OK;
 }
 

@@ -236,6 +236,15 @@ struct sph_ctx {
     unsigned capture_stale_bit = 0;     // stale bit of the light refresh being captured
 };
 
+namespace sphgb {
+// The instances of a batch that share one cell subdivision: their particles
+// occupy the sorted slots [s0, s1) (their cells are laid out group by group)
+struct BatchGroup {
+    int K = 1;
+    int64_t s0 = 0, s1 = 0;
+};
+}  // namespace sphgb
+
 struct sph_batch {
     cudaStream_t stream = nullptr;
     sph_ctx *ctx = nullptr;      // stream + scan scratch for the shared launchers
@@ -258,6 +267,23 @@ struct sph_batch {
     cudaGraphExec_t graph_exec = nullptr;
     int graph_kernels = 0;       // kernel nodes of one replay
     bool ready = false;
+    // per-instance cell subdivision, the groups of equal subdivision and the
+    // regions: a particle that leaves its instance's region stops the step
+    // (every state-writing launch is gated on the error word), the regions
+    // are re-derived from the current extents grown by margin and the step
+    // is repeated
+    std::vector<int> inst_subdiv;
+    std::vector<int> h_uniform_inst;         // 1: the instance's h is uniform
+    std::vector<double> inst_cell;           // reference cell size per instance
+    std::vector<int64_t> inst_off;           // instance offsets (ninst + 1)
+    std::vector<sphgb::BatchGroup> groups;
+    double margin = 1.0;
+    int64_t cell_cap = 0;                    // allocated cell-table entries
+    int64_t *d_off = nullptr;                // instance offsets on the device
+    double *d_ibox = nullptr;                // per-instance box (6 doubles)
+    unsigned long long *d_steps = nullptr;   // completed steps
+    unsigned long long h_steps = 0;
+    long long regrids = 0;
 };
 
 namespace sphgb {
@@ -408,6 +434,8 @@ struct CSum {
         lo = lo + olo + err;
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    // the sum rounded to FP32
+    __device__ __forceinline__ float fvalue() const { return hi + lo; }
 };
 
 // cubic spline normalisation for h = 1 (base/kernels.pyx:437-443)

@@ -41,7 +41,7 @@ EXPORTS = (
     "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
     "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
     "sph_batch_sync", "sph_batch_error_word", "sph_batch_stream",
-    "sph_batch_pair_counts", "sph_ctx_set_skin", "sph_nnps_update", "sph_nnps_stats",
+    "sph_batch_pair_counts", "sph_batch_stats", "sph_ctx_set_skin", "sph_nnps_update", "sph_nnps_stats",
     "sph_ctx_set_symmetric", "sph_ctx_set_periodic", "sph_ctx_set_deferred",
     "sph_nnps_deferred_stats", "sph_ctx_set_bricks", "sph_pair_pass_stats",
     "sph_step_begin", "sph_step_end", "sph_step_run", "sph_step_stats", "sph_step_destroy",
@@ -105,14 +105,15 @@ class AxpyLine(ctypes.Structure):
 class BatchInstance(ctypes.Structure):
     _fields_ = [("offset", ctypes.c_int64), ("n", ctypes.c_int64),
                 ("cell_size", ctypes.c_double), ("lo", ctypes.c_double * 3),
-                ("hi", ctypes.c_double * 3), ("uniform_h", ctypes.c_int)]
+                ("hi", ctypes.c_double * 3), ("uniform_h", ctypes.c_int),
+                ("subdiv", ctypes.c_int)]
 
 
 class BatchRecipe(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int), ("subdiv", ctypes.c_int), ("scheme", ctypes.c_int),
                 ("list_cap", ctypes.c_int), ("radius_scale", ctypes.c_double),
                 ("dt", ctypes.c_double), ("density", DensityParams), ("term", SourceTerm),
-                ("rates", RatesParams)]
+                ("rates", RatesParams), ("margin", ctypes.c_double)]
 
 
 SPH_EFLAG_JUMP = 1
@@ -180,6 +181,7 @@ def load_library(build_if_missing=True):
         L.sph_batch_stream.argtypes = [vp, P(vp)]
         L.sph_batch_pair_counts.argtypes = [vp, P(ctypes.c_uint64)]
         L.sph_batch_error_word.argtypes = [vp, P(ctypes.c_uint32)]
+        L.sph_batch_stats.argtypes = [vp, P(ctypes.c_int64)]
         L.sph_density.argtypes = [vp, i32, P(i32), i32, P(DensityParams), vp, vp, vp]
         L.sph_rates.argtypes = [vp, i32, P(SourceTerm), i32, P(RatesParams), P(vp), P(vp), i32]
         L.sph_tait.argtypes = [vp, i64, vp, vp, d, d, d, vp, vp]

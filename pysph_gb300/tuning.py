@@ -60,8 +60,13 @@ def step_graphs(nparticles=0):
     return nparticles < GRAPH_MAX_PARTICLES
 
 
-# measured defaults: (dimensions with extent) -> subdivision
+# measured defaults: (dimensions with extent) -> subdivision; with the
+# brick-staged passes (one uniform h) the 3D optimum is 2 (1 M-particle
+# lattice, RK2 step: 1.05 ms at subdivision 2 with 6 x 5 x 5-cell bricks
+# against 1.10 ms at 3 with 8^3-cell bricks), for the list-streaming
+# passes 3
 DEFAULT_SUBDIVISION = {1: 1, 2: 2, 3: 3}
+DEFAULT_SUBDIVISION_BRICKS = {1: 1, 2: 2, 3: 2}
 # neighbour-list entries hold the source slot in 32 - code bits (three
 # fields of 2 bits at subdivision 1, of 3 bits at 3; at subdivision 2 three
 # 3-bit fields up to 2^23 particles, above that the offset in base 5 in 7
@@ -84,7 +89,14 @@ def choose_subdivision(cell_manager):
             t = pa.get_device(c)
             if t.numel() and float(t.max() - t.min()) > 0:
                 dims = max(dims, k)
-    sub = DEFAULT_SUBDIVISION[dims]
+    table = DEFAULT_SUBDIVISION
+    if brick_passes():
+        hs = [pa.get_device("h") for pa in cell_manager.arrays_to_bin
+              if pa.get_number_of_particles() > 0]
+        if hs and all(float(h.max()) == float(h.min()) for h in hs) and \
+                len({float(h[0]) for h in hs}) == 1:
+            table = DEFAULT_SUBDIVISION_BRICKS
+    sub = table[dims]
     nmax = max((pa.get_number_of_particles() for pa in cell_manager.arrays_to_bin), default=0)
     while sub > 1 and nmax >= MAX_PARTICLES[sub]:
         sub -= 1
@@ -107,15 +119,56 @@ def time_batch_steps(batch, steps):
     return a.elapsed_time(b)
 
 
-def autotune_batch(instances, candidates=(1, 2, 3), steps=5, **recipe):
-    """Pick the cell subdivision of a batch by timing every candidate on the
-    batch itself.  Returns ``(best_subdiv, {subdiv: ms_per_step})``."""
+def autotune_batch(instances, candidates=(1, 2, 3), steps=5, count_bins=3, dx_bins=2,
+                   **recipe):
+    """Choose each instance's cell subdivision by timing.
+
+    The instances are binned by particle count (``count_bins`` bins of
+    equal membership over the sorted counts) and, within a count bin, by
+    resolution (``dx_bins`` bins over their smoothing lengths).  Every bin's
+    instances are timed as a batch of their own at each candidate
+    subdivision (``steps`` graph steps after the capture), and every
+    instance gets its bin's fastest.  The whole batch is timed too, at each
+    candidate for all instances and with the per-bin choices; the fastest
+    of these is returned.  Returns ``(subdivs, report)``: one subdivision
+    per instance and the timings (ms per step)."""
     from .batch import SimulationBatch
     import copy
-    timings = {}
-    for sub in candidates:
-        b = SimulationBatch(copy.deepcopy(instances), subdiv=sub, **recipe)
-        timings[sub] = time_batch_steps(b, steps) / steps
+    import numpy as np
+    n = np.array([len(p["x"]) for p in instances])
+    h = np.array([float(np.max(p["h"])) for p in instances])
+    order = np.argsort(n, kind="stable")
+    bins = []
+    for cb in np.array_split(order, max(1, min(count_bins, len(order)))):
+        if len(cb) == 0:
+            continue
+        hb = cb[np.argsort(h[cb], kind="stable")]
+        for db in np.array_split(hb, max(1, min(dx_bins, len(hb)))):
+            if len(db):
+                bins.append(sorted(int(i) for i in db))
+
+    def timed(insts, sub):
+        b = SimulationBatch(copy.deepcopy(insts), subdiv=sub, **recipe)
+        ms = time_batch_steps(b, steps) / steps
         del b
-    best = min(timings, key=timings.get)
-    return best, timings
+        return ms
+
+    choice = [candidates[0]] * len(instances)
+    per_bin = []
+    for members in bins:
+        sub_insts = [instances[i] for i in members]
+        t = {sub: timed(sub_insts, sub) for sub in candidates}
+        best = min(t, key=t.get)
+        for i in members:
+            choice[i] = best
+        per_bin.append({"instances": len(members), "particles": int(n[members].sum()),
+                        "ms_per_step": t, "subdiv": best})
+    whole = {str(sub): timed(instances, sub) for sub in candidates}
+    whole["per_instance"] = timed(instances, choice)
+    best_uniform = min(candidates, key=lambda c: whole[str(c)])
+    if whole[str(best_uniform)] < whole["per_instance"]:
+        choice = [best_uniform] * len(instances)
+    report = {"bins": per_bin, "whole_batch_ms_per_step": whole,
+              "chosen": "per_instance" if len(set(choice)) > 1 or
+                        whole["per_instance"] <= whole[str(best_uniform)] else str(best_uniform)}
+    return choice, report

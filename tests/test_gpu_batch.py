@@ -121,3 +121,60 @@ def test_batch_staged_transfers_match_set_and_get():
             assert np.array_equal(x, y), p
     with pytest.raises(ValueError):
         batch.upload(q=np.zeros(batch.n))
+
+
+@pytest.mark.parametrize("integrator", ["euler", "rk2"])
+def test_batch_regions_follow_the_instances(integrator):
+    """Regions re-derived as the drops deform (a small margin: several
+    re-derivations, each after a step stopped on the device and repeated)
+    give the same trajectories, bit for bit, as regions that never change
+    (cell boundaries, and so the sorted order and the neighbour order, do
+    not depend on the region)."""
+    _need_gpu()
+    drops = _drops(4, seed=5)
+    kw = dict(dim=2, dt=1e-5, co=100.0, integrator=integrator)
+    moving = SimulationBatch(drops, margin=0.01, **kw)
+    fixed = SimulationBatch(drops, margin=2.0, **kw)
+    for _ in range(4):
+        moving.step(15)
+        fixed.step(15)
+    st = moving.stats()
+    assert st["regrids"] >= 1 and st["steps"] == 60, st
+    assert fixed.stats()["regrids"] == 0
+    assert st["cells"] < fixed.stats()["cells"]
+    for p in ("x", "y", "u", "v", "rho", "p"):
+        np.testing.assert_array_equal(moving.get_all(p), fixed.get_all(p), err_msg=p)
+
+
+def test_batch_per_instance_subdivisions():
+    """Instances with cell subdivisions 1, 2 and 3 in one batch (one pair
+    launch per group) against the same drops run one by one."""
+    _need_gpu()
+    drops = _drops(6, seed=6)
+    subdiv = [3, 1, 2, 1, 3, 2]
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0, subdiv=subdiv)
+    assert batch.stats()["groups"] == 3
+    batch.step(4)
+    for k, props in enumerate(drops):
+        s, particles = W.setup_drop(API, props, c0=100.0)
+        for _ in range(4):
+            s.integrator.integrate(1e-5)
+        pa = particles.arrays[0]
+        for p in ("x", "y", "u", "v"):
+            assert normwise(batch.get(k, p) - props[p], pa.get(p) - props[p]) < TOL, (k, p)
+        for p in ("rho", "p"):
+            assert normwise(batch.get(k, p), pa.get(p)) < TOL, (k, p)
+    with pytest.raises(ValueError):
+        SimulationBatch(drops, dim=2, dt=1e-5, co=100.0, subdiv=[1, 2])
+
+
+def test_autotune_chooses_per_instance():
+    _need_gpu()
+    from pysph_gb300 import tuning
+    drops = _drops(12, seed=7)
+    choice, report = tuning.autotune_batch(drops, steps=2, dim=2, dt=1e-5, co=100.0)
+    assert len(choice) == 12 and set(choice) <= {1, 2, 3}
+    assert report["bins"] and "per_instance" in report["whole_batch_ms_per_step"]
+    batch = SimulationBatch(drops, dim=2, dt=1e-5, co=100.0, subdiv=choice)
+    batch.step(2)
+    batch.check()

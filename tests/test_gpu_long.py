@@ -86,9 +86,11 @@ def test_dam_break_2000_steps_vs_oracle():
     for r in rows:
         print("  %5d  %.2e | %.2e   %.2e | %.2e   %.2e | %.2e" % r)
     for k, r_g, r_p, p_g, p_p, k_g, k_p in rows:
-        if k <= 250:
+        if k <= 100:
             # before the chaotic growth: the FP32 run follows the FP64 one
-            assert r_g < 1e-4 and p_g < 1e-6 and k_g < 1e-4, (k, r_g, p_g, k_g)
+            # (by step 250 the FP64 run perturbed by 1e-7 already differs by
+            # 8e-4 in density)
+            assert r_g < 1e-5 and p_g < 1e-6 and k_g < 1e-4, (k, r_g, p_g, k_g)
         # density: within the spread of the perturbed FP64 run
         assert r_g <= max(10.0 * r_p, 1e-3), (k, r_g, r_p)
         # momentum and kinetic energy stay within a few per cent of the
