@@ -1130,9 +1130,11 @@ def run_gpu_small(args):
     """Wall-clock and device time per step of the small single-simulation
     configurations, their steps replayed as one CUDA graph each (the default
     below 500 000 particles) and run call by call (PYSPH_GB300_GRAPHS=0).
-    Device time: CUDA events around the timed steps on the stream the steps
-    run on, i.e. the device timeline including any idle gaps the host
-    leaves; device-bound means wall ~ device."""
+    device_ms_per_step: CUDA events around the timed steps on the stream the
+    steps run on (the device timeline, idle gaps the host leaves included);
+    replay_device_ms_per_step: CUDA events around each graph launch, the
+    device's own time for a replayed step -- a step is device-bound when the
+    wall time per step approaches it."""
     import torch
 
     import pysph_gb300
@@ -1166,6 +1168,7 @@ def run_gpu_small(args):
             for _ in range(args.warmup + 2):
                 integ.integrate(dt)
             torch.cuda.synchronize()
+            st0 = integ.step_stats() or {}
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             l0 = native.launch_count()
@@ -1177,11 +1180,20 @@ def run_gpu_small(args):
             b.synchronize()
             wall = (time.perf_counter() - t0) / args.steps * 1e3
             dev = a.elapsed_time(b) / args.steps
+            st1 = integ.step_stats() or {}
             row["particles"] = n
             row[mode] = {"wall_ms_per_step": wall, "device_ms_per_step": dev,
                          "steps_per_s": 1e3 / wall,
                          "launches_per_step": (native.launch_count() - l0) / args.steps,
-                         "step_graphs": integ.step_stats()}
+                         "list_skin": particles.cell_manager.list_skin(),
+                         "step_graphs": st1 or None}
+            g = st1.get("graph_steps", 0) - st0.get("graph_steps", 0)
+            if g > 0:
+                # device time of a replayed step: CUDA events around each
+                # graph launch (no host work inside a graph)
+                row[mode]["timed_graph_steps"] = g
+                row[mode]["replay_device_ms_per_step"] = (
+                    (st1["replay_device_us"] - st0.get("replay_device_us", 0)) / g / 1e3)
         os.environ.pop("PYSPH_GB300_GRAPHS", None)
         row["speedup_graphs"] = row["calls"]["wall_ms_per_step"] / row["graphs"]["wall_ms_per_step"]
         out.append(row)

@@ -233,7 +233,8 @@ int sph_step_end(sph_ctx *ctx, sph_step **out);
 int sph_step_run(sph_step *step, int nsteps);
 /* out[0] graph replays, out[1] eager steps, out[2] steps resumed after a
  * stale refresh, out[3] graph captures, out[4] recorded calls, out[5]
- * kernels of one replay. */
+ * kernels of one replay, out[6] device time of all replays in microseconds
+ * (CUDA events around each graph launch). */
 int sph_step_stats(sph_step *step, int64_t *out);
 int sph_step_destroy(sph_step *step);
 

@@ -151,8 +151,7 @@ class CellManager:
             dim = 3
             h = ctypes.c_void_p()
             native.check(L.sph_ctx_create(dim, ctypes.byref(h)), "sph_ctx_create")
-            from ..tuning import list_skin
-            native.check(L.sph_ctx_set_skin(h, list_skin()), "sph_ctx_set_skin")
+            native.check(L.sph_ctx_set_skin(h, self.list_skin()), "sph_ctx_set_skin")
             native.check(L.sph_ctx_set_symmetric(h, 1 if self.symmetric else 0),
                          "sph_ctx_set_symmetric")
             dom = self.periodic_domain
@@ -177,6 +176,21 @@ class CellManager:
             if self._ctx is not None:
                 native.check(native.lib().sph_ctx_set_symmetric(self._ctx, 1 if on else 0),
                              "sph_ctx_set_symmetric")
+
+    def set_skin(self, fraction):
+        """Neighbour-list skin as a fraction of the search radius, from the
+        next update on (which builds afresh)."""
+        self.skin = float(fraction)
+        if self._ctx is not None:
+            native.check(native.lib().sph_ctx_set_skin(self._ctx, self.skin), "sph_ctx_set_skin")
+
+    def list_skin(self):
+        """The neighbour-list skin in effect."""
+        s = getattr(self, "skin", None)
+        if s is None:
+            from ..tuning import list_skin
+            s = self.skin = list_skin()
+        return s
 
     def set_deferred_check(self, on):
         """Let updates return before the device has checked a light refresh

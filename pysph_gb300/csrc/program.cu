@@ -73,6 +73,9 @@ struct sph_step {
     // host state of the context after a captured step (restored after a replay)
     std::vector<bool> st_fresh;
     cudaEvent_t done = nullptr;
+    // device time of the replays (CUDA events around each graph launch)
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    double replay_us = 0.0;
     // the stream of the steps when the context's is the legacy default
     // stream (which cannot be captured); a blocking stream, so it is ordered
     // with the default stream's work
@@ -85,6 +88,7 @@ struct sph_step {
     int lifetime = 0;              // whole-step replays of the current graph
     bool judged = true;            // the last graph's lifetime was taken into account
     int backoff = 0, skip = 0;
+    double skin = -1.0;            // the list skin the back-off was learnt with
 };
 
 namespace sphgb {
@@ -240,9 +244,14 @@ int capture(sph_step *s) {
 // One step as a graph launch; resumes eagerly after a stale light refresh.
 int replay(sph_step *s) {
     sph_ctx *ctx = s->ctx;
+    SPH_CUDA(cudaEventRecord(s->t0, ctx->stream));
     SPH_CUDA(cudaGraphLaunch(s->exec, ctx->stream));
-    SPH_CUDA(cudaEventRecord(s->done, ctx->stream));
-    SPH_CUDA(cudaEventSynchronize(s->done));
+    SPH_CUDA(cudaEventRecord(s->t1, ctx->stream));
+    SPH_CUDA(cudaEventSynchronize(s->t1));
+    {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->t0, s->t1) == cudaSuccess) s->replay_us += 1e3 * ms;
+    }
     count_launch(s->launches);
     ctx->n_brick_passes += s->passes;
     for (size_t a = 0; a < ctx->arrays.size() && a < s->st_fresh.size(); ++a)
@@ -384,8 +393,12 @@ int sph_step_begin(sph_ctx *ctx) {
     if (ctx->recording) return set_error(SPH_ERR_STATE, "sph_step_begin: already recording");
     sph_step *s = new (std::nothrow) sph_step();
     if (!s) return set_error(SPH_ERR_ARG, "sph_step_begin: out of host memory");
-    const cudaError_t e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
+    cudaError_t e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->t1);
     if (e != cudaSuccess) {
+        if (s->done) cudaEventDestroy(s->done);
+        if (s->t0) cudaEventDestroy(s->t0);
         delete s;
         return cuda_check(e, "sph_step_begin");
     }
@@ -426,6 +439,12 @@ int run_steps(sph_step *s, int nsteps) {
     sph_ctx *ctx = s->ctx;
     for (int k = 0; k < nsteps; ++k) {
         int rc;
+        // another list skin is another regime: forget the back-off
+        if (ctx->skin_frac != s->skin) {
+            s->skin = ctx->skin_frac;
+            s->backoff = s->skip = 0;
+            s->judged = true;
+        }
         // a graph (or its capture) starts from a resolved neighbour update;
         // eager steps leave a pending refresh to their first pass
         if (ctx->pending && (s->settled || (s->exec && s->graph_build == ctx->build_id))) {
@@ -455,7 +474,7 @@ int run_steps(sph_step *s, int nsteps) {
             }
         }
         const long long full0 = ctx->n_full;
-        if (s->exec && s->graph_build == ctx->build_id && !ctx->pending) {
+        if (s->exec && s->graph_build == ctx->build_id && ctx->built && !ctx->pending) {
             rc = replay(s);
         } else {
             rc = run_eager(s, 0);
@@ -481,6 +500,7 @@ int sph_step_stats(sph_step *s, int64_t *out) {
     out[3] = s->n_captures;
     out[4] = (int64_t)s->ops.size();
     out[5] = s->launches;
+    out[6] = (int64_t)(s->replay_us + 0.5);
     return SPH_OK;
 }
 
@@ -489,6 +509,8 @@ int sph_step_destroy(sph_step *s) {
     if (s->ctx && s->ctx->recording == s) s->ctx->recording = nullptr;
     drop_graph(s);
     if (s->done) cudaEventDestroy(s->done);
+    if (s->t0) cudaEventDestroy(s->t0);
+    if (s->t1) cudaEventDestroy(s->t1);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SPH_OK;

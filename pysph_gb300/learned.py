@@ -405,6 +405,8 @@ class GuardedRunner:
 
     def __init__(self, solver, particles, closure, k=10, tol=1e-3, check_every=1, cooldown=4):
         self.integ = solver.integrator
+        # a re-run window must repeat the run it checks: no skin changes
+        self.integ.skin_frozen = True
         self.particles = particles
         self.closure = closure
         self.k = int(k)

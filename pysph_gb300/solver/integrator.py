@@ -436,9 +436,36 @@ class Integrator:
                 self._replay = rp
                 rp.run()
                 self._steps_done += 1
+                self._adapt_skin()
                 return
         self._integrate(dt)
         self._steps_done += 1
+        self._adapt_skin()
+
+    def _adapt_skin(self):
+        """Grow the neighbour-list skin of a small simulation whose lists go
+        stale at most updates (``tuning.adaptive_skin``): every
+        SKIN_WINDOW steps, while more than half of the window's updates were
+        full builds, the skin doubles (up to SKIN_MAX)."""
+        from .. import tuning
+        if (self._steps_done % tuning.SKIN_WINDOW != 0 or getattr(self, "skin_frozen", False)
+                or not torch.cuda.is_available()):
+            return
+        cm = getattr(self.particles, "cell_manager", None)
+        if cm is None or cm._ctx is None:
+            return
+        n = sum(pa.get_number_of_particles() for pa in self.particles.arrays)
+        if not tuning.adaptive_skin(n):
+            return
+        full, light = cm.build_stats()
+        last = getattr(self, "_skin_window", None)
+        self._skin_window = (full, light)
+        if last is None:
+            return
+        df, dl = full - last[0], light - last[1]
+        skin = cm.list_skin()
+        if df + dl > 0 and df > 0.5 * (df + dl) and 0.0 < skin < tuning.SKIN_MAX:
+            cm.set_skin(min(tuning.SKIN_MAX, 2.0 * skin))
 
     def _may_record(self):
         from ..tuning import step_graphs
@@ -717,10 +744,11 @@ class StepReplay:
 
     def stats(self):
         from .. import native
-        out = (ctypes.c_int64 * 6)()
+        out = (ctypes.c_int64 * 7)()
         native.check(native.lib().sph_step_stats(self.handle, out), "sph_step_stats")
         return {"graph_steps": out[0], "eager_steps": out[1], "resumed_steps": out[2],
-                "captures": out[3], "calls": out[4], "kernels_per_replay": out[5]}
+                "captures": out[3], "calls": out[4], "kernels_per_replay": out[5],
+                "replay_device_us": out[6]}
 
     def close(self):
         from .. import native

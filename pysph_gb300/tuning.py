@@ -18,6 +18,22 @@ import os
 DEFAULT_SKIN = 0.03
 
 
+# small simulations whose lists go stale at most updates (the motion of a
+# step reaches half the skin): every SKIN_WINDOW steps the skin doubles, up
+# to SKIN_MAX, while more than half of the window's updates were full builds
+# -- longer-lived lists let a recorded step replay as one graph, and below
+# GRAPH_MAX_PARTICLES the launches, not the longer lists, bound a step
+SKIN_WINDOW = 16
+SKIN_MAX = 0.24
+
+
+def adaptive_skin(nparticles):
+    """Whether the integrators may grow the list skin: no PYSPH_GB300_SKIN
+    set, fewer than GRAPH_MAX_PARTICLES particles (whether or not steps are
+    replayed as graphs, so both ways take the same steps)."""
+    return os.environ.get("PYSPH_GB300_SKIN") is None and nparticles < GRAPH_MAX_PARTICLES
+
+
 def list_skin():
     env = os.environ.get("PYSPH_GB300_SKIN")
     if env is not None:

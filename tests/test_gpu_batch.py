@@ -135,11 +135,13 @@ def test_batch_regions_follow_the_instances(integrator):
     kw = dict(dim=2, dt=1e-5, co=100.0, integrator=integrator)
     moving = SimulationBatch(drops, margin=0.01, **kw)
     fixed = SimulationBatch(drops, margin=2.0, **kw)
-    for _ in range(4):
-        moving.step(15)
-        fixed.step(15)
+    # the edges move by up to ~1e-3 per step: past the four cells of
+    # padding within a few hundred steps
+    for _ in range(8):
+        moving.step(75)
+        fixed.step(75)
     st = moving.stats()
-    assert st["regrids"] >= 1 and st["steps"] == 60, st
+    assert st["regrids"] >= 1 and st["steps"] == 600, st
     assert fixed.stats()["regrids"] == 0
     assert st["cells"] < fixed.stats()["cells"]
     for p in ("x", "y", "u", "v", "rho", "p"):
