@@ -178,11 +178,14 @@ class CellManager:
                              "sph_ctx_set_symmetric")
 
     def set_skin(self, fraction):
-        """Neighbour-list skin as a fraction of the search radius, from the
-        next update on (which builds afresh)."""
+        """Neighbour-list skin as a fraction of the search radius.  With a
+        structure already built, a full build with the new skin follows at
+        once (from the current positions), so every later call finds one."""
         self.skin = float(fraction)
         if self._ctx is not None:
             native.check(native.lib().sph_ctx_set_skin(self._ctx, self.skin), "sph_ctx_set_skin")
+            if getattr(self, "_views", None) is not None:
+                self.rebuild()
 
     def list_skin(self):
         """The neighbour-list skin in effect."""

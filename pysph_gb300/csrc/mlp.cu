@@ -28,10 +28,12 @@
 //   k_mlp_l3    third-layer gradients (FP32 CUDA cores).
 //   k_mlp_reduce  fixed-order sum of the per-CTA partial gradients.
 //   k_mlp_adam  Adam on the FP32 master parameters and the BF16 copies.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
 
 #include "sph_internal.cuh"
@@ -374,6 +376,326 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tbase, F_TMEM_COLS);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward, warp-specialised: tiles and weights brought in by the tensor
+// memory access unit (TMA) into 128-byte-swizzled shared memory, two sample
+// tiles in flight, the first layer's accumulator double-buffered in tensor
+// memory so that a tile's first product runs while the previous tile's
+// epilogues do
+// ---------------------------------------------------------------------------
+// Shared memory, from a 1024-byte aligned base: operands in the canonical
+// K-major layout with 128-byte swizzling, in atoms of 128 rows x 64 BF16
+// (16 KB; the box one TMA load writes): W1 3 atoms (K = 192), W2 2, X two
+// stages of 3, H1 2 (written by the epilogue in the same layout).
+constexpr uint32_t ATOM = 128 * 128;
+constexpr uint32_t G_W1 = 0;
+constexpr uint32_t G_W2 = G_W1 + 3 * ATOM;
+constexpr uint32_t G_X = G_W2 + 2 * ATOM;
+constexpr uint32_t G_H1 = G_X + 2 * 3 * ATOM;
+constexpr uint32_t G_B1 = G_H1 + 2 * ATOM;          // float [128]
+constexpr uint32_t G_B2 = G_B1 + NH * 4;            // float [128]
+constexpr uint32_t G_W3 = G_B2 + NH * 4;            // float [2][128]
+constexpr uint32_t G_B3 = G_W3 + NOUT * NH * 4;     // float [2] (+pad)
+// epilogue warps: four per lane quarter of the accumulators, each a quarter
+// of the columns (four warps per scheduler to hide the epilogue's latency)
+constexpr int G_EPI = 16;
+constexpr int G_COLS = NH / (G_EPI / 4);            // 32 columns per epilogue warp
+constexpr uint32_t G_YP = G_B3 + 16;                // float2 [2 tile parities][4 parts][128]
+constexpr uint32_t G_BAR = G_YP + 2 * (G_EPI / 4) * TILE * 8;
+// mbarriers: weights; X stage full / empty; first accumulator full / empty
+// (two each); H1 full / empty; second accumulator full / empty; output
+// partials of both column halves written (two, by tile parity)
+enum GBar { GB_W = 0, GB_XF0, GB_XF1, GB_XE0, GB_XE1, GB_A1F0, GB_A1F1, GB_A1E0, GB_A1E1,
+            GB_HF, GB_HE, GB_A2F, GB_A2E, GB_Y0, GB_Y1, GB_N };
+constexpr uint32_t G_SLOT = G_BAR + GB_N * 8;        // tensor-memory address
+constexpr uint32_t G_ABORT = G_SLOT + 4;            // a bounded wait gave up
+constexpr uint32_t G_END = G_ABORT + 4;
+constexpr uint32_t G_BYTES = G_END + 1024;          // + alignment of the base
+constexpr int G_THREADS = 32 * (2 + G_EPI);        // producer, MMA, 16 epilogue warps
+constexpr uint32_t G_TMEM_COLS = 512;               // acc1 at 0 and 128, acc2 at 256
+constexpr uint32_t G_XBYTES = 3 * ATOM;
+
+// Shared-memory matrix descriptor, K-major with 128-byte swizzling: start
+// address >> 4, leading offset 16 B (unused for swizzled K-major), stride
+// offset 1024 B (eight 128-byte rows), version 1 (bit 46), swizzle mode 2
+// (bits 61-63).  A K step of 16 BF16 advances the start by 32 B within an
+// atom.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+// 2D tile load (x = column in elements, a multiple of 64, y = row) into
+// shared memory, completing on the mbarrier's transaction count.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t mbar,
+                                            int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(mbar), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Bounded wait that also gives up when another role has (the abort word).
+__device__ __forceinline__ bool gwait(uint32_t mbar, uint32_t parity, volatile int *abort) {
+    for (int it = 0; it < kMaxSpin; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255) == 255 && *abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+// Byte offset of the 16-byte chunk (row r, columns 8c .. 8c + 7) of a
+// 128-byte-swizzled atom.
+__device__ __forceinline__ uint32_t sw128_off(int r, int c) {
+    return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4));
+}
+
+struct MlpMaps {
+    CUtensorMap x, w1, w2;
+};
+
+__global__ void __launch_bounds__(G_THREADS, 1)
+    k_mlp_fwd_tma(const __grid_constant__ MlpMaps maps, const float *__restrict__ params,
+                  const uint16_t *__restrict__ w3b, int64_t n, float *__restrict__ y,
+                  float *__restrict__ z1s, float *__restrict__ z2s, uint16_t *__restrict__ h1s,
+                  uint16_t *__restrict__ h2s, unsigned *err) {
+    extern __shared__ __align__(1024) uint8_t gsm_raw[];
+    const uint32_t raw = smem_u32(gsm_raw);
+    uint8_t *sm = gsm_raw + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t sbase = smem_u32(sm);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    float *b1f = reinterpret_cast<float *>(sm + G_B1);
+    float *b2f = reinterpret_cast<float *>(sm + G_B2);
+    float *w3f = reinterpret_cast<float *>(sm + G_W3);
+    float *b3f = reinterpret_cast<float *>(sm + G_B3);
+    float2 *yp = reinterpret_cast<float2 *>(sm + G_YP);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + G_SLOT);
+    volatile int *abort = reinterpret_cast<volatile int *>(sm + G_ABORT);
+    auto bar = [&](int i) { return sbase + G_BAR + 8u * (uint32_t)i; };
+
+    for (int i = t; i < NH; i += G_THREADS) {
+        b1f[i] = params[OFF_B1 + i];
+        b2f[i] = params[OFF_B2 + i];
+    }
+    for (int i = t; i < NOUT * NH; i += G_THREADS) w3f[i] = __uint_as_float((uint32_t)w3b[i] << 16);
+    if (t < NOUT) b3f[t] = params[OFF_B3 + t];
+    if (t == 0) {
+        *abort = 0;
+        mbar_init(bar(GB_W), 1);
+        mbar_init(bar(GB_XF0), 1);
+        mbar_init(bar(GB_XF1), 1);
+        mbar_init(bar(GB_XE0), 1);
+        mbar_init(bar(GB_XE1), 1);
+        mbar_init(bar(GB_A1F0), 1);
+        mbar_init(bar(GB_A1F1), 1);
+        mbar_init(bar(GB_A1E0), G_EPI);
+        mbar_init(bar(GB_A1E1), G_EPI);
+        mbar_init(bar(GB_HF), G_EPI);
+        mbar_init(bar(GB_HE), 1);
+        mbar_init(bar(GB_A2F), 1);
+        mbar_init(bar(GB_A2E), G_EPI);
+        mbar_init(bar(GB_Y0), G_EPI);
+        mbar_init(bar(GB_Y1), G_EPI);
+    }
+    if (warp == 0) tmem_alloc(smem_u32(slot), G_TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *slot;
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    // this CTA's tiles: blockIdx.x, + gridDim.x, ...
+    const int mine = ntiles > blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+
+    if (warp == 0) {
+        // producer: weights once, then the sample tiles through two stages
+        if (lane == 0) {
+            mbar_expect_tx(bar(GB_W), 5 * ATOM);
+            for (int a = 0; a < 3; ++a) tma_load_2d(sbase + G_W1 + a * ATOM, &maps.w1, bar(GB_W), 64 * a, 0);
+            for (int a = 0; a < 2; ++a) tma_load_2d(sbase + G_W2 + a * ATOM, &maps.w2, bar(GB_W), 64 * a, 0);
+            for (int i = 0; i < mine; ++i) {
+                const int s = i & 1;
+                if (!gwait(bar(GB_XE0 + s), ((i >> 1) + 1) & 1, abort)) break;
+                const int row0 = (int)((blockIdx.x + (int64_t)i * gridDim.x) * TILE);
+                mbar_expect_tx(bar(GB_XF0 + s), G_XBYTES);
+                for (int a = 0; a < 3; ++a)
+                    tma_load_2d(sbase + G_X + (s * 3 + a) * ATOM, &maps.x, bar(GB_XF0 + s), 64 * a, row0);
+            }
+            // every load issued has landed before the CTA may exit
+            for (int i = (mine > 2 ? mine - 2 : 0); i < mine; ++i)
+                gwait(bar(GB_XF0 + (i & 1)), (i >> 1) & 1, abort);
+            gwait(bar(GB_W), 0, abort);
+        }
+    } else if (warp == 1) {
+        // MMA issue: the first layer of tile i + 1 before the second of tile i
+        if (lane == 0) {
+            constexpr uint32_t ID = idesc_bf16(128, NH);
+            bool ok = gwait(bar(GB_W), 0, abort);
+            auto first_layer = [&](int i) -> bool {
+                const int s = i & 1;
+                if (!gwait(bar(GB_XF0 + s), (i >> 1) & 1, abort)) return false;
+                if (!gwait(bar(GB_A1E0 + s), ((i >> 1) + 1) & 1, abort)) return false;
+                tc_fence_after();
+#pragma unroll
+                for (int k = 0; k < NIN / 16; ++k) {
+                    const uint32_t a = sbase + G_X + (s * 3 + (k >> 2)) * ATOM + (k & 3) * 32;
+                    const uint32_t b = sbase + G_W1 + (k >> 2) * ATOM + (k & 3) * 32;
+                    mma_bf16(tbase + s * 128, sdesc_sw128(a), sdesc_sw128(b), ID, k > 0);
+                }
+                mma_commit(bar(GB_XE0 + s));
+                mma_commit(bar(GB_A1F0 + s));
+                return true;
+            };
+            if (ok && mine > 0) ok = first_layer(0);
+            for (int i = 0; ok && i < mine; ++i) {
+                if (i + 1 < mine && !first_layer(i + 1)) break;
+                if (!gwait(bar(GB_HF), i & 1, abort)) break;
+                if (!gwait(bar(GB_A2E), (i + 1) & 1, abort)) break;
+                tc_fence_after();
+#pragma unroll
+                for (int k = 0; k < NH / 16; ++k) {
+                    const uint32_t a = sbase + G_H1 + (k >> 2) * ATOM + (k & 3) * 32;
+                    const uint32_t b = sbase + G_W2 + (k >> 2) * ATOM + (k & 3) * 32;
+                    mma_bf16(tbase + 256, sdesc_sw128(a), sdesc_sw128(b), ID, k > 0);
+                }
+                mma_commit(bar(GB_HE));
+                mma_commit(bar(GB_A2F));
+            }
+        }
+    } else {
+        // epilogues: lane quarter q of the accumulators, column part hf
+        const int q = warp & 3, hf = (warp - 2) >> 2;
+        const int row = q * 32 + lane;
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+        const int cb = hf * G_COLS;
+        for (int i = 0; i < mine; ++i) {
+            const int s = i & 1;
+            const int64_t grow = (blockIdx.x + (int64_t)i * gridDim.x) * TILE + row;
+            const bool valid = grow < n;
+            // layer 1: acc1[s] + b1, GELU -> H1 (and the saved values)
+            if (!gwait(bar(GB_A1F0 + s), (i >> 1) & 1, abort)) break;
+            tc_fence_after();
+            uint32_t hw[G_COLS / 2];
+#pragma unroll
+            for (int c = 0; c < G_COLS / 16; ++c) {
+                float v[16];
+                tmem_ld16(tbase + s * 128 + lane_base + cb + 16 * c, v);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) v[e] += b1f[cb + 16 * c + e];
+                if (valid && z1s) {
+                    float4 *zp = reinterpret_cast<float4 *>(z1s + grow * NH + cb + 16 * c);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        zp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                }
+#pragma unroll
+                for (int e = 0; e < 8; ++e) hw[8 * c + e] = pack2(gelu(v[2 * e]), gelu(v[2 * e + 1]));
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(GB_A1E0 + s));
+            // H1 is free once the second layer of the previous tile has read it
+            if (!gwait(bar(GB_HE), (i + 1) & 1, abort)) break;
+            // columns cb .. cb + 31: atom cb / 64, chunks (cb % 64) / 8 + c
+#pragma unroll
+            for (int c = 0; c < G_COLS / 8; ++c)
+                *reinterpret_cast<uint4 *>(sm + G_H1 + (cb >> 6) * ATOM +
+                                           sw128_off(row, ((cb & 63) >> 3) + c)) =
+                    make_uint4(hw[4 * c], hw[4 * c + 1], hw[4 * c + 2], hw[4 * c + 3]);
+            if (valid && h1s) {
+                uint4 *hp = reinterpret_cast<uint4 *>(h1s + grow * NH + cb);
+#pragma unroll
+                for (int c = 0; c < G_COLS / 8; ++c)
+                    hp[c] = make_uint4(hw[4 * c], hw[4 * c + 1], hw[4 * c + 2], hw[4 * c + 3]);
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(GB_HF));
+            // layer 2: acc2 + b2, GELU, then the output layer on the CUDA cores
+            if (!gwait(bar(GB_A2F), i & 1, abort)) break;
+            tc_fence_after();
+            float y0 = 0.f, y1 = 0.f;
+#pragma unroll
+            for (int c = 0; c < G_COLS / 16; ++c) {
+                float v[16];
+                tmem_ld16(tbase + 256 + lane_base + cb + 16 * c, v);
+                uint32_t w2w[8];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) v[e] += b2f[cb + 16 * c + e];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    w2w[e] = pack2(gelu(v[2 * e]), gelu(v[2 * e + 1]));
+                    const float ha = bf_lo(w2w[e]), hb = bf_hi(w2w[e]);
+                    const int j = cb + 16 * c + 2 * e;
+                    y0 = fmaf(ha, w3f[j], y0);
+                    y0 = fmaf(hb, w3f[j + 1], y0);
+                    y1 = fmaf(ha, w3f[NH + j], y1);
+                    y1 = fmaf(hb, w3f[NH + j + 1], y1);
+                }
+                if (valid && z2s) {
+                    float4 *zp = reinterpret_cast<float4 *>(z2s + grow * NH + cb + 16 * c);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        zp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                }
+                if (valid && h2s) {
+                    uint4 *hp = reinterpret_cast<uint4 *>(h2s + grow * NH + cb + 16 * c);
+                    hp[0] = make_uint4(w2w[0], w2w[1], w2w[2], w2w[3]);
+                    hp[1] = make_uint4(w2w[4], w2w[5], w2w[6], w2w[7]);
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(GB_A2E));
+            // the column parts of a row meet: all write their partial, the
+            // first part adds them in a fixed order (the partials alternate
+            // by tile parity; a tile's H1 barrier orders the reuse)
+            constexpr int NP = G_EPI / 4;
+            yp[(s * NP + hf) * TILE + row] = make_float2(y0, y1);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(GB_Y0 + s));
+            if (hf == 0) {
+                if (!gwait(bar(GB_Y0 + s), (i >> 1) & 1, abort)) break;
+                if (valid) {
+#pragma unroll
+                    for (int pp = 1; pp < NP; ++pp) {
+                        const float2 o = yp[(s * NP + pp) * TILE + row];
+                        y0 += o.x;
+                        y1 += o.y;
+                    }
+                    y[grow * 2] = b3f[0] + y0;
+                    y[grow * 2 + 1] = b3f[1] + y1;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (*abort && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, G_TMEM_COLS);
     }
 }
 
@@ -733,6 +1055,13 @@ int g_num_sms = 0;
 std::once_flag g_attr_once;
 cudaError_t g_attr_err = cudaSuccess;
 
+// the driver's tensor-map encoder, through the runtime's entry-point lookup
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                 const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                 const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled g_encode = nullptr;
+
 cudaError_t init_attrs() {
     std::call_once(g_attr_once, [] {
         int dev = 0;
@@ -741,6 +1070,17 @@ cudaError_t init_attrs() {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, F_BYTES);
         if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     G_BYTES);
+        if (e == cudaSuccess) {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                 cudaEnableDefault, &q);
+            if (e == cudaSuccess && q == cudaDriverEntryPointSuccess)
+                g_encode = reinterpret_cast<EncodeTiled>(fn);
+        }
+        if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, B_BYTES);
         g_attr_err = e;
     });
@@ -748,6 +1088,34 @@ cudaError_t init_attrs() {
 }
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// Tensor map of a row-major BF16 matrix [rows][cols] (cols a multiple of
+// 64): boxes of 64 columns x 128 rows with 128-byte swizzling; rows past
+// the end read as zeros.
+int encode_rows(CUtensorMap *m, const void *base, uint64_t rows, uint64_t cols) {
+    if (!g_encode) return set_error(SPH_ERR_CUDA, "mlp: the tensor-map encoder is unavailable");
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 2};
+    const cuuint32_t box[2] = {64, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims,
+                                strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(SPH_ERR_CUDA, "mlp: cuTensorMapEncodeTiled failed");
+    return SPH_OK;
+}
+
+// environment SPH_MLP_FWD_LEGACY=1: the forward kernel without TMA and
+// warp specialisation, to measure against
+bool legacy_forward() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("SPH_MLP_FWD_LEGACY");
+        v = (e && atoi(e) > 0) ? 1 : 0;
+    }
+    return v == 1;
+}
 
 }  // namespace
 
@@ -777,10 +1145,22 @@ int mlp_forward(const sph_mlp_model *M, const uint16_t *x, int64_t n, float *y, 
         (h2 && !aligned16(h2)) || !aligned16(M->w1) || !aligned16(M->w2))
         return set_error(SPH_ERR_ARG, "mlp forward: buffers must be 16-byte aligned");
     SPH_CUDA(init_attrs());
-    const MlpDev W{M->params, M->w1, M->w2, M->w2t, M->w3};
-    k_mlp_fwd<<<mlp_grid(n), THREADS, F_BYTES, st>>>(W, x, n, y, z1, z2, h1, h2, err);
+    if (legacy_forward()) {
+        const MlpDev W{M->params, M->w1, M->w2, M->w2t, M->w3};
+        k_mlp_fwd<<<mlp_grid(n), THREADS, F_BYTES, st>>>(W, x, n, y, z1, z2, h1, h2, err);
+        count_launch();
+        SPH_LAUNCH_CHECK("k_mlp_fwd");
+        return SPH_OK;
+    }
+    MlpMaps maps;
+    int rc = encode_rows(&maps.x, x, (uint64_t)n, NIN);
+    if (!rc) rc = encode_rows(&maps.w1, M->w1, NH, NIN);
+    if (!rc) rc = encode_rows(&maps.w2, M->w2, NH, NH);
+    if (rc) return rc;
+    k_mlp_fwd_tma<<<mlp_grid(n), G_THREADS, G_BYTES, st>>>(maps, M->params, M->w3, n, y, z1, z2,
+                                                             h1, h2, err);
     count_launch();
-    SPH_LAUNCH_CHECK("k_mlp_fwd");
+    SPH_LAUNCH_CHECK("k_mlp_fwd_tma");
     return SPH_OK;
 }
 

@@ -428,6 +428,8 @@ class Integrator:
         if rp is not None:
             if rp.usable(self, dt):
                 rp.run()
+                self._steps_done += 1
+                self._adapt_skin()
                 return
             self._drop_replay()
         if self._steps_done >= 1 and self._may_record():
@@ -444,9 +446,9 @@ class Integrator:
 
     def _adapt_skin(self):
         """Grow the neighbour-list skin of a small simulation whose lists go
-        stale at most updates (``tuning.adaptive_skin``): every
-        SKIN_WINDOW steps, while more than half of the window's updates were
-        full builds, the skin doubles (up to SKIN_MAX)."""
+        stale within a step or two (``tuning.adaptive_skin``): every
+        SKIN_WINDOW steps, while the window had more than one full build per
+        two steps, the skin doubles (up to SKIN_MAX)."""
         from .. import tuning
         if (self._steps_done % tuning.SKIN_WINDOW != 0 or getattr(self, "skin_frozen", False)
                 or not torch.cuda.is_available()):
@@ -457,14 +459,16 @@ class Integrator:
         n = sum(pa.get_number_of_particles() for pa in self.particles.arrays)
         if not tuning.adaptive_skin(n):
             return
-        full, light = cm.build_stats()
+        # full builds only: steps replayed as graphs and steps run call by
+        # call count them alike (not so the light refreshes a stale one
+        # replaces), so both take the same decisions
+        full = cm.build_stats()[0]
         last = getattr(self, "_skin_window", None)
-        self._skin_window = (full, light)
+        self._skin_window = full
         if last is None:
             return
-        df, dl = full - last[0], light - last[1]
         skin = cm.list_skin()
-        if df + dl > 0 and df > 0.5 * (df + dl) and 0.0 < skin < tuning.SKIN_MAX:
+        if full - last > tuning.SKIN_WINDOW // 2 and 0.0 < skin < tuning.SKIN_MAX:
             cm.set_skin(min(tuning.SKIN_MAX, 2.0 * skin))
 
     def _may_record(self):
