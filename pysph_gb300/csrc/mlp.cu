@@ -702,6 +702,32 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 // ---------------------------------------------------------------------------
 // backward
 // ---------------------------------------------------------------------------
+// Operands in the K-major layout with 128-byte swizzling (as the TMA forward
+// kernel's): an operand of R rows keeps K in atom columns of 64 BF16, each
+// R x 128 B; within one, row r's 16-byte chunk c sits at chunk c ^ (r % 8).
+// The transposed operands are written one 2-byte element per thread (the
+// thread's sample is the K index): the swizzle spreads a warp's 32 samples
+// over four chunks of the row, so a store takes one wavefront.
+__device__ __forceinline__ uint32_t sw_off(int r, int k, int rows) {
+    return (uint32_t)((k >> 6) * rows * 128 + r * 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) +
+                      ((k & 7) << 1));
+}
+
+// Start address of K step s (16 BF16) of an operand of R rows.
+__device__ __forceinline__ uint32_t sw_kstep(uint32_t base, int s, int rows) {
+    return base + (uint32_t)((s >> 2) * rows * 128 + (s & 3) * 32);
+}
+
+// Copy a row-major [rows][K] BF16 matrix into the swizzled layout.
+__device__ __forceinline__ void load_operand_sw(uint8_t *dst, const uint16_t *src, int rows, int K) {
+    const int kc = K / 8;
+    for (int c = threadIdx.x; c < rows * kc; c += blockDim.x) {
+        const int r = c / kc, k8 = c % kc;
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (int64_t)r * K + k8 * 8));
+        *reinterpret_cast<uint4 *>(dst + sw_off(r, k8 * 8, rows)) = v;
+    }
+}
+
 constexpr int H1T_ROWS = NH + 16;    // h1^T plus a row of ones (bias) and zero rows
 constexpr int XT_ROWS = NIN + 16;    // x^T plus a row of ones and zero rows
 constexpr uint32_t B_A1 = 0;                              // dz2 [b][j]
@@ -713,7 +739,7 @@ constexpr uint32_t B_W3 = B_W2T + NH * NH * 2;            // float [2][128]
 constexpr uint32_t B_RED = B_W3 + NOUT * NH * 4;          // float [8] loss per warp
 constexpr uint32_t B_BAR = B_RED + 32;
 constexpr uint32_t B_SLOT = B_BAR + 8;
-constexpr uint32_t B_BYTES = B_SLOT + 8;
+constexpr uint32_t B_BYTES = B_SLOT + 8 + 1024;           // + alignment of the base
 constexpr uint32_t T_DH1 = 0, T_DW2 = 128, T_DW1 = 288;    // tensor-memory columns
 constexpr uint32_t B_TMEM_COLS = 512;
 static_assert(T_DW2 + H1T_ROWS <= T_DW1 && T_DW1 + XT_ROWS <= B_TMEM_COLS, "tensor memory plan");
@@ -724,7 +750,9 @@ __global__ void __launch_bounds__(THREADS, 1)
               const float *__restrict__ y, const float *__restrict__ target, int64_t n,
               float inv_count, float *__restrict__ dy_out, float *__restrict__ part,
               float *__restrict__ part_loss, unsigned *err) {
-    extern __shared__ __align__(1024) uint8_t sm[];
+    extern __shared__ __align__(1024) uint8_t bsm_raw[];
+    const uint32_t raw = smem_u32(bsm_raw);
+    uint8_t *sm = bsm_raw + (((raw + 1023u) & ~1023u) - raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     // row = sample (and tensor-memory lane); the two warps of a lane quarter
     // split the columns
@@ -735,14 +763,14 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t bar = smem_u32(sm + B_BAR);
     uint32_t *slot = reinterpret_cast<uint32_t *>(sm + B_SLOT);
 
-    load_operand(sm + B_W2T, W.w2t, NH, NH);
+    load_operand_sw(sm + B_W2T, W.w2t, NH, NH);
     for (int i = t; i < NOUT * NH; i += THREADS) w3f[i] = __uint_as_float((uint32_t)W.w3[i] << 16);
     // the constant rows: ones at h1^T row 128 and x^T row 192, zeros below
     for (int i = t; i < 16 * TILE; i += THREADS) {
         const int r = i / TILE, b = i % TILE;
         const __nv_bfloat16 one = __float2bfloat16_rn(r == 0 ? 1.f : 0.f);
-        *reinterpret_cast<__nv_bfloat16 *>(sm + B_H1T + core_off(NH + r, b, TILE / 8)) = one;
-        *reinterpret_cast<__nv_bfloat16 *>(sm + B_XT + core_off(NIN + r, b, TILE / 8)) = one;
+        *reinterpret_cast<__nv_bfloat16 *>(sm + B_H1T + sw_off(NH + r, b, H1T_ROWS)) = one;
+        *reinterpret_cast<__nv_bfloat16 *>(sm + B_XT + sw_off(NIN + r, b, XT_ROWS)) = one;
     }
     if (warp == 0) tmem_alloc(smem_u32(slot), B_TMEM_COLS);
     if (t == 0) mbar_init(bar, 1);
@@ -755,8 +783,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t sA1 = smem_u32(sm + B_A1), sA2 = smem_u32(sm + B_A2);
     const uint32_t sH1T = smem_u32(sm + B_H1T), sXT = smem_u32(sm + B_XT);
     const uint32_t sW2T = smem_u32(sm + B_W2T);
-    constexpr uint32_t SBO_T = (TILE / 8) * 128;   // K = 128 samples
-    constexpr uint32_t SBO_H = (NH / 8) * 128;     // K = 128 hidden units
     uint32_t phase = 0;
     bool ok = true, first = true;
     float loss = 0.f;
@@ -797,12 +823,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 w[i / 2] = pack2(g[0], g[1]);
             }
-            *reinterpret_cast<uint4 *>(sm + B_A1 + core_off(row, j0, NH / 8)) =
+            *reinterpret_cast<uint4 *>(sm + B_A1 + sw_off(row, j0, TILE)) =
                 make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const uint16_t hv = (uint16_t)((w[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
-                *reinterpret_cast<uint16_t *>(sm + B_A2 + core_off(j0 + i, row, TILE / 8)) = hv;
+                *reinterpret_cast<uint16_t *>(sm + B_A2 + sw_off(j0 + i, row, NH)) = hv;
             }
         }
         // h1^T and x^T: column `row`
@@ -813,7 +839,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                *reinterpret_cast<uint16_t *>(sm + B_H1T + core_off(i0 + i, row, TILE / 8)) =
+                *reinterpret_cast<uint16_t *>(sm + B_H1T + sw_off(i0 + i, row, H1T_ROWS)) =
                     (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
         }
 #pragma unroll 1
@@ -823,7 +849,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                *reinterpret_cast<uint16_t *>(sm + B_XT + core_off(m0 + i, row, TILE / 8)) =
+                *reinterpret_cast<uint16_t *>(sm + B_XT + sw_off(m0 + i, row, XT_ROWS)) =
                     (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
         }
         fence_async_smem();
@@ -834,13 +860,13 @@ __global__ void __launch_bounds__(THREADS, 1)
             // dh1 [b][i] = dz2 [b][j] W2 [j][i]   (B operand W2^T: rows i, K = j)
 #pragma unroll
             for (int s = 0; s < NH / 16; ++s)
-                mma_bf16(tbase + T_DH1, sdesc(sA1 + s * 256, 128, SBO_H),
-                         sdesc(sW2T + s * 256, 128, SBO_H), idesc_bf16(128, NH), s > 0);
+                mma_bf16(tbase + T_DH1, sdesc_sw128(sw_kstep(sA1, s, TILE)),
+                         sdesc_sw128(sw_kstep(sW2T, s, NH)), idesc_bf16(128, NH), s > 0);
             // dW2 [j][i] (+ db2 at column 128) += dz2^T [j][b] h1 [b][i]
 #pragma unroll
             for (int s = 0; s < TILE / 16; ++s)
-                mma_bf16(tbase + T_DW2, sdesc(sA2 + s * 256, 128, SBO_T),
-                         sdesc(sH1T + s * 256, 128, SBO_T), idesc_bf16(128, H1T_ROWS),
+                mma_bf16(tbase + T_DW2, sdesc_sw128(sw_kstep(sA2, s, NH)),
+                         sdesc_sw128(sw_kstep(sH1T, s, H1T_ROWS)), idesc_bf16(128, H1T_ROWS),
                          (s > 0 || !first) ? 1u : 0u);
             mma_commit(bar);
         }
@@ -865,7 +891,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 const float g = valid ? v[i] * dgelu(z[i]) : 0.f;
-                *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + core_off(c0 + i, row, TILE / 8)) =
+                *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + sw_off(c0 + i, row, NH)) =
                     __float2bfloat16_rn(g);
             }
         }
@@ -877,8 +903,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             // dW1 [j][m] (+ db1 at column 192) += dz1^T [j][b] x [b][m]
 #pragma unroll
             for (int s = 0; s < TILE / 16; ++s)
-                mma_bf16(tbase + T_DW1, sdesc(sA2 + s * 256, 128, SBO_T),
-                         sdesc(sXT + s * 256, 128, SBO_T), idesc_bf16(128, XT_ROWS),
+                mma_bf16(tbase + T_DW1, sdesc_sw128(sw_kstep(sA2, s, NH)),
+                         sdesc_sw128(sw_kstep(sXT, s, XT_ROWS)), idesc_bf16(128, XT_ROWS),
                          (s > 0 || !first) ? 1u : 0u);
             mma_commit(bar);
         }

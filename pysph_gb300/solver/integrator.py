@@ -446,9 +446,9 @@ class Integrator:
 
     def _adapt_skin(self):
         """Grow the neighbour-list skin of a small simulation whose lists go
-        stale within a step or two (``tuning.adaptive_skin``): every
+        stale within a few steps (``tuning.adaptive_skin``): every
         SKIN_WINDOW steps, while the window had more than one full build per
-        two steps, the skin doubles (up to SKIN_MAX)."""
+        four steps, the skin doubles (up to SKIN_MAX)."""
         from .. import tuning
         if (self._steps_done % tuning.SKIN_WINDOW != 0 or getattr(self, "skin_frozen", False)
                 or not torch.cuda.is_available()):
@@ -468,7 +468,7 @@ class Integrator:
         if last is None:
             return
         skin = cm.list_skin()
-        if full - last > tuning.SKIN_WINDOW // 2 and 0.0 < skin < tuning.SKIN_MAX:
+        if full - last > tuning.SKIN_WINDOW // 4 and 0.0 < skin < tuning.SKIN_MAX:
             cm.set_skin(min(tuning.SKIN_MAX, 2.0 * skin))
 
     def _may_record(self):

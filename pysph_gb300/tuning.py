@@ -18,12 +18,11 @@ import os
 DEFAULT_SKIN = 0.03
 
 
-# small simulations whose lists go stale within a step or two (the motion
-# of a step reaches half the skin): every SKIN_WINDOW steps the skin
-# doubles, up to SKIN_MAX, while the window had more than one full build per
-# two steps -- longer-lived lists let a recorded step replay as one graph,
-# and below GRAPH_MAX_PARTICLES the launches, not the longer lists, bound a
-# step
+# small simulations whose lists go stale within a few steps (the motion of
+# a step reaches half the skin): every SKIN_WINDOW steps the skin doubles,
+# up to SKIN_MAX, while the window had more than one full build per four
+# steps -- longer-lived lists let a recorded step replay as one graph, and
+# below GRAPH_MAX_PARTICLES the launches, not the longer lists, bound a step
 SKIN_WINDOW = 16
 SKIN_MAX = 0.24
 
