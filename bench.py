@@ -1106,7 +1106,7 @@ def run_gpu_mlp(args):
         "forward": {"ms": fwd_ms, "tflops": fwd_tf},
         "backward": {"ms": bwd_ms, "tflops": bwd_tf},
         "train_step_ms": train_ms,
-        "roofline": {"bound": "tensor", "kernel": "k_mlp_fwd", "achieved": fwd_tf, "peak": peak,
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_fwd_tma", "achieved": fwd_tf, "peak": peak,
                      "unit": "TFLOP/s", "frac": fwd_tf / peak, "traffic": None,
                      "peak_kind": kind},
         "gpu_launches": launches,
@@ -1169,6 +1169,7 @@ def run_gpu_small(args):
                 integ.integrate(dt)
             torch.cuda.synchronize()
             st0 = integ.step_stats() or {}
+            b0 = particles.cell_manager.build_stats()
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             l0 = native.launch_count()
@@ -1181,11 +1182,14 @@ def run_gpu_small(args):
             wall = (time.perf_counter() - t0) / args.steps * 1e3
             dev = a.elapsed_time(b) / args.steps
             st1 = integ.step_stats() or {}
+            b1 = particles.cell_manager.build_stats()
             row["particles"] = n
             row[mode] = {"wall_ms_per_step": wall, "device_ms_per_step": dev,
                          "steps_per_s": 1e3 / wall,
                          "launches_per_step": (native.launch_count() - l0) / args.steps,
                          "list_skin": particles.cell_manager.list_skin(),
+                         "full_builds_per_step": (b1[0] - b0[0]) / args.steps,
+                         "light_refreshes_per_step": (b1[1] - b0[1]) / args.steps,
                          "step_graphs": st1 or None}
             g = st1.get("graph_steps", 0) - st0.get("graph_steps", 0)
             if g > 0:

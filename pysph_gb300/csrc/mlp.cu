@@ -803,7 +803,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
         // dz2 = (dy W3) * gelu'(z2): row `row` of A1, column `row` of A2
-#pragma unroll 1
+        // (loops unrolled by four so that four rows' loads are in flight)
+#pragma unroll 4
         for (int j0 = ch * (NH / 2); j0 < (ch + 1) * (NH / 2); j0 += 8) {
             float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (valid) {
@@ -832,7 +833,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
         // h1^T and x^T: column `row`
-#pragma unroll 1
+#pragma unroll 4
         for (int i0 = ch * (NH / 2); i0 < (ch + 1) * (NH / 2); i0 += 8) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (valid) v = __ldg(reinterpret_cast<const uint4 *>(h1s + b * NH + i0));
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 *reinterpret_cast<uint16_t *>(sm + B_H1T + sw_off(i0 + i, row, H1T_ROWS)) =
                     (uint16_t)((wv[i / 2] >> ((i & 1) * 16)) & 0xFFFFu);
         }
-#pragma unroll 1
+#pragma unroll 4
         for (int m0 = ch * (NIN / 2); m0 < (ch + 1) * (NIN / 2); m0 += 8) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (valid) v = __ldg(reinterpret_cast<const uint4 *>(x + b * NIN + m0));
@@ -870,27 +871,28 @@ __global__ void __launch_bounds__(THREADS, 1)
                          (s > 0 || !first) ? 1u : 0u);
             mma_commit(bar);
         }
+        // this row's half of z1, requested while the tensor cores work
+        float z1r[NH / 2];
+#pragma unroll
+        for (int q = 0; q < NH / 8; ++q) {
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) a = *reinterpret_cast<const float4 *>(z1s + b * NH + ch * (NH / 2) + 4 * q);
+            z1r[4 * q] = a.x; z1r[4 * q + 1] = a.y; z1r[4 * q + 2] = a.z; z1r[4 * q + 3] = a.w;
+        }
         ok = mbar_wait(bar, phase);
         phase ^= 1;
         if (!__syncthreads_and(ok)) break;
         tc_fence_after();
 
         // dz1 = dh1 * gelu'(z1) -> column `row` of A2 (its previous content is consumed)
-#pragma unroll 1
-        for (int c0 = ch * (NH / 2); c0 < (ch + 1) * (NH / 2); c0 += 16) {
+#pragma unroll
+        for (int cc = 0; cc < NH / 32; ++cc) {
+            const int c0 = ch * (NH / 2) + 16 * cc;
             float v[16];
             tmem_ld16(tbase + T_DH1 + lane_base + c0, v);
-            float z[16];
-            if (valid) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float4 a = *reinterpret_cast<const float4 *>(z1s + b * NH + c0 + 4 * q);
-                    z[4 * q] = a.x; z[4 * q + 1] = a.y; z[4 * q + 2] = a.z; z[4 * q + 3] = a.w;
-                }
-            }
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const float g = valid ? v[i] * dgelu(z[i]) : 0.f;
+                const float g = valid ? v[i] * dgelu(z1r[16 * cc + i]) : 0.f;
                 *reinterpret_cast<__nv_bfloat16 *>(sm + B_A2 + sw_off(c0 + i, row, NH)) =
                     __float2bfloat16_rn(g);
             }
