@@ -234,7 +234,11 @@ int sph_step_run(sph_step *step, int nsteps);
 /* out[0] graph replays, out[1] eager steps, out[2] steps resumed after a
  * stale refresh, out[3] graph captures, out[4] recorded calls, out[5]
  * kernels of one replay, out[6] device time of all replays in microseconds
- * (CUDA events around each graph launch). */
+ * (CUDA events around each graph launch), out[7] capture attempts, out[8]
+ * why the last attempt found no graph: 0 none failed, 1 an update needed a
+ * full build, 2-5 a neighbour list needed building, 6 more than 32
+ * updates, 7 a recorded full build, 8 a call failed while captured, 9 the
+ * build changed, 10 the graph could not be made. */
 int sph_step_stats(sph_step *step, int64_t *out);
 int sph_step_destroy(sph_step *step);
 

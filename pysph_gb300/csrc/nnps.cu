@@ -872,6 +872,7 @@ int nnps_update(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double 
         // a full build needs the host: no step graph for this build
         if (ctx->capturing) {
             ctx->capture_failed = true;
+            ctx->capture_fail_site = 1;   // the update needs a full build
             return SPH_OK;
         }
         return nnps_build(ctx, arrays, narrays, cell_size, radius_scale, subdiv, check_jump);

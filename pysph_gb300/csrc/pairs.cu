@@ -769,6 +769,7 @@ int ensure_list(sph_ctx *ctx, int dst, int src, NbrList **out) {
     if (ctx->capturing) {
         // lists are built at the positions of the build, not inside a step graph
         ctx->capture_failed = true;
+        ctx->capture_fail_site = 2;   // a list to build
         return SPH_OK;
     }
     NbrList &L = **out;
@@ -880,6 +881,7 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
         if (rc) return rc;
         if (stale && ctx->capturing) {
             ctx->capture_failed = true;
+            ctx->capture_fail_site = 3;   // a list to build
             return SPH_OK;
         }
         const bool own = rho != nullptr && rho == D.view.rho &&
@@ -907,6 +909,7 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
         if (rc) return rc;
         if (stale && ctx->capturing) {
             ctx->capture_failed = true;
+            ctx->capture_fail_site = 4;   // a list to build
             return SPH_OK;
         }
         a.s[i] = make_src(ctx->arrays[srcs[i]]);
@@ -980,6 +983,7 @@ int rates_pass(sph_ctx *ctx, int dst, const sph_source_term *terms, int nterms,
         if (rc) return rc;
         if (stale && ctx->capturing) {
             ctx->capture_failed = true;
+            ctx->capture_fail_site = 5;   // a list to build
             return SPH_OK;
         }
         if (stale) {

@@ -81,6 +81,8 @@ struct sph_step {
     // with the default stream's work
     cudaStream_t stream = nullptr;
     long long n_graph = 0, n_eager = 0, n_resumed = 0, n_captures = 0;
+    long long n_attempts = 0;      // capture attempts
+    int last_fail = 0;             // why the last attempt found no graph (see sph_step_stats)
     // capture back-off: a flow whose lists go stale within a step or two of
     // every full build spends a capture per build for no replay; after a
     // graph that never ran a whole step the next 1, 2, 4 .. 64 capture
@@ -173,6 +175,8 @@ int capture(sph_step *s) {
     SPH_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
     ctx->capturing = true;
     ctx->capture_failed = false;
+    ctx->capture_fail_site = 0;
+    s->n_attempts += 1;
     ctx->gate = ctx->d_status + kStaleWord;
     int rc = SPH_OK;
     // error word, displacement, stale word, stale bits
@@ -184,6 +188,7 @@ int capture(sph_step *s) {
         if (o.kind == kOpUpdate) {
             if (u >= 32) {
                 ctx->capture_failed = true;
+                ctx->capture_fail_site = 6;
                 break;
             }
             ctx->capture_stale_bit = 1u << u;
@@ -191,6 +196,7 @@ int capture(sph_step *s) {
         }
         if (o.kind == kOpBuild) {
             ctx->capture_failed = true;
+            ctx->capture_fail_site = 7;
             break;
         }
         rc = run_op(ctx, o);
@@ -227,6 +233,8 @@ int capture(sph_step *s) {
     s->updates = u;
     ctx->n_light = light0;
     if (!ok || !s->exec) {
+        s->last_fail = ctx->capture_failed ? ctx->capture_fail_site
+                       : (rc ? 8 : (ctx->build_id != build ? 9 : 10));
         drop_graph(s);
         for (size_t a = 0; a < ctx->arrays.size() && a < fresh0.size(); ++a) {
             ctx->arrays[a].st_fresh = fresh0[a];
@@ -501,6 +509,8 @@ int sph_step_stats(sph_step *s, int64_t *out) {
     out[4] = (int64_t)s->ops.size();
     out[5] = s->launches;
     out[6] = (int64_t)(s->replay_us + 0.5);
+    out[7] = s->n_attempts;
+    out[8] = s->last_fail;
     return SPH_OK;
 }
 

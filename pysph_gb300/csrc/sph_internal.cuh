@@ -233,6 +233,7 @@ struct sph_ctx {
     struct sph_step *recording = nullptr;
     bool capturing = false;
     bool capture_failed = false;
+    int capture_fail_site = 0;          // where the last capture attempt needed the host
     unsigned capture_stale_bit = 0;     // stale bit of the light refresh being captured
 };
 
