@@ -478,6 +478,11 @@ int run_steps(sph_step *s, int nsteps) {
                 if (s->exec) {
                     s->judged = false;
                     s->lifetime = 0;
+                } else if (s->last_fail >= 2 && s->last_fail <= 5) {
+                    // a neighbour list of this build was not built yet (the
+                    // refresh resolved at the step's start rebuilt): the
+                    // eager step builds it, the next step tries again
+                    s->attempt_build = -1;
                 }
             }
         }
