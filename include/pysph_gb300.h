@@ -238,7 +238,9 @@ int sph_step_run(sph_step *step, int nsteps);
  * why the last attempt found no graph: 0 none failed, 1 an update needed a
  * full build, 2-5 a neighbour list needed building, 6 more than 32
  * updates, 7 a recorded full build, 8 a call failed while captured, 9 the
- * build changed, 10 the graph could not be made. */
+ * build changed, 10 the graph could not be made; out[9] captures that
+ * updated the previous graph's executable in place (cudaGraphExecUpdate)
+ * instead of instantiating a new one.  out holds 10 values. */
 int sph_step_stats(sph_step *step, int64_t *out);
 int sph_step_destroy(sph_step *step);
 

@@ -82,6 +82,7 @@ struct sph_step {
     cudaStream_t stream = nullptr;
     long long n_graph = 0, n_eager = 0, n_resumed = 0, n_captures = 0;
     long long n_attempts = 0;      // capture attempts
+    long long n_updates = 0;       // captures that updated the executable in place
     int last_fail = 0;             // why the last attempt found no graph (see sph_step_stats)
     // capture back-off: a flow whose lists go stale within a step or two of
     // every full build spends a capture per build for no replay; after a
@@ -146,7 +147,12 @@ int run_eager(sph_step *s, size_t from) {
     return SPH_OK;
 }
 
-void drop_graph(sph_step *s) {
+// The graph no longer matches the build; its executable is kept, so that
+// the next capture can update it in place (cudaGraphExecUpdate, far cheaper
+// than instantiating) when its topology has not changed.
+void drop_graph(sph_step *s) { s->graph_build = -1; }
+
+void destroy_graph(sph_step *s) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;
     s->graph_build = -1;
@@ -207,14 +213,29 @@ int capture(sph_step *s) {
     ctx->capturing = false;
     ctx->gate = nullptr;
     e = cudaStreamEndCapture(ctx->stream, &graph);
-    const bool ok = !rc && !ctx->capture_failed && e == cudaSuccess && graph != nullptr &&
-                    ctx->build_id == build;
+    const int rc_capture = rc;
+    bool ok = !rc && !ctx->capture_failed && e == cudaSuccess && graph != nullptr &&
+              ctx->build_id == build;
     if (ok) {
-        e = cudaGraphInstantiate(&s->exec, graph, 0);
-        if (e != cudaSuccess) {
-            s->exec = nullptr;
-            rc = cuda_check(e, "cudaGraphInstantiate (step)");
+        bool made = false;
+        if (s->exec) {
+            // same calls, other arguments: update the executable in place
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(s->exec, graph, &info) == cudaSuccess) {
+                made = true;
+                s->n_updates += 1;
+            } else {
+                cudaGetLastError();
+                cudaGraphExecDestroy(s->exec);
+                s->exec = nullptr;
+            }
         }
+        if (!made) {
+            e = cudaGraphInstantiate(&s->exec, graph, 0);
+            made = e == cudaSuccess;
+            if (!made) s->exec = nullptr;
+        }
+        ok = made;
     }
     if (graph) cudaGraphDestroy(graph);
     cudaGetLastError();
@@ -234,7 +255,7 @@ int capture(sph_step *s) {
     ctx->n_light = light0;
     if (!ok || !s->exec) {
         s->last_fail = ctx->capture_failed ? ctx->capture_fail_site
-                       : (rc ? 8 : (ctx->build_id != build ? 9 : 10));
+                       : (rc_capture ? 8 : (ctx->build_id != build ? 9 : 10));
         drop_graph(s);
         for (size_t a = 0; a < ctx->arrays.size() && a < fresh0.size(); ++a) {
             ctx->arrays[a].st_fresh = fresh0[a];
@@ -475,7 +496,7 @@ int run_steps(sph_step *s, int nsteps) {
             } else {
                 rc = capture(s);
                 if (rc) return rc;
-                if (s->exec) {
+                if (s->graph_build == ctx->build_id) {
                     s->judged = false;
                     s->lifetime = 0;
                 } else if (s->last_fail >= 2 && s->last_fail <= 5) {
@@ -516,13 +537,14 @@ int sph_step_stats(sph_step *s, int64_t *out) {
     out[6] = (int64_t)(s->replay_us + 0.5);
     out[7] = s->n_attempts;
     out[8] = s->last_fail;
+    out[9] = s->n_updates;
     return SPH_OK;
 }
 
 int sph_step_destroy(sph_step *s) {
     if (!s) return SPH_OK;
     if (s->ctx && s->ctx->recording == s) s->ctx->recording = nullptr;
-    drop_graph(s);
+    destroy_graph(s);
     if (s->done) cudaEventDestroy(s->done);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);

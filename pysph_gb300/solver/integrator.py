@@ -748,12 +748,12 @@ class StepReplay:
 
     def stats(self):
         from .. import native
-        out = (ctypes.c_int64 * 9)()
+        out = (ctypes.c_int64 * 10)()
         native.check(native.lib().sph_step_stats(self.handle, out), "sph_step_stats")
         return {"graph_steps": out[0], "eager_steps": out[1], "resumed_steps": out[2],
                 "captures": out[3], "calls": out[4], "kernels_per_replay": out[5],
                 "replay_device_us": out[6], "capture_attempts": out[7],
-                "last_capture_failure": out[8]}
+                "last_capture_failure": out[8], "graph_updates": out[9]}
 
     def close(self):
         from .. import native
