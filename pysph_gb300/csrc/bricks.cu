@@ -346,6 +346,8 @@ template <bool RATES>
 __device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
                                       const int *roff, int T, float csf, uint32_t voff,
                                       uint32_t soff, float halpha = 0.f) {
+    // unrolled so that several records' loads are in flight at once
+#pragma unroll 4
     for (int t = threadIdx.x; t <= T; t += blockDim.x) {
         float4 *prec = reinterpret_cast<float4 *>(brick_smem + ((uint32_t)t << 4));
         float4 *vrec = reinterpret_cast<float4 *>(brick_smem + voff + ((uint32_t)t << 4));
