@@ -114,6 +114,11 @@ struct BrickRatesArgs {
     int dim;
     float alpha, beta, eta2, eps;
     int add_velocity, add_gravity, accumulate;
+    // the sources' cs follows Tait with gamma = 7 from their rho (alpha cs /
+    // 2 = tait_kc (rho / 2)^3): blocks whose sources share one mass then
+    // read two records per pair instead of three
+    int tait_state;
+    float tait_kc;
     double gx, gy, gz;
     double *acc[3];
     double *pos[3];
@@ -271,7 +276,10 @@ __device__ __forceinline__ SmemPtrs smem_ptrs(unsigned char *base, const BrickSm
 // term with it is exactly 0.
 __device__ __forceinline__ float4 pad_pos() { return make_float4(1e15f, 1e15f, 1e15f, 0.f); }
 __device__ __forceinline__ float4 pad_vel() { return make_float4(0.f, 0.f, 0.f, 0.f); }
-__device__ __forceinline__ float2 pad_state() { return make_float2(0.5f, 0.f); }
+// rates pass: the position record carries rho / 2, the state record (m,
+// alpha cs / 2); the padding record has zero mass
+__device__ __forceinline__ float4 pad_rpos() { return make_float4(1e15f, 1e15f, 1e15f, 0.5f); }
+__device__ __forceinline__ float2 pad_rstate() { return make_float2(0.f, 0.f); }
 
 // Source records: staged in shared memory, or (STAGED = false, a brick
 // more populous than the shared memory holds) recomputed from the sorted
@@ -279,22 +287,37 @@ __device__ __forceinline__ float2 pad_state() { return make_float2(0.5f, 0.f); }
 template <bool STAGED, int PSH>
 struct SrcRecords;
 
-// Staged: the position record (x, y, z from the brick's centre cell, m) of
-// source t at byte 16 t of the shared memory, in the rates pass the velocity
-// record (u, v, w, p / rho^2) at voff + 16 t and the state record (rho / 2,
-// alpha cs / 2) at soff + 8 t: 32-bit offsets into the shared array, so a
-// record costs one address operation.  (Position and velocity interleaved
-// in 32-byte records took 11 % longer: twice the bank conflicts of the
-// random reads.)
+// Staged: the position record of source t at byte 16 t of the shared
+// memory (x, y, z from the brick's centre cell, and m in the density pass,
+// rho / 2 in the rates pass), in the rates pass the velocity record (u, v,
+// w, p / rho^2) at voff + 16 t and the state record (m, alpha cs / 2) at
+// soff + 8 t: 32-bit offsets into the shared array, so a record costs one
+// address operation.  (Position and velocity interleaved in 32-byte
+// records took 11 % longer: twice the bank conflicts of the random reads.)
+// A rates pass whose block has one source mass and whose cs follows Tait
+// (FAST) reads the first two only: the state record's 8-byte read was a
+// fifth of the shared-memory wavefronts of a pair.
 template <int PSH>
 struct SrcRecords<true, PSH> {
     uint32_t voff, soff;
     __device__ __forceinline__ float4 pos(int t) const {
         return *reinterpret_cast<const float4 *>(brick_smem + ((uint32_t)t << 4));
     }
-    __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
+    // rates pass: position (w = rho / 2), velocity, mass, alpha cs / 2
+    template <bool FAST>
+    __device__ __forceinline__ void rates_rec(int t, float mb, float tkc, float4 &p, float4 &v,
+                                              float &mj, float &hac) const {
+        p = *reinterpret_cast<const float4 *>(brick_smem + ((uint32_t)t << 4));
         v = *reinterpret_cast<const float4 *>(brick_smem + voff + ((uint32_t)t << 4));
-        s = *reinterpret_cast<const float2 *>(brick_smem + soff + ((uint32_t)t << 3));
+        if (FAST) {
+            // cs = co (rho / ro)^3
+            mj = mb;
+            hac = tkc * (p.w * p.w) * p.w;
+        } else {
+            const float2 s = *reinterpret_cast<const float2 *>(brick_smem + soff + ((uint32_t)t << 3));
+            mj = s.x;
+            hac = s.y;
+        }
     }
 };
 
@@ -313,17 +336,24 @@ struct SrcRecords<false, PSH> {
         const int j = staged_slot(G, rlo, roff, t, cy, cz);
         return rel_pos(src->pm, src->scx, j, cy, cz, G, csf);
     }
-    __device__ __forceinline__ void state(int t, float4 &v, float2 &s) const {
+    template <bool FAST>
+    __device__ __forceinline__ void rates_rec(int t, float, float, float4 &p, float4 &v, float &mj,
+                                              float &hac) const {
         if (t >= T) {
+            p = pad_rpos();
             v = pad_vel();
-            s = pad_state();
+            mj = 0.f;
+            hac = 0.f;
             return;
         }
         int cy, cz;
         const int j = staged_slot(G, rlo, roff, t, cy, cz);
+        p = rel_pos(src->pm, src->scx, j, cy, cz, G, csf);
         const float4 vh = src->velh[j], st = src->st[j];
+        mj = p.w;
+        p.w = 0.5f * st.x;
         v = make_float4(vh.x, vh.y, vh.z, st.y);
-        s = make_float2(0.5f * st.x, halpha * st.z);
+        hac = halpha * st.z;
     }
 };
 
@@ -339,13 +369,15 @@ __device__ __forceinline__ SrcRecords<STAGED, PSH> make_records(const SmemPtrs &
 }
 
 // Copy the block's source records into shared memory (the layout of
-// SrcRecords<true, .>).  Rates records: (u, v, w, p / rho^2) and (rho / 2,
-// alpha cs / 2), the halves that the pair averages of the artificial
-// viscosity add.
+// SrcRecords<true, .>).  Rates records: (x, y, z, rho / 2), (u, v, w,
+// p / rho^2) and (m, alpha cs / 2), with the halves that the pair averages
+// of the artificial viscosity add.  Returns whether every record this
+// thread staged has mass mref.
 template <bool RATES>
-__device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
+__device__ __forceinline__ bool stage(const BrickSrcDev &S, const BlockGeo &G, const int *rlo,
                                       const int *roff, int T, float csf, uint32_t voff,
-                                      uint32_t soff, float halpha = 0.f) {
+                                      uint32_t soff, float halpha = 0.f, float mref = 0.f) {
+    bool same = true;
     // unrolled so that several records' loads are in flight at once
 #pragma unroll 4
     for (int t = threadIdx.x; t <= T; t += blockDim.x) {
@@ -354,22 +386,29 @@ __device__ __forceinline__ void stage(const BrickSrcDev &S, const BlockGeo &G, c
         float2 *srec = reinterpret_cast<float2 *>(brick_smem + soff + ((uint32_t)t << 3));
         if (t == T) {
             // the padding record after the staged ones
-            *prec = pad_pos();
             if (RATES) {
+                *prec = pad_rpos();
                 *vrec = pad_vel();
-                *srec = pad_state();
+                *srec = pad_rstate();
+            } else {
+                *prec = pad_pos();
             }
             continue;
         }
         int cy, cz;
         const int j = staged_slot(G, rlo, roff, t, cy, cz);
-        *prec = rel_pos(S.pm, S.scx, j, cy, cz, G, csf);
+        const float4 pr = rel_pos(S.pm, S.scx, j, cy, cz, G, csf);
         if (RATES) {
             const float4 vh = S.velh[j], st = S.st[j];
+            *prec = make_float4(pr.x, pr.y, pr.z, 0.5f * st.x);
             *vrec = make_float4(vh.x, vh.y, vh.z, st.y);
-            *srec = make_float2(0.5f * st.x, halpha * st.z);
+            *srec = make_float2(pr.w, halpha * st.z);
+            same = same && pr.w == mref;
+        } else {
+            *prec = pr;
         }
     }
+    return same;
 }
 
 // The 16-bit entry i (0..7) of a group.
@@ -761,6 +800,7 @@ struct RatesConst {
     float h, ih, beta, eta2h2;
     float gin0, gin1, gout;     // fac dW/dr / r: gin1 q + gin0 (q < 1), gout (2-q)^2 / r (q < 2)
     WCoef wx;                   // eps fac W(q) (XSPH)
+    float mb, tkc;              // two-record blocks: the sources' mass, alpha cs / 2 per (rho / 2)^3
 };
 
 __device__ __forceinline__ RatesConst rates_const(float h, float fac, float beta, float eta2,
@@ -775,6 +815,8 @@ __device__ __forceinline__ RatesConst rates_const(float h, float fac, float beta
     k.gin0 = -3.f * fac * k.ih * k.ih;
     k.gout = -0.75f * fac * k.ih;
     k.wx = w_coef(fac, eps);
+    k.mb = 0.f;
+    k.tkc = 0.f;
     return k;
 }
 
@@ -794,19 +836,20 @@ struct RatesAcc {
 // with eta = 0, as the reference's class always has, 1/r^2 comes from the
 // rsqrt already taken), and XSPH eps m_j W (v_j - v_i) / rho_ab
 // (xsph_funcs.pyx:44-88), sharing 1 / rho_ab.
+// Source record: pj = (position, rho_j / 2), vj = (velocity, p_j / rho_j^2),
+// mj, hacj = alpha cs_j / 2.
 template <bool XSPH, bool ETA0>
 __device__ __forceinline__ void rates_pair(RatesAcc &a, const RatesConst &k, float rx, float ry,
                                            float rz, const float4 &pj, const float4 &vj,
-                                           const float2 &sj) {
+                                           float mj, float hacj) {
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
     const float rinv = rsqrt_ftz(fmaxf(r2, 1e-30f));
     const float q = r2 * rinv * k.ih;
-    const float mj = pj.w;
     const float dot = (a.vi.x - vj.x) * rx + (a.vi.y - vj.y) * ry + (a.vi.z - vj.z) * rz;
     const float hdot = k.h * fminf(dot, 0.f);
     const float mu = ETA0 ? hdot * rinv * rinv : __fdividef(hdot, r2 + k.eta2h2);
-    const float inv_rhoab = rcp_ftz(a.hrhoi + sj.x);
-    const float piab = mu * fmaf(k.beta, mu, -(a.haci + sj.y)) * inv_rhoab;
+    const float inv_rhoab = rcp_ftz(a.hrhoi + pj.w);
+    const float piab = mu * fmaf(k.beta, mu, -(a.haci + hacj)) * inv_rhoab;
     const float t = -mj * ((a.pri + vj.w) + piab);
     // (2 - q) clamped at 0: the outer branch is 0 beyond q = 2
     const float tq = fmaxf(2.f - q, 0.f);
@@ -835,24 +878,22 @@ __device__ __forceinline__ void rates_flush(RatesAcc &a) {
 
 // The pairs of one group of 8 list entries, records two at a time, then
 // the batch's partial sums folded into the compensated ones.
-template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+template <bool XSPH, bool ETA0, bool FAST, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_group(RatesAcc &acc, const RatesConst &kc,
                                             const SrcRecords<STAGED, PSH> &R, const uint4 &grp,
                                             const float4 &Pi) {
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         float4 pj[2], vj[2];
-        float2 sj[2];
+        float mj[2], hac[2];
 #pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const int t = group_entry(grp, 2 * h + i);
-            pj[i] = R.pos(t);
-            R.state(t, vj[i], sj[i]);
-        }
+        for (int i = 0; i < 2; ++i)
+            R.template rates_rec<FAST>(group_entry(grp, 2 * h + i), kc.mb, kc.tkc, pj[i], vj[i],
+                                       mj[i], hac[i]);
 #pragma unroll
         for (int i = 0; i < 2; ++i)
             rates_pair<XSPH, ETA0>(acc, kc, Pi.x - pj[i].x, Pi.y - pj[i].y, Pi.z - pj[i].z,
-                                   pj[i], vj[i], sj[i]);
+                                   pj[i], vj[i], mj[i], hac[i]);
     }
     rates_flush<XSPH>(acc);
 }
@@ -861,7 +902,7 @@ __device__ __forceinline__ void rates_group(RatesAcc &acc, const RatesConst &kc,
 // each group requested two groups ahead into one of three rotating
 // buffers (the loop body is unrolled over the three, so no buffer is
 // copied).
-template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+template <bool XSPH, bool ETA0, bool FAST, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_stream(RatesAcc &acc, const RatesConst &kc,
                                              const SrcRecords<STAGED, PSH> &R, const uint4 *lst, int D,
                                              int ng, const float4 &Pi, uint4 b0, uint4 b1) {
@@ -871,13 +912,13 @@ __device__ __forceinline__ void rates_stream(RatesAcc &acc, const RatesConst &kc
     for (int gi = 0;;) {
         if (gi >= ng) break;
         b2 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
-        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b0, Pi);
+        rates_group<XSPH, ETA0, FAST, STAGED>(acc, kc, R, b0, Pi);
         if (++gi >= ng) break;
         b0 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
-        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b1, Pi);
+        rates_group<XSPH, ETA0, FAST, STAGED>(acc, kc, R, b1, Pi);
         if (++gi >= ng) break;
         b1 = gi + 2 < ng ? lst[(gi + 2) * step] : zero;
-        rates_group<XSPH, ETA0, STAGED>(acc, kc, R, b2, Pi);
+        rates_group<XSPH, ETA0, FAST, STAGED>(acc, kc, R, b2, Pi);
         ++gi;
     }
 }
@@ -895,10 +936,10 @@ __device__ __forceinline__ void rates_rest(RatesAcc &acc, const RatesConst &kc, 
         [&](int t, float rx, float ry, float rz, bool hit) {
             if (skip > 0) { --skip; return; }
             if (!hit) return;
-            float4 vj;
-            float2 sj;
-            R.state(t, vj, sj);
-            rates_pair<XSPH, ETA0>(acc, kc, rx, ry, rz, R.pos(t), vj, sj);
+            float4 pj, vj;
+            float mj, hac;
+            R.template rates_rec<false>(t, 0.f, 0.f, pj, vj, mj, hac);
+            rates_pair<XSPH, ETA0>(acc, kc, rx, ry, rz, pj, vj, mj, hac);
             rates_flush<XSPH>(acc);
         });
 }
@@ -913,7 +954,7 @@ __device__ __forceinline__ void rates_acc_init(RatesAcc &acc, const float4 &vi, 
 }
 
 // The sums of destination d (listed part) and their store.
-template <bool XSPH, bool ETA0, bool STAGED, int PSH>
+template <bool XSPH, bool ETA0, bool FAST, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_dest(const BrickRatesArgs &A, const SrcRecords<STAGED, PSH> &R,
                                            const RatesConst &kc, const uint4 *lgrp, int D, int d,
                                            const DestPre &pre) {
@@ -922,7 +963,7 @@ __device__ __forceinline__ void rates_dest(const BrickRatesArgs &A, const SrcRec
     RatesAcc acc;
     rates_acc_init(acc, A.d.velh[pre.s], A.d.st[pre.s], 0.5f * A.alpha);
     if (real)
-        rates_stream<XSPH, ETA0, STAGED>(acc, kc, R, lgrp + d, D, (min(pre.c, cap) + 7) >> 3,
+        rates_stream<XSPH, ETA0, FAST, STAGED>(acc, kc, R, lgrp + d, D, (min(pre.c, cap) + 7) >> 3,
                                          pre.P, pre.b0, pre.b1);
     const int orig = pre.orig;
     double a3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
@@ -950,7 +991,7 @@ __device__ __forceinline__ void rates_dest(const BrickRatesArgs &A, const SrcRec
     }
 }
 
-template <int K, bool XSPH, bool ETA0, bool STAGED, int PSH>
+template <int K, bool XSPH, bool ETA0, bool FAST, bool STAGED, int PSH>
 __device__ __forceinline__ void rates_block(const BrickRatesArgs &A, const Grid &g,
                                             const BlockGeo &G, const SmemPtrs &sp,
                                             const SrcRecords<STAGED, PSH> &R, const RatesConst &kc,
@@ -960,11 +1001,12 @@ __device__ __forceinline__ void rates_block(const BrickRatesArgs &A, const Grid 
     const uint4 *lgrp = reinterpret_cast<const uint4 *>(A.nbr) + (size_t)dbase * (cap >> 3);
     // the first destination of the thread from its prefetched record, the
     // others (bricks with more destinations than threads) as they come
-    if ((int)threadIdx.x < D) rates_dest<XSPH, ETA0, STAGED>(A, R, kc, lgrp, D, threadIdx.x, first);
+    if ((int)threadIdx.x < D)
+        rates_dest<XSPH, ETA0, FAST, STAGED>(A, R, kc, lgrp, D, threadIdx.x, first);
     for (int d = threadIdx.x + blockDim.x; d < D; d += blockDim.x) {
         DestPre pre;
         dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, cap, D, dbase, d, pre);
-        rates_dest<XSPH, ETA0, STAGED>(A, R, kc, lgrp, D, d, pre);
+        rates_dest<XSPH, ETA0, FAST, STAGED>(A, R, kc, lgrp, D, d, pre);
     }
     // destinations with more neighbours than their list holds: the rest
     // added to the stored sums
@@ -1006,15 +1048,33 @@ __global__ void __maxnreg__(XSPH ? 80 : 64) k_brates(const __grid_constant__ Bri
         dest_prefetch(A.d, g, G, A.rad, sp, A.cnt, lgrp, A.cap, D, dbase, threadIdx.x, pre);
     }
     const float halpha = 0.5f * A.alpha;
-    if (STAGED) stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.voff, sp.soff, halpha);
-    __syncthreads();
+    // two-record blocks: staged sources of one mass (that of the first) whose
+    // cs follows Tait
+    const bool try_fast = STAGED && A.tait_state != 0 && A.eta2 == 0.f && T > 0;
+    float mref = 0.f;
+    if (try_fast) {
+        int cy, cz;
+        mref = A.s.pm[staged_slot(G, sp.rlo, sp.roff, 0, cy, cz)].w;
+    }
+    bool same = true;
+    if (STAGED) same = stage<true>(A.s, G, sp.rlo, sp.roff, T, g.cs_f, sp.voff, sp.soff, halpha, mref);
+    const bool fast = __syncthreads_and(try_fast && same) != 0;
     const SrcRecords<STAGED, 5> R = make_records<STAGED, 5>(sp, A.s, G, g.cs_f, T, halpha);
     const float ih = __fdividef(1.f, g.h_uniform);
-    const RatesConst kc = rates_const(g.h_uniform, cubic_fac(A.dim, ih), A.beta, A.eta2, A.eps);
-    if (A.eta2 == 0.f)
-        rates_block<K, XSPH, true, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
-    else
-        rates_block<K, XSPH, false, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
+    RatesConst kc = rates_const(g.h_uniform, cubic_fac(A.dim, ih), A.beta, A.eta2, A.eps);
+    if (A.eta2 == 0.f) {
+        if constexpr (STAGED) {
+            if (fast) {
+                kc.mb = mref;
+                kc.tkc = A.tait_kc;
+                rates_block<K, XSPH, true, true, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
+                return;
+            }
+        }
+        rates_block<K, XSPH, true, false, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
+    } else {
+        rates_block<K, XSPH, false, false, STAGED>(A, g, G, sp, R, kc, D, dbase, pre);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1342,6 +1402,15 @@ int brick_rates(sph_ctx *ctx, int dst, const sph_source_term &term, NbrList &L,
     a.add_velocity = prm->add_velocity;
     a.add_gravity = prm->add_gravity;
     a.accumulate = accumulate;
+    // alpha cs / 2 = (alpha / 2) f (2 (rho / 2))^3 with cs = f rho^3; the
+    // environment setting SPH_BRICK_TWO_RECORDS=0 keeps three records
+    static int two = -1;
+    if (two < 0) {
+        const char *e = getenv("SPH_BRICK_TWO_RECORDS");
+        two = (e && atoi(e) == 0) ? 0 : 1;
+    }
+    a.tait_state = two && S.st_tait_f > 0.0 ? 1 : 0;
+    a.tait_kc = (float)(4.0 * term.alpha * S.st_tait_f);
     a.gx = prm->gx; a.gy = prm->gy; a.gz = prm->gz;
     for (int c = 0; c < 3; ++c) {
         a.acc[c] = acc ? acc[c] : nullptr;

@@ -745,6 +745,7 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
             count_launch(3);
             SPH_LAUNCH_CHECK("nnps sort/reorder");
             A.st_fresh = true;
+            A.st_tait_f = 0.0;
             if (g.skin > 0.f) {
                 if (A.pm0_cap < v.n) {
                     cudaFree(A.pm0);
@@ -947,6 +948,7 @@ int ensure_state(sph_ctx *ctx, int a) {
     ArraySnap &A = ctx->arrays[a];
     if (A.st_fresh) return SPH_OK;
     A.st_fresh = true;
+    A.st_tait_f = 0.0;
     if (A.n == 0) return SPH_OK;
     if (!A.inv) return set_error(SPH_ERR_STATE, "state refresh without a light-refresh order");
     k_state<<<grid_blocks(A.n, kThreads, 64), kThreads, 0, ctx->stream>>>(A.view, A.inv, A.st);
@@ -967,6 +969,7 @@ int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view) {
     A.view = *view;
     A.has_nrm = nrm;
     A.st_fresh = true;
+    A.st_tait_f = 0.0;
     if (A.n == 0) return SPH_OK;
     k_reorder<<<grid_blocks(A.n, kThreads), kThreads, 0, ctx->stream>>>(
         A.view, ctx->grid, A.perm, A.key, A.skey, A.scx, A.velh, A.st, nrm ? A.nrm : nullptr,

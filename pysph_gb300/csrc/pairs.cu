@@ -864,6 +864,13 @@ int gated_pass(sph_ctx *ctx, Pass &&pass) {
     return rebuilt ? pass() : SPH_OK;
 }
 
+// cs / rho^3 of the state records a density pass with these parameters
+// writes, when its Tait equation has gamma = 7 (0 otherwise)
+static double st_tait_factor(const sph_density_params *prm) {
+    if (!prm->tait || prm->gamma != 7.0 || !(prm->ro > 0.0)) return 0.0;
+    return prm->co / (prm->ro * prm->ro * prm->ro);
+}
+
 int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_density_params *prm,
                  double *rho, double *p, double *cs) {
     if (!ctx->built) return set_error(SPH_ERR_STATE, "density: no neighbour build");
@@ -889,7 +896,10 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
         const int rb = brick_density(ctx, dst, srcs[0], *L, stale, true, prm, rho, p, cs,
                                      own ? D.st : nullptr);
         if (rb) return rb;
-        if (own) D.st_fresh = true;
+        if (own) {
+            D.st_fresh = true;
+            D.st_tait_f = st_tait_factor(prm);
+        }
         if (stale) L->build = ctx->build_id;
         ctx->n_brick_passes += 1;
         return SPH_OK;
@@ -954,7 +964,10 @@ int density_pass(sph_ctx *ctx, int dst, const int *srcs, int nsrc, const sph_den
 #undef DLAUNCH
     count_launch();
     SPH_LAUNCH_CHECK("k_density");
-    if (a.st_out) D.st_fresh = true;   // every slot's state record rewritten
+    if (a.st_out) {
+        D.st_fresh = true;   // every slot's state record rewritten
+        D.st_tait_f = st_tait_factor(prm);
+    }
     for (int i = 0; i < nsrc; ++i)
         if (built[i]) built[i]->build = ctx->build_id;
     return SPH_OK;

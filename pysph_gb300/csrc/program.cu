@@ -72,6 +72,7 @@ struct sph_step {
     long long passes = 0;          // brick-staged pair passes of one replay
     // host state of the context after a captured step (restored after a replay)
     std::vector<bool> st_fresh;
+    std::vector<double> st_tait_f;
     cudaEvent_t done = nullptr;
     // device time of the replays (CUDA events around each graph launch)
     cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -172,9 +173,11 @@ int capture(sph_step *s) {
     const long long light0 = ctx->n_light;
     // host state the capture may change without running anything
     std::vector<bool> fresh0;
+    std::vector<double> tait0;
     std::vector<sph_array_view> views0;
     for (const auto &A : ctx->arrays) {
         fresh0.push_back(A.st_fresh);
+        tait0.push_back(A.st_tait_f);
         views0.push_back(A.view);
     }
     cudaGraph_t graph = nullptr;
@@ -259,13 +262,18 @@ int capture(sph_step *s) {
         drop_graph(s);
         for (size_t a = 0; a < ctx->arrays.size() && a < fresh0.size(); ++a) {
             ctx->arrays[a].st_fresh = fresh0[a];
+            ctx->arrays[a].st_tait_f = tait0[a];
             ctx->arrays[a].view = views0[a];
         }
         return SPH_OK;
     }
     s->graph_build = build;
     s->st_fresh.clear();
-    for (const auto &A : ctx->arrays) s->st_fresh.push_back(A.st_fresh);
+    s->st_tait_f.clear();
+    for (const auto &A : ctx->arrays) {
+        s->st_fresh.push_back(A.st_fresh);
+        s->st_tait_f.push_back(A.st_tait_f);
+    }
     s->n_captures += 1;
     return SPH_OK;
 }
@@ -283,8 +291,10 @@ int replay(sph_step *s) {
     }
     count_launch(s->launches);
     ctx->n_brick_passes += s->passes;
-    for (size_t a = 0; a < ctx->arrays.size() && a < s->st_fresh.size(); ++a)
+    for (size_t a = 0; a < ctx->arrays.size() && a < s->st_fresh.size(); ++a) {
         ctx->arrays[a].st_fresh = s->st_fresh[a];
+        ctx->arrays[a].st_tait_f = s->st_tait_f[a];
+    }
     list_maxima_collect(ctx);
     const unsigned err = ctx->h_status[0];
     const unsigned bits = ctx->h_status[kStaleBitsWord];

@@ -119,6 +119,9 @@ struct ArraySnap {
     // to the next density pass, or to a state refresh before a pass that
     // reads it)
     bool st_fresh = true;
+    // st's cs was written by the Tait equation with gamma = 7 from st's rho:
+    // cs = st_tait_f rho^3 (co / ro^3); 0 when st came from anything else
+    double st_tait_f = 0.0;
     int *key = nullptr;   // original order, dense cell index
     int *perm = nullptr;  // sorted -> original
     int *skey = nullptr;  // sorted: cell

@@ -91,6 +91,29 @@ def test_drop_euler_step_with_xsph(monkeypatch):
         assert normwise(outs[True][p] - props[p], ref[p] - props[p]) < TOL, p
 
 
+def test_cube_step_mixed_masses(monkeypatch):
+    """A block whose sources share one mass reads two records per pair in
+    the rates pass (cs from rho through Tait), any other block three.  Masses
+    2 % heavier in one corner of the cube mix both kinds of block in one
+    pass: the step matches the list-streaming kernels and the oracle."""
+    _need_gpu()
+    props = W.cube_lattice(32768, seed=25)
+    corner = (props["x"] < 0.3) & (props["y"] < 0.3)
+    props["m"] = np.where(corner, 1.02 * props["m"], props["m"])
+    got, nb = _cube_step(props, True, monkeypatch)
+    ref_list, _ = _cube_step(props, False, monkeypatch)
+    assert nb == 4
+    prob = oracle.Problem({"fluid": props}, oracle.cube_ops(), dim=3)
+    prob.integrate_rk2(1e-4)
+    ref = prob.arrays["fluid"]
+    for p in ("rho", "p", "cs"):
+        assert normwise(got[p], ref_list[p]) < SAME, p
+        assert normwise(got[p], ref[p]) < TOL, p
+    for p in ("x", "y", "z", "u", "v", "w"):
+        assert normwise(got[p] - props[p], ref_list[p] - props[p]) < SAME, p
+        assert normwise(got[p] - props[p], ref[p] - props[p]) < TOL, p
+
+
 def test_light_refresh_trajectory_matches_list_kernels(monkeypatch):
     """Twenty RK2 steps with the list skin (light refreshes between full
     builds): the brick-staged and list-streaming trajectories agree."""
@@ -163,12 +186,14 @@ print("ok")
 
 
 @pytest.mark.parametrize("env", [{"SPH_BRICK_UNSTAGED": "1"}, {"SPH_LIST_CAP": "9"},
-                                 {"SPH_BRICK_UNSTAGED": "1", "SPH_LIST_CAP": "9"}],
-                         ids=["global-records", "over-full-lists", "both"])
+                                 {"SPH_BRICK_UNSTAGED": "1", "SPH_LIST_CAP": "9"},
+                                 {"SPH_BRICK_TWO_RECORDS": "0"}],
+                         ids=["global-records", "over-full-lists", "both", "three-records"])
 def test_brick_fallback_paths_match_oracle(env):
     """Records read from global memory (bricks too populous for shared
-    memory) and lists shorter than the neighbour counts (completed by
-    re-traversal), forced on small sets in a fresh process."""
+    memory), lists shorter than the neighbour counts (completed by
+    re-traversal) and the rates pass's three records per pair in every
+    block, forced on small sets in a fresh process."""
     _need_gpu()
     e = dict(os.environ, PYSPH_GB300_BRICKS="1", **env)
     r = subprocess.run([sys.executable, "-c", _SUB], cwd=ROOT, env=e, capture_output=True,
