@@ -82,3 +82,38 @@ def test_save_copies_the_result():
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), x0 + k1 * 1e-3)
     np.testing.assert_array_equal(save.cpu().numpy(), out.cpu().numpy())
+
+
+def test_lines_of_one_launch_chained_and_independent():
+    """Several lines in one launch.  Independent lines (none reads what
+    another writes) have their loads issued together; a line that reads an
+    earlier line's output sees that output, as in one NumPy statement after
+    the other."""
+    _need_gpu()
+    n = 65_537
+    x0, y0, k1, k2, k3 = _arrays(n, 5, 2)
+    X0, Y0, K1, K2, K3 = (torch.from_numpy(a).cuda() for a in (x0, y0, k1, k2, k3))
+    dt = 3.3e-4
+    cm = _CM()
+    # independent: two RK2-style lines and a copy, each with its own output
+    ox, oy, oc = (torch.empty_like(X0) for _ in range(3))
+    gpu.axpy(cm, n, [(ox, None, X0, K1, K2, 0.5 * dt, 0),
+                     (oy, None, Y0, K3, None, dt, 1),
+                     (oc, None, X0, K1, None, 0.0, 2)])
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ox.cpu().numpy(), x0 + 0.5 * dt * (k1 + k2))
+    np.testing.assert_array_equal(oy.cpu().numpy(), y0 + k3 * dt)
+    np.testing.assert_array_equal(oc.cpu().numpy(), x0)
+    # chained: the second line reads the first's output, the third the
+    # second's saved copy
+    a, b, c, sb = (torch.empty_like(X0) for _ in range(4))
+    gpu.axpy(cm, n, [(a, None, X0, K1, None, dt, 1),
+                     (b, sb, a, K2, None, dt, 1),
+                     (c, None, sb, a, None, 0.0, 3)])
+    torch.cuda.synchronize()
+    ra = x0 + k1 * dt
+    rb = ra + k2 * dt
+    np.testing.assert_array_equal(a.cpu().numpy(), ra)
+    np.testing.assert_array_equal(b.cpu().numpy(), rb)
+    np.testing.assert_array_equal(sb.cpu().numpy(), rb)
+    np.testing.assert_array_equal(c.cpu().numpy(), 2 * rb - ra)
