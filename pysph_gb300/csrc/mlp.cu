@@ -174,6 +174,33 @@ __device__ __forceinline__ float dgelu(float z) {
     return fmaf(0.5f * z * (1.f - t * t), du, 0.5f * (1.f + t));
 }
 
+// The same derivative with s = 1 / (1 + e^(2u)) (so 1 + t = 2 (1 - s) and
+// 1 - t^2 = 4 s (1 - s)):  d gelu / dz = (1 - s) (1 + 2 z s u'), the
+// exponential and the reciprocal by the approximate special-function
+// instructions (relative error near 2^-22; the backward's gradients are
+// compared at 5e-3).
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float kGeluC = 0.79788456080286536f;             // sqrt(2/pi)
+constexpr float kGeluE0 = 2.f * 1.4426950408889634f * kGeluC;   // 2u log2(e) = z (E0 + E1 z^2)
+constexpr float kGeluE1 = kGeluE0 * 0.044715f;
+constexpr float kGeluD0 = 2.f * kGeluC;                    // 2u' = D0 + D1 z^2
+constexpr float kGeluD1 = kGeluD0 * 0.134145f;
+__device__ __forceinline__ float dgelu_s(float z) {
+    const float z2 = z * z;
+    const float e = ex2_approx(z * fmaf(kGeluE1, z2, kGeluE0));
+    const float sg = rcp_approx(1.f + e);
+    return (1.f - sg) * fmaf(z * fmaf(kGeluD1, z2, kGeluD0), sg, 1.f);
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t *>(&h);
@@ -966,6 +993,369 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// backward with TMA tiles and MN-major operands
+// ---------------------------------------------------------------------------
+// The weight gradients contract over the samples of a tile: dW2 [j][i] =
+// sum_b dz2 [b][j] h1 [b][i].  Their operands stay in the sample-major
+// layout they arrive in (h1 and x tiles by TMA, dz2 and dz1 written one row
+// per thread): read with MN-major descriptors (the contiguous dimension is M
+// or N, K = samples strides across 128-byte rows), so nothing is
+// transposed.  The same bytes serve as K-major operands where the
+// contraction runs along the row (dh1 = dz2 W2 and the recomputed z2 =
+// h1 W2^T + b2, which replaces reading the saved z2).  The next tile's h1
+// and x are loaded while this tile's epilogues run.
+//
+// Shared memory, 1024-byte aligned: 14 atoms of 16 KB (128 rows x 128
+// bytes, 128-byte swizzling), placed so that every operand's blocks sit at
+// one stride (the descriptors' offsets):
+//   0 h1 [b][0:64]    1-2 A1 = dz2 [b][j]   3 W2^T [i][0:64]
+//   4 h1 [b][64:128]  5-7 x [b][m]          8 ones (first column 1: the bias
+//                                              gradients db2, db1 in the dW
+//                                              products of h1 and x)
+//   9 W2^T [i][64:128]  10-13 z1 [b][j] in FP32 (32 columns per atom),
+//                       and A2 = dz1 [b][j] in 10-11 once z1 has been read.
+// So h1 as the dW2 operand has blocks 0, 4, 8 (stride 4 atoms), x blocks
+// 5 .. 8, W2^T blocks 3, 9.
+constexpr uint32_t R_AH1 = 0, R_AA1 = 1, R_AW2T = 3, R_AX = 5, R_AONE = 8, R_AZ1 = 10,
+                   R_AA2 = 10, R_ATOMS = 14;
+constexpr uint32_t R_B2 = R_ATOMS * ATOM;             // float [128]
+constexpr uint32_t R_W3 = R_B2 + NH * 4;              // float [2][128]
+constexpr uint32_t R_RED = R_W3 + NOUT * NH * 4;      // float [16] loss per warp
+enum RBar { RB_H = 0, RB_X, RB_Z, RB_M, RB_N };
+constexpr uint32_t R_BAR = R_RED + 16 * 4;
+constexpr uint32_t R_SLOT = R_BAR + RB_N * 8;
+constexpr uint32_t R_ABORT = R_SLOT + 4;
+constexpr uint32_t R_BYTES = R_ABORT + 4 + 1024;      // + alignment of the base
+static_assert(R_BYTES <= 232448, "shared memory of one CTA");
+constexpr int R_WARPS = 16;                           // four per lane quarter, 32 columns each
+constexpr int R_THREADS = 32 * R_WARPS;
+constexpr int R_COLS = NH / (R_WARPS / 4);
+// tensor memory: z2, then dh1, at 0 (128 columns); dW2 | db2 at 128 (144);
+// dW1 | db1 at 288 (208)
+constexpr uint32_t R_TZ = 0, R_TW2 = 128, R_TW1 = 288;
+constexpr int R_N2 = NH + 16, R_N1 = NIN + 16;
+static_assert(R_TW2 + R_N2 <= R_TW1 && R_TW1 + R_N1 <= 512, "tensor memory plan");
+
+// Shared-memory matrix descriptor, MN-major with 128-byte swizzling: blocks
+// of 64 elements along M (or N) at lbo bytes, groups of eight K rows at
+// 1024 B (version 1, swizzle mode 2).  A K step of 16 advances the start by
+// two groups (2048 B).
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t saddr, uint32_t lbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// kind::f16 instruction descriptor with MN-major A (bit 15) and / or B (bit 16)
+constexpr uint32_t idesc_bf16_mn(int M, int N, bool a_mn, bool b_mn) {
+    return idesc_bf16(M, N) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u);
+}
+
+struct BwdMaps {
+    CUtensorMap x, h1, z1;
+};
+
+__global__ void __launch_bounds__(R_THREADS, 1)
+    k_mlp_bwd_tma(const __grid_constant__ BwdMaps maps, const MlpDev W,
+                  const float *__restrict__ y, const float *__restrict__ target, int64_t n,
+                  float inv_count, float *__restrict__ dy_out, float *__restrict__ part,
+                  float *__restrict__ part_loss, unsigned *err) {
+    extern __shared__ __align__(1024) uint8_t rsm_raw[];
+    const uint32_t raw = smem_u32(rsm_raw);
+    uint8_t *sm = rsm_raw + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t sbase = smem_u32(sm);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    // row = sample (tensor-memory lane); the four warps of a lane quarter
+    // take 32 columns each
+    const int q = warp & 3, cp = warp >> 2;
+    const int row = q * 32 + lane;
+    const int cb = cp * R_COLS;
+    float *b2f = reinterpret_cast<float *>(sm + R_B2);
+    float *w3f = reinterpret_cast<float *>(sm + R_W3);
+    float *red = reinterpret_cast<float *>(sm + R_RED);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + R_SLOT);
+    volatile int *abort = reinterpret_cast<volatile int *>(sm + R_ABORT);
+    auto bar = [&](int i) { return sbase + R_BAR + 8u * (uint32_t)i; };
+    auto atom = [&](uint32_t k) { return sbase + k * ATOM; };
+
+    // W2^T [i][j] into atoms 3 and 9 (columns j 0-63, 64-127)
+    for (int c = t; c < NH * (NH / 8); c += R_THREADS) {
+        const int r = c >> 4, k8 = c & 15;
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(W.w2t + r * NH + k8 * 8));
+        const uint32_t a = k8 < 8 ? R_AW2T : R_AW2T + 6;
+        *reinterpret_cast<uint4 *>(sm + a * ATOM + sw128_off(r, k8 & 7)) = v;
+    }
+    for (int i = t; i < NH; i += R_THREADS) b2f[i] = W.params[OFF_B2 + i];
+    for (int i = t; i < NOUT * NH; i += R_THREADS) w3f[i] = __uint_as_float((uint32_t)W.w3[i] << 16);
+    // the ones atom: column 0 one, the rest zero
+    for (int c = t; c < TILE * 8; c += R_THREADS) {
+        const int r = c >> 3, k = c & 7;
+        *reinterpret_cast<uint4 *>(sm + R_AONE * ATOM + sw128_off(r, k)) =
+            make_uint4(k == 0 ? 0x3F80u : 0u, 0u, 0u, 0u);
+    }
+    if (t == 0) {
+        *abort = 0;
+        for (int k = 0; k < RB_N; ++k) mbar_init(bar(k), 1);
+    }
+    if (warp == 0) tmem_alloc(smem_u32(slot), 512);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *slot;
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    const int mine = ntiles > blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    auto tile_row0 = [&](int i) { return (int)((blockIdx.x + (int64_t)i * gridDim.x) * TILE); };
+    auto load_h1 = [&](int i) {
+        mbar_expect_tx(bar(RB_H), 2 * ATOM);
+        tma_load_2d(atom(R_AH1), &maps.h1, bar(RB_H), 0, tile_row0(i));
+        tma_load_2d(atom(R_AH1 + 4), &maps.h1, bar(RB_H), 64, tile_row0(i));
+    };
+    auto load_x = [&](int i) {
+        mbar_expect_tx(bar(RB_X), 3 * ATOM);
+        for (int a = 0; a < 3; ++a)
+            tma_load_2d(atom(R_AX + a), &maps.x, bar(RB_X), 64 * a, tile_row0(i));
+    };
+    auto load_z1 = [&](int i) {
+        mbar_expect_tx(bar(RB_Z), 4 * ATOM);
+        for (int a = 0; a < 4; ++a)
+            tma_load_2d(atom(R_AZ1 + a), &maps.z1, bar(RB_Z), 32 * a, tile_row0(i));
+    };
+    // loads issued, and waited for by thread 0
+    int h_issued = 0, x_issued = 0, z_issued = 0, h_done = 0, x_done = 0, z_done = 0;
+    if (t == 0 && mine > 0) {
+        load_h1(0);
+        load_x(0);
+        load_z1(0);
+        h_issued = x_issued = z_issued = 1;
+    }
+    constexpr uint32_t ID_Z = idesc_bf16_mn(128, NH, false, true);
+    constexpr uint32_t ID_DH = idesc_bf16(128, NH);
+    constexpr uint32_t ID_W2 = idesc_bf16_mn(128, R_N2, true, true);
+    constexpr uint32_t ID_W1 = idesc_bf16_mn(128, R_N1, true, true);
+    // K step s (16 of 128) of a K-major operand in atoms a0 (K 0-63) and a1
+    auto kstep = [&](uint32_t a0, uint32_t a1, int s) {
+        return atom(s < 4 ? a0 : a1) + (uint32_t)(s & 3) * 32;
+    };
+    uint32_t pm = 0;     // phase of the MMA barrier
+    bool ok = true;
+    float loss = 0.f;
+    // this row's outputs and targets, a tile ahead
+    float4 yt = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto load_yt = [&](int i) {
+        const int64_t b = (int64_t)tile_row0(i) + row;
+        if (b < n) {
+            const float2 a = *reinterpret_cast<const float2 *>(y + b * 2);
+            const float2 c = *reinterpret_cast<const float2 *>(target + b * 2);
+            yt = make_float4(a.x, a.y, c.x, c.y);
+        }
+    };
+    if (mine > 0) load_yt(0);
+
+    for (int i = 0; i < mine; ++i) {
+        const int64_t b = (int64_t)tile_row0(i) + row;
+        const bool valid = b < n;
+        // z2 = h1 W2^T (the bias added below)
+        if (t == 0) {
+            ok = gwait(bar(RB_H), i & 1, abort);
+            h_done = i + 1;
+            if (ok) {
+                tc_fence_after();
+#pragma unroll
+                for (int s = 0; s < NH / 16; ++s)
+                    mma_bf16(tbase + R_TZ, sdesc_sw128(kstep(R_AH1, R_AH1 + 4, s)),
+                             sdesc_sw128_mn(atom(R_AW2T) + 2048u * s, 6 * ATOM), ID_Z, s > 0);
+                mma_commit(bar(RB_M));
+            }
+        }
+        float d0 = 0.f, d1 = 0.f;
+        if (valid) {
+            const float e0 = yt.x - yt.z, e1 = yt.y - yt.w;
+            d0 = e0 * inv_count;
+            d1 = e1 * inv_count;
+            if (cp == 0) {
+                loss += e0 * e0 + e1 * e1;
+                *reinterpret_cast<float2 *>(dy_out + b * 2) = make_float2(d0, d1);
+            }
+        }
+        if (i + 1 < mine) load_yt(i + 1);
+        if (!__syncthreads_and(ok)) break;
+        ok = gwait(bar(RB_M), pm, abort);
+        pm ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+        // dz2 = (dy W3) * gelu'(z2) -> A1 row `row`, columns cb .. cb + 31
+#pragma unroll
+        for (int c = 0; c < R_COLS / 16; ++c) {
+            float v[16];
+            tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
+            uint32_t w[8];
+#pragma unroll
+            for (int e4 = 0; e4 < 4; ++e4) {
+                const int j = cb + 16 * c + 4 * e4;
+                const float4 bb = *reinterpret_cast<const float4 *>(b2f + j);
+                const float4 wa = *reinterpret_cast<const float4 *>(w3f + j);
+                const float4 wb = *reinterpret_cast<const float4 *>(w3f + NH + j);
+                const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
+                const float av[4] = {wa.x, wa.y, wa.z, wa.w};
+                const float cv[4] = {wb.x, wb.y, wb.z, wb.w};
+                float g[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const float z = v[4 * e4 + h] + bv[h];
+                    g[h] = valid ? (d0 * av[h] + d1 * cv[h]) * dgelu_s(z) : 0.f;
+                }
+                w[2 * e4] = pack2(g[0], g[1]);
+                w[2 * e4 + 1] = pack2(g[2], g[3]);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int col = cb + 16 * c + 8 * k;
+                *reinterpret_cast<uint4 *>(sm + (R_AA1 + (col >> 6)) * ATOM +
+                                           sw128_off(row, (col & 63) >> 3)) =
+                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+            }
+        }
+        // this row's z1 columns cb .. cb + 31: atom cb / 32 of the z1 tile
+        if (t == 0) z_done = i + 1;
+        ok = gwait(bar(RB_Z), i & 1, abort);
+        float z1r[R_COLS];
+#pragma unroll
+        for (int k = 0; k < R_COLS / 4; ++k) {
+            const float4 a = *reinterpret_cast<const float4 *>(sm + (R_AZ1 + cp) * ATOM + sw128_off(row, k));
+            z1r[4 * k] = a.x; z1r[4 * k + 1] = a.y; z1r[4 * k + 2] = a.z; z1r[4 * k + 3] = a.w;
+        }
+        fence_async_smem();
+        tc_fence_before();
+        if (!__syncthreads_and(ok)) break;
+        if (t == 0) {
+            tc_fence_after();
+            // dh1 [b][i] = dz2 [b][j] W2 [j][i]   (B: W2^T rows i, K = j)
+#pragma unroll
+            for (int s = 0; s < NH / 16; ++s)
+                mma_bf16(tbase + R_TZ, sdesc_sw128(kstep(R_AA1, R_AA1 + 1, s)),
+                         sdesc_sw128(kstep(R_AW2T, R_AW2T + 6, s)), ID_DH, s > 0);
+            // dW2 [j][i] (+ db2 at column 128) += dz2^T [j][b] h1 [b][i]
+#pragma unroll
+            for (int s = 0; s < TILE / 16; ++s)
+                mma_bf16(tbase + R_TW2, sdesc_sw128_mn(atom(R_AA1) + 2048u * s, ATOM),
+                         sdesc_sw128_mn(atom(R_AH1) + 2048u * s, 4 * ATOM), ID_W2,
+                         (s > 0 || i > 0) ? 1u : 0u);
+            mma_commit(bar(RB_M));
+        }
+        ok = gwait(bar(RB_M), pm, abort);
+        pm ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+        // h1 has been read: the next tile's comes in
+        if (t == 0 && i + 1 < mine) {
+            load_h1(i + 1);
+            h_issued = i + 2;
+        }
+        // dz1 = dh1 * gelu'(z1) -> A2 row `row` (over the z1 tile, read above)
+#pragma unroll
+        for (int c = 0; c < R_COLS / 16; ++c) {
+            float v[16];
+            tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
+            uint32_t w[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const float g0 = valid ? v[2 * e] * dgelu_s(z1r[16 * c + 2 * e]) : 0.f;
+                const float g1 = valid ? v[2 * e + 1] * dgelu_s(z1r[16 * c + 2 * e + 1]) : 0.f;
+                w[e] = pack2(g0, g1);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int col = cb + 16 * c + 8 * k;
+                *reinterpret_cast<uint4 *>(sm + (R_AA2 + (col >> 6)) * ATOM +
+                                           sw128_off(row, (col & 63) >> 3)) =
+                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            ok = gwait(bar(RB_X), i & 1, abort);
+            x_done = i + 1;
+            if (ok) {
+                tc_fence_after();
+                // dW1 [j][m] (+ db1 at column 192) += dz1^T [j][b] x [b][m]
+#pragma unroll
+                for (int s = 0; s < TILE / 16; ++s)
+                    mma_bf16(tbase + R_TW1, sdesc_sw128_mn(atom(R_AA2) + 2048u * s, ATOM),
+                             sdesc_sw128_mn(atom(R_AX) + 2048u * s, ATOM), ID_W1,
+                             (s > 0 || i > 0) ? 1u : 0u);
+                mma_commit(bar(RB_M));
+            }
+        }
+        if (!__syncthreads_and(ok)) break;
+        ok = gwait(bar(RB_M), pm, abort);
+        pm ^= 1;
+        if (!__syncthreads_and(ok)) break;
+        tc_fence_after();
+        // x and A2 (over the z1 tile) have been read: the next tile's x and z1
+        if (t == 0 && i + 1 < mine) {
+            load_x(i + 1);
+            load_z1(i + 1);
+            x_issued = z_issued = i + 2;
+        }
+    }
+    // every load issued has landed before the CTA may exit
+    if (t == 0) {
+        for (int k = h_done; k < h_issued; ++k) gwait(bar(RB_H), k & 1, abort);
+        for (int k = x_done; k < x_issued; ++k) gwait(bar(RB_X), k & 1, abort);
+        for (int k = z_done; k < z_issued; ++k) gwait(bar(RB_Z), k & 1, abort);
+    }
+
+    float *P = part + (int64_t)blockIdx.x * NPARAM;
+    if (ok && mine > 0) {
+        // row j = `row` of the accumulated weight (and bias) gradients; the
+        // four warps of a lane quarter take every fourth 16-column chunk
+#pragma unroll 1
+        for (int k = cp; k < R_N2 / 16; k += 4) {
+            const int c0 = 16 * k;
+            float v[16];
+            tmem_ld16(tbase + R_TW2 + lane_base + c0, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int c = c0 + e;
+                if (c < NH) P[OFF_W2 + row * NH + c] = v[e];
+                else if (c == NH) P[OFF_B2 + row] = v[e];
+            }
+        }
+#pragma unroll 1
+        for (int k = cp; k < R_N1 / 16; k += 4) {
+            const int c0 = 16 * k;
+            float v[16];
+            tmem_ld16(tbase + R_TW1 + lane_base + c0, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int c = c0 + e;
+                if (c < NIN) P[OFF_W1 + row * NIN + c] = v[e];
+                else if (c == NIN) P[OFF_B1 + row] = v[e];
+            }
+        }
+    } else if (mine == 0) {
+        for (int k = t; k < OFF_W3; k += R_THREADS) P[k] = 0.f;
+    }
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (lane == 0) red[warp] = loss;
+    if (!ok && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (t == 0) {
+        float sum = 0.f;
+        for (int w = 0; w < R_WARPS; ++w) sum += red[w];
+        part_loss[blockIdx.x] = 0.5f * inv_count * sum;
+    }
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, 512);
+    }
+}
+
 // third layer: dW3 [o][j] = sum_b dy[b][o] h2[b][j], db3 = sum_b dy
 __global__ void k_mlp_l3(const uint16_t *__restrict__ h2s, const float *__restrict__ dy,
                          int64_t n, float *__restrict__ part) {
@@ -1110,6 +1500,9 @@ cudaError_t init_attrs() {
         }
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, B_BYTES);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_bwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     R_BYTES);
         g_attr_err = e;
     });
     return g_attr_err;
@@ -1134,12 +1527,39 @@ int encode_rows(CUtensorMap *m, const void *base, uint64_t rows, uint64_t cols) 
     return SPH_OK;
 }
 
+// Tensor map of a row-major FP32 matrix [rows][cols] (cols a multiple of
+// 32): boxes of 32 columns (128 bytes) x 128 rows with 128-byte swizzling.
+int encode_rows_f32(CUtensorMap *m, const void *base, uint64_t rows, uint64_t cols) {
+    if (!g_encode) return set_error(SPH_ERR_CUDA, "mlp: the tensor-map encoder is unavailable");
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 4};
+    const cuuint32_t box[2] = {32, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims,
+                                strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(SPH_ERR_CUDA, "mlp: cuTensorMapEncodeTiled failed");
+    return SPH_OK;
+}
+
 // environment SPH_MLP_FWD_LEGACY=1: the forward kernel without TMA and
 // warp specialisation, to measure against
 bool legacy_forward() {
     static int v = -1;
     if (v < 0) {
         const char *e = getenv("SPH_MLP_FWD_LEGACY");
+        v = (e && atoi(e) > 0) ? 1 : 0;
+    }
+    return v == 1;
+}
+
+// environment SPH_MLP_BWD_LEGACY=1: the backward kernel that stages
+// transposed copies of its operands and reads the saved z2
+bool legacy_backward() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("SPH_MLP_BWD_LEGACY");
         v = (e && atoi(e) > 0) ? 1 : 0;
     }
     return v == 1;
@@ -1208,10 +1628,22 @@ int mlp_backward(const sph_mlp_model *M, const uint16_t *x, const uint16_t *h1, 
     float *dy = part_loss + grid;
     dy = reinterpret_cast<float *>(((uintptr_t)dy + 15) & ~(uintptr_t)15);
     const MlpDev W{M->params, M->w1, M->w2, M->w2t, M->w3};
-    k_mlp_bwd<<<grid, THREADS, B_BYTES, st>>>(W, x, h1, z1, z2, y, target, n, inv_count, dy, part,
-                                               part_loss, err);
-    count_launch();
-    SPH_LAUNCH_CHECK("k_mlp_bwd");
+    if (legacy_backward()) {
+        k_mlp_bwd<<<grid, THREADS, B_BYTES, st>>>(W, x, h1, z1, z2, y, target, n, inv_count, dy,
+                                                   part, part_loss, err);
+        count_launch();
+        SPH_LAUNCH_CHECK("k_mlp_bwd");
+    } else {
+        BwdMaps maps;
+        int rc = encode_rows(&maps.x, x, (uint64_t)n, NIN);
+        if (!rc) rc = encode_rows(&maps.h1, h1, (uint64_t)n, NH);
+        if (!rc) rc = encode_rows_f32(&maps.z1, z1, (uint64_t)n, NH);
+        if (rc) return rc;
+        k_mlp_bwd_tma<<<grid, R_THREADS, R_BYTES, st>>>(maps, W, y, target, n, inv_count, dy, part,
+                                                         part_loss, err);
+        count_launch();
+        SPH_LAUNCH_CHECK("k_mlp_bwd_tma");
+    }
     k_mlp_l3<<<nl3, NH, 0, st>>>(h2, dy, n, l3);
     count_launch();
     SPH_LAUNCH_CHECK("k_mlp_l3");
