@@ -51,6 +51,9 @@ constexpr int THREADS = 256;   // two warps per tensor-memory lane quarter
 constexpr int L3_PART = NOUT * NH + NOUT;   // third-layer partial per block
 constexpr int L3_ROWS = 1024;               // rows per third-layer block
 constexpr int kMaxSpin = 1 << 22;           // bounded mbarrier wait
+// per-CTA partial gradients of the backward: rows of PART_STRIDE floats
+// (16-byte aligned)
+constexpr int PART_STRIDE = (NPARAM + 3) & ~3;
 
 // ---------------------------------------------------------------------------
 // tcgen05 / mbarrier primitives (inline PTX)
@@ -947,7 +950,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (ok && !first) {
         // row j = `row` of the accumulated weight (and bias) gradients; the
         // two warps of a lane quarter split the 16-column chunks
-        float *P = part + (int64_t)blockIdx.x * NPARAM;
+        float *P = part + (int64_t)blockIdx.x * PART_STRIDE;
         constexpr int C2 = H1T_ROWS / 16, C1 = XT_ROWS / 16;
 #pragma unroll 1
         for (int k = ch ? (C2 + 1) / 2 : 0; k < (ch ? C2 : (C2 + 1) / 2); ++k) {
@@ -974,7 +977,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
     } else if (first) {
-        float *P = part + (int64_t)blockIdx.x * NPARAM;
+        float *P = part + (int64_t)blockIdx.x * PART_STRIDE;
         for (int i = t; i < OFF_W3; i += THREADS) P[i] = 0.f;
     }
     for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
@@ -1009,34 +1012,34 @@ __global__ void __launch_bounds__(THREADS, 1)
 // Shared memory, 1024-byte aligned: 14 atoms of 16 KB (128 rows x 128
 // bytes, 128-byte swizzling), placed so that every operand's blocks sit at
 // one stride (the descriptors' offsets):
-//   0 h1 [b][0:64]    1-2 A1 = dz2 [b][j]   3 W2^T [i][0:64]
-//   4 h1 [b][64:128]  5-7 x [b][m]          8 ones (first column 1: the bias
-//                                              gradients db2, db1 in the dW
-//                                              products of h1 and x)
-//   9 W2^T [i][64:128]  10-13 z1 [b][j] in FP32 (32 columns per atom),
-//                       and A2 = dz1 [b][j] in 10-11 once z1 has been read.
+//   0 h1 [b][0:64]    1-2 A1 = dz2 [b][j], then A2 = dz1 [b][j]
+//   3 W2^T [i][0:64]  4 h1 [b][64:128]     5-7 x [b][m]
+//   8 ones (first column 1: the bias gradients db2, db1 in the dW products
+//     of h1 and x)    9 W2^T [i][64:128]   10-13 z1 [b][j] in FP32 (32
+//                                              columns per atom)
 // So h1 as the dW2 operand has blocks 0, 4, 8 (stride 4 atoms), x blocks
 // 5 .. 8, W2^T blocks 3, 9.
-constexpr uint32_t R_AH1 = 0, R_AA1 = 1, R_AW2T = 3, R_AX = 5, R_AONE = 8, R_AZ1 = 10,
-                   R_AA2 = 10, R_ATOMS = 14;
+constexpr uint32_t R_AH1 = 0, R_AA = 1, R_AW2T = 3, R_AX = 5, R_AONE = 8, R_AZ1 = 10,
+                   R_ATOMS = 14;
 constexpr uint32_t R_B2 = R_ATOMS * ATOM;             // float [128]
 constexpr uint32_t R_W3 = R_B2 + NH * 4;              // float [2][128]
 constexpr uint32_t R_RED = R_W3 + NOUT * NH * 4;      // float [16] loss per warp
-enum RBar { RB_H = 0, RB_X, RB_Z, RB_M, RB_N };
+// mbarriers: TMA tiles full (h1, x, z1); products done (z2, dh1, dW2, dW1);
+// epilogue steps done (A1 written and z1 read, dh1 read, A2 written)
+enum RBar { RB_H = 0, RB_X, RB_Z, RB_FZ, RB_FDH, RB_EH, RB_EX, RB_A1, RB_ZC, RB_A2, RB_N };
 constexpr uint32_t R_BAR = R_RED + 16 * 4;
 constexpr uint32_t R_SLOT = R_BAR + RB_N * 8;
 constexpr uint32_t R_ABORT = R_SLOT + 4;
 constexpr uint32_t R_BYTES = R_ABORT + 4 + 1024;      // + alignment of the base
 static_assert(R_BYTES <= 232448, "shared memory of one CTA");
-constexpr int R_WARPS = 16;                           // four per lane quarter, 32 columns each
-constexpr int R_THREADS = 32 * R_WARPS;
-constexpr int R_COLS = NH / (R_WARPS / 4);
+constexpr int R_EPI = 16;                             // epilogue warps: four per lane quarter
+constexpr int R_THREADS = 32 * (R_EPI + 1);           // + the TMA / MMA warp
+constexpr int R_COLS = NH / (R_EPI / 4);              // 32 columns per epilogue warp
 // tensor memory: z2, then dh1, at 0 (128 columns); dW2 | db2 at 128 (144);
 // dW1 | db1 at 288 (208)
 constexpr uint32_t R_TZ = 0, R_TW2 = 128, R_TW1 = 288;
 constexpr int R_N2 = NH + 16, R_N1 = NIN + 16;
 static_assert(R_TW2 + R_N2 <= R_TW1 && R_TW1 + R_N1 <= 512, "tensor memory plan");
-
 // Shared-memory matrix descriptor, MN-major with 128-byte swizzling: blocks
 // of 64 elements along M (or N) at lbo bytes, groups of eight K rows at
 // 1024 B (version 1, swizzle mode 2).  A K step of 16 advances the start by
@@ -1055,6 +1058,15 @@ struct BwdMaps {
     CUtensorMap x, h1, z1;
 };
 
+// Warp-specialised: warp 16 issues the TMA loads and the products, warps
+// 0-15 run the epilogues.  Per tile i (the products in tensor-core order):
+//   z2(i) = h1 W2^T              after h1(i) landed and dh1(i-1) was read
+//   dW1(i-1) += dz1^T x          after A2(i-1) was written
+//   dh1(i) = dz2 W2, dW2(i) += dz2^T h1   after A1(i) was written
+// so the tensor cores work on z2(i + 1) and dW1(i) while the epilogue warps
+// compute dz1(i), and on dW2(i) during the same epilogue.  h1(i + 1) is
+// loaded once dW2(i) has read h1(i), z1(i + 1) once every epilogue warp has
+// read z1(i), x(i) once dW1(i - 1) has read x(i - 1).
 __global__ void __launch_bounds__(R_THREADS, 1)
     k_mlp_bwd_tma(const __grid_constant__ BwdMaps maps, const MlpDev W,
                   const float *__restrict__ y, const float *__restrict__ target, int64_t n,
@@ -1065,11 +1077,6 @@ __global__ void __launch_bounds__(R_THREADS, 1)
     uint8_t *sm = rsm_raw + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t sbase = smem_u32(sm);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    // row = sample (tensor-memory lane); the four warps of a lane quarter
-    // take 32 columns each
-    const int q = warp & 3, cp = warp >> 2;
-    const int row = q * 32 + lane;
-    const int cb = cp * R_COLS;
     float *b2f = reinterpret_cast<float *>(sm + R_B2);
     float *w3f = reinterpret_cast<float *>(sm + R_W3);
     float *red = reinterpret_cast<float *>(sm + R_RED);
@@ -1095,7 +1102,8 @@ __global__ void __launch_bounds__(R_THREADS, 1)
     }
     if (t == 0) {
         *abort = 0;
-        for (int k = 0; k < RB_N; ++k) mbar_init(bar(k), 1);
+        for (int k = 0; k < RB_N; ++k)
+            mbar_init(bar(k), (k == RB_A1 || k == RB_ZC || k == RB_A2) ? R_EPI : 1);
     }
     if (warp == 0) tmem_alloc(smem_u32(slot), 512);
     fence_async_smem();
@@ -1103,251 +1111,276 @@ __global__ void __launch_bounds__(R_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *slot;
-    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     const int64_t ntiles = (n + TILE - 1) / TILE;
     const int mine = ntiles > blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
     auto tile_row0 = [&](int i) { return (int)((blockIdx.x + (int64_t)i * gridDim.x) * TILE); };
-    auto load_h1 = [&](int i) {
-        mbar_expect_tx(bar(RB_H), 2 * ATOM);
-        tma_load_2d(atom(R_AH1), &maps.h1, bar(RB_H), 0, tile_row0(i));
-        tma_load_2d(atom(R_AH1 + 4), &maps.h1, bar(RB_H), 64, tile_row0(i));
-    };
-    auto load_x = [&](int i) {
-        mbar_expect_tx(bar(RB_X), 3 * ATOM);
-        for (int a = 0; a < 3; ++a)
-            tma_load_2d(atom(R_AX + a), &maps.x, bar(RB_X), 64 * a, tile_row0(i));
-    };
-    auto load_z1 = [&](int i) {
-        mbar_expect_tx(bar(RB_Z), 4 * ATOM);
-        for (int a = 0; a < 4; ++a)
-            tma_load_2d(atom(R_AZ1 + a), &maps.z1, bar(RB_Z), 32 * a, tile_row0(i));
-    };
-    // loads issued, and waited for by thread 0
-    int h_issued = 0, x_issued = 0, z_issued = 0, h_done = 0, x_done = 0, z_done = 0;
-    if (t == 0 && mine > 0) {
-        load_h1(0);
-        load_x(0);
-        load_z1(0);
-        h_issued = x_issued = z_issued = 1;
-    }
-    constexpr uint32_t ID_Z = idesc_bf16_mn(128, NH, false, true);
-    constexpr uint32_t ID_DH = idesc_bf16(128, NH);
-    constexpr uint32_t ID_W2 = idesc_bf16_mn(128, R_N2, true, true);
-    constexpr uint32_t ID_W1 = idesc_bf16_mn(128, R_N1, true, true);
-    // K step s (16 of 128) of a K-major operand in atoms a0 (K 0-63) and a1
-    auto kstep = [&](uint32_t a0, uint32_t a1, int s) {
-        return atom(s < 4 ? a0 : a1) + (uint32_t)(s & 3) * 32;
-    };
-    uint32_t pm = 0;     // phase of the MMA barrier
     bool ok = true;
-    float loss = 0.f;
-    // this row's outputs and targets, a tile ahead
-    float4 yt = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto load_yt = [&](int i) {
-        const int64_t b = (int64_t)tile_row0(i) + row;
-        if (b < n) {
-            const float2 a = *reinterpret_cast<const float2 *>(y + b * 2);
-            const float2 c = *reinterpret_cast<const float2 *>(target + b * 2);
-            yt = make_float4(a.x, a.y, c.x, c.y);
-        }
-    };
-    if (mine > 0) load_yt(0);
 
-    for (int i = 0; i < mine; ++i) {
-        const int64_t b = (int64_t)tile_row0(i) + row;
-        const bool valid = b < n;
-        // z2 = h1 W2^T (the bias added below)
-        if (t == 0) {
-            ok = gwait(bar(RB_H), i & 1, abort);
-            h_done = i + 1;
-            if (ok) {
+    if (warp == R_EPI) {
+        if (lane == 0) {
+            // ---- TMA loads and products ----
+            auto load_h1 = [&](int i) {
+                mbar_expect_tx(bar(RB_H), 2 * ATOM);
+                tma_load_2d(atom(R_AH1), &maps.h1, bar(RB_H), 0, tile_row0(i));
+                tma_load_2d(atom(R_AH1 + 4), &maps.h1, bar(RB_H), 64, tile_row0(i));
+            };
+            auto load_x = [&](int i) {
+                mbar_expect_tx(bar(RB_X), 3 * ATOM);
+                for (int a = 0; a < 3; ++a)
+                    tma_load_2d(atom(R_AX + a), &maps.x, bar(RB_X), 64 * a, tile_row0(i));
+            };
+            auto load_z1 = [&](int i) {
+                mbar_expect_tx(bar(RB_Z), 4 * ATOM);
+                for (int a = 0; a < 4; ++a)
+                    tma_load_2d(atom(R_AZ1 + a), &maps.z1, bar(RB_Z), 32 * a, tile_row0(i));
+            };
+            // K step s (16 of 128) of a K-major operand in atoms a0 (K 0-63) and a1
+            auto kstep = [&](uint32_t a0, uint32_t a1, int s) {
+                return atom(s < 4 ? a0 : a1) + (uint32_t)(s & 3) * 32;
+            };
+            constexpr uint32_t ID_Z = idesc_bf16_mn(128, NH, false, true);
+            constexpr uint32_t ID_DH = idesc_bf16(128, NH);
+            constexpr uint32_t ID_W2 = idesc_bf16_mn(128, R_N2, true, true);
+            constexpr uint32_t ID_W1 = idesc_bf16_mn(128, R_N1, true, true);
+            auto dw1 = [&](int i) -> bool {
+                // dW1 [j][m] (+ db1 at column 192) += dz1^T [j][b] x [b][m]
+                if (!gwait(bar(RB_A2), i & 1, abort) || !gwait(bar(RB_X), i & 1, abort))
+                    return false;
+                tc_fence_after();
+#pragma unroll
+                for (int s = 0; s < TILE / 16; ++s)
+                    mma_bf16(tbase + R_TW1, sdesc_sw128_mn(atom(R_AA) + 2048u * s, ATOM),
+                             sdesc_sw128_mn(atom(R_AX) + 2048u * s, ATOM), ID_W1,
+                             (s > 0 || i > 0) ? 1u : 0u);
+                mma_commit(bar(RB_EX));
+                return true;
+            };
+            int nh = 0, nx = 0, nz = 0;   // loads issued
+            if (mine > 0) {
+                load_h1(0);
+                load_x(0);
+                load_z1(0);
+                nh = nx = nz = 1;
+            }
+            for (int i = 0; i < mine; ++i) {
+                // z2(i) = h1 W2^T (the bias added by the epilogue)
+                if (!gwait(bar(RB_H), i & 1, abort)) break;
+                if (i > 0 && !gwait(bar(RB_ZC), (i - 1) & 1, abort)) break;
                 tc_fence_after();
 #pragma unroll
                 for (int s = 0; s < NH / 16; ++s)
                     mma_bf16(tbase + R_TZ, sdesc_sw128(kstep(R_AH1, R_AH1 + 4, s)),
                              sdesc_sw128_mn(atom(R_AW2T) + 2048u * s, 6 * ATOM), ID_Z, s > 0);
-                mma_commit(bar(RB_M));
-            }
-        }
-        float d0 = 0.f, d1 = 0.f;
-        if (valid) {
-            const float e0 = yt.x - yt.z, e1 = yt.y - yt.w;
-            d0 = e0 * inv_count;
-            d1 = e1 * inv_count;
-            if (cp == 0) {
-                loss += e0 * e0 + e1 * e1;
-                *reinterpret_cast<float2 *>(dy_out + b * 2) = make_float2(d0, d1);
-            }
-        }
-        if (i + 1 < mine) load_yt(i + 1);
-        if (!__syncthreads_and(ok)) break;
-        ok = gwait(bar(RB_M), pm, abort);
-        pm ^= 1;
-        if (!__syncthreads_and(ok)) break;
-        tc_fence_after();
-        // dz2 = (dy W3) * gelu'(z2) -> A1 row `row`, columns cb .. cb + 31
-#pragma unroll
-        for (int c = 0; c < R_COLS / 16; ++c) {
-            float v[16];
-            tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
-            uint32_t w[8];
-#pragma unroll
-            for (int e4 = 0; e4 < 4; ++e4) {
-                const int j = cb + 16 * c + 4 * e4;
-                const float4 bb = *reinterpret_cast<const float4 *>(b2f + j);
-                const float4 wa = *reinterpret_cast<const float4 *>(w3f + j);
-                const float4 wb = *reinterpret_cast<const float4 *>(w3f + NH + j);
-                const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
-                const float av[4] = {wa.x, wa.y, wa.z, wa.w};
-                const float cv[4] = {wb.x, wb.y, wb.z, wb.w};
-                float g[4];
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const float z = v[4 * e4 + h] + bv[h];
-                    g[h] = valid ? (d0 * av[h] + d1 * cv[h]) * dgelu_s(z) : 0.f;
+                mma_commit(bar(RB_FZ));
+                if (i > 0) {
+                    if (!dw1(i - 1)) break;
+                    // x(i) once dW1(i - 1) has read x(i - 1)
+                    if (!gwait(bar(RB_EX), (i - 1) & 1, abort)) break;
+                    load_x(i);
+                    ++nx;
                 }
-                w[2 * e4] = pack2(g[0], g[1]);
-                w[2 * e4 + 1] = pack2(g[2], g[3]);
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int col = cb + 16 * c + 8 * k;
-                *reinterpret_cast<uint4 *>(sm + (R_AA1 + (col >> 6)) * ATOM +
-                                           sw128_off(row, (col & 63) >> 3)) =
-                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-            }
-        }
-        // this row's z1 columns cb .. cb + 31: atom cb / 32 of the z1 tile
-        if (t == 0) z_done = i + 1;
-        ok = gwait(bar(RB_Z), i & 1, abort);
-        float z1r[R_COLS];
-#pragma unroll
-        for (int k = 0; k < R_COLS / 4; ++k) {
-            const float4 a = *reinterpret_cast<const float4 *>(sm + (R_AZ1 + cp) * ATOM + sw128_off(row, k));
-            z1r[4 * k] = a.x; z1r[4 * k + 1] = a.y; z1r[4 * k + 2] = a.z; z1r[4 * k + 3] = a.w;
-        }
-        fence_async_smem();
-        tc_fence_before();
-        if (!__syncthreads_and(ok)) break;
-        if (t == 0) {
-            tc_fence_after();
-            // dh1 [b][i] = dz2 [b][j] W2 [j][i]   (B: W2^T rows i, K = j)
-#pragma unroll
-            for (int s = 0; s < NH / 16; ++s)
-                mma_bf16(tbase + R_TZ, sdesc_sw128(kstep(R_AA1, R_AA1 + 1, s)),
-                         sdesc_sw128(kstep(R_AW2T, R_AW2T + 6, s)), ID_DH, s > 0);
-            // dW2 [j][i] (+ db2 at column 128) += dz2^T [j][b] h1 [b][i]
-#pragma unroll
-            for (int s = 0; s < TILE / 16; ++s)
-                mma_bf16(tbase + R_TW2, sdesc_sw128_mn(atom(R_AA1) + 2048u * s, ATOM),
-                         sdesc_sw128_mn(atom(R_AH1) + 2048u * s, 4 * ATOM), ID_W2,
-                         (s > 0 || i > 0) ? 1u : 0u);
-            mma_commit(bar(RB_M));
-        }
-        ok = gwait(bar(RB_M), pm, abort);
-        pm ^= 1;
-        if (!__syncthreads_and(ok)) break;
-        tc_fence_after();
-        // h1 has been read: the next tile's comes in
-        if (t == 0 && i + 1 < mine) {
-            load_h1(i + 1);
-            h_issued = i + 2;
-        }
-        // dz1 = dh1 * gelu'(z1) -> A2 row `row` (over the z1 tile, read above)
-#pragma unroll
-        for (int c = 0; c < R_COLS / 16; ++c) {
-            float v[16];
-            tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
-            uint32_t w[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const float g0 = valid ? v[2 * e] * dgelu_s(z1r[16 * c + 2 * e]) : 0.f;
-                const float g1 = valid ? v[2 * e + 1] * dgelu_s(z1r[16 * c + 2 * e + 1]) : 0.f;
-                w[e] = pack2(g0, g1);
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int col = cb + 16 * c + 8 * k;
-                *reinterpret_cast<uint4 *>(sm + (R_AA2 + (col >> 6)) * ATOM +
-                                           sw128_off(row, (col & 63) >> 3)) =
-                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-            }
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        if (t == 0) {
-            ok = gwait(bar(RB_X), i & 1, abort);
-            x_done = i + 1;
-            if (ok) {
+                // A1(i) written and z1(i) read: the next z1, then dh1 and dW2
+                if (!gwait(bar(RB_A1), i & 1, abort)) break;
+                if (i + 1 < mine) {
+                    load_z1(i + 1);
+                    ++nz;
+                }
                 tc_fence_after();
-                // dW1 [j][m] (+ db1 at column 192) += dz1^T [j][b] x [b][m]
+                // dh1 [b][i] = dz2 [b][j] W2 [j][i]   (B: W2^T rows i, K = j)
+#pragma unroll
+                for (int s = 0; s < NH / 16; ++s)
+                    mma_bf16(tbase + R_TZ, sdesc_sw128(kstep(R_AA, R_AA + 1, s)),
+                             sdesc_sw128(kstep(R_AW2T, R_AW2T + 6, s)), ID_DH, s > 0);
+                mma_commit(bar(RB_FDH));
+                // dW2 [j][i] (+ db2 at column 128) += dz2^T [j][b] h1 [b][i]
 #pragma unroll
                 for (int s = 0; s < TILE / 16; ++s)
-                    mma_bf16(tbase + R_TW1, sdesc_sw128_mn(atom(R_AA2) + 2048u * s, ATOM),
-                             sdesc_sw128_mn(atom(R_AX) + 2048u * s, ATOM), ID_W1,
+                    mma_bf16(tbase + R_TW2, sdesc_sw128_mn(atom(R_AA) + 2048u * s, ATOM),
+                             sdesc_sw128_mn(atom(R_AH1) + 2048u * s, 4 * ATOM), ID_W2,
                              (s > 0 || i > 0) ? 1u : 0u);
-                mma_commit(bar(RB_M));
+                mma_commit(bar(RB_EH));
+                // h1(i + 1) once dW2(i) has read h1(i)
+                if (i + 1 < mine) {
+                    if (!gwait(bar(RB_EH), i & 1, abort)) break;
+                    load_h1(i + 1);
+                    ++nh;
+                }
             }
+            if (!*abort && mine > 0 && dw1(mine - 1)) gwait(bar(RB_EX), (mine - 1) & 1, abort);
+            // every load issued has landed before the CTA may exit (each
+            // barrier has at most its last phase outstanding; a bounded wait
+            // that does not give up on the abort word)
+            if (nh > 0) mbar_wait(bar(RB_H), (nh - 1) & 1);
+            if (nx > 0) mbar_wait(bar(RB_X), (nx - 1) & 1);
+            if (nz > 0) mbar_wait(bar(RB_Z), (nz - 1) & 1);
         }
-        if (!__syncthreads_and(ok)) break;
-        ok = gwait(bar(RB_M), pm, abort);
-        pm ^= 1;
-        if (!__syncthreads_and(ok)) break;
+        __syncwarp();
+    } else {
+        // ---- epilogues: row = sample (tensor-memory lane), 32 columns ----
+        const int q = warp & 3, cp = warp >> 2;
+        const int row = q * 32 + lane;
+        const int cb = cp * R_COLS;
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+        float loss = 0.f;
+        float4 yt = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto load_yt = [&](int i) {
+            const int64_t b = (int64_t)tile_row0(i) + row;
+            if (b < n) {
+                const float2 a = *reinterpret_cast<const float2 *>(y + b * 2);
+                const float2 c = *reinterpret_cast<const float2 *>(target + b * 2);
+                yt = make_float4(a.x, a.y, c.x, c.y);
+            }
+        };
+        auto store_rows = [&](uint32_t base_atom, int c, const uint32_t (&w)[8]) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int col = cb + 16 * c + 8 * k;
+                *reinterpret_cast<uint4 *>(sm + (base_atom + (col >> 6)) * ATOM +
+                                           sw128_off(row, (col & 63) >> 3)) =
+                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+            }
+        };
+        // a wait every lane of the warp agrees on (the tensor-memory loads
+        // after it are warp-wide)
+        auto wwait = [&](int k, int parity) {
+            return __all_sync(0xffffffffu, gwait(bar(k), (uint32_t)parity & 1u, abort)) != 0;
+        };
+        if (mine > 0) load_yt(0);
+        for (int i = 0; i < mine; ++i) {
+            const int64_t b = (int64_t)tile_row0(i) + row;
+            const bool valid = b < n;
+            float d0 = 0.f, d1 = 0.f;
+            if (valid) {
+                const float e0 = yt.x - yt.z, e1 = yt.y - yt.w;
+                d0 = e0 * inv_count;
+                d1 = e1 * inv_count;
+                if (cp == 0) {
+                    loss += e0 * e0 + e1 * e1;
+                    *reinterpret_cast<float2 *>(dy_out + b * 2) = make_float2(d0, d1);
+                }
+            }
+            if (i + 1 < mine) load_yt(i + 1);
+            // dz2 = (dy W3) * gelu'(z2 + b2), written once dW1(i - 1) has
+            // read A2(i - 1) (the same atoms)
+            if (!wwait(RB_FZ, i)) { ok = false; break; }
+            tc_fence_after();
+            uint32_t w2[2][8];
+#pragma unroll
+            for (int c = 0; c < R_COLS / 16; ++c) {
+                float v[16];
+                tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
+#pragma unroll
+                for (int e4 = 0; e4 < 4; ++e4) {
+                    const int j = cb + 16 * c + 4 * e4;
+                    const float4 bb = *reinterpret_cast<const float4 *>(b2f + j);
+                    const float4 wa = *reinterpret_cast<const float4 *>(w3f + j);
+                    const float4 wb = *reinterpret_cast<const float4 *>(w3f + NH + j);
+                    const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
+                    const float av[4] = {wa.x, wa.y, wa.z, wa.w};
+                    const float cv[4] = {wb.x, wb.y, wb.z, wb.w};
+                    float g[4];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        const float z = v[4 * e4 + h] + bv[h];
+                        g[h] = valid ? (d0 * av[h] + d1 * cv[h]) * dgelu_s(z) : 0.f;
+                    }
+                    w2[c][2 * e4] = pack2(g[0], g[1]);
+                    w2[c][2 * e4 + 1] = pack2(g[2], g[3]);
+                }
+            }
+            if (i > 0 && !wwait(RB_EX, i - 1)) { ok = false; break; }
+#pragma unroll
+            for (int c = 0; c < R_COLS / 16; ++c) store_rows(R_AA, c, w2[c]);
+            // this row's z1 columns cb .. cb + 31: atom cb / 32 of the z1 tile
+            if (!wwait(RB_Z, i)) { ok = false; break; }
+            float z1r[R_COLS];
+#pragma unroll
+            for (int k = 0; k < R_COLS / 4; ++k) {
+                const float4 a = *reinterpret_cast<const float4 *>(sm + (R_AZ1 + cp) * ATOM + sw128_off(row, k));
+                z1r[4 * k] = a.x; z1r[4 * k + 1] = a.y; z1r[4 * k + 2] = a.z; z1r[4 * k + 3] = a.w;
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(RB_A1));
+            // dz1 = dh1 * gelu'(z1) -> A2, once dW2(i) has read A1(i)
+            if (!wwait(RB_FDH, i)) { ok = false; break; }
+            tc_fence_after();
+            float v[R_COLS];
+#pragma unroll
+            for (int c = 0; c < R_COLS / 16; ++c) {
+                float u[16];
+                tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, u);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) v[16 * c + e] = u[e];
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(RB_ZC));
+            uint32_t w1[2][8];
+#pragma unroll
+            for (int c = 0; c < R_COLS / 16; ++c) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const float g0 = valid ? v[16 * c + 2 * e] * dgelu_s(z1r[16 * c + 2 * e]) : 0.f;
+                    const float g1 = valid ? v[16 * c + 2 * e + 1] * dgelu_s(z1r[16 * c + 2 * e + 1]) : 0.f;
+                    w1[c][e] = pack2(g0, g1);
+                }
+            }
+            if (!wwait(RB_EH, i)) { ok = false; break; }
+#pragma unroll
+            for (int c = 0; c < R_COLS / 16; ++c) store_rows(R_AA, c, w1[c]);
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(RB_A2));
+        }
+        // every product has finished before the gradients are read
+        if (ok && mine > 0 && !wwait(RB_EX, mine - 1)) ok = false;
+        for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+        if (lane == 0) red[warp] = loss;
         tc_fence_after();
-        // x and A2 (over the z1 tile) have been read: the next tile's x and z1
-        if (t == 0 && i + 1 < mine) {
-            load_x(i + 1);
-            load_z1(i + 1);
-            x_issued = z_issued = i + 2;
-        }
-    }
-    // every load issued has landed before the CTA may exit
-    if (t == 0) {
-        for (int k = h_done; k < h_issued; ++k) gwait(bar(RB_H), k & 1, abort);
-        for (int k = x_done; k < x_issued; ++k) gwait(bar(RB_X), k & 1, abort);
-        for (int k = z_done; k < z_issued; ++k) gwait(bar(RB_Z), k & 1, abort);
-    }
-
-    float *P = part + (int64_t)blockIdx.x * NPARAM;
-    if (ok && mine > 0) {
-        // row j = `row` of the accumulated weight (and bias) gradients; the
-        // four warps of a lane quarter take every fourth 16-column chunk
+        float *P = part + (int64_t)blockIdx.x * PART_STRIDE;
+        if (ok && !*abort && mine > 0) {
+            // row j = `row` of the accumulated weight (and bias) gradients; the
+            // four warps of a lane quarter take every fourth 16-column chunk
 #pragma unroll 1
-        for (int k = cp; k < R_N2 / 16; k += 4) {
-            const int c0 = 16 * k;
-            float v[16];
-            tmem_ld16(tbase + R_TW2 + lane_base + c0, v);
+            for (int k = cp; k < R_N2 / 16; k += 4) {
+                const int c0 = 16 * k;
+                float u[16];
+                tmem_ld16(tbase + R_TW2 + lane_base + c0, u);
+                if (c0 < NH) {
+                    float4 *dst = reinterpret_cast<float4 *>(P + OFF_W2 + row * NH + c0);
 #pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const int c = c0 + e;
-                if (c < NH) P[OFF_W2 + row * NH + c] = v[e];
-                else if (c == NH) P[OFF_B2 + row] = v[e];
+                    for (int e = 0; e < 4; ++e)
+                        dst[e] = make_float4(u[4 * e], u[4 * e + 1], u[4 * e + 2], u[4 * e + 3]);
+                } else {
+                    P[OFF_B2 + row] = u[0];
+                }
             }
-        }
 #pragma unroll 1
-        for (int k = cp; k < R_N1 / 16; k += 4) {
-            const int c0 = 16 * k;
-            float v[16];
-            tmem_ld16(tbase + R_TW1 + lane_base + c0, v);
+            for (int k = cp; k < R_N1 / 16; k += 4) {
+                const int c0 = 16 * k;
+                float u[16];
+                tmem_ld16(tbase + R_TW1 + lane_base + c0, u);
+                if (c0 < NIN) {
+                    float4 *dst = reinterpret_cast<float4 *>(P + OFF_W1 + row * NIN + c0);
 #pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const int c = c0 + e;
-                if (c < NIN) P[OFF_W1 + row * NIN + c] = v[e];
-                else if (c == NIN) P[OFF_B1 + row] = v[e];
+                    for (int e = 0; e < 4; ++e)
+                        dst[e] = make_float4(u[4 * e], u[4 * e + 1], u[4 * e + 2], u[4 * e + 3]);
+                } else {
+                    P[OFF_B1 + row] = u[0];
+                }
             }
+        } else if (mine == 0) {
+            for (int k = t; k < OFF_W3; k += 32 * R_EPI) P[k] = 0.f;
         }
-    } else if (mine == 0) {
-        for (int k = t; k < OFF_W3; k += R_THREADS) P[k] = 0.f;
     }
-    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
-    if (lane == 0) red[warp] = loss;
-    if (!ok && t == 0) atomicOr(err, SPH_EFLAG_TIMEOUT);
     tc_fence_before();
     __syncthreads();
     if (t == 0) {
+        if (*abort || !ok) atomicOr(err, SPH_EFLAG_TIMEOUT);
         float sum = 0.f;
-        for (int w = 0; w < R_WARPS; ++w) sum += red[w];
+        for (int w = 0; w < R_EPI; ++w) sum += red[w];
         part_loss[blockIdx.x] = 0.5f * inv_count * sum;
     }
     if (warp == 0) {
@@ -1388,7 +1421,7 @@ __global__ void k_mlp_reduce(const float *__restrict__ part, int nparts,
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < OFF_W3) {
         float s = 0.f;
-        for (int c = 0; c < nparts; ++c) s += part[(int64_t)c * NPARAM + p];
+        for (int c = 0; c < nparts; ++c) s += part[(int64_t)c * PART_STRIDE + p];
         grad[p] = s;
     } else if (p < NPARAM) {
         float s = 0.f;
@@ -1576,7 +1609,7 @@ int mlp_grid(int64_t n) {
 int64_t mlp_backward_scratch(int64_t n) {
     const int grid = mlp_grid(n);
     const int64_t nl3 = (n + L3_ROWS - 1) / L3_ROWS;
-    return (int64_t)grid * NPARAM + std::max<int64_t>(nl3, 1) * L3_PART + grid + 2 * n + 4;
+    return (int64_t)grid * PART_STRIDE + std::max<int64_t>(nl3, 1) * L3_PART + grid + 2 * n + 4;
 }
 
 int mlp_sync(const sph_mlp_model *M, cudaStream_t st) {
@@ -1623,7 +1656,7 @@ int mlp_backward(const sph_mlp_model *M, const uint16_t *x, const uint16_t *h1, 
     const int grid = mlp_grid(n);
     const int nl3 = (int)std::max<int64_t>(1, (n + L3_ROWS - 1) / L3_ROWS);
     float *part = scratch;
-    float *l3 = part + (int64_t)grid * NPARAM;
+    float *l3 = part + (int64_t)grid * PART_STRIDE;
     float *part_loss = l3 + (int64_t)nl3 * L3_PART;
     float *dy = part_loss + grid;
     dy = reinterpret_cast<float *>(((uintptr_t)dy + 15) & ~(uintptr_t)15);
