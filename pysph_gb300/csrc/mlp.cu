@@ -153,6 +153,27 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// The same load without its wait: tmem_wait16 on the same registers before
+// they are read (the registers are in-out operands of the wait, so nothing
+// that reads them can be placed before it).
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+}
+
 // byte offset of element (r, k) of a K-major operand with kc = K/8 chunks per row
 __device__ __forceinline__ uint32_t core_off(int r, int k, int kc) {
     return (uint32_t)(((((r >> 3) * kc) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
@@ -202,6 +223,67 @@ __device__ __forceinline__ float dgelu_s(float z) {
     const float e = ex2_approx(z * fmaf(kGeluE1, z2, kGeluE0));
     const float sg = rcp_approx(1.f + e);
     return (1.f - sg) * fmaf(z * fmaf(kGeluD1, z2, kGeluD0), sg, 1.f);
+}
+
+// Pairs of FP32 values in one 64-bit register pair, for the packed FP32
+// arithmetic of sm_100+ (add / sub / mul / fma .rn.f32x2: two lanes per
+// instruction, each rounded like its scalar form).
+__device__ __forceinline__ uint64_t f2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_split(uint64_t r, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// GELU of a pair: z (1 - s), s = 1 / (1 + e^(2u)) (1 + tanh(u) = 2 (1 - s));
+// e^(2u) = 2^(z (E0 + E1 z^2)).  For z -> -inf, e -> 0 and s -> 1; for
+// z -> +inf, e -> inf and s -> 0.
+__device__ __forceinline__ uint64_t gelu2(uint64_t z) {
+    const uint64_t one = f2(1.f, 1.f);
+    const uint64_t ku = mul2(z, fma2(mul2(z, z), f2(kGeluE1, kGeluE1), f2(kGeluE0, kGeluE0)));
+    float k0, k1;
+    f2_split(ku, k0, k1);
+    const uint64_t d = add2(f2(ex2_approx(k0), ex2_approx(k1)), one);
+    float d0, d1;
+    f2_split(d, d0, d1);
+    return mul2(z, sub2(one, f2(rcp_approx(d0), rcp_approx(d1))));
+}
+
+// d gelu / dz of a pair, as dgelu_s: (1 - s) (1 + z (D0 + D1 z^2) s)
+__device__ __forceinline__ uint64_t dgelu2(uint64_t z) {
+    const uint64_t one = f2(1.f, 1.f);
+    const uint64_t zz = mul2(z, z);
+    const uint64_t ku = mul2(z, fma2(zz, f2(kGeluE1, kGeluE1), f2(kGeluE0, kGeluE0)));
+    float k0, k1;
+    f2_split(ku, k0, k1);
+    const uint64_t d = add2(f2(ex2_approx(k0), ex2_approx(k1)), one);
+    float d0, d1;
+    f2_split(d, d0, d1);
+    const uint64_t sg = f2(rcp_approx(d0), rcp_approx(d1));
+    const uint64_t zq = mul2(z, fma2(zz, f2(kGeluD1, kGeluD1), f2(kGeluD0, kGeluD0)));
+    return mul2(sub2(one, sg), fma2(zq, sg, one));
 }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
@@ -436,16 +518,16 @@ constexpr int G_COLS = NH / (G_EPI / 4);            // 32 columns per epilogue w
 constexpr uint32_t G_YP = G_B3 + 16;                // float2 [2 tile parities][4 parts][128]
 constexpr uint32_t G_BAR = G_YP + 2 * (G_EPI / 4) * TILE * 8;
 // mbarriers: weights; X stage full / empty; first accumulator full / empty
-// (two each); H1 full / empty; second accumulator full / empty; output
-// partials of both column halves written (two, by tile parity)
+// (two each); H1 full / empty; second accumulator full / empty (two each);
+// output partials of the column parts written (two, by tile parity)
 enum GBar { GB_W = 0, GB_XF0, GB_XF1, GB_XE0, GB_XE1, GB_A1F0, GB_A1F1, GB_A1E0, GB_A1E1,
-            GB_HF, GB_HE, GB_A2F, GB_A2E, GB_Y0, GB_Y1, GB_N };
+            GB_HF, GB_HE, GB_A2F0, GB_A2F1, GB_A2E0, GB_A2E1, GB_Y0, GB_Y1, GB_N };
 constexpr uint32_t G_SLOT = G_BAR + GB_N * 8;        // tensor-memory address
 constexpr uint32_t G_ABORT = G_SLOT + 4;            // a bounded wait gave up
 constexpr uint32_t G_END = G_ABORT + 4;
 constexpr uint32_t G_BYTES = G_END + 1024;          // + alignment of the base
 constexpr int G_THREADS = 32 * (2 + G_EPI);        // producer, MMA, 16 epilogue warps
-constexpr uint32_t G_TMEM_COLS = 512;               // acc1 at 0 and 128, acc2 at 256
+constexpr uint32_t G_TMEM_COLS = 512;               // acc1 at 0 and 128, acc2 at 256 and 384
 constexpr uint32_t G_XBYTES = 3 * ATOM;
 
 // Shared-memory matrix descriptor, K-major with 128-byte swizzling: start
@@ -544,8 +626,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         mbar_init(bar(GB_A1E1), G_EPI);
         mbar_init(bar(GB_HF), G_EPI);
         mbar_init(bar(GB_HE), 1);
-        mbar_init(bar(GB_A2F), 1);
-        mbar_init(bar(GB_A2E), G_EPI);
+        mbar_init(bar(GB_A2F0), 1);
+        mbar_init(bar(GB_A2F1), 1);
+        mbar_init(bar(GB_A2E0), G_EPI);
+        mbar_init(bar(GB_A2E1), G_EPI);
         mbar_init(bar(GB_Y0), G_EPI);
         mbar_init(bar(GB_Y1), G_EPI);
     }
@@ -600,17 +684,18 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             if (ok && mine > 0) ok = first_layer(0);
             for (int i = 0; ok && i < mine; ++i) {
                 if (i + 1 < mine && !first_layer(i + 1)) break;
+                const int s2 = i & 1;
                 if (!gwait(bar(GB_HF), i & 1, abort)) break;
-                if (!gwait(bar(GB_A2E), (i + 1) & 1, abort)) break;
+                if (!gwait(bar(GB_A2E0 + s2), ((i >> 1) + 1) & 1, abort)) break;
                 tc_fence_after();
 #pragma unroll
                 for (int k = 0; k < NH / 16; ++k) {
                     const uint32_t a = sbase + G_H1 + (k >> 2) * ATOM + (k & 3) * 32;
                     const uint32_t b = sbase + G_W2 + (k >> 2) * ATOM + (k & 3) * 32;
-                    mma_bf16(tbase + 256, sdesc_sw128(a), sdesc_sw128(b), ID, k > 0);
+                    mma_bf16(tbase + 256 + 128 * s2, sdesc_sw128(a), sdesc_sw128(b), ID, k > 0);
                 }
                 mma_commit(bar(GB_HE));
-                mma_commit(bar(GB_A2F));
+                mma_commit(bar(GB_A2F0 + s2));
             }
         }
     } else {
@@ -619,34 +704,61 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         const int row = q * 32 + lane;
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
         const int cb = hf * G_COLS;
-        for (int i = 0; i < mine; ++i) {
+        // a wait every lane of the warp agrees on (the tensor-memory loads
+        // after it are warp-wide)
+        auto wwait = [&](int k, int parity) {
+            return __all_sync(0xffffffffu, gwait(bar(k), (uint32_t)parity & 1u, abort)) != 0;
+        };
+        // layer 1 of tile i: acc1[i % 2] + b1, GELU -> H1 (and the saved values)
+        auto layer1 = [&](int i) -> bool {
             const int s = i & 1;
             const int64_t grow = (blockIdx.x + (int64_t)i * gridDim.x) * TILE + row;
             const bool valid = grow < n;
             // layer 1: acc1[s] + b1, GELU -> H1 (and the saved values)
-            if (!gwait(bar(GB_A1F0 + s), (i >> 1) & 1, abort)) break;
+            if (!wwait(GB_A1F0 + s, (i >> 1) & 1)) return false;
             tc_fence_after();
             uint32_t hw[G_COLS / 2];
+            // the second chunk's load in flight while the first is computed
+            uint32_t rr[2][16];
+            tmem_ld16_async(tbase + s * 128 + lane_base + cb, rr[0]);
+            tmem_wait16(rr[0]);
+            tmem_ld16_async(tbase + s * 128 + lane_base + cb + 16, rr[1]);
 #pragma unroll
             for (int c = 0; c < G_COLS / 16; ++c) {
+                if (c == 1) tmem_wait16(rr[1]);
                 float v[16];
-                tmem_ld16(tbase + s * 128 + lane_base + cb + 16 * c, v);
 #pragma unroll
-                for (int e = 0; e < 16; ++e) v[e] += b1f[cb + 16 * c + e];
+                for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(rr[c][e]);
+                // + b1 and GELU, two columns per packed instruction
+                uint64_t z[8];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float4 bb = *reinterpret_cast<const float4 *>(b1f + cb + 16 * c + 4 * e);
+                    z[2 * e] = add2(f2(v[4 * e], v[4 * e + 1]), f2(bb.x, bb.y));
+                    z[2 * e + 1] = add2(f2(v[4 * e + 2], v[4 * e + 3]), f2(bb.z, bb.w));
+                }
                 if (valid && z1s) {
                     float4 *zp = reinterpret_cast<float4 *>(z1s + grow * NH + cb + 16 * c);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        zp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                    for (int e = 0; e < 4; ++e) {
+                        float a0, a1, a2, a3;
+                        f2_split(z[2 * e], a0, a1);
+                        f2_split(z[2 * e + 1], a2, a3);
+                        zp[e] = make_float4(a0, a1, a2, a3);
+                    }
                 }
 #pragma unroll
-                for (int e = 0; e < 8; ++e) hw[8 * c + e] = pack2(gelu(v[2 * e]), gelu(v[2 * e + 1]));
+                for (int e = 0; e < 8; ++e) {
+                    float g0, g1;
+                    f2_split(gelu2(z[e]), g0, g1);
+                    hw[8 * c + e] = pack2(g0, g1);
+                }
             }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(bar(GB_A1E0 + s));
             // H1 is free once the second layer of the previous tile has read it
-            if (!gwait(bar(GB_HE), (i + 1) & 1, abort)) break;
+            if (!wwait(GB_HE, (i + 1) & 1)) return false;
             // columns cb .. cb + 31: atom cb / 64, chunks (cb % 64) / 8 + c
 #pragma unroll
             for (int c = 0; c < G_COLS / 8; ++c)
@@ -662,32 +774,56 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(bar(GB_HF));
+            return true;
+        };
+        // layer 2 of tile i: acc2[i % 2] + b2, GELU, the output layer
+        auto layer2 = [&](int i) -> bool {
+            const int s = i & 1;
+            const int64_t grow = (blockIdx.x + (int64_t)i * gridDim.x) * TILE + row;
+            const bool valid = grow < n;
             // layer 2: acc2 + b2, GELU, then the output layer on the CUDA cores
-            if (!gwait(bar(GB_A2F), i & 1, abort)) break;
+            const int s2 = i & 1;
+            if (!wwait(GB_A2F0 + s2, (i >> 1) & 1)) return false;
             tc_fence_after();
-            float y0 = 0.f, y1 = 0.f;
+            // the output layer in packed pairs: (y0 over even, odd columns), (y1 ...)
+            uint64_t ya = f2(0.f, 0.f), yb = f2(0.f, 0.f);
+            uint32_t rr2[2][16];
+            tmem_ld16_async(tbase + 256 + 128 * s2 + lane_base + cb, rr2[0]);
+            tmem_wait16(rr2[0]);
+            tmem_ld16_async(tbase + 256 + 128 * s2 + lane_base + cb + 16, rr2[1]);
 #pragma unroll
             for (int c = 0; c < G_COLS / 16; ++c) {
+                if (c == 1) tmem_wait16(rr2[1]);
                 float v[16];
-                tmem_ld16(tbase + 256 + lane_base + cb + 16 * c, v);
-                uint32_t w2w[8];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) v[e] += b2f[cb + 16 * c + e];
+                for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(rr2[c][e]);
+                uint32_t w2w[8];
+                uint64_t z[8];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float4 bb = *reinterpret_cast<const float4 *>(b2f + cb + 16 * c + 4 * e);
+                    z[2 * e] = add2(f2(v[4 * e], v[4 * e + 1]), f2(bb.x, bb.y));
+                    z[2 * e + 1] = add2(f2(v[4 * e + 2], v[4 * e + 3]), f2(bb.z, bb.w));
+                }
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    w2w[e] = pack2(gelu(v[2 * e]), gelu(v[2 * e + 1]));
-                    const float ha = bf_lo(w2w[e]), hb = bf_hi(w2w[e]);
+                    float g0, g1;
+                    f2_split(gelu2(z[e]), g0, g1);
+                    w2w[e] = pack2(g0, g1);
                     const int j = cb + 16 * c + 2 * e;
-                    y0 = fmaf(ha, w3f[j], y0);
-                    y0 = fmaf(hb, w3f[j + 1], y0);
-                    y1 = fmaf(ha, w3f[NH + j], y1);
-                    y1 = fmaf(hb, w3f[NH + j + 1], y1);
+                    const uint64_t h = f2(bf_lo(w2w[e]), bf_hi(w2w[e]));
+                    ya = fma2(h, *reinterpret_cast<const uint64_t *>(w3f + j), ya);
+                    yb = fma2(h, *reinterpret_cast<const uint64_t *>(w3f + NH + j), yb);
                 }
                 if (valid && z2s) {
                     float4 *zp = reinterpret_cast<float4 *>(z2s + grow * NH + cb + 16 * c);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        zp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                    for (int e = 0; e < 4; ++e) {
+                        float a0, a1, a2, a3;
+                        f2_split(z[2 * e], a0, a1);
+                        f2_split(z[2 * e + 1], a2, a3);
+                        zp[e] = make_float4(a0, a1, a2, a3);
+                    }
                 }
                 if (valid && h2s) {
                     uint4 *hp = reinterpret_cast<uint4 *>(h2s + grow * NH + cb + 16 * c);
@@ -695,9 +831,17 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                     hp[1] = make_uint4(w2w[4], w2w[5], w2w[6], w2w[7]);
                 }
             }
+            float y0, y1;
+            {
+                float a0, a1, b0, b1;
+                f2_split(ya, a0, a1);
+                f2_split(yb, b0, b1);
+                y0 = a0 + a1;
+                y1 = b0 + b1;
+            }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(bar(GB_A2E));
+            if (lane == 0) mbar_arrive(bar(GB_A2E0 + s2));
             // the column parts of a row meet: all write their partial, the
             // first part adds them in a fixed order (the partials alternate
             // by tile parity; a tile's H1 barrier orders the reuse)
@@ -706,7 +850,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(bar(GB_Y0 + s));
             if (hf == 0) {
-                if (!gwait(bar(GB_Y0 + s), (i >> 1) & 1, abort)) break;
+                if (!wwait(GB_Y0 + s, (i >> 1) & 1)) return false;
                 if (valid) {
 #pragma unroll
                     for (int pp = 1; pp < NP; ++pp) {
@@ -717,6 +861,15 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                     y[grow * 2] = b3f[0] + y0;
                     y[grow * 2 + 1] = b3f[1] + y1;
                 }
+            }
+            return true;
+        };
+        // the first layer of tile i + 1 before the second of tile i: its math
+        // runs while the tensor cores compute the second product of tile i
+        if (mine > 0 && layer1(0)) {
+            for (int i = 0; i < mine; ++i) {
+                if (i + 1 < mine && !layer1(i + 1)) break;
+                if (!layer2(i)) break;
             }
         }
     }
@@ -1265,27 +1418,29 @@ __global__ void __launch_bounds__(R_THREADS, 1)
             if (!wwait(RB_FZ, i)) { ok = false; break; }
             tc_fence_after();
             uint32_t w2[2][8];
+            const uint64_t dd0 = valid ? f2(d0, d0) : f2(0.f, 0.f);
+            const uint64_t dd1 = valid ? f2(d1, d1) : f2(0.f, 0.f);
+            uint32_t rz[2][16];
+            tmem_ld16_async(tbase + R_TZ + lane_base + cb, rz[0]);
+            tmem_wait16(rz[0]);
+            tmem_ld16_async(tbase + R_TZ + lane_base + cb + 16, rz[1]);
 #pragma unroll
             for (int c = 0; c < R_COLS / 16; ++c) {
+                if (c == 1) tmem_wait16(rz[1]);
                 float v[16];
-                tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, v);
 #pragma unroll
-                for (int e4 = 0; e4 < 4; ++e4) {
-                    const int j = cb + 16 * c + 4 * e4;
-                    const float4 bb = *reinterpret_cast<const float4 *>(b2f + j);
-                    const float4 wa = *reinterpret_cast<const float4 *>(w3f + j);
-                    const float4 wb = *reinterpret_cast<const float4 *>(w3f + NH + j);
-                    const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
-                    const float av[4] = {wa.x, wa.y, wa.z, wa.w};
-                    const float cv[4] = {wb.x, wb.y, wb.z, wb.w};
-                    float g[4];
+                for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(rz[c][e]);
 #pragma unroll
-                    for (int h = 0; h < 4; ++h) {
-                        const float z = v[4 * e4 + h] + bv[h];
-                        g[h] = valid ? (d0 * av[h] + d1 * cv[h]) * dgelu_s(z) : 0.f;
-                    }
-                    w2[c][2 * e4] = pack2(g[0], g[1]);
-                    w2[c][2 * e4 + 1] = pack2(g[2], g[3]);
+                for (int e = 0; e < 8; ++e) {
+                    // columns j, j + 1, two per packed instruction
+                    const int j = cb + 16 * c + 2 * e;
+                    const uint64_t z = add2(f2(v[2 * e], v[2 * e + 1]),
+                                            *reinterpret_cast<const uint64_t *>(b2f + j));
+                    const uint64_t g = fma2(dd1, *reinterpret_cast<const uint64_t *>(w3f + NH + j),
+                                            mul2(dd0, *reinterpret_cast<const uint64_t *>(w3f + j)));
+                    float g0, g1;
+                    f2_split(mul2(g, dgelu2(z)), g0, g1);
+                    w2[c][e] = pack2(g0, g1);
                 }
             }
             if (i > 0 && !wwait(RB_EX, i - 1)) { ok = false; break; }
@@ -1307,12 +1462,16 @@ __global__ void __launch_bounds__(R_THREADS, 1)
             if (!wwait(RB_FDH, i)) { ok = false; break; }
             tc_fence_after();
             float v[R_COLS];
+            {
+                uint32_t rh[2][16];
+                tmem_ld16_async(tbase + R_TZ + lane_base + cb, rh[0]);
+                tmem_ld16_async(tbase + R_TZ + lane_base + cb + 16, rh[1]);
+                tmem_wait16(rh[0]);
+                tmem_wait16(rh[1]);
 #pragma unroll
-            for (int c = 0; c < R_COLS / 16; ++c) {
-                float u[16];
-                tmem_ld16(tbase + R_TZ + lane_base + cb + 16 * c, u);
+                for (int c = 0; c < 2; ++c)
 #pragma unroll
-                for (int e = 0; e < 16; ++e) v[16 * c + e] = u[e];
+                    for (int e = 0; e < 16; ++e) v[16 * c + e] = __uint_as_float(rh[c][e]);
             }
             tc_fence_before();
             __syncwarp();
@@ -1322,9 +1481,10 @@ __global__ void __launch_bounds__(R_THREADS, 1)
             for (int c = 0; c < R_COLS / 16; ++c) {
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const float g0 = valid ? v[16 * c + 2 * e] * dgelu_s(z1r[16 * c + 2 * e]) : 0.f;
-                    const float g1 = valid ? v[16 * c + 2 * e + 1] * dgelu_s(z1r[16 * c + 2 * e + 1]) : 0.f;
-                    w1[c][e] = pack2(g0, g1);
+                    const int k = 16 * c + 2 * e;
+                    float g0, g1;
+                    f2_split(mul2(f2(v[k], v[k + 1]), dgelu2(f2(z1r[k], z1r[k + 1]))), g0, g1);
+                    w1[c][e] = valid ? pack2(g0, g1) : 0u;
                 }
             }
             if (!wwait(RB_EH, i)) { ok = false; break; }
