@@ -1010,10 +1010,82 @@ def run_gpu_closure(args):
                     "max_relative_at_checkpoints": [f[1] for f in floor]},
                 "closure": res}
 
+    def term_timings(dx, dt, column, reps=50):
+        """CUDA-event times of what one rates evaluation of the closure
+        runs against the pair loop it replaces (the fluid-on-itself PGrad +
+        AV pass), at the state after three plain steps."""
+        import ctypes
+
+        from pysph_gb300.sph import gpu
+        fluid, wall = W.dam_break(dx=dx, column=column)
+        s, particles = W.setup_dam_break(api, fluid, wall, dx, c0)
+        for _ in range(3):
+            s.integrator.integrate(dt)
+        fl = particles.arrays[0]
+        cm = particles.cell_manager
+        term = dict(L._self_term(L._fluid_stage(s.integrator, fl)))
+        term["kinds"] = set(L.SELF_KINDS)
+        n = fl.get_number_of_particles()
+        dev = fl.get_device("x").device
+        acc = tuple(torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(3))
+        st = torch.cuda.current_stream()
+
+        def timed(fn):
+            """(device ms, wall ms) per call: the device time with the
+            calls queued behind a spin kernel (so the host has enqueued them
+            all before the first runs), the wall time of calls made one
+            after another from Python."""
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            torch.cuda.synchronize()
+            wall = (time.perf_counter() - t1) * 1e3 / reps
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda._sleep(int(4e7))
+            a.record(st)
+            for _ in range(reps):
+                fn()
+            b.record(st)
+            b.synchronize()
+            return a.elapsed_time(b) / reps, wall
+
+        out = {"fluid_particles": n, "what": "per call: [device ms, wall ms of calls from Python]"}
+        out["pair_loop_ms"] = timed(lambda: gpu.rates(cm, fl, [term], 2, acc=acc))
+        x = L.features(cm, fl, norm)
+        out["features_ms"] = timed(lambda: L.features(cm, fl, norm, out=x))
+        prev = os.environ.get("SPH_FEATURES_THREAD")
+        os.environ["SPH_FEATURES_THREAD"] = "1"
+        out["features_thread_per_destination_ms"] = timed(lambda: L.features(cm, fl, norm, out=x))
+        if prev is None:
+            os.environ.pop("SPH_FEATURES_THREAD", None)
+        else:
+            os.environ["SPH_FEATURES_THREAD"] = prev
+        out["network_ms"] = timed(lambda: model.forward(x))
+        y = model.forward(x)
+        scale = (ctypes.c_double * 2)(*norm.targ_std)
+        mean = (ctypes.c_double * 2)(*norm.targ_mean)
+        ptrs = (ctypes.c_void_p * 3)(*[a.data_ptr() for a in acc])
+
+        def apply():
+            native.check(native.lib().sph_mlp_apply(cm.context(), cm.slot(fl), y.data_ptr(), c0,
+                                                    scale, mean, ptrs, 1), "mlp apply")
+
+        out["apply_ms"] = timed(apply)
+        dev = out["features_ms"][0] + out["network_ms"][0] + out["apply_ms"][0]
+        out["closure_device_ms"] = dev
+        out["closure_device_vs_pair_loop"] = dev / out["pair_loop_ms"][0]
+        return out
+
     # cross-resolution (trained at dx = 0.01, deployed at dx = 0.005, the
     # 80,000-particle case) and in-distribution (trained and deployed at
     # dx = 0.01; the column's aspect ratio 0.5 lies inside the training
     # range but is not one of the training runs)
+    terms = term_timings(0.005, args.dt, (1.0, 2.0))
+    log("per-term times at dx 0.005: %s" % terms)
     cross = deploy(0.005, args.dt, (1.0, 2.0))
     indist = deploy(0.01, args.train_dt, (1.0, 2.0))
     plain_sps = cross["plain_steps_per_s"]
@@ -1032,6 +1104,7 @@ def run_gpu_closure(args):
         "plain_steps_per_s": plain_sps,
         "cross_resolution": cross,
         "in_distribution": indist,
+        "terms_ms": terms,
         "training": {"samples": int(nb * 8192), "epochs": args.epochs, "loss_first": losses[0],
                      "loss_last": losses[-1], "seconds": t_train, "data_seconds": t_data,
                      "tflops_fwd_bwd": flops / t_train / 1e12},

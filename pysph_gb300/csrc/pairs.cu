@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 
 #include "sph_internal.cuh"
@@ -540,6 +541,7 @@ struct FeatureArgs {
     float mean[SPH_MLP_NCH], inv_std[SPH_MLP_NCH];
     uint16_t *out_bf;   // [n][192] BF16 by original index (or null)
     float *out_f;       // [n][192] FP32 by original index (or null)
+    const int *s_skey;  // sorted: cell of each source slot
     const unsigned *gate;
 };
 
@@ -636,6 +638,154 @@ __global__ void __launch_bounds__(kPairBlock) k_features(const __grid_constant__
 #pragma unroll
             for (int i = 0; i < 6; ++i) o[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
         }
+    }
+}
+
+// The same features with one warp per destination (no periodic axis or
+// symmetry plane): lane k takes list entry k of every chunk of 32, the warp
+// sorts the chunk's 64-bit keys (FP32 squared distance bits, sorted slot:
+// the order of the thread-per-destination kernel) with a bitonic network
+// of shuffles and merges them into the 32 nearest so far; lane k then
+// recomputes the offsets of neighbour k with the list pass's operations
+// (the cell offset from the source's cell) and writes row k (a
+// destination's 384-byte row as one contiguous warp store).  Neighbours
+// past an over-full list come from the traversal the thread-per-destination
+// kernel uses, run in lockstep by all lanes (the same destination), each
+// inserted into the sorted set with its own offsets.
+__device__ __forceinline__ uint64_t feat_key(float r2, int j) {
+    return ((uint64_t)__float_as_uint(r2) << 32) | (uint32_t)j;
+}
+
+// compare-exchange stages j0, j0/2, .., 1 of a bitonic network of block k
+__device__ __forceinline__ void feat_stages(uint64_t &key, int lane, int k, int j0) {
+    for (int jj = j0; jj > 0; jj >>= 1) {
+        const uint64_t o = __shfl_xor_sync(0xffffffffu, key, jj);
+        const bool keep_min = ((lane & k) == 0) == ((lane & jj) == 0);
+        key = keep_min ? (o < key ? o : key) : (o > key ? o : key);
+    }
+}
+
+__device__ __forceinline__ void feat_sort32(uint64_t &key, int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) feat_stages(key, lane, k, k >> 1);
+}
+
+// (six blocks per SM: 40 registers, 55 us at 80 000 destinations in 2D
+// against 61 us at the 64 registers of four blocks and 66 us at eight)
+template <int KX>
+__global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant__ FeatureArgs A) {
+    constexpr int NN = SPH_MLP_NNBR, NC = SPH_MLP_NCH;
+    static_assert(NN == 32, "one lane per kept neighbour");
+    const int lane = threadIdx.x & 31;
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (s >= A.d.n || gated_off(A.gate)) return;
+    DestPos d;
+    const bool real = load_dest(A.g, A.d, (int)s, d);
+    const float4 vi = A.d.velh[s];
+    const SrcDev &S = A.s;
+    const float csf = A.g.cs_f;
+    constexpr uint64_t none = ~0ull;
+    uint64_t best = none;
+    // offsets carried by neighbours found by the traversal (flag set)
+    float crx = 0.f, cry = 0.f;
+    bool carried = false;
+    if (real) {
+        using C = Code<KX>;
+        const int c = S.ncnt[s];
+        const int m = min(c, A.cap);
+        auto candidate = [&](int k) {
+            uint64_t key = none;
+            if (k < m) {
+                const uint32_t e = S.nbr[s + (int64_t)k * A.stride];
+                const int j = (int)(e & C::JMASK);
+                const float3 sh = neg_cell_offset<KX>(e);
+                const float4 p = S.pm[j];
+                const float rx = fmaf(sh.x, csf, d.xi_x - p.x);
+                const float ry = fmaf(sh.y, csf, d.xi_y - p.y);
+                const float rz = fmaf(sh.z, csf, d.xi_z - p.z);
+                if (listed_exact<false>(A.g, S, A.d, d, j, rx, ry, rz))
+                    key = feat_key(fmaf(rx, rx, fmaf(ry, ry, rz * rz)), j);
+            }
+            return key;
+        };
+        // the 32 smallest of two ascending sets: a bitonic sequence, then merged
+        auto merge = [&](uint64_t cand) {
+            const uint64_t r = __shfl_sync(0xffffffffu, cand, 31 - lane);
+            if (r < best) best = r;
+            feat_stages(best, lane, 32, 16);
+        };
+        // two chunks of 32 at a time, their loads and sorts side by side
+        for (int k0 = 0; k0 < m; k0 += 64) {
+            uint64_t c0 = candidate(k0 + lane);
+            uint64_t c1 = candidate(k0 + 32 + lane);
+            feat_sort32(c0, lane);
+            if (k0 + 32 < m) feat_sort32(c1, lane);
+            if (k0 == 0) best = c0;
+            else merge(c0);
+            if (k0 + 32 < m) merge(c1);
+        }
+        if (c > A.cap) {
+            // the rest, in the order of the list build, every lane alike
+            int skip = A.cap;
+            for_neighbours<KX, false>(A.g, S, d, A.d.x, A.d.y, A.d.z,
+                [&](int j, float rx, float ry, float rz, int, bool exact) {
+                    if (skip > 0) { --skip; return; }
+                    if (!exact) return;
+                    const uint64_t x = feat_key(fmaf(rx, rx, fmaf(ry, ry, rz * rz)), j);
+                    // insert: lanes past the position shift up by one
+                    const int pos = __popc(__ballot_sync(0xffffffffu, best < x));
+                    const int from = lane > 0 ? lane - 1 : 0;
+                    const uint64_t pk = __shfl_sync(0xffffffffu, best, from);
+                    const float px = __shfl_sync(0xffffffffu, crx, from);
+                    const float py = __shfl_sync(0xffffffffu, cry, from);
+                    const bool pc = __shfl_sync(0xffffffffu, carried, from);
+                    if (lane > pos) {
+                        best = pk; crx = px; cry = py; carried = pc;
+                    } else if (lane == pos) {
+                        best = x; crx = rx; cry = ry; carried = true;
+                    }
+                });
+        }
+    }
+    const bool have = best != none;
+    float raw[NC] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (have) {
+        const int j = (int)(uint32_t)best;
+        float rx = crx, ry = cry;
+        if (!carried) {
+            // the list pass's offsets: cell offset from the source's cell
+            int cxj, cyj, czj;
+            decode_cell(A.g, A.s_skey[j], cxj, cyj, czj);
+            const float4 p = S.pm[j];
+            rx = fmaf((float)(d.cx - cxj), csf, d.xi_x - p.x);
+            ry = fmaf((float)(d.cy - cyj), csf, d.xi_y - p.y);
+        }
+        const float ih = 1.f / vi.w;
+        const float4 vj = S.velh[j];
+        const float4 st = S.st[j];
+        raw[0] = rx * ih;
+        raw[1] = ry * ih;
+        raw[2] = (vj.x - vi.x) * A.inv_c0;
+        raw[3] = (vj.y - vi.y) * A.inv_c0;
+        raw[4] = st.x;
+        raw[5] = st.y * st.x * st.x;
+    }
+    float f[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) f[q] = have ? (raw[q] - A.mean[q]) * A.inv_std[q] : 0.f;
+    const int64_t row = (int64_t)d.orig * (NN * NC) + lane * NC;
+    if (A.out_bf) {
+        uint32_t *o = reinterpret_cast<uint32_t *>(A.out_bf + row);
+#pragma unroll
+        for (int i = 0; i < NC / 2; ++i) {
+            __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+            o[i] = *reinterpret_cast<uint32_t *>(&h);
+        }
+    }
+    if (A.out_f) {
+        float2 *o = reinterpret_cast<float2 *>(A.out_f + row);
+#pragma unroll
+        for (int i = 0; i < NC / 2; ++i) o[i] = make_float2(f[2 * i], f[2 * i + 1]);
     }
 }
 
@@ -1113,12 +1263,19 @@ int features_pass(sph_ctx *ctx, int dst, int src, const sph_mlp_feature_params *
     }
     a.out_bf = out_bf;
     a.out_f = out_f;
+    a.s_skey = ctx->arrays[src].skey;
     a.gate = ctx->gate;
     if (D.n == 0) return SPH_OK;
     const int b = blocks_for(D.n);
     const bool ext = a.g.periodic || a.g.symmetric;
+    // one warp per destination (environment SPH_FEATURES_THREAD=1, read at
+    // every call: one thread per destination)
+    const char *env_thread = getenv("SPH_FEATURES_THREAD");
+    const bool per_thread = env_thread && atoi(env_thread) > 0;
+    const int bw = (int)((D.n * 32 + 255) / 256);
 #define FLAUNCH(K) (ext ? k_features<K, true><<<b, kPairBlock, 0, ctx->stream>>>(a) \
-                        : k_features<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a))
+                    : per_thread ? k_features<K, false><<<b, kPairBlock, 0, ctx->stream>>>(a) \
+                                 : k_features_warp<K><<<bw, 256, 0, ctx->stream>>>(a))
     switch (code_variant(ctx)) {
         case 1: FLAUNCH(1); break;
         case 2: FLAUNCH(2); break;

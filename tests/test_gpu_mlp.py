@@ -165,6 +165,66 @@ def test_features_match_oracle():
     np.testing.assert_allclose(bf, M.bf16(want_s), rtol=1e-2, atol=1e-3)
 
 
+def _feature_state():
+    props = _jittered_drop()
+    s, particles = W.setup_drop(API, props, c0=100.0)
+    integ = s.integrator
+    integ.integrate(1e-5)
+    integ.cstep = 1
+    integ.stages[0].run(integ, "k1")
+    return particles.cell_manager, particles.arrays[0]
+
+
+def test_feature_kernels_agree(monkeypatch):
+    """The warp-per-destination feature kernel (a bitonic sort of each chunk
+    of 32 listed neighbours) and the thread-per-destination one give the
+    same rows, bit for bit, raw and standardised."""
+    _need_gpu()
+    cm, pa = _feature_state()
+    norm = L.Normalisation(100.0, np.array([0.1, -0.2, 0.01, 0.02, 1.0, 5.0]),
+                           np.array([0.9, 0.8, 0.3, 0.4, 0.01, 20.0]))
+    out = {}
+    for thread in ("1", "0"):
+        monkeypatch.setenv("SPH_FEATURES_THREAD", thread)
+        out[thread] = (L.features(cm, pa, norm, raw=True).clone(),
+                       L.features(cm, pa, norm).clone())
+    assert torch.equal(out["1"][0], out["0"][0])
+    assert torch.equal(out["1"][1], out["0"][1])
+    assert float((out["0"][0] != 0).any(dim=1).float().mean()) > 0.5
+
+
+_FEAT_OVERFULL = r"""
+import sys
+sys.path.insert(0, ".")
+sys.path.insert(0, "tests")
+import os, torch
+import test_gpu_mlp as T
+from pysph_gb300 import learned as L
+cm, pa = T._feature_state()
+rows = {}
+for thread in ("1", "0"):
+    os.environ["SPH_FEATURES_THREAD"] = thread
+    rows[thread] = L.features(cm, pa, L.Normalisation(100.0), raw=True).clone()
+assert torch.equal(rows["1"], rows["0"])
+print("ok")
+"""
+
+
+def test_feature_kernels_agree_on_overfull_lists():
+    """Lists shorter than the neighbour counts (completed by the traversal,
+    each neighbour inserted into the warp's sorted set): same rows as the
+    thread-per-destination kernel, in a fresh process."""
+    _need_gpu()
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, SPH_LIST_CAP="9")
+    r = subprocess.run([sys.executable, "-c", _FEAT_OVERFULL], cwd=root, env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-3000:]
+
+
 def _small_dam(dx=0.04):
     fluid, wall = W.dam_break(dx=dx)
     c0 = W.dam_break_c0()
