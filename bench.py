@@ -60,14 +60,14 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # of one ncu capture of the 1M-particle lattice, brick-staged passes at cell
 # subdivision 2); the traffic grows with the particle count, so it is scaled
 # by n
-NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 222.3, "RatesStage": 285.5}
+NCU_TRAFFIC_PER_PARTICLE = {"DensityStage": 222.3, "RatesStage": 286.1}
 # The unit that bounds each pair kernel in the same capture, as a fraction of
 # that unit's peak: the rates pass is bound by the L1 / shared-memory pipe
 # that serves its staged-record reads (and their latency), the density pass
 # by instruction issue
 NCU_LIMITER = {
-    "RatesStage": {"kernel": "k_brates", "unit": "L1 / shared-memory pipe", "frac": 0.795,
-                   "issue_frac": 0.579, "dram_frac": 0.132},
+    "RatesStage": {"kernel": "k_brates", "unit": "L1 / shared-memory pipe", "frac": 0.702,
+                   "issue_frac": 0.618, "dram_frac": 0.141},
     "DensityStage": {"kernel": "k_bdensity", "unit": "instruction issue", "frac": 0.646,
                      "l1_frac": 0.603, "dram_frac": 0.179},
 }
