@@ -5,26 +5,28 @@
 // momentum pair loop (sph/funcs/pressure_funcs.pyx:40-91 and
 // sph/funcs/viscosity_funcs.pyx:41-124) of a fluid array on itself.
 //
-// Operands: BF16, in shared memory in the canonical K-major layout without
-// swizzle -- 8-row x 16-byte core matrices, core matrix (row/8, k/8) at
-// ((row/8) * K/8 + k/8) * 128 bytes, so the leading-dimension offset (next
-// core matrix along K) is 128 B and the stride-dimension offset (next 8
-// rows) is K/8 * 128 B.  One thread issues tcgen05.mma (M = 128 samples or
-// hidden units, kind::f16 with BF16 A and B, FP32 accumulation in tensor
-// memory) and tcgen05.commit signals an mbarrier; the eight warps of the
-// CTA read the accumulator rows back with tcgen05.ld: warps w and w + 4 own
-// lanes 32(w%4)..32(w%4)+31 (one tile row per thread) and split the
-// columns, so the FP32 epilogues, which bound these kernels, have two warps
-// per scheduler to hide their latency.
+// Operands: BF16 in shared memory, FP32 accumulation in tensor memory
+// (tcgen05.mma kind::f16, M = 128 samples or hidden units, issued by one
+// thread, completion through tcgen05.commit onto an mbarrier; the
+// accumulator rows read back with tcgen05.ld by the warps that own their
+// lane quarter).
 //
-//   k_mlp_fwd   per 128-sample tile: X W1^T -> +b1, GELU -> BF16 H1 (smem)
-//               -> H1 W2^T -> +b2, GELU -> BF16 h2 -> h2 W3^T + b3 on the
-//               CUDA cores.  Training saves z1, z2 (FP32) and h1, h2 (BF16).
-//   k_mlp_bwd   per tile: dy = (y - t) / B; dz2 = (dy W3) * gelu'(z2);
-//               dh1 = dz2 W2 (tensor cores); dW2 += dz2^T h1 and
-//               dW1 += dz1^T x accumulated in tensor memory over the CTA's
-//               tiles; an extra row of ones in the B operand of the weight
-//               gradients yields the bias gradients in the same product.
+//   k_mlp_fwd_tma  the forward, warp-specialised: TMA loads of X and the
+//               weights into 128-byte-swizzled K-major atoms, one MMA warp,
+//               16 epilogue warps (X W1^T -> +b1, GELU -> BF16 H1 in shared
+//               memory -> H1 W2^T -> +b2, GELU -> h2 W3^T + b3 on the CUDA
+//               cores, in packed FP32x2 arithmetic).  Training saves z1, z2
+//               (FP32) and h1, h2 (BF16).
+//   k_mlp_bwd_tma  the backward, warp-specialised: per tile z2 = h1 W2^T
+//               + b2 recomputed, dz2 = (dy W3) * gelu'(z2), dh1 = dz2 W2,
+//               dz1 = dh1 * gelu'(z1), and dW2 += dz2^T h1, dW1 += dz1^T x
+//               accumulated in tensor memory over the CTA's tiles, the
+//               sample-major tiles read as MN-major operands (no
+//               transposes); a column of ones yields the bias gradients in
+//               the same products.
+//   k_mlp_fwd, k_mlp_bwd  the kernels these replace (plain staged loads in
+//               the canonical layout without swizzle; transposed staging),
+//               kept to measure against.
 //   k_mlp_l3    third-layer gradients (FP32 CUDA cores).
 //   k_mlp_reduce  fixed-order sum of the per-CTA partial gradients.
 //   k_mlp_adam  Adam on the FP32 master parameters and the BF16 copies.
