@@ -24,9 +24,10 @@
 //               sample-major tiles read as MN-major operands (no
 //               transposes); a column of ones yields the bias gradients in
 //               the same products.
-//   k_mlp_fwd, k_mlp_bwd  the kernels these replace (plain staged loads in
-//               the canonical layout without swizzle; transposed staging),
-//               kept to measure against.
+//   k_mlp_fwd, k_mlp_bwd  the kernels these replace, kept to measure
+//               against: plain staged loads in the canonical layout without
+//               swizzle; operands transposed into 128-byte-swizzled staging
+//               and the saved z2 read.
 //   k_mlp_l3    third-layer gradients (FP32 CUDA cores).
 //   k_mlp_reduce  fixed-order sum of the per-CTA partial gradients.
 //   k_mlp_adam  Adam on the FP32 master parameters and the BF16 copies.
