@@ -16,6 +16,11 @@ import os
 # the skin (PYSPH_GB300_SKIN overrides; 0 rebuilds at every update like the
 # reference)
 DEFAULT_SKIN = 0.03
+# from GRAPH_MAX_PARTICLES up (no adaptive skin): at 1 M particles, 300 RK2
+# steps of the jittered lattice, 1.118 / 1.098 / 1.111 / 1.104 / 1.113 /
+# 1.124 ms per step at skins 0.015 / 0.02 / 0.025 / 0.03 / 0.04 / 0.05
+# (shorter lists against more full builds)
+LARGE_SKIN = 0.02
 
 
 # small simulations whose lists go stale within a few steps (the motion of
@@ -34,13 +39,16 @@ def adaptive_skin(nparticles):
     return os.environ.get("PYSPH_GB300_SKIN") is None and nparticles < GRAPH_MAX_PARTICLES
 
 
-def list_skin():
+def list_skin(nparticles=None):
+    """The list skin a neighbour structure of ``nparticles`` starts with."""
     env = os.environ.get("PYSPH_GB300_SKIN")
     if env is not None:
         v = float(env)
         if not 0.0 <= v <= 0.5:
             raise ValueError("PYSPH_GB300_SKIN must be in [0, 0.5]")
         return v
+    if nparticles is not None and nparticles >= GRAPH_MAX_PARTICLES:
+        return LARGE_SKIN
     return DEFAULT_SKIN
 
 

@@ -209,3 +209,18 @@ def test_base5_cell_offset_decode_is_exact():
                 assert (x - 2, y - 2, z - 2) == (dx, dy, dz)
                 seen.add(c)
     assert len(seen) == 125
+
+
+def test_list_skin_defaults(monkeypatch):
+    """The list skin a neighbour structure starts with: the small default
+    (which the integrators may grow) below 500 000 particles, the large
+    default from there up, the environment setting for any size."""
+    from pysph_gb300 import tuning
+    monkeypatch.delenv("PYSPH_GB300_SKIN", raising=False)
+    assert tuning.list_skin() == tuning.DEFAULT_SKIN
+    assert tuning.list_skin(tuning.GRAPH_MAX_PARTICLES - 1) == tuning.DEFAULT_SKIN
+    assert tuning.list_skin(tuning.GRAPH_MAX_PARTICLES) == tuning.LARGE_SKIN
+    assert tuning.adaptive_skin(1000) and not tuning.adaptive_skin(tuning.GRAPH_MAX_PARTICLES)
+    monkeypatch.setenv("PYSPH_GB300_SKIN", "0.05")
+    assert tuning.list_skin(10) == 0.05 and tuning.list_skin(10 ** 7) == 0.05
+    assert not tuning.adaptive_skin(1000)
