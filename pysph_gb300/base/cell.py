@@ -192,7 +192,7 @@ class CellManager:
         s = getattr(self, "skin", None)
         if s is None:
             from ..tuning import list_skin
-            s = self.skin = list_skin(self.get_number_of_particles())
+            s = self.skin = list_skin()
         return s
 
     def set_deferred_check(self, on):

@@ -446,18 +446,21 @@ class Integrator:
 
     def _adapt_skin(self):
         """Grow the neighbour-list skin of a small simulation whose lists go
-        stale within a few steps (``tuning.adaptive_skin``): every
-        SKIN_WINDOW steps, while the window had more than one full build per
-        four steps, the skin doubles (up to SKIN_MAX)."""
+        stale within a few steps (``tuning.skin_growth``): every SKIN_WINDOW
+        steps, while the window had more than one full build per four steps,
+        the skin doubles (up to SKIN_MAX)."""
         from .. import tuning
-        if (self._steps_done % tuning.SKIN_WINDOW != 0 or getattr(self, "skin_frozen", False)
-                or not torch.cuda.is_available()):
+        if getattr(self, "skin_frozen", False) or not torch.cuda.is_available():
+            return
+        n = sum(pa.get_number_of_particles() for pa in self.particles.arrays)
+        rule = tuning.skin_growth(n)
+        if rule is None:
+            return
+        window, most, factor, ceiling = rule
+        if self._steps_done % window != 0:
             return
         cm = getattr(self.particles, "cell_manager", None)
         if cm is None or cm._ctx is None:
-            return
-        n = sum(pa.get_number_of_particles() for pa in self.particles.arrays)
-        if not tuning.adaptive_skin(n):
             return
         # full builds only: steps replayed as graphs and steps run call by
         # call count them alike (not so the light refreshes a stale one
@@ -468,8 +471,10 @@ class Integrator:
         if last is None:
             return
         skin = cm.list_skin()
-        if full - last > tuning.SKIN_WINDOW // 4 and 0.0 < skin < tuning.SKIN_MAX:
-            cm.set_skin(min(tuning.SKIN_MAX, 2.0 * skin))
+        if full - last > most and 0.0 < skin < ceiling:
+            cm.set_skin(min(ceiling, factor * skin))
+            # the next window starts after the build the new skin forced
+            self._skin_window = cm.build_stats()[0]
 
     def _may_record(self):
         from ..tuning import step_graphs

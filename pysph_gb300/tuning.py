@@ -16,11 +16,6 @@ import os
 # the skin (PYSPH_GB300_SKIN overrides; 0 rebuilds at every update like the
 # reference)
 DEFAULT_SKIN = 0.03
-# from GRAPH_MAX_PARTICLES up (no adaptive skin): at 1 M particles, 300 RK2
-# steps of the jittered lattice, 1.118 / 1.098 / 1.111 / 1.104 / 1.113 /
-# 1.124 ms per step at skins 0.015 / 0.02 / 0.025 / 0.03 / 0.04 / 0.05
-# (shorter lists against more full builds)
-LARGE_SKIN = 0.02
 
 
 # small simulations whose lists go stale within a few steps (the motion of
@@ -32,24 +27,29 @@ SKIN_WINDOW = 16
 SKIN_MAX = 0.24
 
 
-def adaptive_skin(nparticles):
-    """Whether the integrators may grow the list skin: no PYSPH_GB300_SKIN
-    set, fewer than GRAPH_MAX_PARTICLES particles (whether or not steps are
-    replayed as graphs, so both ways take the same steps)."""
-    return os.environ.get("PYSPH_GB300_SKIN") is None and nparticles < GRAPH_MAX_PARTICLES
 
-
-def list_skin(nparticles=None):
-    """The list skin a neighbour structure of ``nparticles`` starts with."""
+def list_skin():
     env = os.environ.get("PYSPH_GB300_SKIN")
     if env is not None:
         v = float(env)
         if not 0.0 <= v <= 0.5:
             raise ValueError("PYSPH_GB300_SKIN must be in [0, 0.5]")
         return v
-    if nparticles is not None and nparticles >= GRAPH_MAX_PARTICLES:
-        return LARGE_SKIN
     return DEFAULT_SKIN
+
+
+def skin_growth(nparticles):
+    """(window, builds above which the skin grows, factor, ceiling) of the
+    integrators' skin adaptation, or None: PYSPH_GB300_SKIN set, or a
+    simulation of GRAPH_MAX_PARTICLES or more, whose step time is flat
+    around the default (1 M particles of the jittered lattice, 300 RK2
+    steps: 1.118 / 1.098 / 1.111 / 1.104 / 1.113 / 1.124 ms per step at
+    skins 0.015 / 0.02 / 0.025 / 0.03 / 0.04 / 0.05; 16.8 M: 18.25 ms at
+    0.03 against 18.33 ms with the skin grown to 0.0675 whenever a window
+    of 32 steps had more than 5 full builds)."""
+    if os.environ.get("PYSPH_GB300_SKIN") is not None or nparticles >= GRAPH_MAX_PARTICLES:
+        return None
+    return SKIN_WINDOW, SKIN_WINDOW // 4, 2.0, SKIN_MAX
 
 
 def brick_passes():

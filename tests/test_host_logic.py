@@ -212,15 +212,15 @@ def test_base5_cell_offset_decode_is_exact():
 
 
 def test_list_skin_defaults(monkeypatch):
-    """The list skin a neighbour structure starts with: the small default
-    (which the integrators may grow) below 500 000 particles, the large
-    default from there up, the environment setting for any size."""
+    """The list skin a neighbour structure starts with and the integrators'
+    rule for growing it: doubling below 500 000 particles, none from there up
+    or when the environment fixes the skin."""
     from pysph_gb300 import tuning
     monkeypatch.delenv("PYSPH_GB300_SKIN", raising=False)
     assert tuning.list_skin() == tuning.DEFAULT_SKIN
-    assert tuning.list_skin(tuning.GRAPH_MAX_PARTICLES - 1) == tuning.DEFAULT_SKIN
-    assert tuning.list_skin(tuning.GRAPH_MAX_PARTICLES) == tuning.LARGE_SKIN
-    assert tuning.adaptive_skin(1000) and not tuning.adaptive_skin(tuning.GRAPH_MAX_PARTICLES)
+    assert tuning.skin_growth(tuning.GRAPH_MAX_PARTICLES - 1) == (
+        tuning.SKIN_WINDOW, tuning.SKIN_WINDOW // 4, 2.0, tuning.SKIN_MAX)
+    assert tuning.skin_growth(tuning.GRAPH_MAX_PARTICLES) is None
     monkeypatch.setenv("PYSPH_GB300_SKIN", "0.05")
-    assert tuning.list_skin(10) == 0.05 and tuning.list_skin(10 ** 7) == 0.05
-    assert not tuning.adaptive_skin(1000)
+    assert tuning.list_skin() == 0.05
+    assert tuning.skin_growth(10) is None
