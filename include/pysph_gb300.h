@@ -336,6 +336,14 @@ int sph_invariants(sph_ctx *ctx, const sph_array_view *a, double *out);
  * to the host and synchronises the stream before it returns. */
 int sph_invariants_noalloc(const sph_array_view *a, double *out, void *stream);
 
+/* Self-check of the integer-operation conversions the light refresh uses in
+ * place of FP64 instructions (no reference counterpart): FP64 -> FP32 round
+ * to nearest against __double2float_rn, int -> FP64 against __int2double_rn
+ * and the FP32-screened cell index against its FP64 form, over n hashed
+ * inputs (all exponents, both signs) and edge values.  mismatches: host
+ * int64, the number of differing results (0 expected).  Synchronises. */
+int sph_selftest_conversions(int64_t n, int64_t *mismatches);
+
 /* ---------------------------------------------------------------------
  * Batches of independent simulations (no counterpart in the reference,
  * which runs one simulation per Solver).  All instances share one

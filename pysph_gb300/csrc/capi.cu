@@ -542,5 +542,9 @@ int sph_mlp_targets(int64_t n, const double *ax, const double *ay, const double 
     return mlp_targets(n, ax, ay, h, c0, mean, inv_std, out, (cudaStream_t)stream);
 }
 
+int sph_selftest_conversions(int64_t n, int64_t *mismatches) {
+    return selftest_conversions(n, mismatches);
+}
+
 }  // extern "C"
 

@@ -316,13 +316,52 @@ struct ListCaps {
 
 constexpr unsigned kLightHChanged = 1u << 8;
 
-__global__ void k_invperm(int64_t n, const int *perm, int *inv) {
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
-         s += (int64_t)gridDim.x * blockDim.x)
-        inv[perm[s]] = (int)s;
+// The integer-operation conversions against the hardware's: input k is a
+// hashed 64-bit pattern (every exponent and sign; NaN patterns skipped), and
+// the first inputs are edge values (zero, extremes of the FP32 range, ties).
+__device__ __forceinline__ unsigned long long selftest_bits(long long k) {
+    unsigned long long z = (unsigned long long)k * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
 }
 
-__global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
+__global__ void k_selftest_conversions(long long n, unsigned long long *bad) {
+    const double edge[] = {0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 3.4028235677973366e38,
+                           1.1754943508222875e-38, 1.1754942106924411e-38, 1.401298464324817e-45,
+                           1.0000000596046448, 1.0000001788139343, 0.5, 1e300, -1e-300,
+                           8388608.5, 16777217.0};
+    constexpr int NE = sizeof(edge) / sizeof(edge[0]);
+    unsigned long long miss = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long b = selftest_bits(k);
+        double x = k < NE ? edge[k] : __longlong_as_double((long long)b);
+        if (x != x) x = __longlong_as_double((long long)(b & 0x800FFFFFFFFFFFFFull));
+        if (__float_as_uint(d2f_rn(x)) != __float_as_uint(__double2float_rn(x))) ++miss;
+        const int iv = (int)(unsigned)b;
+        if (__double_as_longlong(i2d_exact(iv)) != __double_as_longlong(__int2double_rn(iv))) ++miss;
+        // cell indices of positions in [-1000, 1000) at cell sizes 1e-3 .. 1
+        const double pos = ((double)(b >> 11) * (1.0 / 9007199254740992.0)) * 2000.0 - 1000.0;
+        const double inv = 1.0 / (1e-3 + (double)((b >> 3) & 1023) * 1e-3);
+        if (floor_cell_screened(pos, inv, (float)inv) != (int)floor(pos * inv)) ++miss;
+    }
+    if (miss) atomicAdd(bad, miss);
+}
+
+// original -> sorted slot, and the build's position records in original
+// order (so that a light refresh reads them with its other per-particle
+// loads, not through the slot it has yet to load)
+__global__ void k_invperm(int64_t n, const int *perm, const float4 *pm, int *inv, float4 *pm0) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int i = perm[s];
+        inv[i] = (int)s;
+        pm0[i] = pm[s];
+    }
+}
+
+__global__ void __launch_bounds__(256, 5) k_light(sph_array_view a, Grid g, double inv_cs_ref, const int *inv,
                         const int *key, const float4 *pm0, float4 *velh,
                         float4 *nrm, float4 *tan, float4 *pm, int *refcell,
                         int check_jump,
@@ -330,6 +369,7 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
                         unsigned *status, unsigned stale_bit) {
     float dm = 0.f;
     bool jump = false, hch = false;
+    const float inv_ref_f = (float)inv_cs_ref;
     // list maxima: written by the passes before this launch
     if (blockIdx.x == 0 && threadIdx.x < caps.n &&
         (int)status[kListWord0 + threadIdx.x] > caps.cap[threadIdx.x]) {
@@ -342,17 +382,20 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         int cx, cy, cz;
         decode_cell(g, key[i], cx, cy, cz);
         const double px = ld0(a.x, i), py = ld0(a.y, i), pz = ld0(a.z, i);
-        const double ox = (double)(cx + g.bx0), oy = (double)(cy + g.by0), oz = (double)(cz + g.bz0);
-        const float xi = (float)fma(-ox, g.cs, bin_x(g, px));
-        const float yi = (float)fma(-oy, g.cs, py);
-        const float zi = (float)fma(-oz, g.cs, pz);
-        const float4 p0 = pm0[s];
+        // the FP64 work of a refresh is the three offsets from the cell
+        // origin; conversions and comparisons are done with integers
+        const double ox = i2d_exact(cx + g.bx0), oy = i2d_exact(cy + g.by0), oz = i2d_exact(cz + g.bz0);
+        const float xi = d2f_rn(fma(-ox, g.cs, bin_x(g, px)));
+        const float yi = d2f_rn(fma(-oy, g.cs, py));
+        const float zi = d2f_rn(fma(-oz, g.cs, pz));
+        const float4 p0 = pm0[i];
         const float ddx = xi - p0.x, ddy = yi - p0.y, ddz = zi - p0.z;
         dm = fmaxf(dm, fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)));
         const double h = a.h[i];
-        if (h != build_h) hch = true;
-        velh[s] = make_float4((float)ld0(a.u, i), (float)ld0(a.v, i), (float)ld0(a.w, i), (float)h);
-        pm[s] = make_float4(xi, yi, zi, (float)a.m[i]);
+        if (__double_as_longlong(h) != __double_as_longlong(build_h)) hch = true;
+        velh[s] = make_float4(d2f_rn(ld0(a.u, i)), d2f_rn(ld0(a.v, i)), d2f_rn(ld0(a.w, i)),
+                              d2f_rn(h));
+        pm[s] = make_float4(xi, yi, zi, d2f_rn(a.m[i]));
         if (nrm) {
             nrm[s] = make_float4((float)ld0(a.nx, i), (float)ld0(a.ny, i), (float)ld0(a.nz, i), 0.f);
             tan[s] = make_float4((float)ld0(a.tx, i), (float)ld0(a.ty, i), (float)ld0(a.tz, i), 0.f);
@@ -362,7 +405,7 @@ __global__ void __launch_bounds__(256, 6) k_light(sph_array_view a, Grid g, doub
         for (int d = 0; d < 3; ++d) {
             // the reference cell rarely changes between updates: store only
             // a change (no write-back of unchanged lines)
-            const int c = floor_cell(pp[d], inv_cs_ref);
+            const int c = floor_cell_screened(pp[d], inv_cs_ref, inv_ref_f);
             const int c0 = refcell[3 * i + d];
             if (check_jump && abs(c - c0) > 1) jump = true;
             if (c != c0) refcell[3 * i + d] = c;
@@ -756,9 +799,8 @@ int nnps_build(sph_ctx *ctx, const sph_array_view *arrays, int narrays, double c
                     SPH_CUDA(cudaMalloc(&A.inv, sizeof(int) * v.n));
                     A.pm0_cap = v.n;
                 }
-                SPH_CUDA(cudaMemcpyAsync(A.pm0, A.pm, sizeof(float4) * v.n,
-                                         cudaMemcpyDeviceToDevice, st));
-                k_invperm<<<grid_blocks(v.n, kThreads), kThreads, 0, st>>>(v.n, A.perm, A.inv);
+                k_invperm<<<grid_blocks(v.n, kThreads), kThreads, 0, st>>>(v.n, A.perm, A.pm, A.inv,
+                                                                           A.pm0);
                 count_launch();
                 SPH_LAUNCH_CHECK("k_invperm");
             }
@@ -1011,6 +1053,23 @@ int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t
         nullptr, offsets, index);
     count_launch();
     SPH_LAUNCH_CHECK("k_nbr fill");
+    return SPH_OK;
+}
+
+int selftest_conversions(int64_t n, int64_t *mismatches) {
+    if (n < 0 || !mismatches) return set_error(SPH_ERR_ARG, "selftest_conversions: bad argument");
+    unsigned long long *d = nullptr;
+    SPH_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess && n > 0) {
+        k_selftest_conversions<<<grid_blocks(n, kThreads), kThreads>>>((long long)n, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_check(e, "selftest_conversions");
+    *mismatches = (int64_t)h;
     return SPH_OK;
 }
 

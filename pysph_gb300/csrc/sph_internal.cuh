@@ -76,6 +76,75 @@ struct Grid {
     double pxmin = 0.0, plen = 0.0;
 };
 
+// FP64 -> FP32, round to nearest even, by integer operations only: on GB300
+// the FP64 pipe, which also executes the FP64 conversions, runs at a small
+// fraction of the FP32 rate (and a conversion left in the code under a
+// predicate still takes its issue slot there).  The result equals
+// __double2float_rn(x) for every non-NaN x, results below the normal FP32
+// range (rounded to a subnormal or zero) and overflow to infinity included;
+// a NaN gives a quiet NaN.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int E = (int)((hi >> 20) & 0x7ffu);
+    const int e = E - 896;                             // FP32 biased exponent
+    const unsigned m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) ? 1u : 0u;
+    // a carry out of the mantissa raises the exponent (to infinity from 254)
+    unsigned r = sign | (((unsigned)e << 23) + m23 + up);
+    if (e >= 255) {
+        const bool nan = E == 0x7ff && ((hi & 0xfffffu) | lo) != 0u;
+        r = nan ? 0x7fffffffu : (sign | 0x7f800000u);
+    } else if (e <= 0) {
+        // |x| < 2^-126: the FP32 subnormal m 2^-149 nearest to x, with the
+        // full 53-bit significand shifted right by 30 - e (beyond 54 places
+        // it is below half the smallest subnormal: zero; a double zero or
+        // subnormal lands there too)
+        const int sh = 30 - e;
+        const unsigned long long M = (b & 0xfffffffffffffull) | (1ull << 52);
+        unsigned q = 0u;
+        if (sh <= 54) {
+            const unsigned long long lowm = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+            q = (unsigned)(M >> sh);
+            q += (lowm > half || (lowm == half && (q & 1u))) ? 1u : 0u;
+        }
+        r = sign | q;
+    }
+    return __uint_as_float(r);
+}
+
+// int -> FP64 (exact) by integer operations, as d2f_rn
+__device__ __forceinline__ double i2d_exact(int n) {
+    if (n == 0) return 0.0;
+    const unsigned long long sign = n < 0 ? (1ull << 63) : 0ull;
+    const unsigned a = n < 0 ? 0u - (unsigned)n : (unsigned)n;
+    const int e = 31 - __clz(a);                      // a in [2^e, 2^(e+1))
+    const unsigned long long m = ((unsigned long long)a << (52 - e)) & ((1ull << 52) - 1ull);
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | m));
+}
+
+// floor(x * inv) with the product rounded in FP64: a real call, so that its
+// FP64 instructions are issued only by the warps that take it
+static __device__ __noinline__ int floor_cell_fp64(double x, double inv) {
+    return (int)floor(x * inv);
+}
+
+// floor(x * inv) with the product rounded in FP64 (the reference's cell
+// index), screened in FP32: the FP32 product is within |t| 2^-22 of it, so
+// its floor is the same unless a cell boundary lies that close; only then
+// the FP64 product.
+__device__ __forceinline__ int floor_cell_screened(double x, double inv, float invf) {
+    const float tf = d2f_rn(x) * invf;
+    const float at = fabsf(tf);
+    int c = __float2int_rd(tf);
+    const float fr = tf - (float)c;
+    const float tol = fmaf(at, 4.8e-7f, 1e-30f);
+    if (!(at < 4194304.f && fr > tol && fr < 1.f - tol)) c = floor_cell_fp64(x, inv);
+    return c;
+}
+
 // Binning coordinate along x: the position, or on a periodic axis the offset
 // of its image in [pxmin, pxmin + plen) from pxmin.
 __device__ __forceinline__ double bin_x(const Grid &g, double x) {
@@ -133,7 +202,7 @@ struct ArraySnap {
     int64_t cell_cap = 0;
     int *refcell = nullptr; // original order, 3 ints per particle (jump check)
     int64_t ref_n = -1;     // particle count the refcell entries belong to
-    float4 *pm0 = nullptr; // pm at the last full build (skin lists)
+    float4 *pm0 = nullptr; // pm at the last full build, in original order (skin lists)
     int *inv = nullptr;      // original -> sorted slot of the last full build
     int64_t pm0_cap = 0;
     // brick tables of the last full build: exclusive prefix of the
@@ -324,6 +393,7 @@ int nnps_fill(sph_ctx *ctx, int dst, int src, double radius_scale, const int64_t
 int refresh_state(sph_ctx *ctx, int a, const sph_array_view *view);
 // bring the state record st of array a up to date if a light refresh left it
 int ensure_state(sph_ctx *ctx, int a);
+int selftest_conversions(int64_t n, int64_t *mismatches);
 // read the status of a deferred light refresh; *rebuilt: it was stale and a
 // full build replaced it (a gated pass launched since then did nothing)
 int resolve_pending(sph_ctx *ctx, bool *rebuilt);

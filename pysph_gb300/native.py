@@ -38,7 +38,7 @@ EXPORTS = (
     "sph_refresh_state", "sph_density", "sph_rates", "sph_tait", "sph_const_rates",
     "sph_adke_smoothing", "sph_adke_conduction",
     "sph_integrate", "sph_invariants", "sph_error_word", "sph_mean_neighbours",
-    "sph_launch_count", "sph_invariants_noalloc", "sph_nbr_lists",
+    "sph_launch_count", "sph_invariants_noalloc", "sph_selftest_conversions", "sph_nbr_lists",
     "sph_batch_create", "sph_batch_destroy", "sph_batch_setup", "sph_batch_step",
     "sph_batch_sync", "sph_batch_error_word", "sph_batch_stream",
     "sph_batch_pair_counts", "sph_batch_stats", "sph_ctx_set_skin", "sph_nnps_update", "sph_nnps_stats",
@@ -194,6 +194,7 @@ def load_library(build_if_missing=True):
         L.sph_mean_neighbours.argtypes = [vp, i32, i32, P(d)]
         L.sph_launch_count.argtypes = [P(i64)]
         L.sph_invariants_noalloc.argtypes = [P(ArrayView), P(d), vp]
+        L.sph_selftest_conversions.argtypes = [i64, P(i64)]
         f32 = ctypes.c_float
         L.sph_mlp_features.argtypes = [vp, i32, i32, P(MlpFeatureParams), vp, vp]
         L.sph_mlp_sync.argtypes = [P(MlpModel), vp]
