@@ -91,24 +91,37 @@ struct RatesArgs {
 };
 
 // Destination of thread slot s; false for a non-LocalReal particle.
+// (WARP: the 32 lanes of a warp share destination s; one lane does the two
+// FP64 products, which on GB300's FP64 pipe cost a warp 16 clocks each, and
+// the others take them by shuffle.  Every lane of the warp must call it.)
+template <bool WARP = false>
 __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s, DestPos &d) {
     const int orig = D.perm[s];
     d.orig = orig;
-    if (D.tag != nullptr && D.tag[orig] != SPH_TAG_LOCAL_REAL) return false;
+    const bool real = D.tag == nullptr || D.tag[orig] == SPH_TAG_LOCAL_REAL;
+    if (!WARP && !real) return false;
     const float4 p = D.pm[s];
     d.xi_x = p.x; d.xi_y = p.y; d.xi_z = p.z;
     decode_cell(g, D.skey[s], d.cx, d.cy, d.cz);
-    const double radius = __dmul_rn(D.h[orig], g.radius_scale);
-    d.radius2 = __dmul_rn(radius, radius);
-    const float r2 = (float)d.radius2;
+    double radius = 0.0;
+    if (!WARP || (threadIdx.x & 31) == 0) {
+        radius = __dmul_rn(D.h[orig], g.radius_scale);
+        d.radius2 = __dmul_rn(radius, radius);
+    }
+    if (WARP) {
+        radius = __shfl_sync(0xffffffffu, radius, 0);
+        d.radius2 = __shfl_sync(0xffffffffu, d.radius2, 0);
+    }
+    // FP32 copies by integer operations (bit-equal to the conversion)
+    const float r2 = d2f_rn(d.radius2);
     d.r2lo = r2 * (1.f - 1e-5f);
     d.r2hi = r2 * (1.f + 1e-5f);
     d.r2list = 0.f;
     if (g.skin > 0.f) {
-        const float rl = (float)radius + g.skin;
+        const float rl = d2f_rn(radius) + g.skin;
         d.r2list = rl * rl * (1.f + 2e-5f);
     }
-    return true;
+    return real;
 }
 
 // With a list skin the list holds sources up to the list radius: keep the
@@ -657,11 +670,15 @@ __device__ __forceinline__ uint64_t feat_key(float r2, int j) {
 }
 
 // compare-exchange stages j0, j0/2, .., 1 of a bitonic network of block k
+// (one 64-bit comparison: the partner's key is taken when it is smaller on
+// a lane that keeps the minimum, larger on one that keeps the maximum;
+// equal keys are alike either way)
 __device__ __forceinline__ void feat_stages(uint64_t &key, int lane, int k, int j0) {
+#pragma unroll
     for (int jj = j0; jj > 0; jj >>= 1) {
         const uint64_t o = __shfl_xor_sync(0xffffffffu, key, jj);
-        const bool keep_min = ((lane & k) == 0) == ((lane & jj) == 0);
-        key = keep_min ? (o < key ? o : key) : (o > key ? o : key);
+        const bool keep_max = ((lane & k) != 0) != ((lane & jj) != 0);
+        if ((o < key) != keep_max) key = o;
     }
 }
 
@@ -670,8 +687,8 @@ __device__ __forceinline__ void feat_sort32(uint64_t &key, int lane) {
     for (int k = 2; k <= 32; k <<= 1) feat_stages(key, lane, k, k >> 1);
 }
 
-// (six blocks per SM: 40 registers, 55 us at 80 000 destinations in 2D
-// against 61 us at the 64 registers of four blocks and 66 us at eight)
+// (six blocks per SM, 40 registers: 49 us at 80 000 destinations in 2D;
+// four and eight blocks per SM measured slower)
 template <int KX>
 __global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant__ FeatureArgs A) {
     constexpr int NN = SPH_MLP_NNBR, NC = SPH_MLP_NCH;
@@ -680,8 +697,7 @@ __global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant_
     const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (s >= A.d.n || gated_off(A.gate)) return;
     DestPos d;
-    const bool real = load_dest(A.g, A.d, (int)s, d);
-    const float4 vi = A.d.velh[s];
+    const bool real = load_dest<true>(A.g, A.d, (int)s, d);
     const SrcDev &S = A.s;
     const float csf = A.g.cs_f;
     constexpr uint64_t none = ~0ull;
@@ -714,15 +730,12 @@ __global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant_
             if (r < best) best = r;
             feat_stages(best, lane, 32, 16);
         };
-        // two chunks of 32 at a time, their loads and sorts side by side
-        for (int k0 = 0; k0 < m; k0 += 64) {
+        // one chunk of 32 at a time (two side by side spilled registers)
+        for (int k0 = 0; k0 < m; k0 += 32) {
             uint64_t c0 = candidate(k0 + lane);
-            uint64_t c1 = candidate(k0 + 32 + lane);
             feat_sort32(c0, lane);
-            if (k0 + 32 < m) feat_sort32(c1, lane);
             if (k0 == 0) best = c0;
             else merge(c0);
-            if (k0 + 32 < m) merge(c1);
         }
         if (c > A.cap) {
             // the rest, in the order of the list build, every lane alike
@@ -749,6 +762,8 @@ __global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant_
     }
     const bool have = best != none;
     float raw[NC] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // (loaded here, beside the neighbour's records, not live through the sort)
+    const float4 vi = A.d.velh[s];
     if (have) {
         const int j = (int)(uint32_t)best;
         float rx = crx, ry = cry;

@@ -484,9 +484,12 @@ class GuardedRunner:
 
     def stats(self):
         """Windows run, checked, kept and fallen back, with the errors."""
+        errs = sorted(self.errors)
         return {"windows": self.windows, "checks": self.checks, "kept": self.kept,
                 "fallbacks": self.fallbacks,
                 "fallback_rate": self.fallbacks / self.checks if self.checks else None,
+                "min_normwise_density_error": errs[0] if errs else None,
+                "median_normwise_density_error": errs[len(errs) // 2] if errs else None,
                 "max_normwise_density_error": self.max_err,
                 "max_relative_density_error": self.max_err_maxrel}
 
