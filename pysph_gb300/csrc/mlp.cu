@@ -260,18 +260,24 @@ __device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
     return d;
 }
 
-// GELU of a pair: z (1 - s), s = 1 / (1 + e^(2u)) (1 + tanh(u) = 2 (1 - s));
-// e^(2u) = 2^(z (E0 + E1 z^2)).  For z -> -inf, e -> 0 and s -> 1; for
-// z -> +inf, e -> inf and s -> 0.
+// GELU of a pair, z/2 (1 + tanh(u)), with the special-function unit's
+// tanh (tanh.approx.f32: one operation per value, against an exponential
+// and a reciprocal, which made the special-function unit the forward
+// epilogue's limiter).  Its error (about 2^-11 of |tanh u|) moves gelu by
+// at most ~2.5e-4 |z|, below the BF16 rounding of the activations it
+// feeds; tanh saturates to +-1, so both tails are exact in the limit.
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float kGeluU1 = kGeluC * 0.044715f;             // u = z (C + U1 z^2)
 __device__ __forceinline__ uint64_t gelu2(uint64_t z) {
-    const uint64_t one = f2(1.f, 1.f);
-    const uint64_t ku = mul2(z, fma2(mul2(z, z), f2(kGeluE1, kGeluE1), f2(kGeluE0, kGeluE0)));
-    float k0, k1;
-    f2_split(ku, k0, k1);
-    const uint64_t d = add2(f2(ex2_approx(k0), ex2_approx(k1)), one);
-    float d0, d1;
-    f2_split(d, d0, d1);
-    return mul2(z, sub2(one, f2(rcp_approx(d0), rcp_approx(d1))));
+    const uint64_t u = mul2(z, fma2(mul2(z, z), f2(kGeluU1, kGeluU1), f2(kGeluC, kGeluC)));
+    float u0, u1;
+    f2_split(u, u0, u1);
+    const uint64_t hz = mul2(z, f2(0.5f, 0.5f));
+    return fma2(hz, f2(tanh_approx(u0), tanh_approx(u1)), hz);
 }
 
 // d gelu / dz of a pair, as dgelu_s: (1 - s) (1 + z (D0 + D1 z^2) s)
