@@ -491,7 +491,7 @@ int sph_mlp_adam(const sph_mlp_model *m, const float *grad, float *mom, float *v
                  float beta1, float beta2, float eps, int step, void *stream);
 /* acc[c][i] = (or +=) (y[i][c] * scale[c] + mean[c]) * c0^2 / h_i for the
  * LocalReal particles of dst (acc[2], if given, is zeroed when not
- * accumulating). */
+ * accumulating), computed in FP32 and stored as FP64. */
 int sph_mlp_apply(sph_ctx *ctx, int dst, const float *y, double c0, const double *scale,
                   const double *mean, double *const *acc, int accumulate);
 /* out[i][c] = (a_c[i] * h_i / c0^2 - mean[c]) * inv_std[c]: standardised

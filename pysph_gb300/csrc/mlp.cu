@@ -1647,9 +1647,12 @@ __global__ void k_mlp_apply(int64_t n, const float *__restrict__ yv, const int64
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const bool real = tag == nullptr || tag[i] == SPH_TAG_LOCAL_REAL;
-    const double f = real ? c0sq / h[i] : 0.0;
-    const double a0 = real ? ((double)yv[2 * i] * s0 + m0) * f : 0.0;
-    const double a1 = real ? ((double)yv[2 * i + 1] * s1 + m1) * f : 0.0;
+    // in FP32 (the network's output carries BF16-level error): an FP64
+    // division costs a warp about ten instructions on GB300's narrow FP64
+    // pipe, and this kernel did little else
+    const float f = real ? __fdiv_rn((float)c0sq, (float)h[i]) : 0.f;
+    const double a0 = real ? (double)(fmaf(yv[2 * i], (float)s0, (float)m0) * f) : 0.0;
+    const double a1 = real ? (double)(fmaf(yv[2 * i + 1], (float)s1, (float)m1) * f) : 0.0;
     if (accumulate) {
         if (ax) ax[i] += a0;
         if (ay) ay[i] += a1;

@@ -1,6 +1,8 @@
 """Learned momentum closure on the GPU: the tensor-core network kernels
 against the FP64 oracle (forward, gradients, Adam), the feature gather
 against the oracle's neighbour ordering, and the closure in a solver."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -8,6 +10,7 @@ import torch
 import pysph_gb300
 from oracle import mlp as M
 from pysph_gb300 import learned as L
+from pysph_gb300 import native
 from pysph_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -173,6 +176,39 @@ def _feature_state():
     integ.cstep = 1
     integ.stages[0].run(integ, "k1")
     return particles.cell_manager, particles.arrays[0]
+
+
+def test_closure_apply_matches_formula():
+    """sph_mlp_apply: a_c = (y_c scale_c + mean_c) c0^2 / h on LocalReal
+    particles (FP32 arithmetic, FP64 store), added to or replacing acc."""
+    _need_gpu()
+    cm, pa = _feature_state()
+    n = pa.get_number_of_particles()
+    rng = np.random.default_rng(3)
+    y = torch.tensor(rng.normal(0, 1, (n, 2)), dtype=torch.float32, device="cuda")
+    c0, scale, mean = 100.0, (0.7, 1.3), (-0.05, 0.2)
+    h = pa.get("h").astype(np.float64)
+    real = pa.get("tag") == 0
+    want = [np.where(real, (y.cpu().numpy()[:, c].astype(np.float64) * scale[c] + mean[c])
+                     * c0 * c0 / h, 0.0) for c in range(2)]
+    base = [torch.tensor(rng.normal(0, 1, n), dtype=torch.float64, device="cuda")
+            for _ in range(3)]
+    for accumulate in (0, 1):
+        acc = [b.clone() for b in base]
+        ptrs = (ctypes.c_void_p * 3)(*[a.data_ptr() for a in acc])
+        native.check(native.lib().sph_mlp_apply(
+            cm.context(), cm.slot(pa), ctypes.c_void_p(y.data_ptr()), c0,
+            (ctypes.c_double * 2)(*scale), (ctypes.c_double * 2)(*mean), ptrs, accumulate),
+            "sph_mlp_apply")
+        torch.cuda.synchronize()
+        for c in range(2):
+            exp = want[c] + (base[c].cpu().numpy() if accumulate else 0.0)
+            got = acc[c].cpu().numpy()
+            assert np.max(np.abs(got - exp)) <= 1e-6 * np.max(np.abs(exp)), (accumulate, c)
+        if accumulate:
+            assert torch.equal(acc[2], base[2])
+        else:
+            assert torch.count_nonzero(acc[2]) == 0
 
 
 def test_feature_kernels_agree(monkeypatch):
