@@ -91,28 +91,17 @@ struct RatesArgs {
 };
 
 // Destination of thread slot s; false for a non-LocalReal particle.
-// (WARP: the 32 lanes of a warp share destination s; one lane does the two
-// FP64 products, which on GB300's FP64 pipe cost a warp 16 clocks each, and
-// the others take them by shuffle.  Every lane of the warp must call it.)
-template <bool WARP = false>
 __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s, DestPos &d) {
     const int orig = D.perm[s];
     d.orig = orig;
-    const bool real = D.tag == nullptr || D.tag[orig] == SPH_TAG_LOCAL_REAL;
-    if (!WARP && !real) return false;
+    if (D.tag != nullptr && D.tag[orig] != SPH_TAG_LOCAL_REAL) return false;
     const float4 p = D.pm[s];
     d.xi_x = p.x; d.xi_y = p.y; d.xi_z = p.z;
     decode_cell(g, D.skey[s], d.cx, d.cy, d.cz);
-    double radius = 0.0;
-    if (!WARP || (threadIdx.x & 31) == 0) {
-        radius = __dmul_rn(D.h[orig], g.radius_scale);
-        d.radius2 = __dmul_rn(radius, radius);
-    }
-    if (WARP) {
-        radius = __shfl_sync(0xffffffffu, radius, 0);
-        d.radius2 = __shfl_sync(0xffffffffu, d.radius2, 0);
-    }
-    // FP32 copies by integer operations (bit-equal to the conversion)
+    const double radius = __dmul_rn(D.h[orig], g.radius_scale);
+    d.radius2 = __dmul_rn(radius, radius);
+    // FP32 copies by integer operations, bit-equal to the conversion: on
+    // GB300 the narrow FP64 pipe executes the conversions too
     const float r2 = d2f_rn(d.radius2);
     d.r2lo = r2 * (1.f - 1e-5f);
     d.r2hi = r2 * (1.f + 1e-5f);
@@ -121,7 +110,7 @@ __device__ __forceinline__ bool load_dest(const Grid &g, const DestDev &D, int s
         const float rl = d2f_rn(radius) + g.skin;
         d.r2list = rl * rl * (1.f + 2e-5f);
     }
-    return real;
+    return true;
 }
 
 // With a list skin the list holds sources up to the list radius: keep the
@@ -697,7 +686,7 @@ __global__ void __launch_bounds__(256, 6) k_features_warp(const __grid_constant_
     const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (s >= A.d.n || gated_off(A.gate)) return;
     DestPos d;
-    const bool real = load_dest<true>(A.g, A.d, (int)s, d);
+    const bool real = load_dest(A.g, A.d, (int)s, d);
     const SrcDev &S = A.s;
     const float csf = A.g.cs_f;
     constexpr uint64_t none = ~0ull;
