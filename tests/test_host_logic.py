@@ -224,3 +224,22 @@ def test_list_skin_defaults(monkeypatch):
     monkeypatch.setenv("PYSPH_GB300_SKIN", "0.05")
     assert tuning.list_skin() == 0.05
     assert tuning.skin_growth(10) is None
+
+
+def test_guard_stats_report_the_spread_of_window_errors():
+    """GuardedRunner.stats(): windows, checks, kept and fallbacks, and the
+    smallest, median and largest normwise error of the checked windows."""
+    from pysph_gb300 import learned as L
+    r = object.__new__(L.GuardedRunner)
+    r.windows, r.checks, r.kept, r.fallbacks = 7, 5, 2, 3
+    r.errors = [3e-3, 2e-4, 5e-4, 9e-4, 4e-2]
+    r.max_err, r.max_err_maxrel = max(r.errors), 0.1
+    st = r.stats()
+    assert (st["windows"], st["checks"], st["kept"], st["fallbacks"]) == (7, 5, 2, 3)
+    assert st["fallback_rate"] == 0.6
+    assert st["min_normwise_density_error"] == 2e-4
+    assert st["median_normwise_density_error"] == 9e-4
+    assert st["max_normwise_density_error"] == 4e-2
+    r.errors, r.checks = [], 0
+    st = r.stats()
+    assert st["fallback_rate"] is None and st["median_normwise_density_error"] is None
