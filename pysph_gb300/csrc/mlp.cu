@@ -221,12 +221,6 @@ constexpr float kGeluE0 = 2.f * 1.4426950408889634f * kGeluC;   // 2u log2(e) = 
 constexpr float kGeluE1 = kGeluE0 * 0.044715f;
 constexpr float kGeluD0 = 2.f * kGeluC;                    // 2u' = D0 + D1 z^2
 constexpr float kGeluD1 = kGeluD0 * 0.134145f;
-__device__ __forceinline__ float dgelu_s(float z) {
-    const float z2 = z * z;
-    const float e = ex2_approx(z * fmaf(kGeluE1, z2, kGeluE0));
-    const float sg = rcp_approx(1.f + e);
-    return (1.f - sg) * fmaf(z * fmaf(kGeluD1, z2, kGeluD0), sg, 1.f);
-}
 
 // Pairs of FP32 values in one 64-bit register pair, for the packed FP32
 // arithmetic of sm_100+ (add / sub / mul / fma .rn.f32x2: two lanes per
@@ -280,7 +274,7 @@ __device__ __forceinline__ uint64_t gelu2(uint64_t z) {
     return fma2(hz, f2(tanh_approx(u0), tanh_approx(u1)), hz);
 }
 
-// d gelu / dz of a pair, as dgelu_s: (1 - s) (1 + z (D0 + D1 z^2) s)
+// d gelu / dz of a pair in the sigmoid form: (1 - s) (1 + z (D0 + D1 z^2) s)
 __device__ __forceinline__ uint64_t dgelu2(uint64_t z) {
     const uint64_t one = f2(1.f, 1.f);
     const uint64_t zz = mul2(z, z);
